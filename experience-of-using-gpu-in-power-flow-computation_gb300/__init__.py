@@ -1,0 +1,402 @@
+"""gbpf: GB300-native Newton-Raphson AC power flow (Python host mirror).
+
+Thin ctypes layer over ``lib/libgbpf.so`` (C ABI declared in include/gbpf.h).
+It mirrors the reference's process-level interface: ``load_options`` reads a
+data.txt exactly like ``loadFile`` (GPU/sistInfo.h:62-242), ``read_grid`` reads
+a common-data-format file like ``lerArquivoEAlocarMemoria``
+(GPU/arquivo.h:250-295), and ``Solver.solve`` runs ``mNR``
+(GPU/newtonRaphson.cuh:171-623) on the GPU.  There is no CPU fallback: when the
+library is missing or no GPU is present, the solver raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libgbpf.so")
+CLI_PATH = os.path.join(HERE, "lib", "gbpf")
+
+OK, E_INPUT, E_SINGULAR, E_NOCONV, E_CUDA, E_TIMEOUT, E_OOM, E_ARG, E_UNSUPPORTED = range(9)
+METODO = {"esparso": 0, "denso": 1, "hibridoA": 2, "hibridoB": 3, "hibridoC": 4, "nda": 5}
+PREC_FP64, PREC_FP32_IR = 0, 1
+EVENT_TEXT = {
+    1: "PV -> PQ (limite superior)",
+    2: "PQ (limite inferior) -> PQ (limite superior)",
+    3: "PV -> PQ (limite inferior)",
+    4: "PQ (limite superior) -> PQ (limite inferior)",
+    5: "PQ -> PV",
+}
+
+# Every entry point include/gbpf.h declares (checked by the CPU test suite).
+EXPORTS = [
+    "gbpf_options_default", "gbpf_options_parse", "gbpf_options_load",
+    "gbpf_grid_read", "gbpf_grid_create", "gbpf_grid_free", "gbpf_grid_dims", "gbpf_grid_buses",
+    "gbpf_grid_pvpq", "gbpf_grid_branches", "gbpf_grid_set_buses", "gbpf_grid_write_cdf",
+    "gbpf_generate", "gbpf_solver_create", "gbpf_solver_free", "gbpf_solve", "gbpf_solver_set_start",
+    "gbpf_solver_state", "gbpf_solver_events", "gbpf_solver_history", "gbpf_solver_triggers",
+    "gbpf_solver_flows", "gbpf_solver_info", "gbpf_solver_time", "gbpf_ybus", "gbpf_eval_pq",
+    "gbpf_eval_jacobian", "gbpf_newton_step", "gbpf_device_info", "gbpf_last_error", "gbpf_status_str",
+]
+
+
+class GbpfError(RuntimeError):
+    def __init__(self, status, where):
+        self.status = status
+        msg = ""
+        try:
+            msg = _lib.gbpf_last_error().decode(errors="replace")
+        except Exception:
+            pass
+        super().__init__(f"{where}: status {status} ({_status_str(status)}) {msg}")
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [
+        ("metodo", ctypes.c_int), ("v_inicial", ctypes.c_double), ("theta_inicial", ctypes.c_double),
+        ("tolerancia", ctypes.c_double), ("no_max_iter", ctypes.c_int), ("lim_inj_reat", ctypes.c_int),
+        ("openmp", ctypes.c_int), ("laconic_mode", ctypes.c_int), ("verbose_mode", ctypes.c_int),
+        ("output_ans", ctypes.c_int), ("output_iter", ctypes.c_int), ("streams", ctypes.c_int),
+        ("output_bench", ctypes.c_int), ("precision", ctypes.c_int), ("arq_entrada", ctypes.c_char * 1024),
+    ]
+
+
+class _Result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("converged", ctypes.c_int), ("iterations", ctypes.c_int),
+                ("n_events", ctypes.c_int), ("nPQlim", ctypes.c_int), ("final_mismatch", ctypes.c_double)]
+
+
+class _GridDesc(ctypes.Structure):
+    _fields_ = [("nB", ctypes.c_int), ("nL", ctypes.c_int), ("baseMVA", ctypes.c_double),
+                ("id", ctypes.c_void_p), ("bus_type", ctypes.c_void_p)] + \
+               [(n, ctypes.c_void_p) for n in ("V0", "theta0", "Pload", "Qload", "Pg", "Qg", "gsh", "bsh",
+                                               "Qmax", "Qmin", "from_bus", "to_bus", "r", "x", "bch",
+                                               "tap_re", "tap_im", "phase")]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libgbpf.so; raises when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"{LIB_PATH} is missing: run __graft_entry__.build() (nvcc, sm_103a)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name in EXPORTS:
+            getattr(L, name).restype = ctypes.c_int
+        L.gbpf_last_error.restype = ctypes.c_char_p
+        L.gbpf_status_str.restype = ctypes.c_char_p
+        L.gbpf_grid_free.restype = None
+        L.gbpf_solver_free.restype = None
+        _lib = L
+    return _lib
+
+
+def _status_str(st):
+    try:
+        return lib().gbpf_status_str(int(st)).decode()
+    except Exception:
+        return str(st)
+
+
+def _check(st, where):
+    if st != OK:
+        raise GbpfError(st, where)
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, np.float64)
+
+
+def _i32(a):
+    return None if a is None else np.ascontiguousarray(a, np.int32)
+
+
+# --------------------------------------------------------------------- options
+class Options:
+    """The data.txt options (namespace global of GPU/sistInfo.h:37-60)."""
+
+    def __init__(self, raw=None):
+        if raw is None:
+            raw = _Options()
+            lib().gbpf_options_default(ctypes.byref(raw))
+        self._o = raw
+        self.echo = ""
+
+    def __getattr__(self, k):
+        if k.startswith("_") or k == "echo":
+            raise AttributeError(k)
+        v = getattr(self._o, k)
+        return v.decode() if isinstance(v, bytes) else v
+
+    def __setattr__(self, k, v):
+        if k in ("_o", "echo"):
+            object.__setattr__(self, k, v)
+        elif k == "arq_entrada":
+            self._o.arq_entrada = os.fsencode(v)
+        else:
+            setattr(self._o, k, v)
+
+
+def parse_options(text):
+    o = Options()
+    echo = ctypes.create_string_buffer(1 << 16)
+    _check(lib().gbpf_options_parse(text.encode() if isinstance(text, str) else text,
+                                    ctypes.byref(o._o), echo, len(echo)), "gbpf_options_parse")
+    o.echo = echo.value.decode(errors="replace")
+    return o
+
+
+def load_options(path="data.txt"):
+    o = Options()
+    echo = ctypes.create_string_buffer(1 << 16)
+    _check(lib().gbpf_options_load(os.fsencode(path), ctypes.byref(o._o), echo, len(echo)), "gbpf_options_load")
+    o.echo = echo.value.decode(errors="replace")
+    return o
+
+
+# ----------------------------------------------------------------------- grids
+class Grid:
+    """One grid (struct sistema / barra / ramo of GPU/sistema.h:24-126)."""
+
+    def __init__(self, handle):
+        self.h = ctypes.c_void_p(handle)
+        d = np.zeros(8, np.int32)
+        _check(lib().gbpf_grid_dims(self.h, _p(d)), "gbpf_grid_dims")
+        self.nB, self.nL, self.nPV, self.nPQ, self.slack, self.nnzY, base, self.n_notices = (int(x) for x in d)
+        self.baseMVA = float(base)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gbpf_grid_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def buses(self):
+        n = self.nB
+        i = [np.zeros(n, np.int32) for _ in range(2)]
+        f = [np.zeros(n) for _ in range(8)]
+        _check(lib().gbpf_grid_buses(self.h, *[_p(a) for a in i + f]), "gbpf_grid_buses")
+        keys = ("id", "type", "V0", "theta0", "Pload", "Qload", "Pg", "Qg", "gsh", "bsh")
+        return dict(zip(keys, i + f))
+
+    def pvpq(self):
+        pv = np.zeros(self.nPV, np.int32)
+        pq = np.zeros(self.nPQ, np.int32)
+        f = [np.zeros(self.nPV) for _ in range(3)]
+        _check(lib().gbpf_grid_pvpq(self.h, _p(pv), *[_p(a) for a in f], _p(pq)), "gbpf_grid_pvpq")
+        return dict(pv=pv, Qmin=f[0], Qmax=f[1], Vset=f[2], pq=pq)
+
+    def branches(self):
+        m = self.nL
+        i = [np.zeros(m, np.int32) for _ in range(2)]
+        f = [np.zeros(m) for _ in range(6)]
+        _check(lib().gbpf_grid_branches(self.h, *[_p(a) for a in i + f]), "gbpf_grid_branches")
+        return dict(zip(("from_bus", "to_bus", "r", "x", "bch", "tap_re", "tap_im", "phase"), i + f))
+
+    def set_buses(self, Pload=None, Qload=None, Pg=None, Qg=None, V0=None, theta0=None):
+        arrs = [_f64(a) for a in (Pload, Qload, Pg, Qg, V0, theta0)]
+        _check(lib().gbpf_grid_set_buses(self.h, *[_p(a) for a in arrs]), "gbpf_grid_set_buses")
+
+    def write_cdf(self, path, title="synthetic grid"):
+        _check(lib().gbpf_grid_write_cdf(self.h, os.fsencode(path), title.encode()), "gbpf_grid_write_cdf")
+
+
+def read_grid(path, v_inicial=1.0, theta_inicial=0.0):
+    h = ctypes.c_void_p()
+    msg = ctypes.create_string_buffer(1 << 16)
+    _check(lib().gbpf_grid_read(os.fsencode(path), ctypes.c_double(v_inicial), ctypes.c_double(theta_inicial),
+                                ctypes.byref(h), msg, len(msg)), f"gbpf_grid_read({path})")
+    g = Grid(h.value)
+    g.notices = [l for l in msg.value.decode(errors="replace").split("\n") if l]
+    return g
+
+
+def create_grid(bus_type, V0, theta0, from_bus, to_bus, r, x, bch=None, tap_re=None, tap_im=None,
+                phase=None, Pload=None, Qload=None, Pg=None, Qg=None, gsh=None, bsh=None,
+                Qmax=None, Qmin=None, id=None, baseMVA=100.0):
+    keep = {}
+
+    def put(name, a, conv):
+        if a is None:
+            return None
+        a = conv(a)
+        keep[name] = a
+        return _p(a)
+
+    d = _GridDesc()
+    d.nB = len(bus_type)
+    d.nL = len(from_bus)
+    d.baseMVA = baseMVA
+    d.id = put("id", id, _i32)
+    d.bus_type = put("bus_type", bus_type, _i32)
+    for n, a in (("V0", V0), ("theta0", theta0), ("Pload", Pload), ("Qload", Qload), ("Pg", Pg), ("Qg", Qg),
+                 ("gsh", gsh), ("bsh", bsh), ("Qmax", Qmax), ("Qmin", Qmin), ("r", r), ("x", x), ("bch", bch),
+                 ("tap_re", tap_re), ("tap_im", tap_im), ("phase", phase)):
+        setattr(d, n, put(n, a, _f64))
+    d.from_bus = put("from_bus", from_bus, _i32)
+    d.to_bus = put("to_bus", to_bus, _i32)
+    h = ctypes.c_void_p()
+    _check(lib().gbpf_grid_create(ctypes.byref(d), ctypes.byref(h)), "gbpf_grid_create")
+    return Grid(h.value)
+
+
+def generate(kind, seed, tiles=0, nbus=0):
+    """Seeded synthetic grid: 1 = 14-bus, 2 = 118-bus, 3 = tiled 118-bus, 4 = scaled 14-bus style."""
+    h = ctypes.c_void_p()
+    _check(lib().gbpf_generate(int(kind), ctypes.c_ulonglong(seed), int(tiles), int(nbus), ctypes.byref(h)),
+           "gbpf_generate")
+    return Grid(h.value)
+
+
+def device_info(device=0):
+    cnt = ctypes.c_int()
+    name = ctypes.create_string_buffer(256)
+    props = np.zeros(6, np.int32)
+    st = lib().gbpf_device_info(int(device), ctypes.byref(cnt), name, 256, _p(props))
+    if st not in (OK, E_ARG):
+        raise GbpfError(st, "gbpf_device_info")
+    return dict(count=cnt.value, name=name.value.decode(), props=props)
+
+
+# ---------------------------------------------------------------------- solver
+class Solver:
+    """mNR on one GPU: device-resident Newton loop captured in a CUDA graph."""
+
+    def __init__(self, grid, options=None, device=0, **overrides):
+        o = options if options is not None else Options()
+        if isinstance(o, dict):
+            oo = Options()
+            for k, v in o.items():
+                setattr(oo, k, v)
+            o = oo
+        for k, v in overrides.items():
+            setattr(o, k, v)
+        self.grid = grid
+        self.options = o
+        self.h = ctypes.c_void_p()
+        _check(lib().gbpf_solver_create(grid.h, ctypes.byref(o._o), int(device), ctypes.byref(self.h)),
+               "gbpf_solver_create")
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gbpf_solver_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, full=True):
+        r = _Result()
+        st = lib().gbpf_solve(self.h, ctypes.byref(r))
+        if st not in (OK, E_NOCONV, E_SINGULAR):
+            raise GbpfError(st, "gbpf_solve")
+        out = dict(status=r.status, converged=bool(r.converged), iterations=r.iterations,
+                   n_events=r.n_events, nPQlim=r.nPQlim, final_mismatch=r.final_mismatch)
+        if full:
+            out.update(self.state())
+            out["events"] = self.events()
+            out["hist"] = self.history()
+            out.update(self.flows())
+        return out
+
+    def set_start(self, V0=None, theta0=None, Pliq=None, Qliq=None):
+        arrs = [_f64(a) for a in (V0, theta0, Pliq, Qliq)]
+        _check(lib().gbpf_solver_set_start(self.h, *[_p(a) for a in arrs]), "gbpf_solver_set_start")
+
+    def state(self):
+        n = self.grid.nB
+        a = [np.zeros(n) for _ in range(4)]
+        _check(lib().gbpf_solver_state(self.h, *[_p(x) for x in a]), "gbpf_solver_state")
+        return dict(zip(("V", "theta", "Pcalc", "Qcalc"), a))
+
+    def flows(self):
+        m = self.grid.nL
+        a = [np.zeros(m) for _ in range(4)]
+        _check(lib().gbpf_solver_flows(self.h, *[_p(x) for x in a]), "gbpf_solver_flows")
+        return dict(zip(("Pdp", "Ppd", "Qdp", "Qpd"), a))
+
+    def events(self, cap=4096):
+        ev = np.zeros(4 * cap, np.int32)
+        n = ctypes.c_int()
+        st = lib().gbpf_solver_events(self.h, _p(ev), cap, ctypes.byref(n))
+        if st not in (OK, E_ARG):
+            raise GbpfError(st, "gbpf_solver_events")
+        return [tuple(int(x) for x in ev[4 * i:4 * i + 4]) for i in range(n.value)]
+
+    def history(self):
+        cap = self.options.no_max_iter + 2
+        h = np.zeros(cap)
+        n = ctypes.c_int()
+        _check(lib().gbpf_solver_history(self.h, _p(h), cap, ctypes.byref(n)), "gbpf_solver_history")
+        return h[:n.value].copy()
+
+    def triggers(self):
+        cap = self.options.no_max_iter + 2
+        t = np.zeros(cap, np.int32)
+        n = ctypes.c_int()
+        _check(lib().gbpf_solver_triggers(self.h, _p(t), cap, ctypes.byref(n)), "gbpf_solver_triggers")
+        return t[:n.value].copy()
+
+    def info(self):
+        a = np.zeros(8, np.int64)
+        _check(lib().gbpf_solver_info(self.h, _p(a)), "gbpf_solver_info")
+        keys = ("nB", "blocks", "factor_blocks", "update_pairs", "forward_levels", "backward_levels",
+                "graph_nodes", "kernels_per_iteration")
+        return dict(zip(keys, (int(x) for x in a)))
+
+    def time(self, repeats):
+        ms = ctypes.c_double()
+        _check(lib().gbpf_solver_time(self.h, int(repeats), ctypes.byref(ms)), "gbpf_solver_time")
+        return ms.value
+
+    # kernel-level entry points
+    def ybus(self):
+        n, nnz = self.grid.nB, self.grid.nnzY
+        rp = np.zeros(n + 1, np.int32)
+        c = np.zeros(nnz, np.int32)
+        re = np.zeros(nnz)
+        im = np.zeros(nnz)
+        _check(lib().gbpf_ybus(self.h, _p(rp), _p(c), _p(re), _p(im)), "gbpf_ybus")
+        return rp, c, re, im
+
+    def eval_pq(self, V, theta):
+        V, theta = _f64(V), _f64(theta)
+        P = np.zeros(self.grid.nB)
+        Q = np.zeros(self.grid.nB)
+        _check(lib().gbpf_eval_pq(self.h, _p(V), _p(theta), _p(P), _p(Q)), "gbpf_eval_pq")
+        return P, Q
+
+    def eval_jacobian(self, V, theta, limQ=None):
+        V, theta = _f64(V), _f64(theta)
+        limQ = _i32(np.zeros(self.grid.nPV, np.int32) if limQ is None else limQ)
+        cap = 4 * self.grid.nnzY + 16
+        row = np.zeros(cap, np.int32)
+        col = np.zeros(cap, np.int32)
+        val = np.zeros(cap)
+        n = ctypes.c_int()
+        _check(lib().gbpf_eval_jacobian(self.h, _p(V), _p(theta), _p(limQ), _p(row), _p(col), _p(val), cap,
+                                        ctypes.byref(n)), "gbpf_eval_jacobian")
+        k = n.value
+        return row[:k].copy(), col[:k].copy(), val[:k].copy()
+
+    def newton_step(self, V, theta, g, limQ=None):
+        V, theta, g = _f64(V), _f64(theta), _f64(g)
+        limQ = _i32(np.zeros(self.grid.nPV, np.int32) if limQ is None else limQ)
+        dx = np.zeros_like(g)
+        _check(lib().gbpf_newton_step(self.h, _p(V), _p(theta), _p(limQ), _p(g), _p(dx)), "gbpf_newton_step")
+        return dx

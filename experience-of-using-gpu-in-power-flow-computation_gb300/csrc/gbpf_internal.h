@@ -1,0 +1,80 @@
+// gbpf_internal.h -- host-side data model shared by the libgbpf translation units.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "gbpf.h"
+
+namespace gbpf {
+
+// Thread-local text of the last error (returned by gbpf_last_error).
+void set_error(const std::string &msg);
+const std::string &last_error();
+
+// One grid: struct sistema / barra / ramo of the reference (GPU/sistema.h:24-126)
+// as structure-of-arrays, bus indices 1-based in file order.
+struct Grid {
+    int nB = 0, nL = 0, nPV = 0, nPQ = 0, slack = 0;  // slack = barraVO
+    double baseMVA = 100.0;
+    std::vector<int> id, type;                                        // [nB]
+    std::vector<double> V0, theta0, Pload, Qload, Pg, Qg, gsh, bsh;   // [nB]
+    std::vector<double> Vbase;                                        // [nB]
+    std::vector<int> pv, pq;                                          // 1-based, ascending
+    std::vector<double> Qmin, Qmax, Vset;                             // [nPV]
+    std::vector<int> de, para;                                        // [nL] 1-based
+    std::vector<double> r, x, bch, tap_re, tap_im, phase;             // [nL]
+    std::vector<std::string> notices;                                 // reader notices
+
+    double Pliq(int k) const { return Pg[k] - Pload[k]; }
+    double Qliq(int k) const { return Qg[k] - Qload[k]; }
+    void rebuild_lists();  // pv / pq lists from type[]
+};
+
+// Ybus pattern (row-major CSR, sorted columns, explicit diagonal) and the
+// assembly map: for each slot the contributions to sum, in the order Eigen's
+// setFromTriplets sums them (branch stamps in branch order, then the shunt).
+struct YPattern {
+    int n = 0, nnz = 0;
+    std::vector<int> rowptr, col;
+    std::vector<int> diag;            // [nB] slot of (k,k)
+    std::vector<int> cptr, csrc;      // per slot: stamp ids 4*branch+which, or -1-bus for the shunt
+    int find(int r, int c) const;     // slot of (r,c) or -1
+};
+YPattern build_ypattern(const Grid &g);
+
+// Static-pivot block LU symbolic analysis over the non-slack buses.  Block b
+// (0..n-1) is bus bus_of_blk[b]; every block is a 2x2 [dP/dth dP/dV; dQ/dth dQ/dV].
+// Off-diagonal factor structure is symmetric: idx(j) = up_col[up_ptr[j]..up_ptr[j+1])
+// holds the blocks i > j with L(i,j) / U(j,i) != 0 (stored at the same position).
+struct Symbolic {
+    int n = 0;        // blocks
+    int nup = 0;      // off-diagonal block positions per triangle
+    std::vector<int> bus_of_blk, blk_of_bus;     // blk_of_bus[slack-1] = -1
+    std::vector<int> up_ptr, up_col;
+    // Crout gather lists.  Diagonal of step j: sum over dg entries of L(j,k)U(k,j);
+    // dg_pos = position of j in idx(k), dg_k = k.  Off-diagonal entry p (i in idx(j)):
+    // pairs (pos of j in idx(k), pos of i in idx(k)).
+    std::vector<int> dg_ptr, dg_pos, dg_k;
+    std::vector<long long> og_ptr;
+    std::vector<int> og_a, og_b;
+    // Level schedules: forward (factor + L solve) and backward (U solve).
+    std::vector<int> flev_ptr, flev_steps, blev_ptr, blev_steps;
+    // Jacobian fill map over all factor block positions q in [0, n + 2*nup):
+    // q < n: diagonal block q; n <= q < n+nup: L block at p = q-n (row i = up_col[p]);
+    // q >= n+nup: U block at p = q-n-nup.  ysl[q] = Y slot of (row bus, col bus) or -1
+    // for fill; rbus/cbus 0-based.
+    std::vector<int> ysl, rbus, cbus;
+    long long pairs() const { return og_ptr.empty() ? 0 : og_ptr.back(); }
+};
+Symbolic analyse(const Grid &g, const YPattern &y, std::string *why);
+
+// Ordering used by analyse(): minimum degree on the bus graph.
+std::vector<int> min_degree_order(int n, const std::vector<std::vector<int>> &adj);
+
+}  // namespace gbpf
+
+struct gbpf_grid {
+    gbpf::Grid g;
+};

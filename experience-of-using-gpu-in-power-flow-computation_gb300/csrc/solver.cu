@@ -1,0 +1,1030 @@
+// solver.cu -- single-grid Newton-Raphson power flow on one GPU (sm_103a).
+//
+// Replaces mNR (GPU/newtonRaphson.cuh:171-623) and the kernels it drives:
+//   Ybus assembly         calcYbusSp_eficinte  GPU/sistema.h:705-758 (host, Eigen)
+//   injections            calc{P,Q}eficiente_0based  GPU/PQcalc.cuh:177-219
+//   mismatch              calcResPLim / calcResQLim  GPU/newtonRaphson.cuh:35-58
+//   PV->PQ switching      chkLimQ / geraVetPV / geraVetPQ  GPU/limiteInjReat.cuh:5-75
+//   Jacobian fill         SpCalcH/L/M/N  GPU/Jacobiano.cuh:252-415
+//   linear solve          cusolverSpDcsrlsvqr  GPU/newtonRaphson.cuh:455-478
+//   state update          attOlim / attVlim  GPU/newtonRaphson.cuh:76-119
+//   convergence test      maxi + host test  GPU/newtonRaphson.cuh:390-426
+// The whole loop is one CUDA graph: a prologue (reset, injections, limits,
+// mismatch, test) followed by a conditional WHILE node whose body is one Newton
+// iteration; the test kernel sets the loop condition on the device, so a solve
+// is one graph launch and one host synchronisation.
+//
+// Jacobian layout: 2x2 blocks per non-slack bus ([dP/dth dP/dV; dQ/dth dQ/dV]),
+// with a Q row and V column for every non-slack bus.  Buses that are PV (not at
+// a Q limit) get an identity Q row and a zero V column, so PV<->PQ switches
+// never change the symbolic structure; the solution of the remaining equations
+// is the same as that of the reference's reduced system.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "gbpf_internal.h"
+
+using gbpf::Grid;
+using gbpf::set_error;
+using gbpf::Symbolic;
+using gbpf::YPattern;
+
+namespace {
+
+constexpr int kEventCap = 4096;
+
+// 2x2 block, row-major, 32-byte aligned (one 256-bit access per block)
+using blk4 = double4_32a;
+__host__ __device__ __forceinline__ blk4 mk4(double a, double b, double c, double e) {
+    blk4 r;
+    r.x = a; r.y = b; r.z = c; r.w = e;
+    return r;
+}
+
+struct Ctl {
+    int it;          // Newton updates done
+    int done;        // loop finished (converged, iteration cap, failure)
+    int status;      // gbpf_status
+    int n_events;    // switch events recorded (may exceed the log capacity)
+    unsigned long long maxG;   // bits of max|g| (non-negative doubles order as integers)
+    unsigned long long maxDx;  // bits of max|dx| of the last step
+    int converged;
+    int pad;
+};
+
+// Every device pointer and size a kernel needs, passed by value.
+struct Dev {
+    int nB, nL, nnzY, slack, nPV, n, nup, max_iter, lim, hist_cap;
+    double tol;
+    const int *yptr, *ycol;
+    double2 *yval;
+    const int *cptr, *csrc;
+    double2 *stamp;
+    const int *br_f, *br_t;
+    const double *br_r, *br_x, *br_b, *br_tre, *br_tim;
+    const double *gsh, *bsh;
+    double *V, *th, *cs, *sn, *P, *Q;
+    double *V0, *th0, *Pliq, *Qliq;
+    const double *Qload;
+    const int *type;
+    int *act;
+    double *QliqLim;
+    const int *pv_bus;
+    const double *Qmin, *Qmax;
+    int *limQ;
+    const int *bus_of_blk, *blk_of_bus;
+    const int *up_ptr, *up_col, *dg_ptr, *dg_pos, *dg_k;
+    const long long *og_ptr;
+    const int *og_a, *og_b;
+    const int *flev_steps, *blev_steps;
+    const int *ysl, *rbus, *cbus;
+    blk4 *fac, *dinv;
+    double2 *rhs, *ys, *xs;
+    Ctl *ctl;
+    double *hist;
+    int *trig;       // [hist_cap] 1 where the limit check ran (chkLimQ's "\n")
+    int *events;
+    // branch flows
+    const int *fl_skm, *fl_smk;
+    const double *fl_phi, *fl_bkm, *fl_bmk;
+    double *Pdp, *Ppd, *Qdp, *Qpd;
+};
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ blk4 mm(blk4 a, blk4 b) {  // 2x2 row-major product
+    return mk4(a.x * b.x + a.y * b.z, a.x * b.y + a.y * b.w,
+                        a.z * b.x + a.w * b.z, a.z * b.y + a.w * b.w);
+}
+__device__ __forceinline__ blk4 sub4(blk4 a, blk4 b) {
+    return mk4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+}
+__device__ __forceinline__ blk4 add4(blk4 a, blk4 b) {
+    return mk4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+__device__ __forceinline__ double2 mv(blk4 a, double2 v) {
+    return make_double2(a.x * v.x + a.y * v.y, a.z * v.x + a.w * v.y);
+}
+__device__ __forceinline__ blk4 shfl4(blk4 v, int src) {
+    return mk4(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+                        __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
+}
+__device__ __forceinline__ blk4 warp_sum4(blk4 v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        v.z += __shfl_xor_sync(0xffffffffu, v.z, o);
+        v.w += __shfl_xor_sync(0xffffffffu, v.w, o);
+    }
+    return v;
+}
+__device__ __forceinline__ double2 warp_sum2(double2 v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long *a, double v) {
+    atomicMax(a, (unsigned long long)__double_as_longlong(v));
+}
+// Smith's complex division (a+ib)/(c+id).
+__device__ __forceinline__ double2 cdiv(double a, double b, double c, double d) {
+    if (fabs(c) >= fabs(d)) {
+        const double r = d / c, den = c + d * r;
+        return make_double2((a + b * r) / den, (b - a * r) / den);
+    }
+    const double r = c / d, den = c * r + d;
+    return make_double2((a * r + b) / den, (b * r - a) / den);
+}
+
+__device__ __forceinline__ bool stopped(const Dev &d, int guard) {
+    return guard && *(volatile int *)&d.ctl->done;
+}
+
+// ------------------------------------------------------------------ Ybus
+// Branch stamps of calcYbusSp_eficinte (GPU/sistema.h:708-719):
+// (de,para) -y/conj(t), (para,de) -y/t, (de,de) y/|t|^2 + jb/2, (para,para) y + jb/2.
+__global__ void k_ybus_stamps(Dev d) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= d.nL) return;
+    const double2 y = cdiv(1.0, 0.0, d.br_r[b], d.br_x[b]);
+    const double tr = d.br_tre[b], ti = d.br_tim[b];
+    const double2 ft = cdiv(-y.x, -y.y, tr, -ti);
+    const double2 tf = cdiv(-y.x, -y.y, tr, ti);
+    double a = hypot(tr, ti);
+    a = 1.0 / (a * a);
+    const double hb = d.br_b[b] / 2.;
+    d.stamp[4 * b + 0] = ft;
+    d.stamp[4 * b + 1] = tf;
+    d.stamp[4 * b + 2] = make_double2(a * y.x, a * y.y + hb);
+    d.stamp[4 * b + 3] = make_double2(y.x, y.y + hb);
+}
+
+// One slot per thread: contributions summed left to right in triplet order.
+__global__ void k_ybus_sum(Dev d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.nnzY) return;
+    double2 acc = make_double2(0, 0);
+    for (int c = d.cptr[s]; c < d.cptr[s + 1]; c++) {
+        const int src = d.csrc[c];
+        const double2 v = src >= 0 ? d.stamp[src] : make_double2(d.gsh[-1 - src], d.bsh[-1 - src]);
+        if (c == d.cptr[s]) acc = v;
+        else { acc.x += v.x; acc.y += v.y; }
+    }
+    d.yval[s] = acc;
+}
+
+// ------------------------------------------------------------------ Newton kernels
+// Start of a solve: flat/CDF start, limit state of initLim (GPU/limiteInjReat.cuh:188-224).
+__global__ void k_reset(Dev d) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < d.nB) {
+        d.V[k] = d.V0[k];
+        d.th[k] = d.th0[k];
+        d.QliqLim[k] = d.Qliq[k];
+        d.act[k] = (d.type[k] == 0 || d.type[k] == 1);
+    }
+    if (k < d.nPV) d.limQ[k] = 0;
+    if (k < d.hist_cap) d.trig[k] = 0;
+    if (k == 0) {
+        Ctl c = {};
+        c.maxDx = (unsigned long long)__double_as_longlong(INFINITY);
+        *d.ctl = c;
+    }
+}
+
+// Unit phasors of the bus angles; also clears the mismatch maximum.
+__global__ void k_phasor(Dev d, int guard) {
+    if (stopped(d, guard)) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) d.ctl->maxG = 0ull;
+    if (k >= d.nB) return;
+    double s, c;
+    sincos(d.th[k], &s, &c);
+    d.cs[k] = c;
+    d.sn[k] = s;
+}
+
+// P, Q injections: S_k = V_k u_k conj(sum_m Y_km V_m u_m).  Four lanes per bus
+// row, 16-byte loads of (G, B).
+__global__ void k_pq(Dev d, int guard) {
+    if (stopped(d, guard)) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = t >> 2, l = t & 3;
+    const bool live = k < d.nB;
+    double ir = 0, ii = 0;
+    if (live) {
+        for (int p = d.yptr[k] + l; p < d.yptr[k + 1]; p += 4) {
+            const int m = d.ycol[p];
+            const double2 y = d.yval[p];
+            const double em = d.V[m] * d.cs[m], fm = d.V[m] * d.sn[m];
+            ir += y.x * em - y.y * fm;
+            ii += y.x * fm + y.y * em;
+        }
+    }
+    ir += __shfl_xor_sync(0xffffffffu, ir, 1);
+    ii += __shfl_xor_sync(0xffffffffu, ii, 1);
+    ir += __shfl_xor_sync(0xffffffffu, ir, 2);
+    ii += __shfl_xor_sync(0xffffffffu, ii, 2);
+    if (live && l == 0) {
+        const double ek = d.V[k] * d.cs[k], fk = d.V[k] * d.sn[k];
+        d.P[k] = ek * ir + fk * ii;
+        d.Q[k] = fk * ir - ek * ii;
+    }
+}
+
+// chkLimQ (GPU/limiteInjReat.cuh:5-40) for every PV bus, when the previous
+// Newton step was small (trigger of GPU/newtonRaphson.cuh:309-314).  The
+// ascending barrasPQlim merge of geraVetPQ is implicit: a bus's Q row is
+// active when act[bus] = 1.
+__global__ void k_limits(Dev d, int guard) {
+    if (stopped(d, guard)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nPV || !d.lim) return;
+    const int it = d.ctl->it;
+    if (it < 1 || it >= d.max_iter) return;
+    const double mdx = __longlong_as_double((long long)d.ctl->maxDx);
+    if (!(mdx < d.tol * 10.)) return;
+    if (i == 0) d.trig[it] = 1;
+    const int b = d.pv_bus[i];
+    const double qg = d.Q[b] + d.Qload[b];
+    int code = 0;
+    if (qg < d.Qmin[i] - d.tol) {
+        if (!d.limQ[i]) code = 1;
+        else if (d.QliqLim[b] != d.Qmin[i] - d.Qload[b]) code = 2;
+        d.limQ[i] = 1;
+        d.QliqLim[b] = d.Qmin[i] - d.Qload[b];
+    } else if (qg > d.Qmax[i] + d.tol) {
+        if (!d.limQ[i]) code = 3;
+        else if (d.QliqLim[b] != d.Qmax[i] - d.Qload[b]) code = 4;
+        d.limQ[i] = 1;
+        d.QliqLim[b] = d.Qmax[i] - d.Qload[b];
+    } else {
+        if (d.limQ[i]) code = 5;
+        d.limQ[i] = 0;
+    }
+    d.act[b] = d.limQ[i];
+    if (code) {
+        const int e = atomicAdd(&d.ctl->n_events, 1);
+        if (e < kEventCap) {
+            d.events[4 * e + 0] = it;
+            d.events[4 * e + 1] = b + 1;
+            d.events[4 * e + 2] = i;
+            d.events[4 * e + 3] = code;
+        }
+    }
+}
+
+// Mismatch per block: (Pliq - P, QliqLim - Q or 0 on an identity row), and max|g|.
+__global__ void k_mismatch(Dev d, int guard) {
+    if (stopped(d, guard)) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double m = 0;
+    if (j < d.n) {
+        const int k = d.bus_of_blk[j];
+        const double gp = d.Pliq[k] - d.P[k];
+        const double gq = d.act[k] ? d.QliqLim[k] - d.Q[k] : 0.0;
+        d.rhs[j] = make_double2(gp, gq);
+        m = fmax(fabs(gp), fabs(gq));
+        if (m != m) m = __longlong_as_double(0x7ff8000000000000ll);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double t = __shfl_xor_sync(0xffffffffu, m, o);
+        m = (t > m || t != t) ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&d.ctl->maxG, m);
+}
+
+// Convergence test of GPU/newtonRaphson.cuh:417-426; sets the loop condition.
+__global__ void k_control(Dev d, cudaGraphConditionalHandle h, int set_cond) {
+    Ctl *c = d.ctl;
+    if (!c->done) {
+        const double mg = __longlong_as_double((long long)c->maxG);
+        if (c->it < d.hist_cap) d.hist[c->it] = mg;
+        if (mg != mg) { c->status = GBPF_E_NOCONV; c->done = 1; }
+        else if (mg <= d.tol) { c->converged = 1; c->done = 1; }
+        else if (c->it >= d.max_iter) { c->status = GBPF_E_NOCONV; c->done = 1; }
+    }
+    if (set_cond) cudaGraphSetConditional(h, c->done ? 0u : 1u);
+}
+
+// Jacobian block at every factor position (fill-in positions get zeros).
+// Formulas of SpCalcH/L/M/N (GPU/Jacobiano.cuh:252-344) with the angle
+// difference taken from unit phasors: w = u_k conj(Y_km u_m) =
+// (G cos + B sin) + j (G sin - B cos).
+__global__ void k_jfill(Dev d, int guard) {
+    if (stopped(d, guard)) return;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q == 0) d.ctl->maxDx = 0ull;
+    if (q >= d.n + 2 * d.nup) return;
+    const int s = d.ysl[q];
+    blk4 blk = mk4(0, 0, 0, 0);
+    if (s >= 0) {
+        const int k = d.rbus[q], m = d.cbus[q];
+        const double2 y = d.yval[s];
+        const double Vk = d.V[k];
+        const int ak = d.act[k];
+        if (q < d.n) {
+            const double P = d.P[k], Q = d.Q[k], v2 = Vk * Vk;
+            const double H = -Q - v2 * y.y;
+            if (ak) blk = mk4(H, (P + v2 * y.x) / Vk, P - v2 * y.x, (Q - v2 * y.y) / Vk);
+            else blk = mk4(H, 0.0, 0.0, 1.0);
+        } else {
+            const int am = d.act[m];
+            const double ck = d.cs[k], sk = d.sn[k], cm = d.cs[m], sm = d.sn[m];
+            const double tr = y.x * cm - y.y * sm, ti = y.x * sm + y.y * cm;  // Y u_m
+            const double wr = ck * tr + sk * ti, wi = sk * tr - ck * ti;      // u_k conj(Y u_m)
+            const double Vm = d.V[m];
+            const double H = Vk * Vm * wi, N = Vk * wr, M = -Vk * Vm * wr, L = Vk * wi;
+            blk = mk4(H, am ? N : 0.0, ak ? M : 0.0, (ak && am) ? L : 0.0);
+        }
+    }
+    d.fac[q] = blk;
+}
+
+// One forward level: Crout step j per warp (diagonal block, its inverse, the
+// L column and U row of j) fused with the forward substitution y_j.
+__global__ void k_factor(Dev d, int beg, int cnt, int guard) {
+    if (stopped(d, guard)) return;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= cnt) return;
+    const int j = d.flev_steps[beg + w];
+    const blk4 *Lv = d.fac + d.n, *Uv = d.fac + d.n + d.nup;
+    blk4 acc = mk4(0, 0, 0, 0);
+    double2 accy = make_double2(0, 0);
+    for (int t = d.dg_ptr[j] + lane; t < d.dg_ptr[j + 1]; t += 32) {
+        const int a = d.dg_pos[t];
+        const blk4 l = Lv[a];
+        acc = add4(acc, mm(l, Uv[a]));
+        const double2 v = mv(l, d.ys[d.dg_k[t]]);
+        accy.x += v.x;
+        accy.y += v.y;
+    }
+    acc = warp_sum4(acc);
+    accy = warp_sum2(accy);
+    blk4 inv = mk4(0, 0, 0, 0);
+    if (lane == 0) {
+        const blk4 D = sub4(d.fac[j], acc);
+        const double det = D.x * D.w - D.y * D.z;
+        if (det == 0.0 || !isfinite(det)) {
+            d.ctl->status = GBPF_E_SINGULAR;
+            d.ctl->done = 1;
+        }
+        inv = mk4(D.w / det, -D.y / det, -D.z / det, D.x / det);
+        d.fac[j] = D;
+        d.dinv[j] = inv;
+        const double2 r = d.rhs[j];
+        d.ys[j] = make_double2(r.x - accy.x, r.y - accy.y);
+    }
+    inv = shfl4(inv, 0);
+    blk4 *Lw = d.fac + d.n, *Uw = d.fac + d.n + d.nup;
+    for (int p = d.up_ptr[j] + lane; p < d.up_ptr[j + 1]; p += 32) {
+        blk4 aL = Lw[p], aU = Uw[p];
+        for (long long r = d.og_ptr[p]; r < d.og_ptr[p + 1]; r++) {
+            const int a = d.og_a[r], b = d.og_b[r];
+            aL = sub4(aL, mm(Lv[b], Uv[a]));
+            aU = sub4(aU, mm(Lv[a], Uv[b]));
+        }
+        Uw[p] = aU;
+        Lw[p] = mm(aL, inv);
+    }
+}
+
+// One backward level: x_j = D_j^-1 (y_j - sum_i U(j,i) x_i).
+__global__ void k_bsolve(Dev d, int beg, int cnt, int guard) {
+    if (stopped(d, guard)) return;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= cnt) return;
+    const int j = d.blev_steps[beg + w];
+    const blk4 *Uv = d.fac + d.n + d.nup;
+    double2 acc = make_double2(0, 0);
+    for (int p = d.up_ptr[j] + lane; p < d.up_ptr[j + 1]; p += 32) {
+        const double2 v = mv(Uv[p], d.xs[d.up_col[p]]);
+        acc.x += v.x;
+        acc.y += v.y;
+    }
+    acc = warp_sum2(acc);
+    if (lane == 0) {
+        const double2 y = d.ys[j];
+        d.xs[j] = mv(d.dinv[j], make_double2(y.x - acc.x, y.y - acc.y));
+    }
+}
+
+// attOlim / attVlim: theta += dx_theta, V += dx_V on active rows; max|dx|.
+__global__ void k_update(Dev d, int guard) {
+    if (stopped(d, guard)) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double m = 0;
+    if (j < d.n) {
+        const int k = d.bus_of_blk[j];
+        const double2 x = d.xs[j];
+        d.th[k] += x.x;
+        if (d.act[k]) d.V[k] += x.y;
+        m = fmax(fabs(x.x), fabs(x.y));
+        if (m != m) m = __longlong_as_double(0x7ff8000000000000ll);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double t = __shfl_xor_sync(0xffffffffu, m, o);
+        m = (t > m || t != t) ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&d.ctl->maxDx, m);
+    if (j == 0) d.ctl->it += 1;
+}
+
+// Branch flows of d_P_Eficiente_Sp / d_Q_Eficiente_Sp (GPU/PQcalc.cuh:523-545);
+// the phase (phif) and charging (bshf) of each direction are resolved on the
+// host once, so the kernel is O(nL) instead of the reference's O(nL^2) scans.
+__global__ void k_flows(Dev d) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= d.nL) return;
+    const int k = d.br_f[b], m = d.br_t[b];
+    const double a = d.fl_phi[b] + d.th[k] - d.th[m];
+    const double2 ykm = d.yval[d.fl_skm[b]], ymk = d.yval[d.fl_smk[b]];
+    const double Vk = d.V[k], Vm = d.V[m];
+    double sa, ca;
+    sincos(a, &sa, &ca);
+    d.Pdp[b] = Vk * Vk * ykm.x - Vk * Vm * ykm.x * ca - Vk * Vm * ykm.y * sa;
+    d.Ppd[b] = Vm * Vm * ymk.x - Vm * Vk * ymk.x * ca - Vm * Vk * ymk.y * (-sa);
+    d.Qdp[b] = -Vk * Vk * (ykm.y + d.fl_bkm[b]) + Vk * Vm * ykm.y * ca - Vk * Vm * ykm.x * sa;
+    d.Qpd[b] = -Vm * Vm * (ymk.y + d.fl_bmk[b]) + Vm * Vk * ymk.y * ca - Vm * Vk * ymk.x * (-sa);
+}
+
+// ------------------------------------------------------------------ host side
+#define CK(call)                                                                     \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess) {                                                     \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));          \
+            return GBPF_E_CUDA;                                                      \
+        }                                                                            \
+    } while (0)
+
+struct Arena {
+    char *base = nullptr;
+    size_t size = 0, used = 0;
+    template <class T> T *take(size_t count) {
+        used = (used + 255) & ~size_t(255);
+        T *p = reinterpret_cast<T *>(base + used);
+        used += count * sizeof(T);
+        return p;
+    }
+};
+
+inline int cdiv_int(long long a, int b) { return (int)((a + b - 1) / b); }
+
+}  // namespace
+
+struct gbpf_solver {
+    Grid g;
+    YPattern y;
+    Symbolic S;
+    gbpf_options opt{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void *dmem = nullptr;
+    size_t dmem_size = 0;
+    Dev d{};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int graph_nodes = 0, kernels_per_iter = 0;
+    Ctl last{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    ~gbpf_solver() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (dmem) cudaFree(dmem);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    int nfl() const { return (int)S.flev_ptr.size() - 1; }
+    int nbl() const { return (int)S.blev_ptr.size() - 1; }
+
+    // Kernel launches of one Newton step after the mismatch: fill, factor,
+    // forward and backward substitution, update.
+    void launch_step(int guard) {
+        const int T = 256;
+        const int nq = S.n + 2 * S.nup;
+        k_jfill<<<cdiv_int(nq, T), T, 0, stream>>>(d, guard);
+        launch_factor_solve(guard);
+        k_update<<<cdiv_int(S.n, T), T, 0, stream>>>(d, guard);
+    }
+    void launch_factor_solve(int guard) {
+        const int T = 256, W = T / 32;
+        for (int l = 0; l < nfl(); l++) {
+            const int beg = S.flev_ptr[l], cnt = S.flev_ptr[l + 1] - beg;
+            k_factor<<<cdiv_int(cnt, W), T, 0, stream>>>(d, beg, cnt, guard);
+        }
+        for (int l = 0; l < nbl(); l++) {
+            const int beg = S.blev_ptr[l], cnt = S.blev_ptr[l + 1] - beg;
+            k_bsolve<<<cdiv_int(cnt, W), T, 0, stream>>>(d, beg, cnt, guard);
+        }
+    }
+    void launch_eval(int guard) {  // injections, limits, mismatch
+        const int T = 256;
+        k_phasor<<<cdiv_int(g.nB, T), T, 0, stream>>>(d, guard);
+        k_pq<<<cdiv_int(4LL * g.nB, T), T, 0, stream>>>(d, guard);
+        if (opt.lim_inj_reat && g.nPV) k_limits<<<cdiv_int(g.nPV, T), T, 0, stream>>>(d, guard);
+        k_mismatch<<<cdiv_int(S.n, T), T, 0, stream>>>(d, guard);
+    }
+
+    gbpf_status build(const Grid &grid, const gbpf_options &o, int dev);
+    gbpf_status build_graph();
+    gbpf_status run(gbpf_result *r);
+};
+
+gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev) {
+    g = grid;
+    opt = o;
+    device = dev;
+    if (g.nB < 2 || g.slack < 1) { set_error("grid needs at least two buses and one slack"); return GBPF_E_INPUT; }
+    if (o.no_max_iter < 0) { set_error("no_max_iter < 0"); return GBPF_E_INPUT; }
+    for (int b = 0; b < g.nL; b++)
+        if (g.r[b] == 0.0 && g.x[b] == 0.0) { set_error("branch with zero impedance"); return GBPF_E_INPUT; }
+    y = gbpf::build_ypattern(g);
+    std::string why;
+    S = gbpf::analyse(g, y, &why);
+    if (S.n != g.nB - 1) { set_error("symbolic analysis failed: " + why); return GBPF_E_INPUT; }
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&ev0));
+    CK(cudaEventCreate(&ev1));
+
+    const int nB = g.nB, nL = g.nL, n = S.n, nup = S.nup, nq = n + 2 * nup;
+    const long long npairs = S.pairs();
+    const int hist_cap = std::max(o.no_max_iter, 0) + 2;
+    // flows: slot of (k,m), (m,k); phif / bshf of each branch (GPU/PQcalc.cuh:32-97)
+    std::vector<int> skm(nL), smk(nL);
+    std::vector<double> fphi(nL), fbkm(nL), fbmk(nL);
+    for (int b = 0; b < nL; b++) {
+        const int k = g.de[b], m = g.para[b];
+        skm[b] = y.find(k - 1, m - 1);
+        smk[b] = y.find(m - 1, k - 1);
+        double ph = 0;
+        bool found = false;
+        for (int i = 0; i < nL; i++) if (g.de[i] == k && g.para[i] == m) { ph = g.phase[i]; found = true; break; }
+        if (!found) for (int i = 0; i < nL; i++) if (g.de[i] == m && g.para[i] == k) { ph = -g.phase[i]; break; }
+        fphi[b] = ph;
+        auto bshf = [&](int a, int c) {
+            for (int i = 0; i < nL; i++) {
+                if (g.de[i] == a) { if (g.para[i] == c) return g.bch[i]; }
+                else if (g.para[i] == a && g.de[i] == c) return g.bch[i];
+            }
+            return 0.0;
+        };
+        fbkm[b] = bshf(k, m);
+        fbmk[b] = bshf(m, k);
+    }
+
+    // one arena for everything
+    Arena A;
+    for (int pass = 0; pass < 2; pass++) {
+        A.used = 0;
+        d = Dev{};
+        d.nB = nB; d.nL = nL; d.nnzY = y.nnz; d.slack = g.slack - 1; d.nPV = g.nPV;
+        d.n = n; d.nup = nup; d.max_iter = o.no_max_iter; d.lim = o.lim_inj_reat; d.tol = o.tolerancia;
+        d.hist_cap = hist_cap;
+        d.yptr = A.take<int>(nB + 1); d.ycol = A.take<int>(y.nnz); d.yval = A.take<double2>(y.nnz);
+        d.cptr = A.take<int>(y.nnz + 1); d.csrc = A.take<int>(y.csrc.size());
+        d.stamp = A.take<double2>(4 * (size_t)nL + 1);
+        d.br_f = A.take<int>(nL + 1); d.br_t = A.take<int>(nL + 1);
+        d.br_r = A.take<double>(nL + 1); d.br_x = A.take<double>(nL + 1); d.br_b = A.take<double>(nL + 1);
+        d.br_tre = A.take<double>(nL + 1); d.br_tim = A.take<double>(nL + 1);
+        d.gsh = A.take<double>(nB); d.bsh = A.take<double>(nB);
+        d.V = A.take<double>(nB); d.th = A.take<double>(nB); d.cs = A.take<double>(nB); d.sn = A.take<double>(nB);
+        d.P = A.take<double>(nB); d.Q = A.take<double>(nB);
+        d.V0 = A.take<double>(nB); d.th0 = A.take<double>(nB); d.Pliq = A.take<double>(nB); d.Qliq = A.take<double>(nB);
+        d.Qload = A.take<double>(nB); d.type = A.take<int>(nB); d.act = A.take<int>(nB); d.QliqLim = A.take<double>(nB);
+        d.pv_bus = A.take<int>(g.nPV + 1); d.Qmin = A.take<double>(g.nPV + 1); d.Qmax = A.take<double>(g.nPV + 1);
+        d.limQ = A.take<int>(g.nPV + 1);
+        d.bus_of_blk = A.take<int>(n); d.blk_of_bus = A.take<int>(nB);
+        d.up_ptr = A.take<int>(n + 1); d.up_col = A.take<int>(nup + 1);
+        d.dg_ptr = A.take<int>(n + 1); d.dg_pos = A.take<int>(nup + 1); d.dg_k = A.take<int>(nup + 1);
+        d.og_ptr = A.take<long long>(nup + 1); d.og_a = A.take<int>(npairs + 1); d.og_b = A.take<int>(npairs + 1);
+        d.flev_steps = A.take<int>(n); d.blev_steps = A.take<int>(n);
+        d.ysl = A.take<int>(nq); d.rbus = A.take<int>(nq); d.cbus = A.take<int>(nq);
+        d.fac = A.take<blk4>(nq); d.dinv = A.take<blk4>(n);
+        d.rhs = A.take<double2>(n); d.ys = A.take<double2>(n); d.xs = A.take<double2>(n);
+        d.ctl = A.take<Ctl>(1); d.hist = A.take<double>(hist_cap); d.trig = A.take<int>(hist_cap);
+        d.events = A.take<int>(4 * kEventCap);
+        d.fl_skm = A.take<int>(nL + 1); d.fl_smk = A.take<int>(nL + 1);
+        d.fl_phi = A.take<double>(nL + 1); d.fl_bkm = A.take<double>(nL + 1); d.fl_bmk = A.take<double>(nL + 1);
+        d.Pdp = A.take<double>(nL + 1); d.Ppd = A.take<double>(nL + 1); d.Qdp = A.take<double>(nL + 1);
+        d.Qpd = A.take<double>(nL + 1);
+        if (pass == 0) {
+            dmem_size = A.used + 256;
+            cudaError_t e = cudaMalloc(&dmem, dmem_size);
+            if (e != cudaSuccess) { set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e)); return GBPF_E_OOM; }
+            A.base = (char *)dmem;
+            A.size = dmem_size;
+        }
+    }
+    CK(cudaMemsetAsync(dmem, 0, dmem_size, stream));
+    auto up = [&](const void *dst, const void *src, size_t bytes) -> cudaError_t {
+        if (!bytes) return cudaSuccess;
+        return cudaMemcpyAsync(const_cast<void *>(dst), src, bytes, cudaMemcpyHostToDevice, stream);
+    };
+    std::vector<int> f0(nL), t0(nL), pv0(g.nPV);
+    for (int b = 0; b < nL; b++) { f0[b] = g.de[b] - 1; t0[b] = g.para[b] - 1; }
+    for (int i = 0; i < g.nPV; i++) pv0[i] = g.pv[i] - 1;
+    std::vector<double> pliq(nB), qliq(nB);
+    for (int k = 0; k < nB; k++) { pliq[k] = g.Pliq(k); qliq[k] = g.Qliq(k); }
+    CK(up(d.yptr, y.rowptr.data(), (nB + 1) * sizeof(int)));
+    CK(up(d.ycol, y.col.data(), y.nnz * sizeof(int)));
+    CK(up(d.cptr, y.cptr.data(), (y.nnz + 1) * sizeof(int)));
+    CK(up(d.csrc, y.csrc.data(), y.csrc.size() * sizeof(int)));
+    CK(up(d.br_f, f0.data(), nL * sizeof(int)));
+    CK(up(d.br_t, t0.data(), nL * sizeof(int)));
+    CK(up(d.br_r, g.r.data(), nL * sizeof(double)));
+    CK(up(d.br_x, g.x.data(), nL * sizeof(double)));
+    CK(up(d.br_b, g.bch.data(), nL * sizeof(double)));
+    CK(up(d.br_tre, g.tap_re.data(), nL * sizeof(double)));
+    CK(up(d.br_tim, g.tap_im.data(), nL * sizeof(double)));
+    CK(up(d.gsh, g.gsh.data(), nB * sizeof(double)));
+    CK(up(d.bsh, g.bsh.data(), nB * sizeof(double)));
+    CK(up(d.V0, g.V0.data(), nB * sizeof(double)));
+    CK(up(d.th0, g.theta0.data(), nB * sizeof(double)));
+    CK(up(d.Pliq, pliq.data(), nB * sizeof(double)));
+    CK(up(d.Qliq, qliq.data(), nB * sizeof(double)));
+    CK(up(d.Qload, g.Qload.data(), nB * sizeof(double)));
+    CK(up(d.type, g.type.data(), nB * sizeof(int)));
+    CK(up(d.pv_bus, pv0.data(), g.nPV * sizeof(int)));
+    CK(up(d.Qmin, g.Qmin.data(), g.nPV * sizeof(double)));
+    CK(up(d.Qmax, g.Qmax.data(), g.nPV * sizeof(double)));
+    CK(up(d.bus_of_blk, S.bus_of_blk.data(), n * sizeof(int)));
+    CK(up(d.blk_of_bus, S.blk_of_bus.data(), nB * sizeof(int)));
+    CK(up(d.up_ptr, S.up_ptr.data(), (n + 1) * sizeof(int)));
+    CK(up(d.up_col, S.up_col.data(), nup * sizeof(int)));
+    CK(up(d.dg_ptr, S.dg_ptr.data(), (n + 1) * sizeof(int)));
+    CK(up(d.dg_pos, S.dg_pos.data(), nup * sizeof(int)));
+    CK(up(d.dg_k, S.dg_k.data(), nup * sizeof(int)));
+    CK(up(d.og_ptr, S.og_ptr.data(), (nup + 1) * sizeof(long long)));
+    CK(up(d.og_a, S.og_a.data(), npairs * sizeof(int)));
+    CK(up(d.og_b, S.og_b.data(), npairs * sizeof(int)));
+    CK(up(d.flev_steps, S.flev_steps.data(), n * sizeof(int)));
+    CK(up(d.blev_steps, S.blev_steps.data(), n * sizeof(int)));
+    CK(up(d.ysl, S.ysl.data(), nq * sizeof(int)));
+    CK(up(d.rbus, S.rbus.data(), nq * sizeof(int)));
+    CK(up(d.cbus, S.cbus.data(), nq * sizeof(int)));
+    CK(up(d.fl_skm, skm.data(), nL * sizeof(int)));
+    CK(up(d.fl_smk, smk.data(), nL * sizeof(int)));
+    CK(up(d.fl_phi, fphi.data(), nL * sizeof(double)));
+    CK(up(d.fl_bkm, fbkm.data(), nL * sizeof(double)));
+    CK(up(d.fl_bmk, fbmk.data(), nL * sizeof(double)));
+    // Ybus on the device, once per topology
+    const int T = 256;
+    if (nL) k_ybus_stamps<<<cdiv_int(nL, T), T, 0, stream>>>(d);
+    k_ybus_sum<<<cdiv_int(y.nnz, T), T, 0, stream>>>(d);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(stream));
+    return build_graph();
+}
+
+gbpf_status gbpf_solver::build_graph() {
+    CK(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault));
+    // prologue: reset, injections, limits (inactive at iteration 0), mismatch, test
+    CK(cudaStreamBeginCaptureToGraph(stream, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const int T = 256;
+    k_reset<<<cdiv_int(std::max(g.nB, d.hist_cap), T), T, 0, stream>>>(d);
+    launch_eval(0);
+    k_control<<<1, 1, 0, stream>>>(d, h, 1);
+    cudaStreamCaptureStatus cst;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    CK(cudaStreamGetCaptureInfo(stream, &cst, nullptr, nullptr, &deps, nullptr, &ndeps));
+    std::vector<cudaGraphNode_t> last(deps, deps + ndeps);
+    cudaGraph_t g2 = nullptr;
+    CK(cudaStreamEndCapture(stream, &g2));
+    // WHILE node: one Newton iteration per pass
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    CK(cudaGraphAddNode(&wnode, graph, last.data(), nullptr, last.size(), &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    launch_step(1);
+    launch_eval(1);
+    k_control<<<1, 1, 0, stream>>>(d, h, 1);
+    CK(cudaStreamEndCapture(stream, &g2));
+    // epilogue: branch flows of the returned state
+    CK(cudaStreamBeginCaptureToGraph(stream, graph, &wnode, nullptr, 1, cudaStreamCaptureModeThreadLocal));
+    if (g.nL) k_flows<<<cdiv_int(g.nL, T), T, 0, stream>>>(d);
+    CK(cudaStreamEndCapture(stream, &g2));
+    CK(cudaGraphInstantiate(&exec, graph, 0));
+    size_t nn = 0;
+    CK(cudaGraphGetNodes(graph, nullptr, &nn));
+    graph_nodes = (int)nn;
+    kernels_per_iter = nfl() + nbl() + 3 + 3 + (opt.lim_inj_reat && g.nPV ? 1 : 0) + 1;
+    return GBPF_OK;
+}
+
+gbpf_status gbpf_solver::run(gbpf_result *r) {
+    CK(cudaSetDevice(device));
+    CK(cudaGraphLaunch(exec, stream));
+    CK(cudaMemcpyAsync(&last, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    if (r) {
+        r->status = last.status;
+        r->converged = last.converged;
+        r->iterations = last.it;
+        r->n_events = last.n_events;
+        std::memcpy(&r->final_mismatch, &last.maxG, sizeof(double));
+        int npq = 0;
+        // nPQlim = original PQ buses + PV buses at a limit (read back with the events)
+        std::vector<int> lq(g.nPV);
+        if (g.nPV) CK(cudaMemcpy(lq.data(), d.limQ, g.nPV * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int v : lq) npq += v;
+        r->nPQlim = g.nPQ + npq;
+    }
+    return last.status == GBPF_OK ? GBPF_OK : (gbpf_status)last.status;
+}
+
+// ---------------------------------------------------------------------- C ABI
+
+#define ARGCHECK(c) do { if (!(c)) { set_error("invalid argument: " #c); return GBPF_E_ARG; } } while (0)
+
+extern "C" gbpf_status gbpf_solver_create(const gbpf_grid *g, const gbpf_options *o, int device,
+                                          gbpf_solver **out) {
+    ARGCHECK(g && o && out);
+    *out = nullptr;
+    auto s = std::make_unique<gbpf_solver>();
+    gbpf_status st = s->build(g->g, *o, device);
+    if (st != GBPF_OK) return st;
+    *out = s.release();
+    return GBPF_OK;
+}
+
+extern "C" void gbpf_solver_free(gbpf_solver *s) { delete s; }
+
+extern "C" gbpf_status gbpf_solve(gbpf_solver *s, gbpf_result *r) {
+    ARGCHECK(s);
+    return s->run(r);
+}
+
+extern "C" gbpf_status gbpf_solver_set_start(gbpf_solver *s, const double *V0, const double *theta0,
+                                             const double *Pliq, const double *Qliq) {
+    ARGCHECK(s);
+    const size_t b = s->g.nB * sizeof(double);
+    CK(cudaSetDevice(s->device));
+    if (V0) CK(cudaMemcpyAsync(s->d.V0, V0, b, cudaMemcpyHostToDevice, s->stream));
+    if (theta0) CK(cudaMemcpyAsync(s->d.th0, theta0, b, cudaMemcpyHostToDevice, s->stream));
+    if (Pliq) CK(cudaMemcpyAsync(s->d.Pliq, Pliq, b, cudaMemcpyHostToDevice, s->stream));
+    if (Qliq) CK(cudaMemcpyAsync(s->d.Qliq, Qliq, b, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_solver_state(gbpf_solver *s, double *V, double *theta, double *Pcalc,
+                                         double *Qcalc) {
+    ARGCHECK(s);
+    const size_t b = s->g.nB * sizeof(double);
+    CK(cudaSetDevice(s->device));
+    if (V) CK(cudaMemcpyAsync(V, s->d.V, b, cudaMemcpyDeviceToHost, s->stream));
+    if (theta) CK(cudaMemcpyAsync(theta, s->d.th, b, cudaMemcpyDeviceToHost, s->stream));
+    if (Pcalc) CK(cudaMemcpyAsync(Pcalc, s->d.P, b, cudaMemcpyDeviceToHost, s->stream));
+    if (Qcalc) CK(cudaMemcpyAsync(Qcalc, s->d.Q, b, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_solver_events(gbpf_solver *s, int *ev, int cap, int *n) {
+    ARGCHECK(s && n && (cap == 0 || ev));
+    CK(cudaSetDevice(s->device));
+    Ctl c;
+    CK(cudaMemcpy(&c, s->d.ctl, sizeof c, cudaMemcpyDeviceToHost));
+    const int have = std::min(c.n_events, kEventCap);
+    std::vector<int> e(4 * (size_t)have);
+    if (have) CK(cudaMemcpy(e.data(), s->d.events, e.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    // events of one iteration were appended in arbitrary order: sort by
+    // (iteration, PV position), the order chkLimQ prints them
+    std::vector<int> idx(have);
+    for (int i = 0; i < have; i++) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) {
+        return e[4 * a] != e[4 * b] ? e[4 * a] < e[4 * b] : e[4 * a + 2] < e[4 * b + 2];
+    });
+    const int m = std::min(have, cap);
+    for (int i = 0; i < m; i++) std::copy(&e[4 * idx[i]], &e[4 * idx[i]] + 4, ev + 4 * i);
+    *n = m;
+    return c.n_events > kEventCap ? GBPF_E_ARG : GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_solver_history(gbpf_solver *s, double *hist, int cap, int *n) {
+    ARGCHECK(s && n && (cap == 0 || hist));
+    CK(cudaSetDevice(s->device));
+    Ctl c;
+    CK(cudaMemcpy(&c, s->d.ctl, sizeof c, cudaMemcpyDeviceToHost));
+    const int have = std::min(c.it + 1, s->d.hist_cap);
+    const int m = std::min(have, cap);
+    if (m) CK(cudaMemcpy(hist, s->d.hist, m * sizeof(double), cudaMemcpyDeviceToHost));
+    *n = m;
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_solver_triggers(gbpf_solver *s, int *trig, int cap, int *n) {
+    ARGCHECK(s && n && (cap == 0 || trig));
+    CK(cudaSetDevice(s->device));
+    Ctl c;
+    CK(cudaMemcpy(&c, s->d.ctl, sizeof c, cudaMemcpyDeviceToHost));
+    const int have = std::min(c.it + 1, s->d.hist_cap);
+    const int m = std::min(have, cap);
+    if (m) CK(cudaMemcpy(trig, s->d.trig, m * sizeof(int), cudaMemcpyDeviceToHost));
+    *n = m;
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_solver_flows(gbpf_solver *s, double *Pdp, double *Ppd, double *Qdp,
+                                         double *Qpd) {
+    ARGCHECK(s);
+    const size_t b = s->g.nL * sizeof(double);
+    CK(cudaSetDevice(s->device));
+    if (Pdp) CK(cudaMemcpy(Pdp, s->d.Pdp, b, cudaMemcpyDeviceToHost));
+    if (Ppd) CK(cudaMemcpy(Ppd, s->d.Ppd, b, cudaMemcpyDeviceToHost));
+    if (Qdp) CK(cudaMemcpy(Qdp, s->d.Qdp, b, cudaMemcpyDeviceToHost));
+    if (Qpd) CK(cudaMemcpy(Qpd, s->d.Qpd, b, cudaMemcpyDeviceToHost));
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_solver_info(const gbpf_solver *s, long long info[8]) {
+    ARGCHECK(s && info);
+    info[0] = s->g.nB;
+    info[1] = s->S.n;
+    info[2] = s->S.nup;
+    info[3] = s->S.pairs();
+    info[4] = s->nfl();
+    info[5] = s->nbl();
+    info[6] = s->graph_nodes;
+    info[7] = s->kernels_per_iter;
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_solver_time(gbpf_solver *s, int repeats, double *ms_total) {
+    ARGCHECK(s && ms_total && repeats > 0);
+    CK(cudaSetDevice(s->device));
+    CK(cudaEventRecord(s->ev0, s->stream));
+    for (int i = 0; i < repeats; i++) CK(cudaGraphLaunch(s->exec, s->stream));
+    CK(cudaEventRecord(s->ev1, s->stream));
+    CK(cudaEventSynchronize(s->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    *ms_total = ms;
+    CK(cudaMemcpy(&s->last, s->d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_ybus(gbpf_solver *s, int *rowptr, int *col, double *re, double *im) {
+    ARGCHECK(s);
+    CK(cudaSetDevice(s->device));
+    const int nnz = s->y.nnz;
+    std::vector<double2> v(nnz);
+    CK(cudaMemcpy(v.data(), s->d.yval, nnz * sizeof(double2), cudaMemcpyDeviceToHost));
+    if (rowptr) std::copy(s->y.rowptr.begin(), s->y.rowptr.end(), rowptr);
+    if (col) std::copy(s->y.col.begin(), s->y.col.end(), col);
+    for (int i = 0; i < nnz; i++) {
+        if (re) re[i] = v[i].x;
+        if (im) im[i] = v[i].y;
+    }
+    return GBPF_OK;
+}
+
+// Loads (V, theta) and the limit flags into the solver state, and evaluates the
+// injections (no graph, plain launches on the solver stream).
+static gbpf_status load_state(gbpf_solver *s, const double *V, const double *theta, const int *limQ) {
+    const Grid &g = s->g;
+    const size_t b = g.nB * sizeof(double);
+    CK(cudaSetDevice(s->device));
+    CK(cudaMemcpyAsync(s->d.V, V, b, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->d.th, theta, b, cudaMemcpyHostToDevice, s->stream));
+    std::vector<int> act(g.nB);
+    for (int k = 0; k < g.nB; k++) act[k] = (g.type[k] == 0 || g.type[k] == 1);
+    for (int i = 0; i < g.nPV; i++) act[g.pv[i] - 1] = limQ ? (limQ[i] != 0) : 0;
+    CK(cudaMemcpyAsync(s->d.act, act.data(), g.nB * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(s->d.ctl, 0, sizeof(Ctl), s->stream));
+    const int T = 256;
+    k_phasor<<<cdiv_int(g.nB, T), T, 0, s->stream>>>(s->d, 0);
+    k_pq<<<cdiv_int(4LL * g.nB, T), T, 0, s->stream>>>(s->d, 0);
+    CK(cudaGetLastError());
+    // act[] must outlive the async copy
+    CK(cudaStreamSynchronize(s->stream));
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_eval_pq(gbpf_solver *s, const double *V, const double *theta, double *P,
+                                    double *Q) {
+    ARGCHECK(s && V && theta);
+    gbpf_status st = load_state(s, V, theta, nullptr);
+    if (st != GBPF_OK) return st;
+    const size_t b = s->g.nB * sizeof(double);
+    if (P) CK(cudaMemcpy(P, s->d.P, b, cudaMemcpyDeviceToHost));
+    if (Q) CK(cudaMemcpy(Q, s->d.Q, b, cudaMemcpyDeviceToHost));
+    return GBPF_OK;
+}
+
+// Reference numbering of the Jacobian (Jstencil0based, GPU/esparso.h:61-178):
+// P row / theta column of bus k -> k - (k > slack); Q row / V column of an
+// active bus -> nB-1 + its position in the ascending list of active buses.
+static void ref_numbering(const gbpf_solver *s, const int *limQ, std::vector<int> &pn, std::vector<int> &qn) {
+    const Grid &g = s->g;
+    const int sl = g.slack - 1;
+    std::vector<int> act(g.nB);
+    for (int k = 0; k < g.nB; k++) act[k] = (g.type[k] == 0 || g.type[k] == 1);
+    for (int i = 0; i < g.nPV; i++) act[g.pv[i] - 1] = limQ ? (limQ[i] != 0) : 0;
+    pn.assign(g.nB, -1);
+    qn.assign(g.nB, -1);
+    int c = 0;
+    for (int k = 0; k < g.nB; k++) if (k != sl) pn[k] = k - (k > sl);
+    for (int k = 0; k < g.nB; k++) if (k != sl && act[k]) qn[k] = g.nB - 1 + c++;
+}
+
+extern "C" gbpf_status gbpf_eval_jacobian(gbpf_solver *s, const double *V, const double *theta,
+                                          const int *limQ, int *row, int *col, double *val, int cap,
+                                          int *nnz) {
+    ARGCHECK(s && V && theta && nnz);
+    gbpf_status st = load_state(s, V, theta, limQ);
+    if (st != GBPF_OK) return st;
+    const Symbolic &S = s->S;
+    const int nq = S.n + 2 * S.nup, T = 256;
+    k_jfill<<<cdiv_int(nq, T), T, 0, s->stream>>>(s->d, 0);
+    CK(cudaGetLastError());
+    std::vector<blk4> f(nq);
+    CK(cudaMemcpyAsync(f.data(), s->d.fac, nq * sizeof(blk4), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    std::vector<int> pn, qn;
+    ref_numbering(s, limQ, pn, qn);
+    int m = 0;
+    for (int q = 0; q < nq; q++) {
+        if (S.ysl[q] < 0) continue;
+        const int k = S.rbus[q], c = S.cbus[q];
+        const double e[4] = {f[q].x, f[q].y, f[q].z, f[q].w};
+        const int rr[4] = {pn[k], pn[k], qn[k], qn[k]}, cc[4] = {pn[c], qn[c], pn[c], qn[c]};
+        for (int t = 0; t < 4; t++) {
+            if (rr[t] < 0 || cc[t] < 0) continue;
+            if (m < cap) { row[m] = rr[t]; col[m] = cc[t]; val[m] = e[t]; }
+            m++;
+        }
+    }
+    *nnz = m;
+    return m > cap ? GBPF_E_ARG : GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_newton_step(gbpf_solver *s, const double *V, const double *theta,
+                                        const int *limQ, const double *gref, double *dx) {
+    ARGCHECK(s && V && theta && gref && dx);
+    gbpf_status st = load_state(s, V, theta, limQ);
+    if (st != GBPF_OK) return st;
+    const Symbolic &S = s->S;
+    std::vector<int> pn, qn;
+    ref_numbering(s, limQ, pn, qn);
+    std::vector<double2> rhs(S.n);
+    for (int j = 0; j < S.n; j++) {
+        const int k = S.bus_of_blk[j];
+        rhs[j] = make_double2(gref[pn[k]], qn[k] >= 0 ? gref[qn[k]] : 0.0);
+    }
+    CK(cudaMemcpyAsync(s->d.rhs, rhs.data(), S.n * sizeof(double2), cudaMemcpyHostToDevice, s->stream));
+    const int nq = S.n + 2 * S.nup, T = 256;
+    k_jfill<<<cdiv_int(nq, T), T, 0, s->stream>>>(s->d, 0);
+    s->launch_factor_solve(0);
+    CK(cudaGetLastError());
+    std::vector<double2> x(S.n);
+    Ctl c;
+    CK(cudaMemcpyAsync(x.data(), s->d.xs, S.n * sizeof(double2), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(&c, s->d.ctl, sizeof c, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (c.status == GBPF_E_SINGULAR) { set_error("singular Jacobian"); return GBPF_E_SINGULAR; }
+    for (int j = 0; j < S.n; j++) {
+        const int k = S.bus_of_blk[j];
+        dx[pn[k]] = x[j].x;
+        if (qn[k] >= 0) dx[qn[k]] = x[j].y;
+    }
+    return GBPF_OK;
+}
+
+extern "C" const char *gbpf_last_error(void) { return gbpf::last_error().c_str(); }
+
+extern "C" const char *gbpf_status_str(gbpf_status st) {
+    switch (st) {
+    case GBPF_OK: return "ok";
+    case GBPF_E_INPUT: return "invalid input";
+    case GBPF_E_SINGULAR: return "singular Jacobian";
+    case GBPF_E_NOCONV: return "no convergence";
+    case GBPF_E_CUDA: return "CUDA error";
+    case GBPF_E_TIMEOUT: return "device wait timed out";
+    case GBPF_E_OOM: return "out of memory";
+    case GBPF_E_ARG: return "invalid argument";
+    case GBPF_E_UNSUPPORTED: return "unsupported";
+    }
+    return "unknown status";
+}

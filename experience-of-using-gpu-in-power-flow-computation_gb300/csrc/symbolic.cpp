@@ -1,0 +1,256 @@
+// symbolic.cpp -- once-per-topology analysis on the host: Ybus pattern and
+// assembly map, fill-reducing ordering of the buses, symbolic block LU of the
+// Newton Jacobian, its Crout gather lists and level schedules, and the map
+// from factor block positions to Ybus slots used by the Jacobian fill.
+#include <algorithm>
+#include <numeric>
+#include <queue>
+#include <string>
+#include <vector>
+
+#include "gbpf_internal.h"
+
+namespace gbpf {
+
+int YPattern::find(int r, int c) const {
+    auto b = col.begin() + rowptr[r], e = col.begin() + rowptr[r + 1];
+    auto it = std::lower_bound(b, e, c);
+    return (it != e && *it == c) ? (int)(it - col.begin()) : -1;
+}
+
+// Pattern of calcYbusSp_eficinte (GPU/sistema.h:705-758): four stamps per
+// branch and one shunt per bus, duplicates summed.  Slot contributions are
+// listed in the order Eigen's setFromTriplets adds them: the stamps of branch
+// 0 (de,para), (para,de), (de,de), (para,para), then branch 1, ..., then the
+// bus shunts.
+YPattern build_ypattern(const Grid &g) {
+    YPattern y;
+    const int n = g.nB;
+    y.n = n;
+    std::vector<std::vector<int>> rows(n);
+    for (int k = 0; k < n; k++) rows[k].push_back(k);
+    for (int b = 0; b < g.nL; b++) {
+        const int f = g.de[b] - 1, t = g.para[b] - 1;
+        rows[f].push_back(t);
+        rows[t].push_back(f);
+    }
+    y.rowptr.assign(n + 1, 0);
+    for (int k = 0; k < n; k++) {
+        auto &r = rows[k];
+        std::sort(r.begin(), r.end());
+        r.erase(std::unique(r.begin(), r.end()), r.end());
+        y.rowptr[k + 1] = y.rowptr[k] + (int)r.size();
+    }
+    y.nnz = y.rowptr[n];
+    y.col.resize(y.nnz);
+    for (int k = 0; k < n; k++) std::copy(rows[k].begin(), rows[k].end(), y.col.begin() + y.rowptr[k]);
+    y.diag.resize(n);
+    for (int k = 0; k < n; k++) y.diag[k] = y.find(k, k);
+    // contributions in triplet order
+    std::vector<int> cnt(y.nnz, 0);
+    std::vector<std::pair<int, int>> trip;  // (slot, source)
+    trip.reserve(4 * g.nL + n);
+    for (int b = 0; b < g.nL; b++) {
+        const int f = g.de[b] - 1, t = g.para[b] - 1;
+        trip.push_back({y.find(f, t), 4 * b + 0});
+        trip.push_back({y.find(t, f), 4 * b + 1});
+        trip.push_back({y.find(f, f), 4 * b + 2});
+        trip.push_back({y.find(t, t), 4 * b + 3});
+    }
+    for (int k = 0; k < n; k++) trip.push_back({y.diag[k], -1 - k});
+    for (auto &p : trip) cnt[p.first]++;
+    y.cptr.assign(y.nnz + 1, 0);
+    for (int s = 0; s < y.nnz; s++) y.cptr[s + 1] = y.cptr[s] + cnt[s];
+    y.csrc.resize(trip.size());
+    std::vector<int> fill(y.cptr.begin(), y.cptr.end() - 1);
+    for (auto &p : trip) y.csrc[fill[p.first]++] = p.second;
+    return y;
+}
+
+// Minimum degree on an explicit elimination graph (ties broken by the lower
+// index), giving the order in which blocks are eliminated.
+std::vector<int> min_degree_order(int n, const std::vector<std::vector<int>> &adj0) {
+    std::vector<std::vector<int>> adj(adj0);
+    std::vector<int> deg(n), mark(n, 0), done(n, 0), order;
+    order.reserve(n);
+    int stamp = 0;
+    using E = std::pair<int, int>;
+    std::priority_queue<E, std::vector<E>, std::greater<E>> pq;
+    for (int i = 0; i < n; i++) { deg[i] = (int)adj[i].size(); pq.push({deg[i], i}); }
+    std::vector<int> nb, tmp;
+    while ((int)order.size() < n) {
+        E e = pq.top();
+        pq.pop();
+        const int p = e.second;
+        if (done[p] || e.first != deg[p]) continue;
+        done[p] = 1;
+        order.push_back(p);
+        nb.clear();
+        for (int v : adj[p]) if (!done[v]) nb.push_back(v);
+        for (int u : nb) {
+            ++stamp;
+            mark[u] = stamp;
+            tmp.clear();
+            for (int v : adj[u]) if (v != p && !done[v] && mark[v] != stamp) { mark[v] = stamp; tmp.push_back(v); }
+            for (int v : nb) if (mark[v] != stamp) { mark[v] = stamp; tmp.push_back(v); }
+            adj[u] = tmp;
+            deg[u] = (int)tmp.size();
+            pq.push({deg[u], u});
+        }
+        adj[p].clear();
+        adj[p].shrink_to_fit();
+    }
+    return order;
+}
+
+Symbolic analyse(const Grid &g, const YPattern &y, std::string *why) {
+    Symbolic S;
+    const int nB = g.nB, s = g.slack - 1, n = nB - 1;
+    S.n = n;
+    // bus graph without the slack
+    std::vector<int> cidx(nB, -1), cbus;
+    for (int k = 0; k < nB; k++) if (k != s) { cidx[k] = (int)cbus.size(); cbus.push_back(k); }
+    std::vector<std::vector<int>> adj(n);
+    for (int k = 0; k < nB; k++) {
+        if (k == s) continue;
+        for (int p = y.rowptr[k]; p < y.rowptr[k + 1]; p++) {
+            const int m = y.col[p];
+            if (m == s || m == k) continue;
+            adj[cidx[k]].push_back(cidx[m]);
+        }
+    }
+    std::vector<int> ord = min_degree_order(n, adj);
+    S.bus_of_blk.resize(n);
+    S.blk_of_bus.assign(nB, -1);
+    for (int b = 0; b < n; b++) {
+        S.bus_of_blk[b] = cbus[ord[b]];
+        S.blk_of_bus[cbus[ord[b]]] = b;
+    }
+    // lower structure of A in the new order: for column j, rows i > j
+    std::vector<std::vector<int>> alow(n);
+    for (int k = 0; k < nB; k++) {
+        if (k == s) continue;
+        const int bk = S.blk_of_bus[k];
+        for (int p = y.rowptr[k]; p < y.rowptr[k + 1]; p++) {
+            const int m = y.col[p];
+            if (m == s || m == k) continue;
+            const int bm = S.blk_of_bus[m];
+            if (bm > bk) alow[bk].push_back(bm);
+        }
+    }
+    // symbolic factorisation: struct(j) = alow(j) U (struct(c) \ {j}) over the
+    // elimination-tree children c of j
+    std::vector<std::vector<int>> st(n), children(n);
+    std::vector<int> mark(n, -1);
+    for (int j = 0; j < n; j++) {
+        std::vector<int> &out = st[j];
+        mark[j] = j;
+        for (int i : alow[j]) if (mark[i] != j) { mark[i] = j; out.push_back(i); }
+        for (int c : children[j])
+            for (int i : st[c]) if (i != j && mark[i] != j) { mark[i] = j; out.push_back(i); }
+        std::sort(out.begin(), out.end());
+        if (!out.empty()) children[out[0]].push_back(j);
+    }
+    S.up_ptr.assign(n + 1, 0);
+    for (int j = 0; j < n; j++) S.up_ptr[j + 1] = S.up_ptr[j] + (int)st[j].size();
+    S.nup = S.up_ptr[n];
+    S.up_col.resize(S.nup);
+    for (int j = 0; j < n; j++) std::copy(st[j].begin(), st[j].end(), S.up_col.begin() + S.up_ptr[j]);
+    auto pos_in = [&](int j, int i) -> int {
+        auto b = S.up_col.begin() + S.up_ptr[j], e = S.up_col.begin() + S.up_ptr[j + 1];
+        auto it = std::lower_bound(b, e, i);
+        return (it != e && *it == i) ? (int)(it - S.up_col.begin()) : -1;
+    };
+    // row structures rs(j) = {k : j in idx(k)}, k ascending, with positions
+    std::vector<int> rcnt(n, 0);
+    for (int p = 0; p < S.nup; p++) rcnt[S.up_col[p]]++;
+    S.dg_ptr.assign(n + 1, 0);
+    for (int j = 0; j < n; j++) S.dg_ptr[j + 1] = S.dg_ptr[j] + rcnt[j];
+    S.dg_pos.resize(S.nup);
+    S.dg_k.resize(S.nup);
+    {
+        std::vector<int> f(S.dg_ptr.begin(), S.dg_ptr.end() - 1);
+        for (int k = 0; k < n; k++)
+            for (int p = S.up_ptr[k]; p < S.up_ptr[k + 1]; p++) {
+                const int j = S.up_col[p];
+                S.dg_pos[f[j]] = p;
+                S.dg_k[f[j]] = k;
+                f[j]++;
+            }
+    }
+    // off-diagonal gather pairs: for k, a < b in idx(k): entry (j = idx(k)[a], i = idx(k)[b])
+    std::vector<long long> ocnt(S.nup, 0);
+    for (int k = 0; k < n; k++)
+        for (int a = S.up_ptr[k]; a < S.up_ptr[k + 1]; a++)
+            for (int b = a + 1; b < S.up_ptr[k + 1]; b++) {
+                const int p = pos_in(S.up_col[a], S.up_col[b]);
+                if (p < 0) { if (why) *why = "symbolic factorisation is not closed under fill"; return Symbolic(); }
+                ocnt[p]++;
+            }
+    S.og_ptr.assign(S.nup + 1, 0);
+    for (int p = 0; p < S.nup; p++) S.og_ptr[p + 1] = S.og_ptr[p] + ocnt[p];
+    const long long npairs = S.og_ptr[S.nup];
+    S.og_a.resize(npairs);
+    S.og_b.resize(npairs);
+    {
+        std::vector<long long> f(S.og_ptr.begin(), S.og_ptr.end() - 1);
+        for (int k = 0; k < n; k++)
+            for (int a = S.up_ptr[k]; a < S.up_ptr[k + 1]; a++)
+                for (int b = a + 1; b < S.up_ptr[k + 1]; b++) {
+                    const int p = pos_in(S.up_col[a], S.up_col[b]);
+                    S.og_a[f[p]] = a;
+                    S.og_b[f[p]] = b;
+                    f[p]++;
+                }
+    }
+    // level schedules
+    std::vector<int> fl(n, 0), bl(n, 0);
+    int nfl = 0, nbl = 0;
+    for (int j = 0; j < n; j++) {
+        int l = 0;
+        for (int q = S.dg_ptr[j]; q < S.dg_ptr[j + 1]; q++) l = std::max(l, fl[S.dg_k[q]] + 1);
+        fl[j] = l;
+        nfl = std::max(nfl, l + 1);
+    }
+    for (int j = n - 1; j >= 0; j--) {
+        int l = 0;
+        for (int p = S.up_ptr[j]; p < S.up_ptr[j + 1]; p++) l = std::max(l, bl[S.up_col[p]] + 1);
+        bl[j] = l;
+        nbl = std::max(nbl, l + 1);
+    }
+    auto bucket = [n](const std::vector<int> &lev, int nl, std::vector<int> &ptr, std::vector<int> &steps) {
+        ptr.assign(nl + 1, 0);
+        for (int j = 0; j < n; j++) ptr[lev[j] + 1]++;
+        for (int l = 0; l < nl; l++) ptr[l + 1] += ptr[l];
+        steps.resize(n);
+        std::vector<int> f(ptr.begin(), ptr.end() - 1);
+        for (int j = 0; j < n; j++) steps[f[lev[j]]++] = j;
+    };
+    bucket(fl, nfl, S.flev_ptr, S.flev_steps);
+    bucket(bl, nbl, S.blev_ptr, S.blev_steps);
+    // Jacobian fill map over factor block positions
+    const int nq = n + 2 * S.nup;
+    S.ysl.resize(nq);
+    S.rbus.resize(nq);
+    S.cbus.resize(nq);
+    for (int j = 0; j < n; j++) {
+        const int bj = S.bus_of_blk[j];
+        S.ysl[j] = y.diag[bj];
+        S.rbus[j] = bj;
+        S.cbus[j] = bj;
+    }
+    for (int j = 0; j < n; j++)
+        for (int p = S.up_ptr[j]; p < S.up_ptr[j + 1]; p++) {
+            const int bi = S.bus_of_blk[S.up_col[p]], bj = S.bus_of_blk[j];
+            const int ql = n + p, qu = n + S.nup + p;
+            S.ysl[ql] = y.find(bi, bj);  // L(i,j): row bus i, column bus j
+            S.rbus[ql] = bi;
+            S.cbus[ql] = bj;
+            S.ysl[qu] = y.find(bj, bi);  // U(j,i): row bus j, column bus i
+            S.rbus[qu] = bj;
+            S.cbus[qu] = bi;
+        }
+    return S;
+}
+
+}  // namespace gbpf

@@ -1,0 +1,258 @@
+/*
+ * gbpf.h -- C ABI of libgbpf, a GB300 (sm_103a) Newton-Raphson AC power-flow
+ * engine that is a drop-in for the solve path of
+ * joaovdd/Experience-of-Using-GPU-in-Power-Flow-Computation (GPU/ tree).
+ *
+ * The reference has no library interface: its boundary is the process
+ * (data.txt options + a common-data-format file in, a per-bus table and limit
+ * lines out) with the in-process call chain
+ *     loadFile()                      GPU/sistInfo.h:62-242
+ *  -> lerArquivoEAlocarMemoria()      GPU/arquivo.h:250-295
+ *  -> calcYbusSp_eficinte()           GPU/sistema.h:705-758
+ *  -> mNR()                           GPU/newtonRaphson.cuh:171-623
+ *  -> calcFluxf_Eficiente_Sp()        GPU/PQcalc.cuh:547-557
+ *  -> impressao2()                    GPU/impressao.h:47-80
+ * Each entry point below names the reference step it replaces.
+ *
+ * Conventions: plain C types only; the caller owns every host buffer; the
+ * library owns every device allocation; no entry point prints or exits; every
+ * entry point returns a gbpf_status.  One solver handle owns one CUDA stream
+ * and is not thread-safe; different handles may be used from different host
+ * threads.  Bus indices are 1-based in file order, as in the reference.
+ */
+#ifndef GBPF_H
+#define GBPF_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBPF_ABI_VERSION 1
+
+typedef enum {
+    GBPF_OK = 0,
+    GBPF_E_INPUT = 1,       /* malformed data.txt / CDF, inconsistent arrays      */
+    GBPF_E_SINGULAR = 2,    /* zero or non-finite pivot in the Jacobian LU        */
+    GBPF_E_NOCONV = 3,      /* no_max_iter reached with max|g| > tolerancia       */
+    GBPF_E_CUDA = 4,        /* CUDA runtime error (message via gbpf_last_error)   */
+    GBPF_E_TIMEOUT = 5,     /* a bounded device wait ran out                      */
+    GBPF_E_OOM = 6,         /* device or host allocation failed                   */
+    GBPF_E_ARG = 7,         /* NULL handle, bad size, buffer too small            */
+    GBPF_E_UNSUPPORTED = 8  /* option or input format outside the supported path */
+} gbpf_status;
+
+/* metodo values of data.txt (GPU/sistInfo.h:11-17, :89-118). */
+typedef enum {
+    GBPF_METODO_ESPARSO = 0,
+    GBPF_METODO_DENSO = 1,
+    GBPF_METODO_HIBRIDOA = 2,
+    GBPF_METODO_HIBRIDOB = 3,
+    GBPF_METODO_HIBRIDOC = 4,
+    GBPF_METODO_NDA = 5
+} gbpf_metodo;
+
+/* output_bench values (GPU/sistInfo.h:31-35, :190-203). */
+typedef enum { GBPF_BENCH_ALL = 0, GBPF_BENCH_SCREEN = 1, GBPF_BENCH_FILE = 2 } gbpf_output_bench;
+
+/* Numeric form of the linear solve (not a data.txt key of the reference). */
+typedef enum {
+    GBPF_PREC_FP64 = 0,       /* FP64 LU and triangular solves (oracle-matching) */
+    GBPF_PREC_FP32_IR = 1     /* FP32 LU and triangular solves + FP64 refinement  */
+} gbpf_precision;
+
+/* The data.txt options, namespace global of GPU/sistInfo.h:37-60, with the
+ * same defaults. */
+typedef struct {
+    int metodo;                 /* gbpf_metodo */
+    double v_inicial;           /* 1.0 */
+    double theta_inicial;       /* 0.0 */
+    double tolerancia;          /* 1e-4 */
+    int no_max_iter;            /* 100 */
+    int lim_inj_reat;           /* 0 */
+    int openmp;                 /* 1 */
+    int laconic_mode;           /* 0 */
+    int verbose_mode;           /* 0 */
+    int output_ans;             /* 1 */
+    int output_iter;            /* 0  (output_processo_iterativo) */
+    int streams;                /* 1 */
+    int output_bench;           /* gbpf_output_bench, GBPF_BENCH_ALL */
+    int precision;              /* gbpf_precision, GBPF_PREC_FP64 */
+    char arq_entrada[1024];     /* "ieee14.cdf" */
+} gbpf_options;
+
+/* Fills *o with the defaults of GPU/sistInfo.h:37-60. */
+gbpf_status gbpf_options_default(gbpf_options *o);
+
+/* loadFile (GPU/sistInfo.h:62-242) over the text of a data.txt, with the same
+ * key lookup (first occurrence of the key name, value between '=' and ';') and
+ * the same handling of absent keys.  The lines the reference echoes when
+ * laconic_mode is OFF are written to echo (may be NULL). */
+gbpf_status gbpf_options_parse(const char *text, gbpf_options *o, char *echo, size_t echo_cap);
+
+/* Same, reading the file at path (the reference reads "data.txt" from the
+ * working directory). */
+gbpf_status gbpf_options_load(const char *path, gbpf_options *o, char *echo, size_t echo_cap);
+
+/* ------------------------------------------------------------------------ */
+/* Grids: struct sistema / barra / ramo of GPU/sistema.h:24-126              */
+/* ------------------------------------------------------------------------ */
+
+typedef struct gbpf_grid gbpf_grid;
+
+/* lerArquivoEAlocarMemoria (GPU/arquivo.h:250-295): .cdf (GPU/sistema.h:
+ * 386-638) and .cdfx (GPU/arquivo.h:4-248).  Buses start at v_inicial /
+ * theta_inicial except PV and slack voltages and the slack angle, which come
+ * from the file.  Notices the reference prints while reading (parallel
+ * branches whose taps differ) are written to msg. */
+gbpf_status gbpf_grid_read(const char *path, double v_inicial, double theta_inicial,
+                           gbpf_grid **out, char *msg, size_t msg_cap);
+
+/* A grid from caller arrays (already-merged branches, 1-based bus indices).
+ * bus_type: 0/1 = PQ, 2 = PV, 3 = slack (exactly one).  Qmax/Qmin are per bus
+ * in p.u. (read for PV buses only).  V0 / theta0 are the starting state. */
+typedef struct {
+    int nB, nL;
+    double baseMVA;
+    const int *id, *bus_type;
+    const double *V0, *theta0, *Pload, *Qload, *Pg, *Qg, *gsh, *bsh, *Qmax, *Qmin;
+    const int *from_bus, *to_bus;
+    const double *r, *x, *bch, *tap_re, *tap_im, *phase;
+} gbpf_grid_desc;
+gbpf_status gbpf_grid_create(const gbpf_grid_desc *d, gbpf_grid **out);
+
+void gbpf_grid_free(gbpf_grid *g);
+
+/* dims[0..7] = nB, nL, nPV, nPQ, slack (1-based), nnzY, baseMVA, notices. */
+gbpf_status gbpf_grid_dims(const gbpf_grid *g, int dims[8]);
+
+/* Copies of the bus arrays ([nB] each; any pointer may be NULL). */
+gbpf_status gbpf_grid_buses(const gbpf_grid *g, int *id, int *type, double *V0, double *theta0,
+                            double *Pload, double *Qload, double *Pg, double *Qg,
+                            double *gsh, double *bsh);
+/* PV list with limits and setpoints ([nPV]) and PQ list ([nPQ]), 1-based. */
+gbpf_status gbpf_grid_pvpq(const gbpf_grid *g, int *pv, double *Qmin, double *Qmax,
+                           double *Vset, int *pq);
+/* Branch arrays ([nL]). */
+gbpf_status gbpf_grid_branches(const gbpf_grid *g, int *from_bus, int *to_bus, double *r,
+                               double *x, double *bch, double *tap_re, double *tap_im,
+                               double *phase);
+
+/* Replace loads, generation and the starting state of a grid (a scenario);
+ * NULL leaves an array unchanged.  Net injections are recomputed as
+ * Pg - Pload, Qg - Qload (GPU/sistema.h:546-547). */
+gbpf_status gbpf_grid_set_buses(gbpf_grid *g, const double *Pload, const double *Qload,
+                                const double *Pg, const double *Qg, const double *V0,
+                                const double *theta0);
+
+/* Writes the grid as a fixed-column common-data-format file that the reader
+ * above (and the reference's readCDF) reads back. */
+gbpf_status gbpf_grid_write_cdf(const gbpf_grid *g, const char *path, const char *title);
+
+/* Seeded synthetic grids (no counterpart in the reference, which ships IEEE
+ * cases only): kind 1 = 14-bus ring-plus-chords grid, 2 = 118-bus meshed grid,
+ * 3 = `tiles` copies of kind 2 tied into one grid (128 -> 15,104 buses,
+ * 16 -> 1,888 buses), 4 = a kind-1-style grid scaled to `nbus` buses. */
+gbpf_status gbpf_generate(int kind, unsigned long long seed, int tiles, int nbus, gbpf_grid **out);
+
+/* ------------------------------------------------------------------------ */
+/* Solver: mNR (GPU/newtonRaphson.cuh:171-623) on one GPU                    */
+/* ------------------------------------------------------------------------ */
+
+typedef struct gbpf_solver gbpf_solver;
+
+/* Builds everything that depends only on topology, once: the Ybus pattern
+ * and its device assembly (replaces calcYbusSp_eficinte), the fixed Jacobian
+ * block pattern with room for every PV bus (replaces Jstencil_eficiente /
+ * Jstencil0based, GPU/esparso.h:61-178,481-654), the fill-reducing ordering,
+ * the symbolic LU and its level schedule, and the CUDA graph of the Newton
+ * loop.  device = CUDA ordinal. */
+gbpf_status gbpf_solver_create(const gbpf_grid *g, const gbpf_options *o, int device,
+                               gbpf_solver **out);
+void gbpf_solver_free(gbpf_solver *s);
+
+typedef struct {
+    int status;             /* gbpf_status of the solve */
+    int converged;          /* 1 when max|g| <= tolerancia */
+    int iterations;         /* iterPon.iteracao at return (GPU/newtonRaphson.cuh:283,425) */
+    int n_events;           /* PV/PQ switch events recorded */
+    int nPQlim;             /* PQ buses at the end (original PQ + PV at a limit) */
+    double final_mismatch;  /* max|g| of the returned state */
+} gbpf_result;
+
+/* One solve from the grid's starting state (copied to the device at solver
+ * creation or by gbpf_solver_set_start).  One graph launch, one host sync. */
+gbpf_status gbpf_solve(gbpf_solver *s, gbpf_result *r);
+
+/* Starting state and injections for the next solve, from host arrays [nB]
+ * (any may be NULL = unchanged).  Copies host -> device on the solver stream. */
+gbpf_status gbpf_solver_set_start(gbpf_solver *s, const double *V0, const double *theta0,
+                                  const double *Pliq, const double *Qliq);
+
+/* Results of the last solve, device -> host: state and injections [nB]. */
+gbpf_status gbpf_solver_state(gbpf_solver *s, double *V, double *theta, double *Pcalc,
+                              double *Qcalc);
+/* Switch events of the last solve, 4 ints each: iteration, bus (1-based),
+ * PV position, code (1..5, the five chkLimQ lines of GPU/limiteInjReat.cuh:
+ * 12,15,23,26,34).  *n = events copied. */
+gbpf_status gbpf_solver_events(gbpf_solver *s, int *ev, int cap, int *n);
+/* max|g| per iteration of the last solve; *n = entries copied. */
+gbpf_status gbpf_solver_history(gbpf_solver *s, double *hist, int cap, int *n);
+/* Per iteration of the last solve, 1 where the reactive-limit check ran (the
+ * trigger of GPU/newtonRaphson.cuh:309-314 fired); *n = entries copied. */
+gbpf_status gbpf_solver_triggers(gbpf_solver *s, int *trig, int cap, int *n);
+/* Branch flows of the last solve [nL] (calcFluxf_Eficiente_Sp,
+ * GPU/PQcalc.cuh:523-557, computed on the device). */
+gbpf_status gbpf_solver_flows(gbpf_solver *s, double *Pdp, double *Ppd, double *Qdp, double *Qpd);
+
+/* Solver facts: info[0..7] = nB, n blocks (nB-1), factor blocks (off-diagonal
+ * per triangle), update pairs, forward levels, backward levels, graph nodes,
+ * kernels launched per Newton iteration. */
+gbpf_status gbpf_solver_info(const gbpf_solver *s, long long info[8]);
+
+/* Device-resident timing hook: runs `repeats` solves from the stored start
+ * with no host copies and returns the device time in ms (CUDA events on the
+ * solver stream). */
+gbpf_status gbpf_solver_time(gbpf_solver *s, int repeats, double *ms_total);
+
+/* ------------------------------------------------------------------------ */
+/* Kernel-level entry points (each runs the product kernels on host inputs)  */
+/* ------------------------------------------------------------------------ */
+
+/* Device-assembled Ybus values in row-major CSR with sorted columns
+ * (calcYbusSp_eficinte).  rowptr [nB+1], col/re/im [nnzY]. */
+gbpf_status gbpf_ybus(gbpf_solver *s, int *rowptr, int *col, double *re, double *im);
+
+/* P, Q injections at (V, theta) (calcPeficiente_0based / calcQeficiente_0based,
+ * GPU/PQcalc.cuh:177-219). */
+gbpf_status gbpf_eval_pq(gbpf_solver *s, const double *V, const double *theta, double *P,
+                         double *Q);
+
+/* Jacobian at (V, theta) for the limit flags limQ [nPV] (1 = PV bus held at a
+ * Q limit, i.e. in barrasPQlim), returned as COO in the reference's row and
+ * column numbering (Jstencil0based + SpCalcH/L/M/N).  *nnz = entries. */
+gbpf_status gbpf_eval_jacobian(gbpf_solver *s, const double *V, const double *theta,
+                               const int *limQ, int *row, int *col, double *val, int cap,
+                               int *nnz);
+
+/* Newton step: factorises the Jacobian at (V, theta, limQ) on the device and
+ * solves J dx = g for g given in the reference's numbering (length
+ * nB-1+nPQlim); replaces the cusolverSpDcsrlsvqr call of
+ * GPU/newtonRaphson.cuh:455-478. */
+gbpf_status gbpf_newton_step(gbpf_solver *s, const double *V, const double *theta,
+                             const int *limQ, const double *g, double *dx);
+
+/* Device query for the driver's banner (initGPU, GPU/sistema.cuh:426-468):
+ * *count = CUDA devices; name of `device`; props = major, minor, warp size,
+ * max threads per SM, max threads per block, SM count. */
+gbpf_status gbpf_device_info(int device, int *count, char *name, size_t name_cap, int props[6]);
+
+/* Text of the last error on this thread. */
+const char *gbpf_last_error(void);
+const char *gbpf_status_str(gbpf_status st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBPF_H */
