@@ -33,9 +33,9 @@ EXPORTS = [
     "gbpf_options_default", "gbpf_options_parse", "gbpf_options_load",
     "gbpf_grid_read", "gbpf_grid_create", "gbpf_grid_free", "gbpf_grid_dims", "gbpf_grid_buses",
     "gbpf_grid_pvpq", "gbpf_grid_branches", "gbpf_grid_set_buses", "gbpf_grid_write_cdf",
-    "gbpf_generate", "gbpf_solver_create", "gbpf_solver_free", "gbpf_solve", "gbpf_solver_set_start",
+    "gbpf_generate", "gbpf_grid_analyse", "gbpf_solver_create", "gbpf_solver_free", "gbpf_solve", "gbpf_solver_set_start",
     "gbpf_solver_state", "gbpf_solver_events", "gbpf_solver_history", "gbpf_solver_triggers",
-    "gbpf_solver_flows", "gbpf_solver_info", "gbpf_solver_time", "gbpf_ybus", "gbpf_eval_pq",
+    "gbpf_solver_flows", "gbpf_solver_info", "gbpf_solver_time", "gbpf_solver_profile", "gbpf_ybus", "gbpf_eval_pq",
     "gbpf_eval_jacobian", "gbpf_newton_step", "gbpf_device_info", "gbpf_last_error", "gbpf_status_str",
 ]
 
@@ -209,6 +209,14 @@ class Grid:
         arrs = [_f64(a) for a in (Pload, Qload, Pg, Qg, V0, theta0)]
         _check(lib().gbpf_grid_set_buses(self.h, *[_p(a) for a in arrs]), "gbpf_grid_set_buses")
 
+    def analyse(self):
+        """Host-only symbolic analysis of the Newton Jacobian (no GPU needed)."""
+        a = np.zeros(8, np.int64)
+        _check(lib().gbpf_grid_analyse(self.h, _p(a)), "gbpf_grid_analyse")
+        keys = ("blocks", "factor_blocks", "update_pairs", "forward_levels", "backward_levels", "nnzY",
+                "jacobian_blocks", "closed")
+        return dict(zip(keys, (int(x) for x in a)))
+
     def write_cdf(self, path, title="synthetic grid"):
         _check(lib().gbpf_grid_write_cdf(self.h, os.fsencode(path), title.encode()), "gbpf_grid_write_cdf")
 
@@ -363,6 +371,13 @@ class Solver:
         ms = ctypes.c_double()
         _check(lib().gbpf_solver_time(self.h, int(repeats), ctypes.byref(ms)), "gbpf_solver_time")
         return ms.value
+
+    def profile(self, repeats=20):
+        ms = np.zeros(4)
+        by = np.zeros(4, np.int64)
+        _check(lib().gbpf_solver_profile(self.h, int(repeats), _p(ms), _p(by)), "gbpf_solver_profile")
+        names = ("injections_mismatch", "jacobian_fill", "factor_forward", "backward")
+        return {k: dict(ms=float(m), bytes=int(b)) for k, m, b in zip(names, ms, by)}
 
     # kernel-level entry points
     def ybus(self):

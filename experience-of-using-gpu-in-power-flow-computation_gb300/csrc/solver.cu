@@ -885,6 +885,56 @@ extern "C" gbpf_status gbpf_solver_time(gbpf_solver *s, int repeats, double *ms_
     return GBPF_OK;
 }
 
+// Phase timing on the solver stream from the state the last solve left on the
+// device (no host copies): 0 injections + limits + mismatch, 1 Jacobian fill,
+// 2 factorisation + forward substitution (all levels), 3 backward
+// substitution (all levels).  bytes[] = algorithmic bytes of one pass: every
+// array a phase reads or writes counted once.
+extern "C" gbpf_status gbpf_solver_profile(gbpf_solver *s, int repeats, double ms[4], long long bytes[4]) {
+    ARGCHECK(s && ms && bytes && repeats > 0);
+    CK(cudaSetDevice(s->device));
+    const Symbolic &S = s->S;
+    const int T = 256, W = T / 32, nq = S.n + 2 * S.nup;
+    auto phase = [&](int ph) {
+        if (ph == 0) s->launch_eval(0);
+        else if (ph == 1) k_jfill<<<cdiv_int(nq, T), T, 0, s->stream>>>(s->d, 0);
+        else if (ph == 2) {
+            for (int l = 0; l < s->nfl(); l++) {
+                const int beg = S.flev_ptr[l], cnt = S.flev_ptr[l + 1] - beg;
+                k_factor<<<cdiv_int(cnt, W), T, 0, s->stream>>>(s->d, beg, cnt, 0);
+            }
+        } else {
+            for (int l = 0; l < s->nbl(); l++) {
+                const int beg = S.blev_ptr[l], cnt = S.blev_ptr[l + 1] - beg;
+                k_bsolve<<<cdiv_int(cnt, W), T, 0, s->stream>>>(s->d, beg, cnt, 0);
+            }
+        }
+    };
+    CK(cudaMemsetAsync(&s->d.ctl->done, 0, sizeof(int), s->stream));
+    for (int ph = 0; ph < 4; ph++) {
+        phase(ph);  // warm-up
+        CK(cudaEventRecord(s->ev0, s->stream));
+        for (int r = 0; r < repeats; r++) phase(ph);
+        CK(cudaEventRecord(s->ev1, s->stream));
+        CK(cudaEventSynchronize(s->ev1));
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, s->ev0, s->ev1));
+        ms[ph] = t / repeats;
+    }
+    CK(cudaGetLastError());
+    const long long nB = s->g.nB, nnzY = s->y.nnz, n = S.n, nup = S.nup, np = S.pairs();
+    // injections: Y values + columns + row pointers, V/theta/phasors, P/Q out;
+    // mismatch: Pliq/Qliq/act/QliqLim, rhs out
+    bytes[0] = 16 * nnzY + 4 * nnzY + 4 * (nB + 1) + 8 * nB * 2 + 16 * nB + 16 * nB + 8 * nB * 4 + 4 * nB + 16 * n;
+    // fill: map (3 ints per block), Y values, bus state, blocks out
+    bytes[1] = 12LL * nq + 16 * nnzY + 8 * nB * 5 + 4 * nB + 32LL * nq;
+    // factor + forward: blocks in/out, diagonal inverses, gather lists, rhs, y
+    bytes[2] = 64LL * nq + 32 * n + 4 * (n + 1) + 8 * nup + 4 * (nup + 1) + 8 * (nup + 1) + 8 * np + 16 * n * 2 + 4 * n;
+    // backward: U blocks, inverses, columns, y in, x out
+    bytes[3] = 32LL * nup + 32 * n + 4 * (n + 1) + 4 * nup + 16 * n * 2 + 4 * n;
+    return GBPF_OK;
+}
+
 extern "C" gbpf_status gbpf_ybus(gbpf_solver *s, int *rowptr, int *col, double *re, double *im) {
     ARGCHECK(s);
     CK(cudaSetDevice(s->device));

@@ -254,3 +254,33 @@ Symbolic analyse(const Grid &g, const YPattern &y, std::string *why) {
 }
 
 }  // namespace gbpf
+
+extern "C" gbpf_status gbpf_grid_analyse(const gbpf_grid *h, long long info[8]) {
+    if (!h || !info) return GBPF_E_ARG;
+    const gbpf::Grid &g = h->g;
+    if (g.nB < 2 || g.slack < 1) return GBPF_E_INPUT;
+    const gbpf::YPattern y = gbpf::build_ypattern(g);
+    std::string why;
+    const gbpf::Symbolic S = gbpf::analyse(g, y, &why);
+    if (S.n != g.nB - 1) {
+        gbpf::set_error("symbolic analysis failed: " + why);
+        return GBPF_E_INPUT;
+    }
+    long long jblocks = 0;
+    for (int q = 0; q < S.n + 2 * S.nup; q++) jblocks += S.ysl[q] >= 0;
+    // closure: every pair target (a, b) of entry p lies in an earlier step's row
+    bool closed = true;
+    for (int j = 0; j < S.n && closed; j++)
+        for (int p = S.up_ptr[j]; p < S.up_ptr[j + 1] && closed; p++)
+            for (long long r = S.og_ptr[p]; r < S.og_ptr[p + 1]; r++)
+                if (S.og_a[r] >= S.up_ptr[j] || S.og_b[r] >= S.up_ptr[j]) { closed = false; break; }
+    info[0] = S.n;
+    info[1] = S.nup;
+    info[2] = S.pairs();
+    info[3] = (long long)S.flev_ptr.size() - 1;
+    info[4] = (long long)S.blev_ptr.size() - 1;
+    info[5] = y.nnz;
+    info[6] = jblocks;
+    info[7] = closed ? 1 : 0;
+    return GBPF_OK;
+}

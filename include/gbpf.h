@@ -156,6 +156,13 @@ gbpf_status gbpf_grid_write_cdf(const gbpf_grid *g, const char *path, const char
  * 16 -> 1,888 buses), 4 = a kind-1-style grid scaled to `nbus` buses. */
 gbpf_status gbpf_generate(int kind, unsigned long long seed, int tiles, int nbus, gbpf_grid **out);
 
+/* Host-only symbolic analysis of the Newton Jacobian of a grid (the part of
+ * gbpf_solver_create that needs no GPU): info[0..7] = blocks (nB-1), factor
+ * blocks per triangle, update pairs, forward levels, backward levels, Ybus
+ * nonzeros, Jacobian block nonzeros, 1 when every update target exists in
+ * the factor pattern (closure check). */
+gbpf_status gbpf_grid_analyse(const gbpf_grid *g, long long info[8]);
+
 /* ------------------------------------------------------------------------ */
 /* Solver: mNR (GPU/newtonRaphson.cuh:171-623) on one GPU                    */
 /* ------------------------------------------------------------------------ */
@@ -215,6 +222,13 @@ gbpf_status gbpf_solver_info(const gbpf_solver *s, long long info[8]);
  * with no host copies and returns the device time in ms (CUDA events on the
  * solver stream). */
 gbpf_status gbpf_solver_time(gbpf_solver *s, int repeats, double *ms_total);
+
+/* Per-phase device time (ms per pass, CUDA events on the solver stream, the
+ * last solve's state left on the device, `repeats` passes after one warm-up):
+ * [0] injections + limits + mismatch, [1] Jacobian fill, [2] LU
+ * factorisation fused with forward substitution (all levels), [3] backward
+ * substitution (all levels); bytes[] = algorithmic bytes of one pass. */
+gbpf_status gbpf_solver_profile(gbpf_solver *s, int repeats, double ms[4], long long bytes[4]);
 
 /* ------------------------------------------------------------------------ */
 /* Kernel-level entry points (each runs the product kernels on host inputs)  */

@@ -1,0 +1,200 @@
+"""Parity of the GPU solve path with the oracle and with the golden vectors
+produced by the reference's own code.  Every call goes through the C ABI
+(libgbpf.so) and runs the sm_103a kernels.
+
+Tolerances: |V|, theta within 1e-9 of the reference and the oracle (FP64 parity
+target); iteration counts and PV/PQ switch events identical; final max|g| <=
+tolerancia; kernel-level values (Ybus, P/Q, Jacobian) within 1e-12 relative,
+Newton steps within 1e-9 relative (different LU orderings, same mathematics).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, committed_cases, load_golden
+
+pytestmark = pytest.mark.gpu
+
+STATE_TOL = 1e-9
+
+
+def solver(gb, path_or_grid, **opts):
+    grid = gb.read_grid(path_or_grid) if isinstance(path_or_grid, str) else path_or_grid
+    base = dict(tolerancia=1e-8, no_max_iter=100, lim_inj_reat=0, metodo=0)
+    base.update(opts)
+    return grid, gb.Solver(grid, **base)
+
+
+def states(oracle_grid, n=3, seed=0):
+    """Flat start, a perturbed state and a solved state of a grid."""
+    rng = np.random.default_rng(seed)
+    V0, th0 = oracle_grid.V0.copy(), oracle_grid.theta0.copy()
+    out = [(V0, th0)]
+    out.append((V0 * (1 + 0.03 * rng.standard_normal(len(V0))), th0 + 0.2 * rng.standard_normal(len(V0))))
+    r = oracle_grid.solve(1e-8, 50, False)
+    out.append((r["V"], r["theta"]))
+    return out[:n]
+
+
+CDFS = ["c1.cdf", "c2_base.cdf", "c2_s3.cdf"]
+
+
+@pytest.mark.parametrize("name", CDFS)
+def test_ybus_matches_oracle(gb, oracle, name):
+    path = os.path.join(GOLDEN, name)
+    grid, s = solver(gb, path)
+    rp, col, re, im = s.ybus()
+    orp, ocol, ore, oim = oracle.Grid(path).ybus()
+    np.testing.assert_array_equal(rp, orp)
+    np.testing.assert_array_equal(col, ocol)
+    scale = np.max(np.abs(ore + 1j * oim))
+    assert np.max(np.abs(re - ore)) <= 1e-13 * scale
+    assert np.max(np.abs(im - oim)) <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("name", CDFS)
+def test_injections_match_oracle(gb, oracle, name):
+    path = os.path.join(GOLDEN, name)
+    grid, s = solver(gb, path)
+    og = oracle.Grid(path)
+    for V, th in states(og):
+        P, Q = s.eval_pq(V, th)
+        oP, oQ = og.injections(V, th)
+        scale = max(1.0, np.max(np.abs(oP)), np.max(np.abs(oQ)))
+        assert np.max(np.abs(P - oP)) <= 1e-12 * scale
+        assert np.max(np.abs(Q - oQ)) <= 1e-12 * scale
+
+
+def _dense(rows, cols, vals, n):
+    A = np.zeros((n, n))
+    np.add.at(A, (rows, cols), vals)
+    return A
+
+
+@pytest.mark.parametrize("name", CDFS)
+def test_jacobian_matches_oracle(gb, oracle, name):
+    path = os.path.join(GOLDEN, name)
+    grid, s = solver(gb, path)
+    og = oracle.Grid(path)
+    rng = np.random.default_rng(1)
+    for V, th in states(og):
+        for trial in range(2):
+            limQ = np.zeros(og.nPV, np.int32) if trial == 0 else (rng.random(og.nPV) < 0.3).astype(np.int32)
+            pqlim = np.sort(np.concatenate([og.pq, og.pv[limQ == 1]])).astype(np.int32)
+            n = og.nB - 1 + len(pqlim)
+            r, c, v = s.eval_jacobian(V, th, limQ)
+            orp, ocol, oval = og.jacobian(V, th, pqlim)
+            orow = np.repeat(np.arange(n), np.diff(orp))
+            A = _dense(r, c, v, n)
+            B = _dense(orow, ocol, oval, n)
+            # same pattern (the reference's entries) and values
+            assert set(zip(r.tolist(), c.tolist())) == set(zip(orow.tolist(), ocol.tolist()))
+            assert np.max(np.abs(A - B)) <= 1e-12 * max(1.0, np.max(np.abs(B)))
+
+
+@pytest.mark.parametrize("name", CDFS)
+def test_newton_step_matches_oracle(gb, oracle, name):
+    path = os.path.join(GOLDEN, name)
+    grid, s = solver(gb, path)
+    og = oracle.Grid(path)
+    rng = np.random.default_rng(2)
+    for V, th in states(og, n=2):
+        limQ = (rng.random(og.nPV) < 0.25).astype(np.int32)
+        pqlim = np.sort(np.concatenate([og.pq, og.pv[limQ == 1]])).astype(np.int32)
+        orp, ocol, oval = og.jacobian(V, th, pqlim)
+        g = rng.standard_normal(len(orp) - 1)
+        dx = s.newton_step(V, th, g, limQ)
+        ref = oracle.sparse_solve(orp, ocol, oval, g)
+        assert np.max(np.abs(dx - ref)) <= 1e-9 * max(1.0, np.max(np.abs(ref)))
+
+
+def check_solution(res, gold):
+    assert res["iterations"] == gold["iterations"]
+    assert res["converged"] == bool(gold["converged"])
+    ev = [list(e) for e in res["events"]]
+    assert ev[:len(gold["events"])] == gold["events"]
+    if gold["converged"]:
+        assert len(ev) == len(gold["events"])
+        assert res["final_mismatch"] <= gold["tol"]
+        assert np.max(np.abs(res["V"] - np.array(gold["V"]))) < STATE_TOL
+        assert np.max(np.abs(res["theta"] - np.array(gold["theta"]))) < STATE_TOL
+        for k in ("Pcalc", "Qcalc", "Pdp", "Ppd", "Qdp", "Qpd"):
+            assert np.max(np.abs(res[k] - np.array(gold[k]))) < 1e-7, k
+
+
+@pytest.mark.parametrize("case", committed_cases(), ids=lambda c: c["golden"])
+def test_solve_matches_reference_golden(gb, case):
+    grid, s = solver(gb, os.path.join(GOLDEN, case["cdf"]), tolerancia=case["tol"],
+                     no_max_iter=case["max_iter"], lim_inj_reat=case["lim"])
+    check_solution(s.solve(), load_golden(case["golden"]))
+
+
+def compare_with_oracle(gb, oracle, grid, path, lim, tol=1e-8, max_iter=60):
+    s = gb.Solver(grid, tolerancia=tol, no_max_iter=max_iter, lim_inj_reat=lim, metodo=0)
+    res = s.solve()
+    ref = oracle.Grid(path).solve(tol, max_iter, bool(lim))
+    assert ref["converged"]
+    assert res["iterations"] == ref["iterations"]
+    assert [tuple(e) for e in res["events"]] == ref["events"]
+    assert res["final_mismatch"] <= tol
+    assert np.max(np.abs(res["V"] - ref["V"])) < STATE_TOL
+    assert np.max(np.abs(res["theta"] - ref["theta"])) < STATE_TOL
+    return s, res
+
+
+@pytest.mark.parametrize("nbus", [14, 30, 57, 118, 236, 472])
+def test_scaled_grids_match_oracle(gb, oracle, tmp_path, nbus):
+    for seed in (1, 2):
+        g = gb.generate(4, 20261207 + 100 * seed + nbus, nbus=nbus)
+        p = str(tmp_path / f"g{nbus}_{seed}.cdf")
+        g.write_cdf(p)
+        compare_with_oracle(gb, oracle, gb.read_grid(p), p, lim=1)
+
+
+@pytest.mark.parametrize("tiles", [16, 128])
+def test_tiled_grids_match_oracle(gb, oracle, tmp_path, tiles):
+    g = gb.generate(3, 20261206 + tiles, tiles=tiles)
+    p = str(tmp_path / ("t.cdfx" if g.nB > 9999 else "t.cdf"))
+    g.write_cdf(p)
+    s, res = compare_with_oracle(gb, oracle, gb.read_grid(p), p, lim=1)
+    info = s.info()
+    assert info["blocks"] == g.nB - 1 and info["forward_levels"] > 0
+
+
+def test_repeated_solves_are_bitwise_identical(gb):
+    grid, s = solver(gb, os.path.join(GOLDEN, "c2_s3.cdf"), lim_inj_reat=1)
+    a = s.solve()
+    b = s.solve()
+    np.testing.assert_array_equal(a["V"], b["V"])
+    np.testing.assert_array_equal(a["theta"], b["theta"])
+    assert a["events"] == b["events"]
+
+
+def test_set_start_and_scenario(gb, oracle):
+    path = os.path.join(GOLDEN, "c2_base.cdf")
+    grid, s = solver(gb, path)
+    og = oracle.Grid(path)
+    scale = np.linspace(0.8, 1.2, og.nB)
+    Pl, Ql = og.Pload * scale, og.Qload * scale
+    s.set_start(Pliq=og.Pg - Pl, Qliq=og.Qg - Ql)
+    res = s.solve()
+    og.set_bus(Pload=Pl, Qload=Ql)
+    ref = og.solve(1e-8, 100, False)
+    assert res["iterations"] == ref["iterations"]
+    assert np.max(np.abs(res["V"] - ref["V"])) < STATE_TOL
+
+
+def test_iteration_cap_reports_noconv(gb):
+    grid, s = solver(gb, os.path.join(GOLDEN, "c2_base.cdf"), no_max_iter=1)
+    res = s.solve(full=False)
+    assert res["status"] == gb.E_NOCONV and not res["converged"] and res["iterations"] == 1
+
+
+def test_singular_jacobian_is_reported(gb):
+    # bus 3 has no branch and no shunt: its rows of the Jacobian are zero
+    g = gb.create_grid(bus_type=[3, 0, 0], V0=[1.0, 1.0, 1.0], theta0=[0, 0, 0], from_bus=[1], to_bus=[2],
+                       r=[0.01], x=[0.1], Pload=[0, 0.5, 0.1], Qload=[0, 0.1, 0.05])
+    s = gb.Solver(g, tolerancia=1e-8, no_max_iter=10, metodo=0)
+    res = s.solve(full=False)
+    assert res["status"] == gb.E_SINGULAR and not res["converged"]
