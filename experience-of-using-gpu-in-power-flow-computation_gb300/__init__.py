@@ -37,6 +37,8 @@ EXPORTS = [
     "gbpf_solver_state", "gbpf_solver_events", "gbpf_solver_history", "gbpf_solver_triggers",
     "gbpf_solver_flows", "gbpf_solver_info", "gbpf_solver_time", "gbpf_solver_profile", "gbpf_ybus", "gbpf_eval_pq",
     "gbpf_eval_jacobian", "gbpf_newton_step", "gbpf_device_info", "gbpf_last_error", "gbpf_status_str",
+    "gbpf_batch_create", "gbpf_batch_free", "gbpf_batch_set_instances", "gbpf_batch_solve", "gbpf_batch_time",
+    "gbpf_batch_results", "gbpf_batch_events", "gbpf_batch_info",
 ]
 
 
@@ -90,6 +92,7 @@ def lib():
         L.gbpf_status_str.restype = ctypes.c_char_p
         L.gbpf_grid_free.restype = None
         L.gbpf_solver_free.restype = None
+        L.gbpf_batch_free.restype = None
         _lib = L
     return _lib
 
@@ -415,3 +418,86 @@ class Solver:
         dx = np.zeros_like(g)
         _check(lib().gbpf_newton_step(self.h, _p(V), _p(theta), _p(limQ), _p(g), _p(dx)), "gbpf_newton_step")
         return dx
+
+
+# ---------------------------------------------------------------------- batch
+class Batch:
+    """Many scenarios of one or several topologies, solved in one persistent
+    launch (one thread block per instance at a time)."""
+
+    def __init__(self, grids, options=None, device=0, **overrides):
+        o = options if options is not None else Options()
+        for k, v in overrides.items():
+            setattr(o, k, v)
+        self.grids = list(grids)
+        self.options = o
+        arr = (ctypes.c_void_p * len(self.grids))(*[g.h.value for g in self.grids])
+        self.h = ctypes.c_void_p()
+        _check(lib().gbpf_batch_create(arr, len(self.grids), ctypes.byref(o._o), int(device), ctypes.byref(self.h)),
+               "gbpf_batch_create")
+        self.n_inst = 0
+        self.offsets = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gbpf_batch_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_instances(self, grid_of_inst, Pload=None, Qload=None, Pg=None, Qg=None, V0=None, theta0=None):
+        gi = _i32(grid_of_inst)
+        sizes = np.array([self.grids[i].nB for i in gi], np.int64)
+        self.offsets = np.concatenate([[0], np.cumsum(sizes)])
+        self.grid_of_inst = gi
+        arrs = [_f64(a) for a in (Pload, Qload, Pg, Qg, V0, theta0)]
+        for a in arrs:
+            if a is not None and len(a) != self.offsets[-1]:
+                raise ValueError("packed bus arrays must have sum(nB) entries")
+        _check(lib().gbpf_batch_set_instances(self.h, len(gi), _p(gi), *[_p(a) for a in arrs]),
+               "gbpf_batch_set_instances")
+        self.n_inst = len(gi)
+
+    def solve(self):
+        _check(lib().gbpf_batch_solve(self.h), "gbpf_batch_solve")
+
+    def time(self, repeats):
+        ms = ctypes.c_double()
+        _check(lib().gbpf_batch_time(self.h, int(repeats), ctypes.byref(ms)), "gbpf_batch_time")
+        return ms.value
+
+    def results(self, state=True):
+        n, nb = self.n_inst, int(self.offsets[-1])
+        it = np.zeros(n, np.int32)
+        st = np.zeros(n, np.int32)
+        mm = np.zeros(n)
+        ne = np.zeros(n, np.int32)
+        V = np.zeros(nb) if state else None
+        th = np.zeros(nb) if state else None
+        P = np.zeros(nb) if state else None
+        Q = np.zeros(nb) if state else None
+        _check(lib().gbpf_batch_results(self.h, _p(it), _p(st), _p(mm), _p(ne), _p(V), _p(th), _p(P), _p(Q)),
+               "gbpf_batch_results")
+        return dict(iterations=it, status=st, final_mismatch=mm, n_events=ne, V=V, theta=th, Pcalc=P, Qcalc=Q)
+
+    def events(self, inst, cap=16):
+        ev = np.zeros(4 * cap, np.int32)
+        n = ctypes.c_int()
+        st = lib().gbpf_batch_events(self.h, int(inst), _p(ev), cap, ctypes.byref(n))
+        if st not in (OK, E_ARG):
+            raise GbpfError(st, "gbpf_batch_events")
+        return [tuple(int(x) for x in ev[4 * i:4 * i + 4]) for i in range(n.value)]
+
+    def info(self):
+        a = np.zeros(8, np.int64)
+        _check(lib().gbpf_batch_info(self.h, _p(a)), "gbpf_batch_info")
+        keys = ("topologies", "instances", "buses", "blocks", "smem_bytes", "factors_in_smem",
+                "scratch_bytes_per_block", "blobs_in_smem")
+        return dict(zip(keys, (int(x) for x in a)))
+
+    def slice(self, arr, inst):
+        return arr[self.offsets[inst]:self.offsets[inst + 1]]

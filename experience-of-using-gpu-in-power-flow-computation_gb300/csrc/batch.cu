@@ -1,0 +1,890 @@
+// batch.cu -- the whole Newton-Raphson loop of one grid instance inside one
+// thread block; a persistent grid of blocks works through a queue of
+// instances (load scenarios of one or several topologies) in one launch.
+//
+// Per instance, as in mNR (GPU/newtonRaphson.cuh:283-565): phasors, P/Q
+// injections (GPU/PQcalc.cuh:177-219), the reactive-limit check
+// (GPU/limiteInjReat.cuh:5-75 with the trigger of GPU/newtonRaphson.cuh:309-314),
+// mismatch and convergence test (GPU/newtonRaphson.cuh:35-58,417-426), the
+// Jacobian fill (GPU/Jacobiano.cuh:252-344), a static-pivot block LU with
+// forward/backward substitution in place of cusolverSpDcsrlsvqr
+// (GPU/newtonRaphson.cuh:455-478), and the update (GPU/newtonRaphson.cuh:76-119).
+// The state lives in shared memory; the LU factor too when it fits, else in a
+// per-block slice of a global scratch buffer.  All synchronisation is
+// __syncthreads between phases and LU levels: no kernel launches inside a solve.
+//
+// TJ = precision of the Jacobian, the factor and the substitutions (double:
+// the oracle-matching form; float: FP32 LU with FP64 mismatch, test and update).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "blocks.cuh"
+#include "gbpf_internal.h"
+
+using gbpf::Grid;
+using gbpf::set_error;
+using gbpf::Symbolic;
+using gbpf::YPattern;
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+
+template <typename T> struct Blk;
+template <> struct Blk<double> { using b4 = double4_32a; using b2 = double2; };
+template <> struct Blk<float> { using b4 = float4; using b2 = float2; };
+
+template <typename B4> __device__ __forceinline__ B4 bm(B4 a, B4 b) {
+    B4 r;
+    r.x = a.x * b.x + a.y * b.z; r.y = a.x * b.y + a.y * b.w;
+    r.z = a.z * b.x + a.w * b.z; r.w = a.z * b.y + a.w * b.w;
+    return r;
+}
+template <typename B4> __device__ __forceinline__ B4 bsub(B4 a, B4 b) {
+    a.x -= b.x; a.y -= b.y; a.z -= b.z; a.w -= b.w;
+    return a;
+}
+template <typename B4> __device__ __forceinline__ B4 badd(B4 a, B4 b) {
+    a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
+    return a;
+}
+template <typename B4, typename B2> __device__ __forceinline__ B2 bmv(B4 a, B2 v) {
+    B2 r;
+    r.x = a.x * v.x + a.y * v.y;
+    r.y = a.z * v.x + a.w * v.y;
+    return r;
+}
+template <typename B4> __device__ __forceinline__ B4 bshfl_xor(B4 v, int o) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    v.z += __shfl_xor_sync(0xffffffffu, v.z, o);
+    v.w += __shfl_xor_sync(0xffffffffu, v.w, o);
+    return v;
+}
+template <typename B4> __device__ __forceinline__ B4 bcast(B4 v, int src) {
+    v.x = __shfl_sync(0xffffffffu, v.x, src);
+    v.y = __shfl_sync(0xffffffffu, v.y, src);
+    v.z = __shfl_sync(0xffffffffu, v.z, src);
+    v.w = __shfl_sync(0xffffffffu, v.w, src);
+    return v;
+}
+
+// Topology (shared by every instance of it).  All of its read-only arrays live
+// in one blob (byte offsets below) so that a block can stage the whole blob in
+// shared memory with one copy when it fits.
+struct TopoOff {
+    int yptr, ycol, yval, type, pv_bus, Qmin, Qmax, bus_of_blk, up_ptr, up_col, dg_ptr, dg_pos, dg_k,
+        og_ptr, og_a, og_b, flev_ptr, flev_steps, blev_ptr, blev_steps, ysl, rbus, cbus;
+};
+struct Topo {
+    int nB, nL, n, nup, nnzY, nPV, nfl, nbl, fac_smem, blob_smem, blob_bytes;
+    const char *blob;  // global copy
+    TopoOff o;
+};
+// Pointers of a topology's arrays, bound to the staged (shared) or global blob.
+struct TopoView {
+    const int *yptr, *ycol;
+    const double2 *yval;
+    const int *type, *pv_bus;
+    const double *Qmin, *Qmax;
+    const int *bus_of_blk, *up_ptr, *up_col, *dg_ptr, *dg_pos, *dg_k, *og_ptr, *og_a, *og_b;
+    const int *flev_ptr, *flev_steps, *blev_ptr, *blev_steps, *ysl, *rbus, *cbus;
+};
+__device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
+    TopoView v;
+    v.yptr = (const int *)(b + o.yptr); v.ycol = (const int *)(b + o.ycol); v.yval = (const double2 *)(b + o.yval);
+    v.type = (const int *)(b + o.type); v.pv_bus = (const int *)(b + o.pv_bus);
+    v.Qmin = (const double *)(b + o.Qmin); v.Qmax = (const double *)(b + o.Qmax);
+    v.bus_of_blk = (const int *)(b + o.bus_of_blk); v.up_ptr = (const int *)(b + o.up_ptr);
+    v.up_col = (const int *)(b + o.up_col); v.dg_ptr = (const int *)(b + o.dg_ptr);
+    v.dg_pos = (const int *)(b + o.dg_pos); v.dg_k = (const int *)(b + o.dg_k);
+    v.og_ptr = (const int *)(b + o.og_ptr); v.og_a = (const int *)(b + o.og_a); v.og_b = (const int *)(b + o.og_b);
+    v.flev_ptr = (const int *)(b + o.flev_ptr); v.flev_steps = (const int *)(b + o.flev_steps);
+    v.blev_ptr = (const int *)(b + o.blev_ptr); v.blev_steps = (const int *)(b + o.blev_steps);
+    v.ysl = (const int *)(b + o.ysl); v.rbus = (const int *)(b + o.rbus); v.cbus = (const int *)(b + o.cbus);
+    return v;
+}
+
+struct Args {
+    const Topo *topo;
+    int n_inst;
+    const int *inst_topo;          // [n_inst]
+    const long long *inst_off;     // [n_inst] bus offset into the packed arrays
+    const double *V0, *th0, *Pliq, *Qliq, *Qload;  // packed inputs
+    double *V, *th, *P, *Q;                        // packed outputs
+    int *iters, *status, *n_events;
+    double *mism;
+    int *events;                   // [n_inst * ev_cap * 4]
+    int ev_cap;
+    double tol;
+    int max_iter, lim;
+    int *counter;
+    char *scratch;                 // per-block factor slices when not in shared memory
+    long long scratch_stride;
+    int blob_region;               // bytes of dynamic shared memory reserved for a staged blob
+};
+
+__host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
+
+// Shared-memory layout of one instance (state + optionally the factor).
+struct Layout {
+    size_t V, th, cs, sn, P, Q, QL, R, act, lim, ys, xs, fac, dinv, total;
+};
+template <typename TJ>
+__host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fac_smem) {
+    using B4 = typename Blk<TJ>::b4;
+    using B2 = typename Blk<TJ>::b2;
+    Layout L;
+    size_t o = 0;
+    auto take = [&](size_t bytes, size_t al) { o = align_up(o, al); size_t r = o; o += bytes; return r; };
+    L.V = take(8 * nB, 16); L.th = take(8 * nB, 16); L.cs = take(8 * nB, 16); L.sn = take(8 * nB, 16);
+    L.P = take(8 * nB, 16); L.Q = take(8 * nB, 16); L.QL = take(8 * nB, 16);
+    L.R = take(16 * (size_t)n, 16);
+    L.act = take(4 * nB, 16); L.lim = take(4 * (size_t)(nPV + 1), 16);
+    L.ys = take(sizeof(B2) * n, 16); L.xs = take(sizeof(B2) * n, 16);
+    const size_t nq = (size_t)n + 2 * (size_t)nup;
+    if (fac_smem) {
+        L.fac = take(sizeof(B4) * nq, 32);
+        L.dinv = take(sizeof(B4) * n, 32);
+    } else {
+        L.fac = L.dinv = 0;
+    }
+    L.total = align_up(o, 32);
+    return L;
+}
+// Factor slice in global scratch (used when it does not fit in shared memory).
+template <typename TJ> __host__ __device__ inline size_t scratch_bytes(int n, int nup) {
+    using B4 = typename Blk<TJ>::b4;
+    return align_up(sizeof(B4) * ((size_t)n + 2 * (size_t)nup), 32) + align_up(sizeof(B4) * n, 32);
+}
+
+__device__ __forceinline__ double block_max(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const double t = __shfl_xor_sync(0xffffffffu, v, o);
+        v = (t > v || t != t) ? t : v;
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double m = red[0];
+    for (int w = 1; w < kWarps; w++) m = (red[w] > m || red[w] != red[w]) ? red[w] : m;
+    __syncthreads();
+    return m;
+}
+
+template <typename TJ>
+__global__ void __launch_bounds__(kThreads) k_nr_block(Args a) {
+    using B4 = typename Blk<TJ>::b4;
+    using B2 = typename Blk<TJ>::b2;
+    extern __shared__ __align__(32) unsigned char smem[];
+    __shared__ double red[kWarps];
+    __shared__ int s_inst, s_done, s_status, s_it, s_nev, s_topo;
+    __shared__ double s_maxG, s_maxDx;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    unsigned char *ism = smem + a.blob_region;  // per-instance region
+    if (tid == 0) s_topo = -1;
+    for (;;) {
+        if (tid == 0) s_inst = atomicAdd(a.counter, 1);
+        __syncthreads();
+        const int inst = s_inst;
+        if (inst >= a.n_inst) break;
+        const int t_id = a.inst_topo[inst];
+        const Topo T = a.topo[t_id];
+        // stage the topology's blob in shared memory unless it is already there
+        const char *blob = T.blob;
+        if (T.blob_smem) {
+            if (s_topo != t_id) {
+                const int4 *src = (const int4 *)T.blob;
+                int4 *dst = (int4 *)smem;
+                for (int i = tid; i < T.blob_bytes / 16; i += kThreads) dst[i] = src[i];
+                __syncthreads();
+                if (tid == 0) s_topo = t_id;
+            }
+            blob = (const char *)smem;
+        }
+        const TopoView G = bind(T.o, blob);
+        const long long off = a.inst_off[inst];
+        const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, T.fac_smem);
+        double *V = (double *)(ism + L.V), *th = (double *)(ism + L.th);
+        double *cs = (double *)(ism + L.cs), *sn = (double *)(ism + L.sn);
+        double *P = (double *)(ism + L.P), *Q = (double *)(ism + L.Q), *QL = (double *)(ism + L.QL);
+        double2 *R = (double2 *)(ism + L.R);
+        int *act = (int *)(ism + L.act), *limQ = (int *)(ism + L.lim);
+        B2 *ys = (B2 *)(ism + L.ys), *xs = (B2 *)(ism + L.xs);
+        B4 *fac, *dinv;
+        if (T.fac_smem) {
+            fac = (B4 *)(ism + L.fac);
+            dinv = (B4 *)(ism + L.dinv);
+        } else {
+            char *base = a.scratch + (long long)blockIdx.x * a.scratch_stride;
+            fac = (B4 *)base;
+            dinv = (B4 *)(base + align_up(sizeof(B4) * ((size_t)T.n + 2 * (size_t)T.nup), 32));
+        }
+        const int n = T.n, nB = T.nB, nq = T.n + 2 * T.nup;
+        B4 *Lv = fac + n, *Uv = fac + n + T.nup;
+        // initLim (GPU/limiteInjReat.cuh:188-224) and the starting state
+        for (int k = tid; k < nB; k += kThreads) {
+            V[k] = a.V0[off + k];
+            th[k] = a.th0[off + k];
+            QL[k] = a.Qliq[off + k];
+            act[k] = (G.type[k] == 0 || G.type[k] == 1);
+        }
+        for (int i = tid; i < T.nPV; i += kThreads) limQ[i] = 0;
+        if (tid == 0) { s_done = 0; s_status = 0; s_it = 0; s_nev = 0; s_maxDx = INFINITY; }
+        __syncthreads();
+        for (;;) {
+            // phasors and injections
+            for (int k = tid; k < nB; k += kThreads) {
+                double s, c;
+                sincos(th[k], &s, &c);
+                cs[k] = c;
+                sn[k] = s;
+            }
+            __syncthreads();
+            for (int k = tid; k < nB; k += kThreads) {
+                double ir = 0, ii = 0;
+                for (int p = G.yptr[k]; p < G.yptr[k + 1]; p++) {
+                    const int m = G.ycol[p];
+                    const double2 y = G.yval[p];
+                    const double em = V[m] * cs[m], fm = V[m] * sn[m];
+                    ir += y.x * em - y.y * fm;
+                    ii += y.x * fm + y.y * em;
+                }
+                const double ek = V[k] * cs[k], fk = V[k] * sn[k];
+                P[k] = ek * ir + fk * ii;
+                Q[k] = fk * ir - ek * ii;
+            }
+            __syncthreads();
+            const int it = s_it;
+            // reactive limits (chkLimQ) when the previous step was small
+            if (a.lim && it >= 1 && it < a.max_iter && s_maxDx < a.tol * 10.) {
+                for (int i = tid; i < T.nPV; i += kThreads) {
+                    const int b = G.pv_bus[i];
+                    const double ql = a.Qload[off + b], qg = Q[b] + ql;
+                    int code = 0;
+                    if (qg < G.Qmin[i] - a.tol) {
+                        if (!limQ[i]) code = 1;
+                        else if (QL[b] != G.Qmin[i] - ql) code = 2;
+                        limQ[i] = 1;
+                        QL[b] = G.Qmin[i] - ql;
+                    } else if (qg > G.Qmax[i] + a.tol) {
+                        if (!limQ[i]) code = 3;
+                        else if (QL[b] != G.Qmax[i] - ql) code = 4;
+                        limQ[i] = 1;
+                        QL[b] = G.Qmax[i] - ql;
+                    } else {
+                        if (limQ[i]) code = 5;
+                        limQ[i] = 0;
+                    }
+                    act[b] = limQ[i];
+                    if (code) {
+                        const int e = atomicAdd(&s_nev, 1);
+                        if (e < a.ev_cap) {
+                            int *ev = a.events + ((long long)inst * a.ev_cap + e) * 4;
+                            ev[0] = it; ev[1] = b + 1; ev[2] = i; ev[3] = code;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+            // mismatch (FP64) and convergence test
+            double m = 0;
+            for (int j = tid; j < n; j += kThreads) {
+                const int k = G.bus_of_blk[j];
+                const double gp = a.Pliq[off + k] - P[k];
+                const double gq = act[k] ? QL[k] - Q[k] : 0.0;
+                R[j] = make_double2(gp, gq);
+                double t = fmax(fabs(gp), fabs(gq));
+                if (t != t) t = __longlong_as_double(0x7ff8000000000000ll);
+                m = (t > m || t != t) ? t : m;
+            }
+            m = block_max(m, red);
+            if (tid == 0) {
+                s_maxG = m;
+                if (m != m) { s_status = GBPF_E_NOCONV; s_done = 1; }
+                else if (m <= a.tol) s_done = 1;
+                else if (it >= a.max_iter) { s_status = GBPF_E_NOCONV; s_done = 1; }
+            }
+            __syncthreads();
+            if (s_done) break;
+            // Jacobian fill at every factor position (zeros at fill-in)
+            for (int q = tid; q < nq; q += kThreads) {
+                const int s = G.ysl[q];
+                B4 blk;
+                blk.x = blk.y = blk.z = blk.w = 0;
+                if (s >= 0) {
+                    const int k = G.rbus[q], mb = G.cbus[q];
+                    const double2 y = G.yval[s];
+                    const double Vk = V[k];
+                    const int ak = act[k];
+                    if (q < n) {
+                        const double Pk = P[k], Qk = Q[k], v2 = Vk * Vk;
+                        blk.x = (TJ)(-Qk - v2 * y.y);
+                        if (ak) {
+                            blk.y = (TJ)((Pk + v2 * y.x) / Vk);
+                            blk.z = (TJ)(Pk - v2 * y.x);
+                            blk.w = (TJ)((Qk - v2 * y.y) / Vk);
+                        } else {
+                            blk.w = (TJ)1;
+                        }
+                    } else {
+                        // off-diagonal entries in the precision of the factor
+                        const int am = act[mb];
+                        const TJ ck = (TJ)cs[k], sk = (TJ)sn[k], cm = (TJ)cs[mb], sm = (TJ)sn[mb];
+                        const TJ yr = (TJ)y.x, yi = (TJ)y.y, vk = (TJ)Vk, vm = (TJ)V[mb];
+                        const TJ tr = yr * cm - yi * sm, ti = yr * sm + yi * cm;
+                        const TJ wr = ck * tr + sk * ti, wi = sk * tr - ck * ti;
+                        blk.x = vk * vm * wi;
+                        if (am) blk.y = vk * wr;
+                        if (ak) blk.z = -vk * vm * wr;
+                        if (ak && am) blk.w = vk * wi;
+                    }
+                }
+                fac[q] = blk;
+            }
+            __syncthreads();
+            // LU factorisation fused with forward substitution, one level at a time
+            for (int l = 0; l < T.nfl; l++) {
+                const int beg = G.flev_ptr[l], end = G.flev_ptr[l + 1];
+                for (int w = beg + warp; w < end; w += kWarps) {
+                    const int j = G.flev_steps[w];
+                    B4 acc;
+                    acc.x = acc.y = acc.z = acc.w = 0;
+                    B2 accy;
+                    accy.x = accy.y = 0;
+                    for (int t = G.dg_ptr[j] + lane; t < G.dg_ptr[j + 1]; t += 32) {
+                        const int p = G.dg_pos[t];
+                        const B4 lj = Lv[p];
+                        acc = badd(acc, bm(lj, Uv[p]));
+                        const B2 v = bmv(lj, ys[G.dg_k[t]]);
+                        accy.x += v.x;
+                        accy.y += v.y;
+                    }
+                    for (int o = 16; o > 0; o >>= 1) {
+                        acc = bshfl_xor(acc, o);
+                        accy.x += __shfl_xor_sync(0xffffffffu, accy.x, o);
+                        accy.y += __shfl_xor_sync(0xffffffffu, accy.y, o);
+                    }
+                    B4 inv;
+                    inv.x = inv.y = inv.z = inv.w = 0;
+                    if (lane == 0) {
+                        const B4 D = bsub(fac[j], acc);
+                        const TJ det = D.x * D.w - D.y * D.z;
+                        if (det == (TJ)0 || !isfinite(det)) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                        inv.x = D.w / det; inv.y = -D.y / det; inv.z = -D.z / det; inv.w = D.x / det;
+                        fac[j] = D;
+                        dinv[j] = inv;
+                        B2 yj;
+                        yj.x = (TJ)R[j].x - accy.x;
+                        yj.y = (TJ)R[j].y - accy.y;
+                        ys[j] = yj;
+                    }
+                    inv = bcast(inv, 0);
+                    for (int p = G.up_ptr[j] + lane; p < G.up_ptr[j + 1]; p += 32) {
+                        B4 aL = Lv[p], aU = Uv[p];
+                        for (int r = G.og_ptr[p]; r < G.og_ptr[p + 1]; r++) {
+                            const int x = G.og_a[r], y = G.og_b[r];
+                            aL = bsub(aL, bm(Lv[y], Uv[x]));
+                            aU = bsub(aU, bm(Lv[x], Uv[y]));
+                        }
+                        Uv[p] = aU;
+                        Lv[p] = bm(aL, inv);
+                    }
+                }
+                __syncthreads();
+            }
+            if (s_done) break;
+            // backward substitution
+            for (int l = 0; l < T.nbl; l++) {
+                const int beg = G.blev_ptr[l], end = G.blev_ptr[l + 1];
+                for (int w = beg + warp; w < end; w += kWarps) {
+                    const int j = G.blev_steps[w];
+                    B2 acc;
+                    acc.x = acc.y = 0;
+                    for (int p = G.up_ptr[j] + lane; p < G.up_ptr[j + 1]; p += 32) {
+                        const B2 v = bmv(Uv[p], xs[G.up_col[p]]);
+                        acc.x += v.x;
+                        acc.y += v.y;
+                    }
+                    for (int o = 16; o > 0; o >>= 1) {
+                        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+                        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+                    }
+                    if (lane == 0) {
+                        B2 t;
+                        t.x = ys[j].x - acc.x;
+                        t.y = ys[j].y - acc.y;
+                        xs[j] = bmv(dinv[j], t);
+                    }
+                }
+                __syncthreads();
+            }
+            // update (FP64 state) and max|dx|
+            double md = 0;
+            for (int j = tid; j < n; j += kThreads) {
+                const int k = G.bus_of_blk[j];
+                const double dt = (double)xs[j].x, dv = (double)xs[j].y;
+                th[k] += dt;
+                if (act[k]) V[k] += dv;
+                double t = fmax(fabs(dt), fabs(dv));
+                if (t != t) t = __longlong_as_double(0x7ff8000000000000ll);
+                md = (t > md || t != t) ? t : md;
+            }
+            md = block_max(md, red);
+            if (tid == 0) { s_maxDx = md; s_it = it + 1; }
+            __syncthreads();
+        }
+        // results
+        for (int k = tid; k < nB; k += kThreads) {
+            a.V[off + k] = V[k];
+            a.th[off + k] = th[k];
+            a.P[off + k] = P[k];
+            a.Q[off + k] = Q[k];
+        }
+        if (tid == 0) {
+            a.iters[inst] = s_it;
+            a.status[inst] = s_status;
+            a.mism[inst] = s_maxG;
+            a.n_events[inst] = s_nev;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_batch_ybus(const int *cptr, const int *csrc, const double2 *stamp, const double *gsh,
+                             const double *bsh, double2 *yval, int nnz) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nnz) return;
+    double2 acc = make_double2(0, 0);
+    for (int c = cptr[s]; c < cptr[s + 1]; c++) {
+        const int src = csrc[c];
+        const double2 v = src >= 0 ? stamp[src] : make_double2(gsh[-1 - src], bsh[-1 - src]);
+        if (c == cptr[s]) acc = v;
+        else { acc.x += v.x; acc.y += v.y; }
+    }
+    yval[s] = acc;
+}
+
+__device__ __forceinline__ double2 cdiv2(double a, double b, double c, double d) {
+    if (fabs(c) >= fabs(d)) {
+        const double r = d / c, den = c + d * r;
+        return make_double2((a + b * r) / den, (b - a * r) / den);
+    }
+    const double r = c / d, den = c * r + d;
+    return make_double2((a * r + b) / den, (b * r - a) / den);
+}
+
+// Branch stamps of calcYbusSp_eficinte (GPU/sistema.h:708-719).
+__global__ void k_batch_stamps(const double *r, const double *x, const double *bch, const double *tre,
+                               const double *tim, double2 *stamp, int nL) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nL) return;
+    const double2 y = cdiv2(1.0, 0.0, r[b], x[b]);
+    const double2 ft = cdiv2(-y.x, -y.y, tre[b], -tim[b]);
+    const double2 tf = cdiv2(-y.x, -y.y, tre[b], tim[b]);
+    double m = hypot(tre[b], tim[b]);
+    m = 1.0 / (m * m);
+    const double hb = bch[b] / 2.;
+    stamp[4 * b + 0] = ft;
+    stamp[4 * b + 1] = tf;
+    stamp[4 * b + 2] = make_double2(m * y.x, m * y.y + hb);
+    stamp[4 * b + 3] = make_double2(y.x, y.y + hb);
+}
+
+#define CK(call)                                                                     \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess) {                                                     \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));          \
+            return GBPF_E_CUDA;                                                      \
+        }                                                                            \
+    } while (0)
+
+// Owning device allocation (movable, not copyable).
+struct DevBuf {
+    void *p = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p) { o.p = nullptr; }
+    DevBuf &operator=(DevBuf &&o) noexcept {
+        if (this != &o) { reset(); p = o.p; o.p = nullptr; }
+        return *this;
+    }
+    void reset() { if (p) cudaFree(p); p = nullptr; }
+    ~DevBuf() { reset(); }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host object
+// ---------------------------------------------------------------------------
+struct gbpf_batch {
+    int device = 0;
+    int precision = 0;
+    double tol = 1e-8;
+    int max_iter = 100, lim = 0, ev_cap = 16;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<Grid> grids;
+    std::vector<YPattern> ys;
+    std::vector<Symbolic> syms;
+    std::vector<Topo> topo_h;
+    std::vector<DevBuf> topo_mem;  // one allocation per topology
+    DevBuf topo_d;
+    // instances
+    int n_inst = 0;
+    long long n_bus_total = 0;
+    std::vector<int> inst_topo;
+    std::vector<long long> inst_off;
+    DevBuf inst_mem, out_mem, scratch, counter;
+    Args args{};
+    size_t smem = 0;
+    int grid_blocks = 0;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+
+    ~gbpf_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    gbpf_status add_topology(const Grid &g);
+    gbpf_status set_instances(int n, const int *topo_of_inst, const double *Pload, const double *Qload,
+                              const double *Pg, const double *Qg, const double *V0, const double *th0);
+    gbpf_status launch(cudaStream_t st);
+    gbpf_status build_graph();
+};
+
+gbpf_status gbpf_batch::add_topology(const Grid &g) {
+    if (g.nB < 2 || g.slack < 1) { set_error("grid needs at least two buses and one slack"); return GBPF_E_INPUT; }
+    for (int b = 0; b < g.nL; b++)
+        if (g.r[b] == 0.0 && g.x[b] == 0.0) { set_error("branch with zero impedance"); return GBPF_E_INPUT; }
+    YPattern y = gbpf::build_ypattern(g);
+    std::string why;
+    Symbolic S = gbpf::analyse(g, y, &why);
+    if (S.n != g.nB - 1) { set_error("symbolic analysis failed: " + why); return GBPF_E_INPUT; }
+    if (S.pairs() >= (1LL << 31)) { set_error("factor too large for the batched kernel"); return GBPF_E_UNSUPPORTED; }
+    const int nB = g.nB, nL = g.nL, n = S.n, nup = S.nup, nq = n + 2 * nup, nfl = (int)S.flev_ptr.size() - 1,
+              nbl = (int)S.blev_ptr.size() - 1;
+    std::vector<int> pv0(g.nPV), ogp(nup + 1);
+    for (int i = 0; i < g.nPV; i++) pv0[i] = g.pv[i] - 1;
+    for (int p = 0; p <= nup; p++) ogp[p] = (int)S.og_ptr[p];
+    // the blob: every read-only array of the topology, 16-byte aligned pieces
+    std::vector<char> blob;
+    auto put = [&](const void *src, size_t bytes) {
+        const size_t o = align_up(blob.size(), 16);
+        blob.resize(align_up(o + bytes, 16), 0);
+        if (src && bytes) std::memcpy(blob.data() + o, src, bytes);
+        return (int)o;
+    };
+    TopoOff o;
+    o.yptr = put(y.rowptr.data(), (nB + 1) * 4); o.ycol = put(y.col.data(), y.nnz * 4);
+    o.yval = put(nullptr, (size_t)y.nnz * 16);
+    o.type = put(g.type.data(), nB * 4); o.pv_bus = put(pv0.data(), g.nPV * 4);
+    o.Qmin = put(g.Qmin.data(), g.nPV * 8); o.Qmax = put(g.Qmax.data(), g.nPV * 8);
+    o.bus_of_blk = put(S.bus_of_blk.data(), n * 4); o.up_ptr = put(S.up_ptr.data(), (n + 1) * 4);
+    o.up_col = put(S.up_col.data(), nup * 4); o.dg_ptr = put(S.dg_ptr.data(), (n + 1) * 4);
+    o.dg_pos = put(S.dg_pos.data(), nup * 4); o.dg_k = put(S.dg_k.data(), nup * 4);
+    o.og_ptr = put(ogp.data(), (nup + 1) * 4);
+    o.og_a = put(S.og_a.data(), S.og_a.size() * 4); o.og_b = put(S.og_b.data(), S.og_b.size() * 4);
+    o.flev_ptr = put(S.flev_ptr.data(), (nfl + 1) * 4); o.flev_steps = put(S.flev_steps.data(), n * 4);
+    o.blev_ptr = put(S.blev_ptr.data(), (nbl + 1) * 4); o.blev_steps = put(S.blev_steps.data(), n * 4);
+    o.ysl = put(S.ysl.data(), nq * 4); o.rbus = put(S.rbus.data(), nq * 4); o.cbus = put(S.cbus.data(), nq * 4);
+    DevBuf mem, tmp;
+    CK(cudaMalloc(&mem.p, blob.size()));
+    CK(cudaMemcpyAsync(mem.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, stream));
+    // Ybus values into the blob, assembled on the device (calcYbusSp_eficinte)
+    size_t used = 0;
+    auto tk = [&](size_t bytes) { used = align_up(used, 256); size_t r = used; used += bytes; return r; };
+    const size_t t_cptr = tk((y.nnz + 1) * 4), t_csrc = tk(y.csrc.size() * 4), t_stamp = tk(16 * (size_t)(4 * nL + 1));
+    const size_t t_r = tk(nL * 8 + 8), t_x = tk(nL * 8 + 8), t_b = tk(nL * 8 + 8), t_tre = tk(nL * 8 + 8),
+                 t_tim = tk(nL * 8 + 8), t_gsh = tk(nB * 8), t_bsh = tk(nB * 8);
+    CK(cudaMalloc(&tmp.p, used + 256));
+    char *tb = (char *)tmp.p;
+    CK(cudaMemcpyAsync(tb + t_cptr, y.cptr.data(), (y.nnz + 1) * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(tb + t_csrc, y.csrc.data(), y.csrc.size() * 4, cudaMemcpyHostToDevice, stream));
+    if (nL) {
+        CK(cudaMemcpyAsync(tb + t_r, g.r.data(), nL * 8, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(tb + t_x, g.x.data(), nL * 8, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(tb + t_b, g.bch.data(), nL * 8, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(tb + t_tre, g.tap_re.data(), nL * 8, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(tb + t_tim, g.tap_im.data(), nL * 8, cudaMemcpyHostToDevice, stream));
+    }
+    CK(cudaMemcpyAsync(tb + t_gsh, g.gsh.data(), nB * 8, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(tb + t_bsh, g.bsh.data(), nB * 8, cudaMemcpyHostToDevice, stream));
+    if (nL) k_batch_stamps<<<(nL + 255) / 256, 256, 0, stream>>>((const double *)(tb + t_r), (const double *)(tb + t_x),
+                                                                 (const double *)(tb + t_b), (const double *)(tb + t_tre),
+                                                                 (const double *)(tb + t_tim), (double2 *)(tb + t_stamp), nL);
+    k_batch_ybus<<<(y.nnz + 255) / 256, 256, 0, stream>>>((const int *)(tb + t_cptr), (const int *)(tb + t_csrc),
+                                                          (const double2 *)(tb + t_stamp), (const double *)(tb + t_gsh),
+                                                          (const double *)(tb + t_bsh),
+                                                          (double2 *)((char *)mem.p + o.yval), y.nnz);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(stream));
+    Topo t{};
+    t.nB = nB; t.nL = nL; t.n = n; t.nup = nup; t.nnzY = y.nnz; t.nPV = g.nPV; t.nfl = nfl; t.nbl = nbl;
+    t.blob_bytes = (int)blob.size();
+    t.blob = (const char *)mem.p;
+    t.o = o;
+    grids.push_back(g);
+    ys.push_back(std::move(y));
+    syms.push_back(std::move(S));
+    topo_h.push_back(t);
+    topo_mem.push_back(std::move(mem));
+    return GBPF_OK;
+}
+
+gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Pload, const double *Qload,
+                                      const double *Pg, const double *Qg, const double *V0, const double *th0) {
+    n_inst = n;
+    inst_topo.assign(tofi, tofi + n);
+    inst_off.resize(n);
+    long long off = 0;
+    for (int i = 0; i < n; i++) {
+        if (inst_topo[i] < 0 || inst_topo[i] >= (int)grids.size()) { set_error("instance names an unknown grid"); return GBPF_E_ARG; }
+        inst_off[i] = off;
+        off += grids[inst_topo[i]].nB;
+    }
+    n_bus_total = off;
+    // inputs: V0, th0, Pliq, Qliq, Qload (packed); outputs: V, th, P, Q + per-instance results
+    std::vector<double> hV(off), hT(off), hP(off), hQ(off), hQl(off);
+    for (int i = 0; i < n; i++) {
+        const Grid &g = grids[inst_topo[i]];
+        const long long o = inst_off[i];
+        for (int k = 0; k < g.nB; k++) {
+            const double pl = Pload ? Pload[o + k] : g.Pload[k], ql = Qload ? Qload[o + k] : g.Qload[k];
+            const double pg = Pg ? Pg[o + k] : g.Pg[k], qg = Qg ? Qg[o + k] : g.Qg[k];
+            hV[o + k] = V0 ? V0[o + k] : g.V0[k];
+            hT[o + k] = th0 ? th0[o + k] : g.theta0[k];
+            hP[o + k] = pg - pl;
+            hQ[o + k] = qg - ql;
+            hQl[o + k] = ql;
+        }
+    }
+    inst_mem.reset();
+    out_mem.reset();
+    const size_t nb = (size_t)off * 8;
+    const size_t in_bytes = 5 * align_up(nb, 256) + align_up(4 * (size_t)n, 256) + align_up(8 * (size_t)n, 256);
+    CK(cudaMalloc(&inst_mem.p, in_bytes));
+    char *b = (char *)inst_mem.p;
+    size_t o = 0;
+    auto take = [&](size_t bytes) { char *r = b + o; o += align_up(bytes, 256); return r; };
+    args.V0 = (double *)take(nb); args.th0 = (double *)take(nb); args.Pliq = (double *)take(nb);
+    args.Qliq = (double *)take(nb); args.Qload = (double *)take(nb);
+    args.inst_topo = (int *)take(4 * (size_t)n);
+    args.inst_off = (long long *)take(8 * (size_t)n);
+    CK(cudaMemcpyAsync((void *)args.V0, hV.data(), nb, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync((void *)args.th0, hT.data(), nb, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync((void *)args.Pliq, hP.data(), nb, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync((void *)args.Qliq, hQ.data(), nb, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync((void *)args.Qload, hQl.data(), nb, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync((void *)args.inst_topo, inst_topo.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync((void *)args.inst_off, inst_off.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, stream));
+    const size_t out_bytes = 4 * align_up(nb, 256) + 3 * align_up(4 * (size_t)n, 256) + align_up(8 * (size_t)n, 256) +
+                             align_up(16 * (size_t)n * ev_cap, 256);
+    CK(cudaMalloc(&out_mem.p, out_bytes));
+    b = (char *)out_mem.p;
+    o = 0;
+    args.V = (double *)take(nb); args.th = (double *)take(nb); args.P = (double *)take(nb); args.Q = (double *)take(nb);
+    args.iters = (int *)take(4 * (size_t)n); args.status = (int *)take(4 * (size_t)n);
+    args.n_events = (int *)take(4 * (size_t)n); args.mism = (double *)take(8 * (size_t)n);
+    args.events = (int *)take(16 * (size_t)n * ev_cap);
+    args.n_inst = n;
+    CK(cudaStreamSynchronize(stream));
+    if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+    return build_graph();
+}
+
+gbpf_status gbpf_batch::launch(cudaStream_t st) {
+    CK(cudaMemsetAsync(args.counter, 0, sizeof(int), st));
+    if (precision == GBPF_PREC_FP32_IR) k_nr_block<float><<<grid_blocks, kThreads, smem, st>>>(args);
+    else k_nr_block<double><<<grid_blocks, kThreads, smem, st>>>(args);
+    CK(cudaGetLastError());
+    return GBPF_OK;
+}
+
+gbpf_status gbpf_batch::build_graph() {
+    // Shared-memory plan, per topology: its blob is staged in shared memory when
+    // it is at most 48 KB; its factor stays in shared memory when blob region +
+    // state + factor fit in 110 KB (two blocks per SM), otherwise it lives in a
+    // per-block slice of global scratch.
+    const size_t budget = 110 * 1024, blob_cap = 48 * 1024;
+    size_t region = 0, need = 0, scr = 0;
+    const bool fp32 = precision == GBPF_PREC_FP32_IR;
+    for (auto &t : topo_h) {
+        t.blob_smem = (size_t)t.blob_bytes <= blob_cap;
+        if (t.blob_smem) region = std::max(region, align_up((size_t)t.blob_bytes, 32));
+    }
+    for (auto &t : topo_h) {
+        Layout with = fp32 ? layout<float>(t.nB, t.n, t.nup, t.nPV, 1) : layout<double>(t.nB, t.n, t.nup, t.nPV, 1);
+        Layout without = fp32 ? layout<float>(t.nB, t.n, t.nup, t.nPV, 0) : layout<double>(t.nB, t.n, t.nup, t.nPV, 0);
+        if (region + with.total <= budget) { t.fac_smem = 1; need = std::max(need, with.total); }
+        else {
+            t.fac_smem = 0;
+            need = std::max(need, without.total);
+            scr = std::max(scr, fp32 ? scratch_bytes<float>(t.n, t.nup) : scratch_bytes<double>(t.n, t.nup));
+        }
+    }
+    args.blob_region = (int)region;
+    need += region;
+    smem = need;
+    int dev_sm = 0, maxsm = 0;
+    CK(cudaDeviceGetAttribute(&dev_sm, cudaDevAttrMultiProcessorCount, device));
+    CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    if (smem > (size_t)maxsm) { set_error("instance state does not fit in shared memory"); return GBPF_E_UNSUPPORTED; }
+    int occ = 0;
+    if (precision == GBPF_PREC_FP32_IR) {
+        CK(cudaFuncSetAttribute(k_nr_block<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float>, kThreads, smem));
+    } else {
+        CK(cudaFuncSetAttribute(k_nr_block<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double>, kThreads, smem));
+    }
+    grid_blocks = std::max(1, std::min(n_inst, dev_sm * std::max(occ, 1)));
+    scratch.reset();
+    args.scratch = nullptr;
+    args.scratch_stride = (long long)align_up(scr, 256);
+    if (scr) CK(cudaMalloc(&scratch.p, (size_t)args.scratch_stride * grid_blocks));
+    args.scratch = (char *)scratch.p;
+    if (!counter.p) CK(cudaMalloc(&counter.p, 256));
+    args.counter = (int *)counter.p;
+    topo_d.reset();
+    CK(cudaMalloc(&topo_d.p, sizeof(Topo) * topo_h.size()));
+    CK(cudaMemcpy(topo_d.p, topo_h.data(), sizeof(Topo) * topo_h.size(), cudaMemcpyHostToDevice));
+    args.topo = (const Topo *)topo_d.p;
+    args.tol = tol;
+    args.max_iter = max_iter;
+    args.lim = lim;
+    args.ev_cap = ev_cap;
+    // one graph: reset the work counter, one persistent launch
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    gbpf_status st = launch(stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (st != GBPF_OK) return st;
+    if (e != cudaSuccess) { set_error(std::string("capture: ") + cudaGetErrorString(e)); return GBPF_E_CUDA; }
+    graph = g;
+    CK(cudaGraphInstantiate(&exec, graph, 0));
+    return GBPF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+#define ARGCHECK(c) do { if (!(c)) { set_error("invalid argument: " #c); return GBPF_E_ARG; } } while (0)
+
+extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_grids, const gbpf_options *o,
+                                         int device, gbpf_batch **out) {
+    ARGCHECK(grids && n_grids > 0 && o && out);
+    *out = nullptr;
+    auto b = std::make_unique<gbpf_batch>();
+    b->device = device;
+    b->precision = o->precision;
+    b->tol = o->tolerancia;
+    b->max_iter = o->no_max_iter;
+    b->lim = o->lim_inj_reat;
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&b->ev0));
+    CK(cudaEventCreate(&b->ev1));
+    for (int i = 0; i < n_grids; i++) {
+        ARGCHECK(grids[i]);
+        gbpf_status st = b->add_topology(grids[i]->g);
+        if (st != GBPF_OK) return st;
+    }
+    *out = b.release();
+    return GBPF_OK;
+}
+
+extern "C" void gbpf_batch_free(gbpf_batch *b) { delete b; }
+
+extern "C" gbpf_status gbpf_batch_set_instances(gbpf_batch *b, int n_inst, const int *grid_of_inst,
+                                                const double *Pload, const double *Qload, const double *Pg,
+                                                const double *Qg, const double *V0, const double *theta0) {
+    ARGCHECK(b && n_inst > 0 && grid_of_inst);
+    CK(cudaSetDevice(b->device));
+    return b->set_instances(n_inst, grid_of_inst, Pload, Qload, Pg, Qg, V0, theta0);
+}
+
+extern "C" gbpf_status gbpf_batch_solve(gbpf_batch *b) {
+    ARGCHECK(b && b->exec);
+    CK(cudaSetDevice(b->device));
+    CK(cudaGraphLaunch(b->exec, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_batch_time(gbpf_batch *b, int repeats, double *ms_total) {
+    ARGCHECK(b && b->exec && repeats > 0 && ms_total);
+    CK(cudaSetDevice(b->device));
+    CK(cudaEventRecord(b->ev0, b->stream));
+    for (int i = 0; i < repeats; i++) CK(cudaGraphLaunch(b->exec, b->stream));
+    CK(cudaEventRecord(b->ev1, b->stream));
+    CK(cudaEventSynchronize(b->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    *ms_total = ms;
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_batch_results(gbpf_batch *b, int *iterations, int *status, double *final_mismatch,
+                                          int *n_events, double *V, double *theta, double *Pcalc, double *Qcalc) {
+    ARGCHECK(b && b->n_inst > 0);
+    CK(cudaSetDevice(b->device));
+    const size_t n = b->n_inst, nb = (size_t)b->n_bus_total * 8;
+    if (iterations) CK(cudaMemcpyAsync(iterations, b->args.iters, 4 * n, cudaMemcpyDeviceToHost, b->stream));
+    if (status) CK(cudaMemcpyAsync(status, b->args.status, 4 * n, cudaMemcpyDeviceToHost, b->stream));
+    if (final_mismatch) CK(cudaMemcpyAsync(final_mismatch, b->args.mism, 8 * n, cudaMemcpyDeviceToHost, b->stream));
+    if (n_events) CK(cudaMemcpyAsync(n_events, b->args.n_events, 4 * n, cudaMemcpyDeviceToHost, b->stream));
+    if (V) CK(cudaMemcpyAsync(V, b->args.V, nb, cudaMemcpyDeviceToHost, b->stream));
+    if (theta) CK(cudaMemcpyAsync(theta, b->args.th, nb, cudaMemcpyDeviceToHost, b->stream));
+    if (Pcalc) CK(cudaMemcpyAsync(Pcalc, b->args.P, nb, cudaMemcpyDeviceToHost, b->stream));
+    if (Qcalc) CK(cudaMemcpyAsync(Qcalc, b->args.Q, nb, cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_batch_events(gbpf_batch *b, int inst, int *ev, int cap, int *n) {
+    ARGCHECK(b && inst >= 0 && inst < b->n_inst && n && (cap == 0 || ev));
+    CK(cudaSetDevice(b->device));
+    int have = 0;
+    CK(cudaMemcpy(&have, b->args.n_events + inst, 4, cudaMemcpyDeviceToHost));
+    const int m = std::min(std::min(have, b->ev_cap), cap);
+    std::vector<int> e(4 * (size_t)m);
+    if (m) CK(cudaMemcpy(e.data(), b->args.events + (size_t)inst * b->ev_cap * 4, e.size() * 4, cudaMemcpyDeviceToHost));
+    std::vector<int> idx(m);
+    for (int i = 0; i < m; i++) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int x, int y) {
+        return e[4 * x] != e[4 * y] ? e[4 * x] < e[4 * y] : e[4 * x + 2] < e[4 * y + 2];
+    });
+    for (int i = 0; i < m; i++) std::copy(&e[4 * idx[i]], &e[4 * idx[i]] + 4, ev + 4 * i);
+    *n = m;
+    return have > b->ev_cap ? GBPF_E_ARG : GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_batch_info(const gbpf_batch *b, long long info[8]) {
+    ARGCHECK(b && info);
+    long long fs = 0, bs = 0;
+    for (auto &t : b->topo_h) { fs += t.fac_smem; bs += t.blob_smem; }
+    info[0] = (long long)b->topo_h.size();
+    info[1] = b->n_inst;
+    info[2] = b->n_bus_total;
+    info[3] = b->grid_blocks;
+    info[4] = (long long)b->smem;
+    info[5] = fs;
+    info[6] = b->args.scratch_stride;
+    info[7] = bs;
+    return GBPF_OK;
+}

@@ -257,6 +257,49 @@ gbpf_status gbpf_eval_jacobian(gbpf_solver *s, const double *V, const double *th
 gbpf_status gbpf_newton_step(gbpf_solver *s, const double *V, const double *theta,
                              const int *limQ, const double *g, double *dx);
 
+/* ------------------------------------------------------------------------ */
+/* Batched solves: many load scenarios of one or several topologies in one   */
+/* persistent launch (no counterpart in the reference, which solves one grid */
+/* per process run)                                                          */
+/* ------------------------------------------------------------------------ */
+
+typedef struct gbpf_batch gbpf_batch;
+
+/* Topologies (symbolic analysis, device Ybus) for a batch.  Options used:
+ * tolerancia, no_max_iter, lim_inj_reat, precision. */
+gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_grids, const gbpf_options *o,
+                              int device, gbpf_batch **out);
+void gbpf_batch_free(gbpf_batch *b);
+
+/* Instances: grid_of_inst[i] picks the topology of instance i; the bus arrays
+ * are packed in instance order (instance i occupies nB of its grid entries)
+ * and may be NULL (= the grid's own values).  Copies to the device. */
+gbpf_status gbpf_batch_set_instances(gbpf_batch *b, int n_inst, const int *grid_of_inst,
+                                     const double *Pload, const double *Qload, const double *Pg,
+                                     const double *Qg, const double *V0, const double *theta0);
+
+/* Solves every instance: one graph launch (work-counter reset + one
+ * persistent kernel, one thread block per instance at a time). */
+gbpf_status gbpf_batch_solve(gbpf_batch *b);
+
+/* `repeats` batch solves back to back on the batch stream; device ms. */
+gbpf_status gbpf_batch_time(gbpf_batch *b, int repeats, double *ms_total);
+
+/* Per-instance results of the last batch solve (any pointer may be NULL);
+ * V/theta/P/Q packed like the inputs. */
+gbpf_status gbpf_batch_results(gbpf_batch *b, int *iterations, int *status, double *final_mismatch,
+                               int *n_events, double *V, double *theta, double *Pcalc, double *Qcalc);
+
+/* Switch events of one instance (first 16 kept), 4 ints each as in
+ * gbpf_solver_events. */
+gbpf_status gbpf_batch_events(gbpf_batch *b, int inst, int *ev, int cap, int *n);
+
+/* info[0..7] = topologies, instances, packed buses, resident thread blocks,
+ * dynamic shared memory per block, topologies whose factor is in shared
+ * memory, global scratch bytes per block, topologies whose read-only arrays
+ * are staged in shared memory. */
+gbpf_status gbpf_batch_info(const gbpf_batch *b, long long info[8]);
+
 /* Device query for the driver's banner (initGPU, GPU/sistema.cuh:426-468):
  * *count = CUDA devices; name of `device`; props = major, minor, warp size,
  * max threads per SM, max threads per block, SM count. */

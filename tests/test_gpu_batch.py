@@ -1,0 +1,132 @@
+"""Batched solves (one thread block per instance, many instances per launch)
+against the oracle, instance by instance.
+
+FP64 form: identical iteration counts and switch events, |V| and theta within
+1e-9.  FP32-LU form: max|g| <= 1e-8 evaluated in FP64 and |V|, theta within
+1e-6 of the FP64 oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def scenarios(og, n, seed, sigma=0.1):
+    """Per-bus load x lognormal(sigma), generation x U(0.9, 1.1)."""
+    rng = np.random.default_rng(seed)
+    lf = np.exp(rng.normal(-0.5 * sigma * sigma, sigma, (n, og.nB)))
+    gf = rng.uniform(0.9, 1.1, (n, og.nB))
+    return og.Pload * lf, og.Qload * lf, og.Pg * gf
+
+
+def oracle_solve(og, Pl, Ql, Pg, lim, tol=1e-8, maxit=100):
+    og.set_bus(Pload=Pl, Qload=Ql, Pg=Pg)
+    return og.solve(tol, maxit, bool(lim))
+
+
+def run_batch(gb, grids, inst_grid, Pl, Ql, Pg, **opts):
+    base = dict(tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1)
+    base.update(opts)
+    b = gb.Batch(grids, **base)
+    b.set_instances(inst_grid, Pload=Pl, Qload=Ql, Pg=Pg)
+    b.solve()
+    return b, b.results()
+
+
+@pytest.mark.parametrize("cdf", ["c2_base.cdf", "c2_s3.cdf"])
+def test_batch_fp64_matches_oracle(gb, oracle, cdf):
+    path = os.path.join(GOLDEN, cdf)
+    og = oracle.Grid(path)
+    n = 48
+    Pl, Ql, Pg = scenarios(og, n, 7)
+    b, r = run_batch(gb, [gb.read_grid(path)], np.zeros(n, np.int32), Pl.ravel(), Ql.ravel(), Pg.ravel())
+    switched = 0
+    for i in range(n):
+        ref = oracle_solve(og, Pl[i], Ql[i], Pg[i], 1)
+        assert ref["converged"]
+        assert r["status"][i] == 0 and r["iterations"][i] == ref["iterations"], i
+        assert r["final_mismatch"][i] <= 1e-8
+        ev = b.events(i)
+        assert ev == ref["events"][:16], i
+        switched += len(ev) > 0
+        assert np.max(np.abs(b.slice(r["V"], i) - ref["V"])) < 1e-9
+        assert np.max(np.abs(b.slice(r["theta"], i) - ref["theta"])) < 1e-9
+    assert b.info()["factors_in_smem"] == 1
+
+
+def test_batch_mixed_topologies_fp64(gb, oracle, tmp_path):
+    paths = [os.path.join(GOLDEN, "c1.cdf"), os.path.join(GOLDEN, "c2_base.cdf")]
+    for nb in (236, 472):
+        g = gb.generate(4, 20261207 + nb, nbus=nb)
+        p = str(tmp_path / f"g{nb}.cdf")
+        g.write_cdf(p)
+        paths.append(p)
+    grids = [gb.read_grid(p) for p in paths]
+    ogs = [oracle.Grid(p) for p in paths]
+    rng = np.random.default_rng(3)
+    inst = rng.integers(0, len(paths), 40).astype(np.int32)
+    packs = [[], [], []]
+    per = []
+    for i, t in enumerate(inst):
+        Pl, Ql, Pg = scenarios(ogs[t], 1, 100 + i)
+        per.append((Pl[0], Ql[0], Pg[0]))
+        for k in range(3):
+            packs[k].append(per[-1][k])
+    b, r = run_batch(gb, grids, inst, *[np.concatenate(p) for p in packs])
+    info = b.info()
+    assert info["topologies"] == 4 and info["instances"] == 40
+    for i, t in enumerate(inst):
+        ref = oracle_solve(ogs[t], *per[i], 1)
+        assert r["iterations"][i] == ref["iterations"] and r["status"][i] == 0, (i, t)
+        assert np.max(np.abs(b.slice(r["V"], i) - ref["V"])) < 1e-9
+        assert np.max(np.abs(b.slice(r["theta"], i) - ref["theta"])) < 1e-9
+
+
+def test_batch_fp32_lu_accuracy(gb, oracle):
+    path = os.path.join(GOLDEN, "c2_base.cdf")
+    og = oracle.Grid(path)
+    n = 32
+    Pl, Ql, Pg = scenarios(og, n, 11)
+    b, r = run_batch(gb, [gb.read_grid(path)], np.zeros(n, np.int32), Pl.ravel(), Ql.ravel(), Pg.ravel(),
+                     precision=gb.PREC_FP32_IR)
+    for i in range(n):
+        ref = oracle_solve(og, Pl[i], Ql[i], Pg[i], 1)
+        assert r["status"][i] == 0 and r["final_mismatch"][i] <= 1e-8
+        assert r["iterations"][i] <= ref["iterations"] + 3
+        assert np.max(np.abs(b.slice(r["V"], i) - ref["V"])) < 1e-6
+        assert np.max(np.abs(b.slice(r["theta"], i) - ref["theta"])) < 1e-6
+
+
+def test_batch_large_factor_in_scratch(gb, oracle, tmp_path):
+    g = gb.generate(3, 20261208, tiles=16)
+    p = str(tmp_path / "c5.cdf")
+    g.write_cdf(p)
+    og = oracle.Grid(p)
+    n = 6
+    Pl, Ql, Pg = scenarios(og, n, 5)
+    b, r = run_batch(gb, [gb.read_grid(p)], np.zeros(n, np.int32), Pl.ravel(), Ql.ravel(), Pg.ravel(),
+                     lim_inj_reat=0)
+    assert b.info()["factors_in_smem"] == 0 and b.info()["scratch_bytes_per_block"] > 0
+    for i in range(n):
+        ref = oracle_solve(og, Pl[i], Ql[i], Pg[i], 0)
+        assert r["iterations"][i] == ref["iterations"]
+        assert np.max(np.abs(b.slice(r["V"], i) - ref["V"])) < 1e-9
+
+
+def test_batch_repeat_is_deterministic(gb):
+    path = os.path.join(GOLDEN, "c2_s8.cdf")
+    g = gb.read_grid(path)
+    b = gb.Batch([g], tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1)
+    b.set_instances(np.zeros(300, np.int32))
+    b.solve()
+    a = b.results()
+    b.solve()
+    c = b.results()
+    np.testing.assert_array_equal(a["V"], c["V"])
+    np.testing.assert_array_equal(a["iterations"], c["iterations"])
+    # identical instances give identical answers whatever block ran them
+    V = a["V"].reshape(300, g.nB)
+    assert np.all(V == V[0])
