@@ -496,7 +496,7 @@ class Batch:
         a = np.zeros(8, np.int64)
         _check(lib().gbpf_batch_info(self.h, _p(a)), "gbpf_batch_info")
         keys = ("topologies", "instances", "buses", "blocks", "smem_bytes", "factors_in_smem",
-                "scratch_bytes_per_block", "blobs_in_smem")
+                "scratch_bytes_per_block", "warp_instances")
         return dict(zip(keys, (int(x) for x in a)))
 
     def slice(self, arr, inst):

@@ -82,7 +82,8 @@ template <typename B4> __device__ __forceinline__ B4 bcast(B4 v, int src) {
 // shared memory with one copy when it fits.
 struct TopoOff {
     int yptr, ycol, yval, type, pv_bus, Qmin, Qmax, bus_of_blk, up_ptr, up_col, dg_ptr, dg_pos, dg_k,
-        og_ptr, og_a, og_b, flev_ptr, flev_steps, blev_ptr, blev_steps, ysl, rbus, cbus;
+        og_ptr, og_a, og_b, flev_ptr, flev_steps, blev_ptr, blev_steps, ysl, rbus, cbus, fent_ptr, fent_p,
+        fent_j;
 };
 struct Topo {
     int nB, nL, n, nup, nnzY, nPV, nfl, nbl, fac_smem, blob_smem, blob_bytes;
@@ -96,7 +97,7 @@ struct TopoView {
     const int *type, *pv_bus;
     const double *Qmin, *Qmax;
     const int *bus_of_blk, *up_ptr, *up_col, *dg_ptr, *dg_pos, *dg_k, *og_ptr, *og_a, *og_b;
-    const int *flev_ptr, *flev_steps, *blev_ptr, *blev_steps, *ysl, *rbus, *cbus;
+    const int *flev_ptr, *flev_steps, *blev_ptr, *blev_steps, *ysl, *rbus, *cbus, *fent_ptr, *fent_p, *fent_j;
 };
 __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     TopoView v;
@@ -110,6 +111,8 @@ __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     v.flev_ptr = (const int *)(b + o.flev_ptr); v.flev_steps = (const int *)(b + o.flev_steps);
     v.blev_ptr = (const int *)(b + o.blev_ptr); v.blev_steps = (const int *)(b + o.blev_steps);
     v.ysl = (const int *)(b + o.ysl); v.rbus = (const int *)(b + o.rbus); v.cbus = (const int *)(b + o.cbus);
+    v.fent_ptr = (const int *)(b + o.fent_ptr); v.fent_p = (const int *)(b + o.fent_p);
+    v.fent_j = (const int *)(b + o.fent_j);
     return v;
 }
 
@@ -126,7 +129,10 @@ struct Args {
     int ev_cap;
     double tol;
     int max_iter, lim;
-    int *counter;
+    int *counter;                  // claim counter of this launch's queue
+    const int *queue;              // instance ids served by this launch
+    int queue_len;
+    int slice;                     // warp kernel: shared-memory bytes per warp
     char *scratch;                 // per-block factor slices when not in shared memory
     long long scratch_stride;
     int blob_region;               // bytes of dynamic shared memory reserved for a staged blob
@@ -180,7 +186,7 @@ __device__ __forceinline__ double block_max(double v, double *red) {
 }
 
 template <typename TJ>
-__global__ void __launch_bounds__(kThreads) k_nr_block(Args a) {
+__global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
     using B4 = typename Blk<TJ>::b4;
     using B2 = typename Blk<TJ>::b2;
     extern __shared__ __align__(32) unsigned char smem[];
@@ -191,10 +197,13 @@ __global__ void __launch_bounds__(kThreads) k_nr_block(Args a) {
     unsigned char *ism = smem + a.blob_region;  // per-instance region
     if (tid == 0) s_topo = -1;
     for (;;) {
-        if (tid == 0) s_inst = atomicAdd(a.counter, 1);
+        if (tid == 0) {
+            const int q = atomicAdd(a.counter, 1);
+            s_inst = q < a.queue_len ? a.queue[q] : -1;
+        }
         __syncthreads();
         const int inst = s_inst;
-        if (inst >= a.n_inst) break;
+        if (inst < 0) break;
         const int t_id = a.inst_topo[inst];
         const Topo T = a.topo[t_id];
         // stage the topology's blob in shared memory unless it is already there
@@ -350,79 +359,60 @@ __global__ void __launch_bounds__(kThreads) k_nr_block(Args a) {
                 fac[q] = blk;
             }
             __syncthreads();
-            // LU factorisation fused with forward substitution, one level at a time
+            // LU factorisation fused with forward substitution, one level at a
+            // time, in two passes: one thread per pivot j (diagonal block, its
+            // inverse through one reciprocal, y_j), then one thread per
+            // off-diagonal entry of the level (U(j,i) and L(i,j) = (...) D_j^-1).
             for (int l = 0; l < T.nfl; l++) {
-                const int beg = G.flev_ptr[l], end = G.flev_ptr[l + 1];
-                for (int w = beg + warp; w < end; w += kWarps) {
+                for (int w = G.flev_ptr[l] + tid; w < G.flev_ptr[l + 1]; w += kThreads) {
                     const int j = G.flev_steps[w];
-                    B4 acc;
-                    acc.x = acc.y = acc.z = acc.w = 0;
-                    B2 accy;
-                    accy.x = accy.y = 0;
-                    for (int t = G.dg_ptr[j] + lane; t < G.dg_ptr[j + 1]; t += 32) {
+                    B4 D = fac[j];
+                    B2 yj;
+                    yj.x = (TJ)R[j].x;
+                    yj.y = (TJ)R[j].y;
+                    for (int t = G.dg_ptr[j]; t < G.dg_ptr[j + 1]; t++) {
                         const int p = G.dg_pos[t];
                         const B4 lj = Lv[p];
-                        acc = badd(acc, bm(lj, Uv[p]));
+                        D = bsub(D, bm(lj, Uv[p]));
                         const B2 v = bmv(lj, ys[G.dg_k[t]]);
-                        accy.x += v.x;
-                        accy.y += v.y;
+                        yj.x -= v.x;
+                        yj.y -= v.y;
                     }
-                    for (int o = 16; o > 0; o >>= 1) {
-                        acc = bshfl_xor(acc, o);
-                        accy.x += __shfl_xor_sync(0xffffffffu, accy.x, o);
-                        accy.y += __shfl_xor_sync(0xffffffffu, accy.y, o);
-                    }
+                    const TJ det = D.x * D.w - D.y * D.z;
+                    if (det == (TJ)0 || !isfinite(det)) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                    const TJ rd = (TJ)1 / det;
                     B4 inv;
-                    inv.x = inv.y = inv.z = inv.w = 0;
-                    if (lane == 0) {
-                        const B4 D = bsub(fac[j], acc);
-                        const TJ det = D.x * D.w - D.y * D.z;
-                        if (det == (TJ)0 || !isfinite(det)) { s_status = GBPF_E_SINGULAR; s_done = 1; }
-                        inv.x = D.w / det; inv.y = -D.y / det; inv.z = -D.z / det; inv.w = D.x / det;
-                        fac[j] = D;
-                        dinv[j] = inv;
-                        B2 yj;
-                        yj.x = (TJ)R[j].x - accy.x;
-                        yj.y = (TJ)R[j].y - accy.y;
-                        ys[j] = yj;
+                    inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
+                    fac[j] = D;
+                    dinv[j] = inv;
+                    ys[j] = yj;
+                }
+                __syncthreads();
+                for (int e = G.fent_ptr[l] + tid; e < G.fent_ptr[l + 1]; e += kThreads) {
+                    const int p = G.fent_p[e], j = G.fent_j[e];
+                    B4 aL = Lv[p], aU = Uv[p];
+                    for (int r = G.og_ptr[p]; r < G.og_ptr[p + 1]; r++) {
+                        const int x = G.og_a[r], y = G.og_b[r];
+                        aL = bsub(aL, bm(Lv[y], Uv[x]));
+                        aU = bsub(aU, bm(Lv[x], Uv[y]));
                     }
-                    inv = bcast(inv, 0);
-                    for (int p = G.up_ptr[j] + lane; p < G.up_ptr[j + 1]; p += 32) {
-                        B4 aL = Lv[p], aU = Uv[p];
-                        for (int r = G.og_ptr[p]; r < G.og_ptr[p + 1]; r++) {
-                            const int x = G.og_a[r], y = G.og_b[r];
-                            aL = bsub(aL, bm(Lv[y], Uv[x]));
-                            aU = bsub(aU, bm(Lv[x], Uv[y]));
-                        }
-                        Uv[p] = aU;
-                        Lv[p] = bm(aL, inv);
-                    }
+                    Uv[p] = aU;
+                    Lv[p] = bm(aL, dinv[j]);
                 }
                 __syncthreads();
             }
             if (s_done) break;
-            // backward substitution
+            // backward substitution, one thread per pivot of each level
             for (int l = 0; l < T.nbl; l++) {
-                const int beg = G.blev_ptr[l], end = G.blev_ptr[l + 1];
-                for (int w = beg + warp; w < end; w += kWarps) {
+                for (int w = G.blev_ptr[l] + tid; w < G.blev_ptr[l + 1]; w += kThreads) {
                     const int j = G.blev_steps[w];
-                    B2 acc;
-                    acc.x = acc.y = 0;
-                    for (int p = G.up_ptr[j] + lane; p < G.up_ptr[j + 1]; p += 32) {
+                    B2 acc = ys[j];
+                    for (int p = G.up_ptr[j]; p < G.up_ptr[j + 1]; p++) {
                         const B2 v = bmv(Uv[p], xs[G.up_col[p]]);
-                        acc.x += v.x;
-                        acc.y += v.y;
+                        acc.x -= v.x;
+                        acc.y -= v.y;
                     }
-                    for (int o = 16; o > 0; o >>= 1) {
-                        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-                        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
-                    }
-                    if (lane == 0) {
-                        B2 t;
-                        t.x = ys[j].x - acc.x;
-                        t.y = ys[j].y - acc.y;
-                        xs[j] = bmv(dinv[j], t);
-                    }
+                    xs[j] = bmv(dinv[j], acc);
                 }
                 __syncthreads();
             }
@@ -455,6 +445,247 @@ __global__ void __launch_bounds__(kThreads) k_nr_block(Args a) {
             a.n_events[inst] = s_nev;
         }
         __syncthreads();
+    }
+}
+
+
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const double t = __shfl_xor_sync(0xffffffffu, v, o);
+        v = (t > v || t != t) ? t : v;
+    }
+    return v;
+}
+
+// One instance per warp: the same Newton loop as k_nr_block with the 32 lanes
+// of a warp in place of the threads of a block, so the only barriers are
+// __syncwarp.  Each warp owns a slice of the block's dynamic shared memory
+// (state and factor); the topology's read-only blob is read from global
+// memory through the L1 cache.
+template <typename TJ>
+__global__ void __launch_bounds__(256) k_nr_warp(Args a) {
+    using B4 = typename Blk<TJ>::b4;
+    using B2 = typename Blk<TJ>::b2;
+    constexpr unsigned FULL = 0xffffffffu;
+    extern __shared__ __align__(32) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    unsigned char *ism = smem + (size_t)(threadIdx.x >> 5) * a.slice;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    for (;;) {
+        int q = 0;
+        if (lane == 0) q = atomicAdd(a.counter, 1);
+        q = __shfl_sync(FULL, q, 0);
+        if (q >= a.queue_len) break;
+        const int inst = a.queue[q];
+        const int t_id = a.inst_topo[inst];
+        const Topo T = a.topo[t_id];
+        const TopoView G = bind(T.o, T.blob);
+        const long long off = a.inst_off[inst];
+        const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, 1);
+        double *V = (double *)(ism + L.V), *th = (double *)(ism + L.th);
+        double *cs = (double *)(ism + L.cs), *sn = (double *)(ism + L.sn);
+        double *P = (double *)(ism + L.P), *Q = (double *)(ism + L.Q), *QL = (double *)(ism + L.QL);
+        double2 *R = (double2 *)(ism + L.R);
+        int *act = (int *)(ism + L.act), *limQ = (int *)(ism + L.lim);
+        B2 *ys = (B2 *)(ism + L.ys), *xs = (B2 *)(ism + L.xs);
+        B4 *fac = (B4 *)(ism + L.fac), *dinv = (B4 *)(ism + L.dinv);
+        const int n = T.n, nB = T.nB, nq = T.n + 2 * T.nup;
+        B4 *Lv = fac + n, *Uv = fac + n + T.nup;
+        for (int k = lane; k < nB; k += 32) {
+            V[k] = a.V0[off + k];
+            th[k] = a.th0[off + k];
+            QL[k] = a.Qliq[off + k];
+            act[k] = (G.type[k] == 0 || G.type[k] == 1);
+        }
+        for (int i = lane; i < T.nPV; i += 32) limQ[i] = 0;
+        int it = 0, status = 0, nev = 0;
+        double maxDx = INFINITY, maxG = 0;
+        __syncwarp();
+        for (;;) {
+            for (int k = lane; k < nB; k += 32) {
+                double s, c;
+                sincos(th[k], &s, &c);
+                cs[k] = c;
+                sn[k] = s;
+            }
+            __syncwarp();
+            for (int k = lane; k < nB; k += 32) {
+                double ir = 0, ii = 0;
+                for (int p = G.yptr[k]; p < G.yptr[k + 1]; p++) {
+                    const int m = G.ycol[p];
+                    const double2 y = G.yval[p];
+                    const double em = V[m] * cs[m], fm = V[m] * sn[m];
+                    ir += y.x * em - y.y * fm;
+                    ii += y.x * fm + y.y * em;
+                }
+                const double ek = V[k] * cs[k], fk = V[k] * sn[k];
+                P[k] = ek * ir + fk * ii;
+                Q[k] = fk * ir - ek * ii;
+            }
+            __syncwarp();
+            if (a.lim && it >= 1 && it < a.max_iter && maxDx < a.tol * 10.) {
+                for (int i0 = 0; i0 < T.nPV; i0 += 32) {
+                    const int i = i0 + lane;
+                    int code = 0, b = 0;
+                    if (i < T.nPV) {
+                        b = G.pv_bus[i];
+                        const double ql = a.Qload[off + b], qg = Q[b] + ql;
+                        if (qg < G.Qmin[i] - a.tol) {
+                            if (!limQ[i]) code = 1;
+                            else if (QL[b] != G.Qmin[i] - ql) code = 2;
+                            limQ[i] = 1;
+                            QL[b] = G.Qmin[i] - ql;
+                        } else if (qg > G.Qmax[i] + a.tol) {
+                            if (!limQ[i]) code = 3;
+                            else if (QL[b] != G.Qmax[i] - ql) code = 4;
+                            limQ[i] = 1;
+                            QL[b] = G.Qmax[i] - ql;
+                        } else {
+                            if (limQ[i]) code = 5;
+                            limQ[i] = 0;
+                        }
+                        act[b] = limQ[i];
+                    }
+                    // events in PV order, as chkLimQ prints them
+                    const unsigned m = __ballot_sync(FULL, code != 0);
+                    const int e = nev + __popc(m & lt_mask);
+                    if (code && e < a.ev_cap) {
+                        int *ev = a.events + ((long long)inst * a.ev_cap + e) * 4;
+                        ev[0] = it; ev[1] = b + 1; ev[2] = i; ev[3] = code;
+                    }
+                    nev += __popc(m);
+                }
+                __syncwarp();
+            }
+            double mloc = 0;
+            for (int j = lane; j < n; j += 32) {
+                const int k = G.bus_of_blk[j];
+                const double gp = a.Pliq[off + k] - P[k];
+                const double gq = act[k] ? QL[k] - Q[k] : 0.0;
+                R[j] = make_double2(gp, gq);
+                double t = fmax(fabs(gp), fabs(gq));
+                if (t != t) t = __longlong_as_double(0x7ff8000000000000ll);
+                mloc = (t > mloc || t != t) ? t : mloc;
+            }
+            maxG = warp_max(mloc);
+            if (maxG != maxG) { status = GBPF_E_NOCONV; break; }
+            if (maxG <= a.tol) break;
+            if (it >= a.max_iter) { status = GBPF_E_NOCONV; break; }
+            for (int qq = lane; qq < nq; qq += 32) {
+                const int sl = G.ysl[qq];
+                B4 blk;
+                blk.x = blk.y = blk.z = blk.w = 0;
+                if (sl >= 0) {
+                    const int k = G.rbus[qq], mb = G.cbus[qq];
+                    const double2 y = G.yval[sl];
+                    const double Vk = V[k];
+                    const int ak = act[k];
+                    if (qq < n) {
+                        const double Pk = P[k], Qk = Q[k], v2 = Vk * Vk;
+                        blk.x = (TJ)(-Qk - v2 * y.y);
+                        if (ak) {
+                            blk.y = (TJ)((Pk + v2 * y.x) / Vk);
+                            blk.z = (TJ)(Pk - v2 * y.x);
+                            blk.w = (TJ)((Qk - v2 * y.y) / Vk);
+                        } else {
+                            blk.w = (TJ)1;
+                        }
+                    } else {
+                        const int am = act[mb];
+                        const TJ ck = (TJ)cs[k], sk = (TJ)sn[k], cm = (TJ)cs[mb], sm = (TJ)sn[mb];
+                        const TJ yr = (TJ)y.x, yi = (TJ)y.y, vk = (TJ)Vk, vm = (TJ)V[mb];
+                        const TJ tr = yr * cm - yi * sm, ti = yr * sm + yi * cm;
+                        const TJ wr = ck * tr + sk * ti, wi = sk * tr - ck * ti;
+                        blk.x = vk * vm * wi;
+                        if (am) blk.y = vk * wr;
+                        if (ak) blk.z = -vk * vm * wr;
+                        if (ak && am) blk.w = vk * wi;
+                    }
+                }
+                fac[qq] = blk;
+            }
+            __syncwarp();
+            bool sing = false;
+            for (int l = 0; l < T.nfl; l++) {
+                for (int w = G.flev_ptr[l] + lane; w < G.flev_ptr[l + 1]; w += 32) {
+                    const int j = G.flev_steps[w];
+                    B4 D = fac[j];
+                    B2 yj;
+                    yj.x = (TJ)R[j].x;
+                    yj.y = (TJ)R[j].y;
+                    for (int t = G.dg_ptr[j]; t < G.dg_ptr[j + 1]; t++) {
+                        const int p = G.dg_pos[t];
+                        const B4 lj = Lv[p];
+                        D = bsub(D, bm(lj, Uv[p]));
+                        const B2 v = bmv(lj, ys[G.dg_k[t]]);
+                        yj.x -= v.x;
+                        yj.y -= v.y;
+                    }
+                    const TJ det = D.x * D.w - D.y * D.z;
+                    sing |= (det == (TJ)0 || !isfinite(det));
+                    const TJ rd = (TJ)1 / det;
+                    B4 inv;
+                    inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
+                    fac[j] = D;
+                    dinv[j] = inv;
+                    ys[j] = yj;
+                }
+                __syncwarp();
+                for (int e = G.fent_ptr[l] + lane; e < G.fent_ptr[l + 1]; e += 32) {
+                    const int p = G.fent_p[e], j = G.fent_j[e];
+                    B4 aL = Lv[p], aU = Uv[p];
+                    for (int r = G.og_ptr[p]; r < G.og_ptr[p + 1]; r++) {
+                        const int x = G.og_a[r], y = G.og_b[r];
+                        aL = bsub(aL, bm(Lv[y], Uv[x]));
+                        aU = bsub(aU, bm(Lv[x], Uv[y]));
+                    }
+                    Uv[p] = aU;
+                    Lv[p] = bm(aL, dinv[j]);
+                }
+                __syncwarp();
+            }
+            if (__any_sync(FULL, sing)) { status = GBPF_E_SINGULAR; break; }
+            for (int l = 0; l < T.nbl; l++) {
+                for (int w = G.blev_ptr[l] + lane; w < G.blev_ptr[l + 1]; w += 32) {
+                    const int j = G.blev_steps[w];
+                    B2 acc = ys[j];
+                    for (int p = G.up_ptr[j]; p < G.up_ptr[j + 1]; p++) {
+                        const B2 v = bmv(Uv[p], xs[G.up_col[p]]);
+                        acc.x -= v.x;
+                        acc.y -= v.y;
+                    }
+                    xs[j] = bmv(dinv[j], acc);
+                }
+                __syncwarp();
+            }
+            double md = 0;
+            for (int j = lane; j < n; j += 32) {
+                const int k = G.bus_of_blk[j];
+                const double dt = (double)xs[j].x, dv = (double)xs[j].y;
+                th[k] += dt;
+                if (act[k]) V[k] += dv;
+                double t = fmax(fabs(dt), fabs(dv));
+                if (t != t) t = __longlong_as_double(0x7ff8000000000000ll);
+                md = (t > md || t != t) ? t : md;
+            }
+            maxDx = warp_max(md);
+            it++;
+            __syncwarp();
+        }
+        __syncwarp();
+        for (int k = lane; k < nB; k += 32) {
+            a.V[off + k] = V[k];
+            a.th[off + k] = th[k];
+            a.P[off + k] = P[k];
+            a.Q[off + k] = Q[k];
+        }
+        if (lane == 0) {
+            a.iters[inst] = it;
+            a.status[inst] = status;
+            a.mism[inst] = maxG;
+            a.n_events[inst] = nev;
+        }
+        __syncwarp();
     }
 }
 
@@ -545,10 +776,13 @@ struct gbpf_batch {
     long long n_bus_total = 0;
     std::vector<int> inst_topo;
     std::vector<long long> inst_off;
-    DevBuf inst_mem, out_mem, scratch, counter;
-    Args args{};
-    size_t smem = 0;
-    int grid_blocks = 0;
+    DevBuf inst_mem, out_mem, scratch, counter, queues;
+    Args args{};    // block-per-instance launch
+    Args wargs{};   // warp-per-instance launch
+    size_t smem = 0, warp_smem = 0;
+    int grid_blocks = 0, warp_grid = 0, warp_warps = 0, n_block_q = 0, n_warp_q = 0;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
 
@@ -557,6 +791,9 @@ struct gbpf_batch {
         if (graph) cudaGraphDestroy(graph);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
     gbpf_status add_topology(const Grid &g);
@@ -601,6 +838,8 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
     o.flev_ptr = put(S.flev_ptr.data(), (nfl + 1) * 4); o.flev_steps = put(S.flev_steps.data(), n * 4);
     o.blev_ptr = put(S.blev_ptr.data(), (nbl + 1) * 4); o.blev_steps = put(S.blev_steps.data(), n * 4);
     o.ysl = put(S.ysl.data(), nq * 4); o.rbus = put(S.rbus.data(), nq * 4); o.cbus = put(S.cbus.data(), nq * 4);
+    o.fent_ptr = put(S.fent_ptr.data(), (nfl + 1) * 4); o.fent_p = put(S.fent_p.data(), nup * 4);
+    o.fent_j = put(S.fent_j.data(), nup * 4);
     DevBuf mem, tmp;
     CK(cudaMalloc(&mem.p, blob.size()));
     CK(cudaMemcpyAsync(mem.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, stream));
@@ -708,58 +947,108 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
 }
 
 gbpf_status gbpf_batch::launch(cudaStream_t st) {
-    CK(cudaMemsetAsync(args.counter, 0, sizeof(int), st));
-    if (precision == GBPF_PREC_FP32_IR) k_nr_block<float><<<grid_blocks, kThreads, smem, st>>>(args);
-    else k_nr_block<double><<<grid_blocks, kThreads, smem, st>>>(args);
-    CK(cudaGetLastError());
+    const bool fp32 = precision == GBPF_PREC_FP32_IR;
+    CK(cudaMemsetAsync(args.counter, 0, 2 * sizeof(int), st));
+    if (n_block_q) {
+        CK(cudaEventRecord(fork, st));
+        CK(cudaStreamWaitEvent(side, fork, 0));
+        if (fp32) k_nr_block<float><<<grid_blocks, kThreads, smem, side>>>(args);
+        else k_nr_block<double><<<grid_blocks, kThreads, smem, side>>>(args);
+        CK(cudaGetLastError());
+    }
+    if (n_warp_q) {
+        if (fp32) k_nr_warp<float><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wargs);
+        else k_nr_warp<double><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wargs);
+        CK(cudaGetLastError());
+    }
+    if (n_block_q) {
+        CK(cudaEventRecord(join, side));
+        CK(cudaStreamWaitEvent(st, join, 0));
+    }
     return GBPF_OK;
 }
 
 gbpf_status gbpf_batch::build_graph() {
-    // Shared-memory plan, per topology: its blob is staged in shared memory when
-    // it is at most 48 KB; its factor stays in shared memory when blob region +
-    // state + factor fit in 110 KB (two blocks per SM), otherwise it lives in a
-    // per-block slice of global scratch.
-    const size_t budget = 110 * 1024, blob_cap = 48 * 1024;
-    size_t region = 0, need = 0, scr = 0;
     const bool fp32 = precision == GBPF_PREC_FP32_IR;
-    for (auto &t : topo_h) {
-        t.blob_smem = (size_t)t.blob_bytes <= blob_cap;
-        if (t.blob_smem) region = std::max(region, align_up((size_t)t.blob_bytes, 32));
-    }
-    for (auto &t : topo_h) {
-        Layout with = fp32 ? layout<float>(t.nB, t.n, t.nup, t.nPV, 1) : layout<double>(t.nB, t.n, t.nup, t.nPV, 1);
-        Layout without = fp32 ? layout<float>(t.nB, t.n, t.nup, t.nPV, 0) : layout<double>(t.nB, t.n, t.nup, t.nPV, 0);
-        if (region + with.total <= budget) { t.fac_smem = 1; need = std::max(need, with.total); }
-        else {
-            t.fac_smem = 0;
-            need = std::max(need, without.total);
-            scr = std::max(scr, fp32 ? scratch_bytes<float>(t.n, t.nup) : scratch_bytes<double>(t.n, t.nup));
-        }
-    }
-    args.blob_region = (int)region;
-    need += region;
-    smem = need;
     int dev_sm = 0, maxsm = 0;
     CK(cudaDeviceGetAttribute(&dev_sm, cudaDevAttrMultiProcessorCount, device));
     CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
-    if (smem > (size_t)maxsm) { set_error("instance state does not fit in shared memory"); return GBPF_E_UNSUPPORTED; }
-    int occ = 0;
-    if (precision == GBPF_PREC_FP32_IR) {
-        CK(cudaFuncSetAttribute(k_nr_block<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float>, kThreads, smem));
-    } else {
-        CK(cudaFuncSetAttribute(k_nr_block<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double>, kThreads, smem));
+    // Warp-per-instance for topologies whose state and factor fit a warp slice
+    // of shared memory; block-per-instance (factor possibly in scratch) else.
+    const size_t warp_cap = fp32 ? 40 * 1024 : 56 * 1024;
+    std::vector<int> warp_ok(topo_h.size(), 0);
+    size_t slice = 0;
+    for (size_t t = 0; t < topo_h.size(); t++) {
+        const Topo &T = topo_h[t];
+        const Layout w = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1) : layout<double>(T.nB, T.n, T.nup, T.nPV, 1);
+        if (w.total <= warp_cap) { warp_ok[t] = 1; slice = std::max(slice, align_up(w.total, 128)); }
     }
-    grid_blocks = std::max(1, std::min(n_inst, dev_sm * std::max(occ, 1)));
+    std::vector<int> wq, bq;
+    for (int i = 0; i < n_inst; i++) (warp_ok[inst_topo[i]] ? wq : bq).push_back(i);
+    n_warp_q = (int)wq.size();
+    n_block_q = (int)bq.size();
+    queues.reset();
+    CK(cudaMalloc(&queues.p, 4 * (size_t)n_inst + 256));
+    if (n_warp_q) CK(cudaMemcpy(queues.p, wq.data(), 4 * wq.size(), cudaMemcpyHostToDevice));
+    if (n_block_q) CK(cudaMemcpy((int *)queues.p + n_warp_q, bq.data(), 4 * bq.size(), cudaMemcpyHostToDevice));
+    // Block-mode shared-memory plan: the blob is staged in shared memory when
+    // at most 48 KB; the factor stays in shared memory when blob region +
+    // state + factor fit in 110 KB, otherwise it lives in global scratch.
+    const size_t budget = 110 * 1024, blob_cap = 48 * 1024;
+    size_t region = 0, need = 0, scr = 0;
+    for (size_t t = 0; t < topo_h.size(); t++) {
+        Topo &T = topo_h[t];
+        T.blob_smem = !warp_ok[t] && (size_t)T.blob_bytes <= blob_cap;
+        if (T.blob_smem) region = std::max(region, align_up((size_t)T.blob_bytes, 32));
+    }
+    for (size_t t = 0; t < topo_h.size(); t++) {
+        Topo &T = topo_h[t];
+        if (warp_ok[t]) { T.fac_smem = 1; continue; }
+        Layout with = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1) : layout<double>(T.nB, T.n, T.nup, T.nPV, 1);
+        Layout without = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 0) : layout<double>(T.nB, T.n, T.nup, T.nPV, 0);
+        if (region + with.total <= budget) { T.fac_smem = 1; need = std::max(need, with.total); }
+        else {
+            T.fac_smem = 0;
+            need = std::max(need, without.total);
+            scr = std::max(scr, fp32 ? scratch_bytes<float>(T.n, T.nup) : scratch_bytes<double>(T.n, T.nup));
+        }
+    }
+    args.blob_region = (int)region;
+    smem = n_block_q ? need + region : 0;
+    if (smem > (size_t)maxsm) { set_error("instance state does not fit in shared memory"); return GBPF_E_UNSUPPORTED; }
+    grid_blocks = 0;
+    if (n_block_q) {
+        int occ = 0;
+        if (fp32) {
+            CK(cudaFuncSetAttribute(k_nr_block<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float>, kThreads, smem));
+        } else {
+            CK(cudaFuncSetAttribute(k_nr_block<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double>, kThreads, smem));
+        }
+        grid_blocks = std::max(1, std::min(n_block_q, dev_sm * std::max(occ, 1)));
+    }
+    // warp-mode plan: as many warps per block as fit in 200 KB, at most 8
+    warp_grid = 0;
+    if (n_warp_q) {
+        warp_warps = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024) / slice));
+        warp_smem = (size_t)warp_warps * slice;
+        int occ = 0;
+        if (fp32) {
+            CK(cudaFuncSetAttribute(k_nr_warp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warp_smem));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_warp<float>, 32 * warp_warps, warp_smem));
+        } else {
+            CK(cudaFuncSetAttribute(k_nr_warp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warp_smem));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_warp<double>, 32 * warp_warps, warp_smem));
+        }
+        warp_grid = std::max(1, std::min((n_warp_q + warp_warps - 1) / warp_warps, dev_sm * std::max(occ, 1)));
+    }
     scratch.reset();
     args.scratch = nullptr;
     args.scratch_stride = (long long)align_up(scr, 256);
-    if (scr) CK(cudaMalloc(&scratch.p, (size_t)args.scratch_stride * grid_blocks));
+    if (scr && grid_blocks) CK(cudaMalloc(&scratch.p, (size_t)args.scratch_stride * grid_blocks));
     args.scratch = (char *)scratch.p;
     if (!counter.p) CK(cudaMalloc(&counter.p, 256));
-    args.counter = (int *)counter.p;
     topo_d.reset();
     CK(cudaMalloc(&topo_d.p, sizeof(Topo) * topo_h.size()));
     CK(cudaMemcpy(topo_d.p, topo_h.data(), sizeof(Topo) * topo_h.size(), cudaMemcpyHostToDevice));
@@ -768,6 +1057,14 @@ gbpf_status gbpf_batch::build_graph() {
     args.max_iter = max_iter;
     args.lim = lim;
     args.ev_cap = ev_cap;
+    wargs = args;
+    args.counter = (int *)counter.p;
+    args.queue = (const int *)queues.p + n_warp_q;
+    args.queue_len = n_block_q;
+    wargs.counter = (int *)counter.p + 1;
+    wargs.queue = (const int *)queues.p;
+    wargs.queue_len = n_warp_q;
+    wargs.slice = (int)slice;
     // one graph: reset the work counter, one persistent launch
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     gbpf_status st = launch(stream);
@@ -799,6 +1096,9 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
     CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&b->ev0));
     CK(cudaEventCreate(&b->ev1));
+    CK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
     for (int i = 0; i < n_grids; i++) {
         ARGCHECK(grids[i]);
         gbpf_status st = b->add_topology(grids[i]->g);
@@ -881,10 +1181,11 @@ extern "C" gbpf_status gbpf_batch_info(const gbpf_batch *b, long long info[8]) {
     info[0] = (long long)b->topo_h.size();
     info[1] = b->n_inst;
     info[2] = b->n_bus_total;
-    info[3] = b->grid_blocks;
+    info[3] = b->grid_blocks + b->warp_grid;
     info[4] = (long long)b->smem;
     info[5] = fs;
     info[6] = b->args.scratch_stride;
-    info[7] = bs;
+    info[7] = b->n_warp_q;
+    (void)bs;
     return GBPF_OK;
 }

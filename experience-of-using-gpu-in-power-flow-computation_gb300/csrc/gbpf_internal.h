@@ -61,6 +61,9 @@ struct Symbolic {
     std::vector<int> og_a, og_b;
     // Level schedules: forward (factor + L solve) and backward (U solve).
     std::vector<int> flev_ptr, flev_steps, blev_ptr, blev_steps;
+    // Off-diagonal entries of each forward level, flat: entries
+    // fent_ptr[l]..fent_ptr[l+1] are positions fent_p[] of steps fent_j[].
+    std::vector<int> fent_ptr, fent_p, fent_j;
     // Jacobian fill map over all factor block positions q in [0, n + 2*nup):
     // q < n: diagonal block q; n <= q < n+nup: L block at p = q-n (row i = up_col[p]);
     // q >= n+nup: U block at p = q-n-nup.  ysl[q] = Y slot of (row bus, col bus) or -1

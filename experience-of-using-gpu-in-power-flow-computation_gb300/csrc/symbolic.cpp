@@ -228,6 +228,16 @@ Symbolic analyse(const Grid &g, const YPattern &y, std::string *why) {
     };
     bucket(fl, nfl, S.flev_ptr, S.flev_steps);
     bucket(bl, nbl, S.blev_ptr, S.blev_steps);
+    S.fent_ptr.assign(nfl + 1, 0);
+    S.fent_p.clear();
+    S.fent_j.clear();
+    for (int l = 0; l < nfl; l++) {
+        for (int t = S.flev_ptr[l]; t < S.flev_ptr[l + 1]; t++) {
+            const int j = S.flev_steps[t];
+            for (int p = S.up_ptr[j]; p < S.up_ptr[j + 1]; p++) { S.fent_p.push_back(p); S.fent_j.push_back(j); }
+        }
+        S.fent_ptr[l + 1] = (int)S.fent_p.size();
+    }
     // Jacobian fill map over factor block positions
     const int nq = n + 2 * S.nup;
     S.ysl.resize(nq);

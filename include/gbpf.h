@@ -295,9 +295,9 @@ gbpf_status gbpf_batch_results(gbpf_batch *b, int *iterations, int *status, doub
 gbpf_status gbpf_batch_events(gbpf_batch *b, int inst, int *ev, int cap, int *n);
 
 /* info[0..7] = topologies, instances, packed buses, resident thread blocks,
- * dynamic shared memory per block, topologies whose factor is in shared
- * memory, global scratch bytes per block, topologies whose read-only arrays
- * are staged in shared memory. */
+ * dynamic shared memory per block of the block-per-instance kernel,
+ * topologies whose factor is in shared memory, global scratch bytes per
+ * block, instances served by the warp-per-instance kernel. */
 gbpf_status gbpf_batch_info(const gbpf_batch *b, long long info[8]);
 
 /* Device query for the driver's banner (initGPU, GPU/sistema.cuh:426-468):
