@@ -38,7 +38,7 @@ EXPORTS = [
     "gbpf_solver_flows", "gbpf_solver_info", "gbpf_solver_time", "gbpf_solver_profile", "gbpf_ybus", "gbpf_eval_pq",
     "gbpf_eval_jacobian", "gbpf_newton_step", "gbpf_device_info", "gbpf_last_error", "gbpf_status_str",
     "gbpf_batch_create", "gbpf_batch_free", "gbpf_batch_set_instances", "gbpf_batch_solve", "gbpf_batch_time",
-    "gbpf_batch_results", "gbpf_batch_events", "gbpf_batch_info",
+    "gbpf_batch_results", "gbpf_batch_events", "gbpf_batch_info", "gbpf_batch_solve_noalloc",
 ]
 
 
@@ -498,6 +498,17 @@ class Batch:
         keys = ("topologies", "instances", "buses", "blocks", "smem_bytes", "factors_in_smem",
                 "scratch_bytes_per_block", "warp_instances")
         return dict(zip(keys, (int(x) for x in a)))
+
+    def solve_noalloc(self, grid_of_inst, V0, theta0, Pliq, Qliq, Qload, V, theta, Pcalc, Qcalc,
+                      iterations, status, final_mismatch, stream=0):
+        """gbpf_batch_solve_noalloc: every array argument except grid_of_inst
+        is a device address (int); asynchronous on `stream`."""
+        gi = _i32(grid_of_inst)
+        vp = ctypes.c_void_p
+        _check(lib().gbpf_batch_solve_noalloc(
+            self.h, len(gi), _p(gi), vp(V0), vp(theta0), vp(Pliq), vp(Qliq), vp(Qload), vp(V), vp(theta),
+            vp(Pcalc), vp(Qcalc), vp(iterations), vp(status), vp(final_mismatch), vp(stream)),
+            "gbpf_batch_solve_noalloc")
 
     def slice(self, arr, inst):
         return arr[self.offsets[inst]:self.offsets[inst + 1]]

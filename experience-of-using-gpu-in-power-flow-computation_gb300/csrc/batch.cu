@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -755,6 +756,37 @@ struct DevBuf {
 
 }  // namespace
 
+// Scratch of gbpf_batch_solve_noalloc: file-scope device memory, so that the
+// entry point itself allocates nothing.  8 MiB on every GPU that loads the
+// library, held until the process exits.  Every call shares it.
+constexpr size_t kNoAllocBytes = 8u << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch for `device`, which must be current.  In
+// host code the symbol is only a host-side stand-in, so the address comes
+// from cudaGetSymbolAddress, once per device.
+gbpf_status noalloc_setup(int device, void **out) {
+    if (device < 0 || device >= kMaxDevices) { set_error("device ordinal out of range"); return GBPF_E_ARG; }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            set_error(std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+            return GBPF_E_CUDA;
+        }
+        g_noalloc_ptr[device] = p;
+    }
+    *out = g_noalloc_ptr[device];
+    return GBPF_OK;
+}
+}  // namespace
+
 // ---------------------------------------------------------------------------
 // host object
 // ---------------------------------------------------------------------------
@@ -783,6 +815,8 @@ struct gbpf_batch {
     int grid_blocks = 0, warp_grid = 0, warp_warps = 0, n_block_q = 0, n_warp_q = 0;
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    DevBuf topo_na;          // topologies planned for gbpf_batch_solve_noalloc
+    size_t na_smem = 0, na_stride = 0;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
 
@@ -1104,7 +1138,112 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
         gbpf_status st = b->add_topology(grids[i]->g);
         if (st != GBPF_OK) return st;
     }
+    // plan for the allocation-free entry point: blobs read from global memory,
+    // factors in slices of the static scratch
+    {
+        const bool fp32 = b->precision == GBPF_PREC_FP32_IR;
+        std::vector<Topo> na(b->topo_h);
+        for (auto &t : na) {
+            t.blob_smem = 0;
+            t.fac_smem = 0;
+            const Layout l = fp32 ? layout<float>(t.nB, t.n, t.nup, t.nPV, 0) : layout<double>(t.nB, t.n, t.nup, t.nPV, 0);
+            b->na_smem = std::max(b->na_smem, l.total);
+            b->na_stride = std::max(b->na_stride, align_up(fp32 ? scratch_bytes<float>(t.n, t.nup)
+                                                                : scratch_bytes<double>(t.n, t.nup), 256));
+        }
+        CK(cudaMalloc(&b->topo_na.p, sizeof(Topo) * na.size()));
+        CK(cudaMemcpy(b->topo_na.p, na.data(), sizeof(Topo) * na.size(), cudaMemcpyHostToDevice));
+        void *p = nullptr;
+        gbpf_status st = noalloc_setup(device, &p);
+        if (st != GBPF_OK) return st;
+    }
     *out = b.release();
+    return GBPF_OK;
+}
+
+// For callers that cannot allocate device memory at solve time (allocation is
+// forbidden in their stream-capture region, or their memory is owned by
+// another allocator): the batch Newton solve on caller-owned device buffers,
+// with every scratch byte in g_noalloc_scratch.  The batch handle is made
+// beforehand with gbpf_batch_create (which does allocate, once).  Calls share
+// the scratch, so calls that overlap on the GPU race; the work counter is
+// cleared at the start of each call, everything else is fully rewritten.
+// Switch events are not recorded.  Asynchronous on `stream` (NULL = the
+// batch's own stream).
+extern "C" gbpf_status gbpf_batch_solve_noalloc(gbpf_batch *b, int n_inst, const int *grid_of_inst,
+                                                const double *V0, const double *theta0, const double *Pliq,
+                                                const double *Qliq, const double *Qload, double *V,
+                                                double *theta, double *Pcalc, double *Qcalc, int *iterations,
+                                                int *status, double *final_mismatch, void *stream) {
+    ARGCHECK(b && n_inst > 0 && grid_of_inst && V0 && theta0 && Pliq && Qliq && Qload && V && theta && Pcalc &&
+             Qcalc && iterations && status && final_mismatch);
+    CK(cudaSetDevice(b->device));
+    void *base = nullptr;
+    gbpf_status st = noalloc_setup(b->device, &base);
+    if (st != GBPF_OK) return st;
+    const int nt = (int)b->topo_h.size();
+    // per-call metadata: counter | queue | topology ids | bus offsets | event counts | factor slices
+    const size_t o_queue = 256, o_topo = o_queue + align_up(4 * (size_t)n_inst, 256),
+                 o_off = o_topo + align_up(4 * (size_t)n_inst, 256),
+                 o_nev = o_off + align_up(8 * (size_t)n_inst, 256),
+                 o_slices = o_nev + align_up(4 * (size_t)n_inst, 256);
+    if (o_slices + b->na_stride > kNoAllocBytes) {
+        set_error("gbpf_batch_solve_noalloc: " + std::to_string(n_inst) + " instances need " +
+                  std::to_string((o_slices + b->na_stride) >> 10) + " KiB of scratch; the static scratch holds " +
+                  std::to_string(kNoAllocBytes >> 10) + " KiB");
+        return GBPF_E_ARG;
+    }
+    std::vector<int> queue(n_inst), topo(n_inst);
+    std::vector<long long> off(n_inst);
+    long long o = 0;
+    for (int i = 0; i < n_inst; i++) {
+        if (grid_of_inst[i] < 0 || grid_of_inst[i] >= nt) { set_error("instance names an unknown grid"); return GBPF_E_ARG; }
+        queue[i] = i;
+        topo[i] = grid_of_inst[i];
+        off[i] = o;
+        o += b->topo_h[topo[i]].nB;
+    }
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    char *sc = (char *)base;
+    CK(cudaMemsetAsync(sc, 0, sizeof(int), s));
+    CK(cudaMemcpyAsync(sc + o_queue, queue.data(), 4 * (size_t)n_inst, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sc + o_topo, topo.data(), 4 * (size_t)n_inst, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sc + o_off, off.data(), 8 * (size_t)n_inst, cudaMemcpyHostToDevice, s));
+    Args a{};
+    a.topo = (const Topo *)b->topo_na.p;
+    a.n_inst = n_inst;
+    a.inst_topo = (const int *)(sc + o_topo);
+    a.inst_off = (const long long *)(sc + o_off);
+    a.V0 = V0; a.th0 = theta0; a.Pliq = Pliq; a.Qliq = Qliq; a.Qload = Qload;
+    a.V = V; a.th = theta; a.P = Pcalc; a.Q = Qcalc;
+    a.iters = iterations; a.status = status; a.mism = final_mismatch;
+    a.n_events = (int *)(sc + o_nev);
+    a.events = nullptr;
+    a.ev_cap = 0;
+    a.tol = b->tol; a.max_iter = b->max_iter; a.lim = b->lim;
+    a.counter = (int *)sc;
+    a.queue = (const int *)(sc + o_queue);
+    a.queue_len = n_inst;
+    a.scratch = sc + o_slices;
+    a.scratch_stride = (long long)b->na_stride;
+    a.blob_region = 0;
+    const bool fp32 = b->precision == GBPF_PREC_FP32_IR;
+    int dev_sm = 0, occ = 0;
+    CK(cudaDeviceGetAttribute(&dev_sm, cudaDevAttrMultiProcessorCount, b->device));
+    cudaFuncAttributes fa{};
+    if (fp32) CK(cudaFuncGetAttributes(&fa, k_nr_block<float>));
+    else CK(cudaFuncGetAttributes(&fa, k_nr_block<double>));
+    if ((size_t)fa.maxDynamicSharedSizeBytes < b->na_smem) {
+        if (fp32) CK(cudaFuncSetAttribute(k_nr_block<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->na_smem));
+        else CK(cudaFuncSetAttribute(k_nr_block<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->na_smem));
+    }
+    if (fp32) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float>, kThreads, b->na_smem));
+    else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double>, kThreads, b->na_smem));
+    const long long slices = (long long)((kNoAllocBytes - o_slices) / b->na_stride);
+    const int grid = (int)std::max(1LL, std::min<long long>({(long long)n_inst, (long long)dev_sm * std::max(occ, 1), slices}));
+    if (fp32) k_nr_block<float><<<grid, kThreads, b->na_smem, s>>>(a);
+    else k_nr_block<double><<<grid, kThreads, b->na_smem, s>>>(a);
+    CK(cudaGetLastError());
     return GBPF_OK;
 }
 

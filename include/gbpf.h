@@ -294,6 +294,25 @@ gbpf_status gbpf_batch_results(gbpf_batch *b, int *iterations, int *status, doub
  * gbpf_solver_events. */
 gbpf_status gbpf_batch_events(gbpf_batch *b, int inst, int *ev, int cap, int *n);
 
+/* For callers that cannot allocate device memory when they solve: their
+ * solves run inside a stream-capture region where allocation is not allowed,
+ * or their device memory belongs to another allocator.  No counterpart in the
+ * reference.  Solves n_inst instances like gbpf_batch_set_instances +
+ * gbpf_batch_solve, on caller-owned DEVICE buffers packed in instance order
+ * (V0, theta0, Pliq, Qliq, Qload in; V, theta, Pcalc, Qcalc, iterations,
+ * status, final_mismatch out); grid_of_inst is a HOST array.  Allocates
+ * nothing: all scratch lives in one static 8 MiB device array, each GPU that
+ * loads the library holds it until exit, and every call shares it, so calls
+ * that overlap on the GPU race.  gbpf_batch_create does the one-time set-up
+ * for its device.  Rejects with GBPF_E_ARG an instance count or a factor that
+ * does not fit the scratch.  Does not record switch events.  Asynchronous on
+ * `stream` (a cudaStream_t; NULL = the batch's stream). */
+gbpf_status gbpf_batch_solve_noalloc(gbpf_batch *b, int n_inst, const int *grid_of_inst,
+                                     const double *V0, const double *theta0, const double *Pliq,
+                                     const double *Qliq, const double *Qload, double *V,
+                                     double *theta, double *Pcalc, double *Qcalc, int *iterations,
+                                     int *status, double *final_mismatch, void *stream);
+
 /* info[0..7] = topologies, instances, packed buses, resident thread blocks,
  * dynamic shared memory per block of the block-per-instance kernel,
  * topologies whose factor is in shared memory, global scratch bytes per

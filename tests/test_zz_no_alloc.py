@@ -1,0 +1,87 @@
+"""gbpf_batch_solve_noalloc, the entry point that allocates nothing, against
+the allocating batch entry points on the same instances, two calls in a row.
+
+Who needs it: callers that cannot allocate device memory when they solve --
+their solves run inside a CUDA stream-capture region, where allocation is not
+allowed, or their device memory belongs to another allocator.  The entry point
+works on their device buffers and keeps its own scratch in one static 8 MiB
+device array.  Same arithmetic as the allocating path (only the place of the
+factor differs), so |V| and theta must agree to 1e-12, iteration counts and
+statuses exactly.  The second call uses other instances, so stale contents of
+the shared scratch would show up."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def _instances(grids, n, seed):
+    rng = np.random.default_rng(seed)
+    gi = rng.integers(0, len(grids), n).astype(np.int32)
+    cols = {k: [] for k in ("Pload", "Qload", "Pg", "Qg", "V0", "theta0")}
+    for t in gi:
+        b = grids[t].buses()
+        lf = np.exp(rng.normal(-0.005, 0.1, grids[t].nB))
+        gf = rng.uniform(0.9, 1.1, grids[t].nB)
+        cols["Pload"].append(b["Pload"] * lf)
+        cols["Qload"].append(b["Qload"] * lf)
+        cols["Pg"].append(b["Pg"] * gf)
+        cols["Qg"].append(b["Qg"])
+        cols["V0"].append(b["V0"])
+        cols["theta0"].append(b["theta0"])
+    return gi, {k: np.concatenate(v) for k, v in cols.items()}
+
+
+def test_noalloc_matches_batch_on_two_calls(gb):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device visible to torch")
+    grids = [gb.read_grid(os.path.join(GOLDEN, "c1.cdf")), gb.read_grid(os.path.join(GOLDEN, "c2_base.cdf"))]
+    opts = dict(tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1)
+    noalloc = gb.Batch(grids, **opts)
+    reference = gb.Batch(grids, **opts)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    for n, seed in ((24, 1), (37, 2)):
+        gi, c = _instances(grids, n, seed)
+        reference.set_instances(gi, Pload=c["Pload"], Qload=c["Qload"], Pg=c["Pg"], Qg=c["Qg"], V0=c["V0"],
+                                theta0=c["theta0"])
+        reference.solve()
+        ref = reference.results()
+        t = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)
+        V0, th0 = t(c["V0"]), t(c["theta0"])
+        Pliq, Qliq, Qload = t(c["Pg"] - c["Pload"]), t(c["Qg"] - c["Qload"]), t(c["Qload"])
+        nb = len(c["V0"])
+        V, th, P, Q = (torch.full((nb,), float("nan"), dtype=torch.float64, device=dev) for _ in range(4))
+        it = torch.full((n,), -1, dtype=torch.int32, device=dev)
+        st = torch.full((n,), -1, dtype=torch.int32, device=dev)
+        mm = torch.full((n,), float("nan"), dtype=torch.float64, device=dev)
+        noalloc.solve_noalloc(gi, V0.data_ptr(), th0.data_ptr(), Pliq.data_ptr(), Qliq.data_ptr(), Qload.data_ptr(),
+                              V.data_ptr(), th.data_ptr(), P.data_ptr(), Q.data_ptr(), it.data_ptr(), st.data_ptr(),
+                              mm.data_ptr(), stream=stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        np.testing.assert_array_equal(it.cpu().numpy(), ref["iterations"])
+        np.testing.assert_array_equal(st.cpu().numpy(), ref["status"])
+        assert np.max(np.abs(V.cpu().numpy() - ref["V"])) <= 1e-12
+        assert np.max(np.abs(th.cpu().numpy() - ref["theta"])) <= 1e-12
+        assert np.max(np.abs(P.cpu().numpy() - ref["Pcalc"])) <= 1e-10
+        np.testing.assert_allclose(mm.cpu().numpy(), ref["final_mismatch"], rtol=1e-6, atol=1e-14)
+        assert np.all(mm.cpu().numpy() <= 1e-8)
+
+
+def test_noalloc_rejects_too_many_instances(gb):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device visible to torch")
+    grid = gb.read_grid(os.path.join(GOLDEN, "c1.cdf"))
+    b = gb.Batch([grid], tolerancia=1e-8, no_max_iter=100)
+    x = torch.zeros(16, dtype=torch.float64, device="cuda")
+    n = 600000  # metadata alone exceeds the static scratch
+    with pytest.raises(gb.GbpfError) as e:
+        b.solve_noalloc(np.zeros(n, np.int32), *([x.data_ptr()] * 9), x.data_ptr(), x.data_ptr(), x.data_ptr())
+    assert e.value.status == gb.E_ARG
+    assert "static scratch" in str(e.value)
