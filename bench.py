@@ -1,23 +1,28 @@
 #!/usr/bin/env python3
 """Benchmark: converged Newton-Raphson power-flow solves per second on one GB300.
 
-Workloads (seeded synthetic grids of the named shapes, generated in process):
-  c2   118-bus meshed grid (1 slack, 53 PV, 64 PQ, 186 branches), reactive
-       limits on, tolerance 1e-8 p.u., plain FP64 -- the default
-  c1   14-bus ring-plus-chords grid, limits off
-  c3   15,104-bus grid (128 tied copies of the 118-bus grid), limits on
-A step is one solve of the grid from its flat start.  `value` is solves/s with
-the inputs resident in device memory (one CUDA-graph launch per solve, CUDA
-events on the solver stream); `e2e` is the same through the public API with
-host buffers: host->device copy of the start state and injections, the solve,
-device->host copy of |V| and theta, every step.
+Workload c2 (default): the seeded synthetic 118-bus meshed grid (1 slack, 53 PV,
+64 PQ, 177 lines + 9 transformers), 4,096 load scenarios (per-bus load x
+lognormal(sigma 0.1), generator P x U(0.9, 1.1)), reactive limits on, flat start,
+tolerance 1e-8 p.u., no_max_iter 100.  A step solves all 4,096 scenarios.
+  value    batched, FP32 LU + FP64 mismatch/test/update, inputs resident in
+           device memory; one graph launch per step, CUDA events on the batch
+           stream; counts converged scenarios only
+  e2e      the same through the public API with host buffers: host->device copy
+           of every scenario's injections and start, the solve, device->host copy
+           of |V|, theta, iterations and status, every step
+  config   also reports the plain FP64 form (one scenario per gbpf_solve, the
+           oracle-matching path) and batched FP64 on the same scenarios
+Other workloads: c2-plain (one FP64 solve of the grid per step), c3 (the
+15,104-bus grid, one FP64 solve per step), c4 (4,096 instances of 14..472-bus
+grids, batched FP32).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2]
-  python bench.py --impl reference ...   (the CPU restatement of the reference
-                                          path on all host cores)
-Multi-GPU: one process per GPU under torch.distributed.run; a single grid does
-not shard (the LU has one elimination order), so every rank solves its own
-replica and `value` is the sum over ranks ("replicas only").
+  python bench.py --impl reference     the CPU restatement of the reference
+                                       path (oracle/) on every host core
+Multi-GPU (torch.distributed.run, one process per GPU): scenarios are sharded
+over ranks (weak scaling: every rank solves its own 4,096), no collective in
+the data path; a single grid does not shard, so c2-plain/c3 run replicas.
 """
 import argparse
 import importlib
@@ -27,7 +32,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -36,15 +40,17 @@ PKG = "experience-of-using-gpu-in-power-flow-computation_gb300"
 BASE_SEED = 20261203
 METRIC = "converged PF solves/s on 1 GB300 @ mismatch<=1e-8 pu"
 UNIT = "solves/s"
+N_SCEN = 4096
+L2_BYTES = 129 * 1024 * 1024
 
 
 def args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=200)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gbpf", choices=["gbpf", "reference"])
-    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3"])
+    p.add_argument("--workload", default="c2", choices=["c2", "c2-plain", "c3", "c4"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -53,27 +59,27 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
-def workload(gb, name):
-    """(grid, cdf path, limits flag, description)"""
-    if name == "c1":
-        g, lim, desc = gb.generate(1, BASE_SEED + 1), 0, "14-bus ring+chords, limits off"
-    elif name == "c3":
-        g, lim, desc = gb.generate(3, BASE_SEED + 3, tiles=128), 1, "15104-bus (128 tied 118-bus copies), limits on"
-    else:
-        g, lim, desc = gb.generate(2, BASE_SEED + 2), 1, "118-bus meshed (1 slack/53 PV/64 PQ, 186 branches), limits on"
+def write_grid(g):
     d = tempfile.mkdtemp(prefix="gbpf_bench_")
     path = os.path.join(d, "grid.cdfx" if g.nB > 9999 else "grid.cdf")
     g.write_cdf(path)
-    return gb.read_grid(path), path, lim, desc
+    return path
+
+
+def scenarios(np, base, n, seed):
+    """Per-bus load x lognormal(sigma 0.1), generation x U(0.9, 1.1)."""
+    rng = np.random.default_rng(seed)
+    nb = len(base["Pload"])
+    lf = np.exp(rng.normal(-0.005, 0.1, (n, nb)))
+    gf = rng.uniform(0.9, 1.1, (n, nb))
+    return base["Pload"] * lf, base["Qload"] * lf, base["Pg"] * gf
 
 
 class Clocks:
     """nvidia-smi samples during the timed region."""
 
     def __init__(self, device):
-        self.device = device
-        self.proc = None
-        self.out = None
+        self.device, self.proc, self.out = device, None, None
 
     def __enter__(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -84,6 +90,7 @@ class Clocks:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=self.out, stderr=subprocess.DEVNULL)
+            time.sleep(0.5)
         except Exception:
             self.proc = None
         return self
@@ -110,77 +117,329 @@ class Clocks:
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
         sm = [int(r[1]) for r in rows]
-        reasons = set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
-            for n, v in zip(names, r[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": int(rows[0][2]), "reasons": sorted(reasons),
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": int(rows[0][2]), "reasons": reasons,
                 "samples": len(rows)}
 
 
-def cpu_baseline(cdf, lim, target_s=12.0):
-    """The oracle (CPU restatement of the reference path, single thread) on a
-    bounded sample of the same workload: repeated solves of the same grid."""
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return json.load(open(p))["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------- CPU
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
+    oracle.lib()
+    return oracle
+
+
+def _oracle_shard(task):
+    """Worker: solve scenarios [a, b) with the oracle; returns converged count."""
+    cdf, lo, hi, seed, lim, nreps = task
+    import numpy as np
+
+    oracle = _oracle()
+    og = oracle.Grid(cdf)
+    base = dict(Pload=og.Pload.copy(), Qload=og.Qload.copy(), Pg=og.Pg.copy())
+    Pl, Ql, Pg = scenarios(np, base, hi, seed)
+    conv = 0
+    for _ in range(nreps):
+        for i in range(lo, hi):
+            og.set_bus(Pload=Pl[i], Qload=Ql[i], Pg=Pg[i])
+            conv += og.solve(1e-8, 100, bool(lim))["converged"]
+    return conv
+
+
+def cpu_baseline_scenarios(cdf, lim, seed, target_s=12.0):
+    """The oracle on one host core over a bounded sample of the scenarios."""
+    t0 = time.perf_counter()
+    probe = _oracle_shard((cdf, 0, 64, seed, lim, 1))
+    dt = time.perf_counter() - t0
+    n = max(64, min(N_SCEN, int(64 * target_s / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    conv = _oracle_shard((cdf, 0, n, seed, lim, 1))
+    dt = time.perf_counter() - t0
+    return {"value": conv / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"first {n} of the {N_SCEN} scenarios, {conv} converged, {dt:.1f} s single-threaded "
+                      f"oracle (oracle/pf_oracle.c via ctypes)"}
+
+
+def cpu_baseline_repeat(cdf, lim, target_s=12.0):
+    oracle = _oracle()
     if not os.path.exists(oracle.CLI_PATH):
         oracle.build()
-    probe = json.loads(subprocess.run([oracle.CLI_PATH, cdf, "--lim", str(lim), "--repeat", "3"],
+    probe = json.loads(subprocess.run([oracle.CLI_PATH, cdf, "--lim", str(lim), "--repeat", "2"],
                                       capture_output=True, text=True, check=True).stdout)
-    reps = max(3, int(target_s / max(probe["solve_s"], 1e-6)))
+    reps = max(2, int(target_s / max(probe["solve_s"], 1e-6)))
     r = json.loads(subprocess.run([oracle.CLI_PATH, cdf, "--lim", str(lim), "--repeat", str(reps)],
                                   capture_output=True, text=True, check=True).stdout)
     return {"value": 1.0 / r["solve_s"], "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{reps} repeated solves of the same grid ({r['iterations']} iterations each), "
+            "sample": f"{reps} solves of the grid ({r['iterations']} iterations each), "
                       f"{reps * r['solve_s']:.1f} s single-threaded oracle/pforacle"}
 
 
 def run_reference(a):
     """--impl reference: the reference path restated in C (oracle/) on every
-    host core (one single-threaded process per core), same grid and metric.
-    The reference's own executables need MKL or a CUDA 10-era library set, so
-    the restatement stands in for them."""
+    host core, the same scenarios and metric.  The reference's own executables
+    need MKL (absent here, and not available for the Arm host) or cuSPARSE
+    calls removed from CUDA 12+, so the restatement stands in for them."""
     rank, _, world = dist_env()
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
+    import multiprocessing as mp
+    import numpy as np
 
-    if not os.path.exists(oracle.CLI_PATH):
-        oracle.build()
     gb = importlib.import_module(PKG)
-    grid, cdf, lim, desc = workload(gb, a.workload)
+    lim = 1
+    if a.workload in ("c2", "c4"):
+        g = gb.generate(2, BASE_SEED + 2)
+        desc = "118-bus synthetic, 4096 load scenarios, limits on"
+    elif a.workload == "c3":
+        g, lim, desc = gb.generate(3, BASE_SEED + 3, tiles=128), 1, "15104-bus synthetic, limits on"
+    else:
+        g, desc = gb.generate(2, BASE_SEED + 2), "118-bus synthetic, limits on"
+    cdf = write_grid(g)
     cores = os.cpu_count() or 1
-    probe = json.loads(subprocess.run([oracle.CLI_PATH, cdf, "--lim", str(lim), "--repeat", "2"],
-                                      capture_output=True, text=True, check=True).stdout)
-    reps = max(1, int(1.0 / max(probe["solve_s"], 1e-6)))  # about one second per process per step
-
-    def step():
+    steps = min(a.steps, 5)
+    warm = min(a.warmup, 3)
+    if a.workload in ("c2", "c4"):
+        per = (N_SCEN + cores - 1) // cores
+        tasks = [(cdf, i * per, min(N_SCEN, (i + 1) * per), BASE_SEED + 7, lim, 1) for i in range(cores)]
+        tasks = [t for t in tasks if t[1] < t[2]]
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(len(tasks)) as pool:
+            for _ in range(warm):
+                pool.map(_oracle_shard, tasks)
+            t0 = time.perf_counter()
+            conv = 0
+            for _ in range(steps):
+                conv += sum(pool.map(_oracle_shard, tasks))
+            dt = time.perf_counter() - t0
+        value = conv / dt
+        sample = f"each step: all {N_SCEN} scenarios over {len(tasks)} processes (one per core)"
+    else:
+        oracle = _oracle()
+        probe = json.loads(subprocess.run([oracle.CLI_PATH, cdf, "--lim", str(lim), "--repeat", "2"],
+                                          capture_output=True, text=True, check=True).stdout)
+        reps = max(1, int(1.0 / max(probe["solve_s"], 1e-6)))
+        def step():
+            ps = [subprocess.Popen([oracle.CLI_PATH, cdf, "--lim", str(lim), "--repeat", str(reps)],
+                                   stdout=subprocess.PIPE, text=True) for _ in range(cores)]
+            for p in ps:
+                p.communicate()
+        for _ in range(warm):
+            step()
         t0 = time.perf_counter()
-        ps = [subprocess.Popen([oracle.CLI_PATH, cdf, "--lim", str(lim), "--repeat", str(reps)],
-                               stdout=subprocess.PIPE, text=True) for _ in range(cores)]
-        for p in ps:
-            p.communicate()
-        return time.perf_counter() - t0
-
-    for _ in range(min(a.warmup, 3)):
-        step()
-    steps = min(a.steps, 10)
-    total = sum(step() for _ in range(steps))
-    value = steps * cores * reps / total
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": steps,
-            "warmup": min(a.warmup, 3), "ms_per_step": 1e3 * total / steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": a.workload, "grid": desc, "nB": grid.nB, "tolerance": 1e-8,
-                       "lim_inj_reat": lim},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"each step: {cores} processes x {reps} solves of the grid"},
+        for _ in range(steps):
+            step()
+        dt = time.perf_counter() - t0
+        value = steps * cores * reps / dt
+        sample = f"each step: {cores} processes x {reps} solves of the grid"
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": steps, "warmup": warm,
+            "ms_per_step": 1e3 * dt / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": a.workload, "grid": desc, "nB": g.nB, "tolerance": 1e-8, "lim_inj_reat": lim},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------- GPU
+def max_over_ranks(x, dist, device):
+    if not dist:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, dist, device):
+    if not dist:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def bench_batch(a, gb, np, rank, dev, world, dist):
+    if a.workload == "c4":
+        sizes = [14, 30, 57, 118, 236, 472]
+        grids = [gb.generate(4, BASE_SEED + 4 + 1000 * i, nbus=nb) for i, nb in enumerate(sizes)]
+        rng = np.random.default_rng(BASE_SEED + 4 + 97 * rank)
+        gi = rng.integers(0, len(grids), N_SCEN).astype(np.int32)
+        cols = {k: [] for k in ("Pload", "Qload", "Pg")}
+        for t in gi:
+            b = grids[t].buses()
+            lf = np.exp(rng.normal(-0.005, 0.1, grids[t].nB))
+            cols["Pload"].append(b["Pload"] * lf)
+            cols["Qload"].append(b["Qload"] * lf)
+            cols["Pg"].append(b["Pg"] * rng.uniform(0.9, 1.1, grids[t].nB))
+        Pl, Ql, Pg = (np.concatenate(cols[k]) for k in ("Pload", "Qload", "Pg"))
+        desc = "4096 instances of 14/30/57/118/236/472-bus synthetic grids, load x lognormal(0.1), Pg x U(0.9,1.1)"
+        cdf = None
+    else:
+        g0 = gb.generate(2, BASE_SEED + 2)
+        cdf = write_grid(g0)
+        grids = [gb.read_grid(cdf)]
+        base = grids[0].buses()
+        Pl, Ql, Pg = scenarios(np, base, N_SCEN, BASE_SEED + 7 + 1000 * rank)
+        Pl, Ql, Pg = Pl.ravel(), Ql.ravel(), Pg.ravel()
+        gi = np.zeros(N_SCEN, np.int32)
+        desc = "118-bus synthetic meshed grid (1 slack/53 PV/64 PQ, 186 branches), 4096 load scenarios"
+    opts = dict(tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1)
+    fast = gb.Batch(grids, device=dev, precision=gb.PREC_FP32_IR, **opts)
+    fast.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
+    fast.solve()
+    r = fast.results(state=False)
+    conv = int((r["status"] == 0).sum())
+    assert np.all(r["final_mismatch"][r["status"] == 0] <= 1e-8)
+    # device-resident: CUDA events on the batch stream
+    fast.time(max(3, a.warmup))
+    if dist:
+        dist.barrier()
+    with Clocks(dev) as clk:
+        ms = fast.time(a.steps)
+    if dist:
+        dist.barrier()
+    t_dev = max_over_ranks(ms / 1e3, dist, dev)
+    total_conv = sum_over_ranks(conv, dist, dev)
+    value = total_conv * a.steps / t_dev
+    # end to end: host buffers through the API every step
+    nb = len(Pl)
+    for _ in range(max(3, a.warmup)):
+        fast.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
+        fast.solve()
+        fast.results(state=True)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        fast.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
+        fast.solve()
+        res = fast.results(state=True)
+    t_e2e = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    e2e = total_conv * a.steps / t_e2e
+    # the plain FP64 form (one scenario per gbpf_solve) and batched FP64, same scenarios
+    plain = None
+    if cdf is not None:
+        s = gb.Solver(grids[0], device=dev, tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1, metodo=0)
+        base = grids[0].buses()
+        n_plain = 256
+        Pl2, Ql2, Pg2 = Pl.reshape(N_SCEN, -1), Ql.reshape(N_SCEN, -1), Pg.reshape(N_SCEN, -1)
+        nconv = 0
+        t0 = time.perf_counter()
+        for i in range(n_plain):
+            s.set_start(Pliq=Pg2[i] - Pl2[i], Qliq=base["Qg"] - Ql2[i])
+            nconv += s.solve(full=False)["converged"]
+        plain = nconv / (time.perf_counter() - t0)
+    slow = gb.Batch(grids, device=dev, precision=gb.PREC_FP64, **opts)
+    slow.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
+    slow.solve()
+    rs = slow.results(state=False)
+    ms64 = slow.time(max(3, a.steps // 4)) / max(3, a.steps // 4)
+    batched64 = int((rs["status"] == 0).sum()) / (ms64 / 1e3)
+    info = fast.info()
+    peak, src = peak_hbm()
+    # algorithmic bytes of one batch launch: inputs (V0, theta0, Pliq, Qliq, Qload),
+    # outputs (V, theta, P, Q) and per-instance results; topology blobs counted once
+    bytes_launch = nb * 8 * 5 + nb * 8 * 4 + N_SCEN * (4 * 3 + 8)
+    t_launch = ms / a.steps / 1e3
+    achieved = bytes_launch / t_launch / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": max(3, a.warmup), "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": a.workload, "grid": desc, "instances_per_gpu": N_SCEN, "tolerance": 1e-8,
+                   "no_max_iter": 100, "lim_inj_reat": 1,
+                   "form": "batched, FP32 LU + FP64 mismatch/test/update (learned warm start not built)",
+                   "converged_per_step": int(total_conv), "mean_iterations": float(np.mean(r["iterations"])),
+                   "max_iterations": int(np.max(r["iterations"])),
+                   "plain_fp64_solves_per_s": plain, "batched_fp64_solves_per_s": batched64,
+                   "speedup_vs_plain_fp64": (value / plain) if plain else None,
+                   "l2": f"inputs {nb * 8 * 9 / 2**20:.1f} MiB < L2; no flush (per-step inputs rewritten by the "
+                         f"e2e copy only)",
+                   "batch": info, "parallelism": f"scenarios sharded x{world}"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nb * 8 * 5 + N_SCEN * 12,
+                "d2h_bytes_per_step": nb * 8 * 4 + N_SCEN * 20},
+        "roofline": {"bound": "hbm", "kernel": "k_nr_warp/k_nr_block (one persistent launch)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src_note(src), "traffic": None,
+                     "note": "FP64-pipe and latency bound; state lives in shared memory"},
+        "clocks": clk.summary(),
+        "gpu_launches": a.steps * (1 + (1 if info["warp_instances"] else 0) +
+                                   (1 if info["warp_instances"] < N_SCEN else 0)),
+    }
+    if rank == 0 and not a.no_cpu_baseline and cdf is not None:
+        line["cpu_baseline"] = cpu_baseline_scenarios(cdf, 1, BASE_SEED + 7)
+    return line
+
+
+def peak_src_note(src):
+    return f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else "fallback 6.8 TB/s"
+
+
+def bench_single(a, gb, np, rank, dev, world, dist):
+    if a.workload == "c3":
+        g, desc = gb.generate(3, BASE_SEED + 3, tiles=128), "15104-bus (128 tied 118-bus copies), limits on"
+    else:
+        g, desc = gb.generate(2, BASE_SEED + 2), "118-bus meshed (1 slack/53 PV/64 PQ, 186 branches), limits on"
+    cdf = write_grid(g)
+    grid = gb.read_grid(cdf)
+    s = gb.Solver(grid, device=dev, tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1, metodo=0)
+    first = s.solve(full=False)
+    assert first["converged"] and first["final_mismatch"] <= 1e-8, first
+    info = s.info()
+    b = grid.buses()
+    V0, th0, Pliq, Qliq = b["V0"], b["theta0"], b["Pg"] - b["Pload"], b["Qg"] - b["Qload"]
+    s.time(max(3, a.warmup))
+    if dist:
+        dist.barrier()
+    with Clocks(dev) as clk:
+        ms = s.time(a.steps)
+    t_dev = max_over_ranks(ms / 1e3, dist, dev)
+    value = world * a.steps / t_dev
+    for _ in range(max(3, a.warmup)):
+        s.set_start(V0, th0, Pliq, Qliq)
+        s.solve(full=False)
+        s.state()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        s.set_start(V0, th0, Pliq, Qliq)
+        r = s.solve(full=False)
+        s.state()
+    t_e2e = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    prof = s.profile(10)
+    top = max(prof, key=lambda k: prof[k]["ms"])
+    peak, src = peak_hbm()
+    achieved = prof[top]["bytes"] / (prof[top]["ms"] * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": max(3, a.warmup), "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": a.workload, "grid": desc, "nB": grid.nB, "tolerance": 1e-8, "lim_inj_reat": 1,
+                   "form": "plain FP64, one solve per step", "iterations": first["iterations"],
+                   "solver": info, "parallelism": f"replicas x{world}",
+                   "l2": "working set fits in L2; no flush"},
+        "e2e": {"value": world * a.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * grid.nB * 8,
+                "d2h_bytes_per_step": 4 * grid.nB * 8 + 32},
+        "roofline": {"bound": "hbm", "kernel_phase": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src_note(src), "traffic": None, "phases": prof},
+        "clocks": clk.summary(),
+        "gpu_launches": a.steps * (6 + max(1, first["iterations"]) * info["kernels_per_iteration"] + 1),
+    }
+    if rank == 0 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_repeat(cdf, 1)
+    return line
 
 
 def main():
@@ -198,82 +457,12 @@ def main():
 
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     gb = importlib.import_module(PKG)
-    grid, cdf, lim, desc = workload(gb, a.workload)
-    s = gb.Solver(grid, device=local_rank, tolerancia=1e-8, no_max_iter=100, lim_inj_reat=lim, metodo=0)
-    first = s.solve(full=False)
-    assert first["converged"] and first["final_mismatch"] <= 1e-8, first
-    info = s.info()
-    buses = grid.buses()
-    V0, th0 = buses["V0"], buses["theta0"]
-    Pliq, Qliq = buses["Pg"] - buses["Pload"], buses["Qg"] - buses["Qload"]
-
-    def barrier():
-        if dist:
-            dist.barrier()
-
-    # device-resident: one graph launch per solve, CUDA events on the solver stream
-    s.time(max(3, a.warmup))
-    barrier()
-    with Clocks(local_rank) as clk:
-        ms = s.time(a.steps)
-    barrier()
-    t_dev = ms / 1e3
-    if dist:
-        import torch
-
-        t = torch.tensor([t_dev], dtype=torch.float64, device=f"cuda:{local_rank}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_dev = float(t.item())
-    value = world * a.steps / t_dev
-
-    # end to end through the public API with host buffers
-    for _ in range(max(3, a.warmup)):
-        s.set_start(V0, th0, Pliq, Qliq)
-        s.solve(full=False)
-        s.state()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(a.steps):
-        s.set_start(V0, th0, Pliq, Qliq)
-        r = s.solve(full=False)
-        st = s.state()
-    t_e2e = time.perf_counter() - t0
-    assert r["converged"]
-    e2e = world * a.steps / t_e2e
-
-    prof = s.profile(20)
-    top = max(prof, key=lambda k: prof[k]["ms"])
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(peaks_path):
-        peak, peak_src = json.load(open(peaks_path))["hbm_gbs"], "measured"
+    if a.workload in ("c2", "c4"):
+        line = bench_batch(a, gb, np, rank, local_rank, world, dist)
     else:
-        peak, peak_src = 6800.0, "fallback"
-    achieved = prof[top]["bytes"] / (prof[top]["ms"] * 1e-3) / 1e9
-    # prologue (reset, phasors, injections, [limits], mismatch, test) + one body
-    # pass per Newton update + branch flows
-    launches_per_solve = 5 + (1 if lim else 0) + max(1, first["iterations"]) * info["kernels_per_iteration"] + 1
-    if rank != 0:
-        return
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
-        "warmup": max(3, a.warmup), "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": a.workload, "grid": desc, "nB": grid.nB, "nL": grid.nL, "tolerance": 1e-8,
-                   "lim_inj_reat": lim, "form": "plain FP64 sparse, one solve per step",
-                   "iterations": first["iterations"], "switch_events": first["n_events"],
-                   "l2": "working set of a solve fits in L2; no flush between steps",
-                   "solver": info, "parallelism": f"replicas x{world}"},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * grid.nB * 8,
-                "d2h_bytes_per_step": 4 * grid.nB * 8 + 32},
-        "roofline": {"bound": "hbm", "kernel_phase": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
-                     "phases": prof},
-        "clocks": clk.summary(),
-        "gpu_launches": launches_per_solve * a.steps,
-    }
-    if not a.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(cdf, lim)
-    print(json.dumps(line), flush=True)
+        line = bench_single(a, gb, np, rank, local_rank, world, dist)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
 

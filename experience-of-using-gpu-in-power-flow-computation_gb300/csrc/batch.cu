@@ -816,6 +816,8 @@ struct gbpf_batch {
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
     DevBuf topo_na;          // topologies planned for gbpf_batch_solve_noalloc
+    void *h_in = nullptr, *h_out = nullptr;  // pinned mirrors of the input and output regions
+    size_t out_bytes = 0;
     size_t na_smem = 0, na_stride = 0;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
@@ -829,6 +831,8 @@ struct gbpf_batch {
         if (join) cudaEventDestroy(join);
         if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
+        if (h_in) cudaFreeHost(h_in);
+        if (h_out) cudaFreeHost(h_out);
     }
     gbpf_status add_topology(const Grid &g);
     gbpf_status set_instances(int n, const int *topo_of_inst, const double *Pload, const double *Qload,
@@ -920,18 +924,56 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
 
 gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Pload, const double *Qload,
                                       const double *Pg, const double *Qg, const double *V0, const double *th0) {
-    n_inst = n;
-    inst_topo.assign(tofi, tofi + n);
-    inst_off.resize(n);
-    long long off = 0;
-    for (int i = 0; i < n; i++) {
-        if (inst_topo[i] < 0 || inst_topo[i] >= (int)grids.size()) { set_error("instance names an unknown grid"); return GBPF_E_ARG; }
-        inst_off[i] = off;
-        off += grids[inst_topo[i]].nB;
+    for (int i = 0; i < n; i++)
+        if (tofi[i] < 0 || tofi[i] >= (int)grids.size()) { set_error("instance names an unknown grid"); return GBPF_E_ARG; }
+    // the previous copies out of the pinned staging buffers must be complete
+    CK(cudaStreamSynchronize(stream));
+    const bool same = exec && n == n_inst && std::equal(tofi, tofi + n, inst_topo.begin());
+    if (!same) {
+        n_inst = n;
+        inst_topo.assign(tofi, tofi + n);
+        inst_off.resize(n);
+        long long off = 0;
+        for (int i = 0; i < n; i++) {
+            inst_off[i] = off;
+            off += grids[inst_topo[i]].nB;
+        }
+        n_bus_total = off;
     }
-    n_bus_total = off;
-    // inputs: V0, th0, Pliq, Qliq, Qload (packed); outputs: V, th, P, Q + per-instance results
-    std::vector<double> hV(off), hT(off), hP(off), hQ(off), hQl(off);
+    const size_t nb = (size_t)n_bus_total * 8, nba = align_up(nb, 256);
+    if (!same) {
+        // inputs: V0, th0, Pliq, Qliq, Qload (packed, one region with a pinned
+        // mirror); outputs: V, th, P, Q + per-instance results (pinned mirror)
+        inst_mem.reset();
+        out_mem.reset();
+        if (h_in) { cudaFreeHost(h_in); h_in = nullptr; }
+        if (h_out) { cudaFreeHost(h_out); h_out = nullptr; }
+        const size_t in_bytes = 5 * nba + align_up(4 * (size_t)n, 256) + align_up(8 * (size_t)n, 256);
+        CK(cudaMalloc(&inst_mem.p, in_bytes));
+        char *bb = (char *)inst_mem.p;
+        size_t o = 0;
+        auto take = [&](size_t bytes) { char *r = bb + o; o += align_up(bytes, 256); return r; };
+        args.V0 = (double *)take(nb); args.th0 = (double *)take(nb); args.Pliq = (double *)take(nb);
+        args.Qliq = (double *)take(nb); args.Qload = (double *)take(nb);
+        args.inst_topo = (int *)take(4 * (size_t)n);
+        args.inst_off = (long long *)take(8 * (size_t)n);
+        CK(cudaMemcpyAsync((void *)args.inst_topo, inst_topo.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync((void *)args.inst_off, inst_off.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, stream));
+        out_bytes = 4 * nba + 3 * align_up(4 * (size_t)n, 256) + align_up(8 * (size_t)n, 256);
+        const size_t ev_bytes = align_up(16 * (size_t)n * ev_cap, 256);
+        CK(cudaMalloc(&out_mem.p, out_bytes + ev_bytes));
+        bb = (char *)out_mem.p;
+        o = 0;
+        args.V = (double *)take(nb); args.th = (double *)take(nb); args.P = (double *)take(nb); args.Q = (double *)take(nb);
+        args.iters = (int *)take(4 * (size_t)n); args.status = (int *)take(4 * (size_t)n);
+        args.n_events = (int *)take(4 * (size_t)n); args.mism = (double *)take(8 * (size_t)n);
+        args.events = (int *)take(16 * (size_t)n * ev_cap);
+        args.n_inst = n;
+        CK(cudaMallocHost(&h_in, 5 * nba));
+        CK(cudaMallocHost(&h_out, out_bytes));
+    }
+    double *hV = (double *)h_in, *hT = (double *)((char *)h_in + nba), *hP = (double *)((char *)h_in + 2 * nba),
+           *hQ = (double *)((char *)h_in + 3 * nba), *hQl = (double *)((char *)h_in + 4 * nba);
     for (int i = 0; i < n; i++) {
         const Grid &g = grids[inst_topo[i]];
         const long long o = inst_off[i];
@@ -945,35 +987,9 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
             hQl[o + k] = ql;
         }
     }
-    inst_mem.reset();
-    out_mem.reset();
-    const size_t nb = (size_t)off * 8;
-    const size_t in_bytes = 5 * align_up(nb, 256) + align_up(4 * (size_t)n, 256) + align_up(8 * (size_t)n, 256);
-    CK(cudaMalloc(&inst_mem.p, in_bytes));
-    char *b = (char *)inst_mem.p;
-    size_t o = 0;
-    auto take = [&](size_t bytes) { char *r = b + o; o += align_up(bytes, 256); return r; };
-    args.V0 = (double *)take(nb); args.th0 = (double *)take(nb); args.Pliq = (double *)take(nb);
-    args.Qliq = (double *)take(nb); args.Qload = (double *)take(nb);
-    args.inst_topo = (int *)take(4 * (size_t)n);
-    args.inst_off = (long long *)take(8 * (size_t)n);
-    CK(cudaMemcpyAsync((void *)args.V0, hV.data(), nb, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync((void *)args.th0, hT.data(), nb, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync((void *)args.Pliq, hP.data(), nb, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync((void *)args.Qliq, hQ.data(), nb, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync((void *)args.Qload, hQl.data(), nb, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync((void *)args.inst_topo, inst_topo.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync((void *)args.inst_off, inst_off.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, stream));
-    const size_t out_bytes = 4 * align_up(nb, 256) + 3 * align_up(4 * (size_t)n, 256) + align_up(8 * (size_t)n, 256) +
-                             align_up(16 * (size_t)n * ev_cap, 256);
-    CK(cudaMalloc(&out_mem.p, out_bytes));
-    b = (char *)out_mem.p;
-    o = 0;
-    args.V = (double *)take(nb); args.th = (double *)take(nb); args.P = (double *)take(nb); args.Q = (double *)take(nb);
-    args.iters = (int *)take(4 * (size_t)n); args.status = (int *)take(4 * (size_t)n);
-    args.n_events = (int *)take(4 * (size_t)n); args.mism = (double *)take(8 * (size_t)n);
-    args.events = (int *)take(16 * (size_t)n * ev_cap);
-    args.n_inst = n;
+    // one host->device copy of the whole input region
+    CK(cudaMemcpyAsync((void *)args.V0, h_in, 5 * nba, cudaMemcpyHostToDevice, stream));
+    if (same) return GBPF_OK;
     CK(cudaStreamSynchronize(stream));
     if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
     if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
@@ -1280,18 +1296,26 @@ extern "C" gbpf_status gbpf_batch_time(gbpf_batch *b, int repeats, double *ms_to
 
 extern "C" gbpf_status gbpf_batch_results(gbpf_batch *b, int *iterations, int *status, double *final_mismatch,
                                           int *n_events, double *V, double *theta, double *Pcalc, double *Qcalc) {
-    ARGCHECK(b && b->n_inst > 0);
+    ARGCHECK(b && b->n_inst > 0 && b->h_out);
     CK(cudaSetDevice(b->device));
     const size_t n = b->n_inst, nb = (size_t)b->n_bus_total * 8;
-    if (iterations) CK(cudaMemcpyAsync(iterations, b->args.iters, 4 * n, cudaMemcpyDeviceToHost, b->stream));
-    if (status) CK(cudaMemcpyAsync(status, b->args.status, 4 * n, cudaMemcpyDeviceToHost, b->stream));
-    if (final_mismatch) CK(cudaMemcpyAsync(final_mismatch, b->args.mism, 8 * n, cudaMemcpyDeviceToHost, b->stream));
-    if (n_events) CK(cudaMemcpyAsync(n_events, b->args.n_events, 4 * n, cudaMemcpyDeviceToHost, b->stream));
-    if (V) CK(cudaMemcpyAsync(V, b->args.V, nb, cudaMemcpyDeviceToHost, b->stream));
-    if (theta) CK(cudaMemcpyAsync(theta, b->args.th, nb, cudaMemcpyDeviceToHost, b->stream));
-    if (Pcalc) CK(cudaMemcpyAsync(Pcalc, b->args.P, nb, cudaMemcpyDeviceToHost, b->stream));
-    if (Qcalc) CK(cudaMemcpyAsync(Qcalc, b->args.Q, nb, cudaMemcpyDeviceToHost, b->stream));
+    const bool state = V || theta || Pcalc || Qcalc;
+    // one device->host copy into the pinned mirror: the whole output region,
+    // or only its per-instance tail when no state is wanted
+    const char *dev = (const char *)b->out_mem.p;
+    const size_t tail = (const char *)b->args.iters - dev;
+    if (state) CK(cudaMemcpyAsync(b->h_out, dev, b->out_bytes, cudaMemcpyDeviceToHost, b->stream));
+    else CK(cudaMemcpyAsync((char *)b->h_out + tail, dev + tail, b->out_bytes - tail, cudaMemcpyDeviceToHost, b->stream));
     CK(cudaStreamSynchronize(b->stream));
+    auto host = [&](const void *d) { return (const char *)b->h_out + ((const char *)d - dev); };
+    if (iterations) std::memcpy(iterations, host(b->args.iters), 4 * n);
+    if (status) std::memcpy(status, host(b->args.status), 4 * n);
+    if (final_mismatch) std::memcpy(final_mismatch, host(b->args.mism), 8 * n);
+    if (n_events) std::memcpy(n_events, host(b->args.n_events), 4 * n);
+    if (V) std::memcpy(V, host(b->args.V), nb);
+    if (theta) std::memcpy(theta, host(b->args.th), nb);
+    if (Pcalc) std::memcpy(Pcalc, host(b->args.P), nb);
+    if (Qcalc) std::memcpy(Qcalc, host(b->args.Q), nb);
     return GBPF_OK;
 }
 

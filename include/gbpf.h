@@ -273,7 +273,10 @@ void gbpf_batch_free(gbpf_batch *b);
 
 /* Instances: grid_of_inst[i] picks the topology of instance i; the bus arrays
  * are packed in instance order (instance i occupies nB of its grid entries)
- * and may be NULL (= the grid's own values).  Copies to the device. */
+ * and may be NULL (= the grid's own values).  The arrays are packed into a
+ * pinned staging buffer and copied to the device in one transfer (the caller
+ * may reuse them on return).  Calling again with the same grid_of_inst only
+ * replaces the inputs; a different list re-plans the launch. */
 gbpf_status gbpf_batch_set_instances(gbpf_batch *b, int n_inst, const int *grid_of_inst,
                                      const double *Pload, const double *Qload, const double *Pg,
                                      const double *Qg, const double *V0, const double *theta0);
