@@ -39,6 +39,9 @@ EXPORTS = [
     "gbpf_eval_jacobian", "gbpf_newton_step", "gbpf_device_info", "gbpf_last_error", "gbpf_status_str",
     "gbpf_batch_create", "gbpf_batch_free", "gbpf_batch_set_instances", "gbpf_batch_solve", "gbpf_batch_time",
     "gbpf_batch_results", "gbpf_batch_events", "gbpf_batch_info", "gbpf_batch_solve_noalloc",
+    "gbpf_mlp_create", "gbpf_mlp_free", "gbpf_mlp_dims", "gbpf_mlp_set_data", "gbpf_mlp_train", "gbpf_mlp_predict",
+    "gbpf_mlp_gradients", "gbpf_mlp_params", "gbpf_mlp_set_params", "gbpf_mlp_norm", "gbpf_mlp_set_norm",
+    "gbpf_batch_solve_warm", "gbpf_mlp_set_loss_metric",
 ]
 
 
@@ -93,6 +96,7 @@ def lib():
         L.gbpf_grid_free.restype = None
         L.gbpf_solver_free.restype = None
         L.gbpf_batch_free.restype = None
+        L.gbpf_mlp_free.restype = None
         _lib = L
     return _lib
 
@@ -510,5 +514,156 @@ class Batch:
             vp(Pcalc), vp(Qcalc), vp(iterations), vp(status), vp(final_mismatch), vp(stream)),
             "gbpf_batch_solve_noalloc")
 
+    def solve_warm(self, mlp):
+        """gbpf_batch_solve_warm: Newton from the network's predicted start
+        (flat-start fallback).  Returns start_kind (0 own start, 1 predicted
+        start converged, 2 predicted start failed and was replaced),
+        warm_iterations and the device time in ms."""
+        kind = np.zeros(self.n_inst, np.int32)
+        wit = np.zeros(self.n_inst, np.int32)
+        ms = ctypes.c_double()
+        _check(lib().gbpf_batch_solve_warm(self.h, mlp.h, _p(kind), _p(wit), ctypes.byref(ms)),
+               "gbpf_batch_solve_warm")
+        return dict(start_kind=kind, warm_iterations=wit, ms=ms.value)
+
     def slice(self, arr, inst):
         return arr[self.offsets[inst]:self.offsets[inst + 1]]
+
+
+# ---------------------------------------------------------------- warm start
+def warm_features(Pliq, Qliq, V0):
+    """Network features of scenarios of one grid: rows [Pliq | Qliq | V0]
+    (arrays [n, nB] or [nB])."""
+    return np.concatenate([np.atleast_2d(Pliq), np.atleast_2d(Qliq), np.atleast_2d(V0)], axis=1).astype(np.float32)
+
+
+def warm_targets(V, theta):
+    """Network outputs of solved scenarios: rows [|V| | theta]."""
+    return np.concatenate([np.atleast_2d(V), np.atleast_2d(theta)], axis=1).astype(np.float32)
+
+
+def warm_loss_metric(solver, V, theta, out_scale):
+    """A for MLP.set_loss_metric: S J0^T with J0 the Newton Jacobian at
+    (V, theta) (a typical solution, e.g. the mean of the training targets)
+    and S taking normalised outputs [|V| | theta] (scaled by out_scale) to
+    J0's columns (theta of non-slack buses, |V| of PQ buses); scaled so that
+    |A|_F^2 = n_out.  e A is then the linearised mismatch of a start whose
+    normalised error is e."""
+    g = solver.grid
+    nB = g.nB
+    row, col, val = solver.eval_jacobian(V, theta)
+    types = g.buses()["type"]
+    ns = np.where(types != 3)[0]
+    pq = np.where(types <= 1)[0]
+    dim = len(ns) + len(pq)
+    out_of_col = np.concatenate([nB + ns, pq])
+    scale = np.asarray(out_scale, np.float64)[out_of_col]
+    J = np.zeros((dim, dim))
+    np.add.at(J, (row, col), val)
+    A = np.zeros((2 * nB, dim))
+    A[out_of_col] = scale[:, None] * J.T
+    A *= np.sqrt((2 * nB) / max(np.sum(A * A), 1e-300))
+    return A.astype(np.float32)
+
+
+class MLP:
+    """The warm-start network (gbpf_mlp_*): n_in -> n_layers x width (GELU) ->
+    n_out, trained on the GPU by the library's tensor-core kernels."""
+
+    def __init__(self, n_in, n_out, width=512, n_layers=3, skip=True, seed=0, device=0):
+        self.h = ctypes.c_void_p()
+        _check(lib().gbpf_mlp_create(int(n_in), int(width), int(n_layers), int(n_out), int(bool(skip)),
+                                     ctypes.c_ulonglong(seed), int(device), ctypes.byref(self.h)), "gbpf_mlp_create")
+        self.n_in, self.n_out, self.width, self.n_layers = int(n_in), int(n_out), int(width), int(n_layers)
+        self.skip = bool(skip)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gbpf_mlp_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def layer_shapes(self):
+        """(out, in) of every layer, the skip last when present."""
+        dims = [self.n_in] + [self.width] * self.n_layers + [self.n_out]
+        return [(dims[i + 1], dims[i]) for i in range(self.n_layers + 1)] + ([(self.n_out, self.n_in)] if self.skip else [])
+
+    def set_data(self, X, Y):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.ascontiguousarray(Y, np.float32)
+        _check(lib().gbpf_mlp_set_data(self.h, _p(X), _p(Y), len(X)), "gbpf_mlp_set_data")
+
+    def train(self, epochs, batch=256, lr=1e-3, lr_final=None, seed=0):
+        """Adam from lr, decaying along a cosine to lr_final (default: lr,
+        i.e. constant); returns (mean loss per epoch, device ms)."""
+        loss = np.zeros(max(1, epochs), np.float32)
+        ms = ctypes.c_double()
+        lf = lr if lr_final is None else lr_final
+        _check(lib().gbpf_mlp_train(self.h, int(epochs), int(batch), ctypes.c_float(lr), ctypes.c_float(lf),
+                                    ctypes.c_ulonglong(seed), _p(loss), ctypes.byref(ms)), "gbpf_mlp_train")
+        return loss[:epochs], ms.value
+
+    def set_loss_metric(self, A=None, lam=0.01):
+        """Loss (|e A|^2 + lam |e|^2) / (rows * n_out) on the normalised
+        residual e, A [n_out, k]; A None: mean squared error."""
+        Ac = None if A is None else np.ascontiguousarray(A, np.float32)
+        k = 0 if A is None else Ac.shape[1]
+        _check(lib().gbpf_mlp_set_loss_metric(self.h, _p(Ac), int(k), ctypes.c_float(lam)),
+               "gbpf_mlp_set_loss_metric")
+
+    def predict(self, X):
+        X = np.ascontiguousarray(np.atleast_2d(X), np.float32)
+        Y = np.zeros((len(X), self.n_out), np.float32)
+        _check(lib().gbpf_mlp_predict(self.h, _p(X), len(X), _p(Y)), "gbpf_mlp_predict")
+        return Y
+
+    def gradients(self, Xn, Yn):
+        """Loss and per-layer (dW, db) on normalised rows, without an update
+        (the skip, when present, last with db None)."""
+        Xn = np.ascontiguousarray(Xn, np.float32)
+        Yn = np.ascontiguousarray(Yn, np.float32)
+        shapes = self.layer_shapes()
+        nl = self.n_layers + 1
+        dW = np.zeros(sum(o * i for o, i in shapes), np.float32)
+        db = np.zeros(sum(o for o, _ in shapes[:nl]), np.float32)
+        loss = ctypes.c_float()
+        _check(lib().gbpf_mlp_gradients(self.h, _p(Xn), _p(Yn), len(Xn), ctypes.byref(loss), _p(dW), _p(db)),
+               "gbpf_mlp_gradients")
+        out, ow, ob = [], 0, 0
+        for l, (o, i) in enumerate(shapes):
+            out.append((dW[ow:ow + o * i].reshape(o, i), db[ob:ob + o] if l < nl else None))
+            ow += o * i
+            ob += o
+        return loss.value, out
+
+    def params(self):
+        """[(W, b)] of every layer; the skip, when present, last as (S, None)."""
+        out = []
+        nl = self.n_layers + 1
+        for l, (o, i) in enumerate(self.layer_shapes()):
+            W = np.zeros((o, i), np.float32)
+            b = np.zeros(o, np.float32) if l < nl else None
+            _check(lib().gbpf_mlp_params(self.h, l, _p(W), _p(b)), "gbpf_mlp_params")
+            out.append((W, b))
+        return out
+
+    def set_params(self, params):
+        for l, (W, b) in enumerate(params):
+            W = np.ascontiguousarray(W, np.float32)
+            b = None if b is None else np.ascontiguousarray(b, np.float32)
+            _check(lib().gbpf_mlp_set_params(self.h, l, _p(W), _p(b)), "gbpf_mlp_set_params")
+
+    def norm(self):
+        a, b = np.zeros(self.n_in, np.float32), np.zeros(self.n_in, np.float32)
+        c, d = np.zeros(self.n_out, np.float32), np.zeros(self.n_out, np.float32)
+        _check(lib().gbpf_mlp_norm(self.h, _p(a), _p(b), _p(c), _p(d)), "gbpf_mlp_norm")
+        return dict(in_mean=a, in_scale=b, out_mean=c, out_scale=d)
+
+    def set_norm(self, in_mean, in_scale, out_mean, out_scale):
+        arrs = [np.ascontiguousarray(x, np.float32) for x in (in_mean, in_scale, out_mean, out_scale)]
+        _check(lib().gbpf_mlp_set_norm(self.h, *[_p(x) for x in arrs]), "gbpf_mlp_set_norm")

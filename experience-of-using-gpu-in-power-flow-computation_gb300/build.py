@@ -22,7 +22,7 @@ CLI = os.path.join(LIB_DIR, "gbpf")
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CXX_UNITS = ["host_io.cpp", "symbolic.cpp", "capi_misc.cpp"]
-CU_UNITS = ["solver.cu", "batch.cu"]
+CU_UNITS = ["solver.cu", "batch.cu", "mlp.cu"]
 
 
 def _cuda_home():

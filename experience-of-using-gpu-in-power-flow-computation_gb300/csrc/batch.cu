@@ -28,6 +28,7 @@
 
 #include "blocks.cuh"
 #include "gbpf_internal.h"
+#include "mlp_internal.h"
 
 using gbpf::Grid;
 using gbpf::set_error;
@@ -739,6 +740,121 @@ __global__ void k_batch_stamps(const double *r, const double *x, const double *b
         }                                                                            \
     } while (0)
 
+// ---------------------------------------------------------------------------
+// learned warm start
+// ---------------------------------------------------------------------------
+// Network features of every instance, normalised, bf16: [Pliq | Qliq | V0]
+// over the instance's buses, zero padding up to kin.
+__global__ void k_ws_features(const double *Pliq, const double *Qliq, const double *V0, const long long *inst_off,
+                              int n_inst, int nB, int n_in, int kin, const float *mean, const float *iscale,
+                              __nv_bfloat16 *X) {
+    const long long total = (long long)n_inst * kin;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int inst = (int)(i / kin), c = (int)(i % kin);
+        const long long off = inst_off[inst];
+        float v = 0.f;
+        if (c < n_in) {
+            const double x = c < nB ? Pliq[off + c] : c < 2 * nB ? Qliq[off + c - nB] : V0[off + c - 2 * nB];
+            v = (float)((x - (double)mean[c]) * (double)iscale[c]);
+        }
+        X[i] = __float2bfloat16_rn(v);
+    }
+}
+
+// max |g| of the first Newton iteration at the phasors ef (e = V cos th,
+// f = V sin th) of one instance: P rows of the non-slack buses, Q rows of the
+// PQ buses, as the mismatch of k_nr_block / k_nr_warp at iteration 0.
+__device__ double ws_mismatch(const TopoView &G, int nB, const double2 *ef, const double *Pliq, const double *Qliq,
+                              int lane) {
+    double mx = 0;
+    for (int k = lane; k < nB; k += 32) {
+        const int ty = G.type[k];
+        if (ty == 3) continue;
+        double ir = 0, ii = 0;
+        for (int p = G.yptr[k]; p < G.yptr[k + 1]; p++) {
+            const double2 y = G.yval[p], u = ef[G.ycol[p]];
+            ir += y.x * u.x - y.y * u.y;
+            ii += y.x * u.y + y.y * u.x;
+        }
+        const double2 u = ef[k];
+        double t = fabs(Pliq[k] - (u.x * ir + u.y * ii));
+        if (ty == 0 || ty == 1) t = fmax(t, fabs(Qliq[k] - (u.y * ir - u.x * ii)));
+        if (t != t) t = INFINITY;
+        mx = fmax(mx, t);
+    }
+    return warp_max(mx);
+}
+
+// One warp per instance: the predicted start (|V| of the PQ buses and theta of
+// the non-slack buses from the network; the PV set points and the slack angle
+// from the instance's own start) is kept when its initial mismatch is below
+// that of the instance's own (flat) start; otherwise the own start is used.
+// Writes the chosen start to sV/sTh and kind[inst] = 1 (predicted) or 0.
+__global__ void k_ws_select(Args a, const float *pred, int ldp, const float *omean, const float *oscale, double *sV,
+                            double *sTh, double2 *ef, int *kind) {
+    const int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (inst >= a.n_inst) return;
+    const Topo T = a.topo[a.inst_topo[inst]];
+    const TopoView G = bind(T.o, T.blob);
+    const long long off = a.inst_off[inst];
+    const int nB = T.nB;
+    const float *pr = pred + (size_t)inst * ldp;
+    for (int k = lane; k < nB; k += 32) {
+        const int ty = G.type[k];
+        const double v = (ty == 0 || ty == 1) ? (double)pr[k] * oscale[k] + omean[k] : a.V0[off + k];
+        const double t = ty == 3 ? a.th0[off + k] : (double)pr[nB + k] * oscale[nB + k] + omean[nB + k];
+        sV[off + k] = v;
+        sTh[off + k] = t;
+        double s, c;
+        sincos(t, &s, &c);
+        ef[off + k] = make_double2(v * c, v * s);
+    }
+    __syncwarp();
+    const double mc = ws_mismatch(G, nB, ef + off, a.Pliq + off, a.Qliq + off, lane);
+    __syncwarp();
+    for (int k = lane; k < nB; k += 32) {
+        double s, c;
+        sincos(a.th0[off + k], &s, &c);
+        ef[off + k] = make_double2(a.V0[off + k] * c, a.V0[off + k] * s);
+    }
+    __syncwarp();
+    const double mf = ws_mismatch(G, nB, ef + off, a.Pliq + off, a.Qliq + off, lane);
+    const bool use = mc < mf;
+    if (!use)
+        for (int k = lane; k < nB; k += 32) {
+            sV[off + k] = a.V0[off + k];
+            sTh[off + k] = a.th0[off + k];
+        }
+    if (lane == 0) kind[inst] = use ? 1 : 0;
+}
+
+// A converged instance that started from the prediction is rejected (kind 3,
+// solved again from its own start) when its |V| lies far from the predicted
+// start: Newton from a poor start can land on another solution of the
+// power-flow equations (a low-voltage one), which the flat start avoids.
+// Angles are not compared: a smooth angle offset in the prediction is cheap
+// for Newton to remove and does not signal another solution.
+constexpr double kWarmMaxDV = 0.05;
+// Iterations a predicted start gets before it counts as failed: a start good
+// enough to be chosen converges in a handful, and a failing one would
+// otherwise hold its block for no_max_iter iterations before the fallback.
+constexpr int kWarmMaxIter = 10;
+__global__ void k_ws_check(Args a, const double *sV, int *kind) {
+    const int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (inst >= a.n_inst || kind[inst] != 1) return;
+    const Topo T = a.topo[a.inst_topo[inst]];
+    const TopoView G = bind(T.o, T.blob);
+    const long long off = a.inst_off[inst];
+    double dv = 0;
+    for (int k = lane; k < T.nB; k += 32) {
+        const int ty = G.type[k];
+        if (ty == 0 || ty == 1) dv = fmax(dv, fabs(a.V[off + k] - sV[off + k]));
+    }
+    dv = warp_max(dv);
+    if (lane == 0 && !(dv <= kWarmMaxDV)) kind[inst] = 3;
+}
+
 // Owning device allocation (movable, not copyable).
 struct DevBuf {
     void *p = nullptr;
@@ -837,8 +953,19 @@ struct gbpf_batch {
     gbpf_status add_topology(const Grid &g);
     gbpf_status set_instances(int n, const int *topo_of_inst, const double *Pload, const double *Qload,
                               const double *Pg, const double *Qg, const double *V0, const double *th0);
+    std::vector<int> topo_warp;  // per topology: served by k_nr_warp (1) or k_nr_block (0)
+    // learned warm start (solve_warm): features, prediction, chosen start, fallback queue
+    DevBuf warm_mem;
+    int warm_n = 0;
+    __nv_bfloat16 *wX = nullptr;
+    float *wPred = nullptr;
+    double *wV = nullptr, *wTh = nullptr;
+    double2 *wEF = nullptr;
+    int *wKind = nullptr, *wQueue = nullptr;
     gbpf_status launch(cudaStream_t st);
+    gbpf_status launch_with(cudaStream_t st, const Args &ba, const Args &wa);
     gbpf_status build_graph();
+    gbpf_status solve_warm(gbpf_mlp *m, int *kind, int *warm_iters, float *ms);
 };
 
 gbpf_status gbpf_batch::add_topology(const Grid &g) {
@@ -996,22 +1123,25 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
     return build_graph();
 }
 
-gbpf_status gbpf_batch::launch(cudaStream_t st) {
+gbpf_status gbpf_batch::launch(cudaStream_t st) { return launch_with(st, args, wargs); }
+
+// One persistent launch per mode over the queues of ba (blocks) and wa (warps).
+gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args &wa) {
     const bool fp32 = precision == GBPF_PREC_FP32_IR;
     CK(cudaMemsetAsync(args.counter, 0, 2 * sizeof(int), st));
-    if (n_block_q) {
+    if (ba.queue_len) {
         CK(cudaEventRecord(fork, st));
         CK(cudaStreamWaitEvent(side, fork, 0));
-        if (fp32) k_nr_block<float><<<grid_blocks, kThreads, smem, side>>>(args);
-        else k_nr_block<double><<<grid_blocks, kThreads, smem, side>>>(args);
+        if (fp32) k_nr_block<float><<<grid_blocks, kThreads, smem, side>>>(ba);
+        else k_nr_block<double><<<grid_blocks, kThreads, smem, side>>>(ba);
         CK(cudaGetLastError());
     }
-    if (n_warp_q) {
-        if (fp32) k_nr_warp<float><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wargs);
-        else k_nr_warp<double><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wargs);
+    if (wa.queue_len) {
+        if (fp32) k_nr_warp<float><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wa);
+        else k_nr_warp<double><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wa);
         CK(cudaGetLastError());
     }
-    if (n_block_q) {
+    if (ba.queue_len) {
         CK(cudaEventRecord(join, side));
         CK(cudaStreamWaitEvent(st, join, 0));
     }
@@ -1033,6 +1163,7 @@ gbpf_status gbpf_batch::build_graph() {
         const Layout w = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1) : layout<double>(T.nB, T.n, T.nup, T.nPV, 1);
         if (w.total <= warp_cap) { warp_ok[t] = 1; slice = std::max(slice, align_up(w.total, 128)); }
     }
+    topo_warp = warp_ok;
     std::vector<int> wq, bq;
     for (int i = 0; i < n_inst; i++) (warp_ok[inst_topo[i]] ? wq : bq).push_back(i);
     n_warp_q = (int)wq.size();
@@ -1124,6 +1255,83 @@ gbpf_status gbpf_batch::build_graph() {
     if (e != cudaSuccess) { set_error(std::string("capture: ") + cudaGetErrorString(e)); return GBPF_E_CUDA; }
     graph = g;
     CK(cudaGraphInstantiate(&exec, graph, 0));
+    return GBPF_OK;
+}
+
+// Batched Newton from the learned warm start: features of every instance ->
+// network -> per-instance choice between the predicted and the instance's own
+// start (initial mismatch) -> one persistent Newton launch from the chosen
+// starts -> instances whose predicted start did not converge, or converged far
+// from the prediction, are solved again from their own start.  kind[i]: 0 own start chosen up front, 1 predicted
+// start converged, 2 predicted start failed and the own start was used.
+gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, float *ms) {
+    if (!exec || n_inst < 1) { set_error("no instances: call gbpf_batch_set_instances first"); return GBPF_E_ARG; }
+    const gbpf::MlpShape sh = gbpf::mlp_shape(m);
+    const int t0 = inst_topo[0];
+    const int nB = grids[t0].nB;
+    for (int i = 0; i < n_inst; i++)
+        if (inst_topo[i] != t0) { set_error("warm start needs every instance on one grid"); return GBPF_E_ARG; }
+    if (sh.n_in != 3 * nB || sh.n_out != 2 * nB) {
+        set_error("network shape does not match the grid: inputs must be 3*nB and outputs 2*nB");
+        return GBPF_E_ARG;
+    }
+    if (sh.device != device) { set_error("network and batch live on different devices"); return GBPF_E_ARG; }
+    if (warm_n != n_inst) {
+        warm_mem.reset();
+        const size_t xb = align_up(2 * (size_t)n_inst * sh.kin, 256), pb = align_up(4 * (size_t)n_inst * sh.outp, 256),
+                     vb = align_up(8 * (size_t)n_bus_total, 256), ib = align_up(4 * (size_t)n_inst, 256);
+        CK(cudaMalloc(&warm_mem.p, xb + pb + 4 * vb + 2 * ib));
+        char *p = (char *)warm_mem.p;
+        wX = (__nv_bfloat16 *)p; wPred = (float *)(p + xb);
+        wV = (double *)(p + xb + pb); wTh = (double *)(p + xb + pb + vb); wEF = (double2 *)(p + xb + pb + 2 * vb);
+        wKind = (int *)(p + xb + pb + 4 * vb); wQueue = (int *)(p + xb + pb + 4 * vb + ib);
+        warm_n = n_inst;
+    }
+    CK(cudaEventRecord(ev0, stream));
+    k_ws_features<<<1024, 256, 0, stream>>>(args.Pliq, args.Qliq, args.V0, args.inst_off, n_inst, nB, sh.n_in, sh.kin,
+                                            sh.in_mean, sh.in_iscale, wX);
+    CK(cudaGetLastError());
+    gbpf_status st = gbpf::mlp_infer(m, wX, n_inst, wPred, stream);
+    if (st != GBPF_OK) return st;
+    k_ws_select<<<(n_inst * 32 + 255) / 256, 256, 0, stream>>>(args, wPred, sh.outp, sh.out_mean, sh.out_scale, wV,
+                                                                 wTh, wEF, wKind);
+    CK(cudaGetLastError());
+    Args ba = args, wa = wargs;
+    ba.V0 = wa.V0 = wV;
+    ba.th0 = wa.th0 = wTh;
+    ba.max_iter = wa.max_iter = std::min(max_iter, kWarmMaxIter);
+    if ((st = launch_with(stream, ba, wa)) != GBPF_OK) return st;
+    k_ws_check<<<(n_inst * 32 + 255) / 256, 256, 0, stream>>>(args, wV, wKind);
+    CK(cudaGetLastError());
+    std::vector<int> kind(n_inst), status(n_inst), iters(n_inst);
+    CK(cudaMemcpyAsync(kind.data(), wKind, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(status.data(), args.status, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(iters.data(), args.iters, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    std::vector<int> fw, fb;
+    for (int i = 0; i < n_inst; i++) {
+        if (witers_out) witers_out[i] = kind[i] ? iters[i] : 0;
+        if (kind[i] == 3 || (kind[i] == 1 && status[i] != GBPF_OK)) {
+            kind[i] = 2;
+            (topo_warp[inst_topo[i]] ? fw : fb).push_back(i);
+        }
+    }
+    if (!fw.empty() || !fb.empty()) {
+        // the fallback: the same launch from the instances' own starts
+        if (!fw.empty()) CK(cudaMemcpyAsync(wQueue, fw.data(), 4 * fw.size(), cudaMemcpyHostToDevice, stream));
+        if (!fb.empty())
+            CK(cudaMemcpyAsync(wQueue + fw.size(), fb.data(), 4 * fb.size(), cudaMemcpyHostToDevice, stream));
+        Args bf = args, wf = wargs;
+        wf.queue = wQueue;
+        wf.queue_len = (int)fw.size();
+        bf.queue = wQueue + fw.size();
+        bf.queue_len = (int)fb.size();
+        if ((st = launch_with(stream, bf, wf)) != GBPF_OK) return st;
+    }
+    CK(cudaEventRecord(ev1, stream));
+    CK(cudaEventSynchronize(ev1));
+    if (ms) CK(cudaEventElapsedTime(ms, ev0, ev1));
+    if (kind_out) std::copy(kind.begin(), kind.end(), kind_out);
     return GBPF_OK;
 }
 
@@ -1335,6 +1543,16 @@ extern "C" gbpf_status gbpf_batch_events(gbpf_batch *b, int inst, int *ev, int c
     for (int i = 0; i < m; i++) std::copy(&e[4 * idx[i]], &e[4 * idx[i]] + 4, ev + 4 * i);
     *n = m;
     return have > b->ev_cap ? GBPF_E_ARG : GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_batch_solve_warm(gbpf_batch *b, gbpf_mlp *m, int *start_kind, int *warm_iterations,
+                                             double *ms) {
+    ARGCHECK(b && m);
+    CK(cudaSetDevice(b->device));
+    float t = 0;
+    gbpf_status st = b->solve_warm(m, start_kind, warm_iterations, &t);
+    if (ms) *ms = t;
+    return st;
 }
 
 extern "C" gbpf_status gbpf_batch_info(const gbpf_batch *b, long long info[8]) {

@@ -316,6 +316,90 @@ gbpf_status gbpf_batch_solve_noalloc(gbpf_batch *b, int n_inst, const int *grid_
                                      double *theta, double *Pcalc, double *Qcalc, int *iterations,
                                      int *status, double *final_mismatch, void *stream);
 
+/* ------------------------------------------------------------------------ */
+/* Learned warm start (no counterpart in the reference, whose Newton loop    */
+/* always starts from v_inicial / theta_inicial, GPU/sistInfo.h:62-242)      */
+/* ------------------------------------------------------------------------ */
+
+/* A dense network features -> n_hidden_layers x n_hidden_width (GELU) ->
+ * outputs, bf16 weights with fp32 master copies, trained with Adam on the GPU
+ * by the library's own tensor-core (tcgen05) kernels.  linear_skip != 0 adds
+ * a linear path from the features to the outputs (y = MLP(x) + S x), summed
+ * in the output layer's accumulator; it lets the network represent the
+ * near-linear, full-rank response of the bus angles to the injections, which
+ * a hidden width below the bus count cannot.  Layer index n_hidden_layers + 1
+ * of gbpf_mlp_params is S (no bias).  For a warm start of a grid with nB
+ * buses: n_in = 3*nB with features [Pliq | Qliq | V0] of every bus (p.u.,
+ * file bus order) and n_out = 2*nB with outputs [|V| | theta]. */
+typedef struct gbpf_mlp gbpf_mlp;
+gbpf_status gbpf_mlp_create(int n_in, int n_hidden_width, int n_hidden_layers, int n_out, int linear_skip,
+                            unsigned long long seed, int device, gbpf_mlp **out);
+void gbpf_mlp_free(gbpf_mlp *m);
+/* dims = n_in, hidden width, hidden layers, n_out, linear_skip. */
+gbpf_status gbpf_mlp_dims(const gbpf_mlp *m, int dims[5]);
+
+/* Training set: X [n, n_in] and Y [n, n_out] (host, row-major, raw units).
+ * Sets the per-feature normalisation (mean, 1/std of inputs; mean, std of
+ * outputs) from the data and keeps a normalised copy on the device. */
+gbpf_status gbpf_mlp_set_data(gbpf_mlp *m, const float *X, const float *Y, int n);
+
+/* `epochs` passes over the training set in shuffled mini-batches of `batch`
+ * rows (a multiple of 8; the last partial batch of each epoch is dropped),
+ * mean-squared error on the normalised outputs, Adam (beta 0.9 / 0.999,
+ * eps 1e-8) at a learning rate that falls from lr to lr_final along a cosine
+ * over the steps of this call (lr_final == lr: constant).  epoch_loss[e] (may
+ * be NULL) = mean loss of epoch e; *ms_total (may be NULL) = device time of
+ * all epochs. */
+gbpf_status gbpf_mlp_train(gbpf_mlp *m, int epochs, int batch, float lr, float lr_final,
+                           unsigned long long seed, float *epoch_loss, double *ms_total);
+
+/* Training loss over the normalised output residual e (one row per sample):
+ * (|e A|^2 + lam |e|^2) / (rows * n_out) with A [n_out, k] (host, row-major,
+ * rounded to bf16 on the device; the loss stays a sum of squares); A = NULL
+ * restores the mean squared error (lam ignored).  For a warm start, A = S J0^T
+ * with J0 the Newton Jacobian at a typical solution and S the output scales
+ * makes |e A| the linearised mismatch of the predicted start, which is what
+ * decides how many Newton iterations the start saves. */
+gbpf_status gbpf_mlp_set_loss_metric(gbpf_mlp *m, const float *A, int k, float lam);
+
+/* Y [n, n_out] = network(X [n, n_in]), raw units in and out. */
+gbpf_status gbpf_mlp_predict(gbpf_mlp *m, const float *X, int n, float *Y);
+
+/* Loss and gradients of one batch of NORMALISED rows Xn [n, n_in], Yn
+ * [n, n_out] (n a multiple of 8) at the current parameters, without an
+ * update: dW = the weight gradients of every layer concatenated (layer l is
+ * [out_l, in_l] row-major; the skip S last, [n_out, n_in]), db = the bias
+ * gradients concatenated. */
+gbpf_status gbpf_mlp_gradients(gbpf_mlp *m, const float *Xn, const float *Yn, int n, float *loss,
+                               float *dW, float *db);
+
+/* Parameters of layer `layer` (0 = first): W [out, in] row-major, b [out]. */
+gbpf_status gbpf_mlp_params(gbpf_mlp *m, int layer, float *W, float *b);
+gbpf_status gbpf_mlp_set_params(gbpf_mlp *m, int layer, const float *W, const float *b);
+/* Normalisation: x_norm = (x - in_mean) * in_scale; y = y_norm * out_scale + out_mean. */
+gbpf_status gbpf_mlp_norm(const gbpf_mlp *m, float *in_mean, float *in_scale, float *out_mean,
+                          float *out_scale);
+gbpf_status gbpf_mlp_set_norm(gbpf_mlp *m, const float *in_mean, const float *in_scale,
+                              const float *out_mean, const float *out_scale);
+
+/* Batched Newton from the network's start: the current instances (all on one
+ * grid of nB buses; network n_in = 3*nB, n_out = 2*nB) are turned into
+ * features on the device, the network predicts |V| (PQ buses) and theta
+ * (non-slack buses), and each instance starts from the prediction when its
+ * initial mismatch is smaller than that of the instance's own start
+ * (V0/theta0 of gbpf_batch_set_instances, by default the flat start), else
+ * from its own start.  Instances whose predicted start does not converge are
+ * solved again from their own start.  Results as for gbpf_batch_solve
+ * (gbpf_batch_results).  start_kind[i] (may be NULL): 0 own start chosen up
+ * front, 1 predicted start converged, 2 predicted start failed (no
+ * convergence within min(no_max_iter, 10) iterations, or a solution whose
+ * |V| lies more than 0.05 p.u. from the prediction) and was replaced;
+ * warm_iterations[i] (may be NULL): iterations of the predicted-start
+ * attempt (0 when not attempted); *ms (may be NULL): device time of the whole
+ * sequence, the fallback decision included. */
+gbpf_status gbpf_batch_solve_warm(gbpf_batch *b, gbpf_mlp *m, int *start_kind, int *warm_iterations,
+                                  double *ms);
+
 /* info[0..7] = topologies, instances, packed buses, resident thread blocks,
  * dynamic shared memory per block of the block-per-instance kernel,
  * topologies whose factor is in shared memory, global scratch bytes per

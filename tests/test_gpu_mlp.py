@@ -1,0 +1,190 @@
+"""The learned warm start on the GPU.
+
+* The network's tensor-core kernels (tcgen05 GEMMs with fused epilogues)
+  against the CPU oracle (oracle/mlp_oracle.py, same bf16 rounding points):
+  loss and every weight/bias gradient, predictions, and one Adam step.
+  Tolerances: relative 5e-3 in norm for gradients and 2e-3 for predictions.
+  The only differences are fp32 accumulation order and the bf16 values that
+  this order pushes across a rounding boundary (0.4 % each); they compound
+  through the layers, measured 1e-7 at width 128 and 2.3e-3 for the first
+  layer of the 5664 -> 3 x 512 -> 3776 network.  An error in a tile, a tail
+  or an epilogue is of order 1.  Adam: 1e-5 absolute per parameter for a step
+  of lr 1e-3 wherever the gradient's sign is stable.
+* Training on the GPU reduces the loss.
+* What the trained network gains: batched Newton from the predicted start
+  needs fewer iterations than from the flat start, on held-out scenarios,
+  and converges to the same solution (|V|, theta within 1e-6)."""
+import numpy as np
+import pytest
+
+import mlp_oracle as mo
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(1e-30, np.linalg.norm(b)))
+
+
+@pytest.mark.parametrize("n_in,n_out,width,n,skip", [(40, 36, 128, 64, False), (40, 36, 128, 64, True),
+                                                     (300, 200, 256, 136, True), (5664, 3776, 512, 256, True)])
+def test_gradients_match_oracle(gb, n_in, n_out, width, n, skip):
+    m = gb.MLP(n_in, n_out, width=width, n_layers=3, skip=skip, seed=11)
+    rng = np.random.default_rng(n_in)
+    Xn = rng.normal(size=(n, n_in)).astype(np.float32)
+    Yn = rng.normal(size=(n, n_out)).astype(np.float32)
+    params = m.params()
+    # non-zero biases and skip so that those paths are exercised
+    params = [(W, (0.05 * rng.normal(size=b.shape)).astype(np.float32)) if b is not None else
+              ((0.3 / np.sqrt(n_in) * rng.normal(size=W.shape)).astype(np.float32), None) for W, b in params]
+    m.set_params(params)
+    loss, grads = m.gradients(Xn, Yn)
+    lo, go = mo.loss_and_grads(params, Xn, Yn, emulate=True)
+    assert abs(loss - lo) <= 1e-4 * lo
+    assert len(grads) == len(go) == 4 + skip
+    for l, ((gw, gbias), (ow, ob)) in enumerate(zip(grads, go)):
+        assert gw.shape == ow.shape
+        assert rel(gw, ow) < 5e-3, f"layer {l} dW"
+        if ob is not None:
+            assert rel(gbias, ob) < 5e-3, f"layer {l} db"
+
+
+def test_metric_loss_gradients_match_oracle(gb):
+    n_in, n_out, n = 300, 200, 128
+    m = gb.MLP(n_in, n_out, width=256, n_layers=3, seed=12)
+    rng = np.random.default_rng(12)
+    Xn = rng.normal(size=(n, n_in)).astype(np.float32)
+    Yn = rng.normal(size=(n, n_out)).astype(np.float32)
+    A = (rng.normal(size=(n_out, 150)) / np.sqrt(n_out)).astype(np.float32)
+    m.set_loss_metric(A, 0.01)
+    params = m.params()
+    params[-1] = ((0.3 / np.sqrt(n_in) * rng.normal(size=params[-1][0].shape)).astype(np.float32), None)
+    m.set_params(params)
+    loss, grads = m.gradients(Xn, Yn)
+    lo, go = mo.loss_and_grads(params, Xn, Yn, emulate=True, metric=(A, 0.01))
+    assert abs(loss - lo) <= 2e-3 * lo
+    for l, ((gw, gbias), (ow, ob)) in enumerate(zip(grads, go)):
+        assert rel(gw, ow) < 5e-3, f"layer {l} dW"
+        if ob is not None:
+            assert rel(gbias, ob) < 5e-3, f"layer {l} db"
+
+
+def _normalise(m, X, Y):
+    nm = m.norm()
+    Xn = (X.astype(np.float32) - nm["in_mean"]) * nm["in_scale"]
+    Yn = (Y.astype(np.float32) - nm["out_mean"]) / nm["out_scale"]
+    return Xn, Yn, nm
+
+
+def test_predict_matches_oracle(gb):
+    rng = np.random.default_rng(2)
+    m = gb.MLP(300, 200, width=256, n_layers=3, seed=2)
+    X = rng.normal(2.0, 3.0, (333, 300)).astype(np.float32)
+    Y = rng.normal(-1.0, 0.5, (333, 200)).astype(np.float32)
+    m.set_data(X, Y)
+    Xn, _, nm = _normalise(m, X, Y)
+    params = m.params()
+    params[-1] = ((0.05 * rng.normal(size=params[-1][0].shape)).astype(np.float32), None)
+    m.set_params(params)
+    P = m.predict(X)
+    y, _ = mo.forward(params, Xn, emulate=True)
+    ref = y * nm["out_scale"] + nm["out_mean"]
+    assert P.shape == ref.shape
+    assert rel(P - nm["out_mean"], ref - nm["out_mean"]) < 2e-3
+
+
+def test_one_training_step_matches_oracle_adam(gb):
+    rng = np.random.default_rng(3)
+    B = 64
+    m = gb.MLP(40, 36, width=128, n_layers=3, seed=3)
+    X = rng.normal(size=(B, 40)).astype(np.float32)
+    Y = rng.normal(size=(B, 36)).astype(np.float32)
+    m.set_data(X, Y)
+    Xn, Yn, _ = _normalise(m, X, Y)
+    p0 = m.params()
+    loss, _ = m.train(1, batch=B, lr=1e-3, seed=1)
+    p1 = m.params()
+    lo, g = mo.loss_and_grads(p0, Xn, Yn, emulate=True)
+    assert abs(loss[0] - lo) <= 1e-4 * lo
+    z = lambda x: None if x is None else np.zeros_like(x, dtype=np.float64)
+    state = [(z(W), z(W), z(b), z(b)) for W, b in p0]
+    f64 = lambda x: None if x is None else x.astype(np.float64)
+    want, _ = mo.adam_step([(f64(W), f64(b)) for W, b in p0], g, state, t=1, lr=1e-3)
+    assert len(p1) == 5
+    for (W0, b0), (W1, b1), (Ww, bw), (gW, gbias) in zip(p0, p1, want, g):
+        for a0, a1, aw, ga in ((W0, W1, Ww, gW), (b0, b1, bw, gbias)):
+            if a0 is None:
+                continue
+            stable = np.abs(ga) > 1e-2 * np.max(np.abs(ga))
+            assert np.max(np.abs((a1 - a0) - (aw - a0))[stable]) < 1e-5
+            # where the gradient is ~0 the first Adam step is +-lr or 0: bounded by lr
+            assert np.max(np.abs(a1 - a0)) <= 1e-3 * (1 + 1e-3)
+
+
+def test_training_reduces_loss(gb):
+    rng = np.random.default_rng(4)
+    n = 4096
+    X = rng.normal(size=(n, 64)).astype(np.float32)
+    A = rng.normal(size=(64, 48)) / 8
+    Y = (np.tanh(X @ A) + 0.1 * (X[:, :48] ** 2)).astype(np.float32)
+    m = gb.MLP(64, 48, width=256, n_layers=3, seed=4)
+    m.set_data(X, Y)
+    loss, ms = m.train(15, batch=256, lr=1e-3, seed=4)
+    assert np.all(np.isfinite(loss))
+    assert loss[-1] < 0.2 * loss[0]
+    assert ms > 0
+
+
+def _scenarios(base, n, rng):
+    lf = rng.uniform(0.7, 1.3, (n, len(base["Pload"])))
+    gf = rng.uniform(0.85, 1.15, (n, len(base["Pg"])))
+    return base["Pload"] * lf, base["Qload"] * lf, base["Pg"] * gf
+
+
+def test_warm_start_saves_iterations(gb):
+    grid = gb.generate(2, 20261205)
+    base = grid.buses()
+    nB = grid.nB
+    rng = np.random.default_rng(5)
+    opts = dict(tolerancia=1e-8, no_max_iter=30, lim_inj_reat=0)
+    solver = gb.Batch([grid], precision=gb.PREC_FP64, **opts)
+
+    def solve(Pl, Ql, Pg):
+        n = len(Pl)
+        solver.set_instances(np.zeros(n, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
+        solver.solve()
+        return solver.results()
+
+    Pl, Ql, Pg = _scenarios(base, 4096, rng)
+    r = solve(Pl, Ql, Pg)
+    ok = r["status"] == 0
+    assert ok.mean() > 0.95
+    V, th = r["V"].reshape(-1, nB)[ok], r["theta"].reshape(-1, nB)[ok]
+    X = gb.warm_features(Pg[ok] - Pl[ok], base["Qg"] - Ql[ok], np.tile(base["V0"], (ok.sum(), 1)))
+    Y = np.concatenate([V, th], axis=1)
+    m = gb.MLP(3 * nB, 2 * nB, width=256, n_layers=3, seed=5)
+    m.set_data(X, Y)
+    # loss = squared linearised mismatch of the predicted start (+ 1 % MSE)
+    plain = gb.Solver(grid, tolerancia=1e-8, no_max_iter=30, lim_inj_reat=0)
+    M = gb.warm_loss_metric(plain, V.mean(0), th.mean(0), m.norm()["out_scale"])
+    m.set_loss_metric(M, 0.01)
+    loss, _ = m.train(40, batch=128, lr=1e-3, lr_final=1e-5, seed=5)
+    assert loss[-1] < 0.05 * loss[0]
+    # held-out scenarios: flat start, then the learned start
+    Pl, Ql, Pg = _scenarios(base, 512, rng)
+    flat = solve(Pl, Ql, Pg)
+    w = solver.solve_warm(m)
+    warm = solver.results()
+    both = (flat["status"] == 0)
+    assert both.mean() > 0.95
+    assert np.all(warm["status"][both] == 0)
+    assert np.all(warm["final_mismatch"][both] <= 1e-8)
+    sel = np.repeat(both, nB)
+    assert np.max(np.abs(warm["V"][sel] - flat["V"][sel])) <= 1e-6
+    assert np.max(np.abs(warm["theta"][sel] - flat["theta"][sel])) <= 1e-6
+    kind = w["start_kind"]
+    assert (kind == 2).mean() < 0.05
+    assert (kind >= 1).mean() > 0.9
+    it_flat = flat["iterations"][both].mean()
+    it_warm = (warm["iterations"] + np.where(kind == 2, w["warm_iterations"], 0))[both].mean()
+    assert it_warm < it_flat - 0.5, (it_warm, it_flat)
