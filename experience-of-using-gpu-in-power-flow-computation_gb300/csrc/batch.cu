@@ -64,7 +64,13 @@ template <typename B4, typename B2> __device__ __forceinline__ B2 bmv(B4 a, B2 v
     r.y = a.z * v.x + a.w * v.y;
     return r;
 }
-template <typename B4> __device__ __forceinline__ B4 bshfl_xor(B4 v, int o) {
+// v plus the v of lane (lane ^ o): one butterfly step of a sum over lanes
+template <typename B2> __device__ __forceinline__ B2 b2sum_xor(B2 v, int o) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    return v;
+}
+template <typename B4> __device__ __forceinline__ B4 bsum_xor(B4 v, int o) {
     v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
     v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
     v.z += __shfl_xor_sync(0xffffffffu, v.z, o);
@@ -85,7 +91,7 @@ template <typename B4> __device__ __forceinline__ B4 bcast(B4 v, int src) {
 struct TopoOff {
     int yptr, ycol, yval, type, pv_bus, Qmin, Qmax, bus_of_blk, up_ptr, up_col, dg_ptr, dg_pos, dg_k,
         og_ptr, og_a, og_b, flev_ptr, flev_steps, blev_ptr, blev_steps, ysl, rbus, cbus, fent_ptr, fent_p,
-        fent_j;
+        fent_j, lvl_group;
 };
 struct Topo {
     int nB, nL, n, nup, nnzY, nPV, nfl, nbl, fac_smem, blob_smem, blob_bytes;
@@ -100,6 +106,10 @@ struct TopoView {
     const double *Qmin, *Qmax;
     const int *bus_of_blk, *up_ptr, *up_col, *dg_ptr, *dg_pos, *dg_k, *og_ptr, *og_a, *og_b;
     const int *flev_ptr, *flev_steps, *blev_ptr, *blev_steps, *ysl, *rbus, *cbus, *fent_ptr, *fent_p, *fent_j;
+    // log2 of the lanes that share one pivot / one entry / one back-substitution
+    // row in the block kernel: [3 * l] pivots and [3 * l + 1] entries of
+    // forward level l, [3 * l + 2] rows of backward level l
+    const int *lvl_group;
 };
 __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     TopoView v;
@@ -115,6 +125,7 @@ __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     v.ysl = (const int *)(b + o.ysl); v.rbus = (const int *)(b + o.rbus); v.cbus = (const int *)(b + o.cbus);
     v.fent_ptr = (const int *)(b + o.fent_ptr); v.fent_p = (const int *)(b + o.fent_p);
     v.fent_j = (const int *)(b + o.fent_j);
+    v.lvl_group = (const int *)(b + o.lvl_group);
     return v;
 }
 
@@ -365,56 +376,103 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
             // time, in two passes: one thread per pivot j (diagonal block, its
             // inverse through one reciprocal, y_j), then one thread per
             // off-diagonal entry of the level (U(j,i) and L(i,j) = (...) D_j^-1).
+            // Deep levels have few pivots with long gather lists: a group of
+            // 2^g lanes shares one pivot (entry, row), strides over its list
+            // and sums the partial updates with shuffles (lane 0 of the group
+            // starts from the stored value, the others from zero, so g = 0 is
+            // the plain one-thread-per-pivot loop).
             for (int l = 0; l < T.nfl; l++) {
-                for (int w = G.flev_ptr[l] + tid; w < G.flev_ptr[l + 1]; w += kThreads) {
-                    const int j = G.flev_steps[w];
-                    B4 D = fac[j];
-                    B2 yj;
-                    yj.x = (TJ)R[j].x;
-                    yj.y = (TJ)R[j].y;
-                    for (int t = G.dg_ptr[j]; t < G.dg_ptr[j + 1]; t++) {
-                        const int p = G.dg_pos[t];
-                        const B4 lj = Lv[p];
-                        D = bsub(D, bm(lj, Uv[p]));
-                        const B2 v = bmv(lj, ys[G.dg_k[t]]);
-                        yj.x -= v.x;
-                        yj.y -= v.y;
+                {
+                    const int lg = G.lvl_group[3 * l], gs = 1 << lg, gl = tid & (gs - 1), ng = kThreads >> lg;
+                    const int beg = G.flev_ptr[l], cnt = G.flev_ptr[l + 1] - beg;
+                    for (int b0 = 0; b0 < cnt; b0 += ng) {
+                        const int w = b0 + (tid >> lg);
+                        const bool on = w < cnt;
+                        const int j = on ? G.flev_steps[beg + w] : 0;
+                        B4 D;
+                        B2 yj;
+                        D.x = D.y = D.z = D.w = (TJ)0;
+                        yj.x = yj.y = (TJ)0;
+                        if (on && gl == 0) {
+                            D = fac[j];
+                            yj.x = (TJ)R[j].x;
+                            yj.y = (TJ)R[j].y;
+                        }
+                        if (on)
+                            for (int t = G.dg_ptr[j] + gl; t < G.dg_ptr[j + 1]; t += gs) {
+                                const int p = G.dg_pos[t];
+                                const B4 lj = Lv[p];
+                                D = bsub(D, bm(lj, Uv[p]));
+                                const B2 v = bmv(lj, ys[G.dg_k[t]]);
+                                yj.x -= v.x;
+                                yj.y -= v.y;
+                            }
+                        for (int o = gs >> 1; o > 0; o >>= 1) {
+                            D = bsum_xor(D, o);
+                            yj = b2sum_xor(yj, o);
+                        }
+                        if (on && gl == 0) {
+                            const TJ det = D.x * D.w - D.y * D.z;
+                            if (det == (TJ)0 || !isfinite(det)) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                            const TJ rd = (TJ)1 / det;
+                            B4 inv;
+                            inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
+                            fac[j] = D;
+                            dinv[j] = inv;
+                            ys[j] = yj;
+                        }
                     }
-                    const TJ det = D.x * D.w - D.y * D.z;
-                    if (det == (TJ)0 || !isfinite(det)) { s_status = GBPF_E_SINGULAR; s_done = 1; }
-                    const TJ rd = (TJ)1 / det;
-                    B4 inv;
-                    inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
-                    fac[j] = D;
-                    dinv[j] = inv;
-                    ys[j] = yj;
                 }
                 __syncthreads();
-                for (int e = G.fent_ptr[l] + tid; e < G.fent_ptr[l + 1]; e += kThreads) {
-                    const int p = G.fent_p[e], j = G.fent_j[e];
-                    B4 aL = Lv[p], aU = Uv[p];
-                    for (int r = G.og_ptr[p]; r < G.og_ptr[p + 1]; r++) {
-                        const int x = G.og_a[r], y = G.og_b[r];
-                        aL = bsub(aL, bm(Lv[y], Uv[x]));
-                        aU = bsub(aU, bm(Lv[x], Uv[y]));
+                {
+                    const int lg = G.lvl_group[3 * l + 1], gs = 1 << lg, gl = tid & (gs - 1), ng = kThreads >> lg;
+                    const int beg = G.fent_ptr[l], cnt = G.fent_ptr[l + 1] - beg;
+                    for (int b0 = 0; b0 < cnt; b0 += ng) {
+                        const int e = b0 + (tid >> lg);
+                        const bool on = e < cnt;
+                        const int p = on ? G.fent_p[beg + e] : 0, j = on ? G.fent_j[beg + e] : 0;
+                        B4 aL, aU;
+                        aL.x = aL.y = aL.z = aL.w = (TJ)0;
+                        aU = aL;
+                        if (on && gl == 0) { aL = Lv[p]; aU = Uv[p]; }
+                        if (on)
+                            for (int r = G.og_ptr[p] + gl; r < G.og_ptr[p + 1]; r += gs) {
+                                const int x = G.og_a[r], y = G.og_b[r];
+                                aL = bsub(aL, bm(Lv[y], Uv[x]));
+                                aU = bsub(aU, bm(Lv[x], Uv[y]));
+                            }
+                        for (int o = gs >> 1; o > 0; o >>= 1) {
+                            aL = bsum_xor(aL, o);
+                            aU = bsum_xor(aU, o);
+                        }
+                        if (on && gl == 0) {
+                            Uv[p] = aU;
+                            Lv[p] = bm(aL, dinv[j]);
+                        }
                     }
-                    Uv[p] = aU;
-                    Lv[p] = bm(aL, dinv[j]);
                 }
                 __syncthreads();
             }
             if (s_done) break;
-            // backward substitution, one thread per pivot of each level
+            // backward substitution, level by level, grouped like the factor
             for (int l = 0; l < T.nbl; l++) {
-                for (int w = G.blev_ptr[l] + tid; w < G.blev_ptr[l + 1]; w += kThreads) {
-                    const int j = G.blev_steps[w];
-                    B2 acc = ys[j];
-                    for (int p = G.up_ptr[j]; p < G.up_ptr[j + 1]; p++) {
-                        const B2 v = bmv(Uv[p], xs[G.up_col[p]]);
-                        acc.x -= v.x;
-                        acc.y -= v.y;
-                    }
-                    xs[j] = bmv(dinv[j], acc);
+                const int lg = G.lvl_group[3 * l + 2], gs = 1 << lg, gl = tid & (gs - 1), ng = kThreads >> lg;
+                const int beg = G.blev_ptr[l], cnt = G.blev_ptr[l + 1] - beg;
+                for (int b0 = 0; b0 < cnt; b0 += ng) {
+                    const int w = b0 + (tid >> lg);
+                    const bool on = w < cnt;
+                    const int j = on ? G.blev_steps[beg + w] : 0;
+                    B2 acc;
+                    acc.x = acc.y = (TJ)0;
+                    if (on && gl == 0) acc = ys[j];
+                    if (on)
+                        for (int p = G.up_ptr[j] + gl; p < G.up_ptr[j + 1]; p += gs) {
+                            const B2 v = bmv(Uv[p], xs[G.up_col[p]]);
+                            acc.x -= v.x;
+                            acc.y -= v.y;
+                        }
+                    for (int o = gs >> 1; o > 0; o >>= 1) acc = b2sum_xor(acc, o);
+                    if (on && gl == 0) xs[j] = bmv(dinv[j], acc);
                 }
                 __syncthreads();
             }
@@ -1005,6 +1063,36 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
     o.ysl = put(S.ysl.data(), nq * 4); o.rbus = put(S.rbus.data(), nq * 4); o.cbus = put(S.cbus.data(), nq * 4);
     o.fent_ptr = put(S.fent_ptr.data(), (nfl + 1) * 4); o.fent_p = put(S.fent_p.data(), nup * 4);
     o.fent_j = put(S.fent_j.data(), nup * 4);
+    // lanes per pivot / entry / row of each level for the block kernel: as many
+    // as the level's thread budget allows, no more than its longest list needs
+    std::vector<int> grp(3 * (size_t)std::max(nfl, nbl), 0);
+    auto group_of = [](int count, int longest) {
+        int g = 0;
+        while (g < 5 && ((long long)count << (g + 1)) <= kThreads && (1 << g) < longest) g++;
+        return g;
+    };
+    for (int l = 0; l < nfl; l++) {
+        int md = 0, mo = 0;
+        for (int w = S.flev_ptr[l]; w < S.flev_ptr[l + 1]; w++) {
+            const int j = S.flev_steps[w];
+            md = std::max(md, S.dg_ptr[j + 1] - S.dg_ptr[j]);
+        }
+        for (int e = S.fent_ptr[l]; e < S.fent_ptr[l + 1]; e++) {
+            const int pp = S.fent_p[e];
+            mo = std::max(mo, (int)(S.og_ptr[pp + 1] - S.og_ptr[pp]));
+        }
+        grp[3 * l] = group_of(S.flev_ptr[l + 1] - S.flev_ptr[l], md);
+        grp[3 * l + 1] = group_of(S.fent_ptr[l + 1] - S.fent_ptr[l], mo);
+    }
+    for (int l = 0; l < nbl; l++) {
+        int mu = 0;
+        for (int w = S.blev_ptr[l]; w < S.blev_ptr[l + 1]; w++) {
+            const int j = S.blev_steps[w];
+            mu = std::max(mu, S.up_ptr[j + 1] - S.up_ptr[j]);
+        }
+        grp[3 * l + 2] = group_of(S.blev_ptr[l + 1] - S.blev_ptr[l], mu);
+    }
+    o.lvl_group = put(grp.data(), grp.size() * 4);
     DevBuf mem, tmp;
     CK(cudaMalloc(&mem.p, blob.size()));
     CK(cudaMemcpyAsync(mem.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, stream));

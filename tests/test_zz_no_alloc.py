@@ -5,10 +5,13 @@ Who needs it: callers that cannot allocate device memory when they solve --
 their solves run inside a CUDA stream-capture region, where allocation is not
 allowed, or their device memory belongs to another allocator.  The entry point
 works on their device buffers and keeps its own scratch in one static 8 MiB
-device array.  Same arithmetic as the allocating path (only the place of the
-factor differs), so |V| and theta must agree to 1e-12, iteration counts and
-statuses exactly.  The second call uses other instances, so stale contents of
-the shared scratch would show up."""
+device array.  It runs every instance on the block-per-instance kernel, while
+the allocating path serves these small grids with the warp-per-instance
+kernel; the two sum the LU updates of a pivot in different orders, so the
+results agree to rounding: |V| and theta to 1e-12, the final mismatch (itself
+~1e-13) to 1e-12 absolute, iteration counts and statuses exactly.  The second
+call uses other instances, so stale contents of the shared scratch would show
+up."""
 import os
 
 import numpy as np
@@ -69,7 +72,7 @@ def test_noalloc_matches_batch_on_two_calls(gb):
         assert np.max(np.abs(V.cpu().numpy() - ref["V"])) <= 1e-12
         assert np.max(np.abs(th.cpu().numpy() - ref["theta"])) <= 1e-12
         assert np.max(np.abs(P.cpu().numpy() - ref["Pcalc"])) <= 1e-10
-        np.testing.assert_allclose(mm.cpu().numpy(), ref["final_mismatch"], rtol=1e-6, atol=1e-14)
+        np.testing.assert_allclose(mm.cpu().numpy(), ref["final_mismatch"], rtol=0, atol=1e-12)
         assert np.all(mm.cpu().numpy() <= 1e-8)
 
 
