@@ -15,7 +15,10 @@ tolerance 1e-8 p.u., no_max_iter 100.  A step solves all 4,096 scenarios.
            oracle-matching path) and batched FP64 on the same scenarios
 Other workloads: c2-plain (one FP64 solve of the grid per step), c3 (the
 15,104-bus grid, one FP64 solve per step), c4 (4,096 instances of 14..472-bus
-grids, batched FP32).
+grids, batched FP32), c5 (the learned warm start on the 1,888-bus grid: 50,000
+training solves, the 5664 -> 3 x 512 -> 3776 network trained for 20 epochs on
+the GPU, then a step = batched FP32 Newton from the predicted start, flat-start
+fallback, over 8,192 held-out scenarios).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2]
   python bench.py --impl reference     the CPU restatement of the reference
@@ -50,7 +53,7 @@ def args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gbpf", choices=["gbpf", "reference"])
-    p.add_argument("--workload", default="c2", choices=["c2", "c2-plain", "c3", "c4"])
+    p.add_argument("--workload", default="c2", choices=["c2", "c2-plain", "c3", "c4", "c5"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -384,6 +387,182 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     return line
 
 
+C5_TRAIN, C5_TEST = 50000, 8192
+
+
+def c5_scenarios(np, base, n, seed):
+    """Per-bus load x U(0.7, 1.3) (P and Q together), generator P x U(0.85, 1.15)."""
+    rng = np.random.default_rng(seed)
+    nb = len(base["Pload"])
+    lf = rng.uniform(0.7, 1.3, (n, nb))
+    gf = rng.uniform(0.85, 1.15, (n, nb))
+    return base["Pload"] * lf, base["Qload"] * lf, base["Pg"] * gf
+
+
+def train_flops_per_step(nb, width, B, k_metric):
+    """Multiply-add FLOPs of the tensor-core GEMMs of one training step."""
+    kin, out = 3 * nb, 2 * nb
+    fwd = kin * width + 2 * width * width + width * out + kin * out
+    metric = 2 * out * k_metric
+    dh = out * width + 2 * width * width
+    dw = width * kin + 2 * width * width + out * width + out * kin
+    return 2.0 * B * (fwd + metric + dh + dw)
+
+
+def bench_c5(a, gb, np, rank, dev, world, dist):
+    grid = gb.generate(3, BASE_SEED + 5, tiles=16)
+    nB, base = grid.nB, grid.buses()
+    opts = dict(tolerancia=1e-8, no_max_iter=30, lim_inj_reat=0)
+    # training set: solutions of the plain Newton method (batched FP64, flat start)
+    Pl, Ql, Pg = c5_scenarios(np, base, C5_TRAIN, BASE_SEED + 5 + 1000 * rank)
+    gen = gb.Batch([grid], device=dev, precision=gb.PREC_FP64, **opts)
+    t0 = time.perf_counter()
+    gen.set_instances(np.zeros(C5_TRAIN, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
+    gen.solve()
+    r = gen.results()
+    t_gen = time.perf_counter() - t0
+    ok = r["status"] == 0
+    V, th = r["V"].reshape(-1, nB)[ok], r["theta"].reshape(-1, nB)[ok]
+    X = gb.warm_features(Pg[ok] - Pl[ok], base["Qg"] - Ql[ok], np.tile(base["V0"], (int(ok.sum()), 1)))
+    Y = gb.warm_targets(V, th)
+    gen.close()
+    del r, Pl, Ql, Pg
+    width, batch, epochs, lam = 512, 256, 20, 1.0
+    m = gb.MLP(3 * nB, 2 * nB, width=width, n_layers=3, skip=True, seed=BASE_SEED + 5, device=dev)
+    m.set_data(X, Y)
+    plain = gb.Solver(grid, device=dev, metodo=0, **opts)
+    A = gb.warm_loss_metric(plain, V.mean(0), th.mean(0), m.norm()["out_scale"])
+    m.set_loss_metric(A, lam)
+    loss, train_ms = m.train(epochs, batch=batch, lr=1e-3, lr_final=1e-5, seed=BASE_SEED + 5)
+    steps_per_epoch = len(X) // batch
+    train_tflops = train_flops_per_step(nB, width, batch, (A.shape[1] + 7) // 8 * 8) * steps_per_epoch * epochs / (
+        train_ms / 1e3) / 1e12
+    del X, Y, V, th
+    # held-out scenarios
+    Pt, Qt, Gt = c5_scenarios(np, base, C5_TEST, BASE_SEED + 5 + 7 + 1000 * rank)
+    gi = np.zeros(C5_TEST, np.int32)
+    inputs = dict(Pload=Pt.ravel(), Qload=Qt.ravel(), Pg=Gt.ravel())
+    ref = gb.Batch([grid], device=dev, precision=gb.PREC_FP64, **opts)
+    ref.set_instances(gi, **inputs)
+    ref.solve()
+    r64 = ref.results()
+    ms64 = ref.time(3) / 3
+    w64 = ref.solve_warm(m)
+    r64w = ref.results(state=False)
+    fast = gb.Batch([grid], device=dev, precision=gb.PREC_FP32_IR, **opts)
+    fast.set_instances(gi, **inputs)
+    fast.solve()
+    r32 = fast.results(state=False)
+    ms32 = fast.time(3) / 3
+    for _ in range(max(3, a.warmup)):
+        w = fast.solve_warm(m)
+    if dist:
+        dist.barrier()
+    with Clocks(dev) as clk:
+        t_steps = 0.0
+        for _ in range(a.steps):
+            w = fast.solve_warm(m)
+            t_steps += w["ms"]
+    if dist:
+        dist.barrier()
+    rw = fast.results()
+    kind = w["start_kind"]
+    conv = int((rw["status"] == 0).sum())
+    t_dev = max_over_ranks(t_steps / 1e3, dist, dev)
+    value = sum_over_ranks(conv, dist, dev) * a.steps / t_dev
+    both = (r64["status"] == 0) & (rw["status"] == 0)
+    sel = np.repeat(both, nB)
+    err_v = float(np.max(np.abs(rw["V"][sel] - r64["V"][sel]))) if both.any() else None
+    err_t = float(np.max(np.abs(rw["theta"][sel] - r64["theta"][sel]))) if both.any() else None
+    assert np.all(rw["final_mismatch"][rw["status"] == 0] <= 1e-8)
+    it_w = rw["iterations"] + np.where(kind == 2, w["warm_iterations"], 0)
+    # end to end through the public API with host buffers
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        fast.set_instances(gi, **inputs)
+        fast.solve_warm(m)
+        fast.results(state=True)
+    t_e2e = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    e2e = sum_over_ranks(conv, dist, dev) * a.steps / t_e2e
+    # the plain FP64 form: one held-out scenario per gbpf_solve
+    n_plain, nconv = 64, 0
+    t0 = time.perf_counter()
+    for i in range(n_plain):
+        plain.set_start(Pliq=Gt[i] - Pt[i], Qliq=base["Qg"] - Qt[i])
+        nconv += plain.solve(full=False)["converged"]
+    plain_rate = nconv / (time.perf_counter() - t0)
+    peak, src = peak_hbm()
+    nb_tot = C5_TEST * nB
+    bytes_launch = nb_tot * 8 * 5 + nb_tot * 8 * 4 + C5_TEST * 20
+    achieved = bytes_launch / (t_steps / a.steps / 1e3) / 1e9
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if src == "measured" else {}
+    tpeak = peaks.get("bf16_tflops_sustained", 1700.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": max(3, a.warmup), "ms_per_step": t_dev * 1e3 / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "c5", "grid": "1888-bus (16 tied 118-bus copies), limits off",
+                   "instances_per_gpu": C5_TEST, "tolerance": 1e-8, "no_max_iter": 30,
+                   "form": "batched, FP32 LU + FP64 mismatch/test/update, learned warm start with flat-start "
+                           "fallback (network inference, start choice and Newton inside the timed region)",
+                   "network": f"{3 * nB} -> 3 x {width} GELU -> {2 * nB} + linear skip, bf16 weights, fp32 "
+                              f"accumulation; loss |e A|^2 + {lam} |e|^2 (A = S J0^T); Adam lr 1e-3 cosine to "
+                              f"1e-5, {epochs} epochs, batch {batch}",
+                   "train_solves": C5_TRAIN, "train_converged": int(ok.sum()),
+                   "train_generation_s": t_gen, "train_s": train_ms / 1e3,
+                   "train_loss_first_last": [float(loss[0]), float(loss[-1])],
+                   "converged_per_step": conv,
+                   "mean_iterations_flat_fp32": float(r32["iterations"].mean()),
+                   "mean_iterations_warm_fp32": float(it_w.mean()),
+                   "mean_iterations_flat_fp64": float(r64["iterations"].mean()),
+                   "mean_iterations_warm_fp64": float((r64w["iterations"] + np.where(
+                       w64["start_kind"] == 2, w64["warm_iterations"], 0)).mean()),
+                   "start_kind_counts": {"flat_chosen": int((kind == 0).sum()), "predicted": int((kind == 1).sum()),
+                                         "fallback": int((kind == 2).sum())},
+                   "fallback_rate": float((kind == 2).mean()),
+                   "max_abs_err_vs_fp64": {"V": err_v, "theta": err_t},
+                   "plain_fp64_solves_per_s": plain_rate,
+                   "batched_fp64_flat_solves_per_s": int((r64["status"] == 0).sum()) / (ms64 / 1e3),
+                   "batched_fp32_flat_solves_per_s": int((r32["status"] == 0).sum()) / (ms32 / 1e3),
+                   "speedup_vs_plain_fp64": value / plain_rate if plain_rate else None,
+                   "l2": f"per-step inputs {nb_tot * 8 * 9 / 2**20:.0f} MiB > L2",
+                   "parallelism": f"scenarios sharded x{world}"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nb_tot * 8 * 5 + C5_TEST * 12,
+                "d2h_bytes_per_step": nb_tot * 8 * 4 + C5_TEST * 20},
+        "roofline": {"bound": "hbm", "kernel": "k_nr_block<float> (one persistent launch per step)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src_note(src), "traffic": None,
+                     "note": "dependent-load latency bound (factor in L2-resident scratch)"},
+        "roofline_training": {"bound": "tensor", "kernel": "k_gemm (tcgen05 bf16, all training GEMMs)",
+                              "achieved": train_tflops, "peak": tpeak, "unit": "TFLOP/s",
+                              "frac": train_tflops / tpeak,
+                              "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained" if peaks else "fallback"},
+        "clocks": clk.summary(),
+        "gpu_launches": a.steps * (1 + 4 + 1 + 1 + 1 + (1 if (kind == 2).any() else 0)),
+    }
+    if rank == 0 and not a.no_cpu_baseline:
+        cdf = write_grid(grid)
+        line["cpu_baseline"] = cpu_baseline_c5(cdf, Pt, Qt, Gt)
+    return line
+
+
+def cpu_baseline_c5(cdf, Pt, Qt, Gt, target_s=12.0):
+    """The oracle (flat start) on one host core over a bounded sample of the
+    held-out scenarios."""
+    oracle = _oracle()
+    og = oracle.Grid(cdf)
+    conv, n = 0, 0
+    t0 = time.perf_counter()
+    while n < len(Pt) and time.perf_counter() - t0 < target_s:
+        og.set_bus(Pload=Pt[n], Qload=Qt[n], Pg=Gt[n])
+        conv += og.solve(1e-8, 30, False)["converged"]
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": conv / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"first {n} of the {len(Pt)} held-out scenarios, {conv} converged, {dt:.1f} s single-threaded "
+                      f"oracle (oracle/pf_oracle.c via ctypes), flat start"}
+
+
 def peak_src_note(src):
     return f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else "fallback 6.8 TB/s"
 
@@ -459,6 +638,8 @@ def main():
     gb = importlib.import_module(PKG)
     if a.workload in ("c2", "c4"):
         line = bench_batch(a, gb, np, rank, local_rank, world, dist)
+    elif a.workload == "c5":
+        line = bench_c5(a, gb, np, rank, local_rank, world, dist)
     else:
         line = bench_single(a, gb, np, rank, local_rank, world, dist)
     if rank == 0:

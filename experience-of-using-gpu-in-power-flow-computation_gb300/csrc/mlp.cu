@@ -60,7 +60,7 @@ enum Epi : int {
     EPI_OUT_TRAIN = 1,   // y = acc + b; d = y - target; loss += d^2; H = d * gscale; HT = H^T
     EPI_OUT_INFER = 2,   // out = acc + b
     EPI_BWD_HIDDEN = 3,  // dz = acc * gelu'(Z); H = dz; HT = dz^T
-    EPI_WGRAD_ADAM = 4,  // Adam on (Wm, Am, Av) with g = acc; Wb = bf16(W); Wt = Wb^T
+    EPI_WGRAD_ADAM = 4,  // Adam on (Wm, Am, Av) with g = acc; Wb = bf16(W) (Wt by k_transpose_bf16)
     EPI_WGRAD_STORE = 5, // out = acc (gradient, fp32)
     EPI_OUT_RESID = 6,   // e = acc + b - target; E32 = e; H = bf16(e); loss += lam e^2
     EPI_PROJ = 7,        // r = acc (= (e A)[m, n]); loss += r^2; H = bf16(r)
@@ -200,6 +200,94 @@ __device__ __forceinline__ float gelu_grad(float z) {
     return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
 }
 
+// 8 consecutive fp32 / bf16 values (32 / 16 bytes, aligned: every leading
+// dimension and every column group is a multiple of 8 elements)
+__device__ __forceinline__ void ld8(const float *p, float (&x)[8]) {
+    const float4 a = ((const float4 *)p)[0], b = ((const float4 *)p)[1];
+    x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w; x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+}
+__device__ __forceinline__ void st8(float *p, const float (&x)[8]) {
+    ((float4 *)p)[0] = make_float4(x[0], x[1], x[2], x[3]);
+    ((float4 *)p)[1] = make_float4(x[4], x[5], x[6], x[7]);
+}
+__device__ __forceinline__ void st8h(bf16 *p, const float (&x)[8]) {
+    __align__(16) bf16 h[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) h[j] = __float2bfloat16_rn(x[j]);
+    *(uint4 *)p = *(const uint4 *)h;
+}
+// transposed bf16 store: 32 lanes = 32 consecutive rows of the transpose
+__device__ __forceinline__ void st8t(bf16 *p, int ld, int row, int n, const float (&x)[8]) {
+#pragma unroll
+    for (int j = 0; j < 8; j++) p[(size_t)(n + j) * ld + row] = __float2bfloat16_rn(x[j]);
+}
+
+// Epilogue of 8 accumulator values x = C[row, n .. n+7] (one thread).
+__device__ __forceinline__ void epilogue8(const EpiArgs &e, int row, int n, float (&x)[8], float &sq) {
+    float b[8], t[8], y[8];
+    switch (e.mode) {
+    case EPI_HIDDEN:
+        ld8(e.bias + n, b);
+#pragma unroll
+        for (int j = 0; j < 8; j++) { x[j] += b[j]; y[j] = gelu(x[j]); }
+        if (e.Z) st8(e.Z + (size_t)row * e.ldz + n, x);
+        st8h(e.H + (size_t)row * e.ldh + n, y);
+        if (e.HT) st8t(e.HT, e.ldht, row, n, y);
+        break;
+    case EPI_OUT_TRAIN:
+    case EPI_OUT_RESID:
+        ld8(e.bias + n, b);
+        ld8(e.target + (size_t)(e.t_row0 + row) * e.ldt + n, t);
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const float d = n + j < e.n_real ? x[j] + b[j] - t[j] : 0.f;
+            if (e.mode == EPI_OUT_TRAIN) {
+                sq += d * d;
+                y[j] = d * e.gscale;
+            } else {
+                sq += e.lam * d * d;
+                y[j] = d;
+            }
+        }
+        if (e.mode == EPI_OUT_TRAIN) {
+            st8h(e.H + (size_t)row * e.ldh + n, y);
+            st8t(e.HT, e.ldht, row, n, y);
+        } else {
+            st8(e.E32 + (size_t)row * e.lde + n, y);
+            st8h(e.H + (size_t)row * e.ldh + n, y);
+        }
+        break;
+    case EPI_OUT_INFER:
+        ld8(e.bias + n, b);
+#pragma unroll
+        for (int j = 0; j < 8; j++) x[j] += b[j];
+        st8(e.out + (size_t)row * e.ldo + n, x);
+        break;
+    case EPI_PROJ:
+#pragma unroll
+        for (int j = 0; j < 8; j++) sq += x[j] * x[j];
+        st8h(e.H + (size_t)row * e.ldh + n, x);
+        break;
+    case EPI_LOSS_GRAD:
+        ld8(e.E32 + (size_t)row * e.lde + n, t);
+#pragma unroll
+        for (int j = 0; j < 8; j++) y[j] = (x[j] + e.lam * t[j]) * e.gscale;
+        st8h(e.H + (size_t)row * e.ldh + n, y);
+        st8t(e.HT, e.ldht, row, n, y);
+        break;
+    case EPI_BWD_HIDDEN:
+        ld8(e.Z + (size_t)row * e.ldz + n, t);
+#pragma unroll
+        for (int j = 0; j < 8; j++) y[j] = x[j] * gelu_grad(t[j]);
+        st8h(e.H + (size_t)row * e.ldh + n, y);
+        st8t(e.HT, e.ldht, row, n, y);
+        break;
+    default:  // EPI_WGRAD_STORE
+        st8(e.out + (size_t)row * e.ldo + n, x);
+        break;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // the GEMM
 // ---------------------------------------------------------------------------
@@ -288,102 +376,65 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             // copies issued but never consumed are still in flight: wait for them
             for (int kt = *consumed; kt < *issued; kt++) (void)mbar_wait(&full[kt % STAGES], (kt / STAGES) & 1);
         }
+    } else if (e.mode == EPI_WGRAD_ADAM) {
+        // Adam over the gradient tile, staged through shared memory (the
+        // operand ring is idle once the accumulator is complete) so that each
+        // warp then walks whole rows: float4 accesses to the fp32 master
+        // weights and moments, 4 bf16 weights per lane.  Row stride 132 floats
+        // keeps the float4 stores of 8 consecutive rows on distinct banks.
+        constexpr int kLd = BN + 4;
+        float *tile = (float *)smem;
+        for (int c = 0; c < BN / 16; c++) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v);
+            float4 *d = (float4 *)(tile + (warp * 32 + lane) * kLd + c * 16);
+#pragma unroll
+            for (int k = 0; k < 4; k++) d[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+        }
+        __syncthreads();
+        const int ti = *e.adam_t + 1;
+        const float t = (float)ti, lr = sched_lr(e.lr, e.sched, ti);
+        const float c1 = 1.f / (1.f - powf(e.b1, t)), c2 = 1.f / (1.f - powf(e.b2, t));
+        const int col = lane * 4, n = n0 + col;
+        for (int r = warp; r < BM; r += kGemmThreads / 32) {
+            const int m = m0 + r;
+            if (m >= e.M || n >= e.N) continue;
+            const float4 g = *(const float4 *)(tile + r * kLd + col);
+            const size_t i = (size_t)m * e.ldw + n;
+            float4 w = *(const float4 *)(e.Wm + i), am = *(const float4 *)(e.Am + i), av = *(const float4 *)(e.Av + i);
+            float *wp = &w.x, *mp = &am.x, *vp = &av.x;
+            const float *gp = &g.x;
+            __align__(8) bf16 wb[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                mp[k] = e.b1 * mp[k] + (1.f - e.b1) * gp[k];
+                vp[k] = e.b2 * vp[k] + (1.f - e.b2) * gp[k] * gp[k];
+                wp[k] -= lr * (mp[k] * c1) / (sqrtf(vp[k] * c2) + e.eps);
+                wb[k] = __float2bfloat16_rn(wp[k]);
+            }
+            *(float4 *)(e.Wm + i) = w;
+            *(float4 *)(e.Am + i) = am;
+            *(float4 *)(e.Av + i) = av;
+            *(uint2 *)(e.Wb + (size_t)m * e.ldwb + n) = *(const uint2 *)wb;
+        }
     } else {
         const int row = m0 + warp * 32 + lane;
         const bool rv = row < e.M;
         float sq = 0.f;
-        float adam_c1 = 0.f, adam_c2 = 0.f, lr = e.lr;
-        if (e.mode == EPI_WGRAD_ADAM) {
-            const int ti = *e.adam_t + 1;
-            const float t = (float)ti;
-            adam_c1 = 1.f / (1.f - powf(e.b1, t));
-            adam_c2 = 1.f / (1.f - powf(e.b2, t));
-            lr = sched_lr(e.lr, e.sched, ti);
-        }
         for (int c = 0; c < BN / 16; c++) {
             const int nb = n0 + c * 16;
             if (nb >= e.N) break;  // uniform across the CTA
             float v[16];
             tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v);
             if (!rv) continue;
-            const int nv = min(16, e.N - nb);
-            switch (e.mode) {
-            case EPI_HIDDEN:
-                for (int j = 0; j < nv; j++) {
-                    const int n = nb + j;
-                    const float z = v[j] + e.bias[n];
-                    const bf16 h = __float2bfloat16_rn(gelu(z));
-                    if (e.Z) e.Z[(size_t)row * e.ldz + n] = z;
-                    e.H[(size_t)row * e.ldh + n] = h;
-                    if (e.HT) e.HT[(size_t)n * e.ldht + row] = h;
-                }
-                break;
-            case EPI_OUT_TRAIN:
-                for (int j = 0; j < nv; j++) {
-                    const int n = nb + j;
-                    float d = 0.f;
-                    if (n < e.n_real) d = v[j] + e.bias[n] - e.target[(size_t)(e.t_row0 + row) * e.ldt + n];
-                    sq += d * d;
-                    const bf16 g = __float2bfloat16_rn(d * e.gscale);
-                    e.H[(size_t)row * e.ldh + n] = g;
-                    e.HT[(size_t)n * e.ldht + row] = g;
-                }
-                break;
-            case EPI_OUT_INFER:
-                for (int j = 0; j < nv; j++) e.out[(size_t)row * e.ldo + nb + j] = v[j] + e.bias[nb + j];
-                break;
-            case EPI_OUT_RESID:
-                for (int j = 0; j < nv; j++) {
-                    const int n = nb + j;
-                    float d = 0.f;
-                    if (n < e.n_real) d = v[j] + e.bias[n] - e.target[(size_t)(e.t_row0 + row) * e.ldt + n];
-                    sq += e.lam * d * d;
-                    e.E32[(size_t)row * e.lde + n] = d;
-                    e.H[(size_t)row * e.ldh + n] = __float2bfloat16_rn(d);
-                }
-                break;
-            case EPI_PROJ:
-                for (int j = 0; j < nv; j++) {
-                    sq += v[j] * v[j];
-                    e.H[(size_t)row * e.ldh + nb + j] = __float2bfloat16_rn(v[j]);
-                }
-                break;
-            case EPI_LOSS_GRAD:
-                for (int j = 0; j < nv; j++) {
-                    const int n = nb + j;
-                    const float d = e.E32[(size_t)row * e.lde + n];
-                    const bf16 g = __float2bfloat16_rn((v[j] + e.lam * d) * e.gscale);
-                    e.H[(size_t)row * e.ldh + n] = g;
-                    e.HT[(size_t)n * e.ldht + row] = g;
-                }
-                break;
-            case EPI_BWD_HIDDEN:
-                for (int j = 0; j < nv; j++) {
-                    const int n = nb + j;
-                    const bf16 g = __float2bfloat16_rn(v[j] * gelu_grad(e.Z[(size_t)row * e.ldz + n]));
-                    e.H[(size_t)row * e.ldh + n] = g;
-                    e.HT[(size_t)n * e.ldht + row] = g;
-                }
-                break;
-            case EPI_WGRAD_ADAM:
-                for (int j = 0; j < nv; j++) {
-                    const int n = nb + j;
-                    const size_t i = (size_t)row * e.ldw + n;
-                    const float g = v[j];
-                    const float m = e.b1 * e.Am[i] + (1.f - e.b1) * g;
-                    const float s = e.b2 * e.Av[i] + (1.f - e.b2) * g * g;
-                    const float w = e.Wm[i] - lr * (m * adam_c1) / (sqrtf(s * adam_c2) + e.eps);
-                    e.Am[i] = m;
-                    e.Av[i] = s;
-                    e.Wm[i] = w;
-                    const bf16 wb = __float2bfloat16_rn(w);
-                    e.Wb[(size_t)row * e.ldwb + n] = wb;
-                    if (e.Wt) e.Wt[(size_t)n * e.ldwt + row] = wb;
-                }
-                break;
-            default:  // EPI_WGRAD_STORE
-                for (int j = 0; j < nv; j++) e.out[(size_t)row * e.ldo + nb + j] = v[j];
-                break;
+            // N is a multiple of 8: two groups of 8 columns, vector accesses
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (nb + 8 * h >= e.N) break;
+                float x[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) x[j] = v[8 * h + j];
+                epilogue8(e, row, nb + 8 * h, x, sq);
             }
         }
         if (e.mode == EPI_OUT_TRAIN || e.mode == EPI_OUT_RESID || e.mode == EPI_PROJ) {
@@ -464,6 +515,21 @@ __global__ void k_transpose_batches(const bf16 *Xs, int kin, int B, bf16 *XT) {
         if (i < B && k < kin) XT[((size_t)b * kin + k) * B + i] = tile[threadIdx.x][y];
     }
 }
+// Wt [cols, rows] = W^T for bf16 W [rows, cols], through 32 x 32 tiles.
+__global__ void k_transpose_bf16(const bf16 *W, int rows, int cols, bf16 *Wt) {
+    __shared__ bf16 tile[32][34];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int r = r0 + y, c = c0 + threadIdx.x;
+        if (r < rows && c < cols) tile[y][threadIdx.x] = W[(size_t)r * cols + c];
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int c = c0 + y, r = r0 + threadIdx.x;
+        if (r < rows && c < cols) Wt[(size_t)c * rows + r] = tile[threadIdx.x][y];
+    }
+}
+
 // bf16 weights and their transpose from the fp32 master weights
 __global__ void k_cast_weights(const float *Wm, int out, int in, bf16 *Wb, bf16 *Wt) {
     const long long total = (long long)out * in;
@@ -871,6 +937,11 @@ gbpf_status gbpf_mlp::backward(cudaStream_t st, Work &w, const CUtensorMap &mXT,
         }
         const CUtensorMap &mIn = l == 0 ? mXT : w.mHT[l - 1];
         if ((s = gemm(st, mGT, mIn, L[l].out, L[l].in, M, e)) != GBPF_OK) return s;
+        if (adam) {
+            k_transpose_bf16<<<dim3((L[l].in + 31) / 32, (L[l].out + 31) / 32), dim3(32, 8), 0, st>>>(
+                L[l].Wb, L[l].out, L[l].in, L[l].Wt);
+            CK(cudaGetLastError());
+        }
     }
     if (has_skip) {
         // the skip's gradient dY^T X; its transpose is never needed
