@@ -253,32 +253,42 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
-# ---------------------------------------------------------------------- GPU
-def max_over_ranks(x, dist, device):
+# ------------------------------------------------------------- multi-rank
+def shard_seed(seed, rank):
+    """Weak scaling: every rank solves its own scenarios, drawn with this seed
+    (instances are independent, so the data path has no collective)."""
+    return seed + 1000 * rank
+
+
+def _reduce(x, dist, device, op):
     if not dist:
         return x
     import torch
 
-    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    on_gpu = dist.get_backend() == "nccl"
+    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}" if on_gpu else "cpu")
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(x, dist, device):
+    """Step time of the job: the slowest rank."""
+    return _reduce(x, dist, device, dist.ReduceOp.MAX) if dist else x
 
 
 def sum_over_ranks(x, dist, device):
-    if not dist:
-        return x
-    import torch
+    """Converged solves of the job: all ranks."""
+    return _reduce(x, dist, device, dist.ReduceOp.SUM) if dist else x
 
-    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+
+# ---------------------------------------------------------------------- GPU
 
 
 def bench_batch(a, gb, np, rank, dev, world, dist):
     if a.workload == "c4":
         sizes = [14, 30, 57, 118, 236, 472]
         grids = [gb.generate(4, BASE_SEED + 4 + 1000 * i, nbus=nb) for i, nb in enumerate(sizes)]
-        rng = np.random.default_rng(BASE_SEED + 4 + 97 * rank)
+        rng = np.random.default_rng(shard_seed(BASE_SEED + 4, rank))
         gi = rng.integers(0, len(grids), N_SCEN).astype(np.int32)
         cols = {k: [] for k in ("Pload", "Qload", "Pg")}
         for t in gi:
@@ -295,7 +305,7 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
         cdf = write_grid(g0)
         grids = [gb.read_grid(cdf)]
         base = grids[0].buses()
-        Pl, Ql, Pg = scenarios(np, base, N_SCEN, BASE_SEED + 7 + 1000 * rank)
+        Pl, Ql, Pg = scenarios(np, base, N_SCEN, shard_seed(BASE_SEED + 7, rank))
         Pl, Ql, Pg = Pl.ravel(), Ql.ravel(), Pg.ravel()
         gi = np.zeros(N_SCEN, np.int32)
         desc = "118-bus synthetic meshed grid (1 slack/53 PV/64 PQ, 186 branches), 4096 load scenarios"
@@ -414,7 +424,7 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
     nB, base = grid.nB, grid.buses()
     opts = dict(tolerancia=1e-8, no_max_iter=30, lim_inj_reat=0)
     # training set: solutions of the plain Newton method (batched FP64, flat start)
-    Pl, Ql, Pg = c5_scenarios(np, base, C5_TRAIN, BASE_SEED + 5 + 1000 * rank)
+    Pl, Ql, Pg = c5_scenarios(np, base, C5_TRAIN, shard_seed(BASE_SEED + 5, rank))
     gen = gb.Batch([grid], device=dev, precision=gb.PREC_FP64, **opts)
     t0 = time.perf_counter()
     gen.set_instances(np.zeros(C5_TRAIN, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
@@ -439,7 +449,7 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
         train_ms / 1e3) / 1e12
     del X, Y, V, th
     # held-out scenarios
-    Pt, Qt, Gt = c5_scenarios(np, base, C5_TEST, BASE_SEED + 5 + 7 + 1000 * rank)
+    Pt, Qt, Gt = c5_scenarios(np, base, C5_TEST, shard_seed(BASE_SEED + 12, rank))
     gi = np.zeros(C5_TEST, np.int32)
     inputs = dict(Pload=Pt.ravel(), Qload=Qt.ravel(), Pg=Gt.ravel())
     ref = gb.Batch([grid], device=dev, precision=gb.PREC_FP64, **opts)
