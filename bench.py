@@ -55,6 +55,10 @@ def args():
     p.add_argument("--impl", default="gbpf", choices=["gbpf", "reference"])
     p.add_argument("--workload", default="c2", choices=["c2", "c2-plain", "c3", "c4", "c5"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--scenarios", type=int, default=0,
+                   help="scenarios per step (c2, c4: default 4096; c5: held-out, default 8192); smaller cases "
+                        "for profiler captures")
+    p.add_argument("--train", type=int, default=0, help="c5 training solves (default 50000)")
     return p.parse_args()
 
 
@@ -285,6 +289,7 @@ def sum_over_ranks(x, dist, device):
 
 
 def bench_batch(a, gb, np, rank, dev, world, dist):
+    N_SCEN = a.scenarios or globals()["N_SCEN"]
     if a.workload == "c4":
         sizes = [14, 30, 57, 118, 236, 472]
         grids = [gb.generate(4, BASE_SEED + 4 + 1000 * i, nbus=nb) for i, nb in enumerate(sizes)]
@@ -420,6 +425,8 @@ def train_flops_per_step(nb, width, B, k_metric):
 
 
 def bench_c5(a, gb, np, rank, dev, world, dist):
+    C5_TRAIN = a.train or globals()["C5_TRAIN"]
+    C5_TEST = a.scenarios or globals()["C5_TEST"]
     grid = gb.generate(3, BASE_SEED + 5, tiles=16)
     nB, base = grid.nB, grid.buses()
     opts = dict(tolerancia=1e-8, no_max_iter=30, lim_inj_reat=0)

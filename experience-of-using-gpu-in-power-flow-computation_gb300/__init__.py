@@ -41,7 +41,7 @@ EXPORTS = [
     "gbpf_batch_results", "gbpf_batch_events", "gbpf_batch_info", "gbpf_batch_solve_noalloc",
     "gbpf_mlp_create", "gbpf_mlp_free", "gbpf_mlp_dims", "gbpf_mlp_set_data", "gbpf_mlp_train", "gbpf_mlp_predict",
     "gbpf_mlp_gradients", "gbpf_mlp_params", "gbpf_mlp_set_params", "gbpf_mlp_norm", "gbpf_mlp_set_norm",
-    "gbpf_batch_solve_warm", "gbpf_mlp_set_loss_metric",
+    "gbpf_batch_solve_warm", "gbpf_mlp_set_loss_metric", "gbpf_solver_setup_times",
 ]
 
 

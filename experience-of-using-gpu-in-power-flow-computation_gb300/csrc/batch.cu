@@ -820,71 +820,80 @@ __global__ void k_ws_features(const double *Pliq, const double *Qliq, const doub
     }
 }
 
-// max |g| of the first Newton iteration at the phasors ef (e = V cos th,
-// f = V sin th) of one instance: P rows of the non-slack buses, Q rows of the
-// PQ buses, as the mismatch of k_nr_block / k_nr_warp at iteration 0.
-__device__ double ws_mismatch(const TopoView &G, int nB, const double2 *ef, const double *Pliq, const double *Qliq,
-                              int lane) {
-    double mx = 0;
-    for (int k = lane; k < nB; k += 32) {
-        const int ty = G.type[k];
-        if (ty == 3) continue;
-        double ir = 0, ii = 0;
-        for (int p = G.yptr[k]; p < G.yptr[k + 1]; p++) {
-            const double2 y = G.yval[p], u = ef[G.ycol[p]];
-            ir += y.x * u.x - y.y * u.y;
-            ii += y.x * u.y + y.y * u.x;
-        }
-        const double2 u = ef[k];
-        double t = fabs(Pliq[k] - (u.x * ir + u.y * ii));
-        if (ty == 0 || ty == 1) t = fmax(t, fabs(Qliq[k] - (u.y * ir - u.x * ii)));
-        if (t != t) t = INFINITY;
-        mx = fmax(mx, t);
-    }
-    return warp_max(mx);
-}
-
-// One warp per instance: the predicted start (|V| of the PQ buses and theta of
-// the non-slack buses from the network; the PV set points and the slack angle
-// from the instance's own start) is kept when its initial mismatch is below
+// One block per instance: the predicted start (|V| of the PQ buses and theta
+// of the non-slack buses from the network; the PV set points and the slack
+// angle from the instance's own start) is kept when its initial mismatch --
+// max |g| of the first Newton iteration: P rows of the non-slack buses, Q rows
+// of the PQ buses, as in k_nr_block / k_nr_warp at iteration 0 -- is below
 // that of the instance's own (flat) start; otherwise the own start is used.
-// Writes the chosen start to sV/sTh and kind[inst] = 1 (predicted) or 0.
-__global__ void k_ws_select(Args a, const float *pred, int ldp, const float *omean, const float *oscale, double *sV,
-                            double *sTh, double2 *ef, int *kind) {
-    const int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (inst >= a.n_inst) return;
+// Both mismatches come out of one pass over the Ybus rows.  Writes the chosen
+// start to sV/sTh and kind[inst] = 1 (predicted) or 0.  ef holds the phasors
+// (V cos th, V sin th) of both starts, interleaved per bus.
+constexpr int kSelThreads = 256;
+__global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *pred, int ldp, const float *omean,
+                                                           const float *oscale, double *sV, double *sTh, double4_32a *ef,
+                                                           int *kind) {
+    __shared__ double red[2][kSelThreads / 32];
+    const int inst = blockIdx.x, tid = threadIdx.x;
     const Topo T = a.topo[a.inst_topo[inst]];
     const TopoView G = bind(T.o, T.blob);
     const long long off = a.inst_off[inst];
     const int nB = T.nB;
     const float *pr = pred + (size_t)inst * ldp;
-    for (int k = lane; k < nB; k += 32) {
+    double4_32a *e = ef + off;
+    for (int k = tid; k < nB; k += kSelThreads) {
         const int ty = G.type[k];
-        const double v = (ty == 0 || ty == 1) ? (double)pr[k] * oscale[k] + omean[k] : a.V0[off + k];
-        const double t = ty == 3 ? a.th0[off + k] : (double)pr[nB + k] * oscale[nB + k] + omean[nB + k];
+        const double v0 = a.V0[off + k], t0 = a.th0[off + k];
+        const double v = (ty == 0 || ty == 1) ? (double)pr[k] * oscale[k] + omean[k] : v0;
+        const double t = ty == 3 ? t0 : (double)pr[nB + k] * oscale[nB + k] + omean[nB + k];
         sV[off + k] = v;
         sTh[off + k] = t;
-        double s, c;
+        double s, c, s0, c0;
         sincos(t, &s, &c);
-        ef[off + k] = make_double2(v * c, v * s);
+        sincos(t0, &s0, &c0);
+        e[k] = double4_32a{v * c, v * s, v0 * c0, v0 * s0};
     }
-    __syncwarp();
-    const double mc = ws_mismatch(G, nB, ef + off, a.Pliq + off, a.Qliq + off, lane);
-    __syncwarp();
-    for (int k = lane; k < nB; k += 32) {
-        double s, c;
-        sincos(a.th0[off + k], &s, &c);
-        ef[off + k] = make_double2(a.V0[off + k] * c, a.V0[off + k] * s);
+    __syncthreads();
+    double mp = 0, mf = 0;
+    for (int k = tid; k < nB; k += kSelThreads) {
+        const int ty = G.type[k];
+        if (ty == 3) continue;
+        double ir = 0, ii = 0, jr = 0, ji = 0;
+        for (int p = G.yptr[k]; p < G.yptr[k + 1]; p++) {
+            const double2 y = G.yval[p];
+            const double4_32a u = e[G.ycol[p]];
+            ir += y.x * u.x - y.y * u.y;
+            ii += y.x * u.y + y.y * u.x;
+            jr += y.x * u.z - y.y * u.w;
+            ji += y.x * u.w + y.y * u.z;
+        }
+        const double4_32a u = e[k];
+        const double pl = a.Pliq[off + k];
+        double tp = fabs(pl - (u.x * ir + u.y * ii)), tf = fabs(pl - (u.z * jr + u.w * ji));
+        if (ty == 0 || ty == 1) {
+            const double ql = a.Qliq[off + k];
+            tp = fmax(tp, fabs(ql - (u.y * ir - u.x * ii)));
+            tf = fmax(tf, fabs(ql - (u.w * jr - u.z * ji)));
+        }
+        if (tp != tp) tp = INFINITY;
+        if (tf != tf) tf = INFINITY;
+        mp = fmax(mp, tp);
+        mf = fmax(mf, tf);
     }
-    __syncwarp();
-    const double mf = ws_mismatch(G, nB, ef + off, a.Pliq + off, a.Qliq + off, lane);
-    const bool use = mc < mf;
+    mp = warp_max(mp);
+    mf = warp_max(mf);
+    if ((tid & 31) == 0) { red[0][tid >> 5] = mp; red[1][tid >> 5] = mf; }
+    __syncthreads();
+    mp = red[0][0];
+    mf = red[1][0];
+    for (int w = 1; w < kSelThreads / 32; w++) { mp = fmax(mp, red[0][w]); mf = fmax(mf, red[1][w]); }
+    const bool use = mp < mf;
     if (!use)
-        for (int k = lane; k < nB; k += 32) {
+        for (int k = tid; k < nB; k += kSelThreads) {
             sV[off + k] = a.V0[off + k];
             sTh[off + k] = a.th0[off + k];
         }
-    if (lane == 0) kind[inst] = use ? 1 : 0;
+    if (tid == 0) kind[inst] = use ? 1 : 0;
 }
 
 // A converged instance that started from the prediction is rejected (kind 3,
@@ -1018,7 +1027,7 @@ struct gbpf_batch {
     __nv_bfloat16 *wX = nullptr;
     float *wPred = nullptr;
     double *wV = nullptr, *wTh = nullptr;
-    double2 *wEF = nullptr;
+    double4_32a *wEF = nullptr;
     int *wKind = nullptr, *wQueue = nullptr;
     gbpf_status launch(cudaStream_t st);
     gbpf_status launch_with(cudaStream_t st, const Args &ba, const Args &wa);
@@ -1368,11 +1377,11 @@ gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, 
         warm_mem.reset();
         const size_t xb = align_up(2 * (size_t)n_inst * sh.kin, 256), pb = align_up(4 * (size_t)n_inst * sh.outp, 256),
                      vb = align_up(8 * (size_t)n_bus_total, 256), ib = align_up(4 * (size_t)n_inst, 256);
-        CK(cudaMalloc(&warm_mem.p, xb + pb + 4 * vb + 2 * ib));
+        CK(cudaMalloc(&warm_mem.p, xb + pb + 6 * vb + 2 * ib));
         char *p = (char *)warm_mem.p;
         wX = (__nv_bfloat16 *)p; wPred = (float *)(p + xb);
-        wV = (double *)(p + xb + pb); wTh = (double *)(p + xb + pb + vb); wEF = (double2 *)(p + xb + pb + 2 * vb);
-        wKind = (int *)(p + xb + pb + 4 * vb); wQueue = (int *)(p + xb + pb + 4 * vb + ib);
+        wV = (double *)(p + xb + pb); wTh = (double *)(p + xb + pb + vb); wEF = (double4_32a *)(p + xb + pb + 2 * vb);
+        wKind = (int *)(p + xb + pb + 6 * vb); wQueue = (int *)(p + xb + pb + 6 * vb + ib);
         warm_n = n_inst;
     }
     CK(cudaEventRecord(ev0, stream));
@@ -1381,8 +1390,8 @@ gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, 
     CK(cudaGetLastError());
     gbpf_status st = gbpf::mlp_infer(m, wX, n_inst, wPred, stream);
     if (st != GBPF_OK) return st;
-    k_ws_select<<<(n_inst * 32 + 255) / 256, 256, 0, stream>>>(args, wPred, sh.outp, sh.out_mean, sh.out_scale, wV,
-                                                                 wTh, wEF, wKind);
+    k_ws_select<<<n_inst, kSelThreads, 0, stream>>>(args, wPred, sh.outp, sh.out_mean, sh.out_scale, wV, wTh, wEF,
+                                                     wKind);
     CK(cudaGetLastError());
     Args ba = args, wa = wargs;
     ba.V0 = wa.V0 = wV;

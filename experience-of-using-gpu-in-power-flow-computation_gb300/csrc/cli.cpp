@@ -3,10 +3,14 @@
 // given as the first argument), reads arq_entrada, solves on the GPU and prints
 // what the reference prints: the option echo, the method banner, the GPU
 // banner, the reactive-limit lines and max(g) trace, and the per-bus table of
-// impressao2 (GPU/impressao.h:47-80).
+// impressao2 (GPU/impressao.h:47-80), then the execution report on screen
+// (benchmarksPrint, GPU/impressao.h:125-337) and the benchmark CSV row
+// (benchmarksPrintFile, GPU/impressao.h:339-558).
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <string>
 #include <vector>
 
@@ -15,6 +19,129 @@
 static const char *EVENT_TEXT[6] = {
     "", "PV -> PQ (limite superior)", "PQ (limite inferior) -> PQ (limite superior)",
     "PV -> PQ (limite inferior)", "PQ (limite superior) -> PQ (limite inferior)", "PQ -> PV"};
+
+// Times of one run in the reference's benchmark categories (ms).  Set-up
+// phases are wall times measured by the library; the Newton phases are the
+// device time of one pass of each phase (gbpf_solver_profile) -- the Newton
+// loop runs as one CUDA graph, so there is no host-side timer per iteration.
+struct RunTimes {
+    double total = 0, ybus = 0, alloc = 0, upload = 0, lib = 0, stencil = 0;
+    double pq_pass = 0, jac_pass = 0, lin_pass = 0, processo = 0, fluxo = 0;
+    int iters = 0, pq_passes = 0;
+};
+
+static std::string met2str(const gbpf_options &o) {  // GPU/impressao.h:82-101, hibridoC of :342-347
+    switch (o.metodo) {
+    case GBPF_METODO_DENSO: return "denso";
+    case GBPF_METODO_ESPARSO: return "esparso";
+    case GBPF_METODO_HIBRIDOA: return "hibridoA";
+    case GBPF_METODO_HIBRIDOB: return "hibridoB";
+    case GBPF_METODO_HIBRIDOC: return "hibridoC";
+    default: return "nda";
+    }
+}
+
+// printDoubleToFile (GPU/impressao.h:119-123): "%f" with a decimal comma, then ';'
+static std::string csv_num(double x) {
+    char b[64];
+    std::snprintf(b, sizeof b, "%f", x);
+    std::string s(b);
+    const size_t p = s.find('.');
+    if (p != std::string::npos) s[p] = ',';
+    return s + ";";
+}
+
+// The benchmark CSV row of benchmarksPrintFile: file out_<double|float>_<metodo>-<input
+// without extension>.csv, created with the reference's two header lines (byte
+// for byte, including the replacement characters its source file carries),
+// one row appended per run, numbered by the lines already in the file.
+static void write_csv(const gbpf_options &o, const RunTimes &t) {
+    std::string in = o.arq_entrada;
+    const size_t dot = in.find_last_of('.');
+    const std::string name = std::string("out_") + (o.precision == GBPF_PREC_FP32_IR ? "float_" : "double_") +
+                             met2str(o) + "-" + in.substr(0, dot) + ".csv";
+    unsigned n = 1;
+    {
+        std::ifstream f(name, std::ios::binary);
+        if (f.good()) {
+            unsigned lines = 0;
+            char c;
+            while (f.get(c)) lines += c == '\n';
+            n = lines - 1;
+        } else {
+            std::ofstream h(name, std::ios::binary);
+            h << "Execucao;Aviso;ms total;no iteracoes;ms Ybus;ms Init GPU;;;ms Inicializacao;ms calcPQ;;"
+                 "ms Jacobiano;;ms Sistema Linear;;ms Processo;ms Fluxo;\n;;;;;total; Aloca\xEF\xBF\xBD\xEF\xBF\xBDo "
+                 "Vari\xEF\xBF\xBDveis iniciais; Aloca\xEF\xBF\xBD\xEF\xBF\xBDo de vari\xEF\xBF\xBDveis esparsas; "
+                 "Biblioteca; total; medio por iteracao; total; medio por iteracao; total; medio por iteracao; "
+                 "Iterativo;\n";
+        }
+    }
+    const double it = (double)t.iters;
+    const bool dense = o.metodo == GBPF_METODO_DENSO;
+    std::string row = std::to_string(n) + ";" + ";" + csv_num(t.total) + std::to_string(t.iters) + ";";
+    row += csv_num(t.ybus) + csv_num(t.alloc + t.upload) + csv_num(t.alloc) + csv_num(t.upload) + csv_num(t.lib);
+    row += csv_num(t.pq_pass * t.pq_passes) + csv_num(t.pq_pass * t.pq_passes / it);
+    const double jac = t.jac_pass * t.iters + (dense ? 0.0 : t.stencil);
+    row += csv_num(jac) + csv_num(jac / it);
+    row += csv_num(t.lin_pass * t.iters) + csv_num(t.lin_pass * t.iters / it);
+    row += csv_num(t.processo) + csv_num(t.fluxo) + "\n";
+    std::ofstream f(name, std::ios::binary | std::ios::app);
+    f << row;
+}
+
+// The execution report of benchmarksPrint (BENCHMARK_MODE on).
+static void print_report(const gbpf_options &o, const RunTimes &t) {
+    const bool dense = o.metodo == GBPF_METODO_DENSO;
+    std::printf("\n Relatorio de execucao:\n\n");
+    std::printf("*Geral***********************************\n\n ");
+    std::printf(" Tempo total de execucao: %f ms.\n Numero de iteracoes: %d.\n\n", t.total, t.iters);
+    std::printf("*Ybus************************************\n\n");
+    std::printf(" Tempo total: %f ms.\n\n", t.ybus);
+    std::printf("*Init GPU********************************\n\n");
+    std::printf(" acao                        -  tempo de execucao\n");
+    std::printf(" alocacao de memoria inicial - %14f ms (alem do inicio da comunicacao com a GPU)\n", t.alloc);
+    std::printf(" alocacao de varia. esparsas - %14f ms\n", t.upload);
+    std::printf("-----------------------------\n");
+    std::printf(" Tempo total: %f ms.\n\n", t.alloc + t.upload);
+    std::printf("*Inicializacao das Bibliotecas***********\n\n");
+    std::printf(" Tempo total: %f ms.\n\n", t.lib);
+    std::printf("*CalcPQ**********************************\n\n");
+    std::printf("*Tempo nao inclui transferencias de dados para o host!\n\n");
+    std::printf(" iteracao - tempo de execucao\n");
+    for (int i = 0; i < t.pq_passes; i++) std::printf(" %8d - %14f ms\n", i, t.pq_pass);
+    std::printf("-----------------------------\n");
+    std::printf(" Tempo total: %f ms.\n", t.pq_pass * t.pq_passes);
+    std::printf(" Tempo medio: %f ms.\n\n", t.pq_pass * t.pq_passes / (double)t.iters);
+    if (dense) {
+        std::printf("*Jacobiano*******************************\n\n");
+        std::printf(" iteracao - tempo de execucao\n");
+        for (int i = 0; i < t.iters; i++) std::printf(" %8d - %14f ms\n", i, t.jac_pass);
+        std::printf("-----------------------------\n");
+        std::printf(" Tempo total: %f ms.\n", t.jac_pass * t.iters);
+        std::printf(" Tempo medio: %f ms.\n\n", t.jac_pass * t.iters / (double)t.iters);
+    } else {
+        const double tot = t.stencil + t.jac_pass * t.iters;
+        std::printf("*Jacobiano Stencil***********************\n");
+        std::printf("  acao  - iteracao - tempo de execucao\n");
+        std::printf(" constr - %8d - %14f ms\n", 0, t.stencil);
+        for (int i = 0; i < t.iters; i++) std::printf(" preenc - %8d - %14f ms\n", i, t.jac_pass);
+        std::printf("-----------------------------\n");
+        std::printf(" Tempo total: %f ms.\n", tot);
+        std::printf(" Tempo medio: %f ms (por iteracao).\n\n", tot / (double)t.iters);
+    }
+    std::printf("*Sistema Linear**************************\n\n");
+    std::printf(" iteracao - tempo de execucao\n");
+    for (int i = 0; i < t.iters; i++) std::printf(" %8d - %14f ms\n", i, t.lin_pass);
+    std::printf("-----------------------------\n");
+    std::printf(" Tempo total: %f ms.\n", t.lin_pass * t.iters);
+    std::printf(" Tempo medio: %f ms.\n\n", t.lin_pass * t.iters / (double)t.iters);
+    std::printf("*Processo Iterativo**********************\n\n");
+    std::printf(" Tempo total: %f ms.\n\n", t.processo);
+    std::printf("*Fluxo***********************************\n\n");
+    std::printf(" Tempo total: %f ms.\n\n", t.fluxo);
+    std::printf("*****************************************\n");
+}
 
 static int fail(const char *what, gbpf_status st) {
     std::fprintf(stderr, "gbpf: %s: %s (%s)\n", what, gbpf_status_str(st), gbpf_last_error());
@@ -83,12 +210,30 @@ int main(int argc, char **argv) {
                     128 * props[5]);
     }
 
+    using clk = std::chrono::steady_clock;
+    auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
+    RunTimes tm;
+    const auto t_start = clk::now();
     gbpf_solver *s = nullptr;
     st = gbpf_solver_create(g, &o, 0, &s);
     if (st != GBPF_OK) return fail("solver setup", st);
     gbpf_result r{};
+    auto t0 = clk::now();
     st = gbpf_solve(s, &r);
+    tm.processo = ms_since(t0);
     if (st != GBPF_OK && st != GBPF_E_NOCONV) return fail("solve", st);
+    {
+        int dims[8];
+        gbpf_grid_dims(g, dims);
+        std::vector<double> a(dims[0]), b(dims[0]), c(dims[0]), d(dims[0]), f(4 * (size_t)dims[1] + 4);
+        gbpf_solver_state(s, a.data(), b.data(), c.data(), d.data());
+        t0 = clk::now();
+        gbpf_solver_flows(s, f.data(), f.data() + dims[1], f.data() + 2 * dims[1], f.data() + 3 * dims[1]);
+        tm.fluxo = ms_since(t0);
+    }
+    tm.total = ms_since(t_start);
+    tm.iters = r.iterations;
+    tm.pq_passes = r.converged ? r.iterations + 1 : r.iterations;
 
     // trace of mNR in iteration order: limit lines (GPU/limiteInjReat.cuh:6-34)
     // and max(g) (GPU/newtonRaphson.cuh:418-420)
@@ -142,8 +287,24 @@ int main(int argc, char **argv) {
             }
         }
     }
-    if (!o.laconic_mode && (o.output_bench == GBPF_BENCH_SCREEN || o.output_bench == GBPF_BENCH_ALL))
-        std::printf("\n\niteracoes: %d\n", r.iterations);
+    const bool to_file = o.laconic_mode || o.output_bench == GBPF_BENCH_ALL || o.output_bench == GBPF_BENCH_FILE;
+    const bool to_screen = !o.laconic_mode && (o.output_bench == GBPF_BENCH_SCREEN || o.output_bench == GBPF_BENCH_ALL);
+    if (to_file || to_screen) {
+        double setup[5] = {0, 0, 0, 0, 0}, ph[4] = {0, 0, 0, 0};
+        long long bytes[4];
+        gbpf_solver_setup_times(s, setup);
+        if (gbpf_solver_profile(s, 5, ph, bytes) != GBPF_OK) std::fill(ph, ph + 4, 0.0);
+        tm.ybus = setup[0];
+        tm.alloc = setup[1];
+        tm.upload = setup[2];
+        tm.stencil = setup[3];
+        tm.lib = setup[4];
+        tm.pq_pass = ph[0];
+        tm.jac_pass = ph[1];
+        tm.lin_pass = ph[2] + ph[3];
+        if (to_file) write_csv(o, tm);
+        if (to_screen) print_report(o, tm);
+    }
     gbpf_solver_free(s);
     gbpf_grid_free(g);
     return 0;

@@ -21,6 +21,8 @@
 // is the same as that of the reference's reduced system.
 #include <cuda_runtime.h>
 
+#include <chrono>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -442,6 +444,9 @@ struct gbpf_solver {
     int graph_nodes = 0, kernels_per_iter = 0;
     Ctl last{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // wall ms of the set-up phases: Ybus, device allocation, uploads, symbolic
+    // analysis (ordering + factor structure), graph construction
+    double setup_ms[5] = {0, 0, 0, 0, 0};
 
     ~gbpf_solver() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -496,10 +501,17 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
     if (o.no_max_iter < 0) { set_error("no_max_iter < 0"); return GBPF_E_INPUT; }
     for (int b = 0; b < g.nL; b++)
         if (g.r[b] == 0.0 && g.x[b] == 0.0) { set_error("branch with zero impedance"); return GBPF_E_INPUT; }
+    using clk = std::chrono::steady_clock;
+    auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
+    auto tp = clk::now();
     y = gbpf::build_ypattern(g);
+    setup_ms[0] = ms_since(tp);
+    tp = clk::now();
     std::string why;
     S = gbpf::analyse(g, y, &why);
     if (S.n != g.nB - 1) { set_error("symbolic analysis failed: " + why); return GBPF_E_INPUT; }
+    setup_ms[3] = ms_since(tp);
+    tp = clk::now();
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&ev0));
@@ -575,6 +587,9 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
         }
     }
     CK(cudaMemsetAsync(dmem, 0, dmem_size, stream));
+    CK(cudaStreamSynchronize(stream));
+    setup_ms[1] = ms_since(tp);
+    tp = clk::now();
     auto up = [&](const void *dst, const void *src, size_t bytes) -> cudaError_t {
         if (!bytes) return cudaSuccess;
         return cudaMemcpyAsync(const_cast<void *>(dst), src, bytes, cudaMemcpyHostToDevice, stream);
@@ -626,13 +641,20 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
     CK(up(d.fl_phi, fphi.data(), nL * sizeof(double)));
     CK(up(d.fl_bkm, fbkm.data(), nL * sizeof(double)));
     CK(up(d.fl_bmk, fbmk.data(), nL * sizeof(double)));
+    CK(cudaStreamSynchronize(stream));
+    setup_ms[2] = ms_since(tp);
+    tp = clk::now();
     // Ybus on the device, once per topology
     const int T = 256;
     if (nL) k_ybus_stamps<<<cdiv_int(nL, T), T, 0, stream>>>(d);
     k_ybus_sum<<<cdiv_int(y.nnz, T), T, 0, stream>>>(d);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(stream));
-    return build_graph();
+    setup_ms[0] += ms_since(tp);
+    tp = clk::now();
+    const gbpf_status st = build_graph();
+    setup_ms[4] = ms_since(tp);
+    return st;
 }
 
 gbpf_status gbpf_solver::build_graph() {
@@ -836,6 +858,12 @@ extern "C" gbpf_status gbpf_solver_time(gbpf_solver *s, int repeats, double *ms_
 // 2 factorisation + forward substitution (all levels), 3 backward
 // substitution (all levels).  bytes[] = algorithmic bytes of one pass: every
 // array a phase reads or writes counted once.
+extern "C" gbpf_status gbpf_solver_setup_times(const gbpf_solver *s, double ms[5]) {
+    if (!s || !ms) { set_error("invalid argument: s && ms"); return GBPF_E_ARG; }
+    for (int i = 0; i < 5; i++) ms[i] = s->setup_ms[i];
+    return GBPF_OK;
+}
+
 extern "C" gbpf_status gbpf_solver_profile(gbpf_solver *s, int repeats, double ms[4], long long bytes[4]) {
     ARGCHECK(s && ms && bytes && repeats > 0);
     CK(cudaSetDevice(s->device));

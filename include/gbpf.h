@@ -223,6 +223,14 @@ gbpf_status gbpf_solver_info(const gbpf_solver *s, long long info[8]);
  * solver stream). */
 gbpf_status gbpf_solver_time(gbpf_solver *s, int repeats, double *ms_total);
 
+/* Wall ms of the set-up done by gbpf_solver_create: [0] Ybus (pattern on the
+ * host, values on the device; calcYbusSp_eficinte), [1] device allocation,
+ * [2] uploads of the grid and the factor structure (d_init* + cpyH2D of
+ * GPU/main.cu:94-130), [3] symbolic analysis: ordering and factor structure
+ * (Jstencil, GPU/limiteInjReat.cuh:220), [4] CUDA graph construction (the
+ * library set-up of GPU/newtonRaphson.cuh:198-265). */
+gbpf_status gbpf_solver_setup_times(const gbpf_solver *s, double ms[5]);
+
 /* Per-phase device time (ms per pass, CUDA events on the solver stream, the
  * last solve's state left on the device, `repeats` passes after one warm-up):
  * [0] injections + limits + mismatch, [1] Jacobian fill, [2] LU

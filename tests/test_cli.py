@@ -64,3 +64,35 @@ def test_cli_missing_data_txt(gb, tmp_path):
     out = subprocess.run([gb.CLI_PATH], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert out.returncode != 0
     assert "ERRO: A ABERTURA DO ARQUIVO FALHOU!" in out.stdout
+
+
+def test_cli_benchmark_csv_and_report(gb, tmp_path):
+    """benchmarksPrintFile / benchmarksPrint (GPU/impressao.h:125-558): the CSV
+    out_double_esparso-<input>.csv with the reference's two header lines, one
+    row per run numbered from 1, 17 ';'-separated fields with decimal commas;
+    the screen report with the total time and the iteration count."""
+    cdf = "c2_s3.cdf"
+    gold = load_golden("c2_s3_lim1.json")
+    shutil.copy(os.path.join(GOLDEN, cdf), tmp_path / cdf)
+    (tmp_path / "data.txt").write_text(DATA.format(metodo="esparso", cdf=cdf).replace("SCREEN", "ALL"))
+    for _ in range(2):
+        out = subprocess.run([gb.CLI_PATH], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+        assert out.returncode == 0, out.stderr
+    assert " Relatorio de execucao:" in out.stdout
+    assert f" Numero de iteracoes: {gold['iterations']}." in out.stdout
+    raw = (tmp_path / "out_double_esparso-c2_s3.csv").read_bytes()
+    lines = raw.split(b"\n")
+    assert lines[0] == (b"Execucao;Aviso;ms total;no iteracoes;ms Ybus;ms Init GPU;;;ms Inicializacao;ms calcPQ;;"
+                        b"ms Jacobiano;;ms Sistema Linear;;ms Processo;ms Fluxo;")
+    assert lines[1].startswith(b";;;;;total; Aloca\xef\xbf\xbd\xef\xbf\xbdo Vari\xef\xbf\xbdveis iniciais;")
+    assert lines[-1] == b""
+    rows = [l.decode() for l in lines[2:-1]]
+    assert len(rows) == 2
+    for k, row in enumerate(rows, start=1):
+        f = row.split(";")
+        assert len(f) == 18 and f[-1] == ""
+        assert f[0] == str(k) and f[1] == ""
+        assert f[3] == str(gold["iterations"])
+        for x in f[2:3] + f[4:17]:
+            assert "," in x and "." not in x
+            assert float(x.replace(",", ".")) >= 0
