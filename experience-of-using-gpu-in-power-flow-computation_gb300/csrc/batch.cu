@@ -39,6 +39,11 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
+// Iteration at which an instance still running on the warp-per-instance
+// kernel moves to a thread block of its own: a batch finishes when its slowest
+// instance does, and a warp runs one Newton iteration several times slower
+// than a block.
+constexpr int kHandoffIt = 12;
 
 template <typename T> struct Blk;
 template <> struct Blk<double> { using b4 = double4_32a; using b2 = double2; };
@@ -149,6 +154,17 @@ struct Args {
     char *scratch;                 // per-block factor slices when not in shared memory
     long long scratch_stride;
     int blob_region;               // bytes of dynamic shared memory reserved for a staged blob
+    // Straggler hand-off.  Warp kernel: an instance still iterating when it
+    // reaches iteration handoff_it (> 0) is parked -- V, theta into V/th,
+    // QliqLim into Q, the PV limit flags into P, the iteration count, event
+    // count and last max|dx| into iters / n_events / mism -- and its id pushed
+    // to handoff_q (count in *handoff_n).  Block kernel with resume = 1: the
+    // queue is handoff_q of length *handoff_n and every instance continues
+    // from its parked state.  no_group = 1 makes the block kernel sum exactly
+    // like the warp kernel (one lane per pivot, entry and row).
+    int handoff_it;
+    int *handoff_q, *handoff_n;
+    int resume, no_group;
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
@@ -212,7 +228,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
     for (;;) {
         if (tid == 0) {
             const int q = atomicAdd(a.counter, 1);
-            s_inst = q < a.queue_len ? a.queue[q] : -1;
+            const int qlen = a.resume ? *a.handoff_n : a.queue_len;
+            s_inst = q < qlen ? a.queue[q] : -1;
         }
         __syncthreads();
         const int inst = s_inst;
@@ -251,15 +268,34 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
         }
         const int n = T.n, nB = T.nB, nq = T.n + 2 * T.nup;
         B4 *Lv = fac + n, *Uv = fac + n + T.nup;
-        // initLim (GPU/limiteInjReat.cuh:188-224) and the starting state
-        for (int k = tid; k < nB; k += kThreads) {
-            V[k] = a.V0[off + k];
-            th[k] = a.th0[off + k];
-            QL[k] = a.Qliq[off + k];
-            act[k] = (G.type[k] == 0 || G.type[k] == 1);
+        if (!a.resume) {
+            // initLim (GPU/limiteInjReat.cuh:188-224) and the starting state
+            for (int k = tid; k < nB; k += kThreads) {
+                V[k] = a.V0[off + k];
+                th[k] = a.th0[off + k];
+                QL[k] = a.Qliq[off + k];
+                act[k] = (G.type[k] == 0 || G.type[k] == 1);
+            }
+            for (int i = tid; i < T.nPV; i += kThreads) limQ[i] = 0;
+            if (tid == 0) { s_done = 0; s_status = 0; s_it = 0; s_nev = 0; s_maxDx = INFINITY; }
+        } else {
+            // the state a warp parked at the hand-off
+            for (int k = tid; k < nB; k += kThreads) {
+                V[k] = a.V[off + k];
+                th[k] = a.th[off + k];
+                QL[k] = a.Q[off + k];
+                act[k] = (G.type[k] == 0 || G.type[k] == 1);
+            }
+            __syncthreads();
+            for (int i = tid; i < T.nPV; i += kThreads) {
+                limQ[i] = (int)a.P[off + i];
+                act[G.pv_bus[i]] = limQ[i];
+            }
+            if (tid == 0) {
+                s_done = 0; s_status = 0;
+                s_it = a.iters[inst]; s_nev = a.n_events[inst]; s_maxDx = a.mism[inst];
+            }
         }
-        for (int i = tid; i < T.nPV; i += kThreads) limQ[i] = 0;
-        if (tid == 0) { s_done = 0; s_status = 0; s_it = 0; s_nev = 0; s_maxDx = INFINITY; }
         __syncthreads();
         for (;;) {
             // phasors and injections
@@ -383,7 +419,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
             // the plain one-thread-per-pivot loop).
             for (int l = 0; l < T.nfl; l++) {
                 {
-                    const int lg = G.lvl_group[3 * l], gs = 1 << lg, gl = tid & (gs - 1), ng = kThreads >> lg;
+                    const int lg = a.no_group ? 0 : G.lvl_group[3 * l], gs = 1 << lg, gl = tid & (gs - 1),
+                              ng = kThreads >> lg;
                     const int beg = G.flev_ptr[l], cnt = G.flev_ptr[l + 1] - beg;
                     for (int b0 = 0; b0 < cnt; b0 += ng) {
                         const int w = b0 + (tid >> lg);
@@ -425,7 +462,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
                 }
                 __syncthreads();
                 {
-                    const int lg = G.lvl_group[3 * l + 1], gs = 1 << lg, gl = tid & (gs - 1), ng = kThreads >> lg;
+                    const int lg = a.no_group ? 0 : G.lvl_group[3 * l + 1], gs = 1 << lg, gl = tid & (gs - 1),
+                              ng = kThreads >> lg;
                     const int beg = G.fent_ptr[l], cnt = G.fent_ptr[l + 1] - beg;
                     for (int b0 = 0; b0 < cnt; b0 += ng) {
                         const int e = b0 + (tid >> lg);
@@ -456,7 +494,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
             if (s_done) break;
             // backward substitution, level by level, grouped like the factor
             for (int l = 0; l < T.nbl; l++) {
-                const int lg = G.lvl_group[3 * l + 2], gs = 1 << lg, gl = tid & (gs - 1), ng = kThreads >> lg;
+                const int lg = a.no_group ? 0 : G.lvl_group[3 * l + 2], gs = 1 << lg, gl = tid & (gs - 1),
+                          ng = kThreads >> lg;
                 const int beg = G.blev_ptr[l], cnt = G.blev_ptr[l + 1] - beg;
                 for (int b0 = 0; b0 < cnt; b0 += ng) {
                     const int w = b0 + (tid >> lg);
@@ -560,8 +599,26 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
         for (int i = lane; i < T.nPV; i += 32) limQ[i] = 0;
         int it = 0, status = 0, nev = 0;
         double maxDx = INFINITY, maxG = 0;
+        bool parked = false;
         __syncwarp();
         for (;;) {
+            if (a.handoff_it > 0 && it == a.handoff_it) {
+                // still iterating: park the state for the block-per-instance kernel
+                for (int k = lane; k < nB; k += 32) {
+                    a.V[off + k] = V[k];
+                    a.th[off + k] = th[k];
+                    a.Q[off + k] = QL[k];
+                }
+                for (int i = lane; i < T.nPV; i += 32) a.P[off + i] = (double)limQ[i];
+                if (lane == 0) {
+                    a.iters[inst] = it;
+                    a.n_events[inst] = nev;
+                    a.mism[inst] = maxDx;
+                    a.handoff_q[atomicAdd(a.handoff_n, 1)] = inst;
+                }
+                parked = true;
+                break;
+            }
             for (int k = lane; k < nB; k += 32) {
                 double s, c;
                 sincos(th[k], &s, &c);
@@ -733,6 +790,7 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
             __syncwarp();
         }
         __syncwarp();
+        if (parked) continue;
         for (int k = lane; k < nB; k += 32) {
             a.V[off + k] = V[k];
             a.th[off + k] = th[k];
@@ -991,11 +1049,12 @@ struct gbpf_batch {
     long long n_bus_total = 0;
     std::vector<int> inst_topo;
     std::vector<long long> inst_off;
-    DevBuf inst_mem, out_mem, scratch, counter, queues;
+    DevBuf inst_mem, out_mem, scratch, counter, queues, handoff, topo_resume;
+    int resume_region = 0;  // shared-memory bytes for the staged blob of a resumed instance
     Args args{};    // block-per-instance launch
     Args wargs{};   // warp-per-instance launch
-    size_t smem = 0, warp_smem = 0;
-    int grid_blocks = 0, warp_grid = 0, warp_warps = 0, n_block_q = 0, n_warp_q = 0;
+    size_t smem = 0, warp_smem = 0, resume_smem = 0;
+    int grid_blocks = 0, warp_grid = 0, warp_warps = 0, n_block_q = 0, n_warp_q = 0, resume_grid = 0;
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
     DevBuf topo_na;          // topologies planned for gbpf_batch_solve_noalloc
@@ -1225,7 +1284,7 @@ gbpf_status gbpf_batch::launch(cudaStream_t st) { return launch_with(st, args, w
 // One persistent launch per mode over the queues of ba (blocks) and wa (warps).
 gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args &wa) {
     const bool fp32 = precision == GBPF_PREC_FP32_IR;
-    CK(cudaMemsetAsync(args.counter, 0, 2 * sizeof(int), st));
+    CK(cudaMemsetAsync(args.counter, 0, 4 * sizeof(int), st));
     if (ba.queue_len) {
         CK(cudaEventRecord(fork, st));
         CK(cudaStreamWaitEvent(side, fork, 0));
@@ -1237,6 +1296,19 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
         if (fp32) k_nr_warp<float><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wa);
         else k_nr_warp<double><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wa);
         CK(cudaGetLastError());
+        if (wa.handoff_it > 0) {
+            // the instances the warps parked, one block each, same arithmetic
+            Args ra = wa;
+            ra.resume = 1;
+            ra.no_group = 1;
+            ra.queue = wa.handoff_q;
+            ra.counter = args.counter + 2;
+            ra.topo = (const Topo *)topo_resume.p;
+            ra.blob_region = resume_region;
+            if (fp32) k_nr_block<float><<<resume_grid, kThreads, resume_smem, st>>>(ra);
+            else k_nr_block<double><<<resume_grid, kThreads, resume_smem, st>>>(ra);
+            CK(cudaGetLastError());
+        }
     }
     if (ba.queue_len) {
         CK(cudaEventRecord(join, side));
@@ -1294,17 +1366,50 @@ gbpf_status gbpf_batch::build_graph() {
     args.blob_region = (int)region;
     smem = n_block_q ? need + region : 0;
     if (smem > (size_t)maxsm) { set_error("instance state does not fit in shared memory"); return GBPF_E_UNSUPPORTED; }
+    // stragglers of the warp kernel resume on blocks with their factor and,
+    // when it fits next to the state, the topology's blob in shared memory
+    // (few instances per SM get that far, so shared memory is not scarce)
+    resume_smem = 0;
+    resume_region = 0;
+    std::vector<Topo> rt(topo_h);
+    {
+        size_t state = 0, region_r = 0;
+        for (size_t t = 0; t < topo_h.size(); t++) {
+            if (!warp_ok[t]) continue;
+            const Topo &T = topo_h[t];
+            state = std::max(state, fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1).total
+                                         : layout<double>(T.nB, T.n, T.nup, T.nPV, 1).total);
+            region_r = std::max(region_r, align_up((size_t)T.blob_bytes, 32));
+        }
+        const bool stage = state + region_r <= (size_t)maxsm;
+        for (size_t t = 0; t < rt.size(); t++) {
+            rt[t].fac_smem = 1;
+            rt[t].blob_smem = warp_ok[t] && stage;
+        }
+        resume_region = stage ? (int)region_r : 0;
+        resume_smem = state + resume_region;
+    }
+    const bool use_handoff = n_warp_q > 0 && max_iter > kHandoffIt;
     grid_blocks = 0;
+    resume_grid = 0;
+    {
+        const size_t attr = std::max(smem, use_handoff ? resume_smem : 0);
+        if (attr) {
+            if (fp32) CK(cudaFuncSetAttribute(k_nr_block<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)attr));
+            else CK(cudaFuncSetAttribute(k_nr_block<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)attr));
+        }
+    }
     if (n_block_q) {
         int occ = 0;
-        if (fp32) {
-            CK(cudaFuncSetAttribute(k_nr_block<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float>, kThreads, smem));
-        } else {
-            CK(cudaFuncSetAttribute(k_nr_block<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double>, kThreads, smem));
-        }
+        if (fp32) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float>, kThreads, smem));
+        else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double>, kThreads, smem));
         grid_blocks = std::max(1, std::min(n_block_q, dev_sm * std::max(occ, 1)));
+    }
+    if (use_handoff) {
+        int occ = 0;
+        if (fp32) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float>, kThreads, resume_smem));
+        else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double>, kThreads, resume_smem));
+        resume_grid = std::max(1, std::min(n_warp_q, dev_sm * std::max(occ, 1)));
     }
     // warp-mode plan: as many warps per block as fit in 200 KB, at most 8
     warp_grid = 0;
@@ -1343,6 +1448,17 @@ gbpf_status gbpf_batch::build_graph() {
     wargs.queue = (const int *)queues.p;
     wargs.queue_len = n_warp_q;
     wargs.slice = (int)slice;
+    handoff.reset();
+    topo_resume.reset();
+    wargs.handoff_it = 0;
+    if (use_handoff) {
+        CK(cudaMalloc(&topo_resume.p, sizeof(Topo) * rt.size()));
+        CK(cudaMemcpy(topo_resume.p, rt.data(), sizeof(Topo) * rt.size(), cudaMemcpyHostToDevice));
+        CK(cudaMalloc(&handoff.p, 4 * (size_t)n_warp_q + 256));
+        wargs.handoff_it = kHandoffIt;
+        wargs.handoff_q = (int *)handoff.p;
+        wargs.handoff_n = (int *)counter.p + 3;
+    }
     // one graph: reset the work counter, one persistent launch
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     gbpf_status st = launch(stream);

@@ -130,3 +130,51 @@ def test_batch_repeat_is_deterministic(gb):
     # identical instances give identical answers whatever block ran them
     V = a["V"].reshape(300, g.nB)
     assert np.all(V == V[0])
+
+
+def test_batch_handoff_of_long_instances(gb, oracle):
+    """Instances still iterating at iteration 12 leave the warp-per-instance
+    kernel for a thread block of their own, which continues from the parked
+    state with the same arithmetic.  Scenarios of the bench workload that take
+    14, 17, 23 and 100 (no convergence, limit cycling) iterations, among
+    ordinary ones: FP64 iteration counts, statuses and switch events equal the
+    oracle's, |V| and theta within 1e-9 for the converged.  The FP32-LU form
+    converges on the same instances; where its PV -> PQ switch sequence is the
+    FP64 one, |V| and theta are within 1e-6 of the oracle.  With reactive
+    limits a generator whose Q sits within rounding of its limit when the
+    check runs can switch on another iteration in FP32, and the solve then
+    ends at another valid operating point: at most 2 of the 36 here."""
+    import bench
+
+    path = os.path.join(GOLDEN, "c2_base.cdf")
+    og = oracle.Grid(path)
+    base = dict(Pload=og.Pload.copy(), Qload=og.Qload.copy(), Pg=og.Pg.copy())
+    Pl, Ql, Pg = bench.scenarios(np, base, 4096, bench.BASE_SEED + 7)
+    pick = list(range(32)) + [1943, 2749, 3628, 4084]  # 23 (23 iterations) is among the first 32
+    Pl, Ql, Pg = Pl[pick], Ql[pick], Pg[pick]
+    n = len(pick)
+    grid = gb.read_grid(path)
+    b, r = run_batch(gb, [grid], np.zeros(n, np.int32), Pl.ravel(), Ql.ravel(), Pg.ravel())
+    assert b.info()["warp_instances"] == n
+    b32, r32 = run_batch(gb, [grid], np.zeros(n, np.int32), Pl.ravel(), Ql.ravel(), Pg.ravel(),
+                         precision=gb.PREC_FP32_IR)
+    long_ = other_path = 0
+    for i in range(n):
+        ref = oracle_solve(og, Pl[i], Ql[i], Pg[i], 1)
+        assert r["iterations"][i] == ref["iterations"], i
+        assert (r["status"][i] == 0) == ref["converged"], i
+        assert b.events(i) == ref["events"][:16], i
+        long_ += ref["iterations"] > 12
+        if ref["converged"]:
+            assert np.max(np.abs(b.slice(r["V"], i) - ref["V"])) < 1e-9
+            assert np.max(np.abs(b.slice(r["theta"], i) - ref["theta"])) < 1e-9
+            assert r32["status"][i] == 0 and r32["final_mismatch"][i] <= 1e-8
+            if [e[1:] for e in b32.events(i)] == [e[1:] for e in ref["events"][:16]]:
+                assert np.max(np.abs(b32.slice(r32["V"], i) - ref["V"])) < 1e-6
+                assert np.max(np.abs(b32.slice(r32["theta"], i) - ref["theta"])) < 1e-6
+            else:
+                other_path += 1
+        else:
+            assert r["iterations"][i] == 100
+    assert long_ == 5
+    assert other_path <= 2
