@@ -386,7 +386,7 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": a.workload, "grid": desc, "instances_per_gpu": N_SCEN, "tolerance": 1e-8,
                    "no_max_iter": 100, "lim_inj_reat": 1,
-                   "form": "batched, FP32 LU + FP64 mismatch/test/update (learned warm start not built)",
+                   "form": "batched, FP32 LU + FP64 mismatch/test/update, flat start (the learned start: workload c5)",
                    "converged_per_step": int(total_conv), "mean_iterations": float(np.mean(r["iterations"])),
                    "max_iterations": int(np.max(r["iterations"])),
                    "plain_fp64_solves_per_s": plain, "batched_fp64_solves_per_s": batched64,
