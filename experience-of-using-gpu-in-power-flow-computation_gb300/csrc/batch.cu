@@ -96,7 +96,7 @@ template <typename B4> __device__ __forceinline__ B4 bcast(B4 v, int src) {
 struct TopoOff {
     int yptr, ycol, yval, type, pv_bus, Qmin, Qmax, bus_of_blk, up_ptr, up_col, dg_ptr, dg_pos, dg_k,
         og_ptr, og_a, og_b, flev_ptr, flev_steps, blev_ptr, blev_steps, ysl, rbus, cbus, fent_ptr, fent_p,
-        fent_j, lvl_group;
+        fent_j, lvl_group, yval32;
 };
 struct Topo {
     int nB, nL, n, nup, nnzY, nPV, nfl, nbl, fac_smem, blob_smem, blob_bytes;
@@ -115,6 +115,7 @@ struct TopoView {
     // row in the block kernel: [3 * l] pivots and [3 * l + 1] entries of
     // forward level l, [3 * l + 2] rows of backward level l
     const int *lvl_group;
+    const float2 *yval32;  // Ybus values rounded to FP32 (the FP32-LU form's Jacobian)
 };
 __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     TopoView v;
@@ -131,6 +132,7 @@ __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     v.fent_ptr = (const int *)(b + o.fent_ptr); v.fent_p = (const int *)(b + o.fent_p);
     v.fent_j = (const int *)(b + o.fent_j);
     v.lvl_group = (const int *)(b + o.lvl_group);
+    v.yval32 = (const float2 *)(b + o.yval32);
     return v;
 }
 
@@ -171,7 +173,7 @@ __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a -
 
 // Shared-memory layout of one instance (state + optionally the factor).
 struct Layout {
-    size_t V, th, cs, sn, P, Q, QL, R, act, lim, ys, xs, fac, dinv, total;
+    size_t V, th, cs, sn, ef, f32, P, Q, QL, act, lim, ys, fac, dinv, total;
 };
 template <typename TJ>
 __host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fac_smem) {
@@ -181,10 +183,14 @@ __host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fa
     size_t o = 0;
     auto take = [&](size_t bytes, size_t al) { o = align_up(o, al); size_t r = o; o += bytes; return r; };
     L.V = take(8 * nB, 16); L.th = take(8 * nB, 16); L.cs = take(8 * nB, 16); L.sn = take(8 * nB, 16);
+    // e = V cos th, f = V sin th (FP64); cos, sin, V in FP32 for the FP32-LU form's Jacobian
+    L.ef = take(16 * (size_t)nB, 16);
+    L.f32 = take(sizeof(TJ) == 4 ? 16 * (size_t)nB : 0, 16);
     L.P = take(8 * nB, 16); L.Q = take(8 * nB, 16); L.QL = take(8 * nB, 16);
-    L.R = take(16 * (size_t)n, 16);
-    L.act = take(4 * nB, 16); L.lim = take(4 * (size_t)(nPV + 1), 16);
-    L.ys = take(sizeof(B2) * n, 16); L.xs = take(sizeof(B2) * n, 16);
+    L.act = take(nB, 16); L.lim = take(4 * (size_t)(nPV + 1), 16);
+    // ys: the mismatch, then (forward) the substituted right-hand side, then
+    // (backward, in place) the Newton step
+    L.ys = take(sizeof(B2) * n, 16);
     const size_t nq = (size_t)n + 2 * (size_t)nup;
     if (fac_smem) {
         L.fac = take(sizeof(B4) * nq, 32);
@@ -212,6 +218,82 @@ __device__ __forceinline__ double block_max(double v, double *red) {
     for (int w = 1; w < kWarps; w++) m = (red[w] > m || red[w] != red[w]) ? red[w] : m;
     __syncthreads();
     return m;
+}
+
+// FP32-LU form only: the phasor (cos, sin) of th + d from that of th.  For
+// |d| <= 0.1 a rotation by d, with sin d and cos d from their Taylor series,
+// cut where the next term is below 3e-19 for the step's size class; a larger
+// step takes a full sincos of the new angle.  Each rotation adds a few ulps, far below the
+// 1e-8 mismatch the Newton loop tests; the FP64 form keeps a full sincos.
+__device__ __forceinline__ void rotate_phasor(double th_new, double d, double &c, double &s) {
+    const double ad = fabs(d), d2 = d * d;
+    double sd, cd;
+    if (ad <= 1e-4) {  // next terms d^5/5!, d^6/6!: below 1e-22
+        sd = d * (1.0 + d2 * (-1.0 / 6.0));
+        cd = 1.0 + d2 * (-0.5 + d2 * (1.0 / 24.0));
+    } else if (ad <= 1e-2) {  // next terms d^9/9!, d^10/10!: below 3e-24
+        sd = d * (1.0 + d2 * (-1.0 / 6.0 + d2 * (1.0 / 120.0 + d2 * (-1.0 / 5040.0))));
+        cd = 1.0 + d2 * (-0.5 + d2 * (1.0 / 24.0 + d2 * (-1.0 / 720.0 + d2 * (1.0 / 40320.0))));
+    } else if (ad <= 0.1) {  // next terms d^11/11!, d^12/12!: below 3e-19
+        sd = d * (1.0 + d2 * (-1.0 / 6.0 + d2 * (1.0 / 120.0 + d2 * (-1.0 / 5040.0 + d2 * (1.0 / 362880.0)))));
+        cd = 1.0 + d2 * (-0.5 + d2 * (1.0 / 24.0 + d2 * (-1.0 / 720.0 + d2 * (1.0 / 40320.0 + d2 * (-1.0 / 3628800.0)))));
+    } else {
+        sincos(th_new, &s, &c);
+        return;
+    }
+    const double cn = c * cd - s * sd, sn = s * cd + c * sd;
+    c = cn;
+    s = sn;
+}
+
+// Diagonal Jacobian block of bus k (dP/dth, dP/dV; dQ/dth, dQ/dV at the
+// injections P, Q): FP64 for the FP64 form, FP32 arithmetic for the FP32-LU
+// form, whose factor holds FP32 values anyway.
+template <typename TJ, typename B4>
+__device__ __forceinline__ B4 diag_block(double Pk_, double Qk_, double Vk_, double2 y, int ak) {
+    B4 blk;
+    blk.y = blk.z = (TJ)0;
+    if constexpr (sizeof(TJ) == 4) {
+        const float Pk = (float)Pk_, Qk = (float)Qk_, vk = (float)Vk_, v2 = vk * vk, g = (float)y.x, b = (float)y.y;
+        blk.x = -Qk - v2 * b;
+        if (ak) {
+            const float iv = 1.f / vk;
+            blk.y = (Pk + v2 * g) * iv;
+            blk.z = Pk - v2 * g;
+            blk.w = (Qk - v2 * b) * iv;
+        } else {
+            blk.w = 1.f;
+        }
+    } else {
+        const double v2 = Vk_ * Vk_;
+        blk.x = -Qk_ - v2 * y.y;
+        if (ak) {
+            blk.y = (Pk_ + v2 * y.x) / Vk_;
+            blk.z = Pk_ - v2 * y.x;
+            blk.w = (Qk_ - v2 * y.y) / Vk_;
+        } else {
+            blk.w = 1.0;
+        }
+    }
+    return blk;
+}
+
+// Diagonal block for the FP32-LU form from FP32 inputs (P, Q, V, Ybus).
+template <typename B4>
+__device__ __forceinline__ B4 diag_block32(float Pk, float Qk, float vk, float2 y, int ak) {
+    B4 blk;
+    const float v2 = vk * vk;
+    blk.x = -Qk - v2 * y.y;
+    blk.y = blk.z = 0.f;
+    if (ak) {
+        const float iv = 1.f / vk;
+        blk.y = (Pk + v2 * y.x) * iv;
+        blk.z = Pk - v2 * y.x;
+        blk.w = (Qk - v2 * y.y) * iv;
+    } else {
+        blk.w = 1.f;
+    }
+    return blk;
 }
 
 template <typename TJ>
@@ -253,10 +335,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
         const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, T.fac_smem);
         double *V = (double *)(ism + L.V), *th = (double *)(ism + L.th);
         double *cs = (double *)(ism + L.cs), *sn = (double *)(ism + L.sn);
+        double2 *ef = (double2 *)(ism + L.ef);
+        float4 *f32 = (float4 *)(ism + L.f32);
         double *P = (double *)(ism + L.P), *Q = (double *)(ism + L.Q), *QL = (double *)(ism + L.QL);
-        double2 *R = (double2 *)(ism + L.R);
-        int *act = (int *)(ism + L.act), *limQ = (int *)(ism + L.lim);
-        B2 *ys = (B2 *)(ism + L.ys), *xs = (B2 *)(ism + L.xs);
+        unsigned char *act = ism + L.act;
+        int *limQ = (int *)(ism + L.lim);
+        B2 *ys = (B2 *)(ism + L.ys);
         B4 *fac, *dinv;
         if (T.fac_smem) {
             fac = (B4 *)(ism + L.fac);
@@ -297,25 +381,29 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
             }
         }
         __syncthreads();
+        bool fresh = true;
         for (;;) {
-            // phasors and injections
-            for (int k = tid; k < nB; k += kThreads) {
-                double s, c;
-                sincos(th[k], &s, &c);
-                cs[k] = c;
-                sn[k] = s;
-            }
+            // phasors (the FP32-LU form rotates them in the update after the
+            // first pass) and injections
+            if (sizeof(TJ) == 8 || fresh)
+                for (int k = tid; k < nB; k += kThreads) {
+                    double s, c;
+                    sincos(th[k], &s, &c);
+                    cs[k] = c;
+                    sn[k] = s;
+                    ef[k] = make_double2(V[k] * c, V[k] * s);
+                    if (sizeof(TJ) == 4) f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
+                }
+            fresh = false;
             __syncthreads();
             for (int k = tid; k < nB; k += kThreads) {
                 double ir = 0, ii = 0;
                 for (int p = G.yptr[k]; p < G.yptr[k + 1]; p++) {
-                    const int m = G.ycol[p];
-                    const double2 y = G.yval[p];
-                    const double em = V[m] * cs[m], fm = V[m] * sn[m];
-                    ir += y.x * em - y.y * fm;
-                    ii += y.x * fm + y.y * em;
+                    const double2 y = G.yval[p], u = ef[G.ycol[p]];
+                    ir += y.x * u.x - y.y * u.y;
+                    ii += y.x * u.y + y.y * u.x;
                 }
-                const double ek = V[k] * cs[k], fk = V[k] * sn[k];
+                const double ek = ef[k].x, fk = ef[k].y;
                 P[k] = ek * ir + fk * ii;
                 Q[k] = fk * ir - ek * ii;
             }
@@ -358,7 +446,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
                 const int k = G.bus_of_blk[j];
                 const double gp = a.Pliq[off + k] - P[k];
                 const double gq = act[k] ? QL[k] - Q[k] : 0.0;
-                R[j] = make_double2(gp, gq);
+                B2 r;
+                r.x = (TJ)gp;
+                r.y = (TJ)gq;
+                ys[j] = r;
                 double t = fmax(fabs(gp), fabs(gq));
                 if (t != t) t = __longlong_as_double(0x7ff8000000000000ll);
                 m = (t > m || t != t) ? t : m;
@@ -379,30 +470,40 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
                 blk.x = blk.y = blk.z = blk.w = 0;
                 if (s >= 0) {
                     const int k = G.rbus[q], mb = G.cbus[q];
-                    const double2 y = G.yval[s];
-                    const double Vk = V[k];
                     const int ak = act[k];
-                    if (q < n) {
-                        const double Pk = P[k], Qk = Q[k], v2 = Vk * Vk;
-                        blk.x = (TJ)(-Qk - v2 * y.y);
-                        if (ak) {
-                            blk.y = (TJ)((Pk + v2 * y.x) / Vk);
-                            blk.z = (TJ)(Pk - v2 * y.x);
-                            blk.w = (TJ)((Qk - v2 * y.y) / Vk);
+                    if constexpr (sizeof(TJ) == 4) {
+                        // FP32-LU form: FP32 copies of the phasors, V and Ybus
+                        const float4 fk = f32[k];
+                        const float2 y = G.yval32[s];
+                        if (q < n) {
+                            blk = diag_block32<B4>((float)P[k], (float)Q[k], fk.z, y, ak);
                         } else {
-                            blk.w = (TJ)1;
+                            const int am = act[mb];
+                            const float4 fm = f32[mb];
+                            const float tr = y.x * fm.x - y.y * fm.y, ti = y.x * fm.y + y.y * fm.x;
+                            const float wr = fk.x * tr + fk.y * ti, wi = fk.y * tr - fk.x * ti;
+                            blk.x = fk.z * fm.z * wi;
+                            if (am) blk.y = fk.z * wr;
+                            if (ak) blk.z = -fk.z * fm.z * wr;
+                            if (ak && am) blk.w = fk.z * wi;
                         }
                     } else {
-                        // off-diagonal entries in the precision of the factor
-                        const int am = act[mb];
-                        const TJ ck = (TJ)cs[k], sk = (TJ)sn[k], cm = (TJ)cs[mb], sm = (TJ)sn[mb];
-                        const TJ yr = (TJ)y.x, yi = (TJ)y.y, vk = (TJ)Vk, vm = (TJ)V[mb];
-                        const TJ tr = yr * cm - yi * sm, ti = yr * sm + yi * cm;
-                        const TJ wr = ck * tr + sk * ti, wi = sk * tr - ck * ti;
-                        blk.x = vk * vm * wi;
-                        if (am) blk.y = vk * wr;
-                        if (ak) blk.z = -vk * vm * wr;
-                        if (ak && am) blk.w = vk * wi;
+                        const double2 y = G.yval[s];
+                        const double Vk = V[k];
+                        if (q < n) {
+                            blk = diag_block<TJ, B4>(P[k], Q[k], Vk, y, ak);
+                        } else {
+                            // off-diagonal entries in the precision of the factor
+                            const int am = act[mb];
+                            const TJ ck = (TJ)cs[k], sk = (TJ)sn[k], cm = (TJ)cs[mb], sm = (TJ)sn[mb];
+                            const TJ yr = (TJ)y.x, yi = (TJ)y.y, vk = (TJ)Vk, vm = (TJ)V[mb];
+                            const TJ tr = yr * cm - yi * sm, ti = yr * sm + yi * cm;
+                            const TJ wr = ck * tr + sk * ti, wi = sk * tr - ck * ti;
+                            blk.x = vk * vm * wi;
+                            if (am) blk.y = vk * wr;
+                            if (ak) blk.z = -vk * vm * wr;
+                            if (ak && am) blk.w = vk * wi;
+                        }
                     }
                 }
                 fac[q] = blk;
@@ -432,8 +533,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
                         yj.x = yj.y = (TJ)0;
                         if (on && gl == 0) {
                             D = fac[j];
-                            yj.x = (TJ)R[j].x;
-                            yj.y = (TJ)R[j].y;
+                            yj = ys[j];
                         }
                         if (on)
                             for (int t = G.dg_ptr[j] + gl; t < G.dg_ptr[j + 1]; t += gs) {
@@ -506,12 +606,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
                     if (on && gl == 0) acc = ys[j];
                     if (on)
                         for (int p = G.up_ptr[j] + gl; p < G.up_ptr[j + 1]; p += gs) {
-                            const B2 v = bmv(Uv[p], xs[G.up_col[p]]);
+                            const B2 v = bmv(Uv[p], ys[G.up_col[p]]);
                             acc.x -= v.x;
                             acc.y -= v.y;
                         }
                     for (int o = gs >> 1; o > 0; o >>= 1) acc = b2sum_xor(acc, o);
-                    if (on && gl == 0) xs[j] = bmv(dinv[j], acc);
+                    if (on && gl == 0) ys[j] = bmv(dinv[j], acc);
                 }
                 __syncthreads();
             }
@@ -519,9 +619,17 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
             double md = 0;
             for (int j = tid; j < n; j += kThreads) {
                 const int k = G.bus_of_blk[j];
-                const double dt = (double)xs[j].x, dv = (double)xs[j].y;
+                const double dt = (double)ys[j].x, dv = (double)ys[j].y;
                 th[k] += dt;
                 if (act[k]) V[k] += dv;
+                if (sizeof(TJ) == 4) {
+                    double c = cs[k], s = sn[k];
+                    rotate_phasor(th[k], dt, c, s);
+                    cs[k] = c;
+                    sn[k] = s;
+                    ef[k] = make_double2(V[k] * c, V[k] * s);
+                    f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
+                }
                 double t = fmax(fabs(dt), fabs(dv));
                 if (t != t) t = __longlong_as_double(0x7ff8000000000000ll);
                 md = (t > md || t != t) ? t : md;
@@ -583,10 +691,12 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
         const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, 1);
         double *V = (double *)(ism + L.V), *th = (double *)(ism + L.th);
         double *cs = (double *)(ism + L.cs), *sn = (double *)(ism + L.sn);
+        double2 *ef = (double2 *)(ism + L.ef);
+        float4 *f32 = (float4 *)(ism + L.f32);
         double *P = (double *)(ism + L.P), *Q = (double *)(ism + L.Q), *QL = (double *)(ism + L.QL);
-        double2 *R = (double2 *)(ism + L.R);
-        int *act = (int *)(ism + L.act), *limQ = (int *)(ism + L.lim);
-        B2 *ys = (B2 *)(ism + L.ys), *xs = (B2 *)(ism + L.xs);
+        unsigned char *act = ism + L.act;
+        int *limQ = (int *)(ism + L.lim);
+        B2 *ys = (B2 *)(ism + L.ys);
         B4 *fac = (B4 *)(ism + L.fac), *dinv = (B4 *)(ism + L.dinv);
         const int n = T.n, nB = T.nB, nq = T.n + 2 * T.nup;
         B4 *Lv = fac + n, *Uv = fac + n + T.nup;
@@ -619,23 +729,24 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
                 parked = true;
                 break;
             }
-            for (int k = lane; k < nB; k += 32) {
-                double s, c;
-                sincos(th[k], &s, &c);
-                cs[k] = c;
-                sn[k] = s;
-            }
+            if (sizeof(TJ) == 8 || it == 0)
+                for (int k = lane; k < nB; k += 32) {
+                    double s, c;
+                    sincos(th[k], &s, &c);
+                    cs[k] = c;
+                    sn[k] = s;
+                    ef[k] = make_double2(V[k] * c, V[k] * s);
+                    if (sizeof(TJ) == 4) f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
+                }
             __syncwarp();
             for (int k = lane; k < nB; k += 32) {
                 double ir = 0, ii = 0;
                 for (int p = G.yptr[k]; p < G.yptr[k + 1]; p++) {
-                    const int m = G.ycol[p];
-                    const double2 y = G.yval[p];
-                    const double em = V[m] * cs[m], fm = V[m] * sn[m];
-                    ir += y.x * em - y.y * fm;
-                    ii += y.x * fm + y.y * em;
+                    const double2 y = G.yval[p], u = ef[G.ycol[p]];
+                    ir += y.x * u.x - y.y * u.y;
+                    ii += y.x * u.y + y.y * u.x;
                 }
-                const double ek = V[k] * cs[k], fk = V[k] * sn[k];
+                const double ek = ef[k].x, fk = ef[k].y;
                 P[k] = ek * ir + fk * ii;
                 Q[k] = fk * ir - ek * ii;
             }
@@ -679,7 +790,10 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
                 const int k = G.bus_of_blk[j];
                 const double gp = a.Pliq[off + k] - P[k];
                 const double gq = act[k] ? QL[k] - Q[k] : 0.0;
-                R[j] = make_double2(gp, gq);
+                B2 r;
+                r.x = (TJ)gp;
+                r.y = (TJ)gq;
+                ys[j] = r;
                 double t = fmax(fabs(gp), fabs(gq));
                 if (t != t) t = __longlong_as_double(0x7ff8000000000000ll);
                 mloc = (t > mloc || t != t) ? t : mloc;
@@ -694,29 +808,40 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
                 blk.x = blk.y = blk.z = blk.w = 0;
                 if (sl >= 0) {
                     const int k = G.rbus[qq], mb = G.cbus[qq];
-                    const double2 y = G.yval[sl];
-                    const double Vk = V[k];
                     const int ak = act[k];
-                    if (qq < n) {
-                        const double Pk = P[k], Qk = Q[k], v2 = Vk * Vk;
-                        blk.x = (TJ)(-Qk - v2 * y.y);
-                        if (ak) {
-                            blk.y = (TJ)((Pk + v2 * y.x) / Vk);
-                            blk.z = (TJ)(Pk - v2 * y.x);
-                            blk.w = (TJ)((Qk - v2 * y.y) / Vk);
+                    if constexpr (sizeof(TJ) == 4) {
+                        // FP32-LU form: FP32 copies of the phasors, V and Ybus
+                        const float4 fk = f32[k];
+                        const float2 y = G.yval32[sl];
+                        if (qq < n) {
+                            blk = diag_block32<B4>((float)P[k], (float)Q[k], fk.z, y, ak);
                         } else {
-                            blk.w = (TJ)1;
+                            const int am = act[mb];
+                            const float4 fm = f32[mb];
+                            const float tr = y.x * fm.x - y.y * fm.y, ti = y.x * fm.y + y.y * fm.x;
+                            const float wr = fk.x * tr + fk.y * ti, wi = fk.y * tr - fk.x * ti;
+                            blk.x = fk.z * fm.z * wi;
+                            if (am) blk.y = fk.z * wr;
+                            if (ak) blk.z = -fk.z * fm.z * wr;
+                            if (ak && am) blk.w = fk.z * wi;
                         }
                     } else {
-                        const int am = act[mb];
-                        const TJ ck = (TJ)cs[k], sk = (TJ)sn[k], cm = (TJ)cs[mb], sm = (TJ)sn[mb];
-                        const TJ yr = (TJ)y.x, yi = (TJ)y.y, vk = (TJ)Vk, vm = (TJ)V[mb];
-                        const TJ tr = yr * cm - yi * sm, ti = yr * sm + yi * cm;
-                        const TJ wr = ck * tr + sk * ti, wi = sk * tr - ck * ti;
-                        blk.x = vk * vm * wi;
-                        if (am) blk.y = vk * wr;
-                        if (ak) blk.z = -vk * vm * wr;
-                        if (ak && am) blk.w = vk * wi;
+                        const double2 y = G.yval[sl];
+                        const double Vk = V[k];
+                        if (qq < n) {
+                            blk = diag_block<TJ, B4>(P[k], Q[k], Vk, y, ak);
+                        } else {
+                            // off-diagonal entries in the precision of the factor
+                            const int am = act[mb];
+                            const TJ ck = (TJ)cs[k], sk = (TJ)sn[k], cm = (TJ)cs[mb], sm = (TJ)sn[mb];
+                            const TJ yr = (TJ)y.x, yi = (TJ)y.y, vk = (TJ)Vk, vm = (TJ)V[mb];
+                            const TJ tr = yr * cm - yi * sm, ti = yr * sm + yi * cm;
+                            const TJ wr = ck * tr + sk * ti, wi = sk * tr - ck * ti;
+                            blk.x = vk * vm * wi;
+                            if (am) blk.y = vk * wr;
+                            if (ak) blk.z = -vk * vm * wr;
+                            if (ak && am) blk.w = vk * wi;
+                        }
                     }
                 }
                 fac[qq] = blk;
@@ -728,8 +853,7 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
                     const int j = G.flev_steps[w];
                     B4 D = fac[j];
                     B2 yj;
-                    yj.x = (TJ)R[j].x;
-                    yj.y = (TJ)R[j].y;
+                    yj = ys[j];
                     for (int t = G.dg_ptr[j]; t < G.dg_ptr[j + 1]; t++) {
                         const int p = G.dg_pos[t];
                         const B4 lj = Lv[p];
@@ -767,20 +891,28 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
                     const int j = G.blev_steps[w];
                     B2 acc = ys[j];
                     for (int p = G.up_ptr[j]; p < G.up_ptr[j + 1]; p++) {
-                        const B2 v = bmv(Uv[p], xs[G.up_col[p]]);
+                        const B2 v = bmv(Uv[p], ys[G.up_col[p]]);
                         acc.x -= v.x;
                         acc.y -= v.y;
                     }
-                    xs[j] = bmv(dinv[j], acc);
+                    ys[j] = bmv(dinv[j], acc);
                 }
                 __syncwarp();
             }
             double md = 0;
             for (int j = lane; j < n; j += 32) {
                 const int k = G.bus_of_blk[j];
-                const double dt = (double)xs[j].x, dv = (double)xs[j].y;
+                const double dt = (double)ys[j].x, dv = (double)ys[j].y;
                 th[k] += dt;
                 if (act[k]) V[k] += dv;
+                if (sizeof(TJ) == 4) {
+                    double c = cs[k], s = sn[k];
+                    rotate_phasor(th[k], dt, c, s);
+                    cs[k] = c;
+                    sn[k] = s;
+                    ef[k] = make_double2(V[k] * c, V[k] * s);
+                    f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
+                }
                 double t = fmax(fabs(dt), fabs(dv));
                 if (t != t) t = __longlong_as_double(0x7ff8000000000000ll);
                 md = (t > md || t != t) ? t : md;
@@ -808,7 +940,7 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
 }
 
 __global__ void k_batch_ybus(const int *cptr, const int *csrc, const double2 *stamp, const double *gsh,
-                             const double *bsh, double2 *yval, int nnz) {
+                             const double *bsh, double2 *yval, float2 *yval32, int nnz) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nnz) return;
     double2 acc = make_double2(0, 0);
@@ -819,6 +951,7 @@ __global__ void k_batch_ybus(const int *cptr, const int *csrc, const double2 *st
         else { acc.x += v.x; acc.y += v.y; }
     }
     yval[s] = acc;
+    yval32[s] = make_float2((float)acc.x, (float)acc.y);
 }
 
 __device__ __forceinline__ double2 cdiv2(double a, double b, double c, double d) {
@@ -1161,6 +1294,7 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
         grp[3 * l + 2] = group_of(S.blev_ptr[l + 1] - S.blev_ptr[l], mu);
     }
     o.lvl_group = put(grp.data(), grp.size() * 4);
+    o.yval32 = put(nullptr, (size_t)y.nnz * 8);
     DevBuf mem, tmp;
     CK(cudaMalloc(&mem.p, blob.size()));
     CK(cudaMemcpyAsync(mem.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, stream));
@@ -1189,7 +1323,8 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
     k_batch_ybus<<<(y.nnz + 255) / 256, 256, 0, stream>>>((const int *)(tb + t_cptr), (const int *)(tb + t_csrc),
                                                           (const double2 *)(tb + t_stamp), (const double *)(tb + t_gsh),
                                                           (const double *)(tb + t_bsh),
-                                                          (double2 *)((char *)mem.p + o.yval), y.nnz);
+                                                          (double2 *)((char *)mem.p + o.yval),
+                                                          (float2 *)((char *)mem.p + o.yval32), y.nnz);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(stream));
     Topo t{};
