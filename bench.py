@@ -378,8 +378,16 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     # algorithmic bytes of one batch launch: inputs (V0, theta0, Pliq, Qliq, Qload),
     # outputs (V, theta, P, Q) and per-instance results; topology blobs counted once
     bytes_launch = nb * 8 * 5 + nb * 8 * 4 + N_SCEN * (4 * 3 + 8)
-    t_launch = ms / a.steps / 1e3
+    # the dominant kernel's own time per launch: CUDA events recorded inside
+    # the graph around each kernel, on the stream it runs on
+    kt = fast.kernel_times(max(3, a.steps // 4))
+    main_kernel = "k_nr_warp<float>" if info["warp_instances"] else "k_nr_block<float>"
+    t_launch = (kt["warp"] if info["warp_instances"] else kt["block"]) / 1e3
     achieved = bytes_launch / t_launch / 1e9
+    # DRAM traffic of one k_nr_warp<float> launch of the 32,768 c2 scenarios
+    # (ncu dram__bytes_read.sum + dram__bytes_write.sum, one-pass capture of the
+    # full-size run, profiles/k_nr_warp_fp32_c2_32768.md), scaled by instances
+    traffic = 202.9e6 * N_SCEN / 32768 if a.workload == "c2" else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": max(3, a.warmup), "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True,
@@ -396,10 +404,14 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
                    "batch": info, "parallelism": f"scenarios sharded x{world}"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nb * 8 * 5 + N_SCEN * 12,
                 "d2h_bytes_per_step": nb * 8 * 4 + N_SCEN * 20},
-        "roofline": {"bound": "hbm", "kernel": "k_nr_warp/k_nr_block (one persistent launch)",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src_note(src), "traffic": None,
-                     "note": "FP64-pipe and latency bound; state lives in shared memory"},
+        "roofline": {"bound": "hbm", "kernel": main_kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src_note(src),
+                     "traffic": traffic / 1e9 if traffic else None, "traffic_unit": "GB per launch",
+                     "algorithmic_bytes_per_launch": bytes_launch,
+                     "kernel_ms_per_launch": kt,
+                     "note": "FP64-pipe and dependent-latency bound (ncu: FP64 pipe ~50 % of active cycles); state "
+                             "lives in shared memory, the step's remaining time is the hand-off launch of the few "
+                             "instances that run all 100 iterations"},
         "clocks": clk.summary(),
         "gpu_launches": a.steps * (1 + (1 if info["warp_instances"] else 0) +
                                    (1 if info["warp_instances"] < N_SCEN else 0)),

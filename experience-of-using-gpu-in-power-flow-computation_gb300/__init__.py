@@ -41,7 +41,7 @@ EXPORTS = [
     "gbpf_batch_results", "gbpf_batch_events", "gbpf_batch_info", "gbpf_batch_solve_noalloc",
     "gbpf_mlp_create", "gbpf_mlp_free", "gbpf_mlp_dims", "gbpf_mlp_set_data", "gbpf_mlp_train", "gbpf_mlp_predict",
     "gbpf_mlp_gradients", "gbpf_mlp_params", "gbpf_mlp_set_params", "gbpf_mlp_norm", "gbpf_mlp_set_norm",
-    "gbpf_batch_solve_warm", "gbpf_mlp_set_loss_metric", "gbpf_solver_setup_times",
+    "gbpf_batch_solve_warm", "gbpf_mlp_set_loss_metric", "gbpf_solver_setup_times", "gbpf_batch_kernel_times",
 ]
 
 
@@ -473,6 +473,13 @@ class Batch:
         ms = ctypes.c_double()
         _check(lib().gbpf_batch_time(self.h, int(repeats), ctypes.byref(ms)), "gbpf_batch_time")
         return ms.value
+
+    def kernel_times(self, repeats=3):
+        """Device ms per launch of each kernel of the batch graph: block,
+        warp, hand-off (gbpf_batch_kernel_times)."""
+        ms = np.zeros(3)
+        _check(lib().gbpf_batch_kernel_times(self.h, int(repeats), _p(ms)), "gbpf_batch_kernel_times")
+        return dict(block=float(ms[0]), warp=float(ms[1]), handoff=float(ms[2]))
 
     def results(self, state=True):
         n, nb = self.n_inst, int(self.offsets[-1])

@@ -1190,6 +1190,8 @@ struct gbpf_batch {
     int grid_blocks = 0, warp_grid = 0, warp_warps = 0, n_block_q = 0, n_warp_q = 0, resume_grid = 0;
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    // events around each kernel of the captured graph (block, warp, hand-off)
+    cudaEvent_t kev[6] = {};
     DevBuf topo_na;          // topologies planned for gbpf_batch_solve_noalloc
     void *h_in = nullptr, *h_out = nullptr;  // pinned mirrors of the input and output regions
     size_t out_bytes = 0;
@@ -1204,6 +1206,7 @@ struct gbpf_batch {
         if (ev1) cudaEventDestroy(ev1);
         if (fork) cudaEventDestroy(fork);
         if (join) cudaEventDestroy(join);
+        for (auto &e : kev) if (e) cudaEventDestroy(e);
         if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
         if (h_in) cudaFreeHost(h_in);
@@ -1222,7 +1225,7 @@ struct gbpf_batch {
     double4_32a *wEF = nullptr;
     int *wKind = nullptr, *wQueue = nullptr;
     gbpf_status launch(cudaStream_t st);
-    gbpf_status launch_with(cudaStream_t st, const Args &ba, const Args &wa);
+    gbpf_status launch_with(cudaStream_t st, const Args &ba, const Args &wa, bool timed = false);
     gbpf_status build_graph();
     gbpf_status solve_warm(gbpf_mlp *m, int *kind, int *warm_iters, float *ms);
 };
@@ -1414,23 +1417,27 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
     return build_graph();
 }
 
-gbpf_status gbpf_batch::launch(cudaStream_t st) { return launch_with(st, args, wargs); }
+gbpf_status gbpf_batch::launch(cudaStream_t st) { return launch_with(st, args, wargs, true); }
 
 // One persistent launch per mode over the queues of ba (blocks) and wa (warps).
-gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args &wa) {
+gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args &wa, bool timed) {
     const bool fp32 = precision == GBPF_PREC_FP32_IR;
     CK(cudaMemsetAsync(args.counter, 0, 4 * sizeof(int), st));
     if (ba.queue_len) {
         CK(cudaEventRecord(fork, st));
         CK(cudaStreamWaitEvent(side, fork, 0));
+        if (timed) CK(cudaEventRecord(kev[0], side));
         if (fp32) k_nr_block<float><<<grid_blocks, kThreads, smem, side>>>(ba);
         else k_nr_block<double><<<grid_blocks, kThreads, smem, side>>>(ba);
         CK(cudaGetLastError());
+        if (timed) CK(cudaEventRecord(kev[1], side));
     }
     if (wa.queue_len) {
+        if (timed) CK(cudaEventRecord(kev[2], st));
         if (fp32) k_nr_warp<float><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wa);
         else k_nr_warp<double><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wa);
         CK(cudaGetLastError());
+        if (timed) CK(cudaEventRecord(kev[3], st));
         if (wa.handoff_it > 0) {
             // the instances the warps parked, one block each, same arithmetic
             Args ra = wa;
@@ -1443,6 +1450,7 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
             if (fp32) k_nr_block<float><<<resume_grid, kThreads, resume_smem, st>>>(ra);
             else k_nr_block<double><<<resume_grid, kThreads, resume_smem, st>>>(ra);
             CK(cudaGetLastError());
+            if (timed) CK(cudaEventRecord(kev[4], st));
         }
     }
     if (ba.queue_len) {
@@ -1688,6 +1696,25 @@ gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, 
 // ---------------------------------------------------------------------------
 #define ARGCHECK(c) do { if (!(c)) { set_error("invalid argument: " #c); return GBPF_E_ARG; } } while (0)
 
+extern "C" gbpf_status gbpf_batch_kernel_times(gbpf_batch *b, int repeats, double ms[3]) {
+    ARGCHECK(b && b->exec && repeats > 0 && ms);
+    CK(cudaSetDevice(b->device));
+    ms[0] = ms[1] = ms[2] = 0;
+    for (int r = 0; r < repeats; r++) {
+        CK(cudaGraphLaunch(b->exec, b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+        float t = 0;
+        if (b->n_block_q) { CK(cudaEventElapsedTime(&t, b->kev[0], b->kev[1])); ms[0] += t; }
+        if (b->n_warp_q) {
+            CK(cudaEventElapsedTime(&t, b->kev[2], b->kev[3]));
+            ms[1] += t;
+            if (b->wargs.handoff_it > 0) { CK(cudaEventElapsedTime(&t, b->kev[3], b->kev[4])); ms[2] += t; }
+        }
+    }
+    for (int i = 0; i < 3; i++) ms[i] /= repeats;
+    return GBPF_OK;
+}
+
 extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_grids, const gbpf_options *o,
                                          int device, gbpf_batch **out) {
     ARGCHECK(grids && n_grids > 0 && o && out);
@@ -1705,6 +1732,7 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
     CK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
+    for (auto &e : b->kev) CK(cudaEventCreate(&e));
     for (int i = 0; i < n_grids; i++) {
         ARGCHECK(grids[i]);
         gbpf_status st = b->add_topology(grids[i]->g);

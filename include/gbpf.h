@@ -296,6 +296,14 @@ gbpf_status gbpf_batch_solve(gbpf_batch *b);
 /* `repeats` batch solves back to back on the batch stream; device ms. */
 gbpf_status gbpf_batch_time(gbpf_batch *b, int repeats, double *ms_total);
 
+/* Device time of each kernel of the batch graph, averaged over `repeats`
+ * launches (one synchronisation after each): ms[0] the block-per-instance
+ * kernel, ms[1] the warp-per-instance kernel, ms[2] the hand-off launch that
+ * resumes the warp kernel's long instances (CUDA events recorded inside the
+ * graph, on the stream each kernel runs on).  0 for a kernel the batch does
+ * not use. */
+gbpf_status gbpf_batch_kernel_times(gbpf_batch *b, int repeats, double ms[3]);
+
 /* Per-instance results of the last batch solve (any pointer may be NULL);
  * V/theta/P/Q packed like the inputs. */
 gbpf_status gbpf_batch_results(gbpf_batch *b, int *iterations, int *status, double *final_mismatch,
