@@ -1426,18 +1426,18 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
     if (ba.queue_len) {
         CK(cudaEventRecord(fork, st));
         CK(cudaStreamWaitEvent(side, fork, 0));
-        if (timed) CK(cudaEventRecord(kev[0], side));
+        if (timed) CK(cudaEventRecordWithFlags(kev[0], side, cudaEventRecordExternal));
         if (fp32) k_nr_block<float><<<grid_blocks, kThreads, smem, side>>>(ba);
         else k_nr_block<double><<<grid_blocks, kThreads, smem, side>>>(ba);
         CK(cudaGetLastError());
-        if (timed) CK(cudaEventRecord(kev[1], side));
+        if (timed) CK(cudaEventRecordWithFlags(kev[1], side, cudaEventRecordExternal));
     }
     if (wa.queue_len) {
-        if (timed) CK(cudaEventRecord(kev[2], st));
+        if (timed) CK(cudaEventRecordWithFlags(kev[2], st, cudaEventRecordExternal));
         if (fp32) k_nr_warp<float><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wa);
         else k_nr_warp<double><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wa);
         CK(cudaGetLastError());
-        if (timed) CK(cudaEventRecord(kev[3], st));
+        if (timed) CK(cudaEventRecordWithFlags(kev[3], st, cudaEventRecordExternal));
         if (wa.handoff_it > 0) {
             // the instances the warps parked, one block each, same arithmetic
             Args ra = wa;
@@ -1450,7 +1450,7 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
             if (fp32) k_nr_block<float><<<resume_grid, kThreads, resume_smem, st>>>(ra);
             else k_nr_block<double><<<resume_grid, kThreads, resume_smem, st>>>(ra);
             CK(cudaGetLastError());
-            if (timed) CK(cudaEventRecord(kev[4], st));
+            if (timed) CK(cudaEventRecordWithFlags(kev[4], st, cudaEventRecordExternal));
         }
     }
     if (ba.queue_len) {
