@@ -186,8 +186,8 @@ int main(int argc, char **argv) {
     }
     if (banner) std::printf(o.laconic_mode ? "%s\n\n" : "\n\n%s\n\n", banner);
     else std::printf("[METODO] METODO INVALIDO LIDO DO ARQUIVO!\n\n");
-    if (o.metodo != GBPF_METODO_ESPARSO && o.metodo != GBPF_METODO_NDA)
-        std::fprintf(stderr, "gbpf: metodo %s runs the GPU sparse solve (no host or dense library solve)\n",
+    if (o.metodo != GBPF_METODO_ESPARSO && o.metodo != GBPF_METODO_DENSO && o.metodo != GBPF_METODO_NDA)
+        std::fprintf(stderr, "gbpf: metodo %s runs the GPU sparse solve (no host library solve)\n",
                      banner ? banner : "?");
 
     // GPU banner of initGPU (GPU/sistema.cuh:426-468)

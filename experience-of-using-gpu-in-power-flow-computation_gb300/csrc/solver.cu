@@ -90,6 +90,11 @@ struct Dev {
     const int *fl_skm, *fl_smk;
     const double *fl_phi, *fl_bkm, *fl_bmk;
     double *Pdp, *Ppd, *Qdp, *Qpd;
+    // metodo = denso: the dense Jacobian / LU factor [N x N], column-major, and
+    // its row interchanges; dense_rule selects calcYbus's off-diagonal rule
+    double *A;
+    int *ipiv;
+    int N, dense_rule;
 };
 
 __device__ __forceinline__ bool stopped(const Dev &d, int guard) {
@@ -116,14 +121,23 @@ __global__ void k_ybus_stamps(Dev d) {
 }
 
 // One slot per thread: contributions summed left to right in triplet order.
+// metodo = denso builds Ybus with calcYbus (GPU/sistema.h:673-703), which
+// assigns the off-diagonal entries branch by branch instead of summing them:
+// there an off-diagonal slot takes its last contribution only (the two agree
+// unless two branches join the same buses in opposite directions).
 __global__ void k_ybus_sum(Dev d) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.nnzY) return;
     double2 acc = make_double2(0, 0);
-    for (int c = d.cptr[s]; c < d.cptr[s + 1]; c++) {
+    int c0 = d.cptr[s];
+    if (d.dense_rule && c0 < d.cptr[s + 1]) {
+        const int src = d.csrc[c0];
+        if (src >= 0 && (src & 3) < 2) c0 = d.cptr[s + 1] - 1;
+    }
+    for (int c = c0; c < d.cptr[s + 1]; c++) {
         const int src = d.csrc[c];
         const double2 v = src >= 0 ? d.stamp[src] : make_double2(d.gsh[-1 - src], d.bsh[-1 - src]);
-        if (c == d.cptr[s]) acc = v;
+        if (c == c0) acc = v;
         else { acc.x += v.x; acc.y += v.y; }
     }
     d.yval[s] = acc;
@@ -404,6 +418,12 @@ __global__ void k_flows(Dev d) {
     d.Qpd[b] = -Vm * Vm * (ymk.y + d.fl_bmk[b]) + Vm * Vk * ymk.y * ca - Vm * Vk * ymk.x * (-sa);
 }
 
+#include "dense.cuh"
+
+// Largest dense system of metodo = denso: a 16384 x 16384 FP64 matrix (2 GiB),
+// 8,193 buses; the right-hand side of the triangular solves sits in shared memory.
+constexpr int kDenseMaxN = 16384;
+
 // ------------------------------------------------------------------ host side
 #define CK(call)                                                                     \
     do {                                                                             \
@@ -480,6 +500,25 @@ struct gbpf_solver {
             k_bsolve<<<cdiv_int(cnt, W), T, 0, stream>>>(d, beg, cnt, guard);
         }
     }
+    // metodo = denso: dense Jacobian, blocked LU with partial pivoting, the
+    // triangular solves, update
+    void launch_step_dense(int guard) {
+        const int T = 256, N = d.N;
+        k_dzero<<<std::min(cdiv_int((long long)N * N / 2, T), 4096), T, 0, stream>>>(d, guard);
+        k_dfill<<<cdiv_int(g.nB, T), T, 0, stream>>>(d, guard);
+        for (int k0 = 0; k0 < N; k0 += kDPanel) {
+            const int k1 = std::min(N, k0 + kDPanel);
+            k_dpanel<<<1, kDPanelThreads, 0, stream>>>(d, k0, guard);
+            k_dlaswp<<<cdiv_int(N, T), T, 0, stream>>>(d, k0, guard);
+            if (k1 < N) {
+                k_dtrsm<<<cdiv_int(N - k1, 128), 128, 0, stream>>>(d, k0, guard);
+                const int t = cdiv_int(N - k1, 64);
+                k_dgemm<<<dim3(t, t), 256, 0, stream>>>(d, k0, guard);
+            }
+        }
+        k_dsolve<<<1, kDSolveThreads, (size_t)N * sizeof(double), stream>>>(d, guard);
+        k_update<<<cdiv_int(S.n, T), T, 0, stream>>>(d, guard);
+    }
     void launch_eval(int guard) {  // injections, limits, mismatch
         const int T = 256;
         k_phasor<<<cdiv_int(g.nB, T), T, 0, stream>>>(d, guard);
@@ -499,6 +538,11 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
     device = dev;
     if (g.nB < 2 || g.slack < 1) { set_error("grid needs at least two buses and one slack"); return GBPF_E_INPUT; }
     if (o.no_max_iter < 0) { set_error("no_max_iter < 0"); return GBPF_E_INPUT; }
+    if (o.metodo == GBPF_METODO_DENSO && 2LL * (g.nB - 1) > kDenseMaxN) {
+        set_error("metodo = denso: the dense Jacobian of " + std::to_string(g.nB) + " buses exceeds " +
+                  std::to_string(kDenseMaxN) + " x " + std::to_string(kDenseMaxN) + "; use esparso");
+        return GBPF_E_UNSUPPORTED;
+    }
     for (int b = 0; b < g.nL; b++)
         if (g.r[b] == 0.0 && g.x[b] == 0.0) { set_error("branch with zero impedance"); return GBPF_E_INPUT; }
     using clk = std::chrono::steady_clock;
@@ -550,6 +594,12 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
         d = Dev{};
         d.nB = nB; d.nL = nL; d.nnzY = y.nnz; d.slack = g.slack - 1; d.nPV = g.nPV;
         d.n = n; d.nup = nup; d.max_iter = o.no_max_iter; d.lim = o.lim_inj_reat; d.tol = o.tolerancia;
+        d.dense_rule = o.metodo == GBPF_METODO_DENSO;
+        d.N = d.dense_rule ? 2 * n : 0;
+        if (d.dense_rule) {
+            d.A = A.take<double>((size_t)d.N * d.N);
+            d.ipiv = A.take<int>(d.N);
+        }
         d.hist_cap = hist_cap;
         d.yptr = A.take<int>(nB + 1); d.ycol = A.take<int>(y.nnz); d.yval = A.take<double2>(y.nnz);
         d.cptr = A.take<int>(y.nnz + 1); d.csrc = A.take<int>(y.csrc.size());
@@ -658,6 +708,8 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
 }
 
 gbpf_status gbpf_solver::build_graph() {
+    if (d.dense_rule)
+        CK(cudaFuncSetAttribute(k_dsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, d.N * (int)sizeof(double)));
     CK(cudaGraphCreate(&graph, 0));
     cudaGraphConditionalHandle h;
     CK(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault));
@@ -684,7 +736,8 @@ gbpf_status gbpf_solver::build_graph() {
     CK(cudaGraphAddNode(&wnode, graph, last.data(), nullptr, last.size(), &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     CK(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    launch_step(1);
+    if (d.dense_rule) launch_step_dense(1);
+    else launch_step(1);
     launch_eval(1);
     k_control<<<1, 1, 0, stream>>>(d, h, 1);
     CK(cudaStreamEndCapture(stream, &g2));
@@ -697,6 +750,10 @@ gbpf_status gbpf_solver::build_graph() {
     CK(cudaGraphGetNodes(graph, nullptr, &nn));
     graph_nodes = (int)nn;
     kernels_per_iter = nfl() + nbl() + 3 + 3 + (opt.lim_inj_reat && g.nPV ? 1 : 0) + 1;
+    if (d.dense_rule) {
+        const int panels = (d.N + kDPanel - 1) / kDPanel;
+        kernels_per_iter = 2 + 4 * panels - 2 + 2 + 3 + (opt.lim_inj_reat && g.nPV ? 1 : 0) + 1;
+    }
     return GBPF_OK;
 }
 

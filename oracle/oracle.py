@@ -42,7 +42,7 @@ def lib():
         L.orc_h_open.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double,
                                  ctypes.c_char_p, ctypes.c_int]
         for name in ("orc_h_close", "orc_h_dims", "orc_h_bus", "orc_h_pv", "orc_h_branch",
-                     "orc_h_set_bus", "orc_h_ybus", "orc_h_pq", "orc_h_result"):
+                     "orc_h_set_bus", "orc_h_ybus", "orc_h_pq", "orc_h_result", "orc_h_set_dense_ybus"):
             getattr(L, name).restype = None
         L.orc_h_jacobian.restype = ctypes.c_int
         L.orc_h_solve.restype = ctypes.c_int
@@ -122,6 +122,11 @@ class Grid:
             self.V0 = np.array(V, np.float64)
         if theta is not None:
             self.theta0 = np.array(theta, np.float64)
+
+    def set_dense_ybus(self, dense=True):
+        """Ybus by calcYbus's rule (metodo = denso: off-diagonal entries
+        assigned branch by branch, GPU/sistema.h:673-703) or calcYbusSp's."""
+        lib().orc_h_set_dense_ybus(self.h, int(bool(dense)))
 
     def ybus(self):
         rp = np.zeros(self.nB + 1, np.int32)

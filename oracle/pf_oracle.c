@@ -306,6 +306,13 @@ int orc_build_ybus(const orc_grid *g, orc_ybus *y) {
     int nnz = 0;
     for (int i = 0; i < nt; i++) {
         if (nnz > 0 && i > 0 && t[i].r == t[i - 1].r && t[i].c == t[i - 1].c) {
+            if (g->dense_ybus && t[i].r != t[i].c) {
+                /* calcYbus (GPU/sistema.h:673-703, metodo = denso) assigns the
+                 * off-diagonal entries branch by branch: the last one stays */
+                y->re[nnz - 1] = t[i].re;
+                y->im[nnz - 1] = t[i].im;
+                continue;
+            }
             y->re[nnz - 1] += t[i].re;
             y->im[nnz - 1] += t[i].im;
         } else {

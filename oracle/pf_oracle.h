@@ -35,6 +35,7 @@ typedef struct {
     int *de, *para;                   /* [nL] 1-based, after parallel merge */
     double *z_re, *z_im, *bsh_br, *tap_re, *tap_im, *phi; /* [nL] */
     int n_warn;                       /* parallel branches with different taps */
+    int dense_ybus;                   /* 1: calcYbus's rule (metodo = denso) */
 } orc_grid;
 
 /* Row-major CSR Ybus, sorted columns, explicit diagonal (GPU/sistema.h:705-758). */

@@ -23,6 +23,14 @@ void *orc_h_open(const char *path, double v0, double th0, char *err, int errlen)
     return h;
 }
 
+/* Ybus by calcYbus's rule (metodo = denso) when dense != 0, else calcYbusSp's. */
+void orc_h_set_dense_ybus(void *hv, int dense) {
+    orc_handle *h = (orc_handle *)hv;
+    h->g.dense_ybus = dense != 0;
+    orc_ybus_free(&h->y);
+    orc_build_ybus(&h->g, &h->y);
+}
+
 void orc_h_close(void *hv) {
     orc_handle *h = (orc_handle *)hv;
     if (!h) return;
