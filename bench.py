@@ -57,7 +57,7 @@ def args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gbpf", choices=["gbpf", "reference"])
-    p.add_argument("--workload", default="c2", choices=["c2", "c2-plain", "c3", "c4", "c5"])
+    p.add_argument("--workload", default="c2", choices=["c2", "c2-plain", "c2-dense", "c3", "c4", "c5", "c5-dense"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--scenarios", type=int, default=0,
                    help="scenarios per step (c2, c4: default 4096; c5: held-out, default 8192); smaller cases "
@@ -604,13 +604,17 @@ def peak_src_note(src):
 
 
 def bench_single(a, gb, np, rank, dev, world, dist):
+    dense = a.workload.endswith("-dense")
+    lim = 1
     if a.workload == "c3":
         g, desc = gb.generate(3, BASE_SEED + 3, tiles=128), "15104-bus (128 tied 118-bus copies), limits on"
+    elif a.workload == "c5-dense":
+        g, desc, lim = gb.generate(3, BASE_SEED + 5, tiles=16), "1888-bus (16 tied 118-bus copies), limits off", 0
     else:
         g, desc = gb.generate(2, BASE_SEED + 2), "118-bus meshed (1 slack/53 PV/64 PQ, 186 branches), limits on"
     cdf = write_grid(g)
     grid = gb.read_grid(cdf)
-    s = gb.Solver(grid, device=dev, tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1, metodo=0)
+    s = gb.Solver(grid, device=dev, tolerancia=1e-8, no_max_iter=100, lim_inj_reat=lim, metodo=1 if dense else 0)
     first = s.solve(full=False)
     assert first["converged"] and first["final_mismatch"] <= 1e-8, first
     info = s.info()
@@ -633,16 +637,29 @@ def bench_single(a, gb, np, rank, dev, world, dist):
         r = s.solve(full=False)
         s.state()
     t_e2e = max_over_ranks(time.perf_counter() - t0, dist, dev)
-    prof = s.profile(10)
-    top = max(prof, key=lambda k: prof[k]["ms"])
     peak, src = peak_hbm()
-    achieved = prof[top]["bytes"] / (prof[top]["ms"] * 1e-3) / 1e9
+    if dense:
+        # metodo = denso: per Newton iteration the N x N FP64 matrix is written
+        # by the fill and read and written once by the LU's panel sweep (lower
+        # bound on its traffic); the LU does 2/3 N^3 + 2 N^2 flops
+        N = 2 * (grid.nB - 1)
+        it = max(1, first["iterations"])
+        t_it = t_dev / a.steps / it
+        achieved = 3 * N * N * 8 / t_it / 1e9
+        top, prof = "dense fill + LU + solves", {"matrix_order": N, "iterations": first["iterations"],
+                                                 "ms_per_iteration": 1e3 * t_it,
+                                                 "lu_fp64_gflops": (2 / 3 * N ** 3 + 2 * N * N) / t_it / 1e9}
+    else:
+        prof = s.profile(10)
+        top = max(prof, key=lambda k: prof[k]["ms"])
+        achieved = prof[top]["bytes"] / (prof[top]["ms"] * 1e-3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": max(3, a.warmup), "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": a.workload, "grid": desc, "nB": grid.nB, "tolerance": 1e-8, "lim_inj_reat": 1,
-                   "form": "plain FP64, one solve per step", "iterations": first["iterations"],
+        "config": {"workload": a.workload, "grid": desc, "nB": grid.nB, "tolerance": 1e-8, "lim_inj_reat": lim,
+                   "form": ("metodo = denso: dense FP64 Jacobian and LU with partial pivoting, one solve per step"
+                            if dense else "plain FP64, one solve per step"), "iterations": first["iterations"],
                    "solver": info, "parallelism": f"replicas x{world}",
                    "l2": "working set fits in L2; no flush"},
         "e2e": {"value": world * a.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * grid.nB * 8,
@@ -653,7 +670,7 @@ def bench_single(a, gb, np, rank, dev, world, dist):
         "gpu_launches": a.steps * (6 + max(1, first["iterations"]) * info["kernels_per_iteration"] + 1),
     }
     if rank == 0 and not a.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_repeat(cdf, 1)
+        line["cpu_baseline"] = cpu_baseline_repeat(cdf, lim)
     return line
 
 
