@@ -20,6 +20,7 @@ CLI_PATH = os.path.join(HERE, "lib", "gbpf")
 OK, E_INPUT, E_SINGULAR, E_NOCONV, E_CUDA, E_TIMEOUT, E_OOM, E_ARG, E_UNSUPPORTED = range(9)
 METODO = {"esparso": 0, "denso": 1, "hibridoA": 2, "hibridoB": 3, "hibridoC": 4, "nda": 5}
 PREC_FP64, PREC_FP32_IR = 0, 1
+YBUS_CDF, YBUS_MATPOWER = 0, 1
 EVENT_TEXT = {
     1: "PV -> PQ (limite superior)",
     2: "PQ (limite inferior) -> PQ (limite superior)",
@@ -42,6 +43,7 @@ EXPORTS = [
     "gbpf_mlp_create", "gbpf_mlp_free", "gbpf_mlp_dims", "gbpf_mlp_set_data", "gbpf_mlp_train", "gbpf_mlp_predict",
     "gbpf_mlp_gradients", "gbpf_mlp_params", "gbpf_mlp_set_params", "gbpf_mlp_norm", "gbpf_mlp_set_norm",
     "gbpf_batch_solve_warm", "gbpf_mlp_set_loss_metric", "gbpf_solver_setup_times", "gbpf_batch_kernel_times",
+    "gbpf_grid_write_m", "gbpf_grid_ybus_form", "gbpf_grid_set_ybus_form",
 ]
 
 
@@ -226,6 +228,18 @@ class Grid:
 
     def write_cdf(self, path, title="synthetic grid"):
         _check(lib().gbpf_grid_write_cdf(self.h, os.fsencode(path), title.encode()), "gbpf_grid_write_cdf")
+
+    def write_m(self, path, title="synthetic grid"):
+        """MATPOWER case (version 2) that read_grid and the reference's .m reader read back."""
+        _check(lib().gbpf_grid_write_m(self.h, os.fsencode(path), title.encode()), "gbpf_grid_write_m")
+
+    @property
+    def ybus_form(self):
+        """YBUS_CDF (calcYbusSp_eficinte) or YBUS_MATPOWER (calcYbusSp_Matpower, .m input)."""
+        return int(lib().gbpf_grid_ybus_form(self.h))
+
+    def set_ybus_form(self, form):
+        _check(lib().gbpf_grid_set_ybus_form(self.h, int(form)), "gbpf_grid_set_ybus_form")
 
 
 def read_grid(path, v_inicial=1.0, theta_inicial=0.0):

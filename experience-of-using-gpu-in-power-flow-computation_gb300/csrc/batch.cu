@@ -963,20 +963,27 @@ __device__ __forceinline__ double2 cdiv2(double a, double b, double c, double d)
     return make_double2((a * r + b) / den, (b * r - a) / den);
 }
 
-// Branch stamps of calcYbusSp_eficinte (GPU/sistema.h:708-719).
+// Branch stamps of calcYbusSp_eficinte (GPU/sistema.h:708-719) or, for a grid
+// read from a .m file, calcYbusSp_Matpower (GPU/sistema.h:760-855): the
+// from-side term (y + jb/2)/|t|^2 and the off-diagonals as (-1/conj(t))/z, (-1/t)/z.
 __global__ void k_batch_stamps(const double *r, const double *x, const double *bch, const double *tre,
-                               const double *tim, double2 *stamp, int nL) {
+                               const double *tim, double2 *stamp, int nL, int form) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nL) return;
     const double2 y = cdiv2(1.0, 0.0, r[b], x[b]);
-    const double2 ft = cdiv2(-y.x, -y.y, tre[b], -tim[b]);
-    const double2 tf = cdiv2(-y.x, -y.y, tre[b], tim[b]);
     double m = hypot(tre[b], tim[b]);
     m = 1.0 / (m * m);
     const double hb = bch[b] / 2.;
-    stamp[4 * b + 0] = ft;
-    stamp[4 * b + 1] = tf;
-    stamp[4 * b + 2] = make_double2(m * y.x, m * y.y + hb);
+    if (form == GBPF_YBUS_MATPOWER) {
+        const double2 uf = cdiv2(-1.0, 0.0, tre[b], -tim[b]), ut = cdiv2(-1.0, 0.0, tre[b], tim[b]);
+        stamp[4 * b + 0] = cdiv2(uf.x, uf.y, r[b], x[b]);
+        stamp[4 * b + 1] = cdiv2(ut.x, ut.y, r[b], x[b]);
+        stamp[4 * b + 2] = make_double2(y.x * m, (y.y + hb) * m);
+    } else {
+        stamp[4 * b + 0] = cdiv2(-y.x, -y.y, tre[b], -tim[b]);
+        stamp[4 * b + 1] = cdiv2(-y.x, -y.y, tre[b], tim[b]);
+        stamp[4 * b + 2] = make_double2(m * y.x, m * y.y + hb);
+    }
     stamp[4 * b + 3] = make_double2(y.x, y.y + hb);
 }
 
@@ -1301,7 +1308,8 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
     DevBuf mem, tmp;
     CK(cudaMalloc(&mem.p, blob.size()));
     CK(cudaMemcpyAsync(mem.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, stream));
-    // Ybus values into the blob, assembled on the device (calcYbusSp_eficinte)
+    // Ybus values into the blob, assembled on the device (calcYbusSp_eficinte or
+    // calcYbusSp_Matpower, by the grid's form)
     size_t used = 0;
     auto tk = [&](size_t bytes) { used = align_up(used, 256); size_t r = used; used += bytes; return r; };
     const size_t t_cptr = tk((y.nnz + 1) * 4), t_csrc = tk(y.csrc.size() * 4), t_stamp = tk(16 * (size_t)(4 * nL + 1));
@@ -1322,7 +1330,8 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
     CK(cudaMemcpyAsync(tb + t_bsh, g.bsh.data(), nB * 8, cudaMemcpyHostToDevice, stream));
     if (nL) k_batch_stamps<<<(nL + 255) / 256, 256, 0, stream>>>((const double *)(tb + t_r), (const double *)(tb + t_x),
                                                                  (const double *)(tb + t_b), (const double *)(tb + t_tre),
-                                                                 (const double *)(tb + t_tim), (double2 *)(tb + t_stamp), nL);
+                                                                 (const double *)(tb + t_tim), (double2 *)(tb + t_stamp), nL,
+                                                                 g.ybus_form);
     k_batch_ybus<<<(y.nnz + 255) / 256, 256, 0, stream>>>((const int *)(tb + t_cptr), (const int *)(tb + t_csrc),
                                                           (const double2 *)(tb + t_stamp), (const double *)(tb + t_gsh),
                                                           (const double *)(tb + t_bsh),

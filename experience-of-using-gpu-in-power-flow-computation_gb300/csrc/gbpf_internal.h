@@ -26,6 +26,7 @@ struct Grid {
     std::vector<int> de, para;                                        // [nL] 1-based
     std::vector<double> r, x, bch, tap_re, tap_im, phase;             // [nL]
     std::vector<std::string> notices;                                 // reader notices
+    int ybus_form = GBPF_YBUS_CDF;                                    // branch stamps of the Ybus
 
     double Pliq(int k) const { return Pg[k] - Pload[k]; }
     double Qliq(int k) const { return Qg[k] - Qload[k]; }

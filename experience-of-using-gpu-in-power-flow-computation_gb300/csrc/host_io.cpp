@@ -260,6 +260,184 @@ void cdiv(double a, double b, double c, double d, double *re, double *im) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// MATPOWER case reader: lerArquivoMatPOWEReficiente (GPU/m.h:485-599) with
+// cleanLine / readMatrix (GPU/m.h:445-483) and storeMatPOWER (GPU/m.h:296-443).
+// A grid read here takes calcYbusSp_Matpower's branch stamps (GPU/main.cu:78-81).
+// ---------------------------------------------------------------------------
+
+// cleanLine: drop a '%' comment, then trailing blanks, one ';' and blanks
+// ('\r' counts as a blank, so CRLF files read like LF files).
+void m_clean(std::string &s) {
+    const size_t c = s.find('%');
+    if (c != std::string::npos) s.resize(c);
+    auto blank = [](char ch) { return ch == ' ' || ch == '\t' || ch == '\r'; };
+    while (!s.empty() && blank(s.back())) s.pop_back();
+    if (!s.empty() && s.back() == ';') s.pop_back();
+    while (!s.empty() && blank(s.back())) s.pop_back();
+}
+
+// Removes the first "mpc.<name>[ \t]*=[ \t]*" (and '[' when `bracket`) from s,
+// as the regex_search / regex_replace pairs of GPU/m.h:505-536 do.
+bool m_take(std::string &s, const std::string &name, bool bracket) {
+    const std::string key = "mpc." + name;
+    for (size_t p = s.find(key); p != std::string::npos; p = s.find(key, p + 1)) {
+        size_t q = p + key.size();
+        while (q < s.size() && (s[q] == ' ' || s[q] == '\t')) q++;
+        if (q >= s.size() || s[q] != '=') continue;
+        q++;
+        while (q < s.size() && (s[q] == ' ' || s[q] == '\t')) q++;
+        if (bracket) {
+            if (q >= s.size() || s[q] != '[') continue;
+            q++;
+        }
+        s.erase(p, q - p);
+        return true;
+    }
+    return false;
+}
+
+// One matrix row: tokens split on tabs (the reference's tokenize(line, "\t"),
+// GPU/m.h:122-142) or blanks, each read by strtod like std::stod.  False when
+// a token does not start with a number (std::stod would throw there).
+bool m_row(const std::string &s, std::vector<std::vector<double>> &rows) {
+    std::vector<double> r;
+    const char *p = s.c_str();
+    for (;;) {
+        while (*p == '\t' || *p == ' ' || *p == '\r') p++;
+        if (!*p) break;
+        char *end;
+        const double v = std::strtod(p, &end);
+        if (end == p) return false;
+        while (*end && *end != '\t' && *end != ' ' && *end != '\r') end++;
+        r.push_back(v);
+        p = end;
+    }
+    if (!r.empty()) rows.push_back(std::move(r));
+    return true;
+}
+
+gbpf_status read_m(const std::string &path, double v0, double th0, Grid &g, std::string &err) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) { err = "Erro na leitura do arquivo. Ele existe? " + path; return GBPF_E_INPUT; }
+    static const char *NAMES[3] = {"bus", "gen", "branch"};
+    std::vector<std::vector<double>> M[3];
+    double base = 0;
+    bool have_base = false, bad = false;
+    std::string line;
+    while (std::getline(f, line)) {
+        m_clean(line);
+        if (line.empty()) continue;
+        for (int k = 0; k < 3; k++) {
+            if (!m_take(line, NAMES[k], true)) continue;
+            // readMatrix: rows up to and including the line that holds ']'
+            for (;;) {
+                const bool last = line.find(']') != std::string::npos;
+                if (last) line.erase(std::remove(line.begin(), line.end(), ']'), line.end());
+                m_clean(line);
+                if (!line.empty() && !m_row(line, M[k])) bad = true;
+                if (last || !std::getline(f, line)) break;
+            }
+            break;
+        }
+        if (m_take(line, "baseMVA", false)) {
+            line.erase(std::remove_if(line.begin(), line.end(), [](char c) { return c == '"' || c == '\''; }),
+                       line.end());
+            char *end;
+            base = std::strtod(line.c_str(), &end);
+            have_base = end != line.c_str();
+        }
+    }
+    if (bad) { err = "a matrix entry of the .m file is not a number"; return GBPF_E_INPUT; }
+    if (!have_base) { err = "mpc.baseMVA not found"; return GBPF_E_INPUT; }
+    // columns this reader uses: bus BUS_I..BASE_KV, gen GEN_BUS..QMIN, branch F_BUS..SHIFT
+    static const size_t NEED[3] = {10, 5, 10};
+    for (int k = 0; k < 3; k++)
+        for (size_t i = 0; i < M[k].size(); i++)
+            if (M[k][i].size() < NEED[k]) {
+                err = std::string("mpc.") + NAMES[k] + " row " + std::to_string(i + 1) + " has " +
+                      std::to_string(M[k][i].size()) + " columns, " + std::to_string(NEED[k]) + " needed";
+                return GBPF_E_INPUT;
+            }
+    const auto &B = M[0], &G = M[1], &R = M[2];
+    int nsl = 0;
+    for (const auto &b : B) {
+        const int t = (int)b[1];
+        if (t < 1 || t > 3) { err = "ERRO: valor de tipo de barra invalido! (" + std::to_string(t) + ")"; return GBPF_E_INPUT; }
+        nsl += t == 3;
+    }
+    if (nsl != 1) {
+        err = nsl ? "ERRO: mais de uma barrra swing definida!" : "no slack bus (type 3) in the file";
+        return GBPF_E_INPUT;
+    }
+    const int nB = (int)B.size();
+    g = Grid();
+    g.nB = nB;
+    g.baseMVA = base;
+    g.ybus_form = GBPF_YBUS_MATPOWER;
+    g.id.assign(nB, 0); g.type.assign(nB, 0);
+    g.V0.assign(nB, v0); g.theta0.assign(nB, th0);
+    g.Pload.assign(nB, 0); g.Qload.assign(nB, 0); g.Pg.assign(nB, 0); g.Qg.assign(nB, 0);
+    g.gsh.assign(nB, 0); g.bsh.assign(nB, 0); g.Vbase.assign(nB, 0);
+    std::vector<double> qmax_bus(nB, 0), qmin_bus(nB, 0);
+    for (int k = 0; k < nB; k++) {
+        const auto &b = B[k];
+        const int t = (int)b[1];
+        g.id[k] = (int)b[0];
+        g.type[k] = t == 1 ? 0 : t;  // MATPOWER PQ = 1 is the CDF's 0
+        int gi = -1;
+        if (t != 1) {
+            // the first generator row on the bus (std::find over GEN_BUS); a
+            // generator on a PQ bus is never looked up
+            for (size_t j = 0; j < G.size(); j++)
+                if ((int)G[j][0] == g.id[k]) { gi = (int)j; break; }
+            g.V0[k] = b[7];
+            if (t == 3) g.theta0[k] = b[8] * PI_REF / 180.;
+            if (gi < 0) {
+                g.notices.push_back("barra " + std::to_string(g.id[k]) + ", de tipo " + (t == 2 ? "PV" : "VO") +
+                                    ", n\xc3\xa3o possui de gera\xc3\xa7\xc3\xa3o!");
+            } else if (t == 2) {
+                qmax_bus[k] = G[gi][3] / base;
+                qmin_bus[k] = G[gi][4] / base;
+            }
+        }
+        g.Pload[k] = b[2] / base;
+        g.Qload[k] = b[3] / base;
+        g.Pg[k] = gi < 0 ? 0 : G[gi][1] / base;
+        g.Qg[k] = gi < 0 ? 0 : G[gi][2] / base;
+        g.Vbase[k] = b[9];
+        g.bsh[k] = b[5] / base;
+        g.gsh[k] = b[4] / base;
+    }
+    g.rebuild_lists();
+    for (int i = 0; i < g.nPV; i++) {
+        const int k = g.pv[i] - 1;
+        g.Qmax.push_back(qmax_bus[k]);
+        g.Qmin.push_back(qmin_bus[k]);
+        g.Vset.push_back(g.V0[k]);
+    }
+    // branches: id2i (GPU/sistema.h:465-472), every row its own branch (the
+    // reference's storeMatPOWER never merges repeated pairs)
+    for (const auto &r : R) {
+        const int idde = (int)r[0], idpa = (int)r[1];
+        int de = 0, pa = 0;
+        for (int b = 0; b < nB; b++) if (g.id[b] == idde) { de = b + 1; break; }
+        for (int b = 0; b < nB; b++) if (g.id[b] == idpa) { pa = b + 1; break; }
+        if (!de || !pa) {
+            err = "branch " + std::to_string(idde) + "-" + std::to_string(idpa) + " names an unknown bus";
+            return GBPF_E_INPUT;
+        }
+        const double a = r[8], ph = r[9] * PI_REF / 180.;
+        g.de.push_back(de); g.para.push_back(pa);
+        g.r.push_back(r[2]); g.x.push_back(r[3]); g.bch.push_back(r[4]);
+        g.phase.push_back(ph);
+        if (a != 0.) { g.tap_re.push_back(a * std::cos(ph)); g.tap_im.push_back(a * std::sin(ph)); }
+        else { g.tap_re.push_back(std::cos(ph)); g.tap_im.push_back(std::sin(ph)); }
+        g.nL++;
+    }
+    return GBPF_OK;
+}
+
 gbpf_status read_cdf(const std::string &path, double v0, double th0, Grid &g, std::string &err) {
     const size_t dot = path.find_last_of('.');
     std::string ext = dot == std::string::npos ? std::string() : path.substr(dot + 1);
@@ -267,7 +445,7 @@ gbpf_status read_cdf(const std::string &path, double v0, double th0, Grid &g, st
     const Cols *C;
     if (ext == "cdf") C = &CDF_COLS;
     else if (ext == "cdfx") C = &CDFX_COLS;
-    else if (ext == "m") { err = "MATPOWER .m input is not supported"; return GBPF_E_UNSUPPORTED; }
+    else if (ext == "m") return read_m(path, v0, th0, g, err);
     else { err = "nda == " + ext; return GBPF_E_INPUT; }
 
     std::ifstream f(path, std::ios::binary);
@@ -600,6 +778,67 @@ extern "C" gbpf_status gbpf_grid_write_cdf(const gbpf_grid *h, const char *path,
     std::fprintf(f, "TIE LINES FOLLOWS                     0 ITEMS\r\n-999\r\nEND OF DATA\r\n");
     std::fclose(f);
     if (bad) { set_error("a written line contains the section terminator -999"); return GBPF_E_INPUT; }
+    return GBPF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// MATPOWER writer (rows read back by read_m above)
+// ---------------------------------------------------------------------------
+
+extern "C" gbpf_status gbpf_grid_write_m(const gbpf_grid *h, const char *path, const char *title) {
+    if (!h || !path) return GBPF_E_ARG;
+    const Grid &g = h->g;
+    FILE *f = std::fopen(path, "wb");
+    if (!f) { set_error(std::string("cannot write ") + path); return GBPF_E_INPUT; }
+    const double base = g.baseMVA;
+    auto row = [f](const std::vector<double> &v) {
+        for (double x : v) std::fprintf(f, "\t%.17g", x);
+        std::fprintf(f, ";\n");
+    };
+    std::fprintf(f, "function mpc = gbpf_case\n%%%s\n\n", title ? title : "synthetic grid");
+    std::fprintf(f, "%%%% MATPOWER Case Format : Version 2\nmpc.version = '2';\n\n");
+    std::fprintf(f, "%%%%-----  Power Flow Data  -----%%%%\n%%%% system MVA base\nmpc.baseMVA = %.17g;\n\n", base);
+    std::fprintf(f, "%%%% bus data\n%%\tbus_i\ttype\tPd\tQd\tGs\tBs\tarea\tVm\tVa\tbaseKV\tzone\tVmax\tVmin\nmpc.bus = [\n");
+    for (int k = 0; k < g.nB; k++) {
+        const int t = g.type[k];
+        const bool gen = t >= 2;
+        // generation at a PQ bus folds into its load: the injection is kept
+        const double pd = gen ? g.Pload[k] : g.Pload[k] - g.Pg[k];
+        const double qd = gen ? g.Qload[k] : g.Qload[k] - g.Qg[k];
+        row({(double)g.id[k], (double)(t <= 1 ? 1 : t), pd * base, qd * base, g.gsh[k] * base, g.bsh[k] * base, 1,
+             g.V0[k], t == 3 ? g.theta0[k] * 180.0 / PI_REF : 0.0, g.Vbase[k], 1, 1.1, 0.9});
+    }
+    std::fprintf(f, "];\n\n%%%% generator data\n%%\tbus\tPg\tQg\tQmax\tQmin\tVg\tmBase\tstatus\tPmax\tPmin\tPc1\tPc2"
+                    "\tQc1min\tQc1max\tQc2min\tQc2max\tramp_agc\tramp_10\tramp_30\tramp_q\tapf\nmpc.gen = [\n");
+    std::vector<double> qmax(g.nB, 0), qmin(g.nB, 0);
+    for (int i = 0; i < g.nPV; i++) { qmax[g.pv[i] - 1] = g.Qmax[i]; qmin[g.pv[i] - 1] = g.Qmin[i]; }
+    for (int k = 0; k < g.nB; k++) {
+        if (g.type[k] < 2) continue;
+        const bool sl = g.type[k] == 3;
+        std::vector<double> v = {(double)g.id[k], g.Pg[k] * base, g.Qg[k] * base, sl ? 9999.0 : qmax[k] * base,
+                                 sl ? -9999.0 : qmin[k] * base, g.V0[k], base, 1, std::max(0.0, 2 * g.Pg[k] * base), 0};
+        v.resize(21, 0.0);
+        row(v);
+    }
+    std::fprintf(f, "];\n\n%%%% branch data\n%%\tfbus\ttbus\tr\tx\tb\trateA\trateB\trateC\tratio\tangle\tstatus"
+                    "\tangmin\tangmax\nmpc.branch = [\n");
+    for (int b = 0; b < g.nL; b++) {
+        const double a = std::hypot(g.tap_re[b], g.tap_im[b]);
+        const bool line = a == 1.0 && g.phase[b] == 0.0;
+        row({(double)g.id[g.de[b] - 1], (double)g.id[g.para[b] - 1], g.r[b], g.x[b], g.bch[b], 0, 0, 0,
+             line ? 0.0 : a, g.phase[b] * 180.0 / PI_REF, 1, -360, 360});
+    }
+    std::fprintf(f, "];\n");
+    const bool ok = std::fclose(f) == 0;
+    if (!ok) { set_error(std::string("cannot write ") + path); return GBPF_E_INPUT; }
+    return GBPF_OK;
+}
+
+extern "C" int gbpf_grid_ybus_form(const gbpf_grid *h) { return h ? h->g.ybus_form : -1; }
+
+extern "C" gbpf_status gbpf_grid_set_ybus_form(gbpf_grid *h, int form) {
+    if (!h || (form != GBPF_YBUS_CDF && form != GBPF_YBUS_MATPOWER)) return GBPF_E_ARG;
+    h->g.ybus_form = form;
     return GBPF_OK;
 }
 

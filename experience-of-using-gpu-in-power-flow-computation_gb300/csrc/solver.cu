@@ -95,6 +95,7 @@ struct Dev {
     double *A;
     int *ipiv;
     int N, dense_rule;
+    int ybus_form;  // gbpf_ybus_form of the grid
 };
 
 __device__ __forceinline__ bool stopped(const Dev &d, int guard) {
@@ -102,21 +103,29 @@ __device__ __forceinline__ bool stopped(const Dev &d, int guard) {
 }
 
 // ------------------------------------------------------------------ Ybus
-// Branch stamps of calcYbusSp_eficinte (GPU/sistema.h:708-719):
-// (de,para) -y/conj(t), (para,de) -y/t, (de,de) y/|t|^2 + jb/2, (para,para) y + jb/2.
+// Branch stamps of calcYbusSp_eficinte (GPU/sistema.h:708-719) and calcYbus
+// (metodo = denso): (de,para) -y/conj(t), (para,de) -y/t, (de,de) y/|t|^2 + jb/2,
+// (para,para) y + jb/2.  calcYbusSp_Matpower (GPU/sistema.h:760-855, .m input):
+// (de,para) (-1/conj(t))/z, (para,de) (-1/t)/z, (de,de) (y + jb/2)/|t|^2.
 __global__ void k_ybus_stamps(Dev d) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= d.nL) return;
-    const double2 y = cdiv(1.0, 0.0, d.br_r[b], d.br_x[b]);
+    const double zr = d.br_r[b], zi = d.br_x[b];
+    const double2 y = cdiv(1.0, 0.0, zr, zi);
     const double tr = d.br_tre[b], ti = d.br_tim[b];
-    const double2 ft = cdiv(-y.x, -y.y, tr, -ti);
-    const double2 tf = cdiv(-y.x, -y.y, tr, ti);
     double a = hypot(tr, ti);
     a = 1.0 / (a * a);
     const double hb = d.br_b[b] / 2.;
-    d.stamp[4 * b + 0] = ft;
-    d.stamp[4 * b + 1] = tf;
-    d.stamp[4 * b + 2] = make_double2(a * y.x, a * y.y + hb);
+    if (d.ybus_form == GBPF_YBUS_MATPOWER && !d.dense_rule) {
+        const double2 uf = cdiv(-1.0, 0.0, tr, -ti), ut = cdiv(-1.0, 0.0, tr, ti);
+        d.stamp[4 * b + 0] = cdiv(uf.x, uf.y, zr, zi);
+        d.stamp[4 * b + 1] = cdiv(ut.x, ut.y, zr, zi);
+        d.stamp[4 * b + 2] = make_double2(y.x * a, (y.y + hb) * a);
+    } else {
+        d.stamp[4 * b + 0] = cdiv(-y.x, -y.y, tr, -ti);
+        d.stamp[4 * b + 1] = cdiv(-y.x, -y.y, tr, ti);
+        d.stamp[4 * b + 2] = make_double2(a * y.x, a * y.y + hb);
+    }
     d.stamp[4 * b + 3] = make_double2(y.x, y.y + hb);
 }
 
@@ -595,6 +604,7 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
         d.nB = nB; d.nL = nL; d.nnzY = y.nnz; d.slack = g.slack - 1; d.nPV = g.nPV;
         d.n = n; d.nup = nup; d.max_iter = o.no_max_iter; d.lim = o.lim_inj_reat; d.tol = o.tolerancia;
         d.dense_rule = o.metodo == GBPF_METODO_DENSO;
+        d.ybus_form = g.ybus_form;
         d.N = d.dense_rule ? 2 * n : 0;
         if (d.dense_rule) {
             d.A = A.take<double>((size_t)d.N * d.N);

@@ -56,6 +56,14 @@ typedef enum {
 /* output_bench values (GPU/sistInfo.h:31-35, :190-203). */
 typedef enum { GBPF_BENCH_ALL = 0, GBPF_BENCH_SCREEN = 1, GBPF_BENCH_FILE = 2 } gbpf_output_bench;
 
+/* Branch stamps of a grid's Ybus.  GBPF_YBUS_CDF: calcYbusSp_eficinte
+ * (GPU/sistema.h:705-758), the line charging b/2 added undivided on both
+ * sides.  GBPF_YBUS_MATPOWER: calcYbusSp_Matpower (GPU/sistema.h:760-855),
+ * chosen by the reference for .m input (GPU/main.cu:78-81): the from-side
+ * term (1/z + j b/2) divided by |tap|^2.  metodo = denso always uses calcYbus
+ * (GPU/sistema.h:673-703), whose stamps are the CDF form. */
+typedef enum { GBPF_YBUS_CDF = 0, GBPF_YBUS_MATPOWER = 1 } gbpf_ybus_form;
+
 /* Numeric form of the linear solve (not a data.txt key of the reference). */
 typedef enum {
     GBPF_PREC_FP64 = 0,       /* FP64 LU and triangular solves (oracle-matching) */
@@ -102,10 +110,12 @@ gbpf_status gbpf_options_load(const char *path, gbpf_options *o, char *echo, siz
 typedef struct gbpf_grid gbpf_grid;
 
 /* lerArquivoEAlocarMemoria (GPU/arquivo.h:250-295): .cdf (GPU/sistema.h:
- * 386-638) and .cdfx (GPU/arquivo.h:4-248).  Buses start at v_inicial /
+ * 386-638), .cdfx (GPU/arquivo.h:4-248) and MATPOWER .m (GPU/m.h:296-622;
+ * such a grid gets GBPF_YBUS_MATPOWER).  Buses start at v_inicial /
  * theta_inicial except PV and slack voltages and the slack angle, which come
  * from the file.  Notices the reference prints while reading (parallel
- * branches whose taps differ) are written to msg. */
+ * branches whose taps differ, PV or slack buses without a generator row) are
+ * written to msg. */
 gbpf_status gbpf_grid_read(const char *path, double v_inicial, double theta_inicial,
                            gbpf_grid **out, char *msg, size_t msg_cap);
 
@@ -149,6 +159,19 @@ gbpf_status gbpf_grid_set_buses(gbpf_grid *g, const double *Pload, const double 
 /* Writes the grid as a fixed-column common-data-format file that the reader
  * above (and the reference's readCDF) reads back. */
 gbpf_status gbpf_grid_write_cdf(const gbpf_grid *g, const char *path, const char *title);
+
+/* Writes the grid as a MATPOWER case (version 2, tab-separated rows of 13 bus,
+ * 21 generator and 13 branch columns) that the reader above and the
+ * reference's lerArquivoMatPOWEReficiente read back.  Values are printed with
+ * 17 significant digits.  Generation at a PQ bus is written as negative load,
+ * because the reference's .m reader looks generators up for PV and slack
+ * buses only (GPU/m.h:310-357). */
+gbpf_status gbpf_grid_write_m(const gbpf_grid *g, const char *path, const char *title);
+
+/* The grid's Ybus form (gbpf_ybus_form); the setter lets a grid built by
+ * gbpf_grid_create take the MATPOWER form. */
+int gbpf_grid_ybus_form(const gbpf_grid *g);
+gbpf_status gbpf_grid_set_ybus_form(gbpf_grid *g, int form);
 
 /* Seeded synthetic grids (no counterpart in the reference, which ships IEEE
  * cases only): kind 1 = 14-bus ring-plus-chords grid, 2 = 118-bus meshed grid,

@@ -42,8 +42,9 @@ def lib():
         L.orc_h_open.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double,
                                  ctypes.c_char_p, ctypes.c_int]
         for name in ("orc_h_close", "orc_h_dims", "orc_h_bus", "orc_h_pv", "orc_h_branch",
-                     "orc_h_set_bus", "orc_h_ybus", "orc_h_pq", "orc_h_result", "orc_h_set_dense_ybus"):
+                     "orc_h_set_bus", "orc_h_ybus", "orc_h_pq", "orc_h_result", "orc_h_set_dense_ybus", "orc_h_set_ybus_form"):
             getattr(L, name).restype = None
+        L.orc_h_ybus_form.restype = ctypes.c_int
         L.orc_h_jacobian.restype = ctypes.c_int
         L.orc_h_solve.restype = ctypes.c_int
         L.orc_h_sparse_solve.restype = ctypes.c_int
@@ -56,7 +57,8 @@ def _p(a):
 
 
 class Grid:
-    """One grid read by the oracle's CDF reader (GPU/sistema.h:386-638)."""
+    """One grid read by the oracle's reader: CDF (GPU/sistema.h:386-638) or
+    MATPOWER .m (GPU/m.h:296-622, Ybus by calcYbusSp_Matpower)."""
 
     def __init__(self, path, v_inicial=1.0, theta_inicial=0.0):
         L = lib()
@@ -87,6 +89,7 @@ class Grid:
         b = [np.zeros(m) for _ in range(6)]
         L.orc_h_branch(self.h, _p(self.de), _p(self.para), *[_p(a) for a in b])
         self.z_re, self.z_im, self.bsh_br, self.tap_re, self.tap_im, self.phi = b
+        self.ybus_form = int(L.orc_h_ybus_form(self.h))
 
     def close(self):
         if self.h:
@@ -127,6 +130,11 @@ class Grid:
         """Ybus by calcYbus's rule (metodo = denso: off-diagonal entries
         assigned branch by branch, GPU/sistema.h:673-703) or calcYbusSp's."""
         lib().orc_h_set_dense_ybus(self.h, int(bool(dense)))
+
+    def set_ybus_form(self, form):
+        """0: calcYbusSp_eficinte's branch stamps, 1: calcYbusSp_Matpower's."""
+        lib().orc_h_set_ybus_form(self.h, int(form))
+        self.ybus_form = int(form)
 
     def ybus(self):
         rp = np.zeros(self.nB + 1, np.int32)

@@ -114,6 +114,7 @@ int orc_read_cdf(const char *path, double v_inicial, double theta_inicial,
     const cdf_cols *C;
     if (!strcmp(ext, "cdf")) C = &COLS_CDF;
     else if (!strcmp(ext, "cdfx")) C = &COLS_CDFX;
+    else if (!strcmp(ext, "m")) return orc_read_m(path, v_inicial, theta_inicial, g, err, errlen);
     else { snprintf(err, errlen, "unsupported input extension '%s'", ext); return 1; }
 
     lines_t L;
@@ -255,6 +256,230 @@ int orc_read_cdf(const char *path, double v_inicial, double theta_inicial,
     return 0;
 }
 
+/* ------------------------------------------------------------------------- */
+/* MATPOWER case reader: lerArquivoMatPOWEReficiente GPU/m.h:485-599,        */
+/* cleanLine / readMatrix GPU/m.h:445-483, storeMatPOWER GPU/m.h:296-443     */
+/* ------------------------------------------------------------------------- */
+
+/* cleanLine (GPU/m.h:445-449): drop a '%' comment, then trailing blanks, one
+ * ';' and blanks.  A '\r' counts as a blank here. */
+static void m_clean(char *s) {
+    char *c = strchr(s, '%');
+    if (c) *c = 0;
+    size_t n = strlen(s);
+    while (n && (s[n - 1] == ' ' || s[n - 1] == '\t' || s[n - 1] == '\r')) n--;
+    if (n && s[n - 1] == ';') n--;
+    while (n && (s[n - 1] == ' ' || s[n - 1] == '\t' || s[n - 1] == '\r')) n--;
+    s[n] = 0;
+}
+
+/* Removes the first "mpc.<name>[ \t]*=[ \t]*" (plus '[' when bracket) from s
+ * and returns 1, as the regex_search + regex_replace pairs of GPU/m.h:505-536
+ * do; 0 when s holds no such text. */
+static int m_take(char *s, const char *name, int bracket) {
+    char key[32];
+    snprintf(key, sizeof key, "mpc.%s", name);
+    for (char *p = strstr(s, key); p; p = strstr(p + 1, key)) {
+        char *q = p + strlen(key);
+        while (*q == ' ' || *q == '\t') q++;
+        if (*q != '=') continue;
+        q++;
+        while (*q == ' ' || *q == '\t') q++;
+        if (bracket) { if (*q != '[') continue; q++; }
+        memmove(p, q, strlen(q) + 1);
+        return 1;
+    }
+    return 0;
+}
+
+typedef struct { int rows, cap; int *ncol; double **v; } mmat_t;
+
+/* One matrix row: tokens split on tabs (tokenize(line, "\t"), GPU/m.h:122-142;
+ * blanks split too), each read by strtod like std::stod.  A token with no
+ * number in front sets *bad (std::stod would throw). */
+static void m_row(mmat_t *m, const char *s, int *bad) {
+    double *row = NULL;
+    int n = 0, cap = 0;
+    const char *p = s;
+    for (;;) {
+        while (*p == '\t' || *p == ' ' || *p == '\r') p++;
+        if (!*p) break;
+        char *end;
+        double v = strtod(p, &end);
+        if (end == p) *bad = 1;
+        while (*end && *end != '\t' && *end != ' ' && *end != '\r') end++;
+        if (n == cap) { cap = cap ? 2 * cap : 16; row = (double *)realloc(row, cap * sizeof(double)); }
+        row[n++] = v;
+        p = end;
+    }
+    if (!n) return;
+    if (m->rows == m->cap) {
+        m->cap = m->cap ? 2 * m->cap : 64;
+        m->ncol = (int *)realloc(m->ncol, m->cap * sizeof(int));
+        m->v = (double **)realloc(m->v, m->cap * sizeof(double *));
+    }
+    m->ncol[m->rows] = n;
+    m->v[m->rows++] = row;
+}
+
+static void m_free(mmat_t *m) {
+    for (int i = 0; i < m->rows; i++) free(m->v[i]);
+    free(m->ncol); free(m->v);
+    memset(m, 0, sizeof(*m));
+}
+
+int orc_read_m(const char *path, double v_inicial, double theta_inicial,
+               orc_grid *g, char *err, int errlen) {
+    memset(g, 0, sizeof(*g));
+    lines_t L;
+    if (read_lines(path, &L)) { snprintf(err, errlen, "cannot open %s", path); return 1; }
+    mmat_t M[3] = {{0}};
+    static const char *NAMES[3] = {"bus", "gen", "branch"};
+    double base = 0;
+    int have_base = 0, bad = 0;
+    for (int li = 0; li < L.cnt; li++) {
+        char *s = L.l[li];
+        m_clean(s);
+        if (!*s) continue;
+        for (int k = 0; k < 3; k++) {
+            if (!m_take(s, NAMES[k], 1)) continue;
+            /* readMatrix (GPU/m.h:451-483): rows up to the line holding ']' */
+            for (;;) {
+                const int last = strchr(s, ']') != NULL;
+                if (last) { char *w = s; for (char *r = s; *r; r++) if (*r != ']') *w++ = *r; *w = 0; }
+                m_clean(s);
+                if (*s) m_row(&M[k], s, &bad);
+                if (last || li + 1 >= L.cnt) break;
+                s = L.l[++li];
+            }
+            break;
+        }
+        if (m_take(s, "baseMVA", 0)) {
+            char *w = s;
+            for (char *r = s; *r; r++) if (*r != '"' && *r != '\'') *w++ = *r;
+            *w = 0;
+            char *end;
+            base = strtod(s, &end);
+            have_base = end != s;
+        }
+    }
+    free_lines(&L);
+    int rc = 1;
+    if (bad) { snprintf(err, errlen, "a matrix entry is not a number"); goto out; }
+    if (!have_base) { snprintf(err, errlen, "mpc.baseMVA not found"); goto out; }
+    /* columns read: bus BUS_I..BASE_KV, gen GEN_BUS..QMIN, branch F_BUS..SHIFT */
+    static const int NEED[3] = {10, 5, 10};
+    for (int k = 0; k < 3; k++)
+        for (int i = 0; i < M[k].rows; i++)
+            if (M[k].ncol[i] < NEED[k]) {
+                snprintf(err, errlen, "mpc.%s row %d has %d columns, %d needed", NAMES[k], i + 1, M[k].ncol[i], NEED[k]);
+                goto out;
+            }
+    /* lerMatPowerEAlocarMemoria GPU/m.h:603-622: sizes by bus type */
+    int nbus = M[0].rows, nPQ = 0, nPV = 0, nsl = 0;
+    for (int i = 0; i < nbus; i++) {
+        int t = (int)M[0].v[i][1];
+        if (t == 1) nPQ++;
+        else if (t == 2) nPV++;
+        else if (t == 3) nsl++;
+        else { snprintf(err, errlen, "ERRO: valor de tipo de barra invalido! (%d)", t); goto out; }
+    }
+    if (nsl != 1) {
+        snprintf(err, errlen, nsl ? "ERRO: mais de uma barrra swing definida!" : "no slack bus (type 3) in the file");
+        goto out;
+    }
+    int n = nPQ + nPV + 1;
+    g->nB = n; g->nPQ = nPQ; g->nPV = nPV; g->baseMVA = base;
+    g->id = (int *)xcalloc(n, sizeof(int));
+    g->type = (int *)xcalloc(n, sizeof(int));
+    g->V = (double *)xcalloc(n, sizeof(double));
+    g->theta = (double *)xcalloc(n, sizeof(double));
+    g->Pload = (double *)xcalloc(n, sizeof(double));
+    g->Qload = (double *)xcalloc(n, sizeof(double));
+    g->Pg = (double *)xcalloc(n, sizeof(double));
+    g->Qg = (double *)xcalloc(n, sizeof(double));
+    g->Pliq = (double *)xcalloc(n, sizeof(double));
+    g->Qliq = (double *)xcalloc(n, sizeof(double));
+    g->gsh = (double *)xcalloc(n, sizeof(double));
+    g->bsh = (double *)xcalloc(n, sizeof(double));
+    g->Vbase = (double *)xcalloc(n, sizeof(double));
+    g->barrasPV = (int *)xcalloc(nPV, sizeof(int));
+    g->barrasPQ = (int *)xcalloc(nPQ, sizeof(int));
+    g->Qmin = (double *)xcalloc(nPV, sizeof(double));
+    g->Qmax = (double *)xcalloc(nPV, sizeof(double));
+    g->Vset = (double *)xcalloc(nPV, sizeof(double));
+    g->ybus_form = 1; /* calcYbusSp_Matpower, GPU/main.cu:78-81 */
+    for (int i = 0; i < n; i++) { g->V[i] = v_inicial; g->theta[i] = theta_inicial; }
+    /* storeMatPOWER GPU/m.h:304-384 */
+    int ipv = 0, ipq = 0;
+    for (int k = 0; k < n; k++) {
+        const double *b = M[0].v[k];
+        const int t = (int)b[1];
+        g->id[k] = (int)b[0];
+        int gi = -1;
+        if (t == 1) {
+            g->type[k] = 0;
+            g->barrasPQ[ipq++] = k + 1;
+        } else {
+            g->type[k] = t;
+            g->V[k] = b[7];
+            if (t == 3) { g->slack = k + 1; g->theta[k] = b[8] * PI_REF / 180.; }
+            for (int j = 0; j < M[1].rows; j++) if ((int)M[1].v[j][0] == g->id[k]) { gi = j; break; }
+            if (t == 2) {
+                g->barrasPV[ipv] = k + 1;
+                g->Vset[ipv] = g->V[k];
+                /* a PV bus with no generator keeps zero limits */
+                if (gi >= 0) { g->Qmax[ipv] = M[1].v[gi][3] / base; g->Qmin[ipv] = M[1].v[gi][4] / base; }
+                else g->n_warn++;
+                ipv++;
+            }
+        }
+        g->Pload[k] = b[2] / base;
+        g->Qload[k] = b[3] / base;
+        g->Pg[k] = gi < 0 ? 0 : M[1].v[gi][1] / base;
+        g->Qg[k] = gi < 0 ? 0 : M[1].v[gi][2] / base;
+        g->Vbase[k] = b[9];
+        g->bsh[k] = b[5] / base;
+        g->gsh[k] = b[4] / base;
+        g->Pliq[k] = g->Pg[k] - g->Pload[k];
+        g->Qliq[k] = g->Qg[k] - g->Qload[k];
+    }
+    /* branches GPU/m.h:386-407: id2i, no merge of repeated pairs */
+    int nL = M[2].rows;
+    g->de = (int *)xcalloc(nL, sizeof(int));
+    g->para = (int *)xcalloc(nL, sizeof(int));
+    g->z_re = (double *)xcalloc(nL, sizeof(double));
+    g->z_im = (double *)xcalloc(nL, sizeof(double));
+    g->bsh_br = (double *)xcalloc(nL, sizeof(double));
+    g->tap_re = (double *)xcalloc(nL, sizeof(double));
+    g->tap_im = (double *)xcalloc(nL, sizeof(double));
+    g->phi = (double *)xcalloc(nL, sizeof(double));
+    for (int i = 0; i < nL; i++) {
+        const double *r = M[2].v[i];
+        const int idde = (int)r[0], idpa = (int)r[1];
+        int de = 0, pa = 0;
+        for (int b = 0; b < n; b++) { if (g->id[b] == idde) { de = b + 1; break; } } /* id2i GPU/sistema.h:465-472 */
+        for (int b = 0; b < n; b++) { if (g->id[b] == idpa) { pa = b + 1; break; } }
+        if (!de || !pa) {
+            snprintf(err, errlen, "branch %d-%d names an unknown bus", idde, idpa);
+            orc_grid_free(g);
+            goto out;
+        }
+        const double a = r[8], ph = r[9] * PI_REF / 180.;
+        g->de[i] = de; g->para[i] = pa;
+        g->z_re[i] = r[2]; g->z_im[i] = r[3];
+        g->phi[i] = ph;
+        if (a != 0.) { g->tap_re[i] = a * cos(ph); g->tap_im[i] = a * sin(ph); }
+        else { g->tap_re[i] = cos(ph); g->tap_im[i] = sin(ph); }
+        g->bsh_br[i] = r[4];
+    }
+    g->nL = nL;
+    rc = 0;
+out:
+    for (int k = 0; k < 3; k++) m_free(&M[k]);
+    return rc;
+}
+
 void orc_grid_free(orc_grid *g) {
     free(g->id); free(g->type); free(g->V); free(g->theta); free(g->Pload); free(g->Qload);
     free(g->Pg); free(g->Qg); free(g->Pliq); free(g->Qliq); free(g->gsh); free(g->bsh);
@@ -287,12 +512,27 @@ int orc_build_ybus(const orc_grid *g, orc_ybus *y) {
         cdiv(1., 0., g->z_re[i], g->z_im[i], &ar, &ai);
         int f = g->de[i] - 1, to = g->para[i] - 1;
         double vr, vi;
+        double d = hypot(g->tap_re[i], g->tap_im[i]);
+        d = 1. / (d * d);
+        if (g->ybus_form == 1 && !g->dense_ybus) {
+            /* calcYbusSp_Matpower (GPU/sistema.h:760-855): Yft = (-1/conj(t))/z,
+             * Ytf = (-1/t)/z, Yff = (1/z + j b/2)/|t|^2, Ytt = 1/z + j b/2, summed
+             * through the incidence products Cf'Yf + Ct'Yt + Ysh */
+            double ur, ui;
+            cdiv(-1., 0., g->tap_re[i], -g->tap_im[i], &ur, &ui);
+            cdiv(ur, ui, g->z_re[i], g->z_im[i], &vr, &vi);
+            t[k] = (trip_t){f, to, k, vr, vi}; k++;
+            cdiv(-1., 0., g->tap_re[i], g->tap_im[i], &ur, &ui);
+            cdiv(ur, ui, g->z_re[i], g->z_im[i], &vr, &vi);
+            t[k] = (trip_t){to, f, k, vr, vi}; k++;
+            t[k] = (trip_t){f, f, k, ar * d, (ai + g->bsh_br[i] / 2.) * d}; k++;
+            t[k] = (trip_t){to, to, k, ar, ai + g->bsh_br[i] / 2.}; k++;
+            continue;
+        }
         cdiv(-ar, -ai, g->tap_re[i], -g->tap_im[i], &vr, &vi); /* -aux/conj(t) */
         t[k] = (trip_t){f, to, k, vr, vi}; k++;
         cdiv(-ar, -ai, g->tap_re[i], g->tap_im[i], &vr, &vi);  /* -aux/t */
         t[k] = (trip_t){to, f, k, vr, vi}; k++;
-        double d = hypot(g->tap_re[i], g->tap_im[i]);
-        d = 1. / (d * d);
         t[k] = (trip_t){f, f, k, d * ar, d * ai + g->bsh_br[i] / 2.}; k++;
         t[k] = (trip_t){to, to, k, ar, ai + g->bsh_br[i] / 2.}; k++;
     }

@@ -34,8 +34,9 @@ typedef struct {
     double *Qmin, *Qmax, *Vset;       /* [nPV] limQinf, limQsup, VfixadaPV */
     int *de, *para;                   /* [nL] 1-based, after parallel merge */
     double *z_re, *z_im, *bsh_br, *tap_re, *tap_im, *phi; /* [nL] */
-    int n_warn;                       /* parallel branches with different taps */
+    int n_warn;                       /* parallel branches with different taps; PV buses with no generator (.m) */
     int dense_ybus;                   /* 1: calcYbus's rule (metodo = denso) */
+    int ybus_form;                    /* 0: calcYbusSp_eficinte, 1: calcYbusSp_Matpower (.m input) */
 } orc_grid;
 
 /* Row-major CSR Ybus, sorted columns, explicit diagonal (GPU/sistema.h:705-758). */
@@ -79,6 +80,9 @@ typedef struct {
  * Returns 0 on success, nonzero on error (message in err). */
 int orc_read_cdf(const char *path, double v_inicial, double theta_inicial,
                  orc_grid *g, char *err, int errlen);
+/* Read a MATPOWER case (.m): GPU/m.h:296-622.  Sets ybus_form = 1. */
+int orc_read_m(const char *path, double v_inicial, double theta_inicial,
+               orc_grid *g, char *err, int errlen);
 void orc_grid_free(orc_grid *g);
 
 int orc_build_ybus(const orc_grid *g, orc_ybus *y);

@@ -31,6 +31,15 @@ void orc_h_set_dense_ybus(void *hv, int dense) {
     orc_build_ybus(&h->g, &h->y);
 }
 
+/* 0: calcYbusSp_eficinte's branch stamps, 1: calcYbusSp_Matpower's (.m input). */
+int orc_h_ybus_form(void *hv) { return ((orc_handle *)hv)->g.ybus_form; }
+void orc_h_set_ybus_form(void *hv, int form) {
+    orc_handle *h = (orc_handle *)hv;
+    h->g.ybus_form = form;
+    orc_ybus_free(&h->y);
+    orc_build_ybus(&h->g, &h->y);
+}
+
 void orc_h_close(void *hv) {
     orc_handle *h = (orc_handle *)hv;
     if (!h) return;

@@ -5,7 +5,10 @@
 //   reader      CPU/leitura/arquivo.cpp, CPU/leitura/cdf.cpp (byte-identical
 //               logic to GPU/sistema.h:386-638)
 //   Ybus        calcYbusSp_eficinte CPU/esparso/spCalcYbus.cpp:92-144
-//               (same code as GPU/sistema.h:705-758)
+//               (same code as GPU/sistema.h:705-758); for .m input
+//               calcYbusSp_Matpower CPU/esparso/spCalcYbus.cpp:4-90
+//               (same code as GPU/sistema.h:760-855)
+//   .m reader   CPU/leitura/m.cpp (same logic as GPU/m.h:296-622)
 //   PQ          spCalcP / spCalcQ CPU/esparso/potencia/spCalcPQliq.cpp:3-45
 //               (same arithmetic as GPU/PQcalc.cuh:177-219)
 //   Jacobian    Jstencil0based + fillJstencil0based CPU/esparso/spCalcJac.cpp:54-224
@@ -22,6 +25,7 @@
 // Output: one JSON object on stdout with the grid sizes, the Newton history,
 // the switch events and the final state at %.17g.
 
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -59,7 +63,7 @@ static void jarr(const char *name, const double *v, int n, bool last = false) {
 
 int main(int argc, char **argv) {
     if (argc < 2) {
-        std::fprintf(stderr, "usage: ref_nr <file.cdf> [tol] [max_iter] [lim_inj_reat] [v_inicial] [theta_inicial]\n");
+        std::fprintf(stderr, "usage: ref_nr <file.cdf|.cdfx|.m> [tol] [max_iter] [lim_inj_reat] [v_inicial] [theta_inicial]\n");
         return 2;
     }
     global::arq_entrada = argv[1];
@@ -83,7 +87,14 @@ int main(int argc, char **argv) {
     ramoType R{};
     iterativoType I{};
     lerArquivoEAlocarMemoria(S, B, R, I);
-    calcYbusSp_eficinte(S, B, R);
+    // Ybus form by input kind, as GPU/main.cu:73-82 chooses it: .m files
+    // (global::isMatpower, GPU/arquivo.h:283-291) take calcYbusSp_Matpower.
+    const std::string in(argv[1]);
+    const size_t dot = in.find_last_of('.');
+    std::string ext = dot == std::string::npos ? std::string() : in.substr(dot + 1);
+    for (auto &c : ext) c = (char)std::tolower((unsigned char)c);
+    if (ext == "m") calcYbusSp_Matpower(S, B, R);
+    else calcYbusSp_eficinte(S, B, R);
 
     const int nB = S.nB, nPV = S.nPV, nPQ = S.nPQ;
     const double tol = global::tol;

@@ -5,9 +5,9 @@ oracle/_ref/ref_nr, built by oracle/ref/Makefile from the reference's CPU/ tree
 sources (reader, Ybus, injections, Jacobian pattern and values) with a driver
 that replays the reference GPU Newton loop and its limit rules.  Inputs are
 
-* the synthetic grids written here (c1.cdf: 14-bus, c2_*.cdf: 118-bus), which
-  are committed so that the GPU machine, which has no reference checkout, reads the
-  very same bytes, and
+* the synthetic grids written here (c1.cdf: 14-bus, c2_*.cdf: 118-bus, and the
+  MATPOWER cases m_edge.m and c2_tx.m), which are committed so that the GPU
+  box, which has no reference checkout, reads the very same bytes, and
 * the reference's IEEE cases, read in place from the reference checkout (only
   their solutions are stored, as ieee_*.json).
 
@@ -20,6 +20,8 @@ import json
 import os
 import subprocess
 import sys
+
+import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
@@ -36,10 +38,79 @@ def run_ref(path, tol, maxit, lim):
     out = subprocess.run([REF_NR, path, repr(tol), str(maxit), str(int(lim))], capture_output=True,
                          text=True, check=True).stdout
     r = json.loads(out)
-    r.pop("Y_re", None)
-    r.pop("Y_im", None)
+    if not path.endswith(".m"):  # .m cases keep calcYbusSp_Matpower's values
+        r.pop("Y_re", None)
+        r.pop("Y_im", None)
     r["file"] = os.path.basename(path)
     return r
+
+
+# A hand-written MATPOWER case for the reader's corner cases: non-consecutive
+# bus ids, a generator row on a PQ bus (never looked up), two generator rows on
+# one PV bus (the first is used), a repeated branch (kept as two branches), a
+# transformer with line charging (where calcYbusSp_Matpower's from-side
+# (1/z + jb/2)/|t|^2 differs from the CDF form), a phase shifter written with
+# ratio 0, comments, a blank line and a gencost block the reader skips.
+M_EDGE = """function mpc = m_edge
+%% six buses, eight branches
+mpc.version = '2';
+mpc.baseMVA = 100;
+
+%% bus data
+%\tbus_i\ttype\tPd\tQd\tGs\tBs\tarea\tVm\tVa\tbaseKV\tzone\tVmax\tVmin
+mpc.bus = [
+\t10\t3\t0\t0\t0\t0\t1\t1.02\t5\t230\t1\t1.1\t0.9;
+\t20\t2\t20\t10\t0\t0\t1\t1.01\t0\t230\t1\t1.1\t0.9;
+\t30\t1\t45\t15\t0\t0\t1\t1\t0\t230\t1\t1.1\t0.9;\t% a generator row names this PQ bus
+\t40\t1\t40\t5\t0\t19\t1\t1\t0\t230\t1\t1.1\t0.9;
+
+\t50\t2\t10\t3\t0\t0\t1\t0.995\t0\t230\t1\t1.1\t0.9;
+\t60\t1\t60\t12\t2\t-5\t1\t1\t0\t230\t1\t1.1\t0.9;
+];
+
+%% generator data
+mpc.gen = [
+\t10\t0\t0\t300\t-300\t1.02\t100\t1\t300\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0;
+\t20\t40\t0\t30\t-10\t1.01\t100\t1\t100\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0;
+\t30\t25\t5\t10\t-10\t1\t100\t1\t50\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0;
+\t50\t30\t0\t25\t-5\t0.995\t100\t1\t60\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0;
+\t50\t99\t0\t99\t-99\t1\t100\t1\t99\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0\t0;
+];
+
+%% branch data
+%\tfbus\ttbus\tr\tx\tb\trateA\trateB\trateC\tratio\tangle\tstatus\tangmin\tangmax
+mpc.branch = [
+\t10\t20\t0.01\t0.06\t0.05\t0\t0\t0\t0\t0\t1\t-360\t360;
+\t10\t20\t0.02\t0.08\t0.04\t0\t0\t0\t0\t0\t1\t-360\t360;
+\t20\t30\t0.005\t0.05\t0.03\t0\t0\t0\t0.97\t0\t1\t-360\t360;
+% a phase shifter written with ratio 0
+\t30\t40\t0\t0.04\t0\t0\t0\t0\t0\t-3\t1\t-360\t360;
+\t40\t50\t0.02\t0.1\t0.02\t0\t0\t0\t1.03\t2\t1\t-360\t360;
+\t50\t60\t0.015\t0.07\t0.02\t0\t0\t0\t0\t0\t1\t-360\t360;
+\t60\t10\t0.01\t0.05\t0.03\t0\t0\t0\t0\t0\t1\t-360\t360;
+\t20\t60\t0.03\t0.12\t0.025\t0\t0\t0\t0\t0\t1\t-360\t360;
+];
+
+%% generator cost data
+mpc.gencost = [
+\t2\t0\t0\t3\t0.01\t40\t0;
+];
+"""
+
+
+def with_transformer_charging(grid):
+    """The grid with line charging on its off-nominal-tap branches, so that the
+    two Ybus forms differ (same buses and branches otherwise)."""
+    b, br, pv = grid.buses(), grid.branches(), grid.pvpq()
+    tap = np.hypot(br["tap_re"], br["tap_im"])
+    bch = np.where(np.abs(tap - 1) > 1e-12, 0.04, br["bch"])
+    qmax = np.zeros(grid.nB)
+    qmin = np.zeros(grid.nB)
+    qmax[pv["pv"] - 1] = pv["Qmax"]
+    qmin[pv["pv"] - 1] = pv["Qmin"]
+    return gb.create_grid(b["type"], b["V0"], b["theta0"], br["from_bus"], br["to_bus"], br["r"], br["x"], bch,
+                          br["tap_re"], br["tap_im"], br["phase"], b["Pload"], b["Qload"], b["Pg"], b["Qg"],
+                          b["gsh"], b["bsh"], qmax, qmin, b["id"], grid.baseMVA)
 
 
 def write(name, rec):
@@ -73,6 +144,14 @@ def main():
             picked += 1
     if os.path.exists(os.path.join(HERE, "_probe.cdf")):
         os.remove(os.path.join(HERE, "_probe.cdf"))
+    # MATPOWER cases: the corner-case file above and the 118-bus base grid with
+    # charged transformers, both read by the reference's own .m reader
+    with open(os.path.join(HERE, "m_edge.m"), "w") as f:
+        f.write(M_EDGE)
+    cases += [("m_edge.m", 1e-8, 100, 0), ("m_edge.m", 1e-8, 100, 1)]
+    with_transformer_charging(gb.read_grid(os.path.join(HERE, "c2_base.cdf"))).write_m(
+        os.path.join(HERE, "c2_tx.m"), "config 2 118-bus, charged transformers")
+    cases += [("c2_tx.m", 1e-8, 100, 0), ("c2_tx.m", 1e-8, 100, 1)]
     index = []
     for name, tol, maxit, lim in cases:
         r = run_ref(os.path.join(HERE, name), tol, maxit, lim)

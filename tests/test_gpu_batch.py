@@ -36,7 +36,7 @@ def run_batch(gb, grids, inst_grid, Pl, Ql, Pg, **opts):
     return b, b.results()
 
 
-@pytest.mark.parametrize("cdf", ["c2_base.cdf", "c2_s3.cdf"])
+@pytest.mark.parametrize("cdf", ["c2_base.cdf", "c2_s3.cdf", "c2_tx.m"])
 def test_batch_fp64_matches_oracle(gb, oracle, cdf):
     path = os.path.join(GOLDEN, cdf)
     og = oracle.Grid(path)

@@ -20,7 +20,10 @@ pytestmark = pytest.mark.gpu
 DENSO = 1
 
 
-@pytest.mark.parametrize("case", committed_cases(), ids=lambda c: c["golden"])
+# The .m goldens hold calcYbusSp_Matpower's solution; metodo = denso builds
+# Ybus with calcYbus for every input (GPU/main.cu:73-76), checked below.
+@pytest.mark.parametrize("case", [c for c in committed_cases() if not c["cdf"].endswith(".m")],
+                         ids=lambda c: c["golden"])
 def test_dense_solve_matches_reference_golden(gb, case):
     grid, s = solver(gb, os.path.join(GOLDEN, case["cdf"]), tolerancia=case["tol"],
                      no_max_iter=case["max_iter"], lim_inj_reat=case["lim"], metodo=DENSO)
@@ -40,6 +43,13 @@ def _compare(gb, oracle, path, lim, dense_rule=True, max_iter=60):
     assert np.max(np.abs(res["V"] - ref["V"])) < STATE_TOL
     assert np.max(np.abs(res["theta"] - ref["theta"])) < STATE_TOL
     return res
+
+
+@pytest.mark.parametrize("name,lim", [("m_edge.m", 0), ("m_edge.m", 1), ("c2_tx.m", 1)])
+def test_dense_matpower_input_uses_calcybus(gb, oracle, name, lim):
+    """A .m grid under metodo = denso: calcYbus's stamps and off-diagonal
+    rule, not calcYbusSp_Matpower's."""
+    _compare(gb, oracle, os.path.join(GOLDEN, name), lim)
 
 
 @pytest.mark.parametrize("nbus", [14, 57, 118, 472])

@@ -37,7 +37,8 @@ def states(oracle_grid, n=3, seed=0):
     return out[:n]
 
 
-CDFS = ["c1.cdf", "c2_base.cdf", "c2_s3.cdf"]
+# the .m files take calcYbusSp_Matpower's stamps (GPU/main.cu:78-81)
+CDFS = ["c1.cdf", "c2_base.cdf", "c2_s3.cdf", "m_edge.m", "c2_tx.m"]
 
 
 @pytest.mark.parametrize("name", CDFS)

@@ -148,8 +148,11 @@ def test_reader_errors(gb, tmp_path):
     with pytest.raises(gb.GbpfError):
         gb.read_grid(_write(tmp_path, "h.cdf", "\r\n".join(short)))
     with pytest.raises(gb.GbpfError) as e:
-        gb.read_grid(_write(tmp_path, "x.m", "mpc = 1;"))
-    assert e.value.status == gb.E_UNSUPPORTED
+        gb.read_grid(_write(tmp_path, "x.m", "mpc = 1;"))  # a .m file with no mpc.baseMVA
+    assert e.value.status == gb.E_INPUT
+    with pytest.raises(gb.GbpfError) as e:
+        gb.read_grid(_write(tmp_path, "x.pwf", "TITU"))
+    assert e.value.status == gb.E_INPUT
 
 
 def test_generator_shapes_and_determinism(gb):
