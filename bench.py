@@ -60,9 +60,11 @@ def args():
     p.add_argument("--workload", default="c2", choices=["c2", "c2-plain", "c2-dense", "c3", "c4", "c5", "c5-dense"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--scenarios", type=int, default=0,
-                   help="scenarios per step (c2, c4: default 4096; c5: held-out, default 8192); smaller cases "
+                   help="scenarios per step (c2: default 32768, c4: 4096; c5: held-out, default 8192); smaller cases "
                         "for profiler captures")
     p.add_argument("--train", type=int, default=0, help="c5 training solves (default 50000)")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="batched workloads: keep the default launch plan instead of the autotuner's")
     return p.parse_args()
 
 
@@ -295,6 +297,13 @@ def sum_over_ranks(x, dist, device):
 # ---------------------------------------------------------------------- GPU
 
 
+def launches_per_solve(plan):
+    """Kernels of one batch graph launch: the block kernel, the warp kernel and
+    the hand-off launch, each when the plan uses it."""
+    warp = plan["warp_instances"] > 0
+    return int(plan["block_instances"] > 0) + int(warp) + int(warp and plan["handoff_it"] > 0)
+
+
 def bench_batch(a, gb, np, rank, dev, world, dist):
     N_SCEN = a.scenarios or (globals()["N_SCEN"] if a.workload == "c4" else N_SCEN_C2)
     if a.workload == "c4":
@@ -324,6 +333,13 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     opts = dict(tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1)
     fast = gb.Batch(grids, device=dev, precision=gb.PREC_FP32_IR, **opts)
     fast.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
+    fast.solve()
+    # launch plan: the autotuner's coordinate search on these instances (setup,
+    # outside the timed region), or the default plan with --no-autotune
+    tune = None
+    if not a.no_autotune:
+        plan, ms0, ms1 = fast.autotune(repeats=3)
+        tune = {"plan": plan, "ms_default_plan": ms0, "ms_chosen_plan": ms1}
     fast.solve()
     r = fast.results(state=False)
     conv = int((r["status"] == 0).sum())
@@ -369,6 +385,8 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
         plain = nconv / (time.perf_counter() - t0)
     slow = gb.Batch(grids, device=dev, precision=gb.PREC_FP64, **opts)
     slow.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
+    if not a.no_autotune:
+        slow.autotune(repeats=2)
     slow.solve()
     rs = slow.results(state=False)
     ms64 = slow.time(max(3, a.steps // 4)) / max(3, a.steps // 4)
@@ -401,7 +419,8 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
                    "speedup_vs_plain_fp64": (value / plain) if plain else None,
                    "l2": (f"inputs+outputs {nb * 8 * 9 / 2**20:.0f} MiB > L2 (129 MB)" if nb * 72 > L2_BYTES else
                           f"inputs+outputs {nb * 8 * 9 / 2**20:.1f} MiB < L2; no flush"),
-                   "batch": info, "parallelism": f"scenarios sharded x{world}"},
+                   "batch": info, "plan": fast.plan(), "autotune": tune,
+                   "parallelism": f"scenarios sharded x{world}"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nb * 8 * 5 + N_SCEN * 12,
                 "d2h_bytes_per_step": nb * 8 * 4 + N_SCEN * 20},
         "roofline": {"bound": "hbm", "kernel": main_kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -413,8 +432,7 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
                              "lives in shared memory, the step's remaining time is the hand-off launch of the few "
                              "instances that run all 100 iterations"},
         "clocks": clk.summary(),
-        "gpu_launches": a.steps * (1 + (1 if info["warp_instances"] else 0) +
-                                   (1 if info["warp_instances"] < N_SCEN else 0)),
+        "gpu_launches": a.steps * launches_per_solve(fast.plan()),
     }
     if rank == 0 and not a.no_cpu_baseline and cdf is not None:
         line["cpu_baseline"] = cpu_baseline_scenarios(cdf, 1, BASE_SEED + 7, N_SCEN)

@@ -44,6 +44,7 @@ EXPORTS = [
     "gbpf_mlp_gradients", "gbpf_mlp_params", "gbpf_mlp_set_params", "gbpf_mlp_norm", "gbpf_mlp_set_norm",
     "gbpf_batch_solve_warm", "gbpf_mlp_set_loss_metric", "gbpf_solver_setup_times", "gbpf_batch_kernel_times",
     "gbpf_grid_write_m", "gbpf_grid_ybus_form", "gbpf_grid_set_ybus_form",
+    "gbpf_batch_get_plan", "gbpf_batch_set_plan", "gbpf_batch_autotune",
 ]
 
 
@@ -516,6 +517,27 @@ class Batch:
         if st not in (OK, E_ARG):
             raise GbpfError(st, "gbpf_batch_events")
         return [tuple(int(x) for x in ev[4 * i:4 * i + 4]) for i in range(n.value)]
+
+    PLAN_KEYS = ("warp_mode", "warps_per_block", "handoff_it", "resume_group", "warp_group", "narrow",
+                 "warps_per_block_used", "warp_instances", "block_instances")
+
+    def plan(self):
+        """The launch plan (gbpf_batch_get_plan)."""
+        a = np.zeros(10, np.int32)
+        _check(lib().gbpf_batch_get_plan(self.h, _p(a)), "gbpf_batch_get_plan")
+        return dict(zip(self.PLAN_KEYS, (int(x) for x in a)))
+
+    def set_plan(self, warp_mode=1, warps_per_block=0, handoff_it=12, resume_group=1, warp_group=1, narrow=1):
+        a = np.array([warp_mode, warps_per_block, handoff_it, resume_group, warp_group, narrow], np.int32)
+        _check(lib().gbpf_batch_set_plan(self.h, _p(a)), "gbpf_batch_set_plan")
+
+    def autotune(self, repeats=3):
+        """Coordinate search over the launch plan on the current instances;
+        returns (plan, ms of the starting plan, ms of the chosen plan)."""
+        a = np.zeros(10, np.int32)
+        ms = np.zeros(2, np.float32)
+        _check(lib().gbpf_batch_autotune(self.h, int(repeats), _p(a), _p(ms)), "gbpf_batch_autotune")
+        return dict(zip(self.PLAN_KEYS, (int(x) for x in a))), float(ms[0]), float(ms[1])
 
     def info(self):
         a = np.zeros(8, np.int64)

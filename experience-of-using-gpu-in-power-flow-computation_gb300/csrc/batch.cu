@@ -96,7 +96,7 @@ template <typename B4> __device__ __forceinline__ B4 bcast(B4 v, int src) {
 struct TopoOff {
     int yptr, ycol, yval, type, pv_bus, Qmin, Qmax, bus_of_blk, up_ptr, up_col, dg_ptr, dg_pos, dg_k,
         og_ptr, og_a, og_b, flev_ptr, flev_steps, blev_ptr, blev_steps, ysl, rbus, cbus, fent_ptr, fent_p,
-        fent_j, lvl_group, yval32;
+        fent_j, lvl_group, lvl_group_w, lvl_narrow, yval32;
 };
 struct Topo {
     int nB, nL, n, nup, nnzY, nPV, nfl, nbl, fac_smem, blob_smem, blob_bytes;
@@ -115,7 +115,11 @@ struct TopoView {
     // row in the block kernel: [3 * l] pivots and [3 * l + 1] entries of
     // forward level l, [3 * l + 2] rows of backward level l
     const int *lvl_group;
-    const float2 *yval32;  // Ybus values rounded to FP32 (the FP32-LU form's Jacobian)
+    const int *lvl_group_w;  // the same for the 32 lanes of the warp kernel
+    // per level: bit 0 forward level l, bit 1 backward level l has at most 32
+    // pivots and 32 entries (rows): the block kernel runs it on one warp
+    const int *lvl_narrow;
+    const float2 *yval32;    // Ybus values rounded to FP32 (the FP32-LU form's Jacobian)
 };
 __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     TopoView v;
@@ -132,6 +136,8 @@ __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     v.fent_ptr = (const int *)(b + o.fent_ptr); v.fent_p = (const int *)(b + o.fent_p);
     v.fent_j = (const int *)(b + o.fent_j);
     v.lvl_group = (const int *)(b + o.lvl_group);
+    v.lvl_group_w = (const int *)(b + o.lvl_group_w);
+    v.lvl_narrow = (const int *)(b + o.lvl_narrow);
     v.yval32 = (const float2 *)(b + o.yval32);
     return v;
 }
@@ -167,6 +173,12 @@ struct Args {
     int handoff_it;
     int *handoff_q, *handoff_n;
     int resume, no_group;
+    // warp kernel: lanes grouped per pivot / entry / row on levels with few of
+    // them (lvl_group_w); 0 keeps one lane per pivot, entry and row
+    int warp_group;
+    // block kernel: levels with at most 32 pivots and entries (rows) run on
+    // warp 0 alone (lvl_narrow); 0 runs every level on the whole block
+    int narrow;
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
@@ -207,17 +219,47 @@ template <typename TJ> __host__ __device__ inline size_t scratch_bytes(int n, in
     return align_up(sizeof(B4) * ((size_t)n + 2 * (size_t)nup), 32) + align_up(sizeof(B4) * n, 32);
 }
 
-__device__ __forceinline__ double block_max(double v, double *red) {
-    for (int o = 16; o > 0; o >>= 1) {
-        const double t = __shfl_xor_sync(0xffffffffu, v, o);
-        v = (t > v || t != t) ? t : v;
-    }
+// Maxima of |x| over FP64 values taken on their bit patterns: with the sign
+// bit cleared, the unsigned order of the patterns is the order of the
+// magnitudes, and every NaN pattern lies above +inf, so a NaN wins the
+// maximum as the FP64 comparison chains did.  Integer instructions instead of
+// FP64 compares (GB300 runs FP64 at a small fraction of its FP32 rate).
+constexpr unsigned long long kAbsMask = 0x7fffffffffffffffull, kInfBits = 0x7ff0000000000000ull;
+__device__ __forceinline__ unsigned long long abits(double x) {
+    return (unsigned long long)__double_as_longlong(x) & kAbsMask;
+}
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
+    return a > b ? a : b;
+}
+__device__ __forceinline__ unsigned long long warp_umax(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v = umax64(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ unsigned long long block_umax(unsigned long long v, unsigned long long *red) {
+    v = warp_umax(v);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
-    double m = red[0];
-    for (int w = 1; w < kWarps; w++) m = (red[w] > m || red[w] != red[w]) ? red[w] : m;
+    unsigned long long m = red[0];
+    for (int w = 1; w < kWarps; w++) m = umax64(m, red[w]);
     __syncthreads();
     return m;
+}
+
+// P + jQ of bus k: conj(sum_m Y_km e_m) times e_k, e = V (cos th + j sin th),
+// with fused multiply-adds (four per Ybus entry)
+__device__ __forceinline__ void injection(const int *yptr, const int *ycol, const double2 *yval, const double2 *ef,
+                                          int k, double &P, double &Q) {
+    double ir = 0, ii = 0;
+    for (int p = yptr[k]; p < yptr[k + 1]; p++) {
+        const double2 y = yval[p], u = ef[ycol[p]];
+        ir = fma(y.x, u.x, ir);
+        ir = fma(-y.y, u.y, ir);
+        ii = fma(y.x, u.y, ii);
+        ii = fma(y.y, u.x, ii);
+    }
+    const double ek = ef[k].x, fk = ef[k].y;
+    P = fma(ek, ir, fk * ii);
+    Q = fma(fk, ir, -ek * ii);
 }
 
 // FP32-LU form only: the phasor (cos, sin) of th + d from that of th.  For
@@ -226,15 +268,17 @@ __device__ __forceinline__ double block_max(double v, double *red) {
 // step takes a full sincos of the new angle.  Each rotation adds a few ulps, far below the
 // 1e-8 mismatch the Newton loop tests; the FP64 form keeps a full sincos.
 __device__ __forceinline__ void rotate_phasor(double th_new, double d, double &c, double &s) {
-    const double ad = fabs(d), d2 = d * d;
+    // size class from the bit pattern of |d| (integer compares)
+    const unsigned long long ad = abits(d);
+    const double d2 = d * d;
     double sd, cd;
-    if (ad <= 1e-4) {  // next terms d^5/5!, d^6/6!: below 1e-22
+    if (ad <= 0x3f1a36e2eb1c432dull) {  // |d| <= 1e-4; next terms d^5/5!, d^6/6!: below 1e-22
         sd = d * (1.0 + d2 * (-1.0 / 6.0));
         cd = 1.0 + d2 * (-0.5 + d2 * (1.0 / 24.0));
-    } else if (ad <= 1e-2) {  // next terms d^9/9!, d^10/10!: below 3e-24
+    } else if (ad <= 0x3f847ae147ae147bull) {  // |d| <= 1e-2; next terms d^9/9!, d^10/10!: below 3e-24
         sd = d * (1.0 + d2 * (-1.0 / 6.0 + d2 * (1.0 / 120.0 + d2 * (-1.0 / 5040.0))));
         cd = 1.0 + d2 * (-0.5 + d2 * (1.0 / 24.0 + d2 * (-1.0 / 720.0 + d2 * (1.0 / 40320.0))));
-    } else if (ad <= 0.1) {  // next terms d^11/11!, d^12/12!: below 3e-19
+    } else if (ad <= 0x3fb999999999999aull) {  // |d| <= 0.1; next terms d^11/11!, d^12/12!: below 3e-19
         sd = d * (1.0 + d2 * (-1.0 / 6.0 + d2 * (1.0 / 120.0 + d2 * (-1.0 / 5040.0 + d2 * (1.0 / 362880.0)))));
         cd = 1.0 + d2 * (-0.5 + d2 * (1.0 / 24.0 + d2 * (-1.0 / 720.0 + d2 * (1.0 / 40320.0 + d2 * (-1.0 / 3628800.0)))));
     } else {
@@ -296,14 +340,129 @@ __device__ __forceinline__ B4 diag_block32(float Pk, float Qk, float vk, float2 
     return blk;
 }
 
+// One elimination level, shared by both Newton kernels.  NT threads take
+// part (t = 0..NT-1); a group of 2^lg of them shares one pivot (entry, row),
+// strides over its gather list and sums the partial updates with shuffles
+// (lane 0 of the group starts from the stored value, the others from zero, so
+// lg = 0 is one thread per pivot with the list summed in order).
+//
+// Pivots of forward level l: diagonal block D_j (left-looking gather of
+// L(j,k) U(k,j)), its inverse through one reciprocal, and y_j of the forward
+// substitution.  Returns true when a pivot block is singular.
+template <typename TJ, int NT>
+__device__ __forceinline__ bool lu_pivots(const TopoView &G, int l, int lg, int t, typename Blk<TJ>::b4 *fac,
+                                          typename Blk<TJ>::b4 *dinv, typename Blk<TJ>::b2 *ys,
+                                          const typename Blk<TJ>::b4 *Lv, const typename Blk<TJ>::b4 *Uv) {
+    using B4 = typename Blk<TJ>::b4;
+    using B2 = typename Blk<TJ>::b2;
+    const int gs = 1 << lg, gl = t & (gs - 1), ng = NT >> lg;
+    const int beg = G.flev_ptr[l], cnt = G.flev_ptr[l + 1] - beg;
+    bool sing = false;
+    for (int b0 = 0; b0 < cnt; b0 += ng) {
+        const int w = b0 + (t >> lg);
+        const bool on = w < cnt;
+        const int j = on ? G.flev_steps[beg + w] : 0;
+        B4 D;
+        B2 yj;
+        D.x = D.y = D.z = D.w = (TJ)0;
+        yj.x = yj.y = (TJ)0;
+        if (on && gl == 0) {
+            D = fac[j];
+            yj = ys[j];
+        }
+        if (on)
+            for (int q = G.dg_ptr[j] + gl; q < G.dg_ptr[j + 1]; q += gs) {
+                const int p = G.dg_pos[q];
+                const B4 lj = Lv[p];
+                D = bsub(D, bm(lj, Uv[p]));
+                const B2 v = bmv(lj, ys[G.dg_k[q]]);
+                yj.x -= v.x;
+                yj.y -= v.y;
+            }
+        for (int o = gs >> 1; o > 0; o >>= 1) {
+            D = bsum_xor(D, o);
+            yj = b2sum_xor(yj, o);
+        }
+        if (on && gl == 0) {
+            const TJ det = D.x * D.w - D.y * D.z;
+            sing |= (det == (TJ)0 || !isfinite(det));
+            const TJ rd = (TJ)1 / det;
+            B4 inv;
+            inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
+            fac[j] = D;
+            dinv[j] = inv;
+            ys[j] = yj;
+        }
+    }
+    return sing;
+}
+
+// Off-diagonal entries of forward level l: U(j,i) and L(i,j) = (...) D_j^-1.
+template <typename TJ, int NT>
+__device__ __forceinline__ void lu_entries(const TopoView &G, int l, int lg, int t, const typename Blk<TJ>::b4 *dinv,
+                                           typename Blk<TJ>::b4 *Lv, typename Blk<TJ>::b4 *Uv) {
+    using B4 = typename Blk<TJ>::b4;
+    const int gs = 1 << lg, gl = t & (gs - 1), ng = NT >> lg;
+    const int beg = G.fent_ptr[l], cnt = G.fent_ptr[l + 1] - beg;
+    for (int b0 = 0; b0 < cnt; b0 += ng) {
+        const int e = b0 + (t >> lg);
+        const bool on = e < cnt;
+        const int p = on ? G.fent_p[beg + e] : 0, j = on ? G.fent_j[beg + e] : 0;
+        B4 aL, aU;
+        aL.x = aL.y = aL.z = aL.w = (TJ)0;
+        aU = aL;
+        if (on && gl == 0) { aL = Lv[p]; aU = Uv[p]; }
+        if (on)
+            for (int r = G.og_ptr[p] + gl; r < G.og_ptr[p + 1]; r += gs) {
+                const int x = G.og_a[r], y = G.og_b[r];
+                aL = bsub(aL, bm(Lv[y], Uv[x]));
+                aU = bsub(aU, bm(Lv[x], Uv[y]));
+            }
+        for (int o = gs >> 1; o > 0; o >>= 1) {
+            aL = bsum_xor(aL, o);
+            aU = bsum_xor(aU, o);
+        }
+        if (on && gl == 0) {
+            Uv[p] = aU;
+            Lv[p] = bm(aL, dinv[j]);
+        }
+    }
+}
+
+// Rows of backward level l: x_j = D_j^-1 (y_j - sum_i U(j,i) x_i), in place in ys.
+template <typename TJ, int NT>
+__device__ __forceinline__ void back_rows(const TopoView &G, int l, int lg, int t, const typename Blk<TJ>::b4 *dinv,
+                                          const typename Blk<TJ>::b4 *Uv, typename Blk<TJ>::b2 *ys) {
+    using B2 = typename Blk<TJ>::b2;
+    const int gs = 1 << lg, gl = t & (gs - 1), ng = NT >> lg;
+    const int beg = G.blev_ptr[l], cnt = G.blev_ptr[l + 1] - beg;
+    for (int b0 = 0; b0 < cnt; b0 += ng) {
+        const int w = b0 + (t >> lg);
+        const bool on = w < cnt;
+        const int j = on ? G.blev_steps[beg + w] : 0;
+        B2 acc;
+        acc.x = acc.y = (TJ)0;
+        if (on && gl == 0) acc = ys[j];
+        if (on)
+            for (int p = G.up_ptr[j] + gl; p < G.up_ptr[j + 1]; p += gs) {
+                const B2 v = bmv(Uv[p], ys[G.up_col[p]]);
+                acc.x -= v.x;
+                acc.y -= v.y;
+            }
+        for (int o = gs >> 1; o > 0; o >>= 1) acc = b2sum_xor(acc, o);
+        if (on && gl == 0) ys[j] = bmv(dinv[j], acc);
+    }
+}
+
 template <typename TJ>
-__global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
+__global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
     using B4 = typename Blk<TJ>::b4;
     using B2 = typename Blk<TJ>::b2;
     extern __shared__ __align__(32) unsigned char smem[];
-    __shared__ double red[kWarps];
+    __shared__ unsigned long long red[kWarps];
     __shared__ int s_inst, s_done, s_status, s_it, s_nev, s_topo;
     __shared__ double s_maxG, s_maxDx;
+    const unsigned long long tol_bits = abits(a.tol), tol10_bits = abits(a.tol * 10.);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     unsigned char *ism = smem + a.blob_region;  // per-instance region
     if (tid == 0) s_topo = -1;
@@ -396,21 +555,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
                 }
             fresh = false;
             __syncthreads();
-            for (int k = tid; k < nB; k += kThreads) {
-                double ir = 0, ii = 0;
-                for (int p = G.yptr[k]; p < G.yptr[k + 1]; p++) {
-                    const double2 y = G.yval[p], u = ef[G.ycol[p]];
-                    ir += y.x * u.x - y.y * u.y;
-                    ii += y.x * u.y + y.y * u.x;
-                }
-                const double ek = ef[k].x, fk = ef[k].y;
-                P[k] = ek * ir + fk * ii;
-                Q[k] = fk * ir - ek * ii;
-            }
+            for (int k = tid; k < nB; k += kThreads) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
             __syncthreads();
             const int it = s_it;
             // reactive limits (chkLimQ) when the previous step was small
-            if (a.lim && it >= 1 && it < a.max_iter && s_maxDx < a.tol * 10.) {
+            if (a.lim && it >= 1 && it < a.max_iter && abits(s_maxDx) < tol10_bits) {
                 for (int i = tid; i < T.nPV; i += kThreads) {
                     const int b = G.pv_bus[i];
                     const double ql = a.Qload[off + b], qg = Q[b] + ql;
@@ -441,7 +590,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
                 __syncthreads();
             }
             // mismatch (FP64) and convergence test
-            double m = 0;
+            unsigned long long m = 0;
             for (int j = tid; j < n; j += kThreads) {
                 const int k = G.bus_of_blk[j];
                 const double gp = a.Pliq[off + k] - P[k];
@@ -450,15 +599,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
                 r.x = (TJ)gp;
                 r.y = (TJ)gq;
                 ys[j] = r;
-                double t = fmax(fabs(gp), fabs(gq));
-                if (t != t) t = __longlong_as_double(0x7ff8000000000000ll);
-                m = (t > m || t != t) ? t : m;
+                m = umax64(m, umax64(abits(gp), abits(gq)));
             }
-            m = block_max(m, red);
+            m = block_umax(m, red);
             if (tid == 0) {
-                s_maxG = m;
-                if (m != m) { s_status = GBPF_E_NOCONV; s_done = 1; }
-                else if (m <= a.tol) s_done = 1;
+                s_maxG = __longlong_as_double((long long)m);
+                if (m > kInfBits) { s_status = GBPF_E_NOCONV; s_done = 1; }
+                else if (m <= tol_bits) s_done = 1;
                 else if (it >= a.max_iter) { s_status = GBPF_E_NOCONV; s_done = 1; }
             }
             __syncthreads();
@@ -510,113 +657,48 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
             }
             __syncthreads();
             // LU factorisation fused with forward substitution, one level at a
-            // time, in two passes: one thread per pivot j (diagonal block, its
-            // inverse through one reciprocal, y_j), then one thread per
-            // off-diagonal entry of the level (U(j,i) and L(i,j) = (...) D_j^-1).
-            // Deep levels have few pivots with long gather lists: a group of
-            // 2^g lanes shares one pivot (entry, row), strides over its list
-            // and sums the partial updates with shuffles (lane 0 of the group
-            // starts from the stored value, the others from zero, so g = 0 is
-            // the plain one-thread-per-pivot loop).
+            // time, in two passes: pivots (diagonal block, its inverse, y_j),
+            // then the level's off-diagonal entries.  A level narrow enough
+            // for one warp (lvl_narrow) runs on warp 0 alone with warp
+            // syncs, lanes grouped by lvl_group_w, and the block meets at a
+            // barrier only where a wide level follows; wide levels use the
+            // whole block, lanes grouped by lvl_group.
             for (int l = 0; l < T.nfl; l++) {
-                {
-                    const int lg = a.no_group ? 0 : G.lvl_group[3 * l], gs = 1 << lg, gl = tid & (gs - 1),
-                              ng = kThreads >> lg;
-                    const int beg = G.flev_ptr[l], cnt = G.flev_ptr[l + 1] - beg;
-                    for (int b0 = 0; b0 < cnt; b0 += ng) {
-                        const int w = b0 + (tid >> lg);
-                        const bool on = w < cnt;
-                        const int j = on ? G.flev_steps[beg + w] : 0;
-                        B4 D;
-                        B2 yj;
-                        D.x = D.y = D.z = D.w = (TJ)0;
-                        yj.x = yj.y = (TJ)0;
-                        if (on && gl == 0) {
-                            D = fac[j];
-                            yj = ys[j];
-                        }
-                        if (on)
-                            for (int t = G.dg_ptr[j] + gl; t < G.dg_ptr[j + 1]; t += gs) {
-                                const int p = G.dg_pos[t];
-                                const B4 lj = Lv[p];
-                                D = bsub(D, bm(lj, Uv[p]));
-                                const B2 v = bmv(lj, ys[G.dg_k[t]]);
-                                yj.x -= v.x;
-                                yj.y -= v.y;
-                            }
-                        for (int o = gs >> 1; o > 0; o >>= 1) {
-                            D = bsum_xor(D, o);
-                            yj = b2sum_xor(yj, o);
-                        }
-                        if (on && gl == 0) {
-                            const TJ det = D.x * D.w - D.y * D.z;
-                            if (det == (TJ)0 || !isfinite(det)) { s_status = GBPF_E_SINGULAR; s_done = 1; }
-                            const TJ rd = (TJ)1 / det;
-                            B4 inv;
-                            inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
-                            fac[j] = D;
-                            dinv[j] = inv;
-                            ys[j] = yj;
-                        }
+                if (a.narrow && (G.lvl_narrow[l] & 1)) {
+                    if (warp == 0) {
+                        const bool sing = lu_pivots<TJ, 32>(G, l, a.no_group ? 0 : G.lvl_group_w[3 * l], lane, fac,
+                                                             dinv, ys, Lv, Uv);
+                        if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                        __syncwarp();
+                        lu_entries<TJ, 32>(G, l, a.no_group ? 0 : G.lvl_group_w[3 * l + 1], lane, dinv, Lv, Uv);
+                        __syncwarp();
                     }
+                    if (l + 1 == T.nfl || !(G.lvl_narrow[l + 1] & 1)) __syncthreads();
+                } else {
+                    const bool sing = lu_pivots<TJ, kThreads>(G, l, a.no_group ? 0 : G.lvl_group[3 * l], tid, fac,
+                                                              dinv, ys, Lv, Uv);
+                    if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                    __syncthreads();
+                    lu_entries<TJ, kThreads>(G, l, a.no_group ? 0 : G.lvl_group[3 * l + 1], tid, dinv, Lv, Uv);
+                    __syncthreads();
                 }
-                __syncthreads();
-                {
-                    const int lg = a.no_group ? 0 : G.lvl_group[3 * l + 1], gs = 1 << lg, gl = tid & (gs - 1),
-                              ng = kThreads >> lg;
-                    const int beg = G.fent_ptr[l], cnt = G.fent_ptr[l + 1] - beg;
-                    for (int b0 = 0; b0 < cnt; b0 += ng) {
-                        const int e = b0 + (tid >> lg);
-                        const bool on = e < cnt;
-                        const int p = on ? G.fent_p[beg + e] : 0, j = on ? G.fent_j[beg + e] : 0;
-                        B4 aL, aU;
-                        aL.x = aL.y = aL.z = aL.w = (TJ)0;
-                        aU = aL;
-                        if (on && gl == 0) { aL = Lv[p]; aU = Uv[p]; }
-                        if (on)
-                            for (int r = G.og_ptr[p] + gl; r < G.og_ptr[p + 1]; r += gs) {
-                                const int x = G.og_a[r], y = G.og_b[r];
-                                aL = bsub(aL, bm(Lv[y], Uv[x]));
-                                aU = bsub(aU, bm(Lv[x], Uv[y]));
-                            }
-                        for (int o = gs >> 1; o > 0; o >>= 1) {
-                            aL = bsum_xor(aL, o);
-                            aU = bsum_xor(aU, o);
-                        }
-                        if (on && gl == 0) {
-                            Uv[p] = aU;
-                            Lv[p] = bm(aL, dinv[j]);
-                        }
-                    }
-                }
-                __syncthreads();
             }
             if (s_done) break;
-            // backward substitution, level by level, grouped like the factor
+            // backward substitution, level by level, narrow levels on warp 0
             for (int l = 0; l < T.nbl; l++) {
-                const int lg = a.no_group ? 0 : G.lvl_group[3 * l + 2], gs = 1 << lg, gl = tid & (gs - 1),
-                          ng = kThreads >> lg;
-                const int beg = G.blev_ptr[l], cnt = G.blev_ptr[l + 1] - beg;
-                for (int b0 = 0; b0 < cnt; b0 += ng) {
-                    const int w = b0 + (tid >> lg);
-                    const bool on = w < cnt;
-                    const int j = on ? G.blev_steps[beg + w] : 0;
-                    B2 acc;
-                    acc.x = acc.y = (TJ)0;
-                    if (on && gl == 0) acc = ys[j];
-                    if (on)
-                        for (int p = G.up_ptr[j] + gl; p < G.up_ptr[j + 1]; p += gs) {
-                            const B2 v = bmv(Uv[p], ys[G.up_col[p]]);
-                            acc.x -= v.x;
-                            acc.y -= v.y;
-                        }
-                    for (int o = gs >> 1; o > 0; o >>= 1) acc = b2sum_xor(acc, o);
-                    if (on && gl == 0) ys[j] = bmv(dinv[j], acc);
+                if (a.narrow && (G.lvl_narrow[l] & 2)) {
+                    if (warp == 0) {
+                        back_rows<TJ, 32>(G, l, a.no_group ? 0 : G.lvl_group_w[3 * l + 2], lane, dinv, Uv, ys);
+                        __syncwarp();
+                    }
+                    if (l + 1 == T.nbl || !(G.lvl_narrow[l + 1] & 2)) __syncthreads();
+                } else {
+                    back_rows<TJ, kThreads>(G, l, a.no_group ? 0 : G.lvl_group[3 * l + 2], tid, dinv, Uv, ys);
+                    __syncthreads();
                 }
-                __syncthreads();
             }
             // update (FP64 state) and max|dx|
-            double md = 0;
+            unsigned long long md = 0;
             for (int j = tid; j < n; j += kThreads) {
                 const int k = G.bus_of_blk[j];
                 const double dt = (double)ys[j].x, dv = (double)ys[j].y;
@@ -630,12 +712,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_nr_block(Args a) {
                     ef[k] = make_double2(V[k] * c, V[k] * s);
                     f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
                 }
-                double t = fmax(fabs(dt), fabs(dv));
-                if (t != t) t = __longlong_as_double(0x7ff8000000000000ll);
-                md = (t > md || t != t) ? t : md;
+                md = umax64(md, umax64(abits(dt), abits(dv)));
             }
-            md = block_max(md, red);
-            if (tid == 0) { s_maxDx = md; s_it = it + 1; }
+            md = block_umax(md, red);
+            if (tid == 0) { s_maxDx = __longlong_as_double((long long)md); s_it = it + 1; }
             __syncthreads();
         }
         // results
@@ -670,7 +750,7 @@ __device__ __forceinline__ double warp_max(double v) {
 // (state and factor); the topology's read-only blob is read from global
 // memory through the L1 cache.
 template <typename TJ>
-__global__ void __launch_bounds__(256) k_nr_warp(Args a) {
+__global__ void __launch_bounds__(256, 2) k_nr_warp(Args a) {
     using B4 = typename Blk<TJ>::b4;
     using B2 = typename Blk<TJ>::b2;
     constexpr unsigned FULL = 0xffffffffu;
@@ -678,6 +758,7 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
     const int lane = threadIdx.x & 31;
     unsigned char *ism = smem + (size_t)(threadIdx.x >> 5) * a.slice;
     const unsigned lt_mask = (1u << lane) - 1u;
+    const unsigned long long tol_bits = abits(a.tol), tol10_bits = abits(a.tol * 10.);
     for (;;) {
         int q = 0;
         if (lane == 0) q = atomicAdd(a.counter, 1);
@@ -739,19 +820,9 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
                     if (sizeof(TJ) == 4) f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
                 }
             __syncwarp();
-            for (int k = lane; k < nB; k += 32) {
-                double ir = 0, ii = 0;
-                for (int p = G.yptr[k]; p < G.yptr[k + 1]; p++) {
-                    const double2 y = G.yval[p], u = ef[G.ycol[p]];
-                    ir += y.x * u.x - y.y * u.y;
-                    ii += y.x * u.y + y.y * u.x;
-                }
-                const double ek = ef[k].x, fk = ef[k].y;
-                P[k] = ek * ir + fk * ii;
-                Q[k] = fk * ir - ek * ii;
-            }
+            for (int k = lane; k < nB; k += 32) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
             __syncwarp();
-            if (a.lim && it >= 1 && it < a.max_iter && maxDx < a.tol * 10.) {
+            if (a.lim && it >= 1 && it < a.max_iter && abits(maxDx) < tol10_bits) {
                 for (int i0 = 0; i0 < T.nPV; i0 += 32) {
                     const int i = i0 + lane;
                     int code = 0, b = 0;
@@ -785,7 +856,7 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
                 }
                 __syncwarp();
             }
-            double mloc = 0;
+            unsigned long long mloc = 0;
             for (int j = lane; j < n; j += 32) {
                 const int k = G.bus_of_blk[j];
                 const double gp = a.Pliq[off + k] - P[k];
@@ -794,13 +865,12 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
                 r.x = (TJ)gp;
                 r.y = (TJ)gq;
                 ys[j] = r;
-                double t = fmax(fabs(gp), fabs(gq));
-                if (t != t) t = __longlong_as_double(0x7ff8000000000000ll);
-                mloc = (t > mloc || t != t) ? t : mloc;
+                mloc = umax64(mloc, umax64(abits(gp), abits(gq)));
             }
-            maxG = warp_max(mloc);
-            if (maxG != maxG) { status = GBPF_E_NOCONV; break; }
-            if (maxG <= a.tol) break;
+            mloc = warp_umax(mloc);
+            maxG = __longlong_as_double((long long)mloc);
+            if (mloc > kInfBits) { status = GBPF_E_NOCONV; break; }
+            if (mloc <= tol_bits) break;
             if (it >= a.max_iter) { status = GBPF_E_NOCONV; break; }
             for (int qq = lane; qq < nq; qq += 32) {
                 const int sl = G.ysl[qq];
@@ -847,59 +917,21 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
                 fac[qq] = blk;
             }
             __syncwarp();
+            // LU fused with forward substitution, level by level, and the
+            // backward substitution, as in the block kernel with 32 lanes
             bool sing = false;
             for (int l = 0; l < T.nfl; l++) {
-                for (int w = G.flev_ptr[l] + lane; w < G.flev_ptr[l + 1]; w += 32) {
-                    const int j = G.flev_steps[w];
-                    B4 D = fac[j];
-                    B2 yj;
-                    yj = ys[j];
-                    for (int t = G.dg_ptr[j]; t < G.dg_ptr[j + 1]; t++) {
-                        const int p = G.dg_pos[t];
-                        const B4 lj = Lv[p];
-                        D = bsub(D, bm(lj, Uv[p]));
-                        const B2 v = bmv(lj, ys[G.dg_k[t]]);
-                        yj.x -= v.x;
-                        yj.y -= v.y;
-                    }
-                    const TJ det = D.x * D.w - D.y * D.z;
-                    sing |= (det == (TJ)0 || !isfinite(det));
-                    const TJ rd = (TJ)1 / det;
-                    B4 inv;
-                    inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
-                    fac[j] = D;
-                    dinv[j] = inv;
-                    ys[j] = yj;
-                }
+                sing |= lu_pivots<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l] : 0, lane, fac, dinv, ys, Lv, Uv);
                 __syncwarp();
-                for (int e = G.fent_ptr[l] + lane; e < G.fent_ptr[l + 1]; e += 32) {
-                    const int p = G.fent_p[e], j = G.fent_j[e];
-                    B4 aL = Lv[p], aU = Uv[p];
-                    for (int r = G.og_ptr[p]; r < G.og_ptr[p + 1]; r++) {
-                        const int x = G.og_a[r], y = G.og_b[r];
-                        aL = bsub(aL, bm(Lv[y], Uv[x]));
-                        aU = bsub(aU, bm(Lv[x], Uv[y]));
-                    }
-                    Uv[p] = aU;
-                    Lv[p] = bm(aL, dinv[j]);
-                }
+                lu_entries<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l + 1] : 0, lane, dinv, Lv, Uv);
                 __syncwarp();
             }
             if (__any_sync(FULL, sing)) { status = GBPF_E_SINGULAR; break; }
             for (int l = 0; l < T.nbl; l++) {
-                for (int w = G.blev_ptr[l] + lane; w < G.blev_ptr[l + 1]; w += 32) {
-                    const int j = G.blev_steps[w];
-                    B2 acc = ys[j];
-                    for (int p = G.up_ptr[j]; p < G.up_ptr[j + 1]; p++) {
-                        const B2 v = bmv(Uv[p], ys[G.up_col[p]]);
-                        acc.x -= v.x;
-                        acc.y -= v.y;
-                    }
-                    ys[j] = bmv(dinv[j], acc);
-                }
+                back_rows<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l + 2] : 0, lane, dinv, Uv, ys);
                 __syncwarp();
             }
-            double md = 0;
+            unsigned long long md = 0;
             for (int j = lane; j < n; j += 32) {
                 const int k = G.bus_of_blk[j];
                 const double dt = (double)ys[j].x, dv = (double)ys[j].y;
@@ -913,11 +945,9 @@ __global__ void __launch_bounds__(256) k_nr_warp(Args a) {
                     ef[k] = make_double2(V[k] * c, V[k] * s);
                     f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
                 }
-                double t = fmax(fabs(dt), fabs(dv));
-                if (t != t) t = __longlong_as_double(0x7ff8000000000000ll);
-                md = (t > md || t != t) ? t : md;
+                md = umax64(md, umax64(abits(dt), abits(dv)));
             }
-            maxDx = warp_max(md);
+            maxDx = __longlong_as_double((long long)warp_umax(md));
             it++;
             __syncwarp();
         }
@@ -1223,6 +1253,27 @@ struct gbpf_batch {
     gbpf_status set_instances(int n, const int *topo_of_inst, const double *Pload, const double *Qload,
                               const double *Pg, const double *Qg, const double *V0, const double *th0);
     std::vector<int> topo_warp;  // per topology: served by k_nr_warp (1) or k_nr_block (0)
+    // Launch plan (gbpf_batch_set_plan, gbpf_batch_autotune): warp_mode 0 puts
+    // every instance on k_nr_block; warp_warps 0 = as many warps per block as
+    // fit; handoff_it 0 = no hand-off; resume_group / warp_group switch the
+    // grouped lanes of deep levels in the hand-off blocks and in the warps;
+    // narrow = 1 runs the narrow levels of the block kernel on one warp.
+    struct Plan {
+        int warp_mode = 1, warp_warps = 0, handoff_it = kHandoffIt, resume_group = 1, warp_group = 1, narrow = 1;
+    } plan;
+    gbpf_status rebuild() {
+        CK(cudaStreamSynchronize(stream));
+        if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+        if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+        return build_graph();
+    }
+    gbpf_status autotune(int repeats, float *best_ms, float *first_ms);
+    // state and factor of one instance fit a warp's slice of shared memory
+    bool warp_fits(const Topo &T) const {
+        const bool fp32 = precision == GBPF_PREC_FP32_IR;
+        const Layout w = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1) : layout<double>(T.nB, T.n, T.nup, T.nPV, 1);
+        return w.total <= (fp32 ? 40u : 56u) * 1024;
+    }
     // learned warm start (solve_warm): features, prediction, chosen start, fallback queue
     DevBuf warm_mem;
     int warm_n = 0;
@@ -1276,10 +1327,11 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
     o.fent_j = put(S.fent_j.data(), nup * 4);
     // lanes per pivot / entry / row of each level for the block kernel: as many
     // as the level's thread budget allows, no more than its longest list needs
-    std::vector<int> grp(3 * (size_t)std::max(nfl, nbl), 0);
-    auto group_of = [](int count, int longest) {
+    // (grp), and the same for the 32 lanes of the warp kernel (grpw)
+    std::vector<int> grp(3 * (size_t)std::max(nfl, nbl), 0), grpw(grp.size(), 0);
+    auto group_of = [](int count, int longest, int threads) {
         int g = 0;
-        while (g < 5 && ((long long)count << (g + 1)) <= kThreads && (1 << g) < longest) g++;
+        while (g < 5 && ((long long)count << (g + 1)) <= threads && (1 << g) < longest) g++;
         return g;
     };
     for (int l = 0; l < nfl; l++) {
@@ -1292,8 +1344,12 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
             const int pp = S.fent_p[e];
             mo = std::max(mo, (int)(S.og_ptr[pp + 1] - S.og_ptr[pp]));
         }
-        grp[3 * l] = group_of(S.flev_ptr[l + 1] - S.flev_ptr[l], md);
-        grp[3 * l + 1] = group_of(S.fent_ptr[l + 1] - S.fent_ptr[l], mo);
+        for (int w = 0; w < 2; w++) {
+            std::vector<int> &gv = w ? grpw : grp;
+            const int th = w ? 32 : kThreads;
+            gv[3 * l] = group_of(S.flev_ptr[l + 1] - S.flev_ptr[l], md, th);
+            gv[3 * l + 1] = group_of(S.fent_ptr[l + 1] - S.fent_ptr[l], mo, th);
+        }
     }
     for (int l = 0; l < nbl; l++) {
         int mu = 0;
@@ -1301,9 +1357,17 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
             const int j = S.blev_steps[w];
             mu = std::max(mu, S.up_ptr[j + 1] - S.up_ptr[j]);
         }
-        grp[3 * l + 2] = group_of(S.blev_ptr[l + 1] - S.blev_ptr[l], mu);
+        grp[3 * l + 2] = group_of(S.blev_ptr[l + 1] - S.blev_ptr[l], mu, kThreads);
+        grpw[3 * l + 2] = group_of(S.blev_ptr[l + 1] - S.blev_ptr[l], mu, 32);
     }
     o.lvl_group = put(grp.data(), grp.size() * 4);
+    o.lvl_group_w = put(grpw.data(), grpw.size() * 4);
+    std::vector<int> narrow(std::max(nfl, nbl), 0);
+    for (int l = 0; l < nfl; l++)
+        if (S.flev_ptr[l + 1] - S.flev_ptr[l] <= 32 && S.fent_ptr[l + 1] - S.fent_ptr[l] <= 32) narrow[l] |= 1;
+    for (int l = 0; l < nbl; l++)
+        if (S.blev_ptr[l + 1] - S.blev_ptr[l] <= 32) narrow[l] |= 2;
+    o.lvl_narrow = put(narrow.data(), narrow.size() * 4);
     o.yval32 = put(nullptr, (size_t)y.nnz * 8);
     DevBuf mem, tmp;
     CK(cudaMalloc(&mem.p, blob.size()));
@@ -1451,7 +1515,8 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
             // the instances the warps parked, one block each, same arithmetic
             Args ra = wa;
             ra.resume = 1;
-            ra.no_group = 1;
+            ra.no_group = plan.resume_group ? 0 : 1;
+            ra.narrow = plan.narrow;
             ra.queue = wa.handoff_q;
             ra.counter = args.counter + 2;
             ra.topo = (const Topo *)topo_resume.p;
@@ -1476,13 +1541,15 @@ gbpf_status gbpf_batch::build_graph() {
     CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
     // Warp-per-instance for topologies whose state and factor fit a warp slice
     // of shared memory; block-per-instance (factor possibly in scratch) else.
-    const size_t warp_cap = fp32 ? 40 * 1024 : 56 * 1024;
     std::vector<int> warp_ok(topo_h.size(), 0);
     size_t slice = 0;
     for (size_t t = 0; t < topo_h.size(); t++) {
         const Topo &T = topo_h[t];
-        const Layout w = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1) : layout<double>(T.nB, T.n, T.nup, T.nPV, 1);
-        if (w.total <= warp_cap) { warp_ok[t] = 1; slice = std::max(slice, align_up(w.total, 128)); }
+        if (plan.warp_mode && warp_fits(T)) {
+            warp_ok[t] = 1;
+            const Layout w = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1) : layout<double>(T.nB, T.n, T.nup, T.nPV, 1);
+            slice = std::max(slice, align_up(w.total, 128));
+        }
     }
     topo_warp = warp_ok;
     std::vector<int> wq, bq;
@@ -1541,7 +1608,7 @@ gbpf_status gbpf_batch::build_graph() {
         resume_region = stage ? (int)region_r : 0;
         resume_smem = state + resume_region;
     }
-    const bool use_handoff = n_warp_q > 0 && max_iter > kHandoffIt;
+    const bool use_handoff = n_warp_q > 0 && plan.handoff_it > 0 && max_iter > plan.handoff_it;
     grid_blocks = 0;
     resume_grid = 0;
     {
@@ -1567,6 +1634,7 @@ gbpf_status gbpf_batch::build_graph() {
     warp_grid = 0;
     if (n_warp_q) {
         warp_warps = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024) / slice));
+        if (plan.warp_warps > 0) warp_warps = std::min(warp_warps, plan.warp_warps);
         warp_smem = (size_t)warp_warps * slice;
         int occ = 0;
         if (fp32) {
@@ -1600,6 +1668,8 @@ gbpf_status gbpf_batch::build_graph() {
     wargs.queue = (const int *)queues.p;
     wargs.queue_len = n_warp_q;
     wargs.slice = (int)slice;
+    wargs.warp_group = plan.warp_group;
+    args.narrow = plan.narrow;
     handoff.reset();
     topo_resume.reset();
     wargs.handoff_it = 0;
@@ -1607,7 +1677,7 @@ gbpf_status gbpf_batch::build_graph() {
         CK(cudaMalloc(&topo_resume.p, sizeof(Topo) * rt.size()));
         CK(cudaMemcpy(topo_resume.p, rt.data(), sizeof(Topo) * rt.size(), cudaMemcpyHostToDevice));
         CK(cudaMalloc(&handoff.p, 4 * (size_t)n_warp_q + 256));
-        wargs.handoff_it = kHandoffIt;
+        wargs.handoff_it = plan.handoff_it;
         wargs.handoff_q = (int *)handoff.p;
         wargs.handoff_n = (int *)counter.p + 3;
     }
@@ -1704,6 +1774,113 @@ gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, 
 // C ABI
 // ---------------------------------------------------------------------------
 #define ARGCHECK(c) do { if (!(c)) { set_error("invalid argument: " #c); return GBPF_E_ARG; } } while (0)
+
+// Coordinate search over the launch plan on the current instances: each knob
+// in turn takes each of its values with the others fixed, and a value is kept
+// when the whole batch (one graph launch, CUDA events on the batch stream,
+// best of `repeats` after one warm-up run) gets at least 2 % faster.  The
+// instances' outputs are overwritten by the trial solves; the winning plan
+// stays set.  Trial solves of one plan differ from another's only in the
+// FP32/FP64 summation order of grouped lanes.
+gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
+    auto timed = [&](const Plan &p, float *ms) -> gbpf_status {
+        plan = p;
+        gbpf_status st = rebuild();
+        if (st != GBPF_OK) return st;
+        CK(cudaGraphLaunch(exec, stream));
+        float best = INFINITY;
+        for (int r = 0; r < repeats; r++) {
+            CK(cudaEventRecord(ev0, stream));
+            CK(cudaGraphLaunch(exec, stream));
+            CK(cudaEventRecord(ev1, stream));
+            CK(cudaEventSynchronize(ev1));
+            float t = 0;
+            CK(cudaEventElapsedTime(&t, ev0, ev1));
+            best = std::min(best, t);
+        }
+        *ms = best;
+        return GBPF_OK;
+    };
+    Plan cur = plan;
+    float cur_ms = 0;
+    gbpf_status st = timed(cur, &cur_ms);
+    if (st != GBPF_OK) return st;
+    if (first_ms) *first_ms = cur_ms;
+    bool any_warp = false;
+    for (const Topo &T : topo_h) any_warp |= warp_fits(T);
+    struct Knob { int Plan::*field; std::vector<int> values; bool needs_warp, needs_handoff; };
+    const std::vector<Knob> knobs = {
+        {&Plan::warp_mode, {1, 0}, false, false},
+        {&Plan::warp_group, {1, 0}, true, false},
+        {&Plan::warp_warps, {0, 6, 4, 2}, true, false},
+        {&Plan::handoff_it, {kHandoffIt, 6, 8, 16, 24, 0}, true, false},
+        {&Plan::resume_group, {1, 0}, true, true},
+        {&Plan::narrow, {1, 0}, false, false},
+    };
+    for (const Knob &k : knobs) {
+        if (k.needs_warp && (!any_warp || !cur.warp_mode)) continue;
+        if (k.needs_handoff && cur.handoff_it == 0) continue;
+        if (k.field == &Plan::warp_mode && !any_warp) continue;
+        const int start = cur.*(k.field);
+        for (int v : k.values) {
+            if (v == start) continue;
+            Plan c = cur;
+            c.*(k.field) = v;
+            float ms = 0;
+            st = timed(c, &ms);
+            if (st != GBPF_OK) return st;
+            if (ms < 0.98f * cur_ms) { cur = c; cur_ms = ms; }
+        }
+    }
+    plan = cur;
+    st = rebuild();
+    if (best_ms) *best_ms = cur_ms;
+    return st;
+}
+
+static void plan_out(const gbpf_batch *b, int plan[10]) {
+    plan[0] = b->plan.warp_mode;
+    plan[1] = b->plan.warp_warps;
+    plan[2] = b->plan.handoff_it;
+    plan[3] = b->plan.resume_group;
+    plan[4] = b->plan.warp_group;
+    plan[5] = b->plan.narrow;
+    plan[6] = b->warp_warps;  // warps per block in use
+    plan[7] = b->n_warp_q;
+    plan[8] = b->n_block_q;
+    plan[9] = 0;
+}
+
+extern "C" gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[10]) {
+    ARGCHECK(b && plan);
+    plan_out(b, plan);
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[6]) {
+    ARGCHECK(b && plan && (plan[0] == 0 || plan[0] == 1) && plan[1] >= 0 && plan[1] <= 8 && plan[2] >= 0 &&
+             (plan[3] == 0 || plan[3] == 1) && (plan[4] == 0 || plan[4] == 1) && (plan[5] == 0 || plan[5] == 1));
+    CK(cudaSetDevice(b->device));
+    b->plan.warp_mode = plan[0];
+    b->plan.warp_warps = plan[1];
+    b->plan.handoff_it = plan[2];
+    b->plan.resume_group = plan[3];
+    b->plan.warp_group = plan[4];
+    b->plan.narrow = plan[5];
+    if (!b->n_inst) return GBPF_OK;
+    return b->rebuild();
+}
+
+extern "C" gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[10], float ms[2]) {
+    ARGCHECK(b && b->exec && repeats > 0);
+    CK(cudaSetDevice(b->device));
+    float best = 0, first = 0;
+    const gbpf_status st = b->autotune(repeats, &best, &first);
+    if (st != GBPF_OK) return st;
+    if (plan) plan_out(b, plan);
+    if (ms) { ms[0] = first; ms[1] = best; }
+    return GBPF_OK;
+}
 
 extern "C" gbpf_status gbpf_batch_kernel_times(gbpf_batch *b, int repeats, double ms[3]) {
     ARGCHECK(b && b->exec && repeats > 0 && ms);

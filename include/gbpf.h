@@ -327,6 +327,30 @@ gbpf_status gbpf_batch_time(gbpf_batch *b, int repeats, double *ms_total);
  * not use. */
 gbpf_status gbpf_batch_kernel_times(gbpf_batch *b, int repeats, double ms[3]);
 
+/* Launch plan of the batch graph (no counterpart in the reference, which
+ * solves one grid per process).  plan[0] warp mode: 1 = instances whose state
+ * and factor fit a warp's slice of shared memory run one per warp, 0 = every
+ * instance on a thread block of its own; plan[1] warps per block of the warp
+ * kernel, 0 = as many as fit (at most 8); plan[2] the iteration at which an
+ * instance still running leaves its warp for a thread block (0 = never);
+ * plan[3] / plan[4] grouped lanes on levels with few pivots in those blocks /
+ * in the warps (1 = on); plan[5] 1 = the thread-block kernel runs elimination
+ * levels of at most 32 pivots and entries on one warp, without block
+ * barriers between them.  get_plan also returns plan[6] warps per block in
+ * use, plan[7] instances on warps, plan[8] instances on blocks (plan[9] = 0).
+ * Setting a plan rebuilds the batch graph. */
+gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[10]);
+gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[6]);
+
+/* Autotuner: a coordinate search over plan[0..5] on the current instances.
+ * Each knob takes each of its values in turn with the others fixed; a value
+ * is kept when the whole batch solve (best of `repeats` timed graph launches
+ * after one warm-up, CUDA events on the batch stream) is at least 2 % faster.
+ * The best plan stays set; plan receives it (as gbpf_batch_get_plan) and
+ * ms[0] / ms[1] the batch time of the starting and of the chosen plan.  The
+ * trial solves overwrite the instances' results. */
+gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[10], float ms[2]);
+
 /* Per-instance results of the last batch solve (any pointer may be NULL);
  * V/theta/P/Q packed like the inputs. */
 gbpf_status gbpf_batch_results(gbpf_batch *b, int *iterations, int *status, double *final_mismatch,

@@ -178,3 +178,71 @@ def test_batch_handoff_of_long_instances(gb, oracle):
             assert r["iterations"][i] == 100
     assert long_ == 5
     assert other_path <= 2
+
+
+PLANS = [
+    dict(),                                             # default: warps, grouped lanes, hand-off at 12
+    dict(warp_group=0, resume_group=0),                 # one lane per pivot everywhere
+    dict(handoff_it=0),                                 # no hand-off: long instances stay on their warp
+    dict(handoff_it=6, warps_per_block=2),
+    dict(warp_mode=0),                                  # every instance on a thread block
+    dict(warp_mode=0, narrow=0),                        # ... every level on the whole block
+]
+
+
+@pytest.mark.parametrize("plan", PLANS, ids=lambda p: ",".join(f"{k}={v}" for k, v in p.items()) or "default")
+def test_batch_plans_match_oracle(gb, oracle, plan):
+    """Every launch plan the autotuner can choose gives the oracle's FP64
+    answers: iteration counts, statuses, switch events, |V| and theta within
+    1e-9 (plans differ only in the summation order of grouped lanes)."""
+    import bench
+
+    path = os.path.join(GOLDEN, "c2_base.cdf")
+    og = oracle.Grid(path)
+    base = dict(Pload=og.Pload.copy(), Qload=og.Qload.copy(), Pg=og.Pg.copy())
+    Pl, Ql, Pg = bench.scenarios(np, base, 4096, bench.BASE_SEED + 7)
+    pick = list(range(24)) + [1943, 2749, 3628, 4084]
+    Pl, Ql, Pg = Pl[pick], Ql[pick], Pg[pick]
+    n = len(pick)
+    b = gb.Batch([gb.read_grid(path)], tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1)
+    full = dict(warp_mode=1, warps_per_block=0, handoff_it=12, resume_group=1, warp_group=1, narrow=1)
+    full.update(plan)
+    b.set_plan(**full)
+    b.set_instances(np.zeros(n, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
+    b.solve()
+    r = b.results()
+    got = b.plan()
+    assert got["warp_mode"] == full["warp_mode"] and got["handoff_it"] == full["handoff_it"]
+    assert got["warp_instances"] == (n if full["warp_mode"] else 0)
+    for i in range(n):
+        ref = oracle_solve(og, Pl[i], Ql[i], Pg[i], 1)
+        assert r["iterations"][i] == ref["iterations"], i
+        assert (r["status"][i] == 0) == ref["converged"], i
+        assert b.events(i) == ref["events"][:16], i
+        if ref["converged"]:
+            assert np.max(np.abs(b.slice(r["V"], i) - ref["V"])) < 1e-9
+            assert np.max(np.abs(b.slice(r["theta"], i) - ref["theta"])) < 1e-9
+
+
+def test_batch_autotune(gb, oracle):
+    """The autotuner returns a valid plan no slower than the one it started
+    from, and the batch solved with it still matches the oracle."""
+    path = os.path.join(GOLDEN, "c2_s3.cdf")
+    og = oracle.Grid(path)
+    n = 512
+    Pl, Ql, Pg = scenarios(og, n, 11)
+    b, _ = run_batch(gb, [gb.read_grid(path)], np.zeros(n, np.int32), Pl.ravel(), Ql.ravel(), Pg.ravel(),
+                     precision=gb.PREC_FP32_IR)
+    plan, ms0, ms1 = b.autotune(repeats=2)
+    assert 0 < ms1 <= ms0 * 1.05
+    assert plan["warp_mode"] in (0, 1) and plan["handoff_it"] >= 0
+    assert b.plan() == plan
+    b.solve()
+    r = b.results()
+    for i in range(0, n, 37):
+        ref = oracle_solve(og, Pl[i], Ql[i], Pg[i], 1)
+        assert (r["status"][i] == 0) == ref["converged"], i
+        if ref["converged"]:
+            assert r["final_mismatch"][i] <= 1e-8
+            if [e[1:] for e in b.events(i)] == [e[1:] for e in ref["events"][:16]]:
+                assert np.max(np.abs(b.slice(r["V"], i) - ref["V"])) < 1e-6
