@@ -357,17 +357,18 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     value = total_conv * a.steps / t_dev
     # end to end: host buffers through the API every step
     nb = len(Pl)
+    res = None
     for _ in range(max(3, a.warmup)):
         fast.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
         fast.solve()
-        fast.results(state=True)
+        res = fast.results(state=True, out=res)
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(a.steps):
         fast.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
         fast.solve()
-        res = fast.results(state=True)
+        res = fast.results(state=True, out=res)
     t_e2e = max_over_ranks(time.perf_counter() - t0, dist, dev)
     e2e = total_conv * a.steps / t_e2e
     # the plain FP64 form (one scenario per gbpf_solve) and batched FP64, same scenarios
@@ -531,11 +532,12 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
     assert np.all(rw["final_mismatch"][rw["status"] == 0] <= 1e-8)
     it_w = rw["iterations"] + np.where(kind == 2, w["warm_iterations"], 0)
     # end to end through the public API with host buffers
+    res = fast.results(state=True)
     t0 = time.perf_counter()
     for _ in range(a.steps):
         fast.set_instances(gi, **inputs)
         fast.solve_warm(m)
-        fast.results(state=True)
+        res = fast.results(state=True, out=res)
     t_e2e = max_over_ranks(time.perf_counter() - t0, dist, dev)
     e2e = sum_over_ranks(conv, dist, dev) * a.steps / t_e2e
     # the plain FP64 form: one held-out scenario per gbpf_solve

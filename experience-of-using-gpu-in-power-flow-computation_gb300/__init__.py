@@ -470,9 +470,11 @@ class Batch:
 
     def set_instances(self, grid_of_inst, Pload=None, Qload=None, Pg=None, Qg=None, V0=None, theta0=None):
         gi = _i32(grid_of_inst)
-        sizes = np.array([self.grids[i].nB for i in gi], np.int64)
-        self.offsets = np.concatenate([[0], np.cumsum(sizes)])
-        self.grid_of_inst = gi
+        prev = getattr(self, "grid_of_inst", None)
+        if prev is None or prev.shape != gi.shape or not np.array_equal(prev, gi):
+            nbs = np.array([g.nB for g in self.grids], np.int64)
+            self.offsets = np.concatenate([[0], np.cumsum(nbs[gi])])
+            self.grid_of_inst = gi.copy()
         arrs = [_f64(a) for a in (Pload, Qload, Pg, Qg, V0, theta0)]
         for a in arrs:
             if a is not None and len(a) != self.offsets[-1]:
@@ -496,16 +498,24 @@ class Batch:
         _check(lib().gbpf_batch_kernel_times(self.h, int(repeats), _p(ms)), "gbpf_batch_kernel_times")
         return dict(block=float(ms[0]), warp=float(ms[1]), handoff=float(ms[2]))
 
-    def results(self, state=True):
+    def results(self, state=True, out=None):
+        """Per-instance results and (state=True) the packed V, theta, Pcalc,
+        Qcalc.  out: the dict of an earlier call of the same batch, whose
+        arrays are filled in place (no new allocation per solve)."""
         n, nb = self.n_inst, int(self.offsets[-1])
-        it = np.zeros(n, np.int32)
-        st = np.zeros(n, np.int32)
-        mm = np.zeros(n)
-        ne = np.zeros(n, np.int32)
-        V = np.zeros(nb) if state else None
-        th = np.zeros(nb) if state else None
-        P = np.zeros(nb) if state else None
-        Q = np.zeros(nb) if state else None
+
+        def arr(key, size, dt):
+            a = out.get(key) if out else None
+            return a if a is not None and a.shape == (size,) and a.dtype == dt else np.empty(size, dt)
+
+        it = arr("iterations", n, np.int32)
+        st = arr("status", n, np.int32)
+        mm = arr("final_mismatch", n, np.float64)
+        ne = arr("n_events", n, np.int32)
+        V = arr("V", nb, np.float64) if state else None
+        th = arr("theta", nb, np.float64) if state else None
+        P = arr("Pcalc", nb, np.float64) if state else None
+        Q = arr("Qcalc", nb, np.float64) if state else None
         _check(lib().gbpf_batch_results(self.h, _p(it), _p(st), _p(mm), _p(ne), _p(V), _p(th), _p(P), _p(Q)),
                "gbpf_batch_results")
         return dict(iterations=it, status=st, final_mismatch=mm, n_events=ne, V=V, theta=th, Pcalc=P, Qcalc=Q)

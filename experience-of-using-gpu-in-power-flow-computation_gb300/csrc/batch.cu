@@ -24,6 +24,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "blocks.cuh"
@@ -1198,6 +1199,30 @@ gbpf_status noalloc_setup(int device, void **out) {
 }
 }  // namespace
 
+// Runs f(begin, end) over [0, n) split across up to 16 host threads (the
+// calling thread takes the first range), each range at least `grain` long:
+// the packing of scenario inputs into the pinned staging buffer and the
+// copies of results out of it are memory-bound host loops over hundreds of MB.
+template <typename F> void host_parallel(size_t n, size_t grain, F f) {
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t t = std::min<size_t>(std::min<size_t>(hw, 16), std::max<size_t>(1, n / std::max<size_t>(grain, 1)));
+    if (t <= 1) { f((size_t)0, n); return; }
+    const size_t step = (n + t - 1) / t;
+    std::vector<std::thread> pool;
+    for (size_t i = 1; i < t; i++) {
+        const size_t b = i * step, e = std::min(n, b + step);
+        if (b < e) pool.emplace_back(f, b, e);
+    }
+    f((size_t)0, std::min(n, step));
+    for (auto &th : pool) th.join();
+}
+
+void par_memcpy(void *dst, const void *src, size_t bytes) {
+    host_parallel(bytes, (size_t)8 << 20, [&](size_t b, size_t e) {
+        std::memcpy((char *)dst + b, (const char *)src + b, e - b);
+    });
+}
+
 // ---------------------------------------------------------------------------
 // host object
 // ---------------------------------------------------------------------------
@@ -1468,19 +1493,21 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
     }
     double *hV = (double *)h_in, *hT = (double *)((char *)h_in + nba), *hP = (double *)((char *)h_in + 2 * nba),
            *hQ = (double *)((char *)h_in + 3 * nba), *hQl = (double *)((char *)h_in + 4 * nba);
-    for (int i = 0; i < n; i++) {
-        const Grid &g = grids[inst_topo[i]];
-        const long long o = inst_off[i];
-        for (int k = 0; k < g.nB; k++) {
-            const double pl = Pload ? Pload[o + k] : g.Pload[k], ql = Qload ? Qload[o + k] : g.Qload[k];
-            const double pg = Pg ? Pg[o + k] : g.Pg[k], qg = Qg ? Qg[o + k] : g.Qg[k];
-            hV[o + k] = V0 ? V0[o + k] : g.V0[k];
-            hT[o + k] = th0 ? th0[o + k] : g.theta0[k];
-            hP[o + k] = pg - pl;
-            hQ[o + k] = qg - ql;
-            hQl[o + k] = ql;
+    host_parallel((size_t)n, 1024, [&](size_t i0, size_t i1) {
+        for (size_t i = i0; i < i1; i++) {
+            const Grid &g = grids[inst_topo[i]];
+            const long long o = inst_off[i];
+            for (int k = 0; k < g.nB; k++) {
+                const double pl = Pload ? Pload[o + k] : g.Pload[k], ql = Qload ? Qload[o + k] : g.Qload[k];
+                const double pg = Pg ? Pg[o + k] : g.Pg[k], qg = Qg ? Qg[o + k] : g.Qg[k];
+                hV[o + k] = V0 ? V0[o + k] : g.V0[k];
+                hT[o + k] = th0 ? th0[o + k] : g.theta0[k];
+                hP[o + k] = pg - pl;
+                hQ[o + k] = qg - ql;
+                hQl[o + k] = ql;
+            }
         }
-    }
+    });
     // one host->device copy of the whole input region
     CK(cudaMemcpyAsync((void *)args.V0, h_in, 5 * nba, cudaMemcpyHostToDevice, stream));
     if (same) return GBPF_OK;
@@ -2082,10 +2109,10 @@ extern "C" gbpf_status gbpf_batch_results(gbpf_batch *b, int *iterations, int *s
     if (status) std::memcpy(status, host(b->args.status), 4 * n);
     if (final_mismatch) std::memcpy(final_mismatch, host(b->args.mism), 8 * n);
     if (n_events) std::memcpy(n_events, host(b->args.n_events), 4 * n);
-    if (V) std::memcpy(V, host(b->args.V), nb);
-    if (theta) std::memcpy(theta, host(b->args.th), nb);
-    if (Pcalc) std::memcpy(Pcalc, host(b->args.P), nb);
-    if (Qcalc) std::memcpy(Qcalc, host(b->args.Q), nb);
+    if (V) par_memcpy(V, host(b->args.V), nb);
+    if (theta) par_memcpy(theta, host(b->args.th), nb);
+    if (Pcalc) par_memcpy(Pcalc, host(b->args.P), nb);
+    if (Qcalc) par_memcpy(Qcalc, host(b->args.Q), nb);
     return GBPF_OK;
 }
 
