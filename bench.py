@@ -422,8 +422,10 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
                           f"inputs+outputs {nb * 8 * 9 / 2**20:.1f} MiB < L2; no flush"),
                    "batch": info, "plan": fast.plan(), "autotune": tune,
                    "parallelism": f"scenarios sharded x{world}"},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nb * 8 * 5 + N_SCEN * 12,
-                "d2h_bytes_per_step": nb * 8 * 4 + N_SCEN * 20},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nb * 8 * 3,
+                "d2h_bytes_per_step": nb * 8 * 4 + N_SCEN * 20,
+                "note": "per step: Pliq, Qliq, Qload up (the grid's own starting state stays on the device while "
+                        "the instance layout is unchanged); V, theta, Pcalc, Qcalc and per-instance results down"},
         "roofline": {"bound": "hbm", "kernel": main_kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src_note(src),
                      "traffic": traffic / 1e9 if traffic else None, "traffic_unit": "GB per launch",
@@ -583,7 +585,7 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
                    "speedup_vs_plain_fp64": value / plain_rate if plain_rate else None,
                    "l2": f"per-step inputs {nb_tot * 8 * 9 / 2**20:.0f} MiB > L2",
                    "parallelism": f"scenarios sharded x{world}"},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nb_tot * 8 * 5 + C5_TEST * 12,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nb_tot * 8 * 3,
                 "d2h_bytes_per_step": nb_tot * 8 * 4 + C5_TEST * 20},
         "roofline": {"bound": "hbm", "kernel": "k_nr_block<float> (one persistent launch per step)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

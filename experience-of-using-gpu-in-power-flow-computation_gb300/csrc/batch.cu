@@ -97,7 +97,7 @@ template <typename B4> __device__ __forceinline__ B4 bcast(B4 v, int src) {
 struct TopoOff {
     int yptr, ycol, yval, type, pv_bus, Qmin, Qmax, bus_of_blk, up_ptr, up_col, dg_ptr, dg_pos, dg_k,
         og_ptr, og_a, og_b, flev_ptr, flev_steps, blev_ptr, blev_steps, ysl, rbus, cbus, fent_ptr, fent_p,
-        fent_j, lvl_group, lvl_group_w, lvl_narrow, yval32;
+        fent_j, lvl_group, lvl_group_w, lvl_narrow, lvl_rot, og_k, yval32;
 };
 struct Topo {
     int nB, nL, n, nup, nnzY, nPV, nfl, nbl, fac_smem, blob_smem, blob_bytes;
@@ -120,6 +120,11 @@ struct TopoView {
     // per level: bit 0 forward level l, bit 1 backward level l has at most 32
     // pivots and 32 entries (rows): the block kernel runs it on one warp
     const int *lvl_narrow;
+    // one-pass levels: lanes by which the entries of level l are rotated away
+    // from its pivots (bits 0-15 the block kernel's 256 threads, bits 16-31
+    // the warp's 32 lanes), so that both run side by side
+    const int *lvl_rot;
+    const int *og_k;  // the step k of each gather pair
     const float2 *yval32;    // Ybus values rounded to FP32 (the FP32-LU form's Jacobian)
 };
 __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
@@ -139,6 +144,8 @@ __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     v.lvl_group = (const int *)(b + o.lvl_group);
     v.lvl_group_w = (const int *)(b + o.lvl_group_w);
     v.lvl_narrow = (const int *)(b + o.lvl_narrow);
+    v.lvl_rot = (const int *)(b + o.lvl_rot);
+    v.og_k = (const int *)(b + o.og_k);
     v.yval32 = (const float2 *)(b + o.yval32);
     return v;
 }
@@ -180,13 +187,15 @@ struct Args {
     // block kernel: levels with at most 32 pivots and entries (rows) run on
     // warp 0 alone (lvl_narrow); 0 runs every level on the whole block
     int narrow;
+    // both kernels: one pass per elimination level (lu_level1) instead of two
+    int lu1;
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
 
 // Shared-memory layout of one instance (state + optionally the factor).
 struct Layout {
-    size_t V, th, cs, sn, ef, f32, P, Q, QL, act, lim, ys, fac, dinv, total;
+    size_t V, th, cs, sn, ef, f32, P, Q, QL, act, lim, ys, zs, fac, dinv, total;
 };
 template <typename TJ>
 __host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fac_smem) {
@@ -204,6 +213,8 @@ __host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fa
     // ys: the mismatch, then (forward) the substituted right-hand side, then
     // (backward, in place) the Newton step
     L.ys = take(sizeof(B2) * n, 16);
+    // zs: D_j^-1 y_j of the forward substitution (one-pass levels)
+    L.zs = take(sizeof(B2) * n, 16);
     const size_t nq = (size_t)n + 2 * (size_t)nup;
     if (fac_smem) {
         L.fac = take(sizeof(B4) * nq, 32);
@@ -455,6 +466,97 @@ __device__ __forceinline__ void back_rows(const TopoView &G, int l, int lg, int 
     }
 }
 
+// One-pass level l: pivots and off-diagonal entries of the level together.
+// L is kept unscaled, Lt(i,k) = L(i,k) D_k, so no entry of a level waits for
+// the inverse of its own pivot; consumers apply D_k^-1 themselves:
+//   D_j    = A_jj   - sum_k Lt(j,k) D_k^-1 U(k,j)
+//   y_j    = b_j    - sum_k Lt(j,k) z_k,   z_k = D_k^-1 y_k
+//   Lt(i,j) = A_ij  - sum_k Lt(i,k) D_k^-1 U(k,j)
+//   U(j,i)  = A_ji  - sum_k Lt(j,k) D_k^-1 U(k,i)
+// (every k of a gather lies on an earlier level).  The backward
+// substitution is unchanged.  Entries run on lanes rotated by `rot` (a
+// multiple of their group size) so that they overlap the pivots' lanes as
+// little as possible.  Returns true when a pivot block is singular.
+template <typename TJ, int NT>
+__device__ __forceinline__ bool lu_level1(const TopoView &G, int l, int lgp, int lge, int rot, int t,
+                                          typename Blk<TJ>::b4 *fac, typename Blk<TJ>::b4 *dinv,
+                                          typename Blk<TJ>::b2 *ys, typename Blk<TJ>::b2 *zs,
+                                          typename Blk<TJ>::b4 *Lv, typename Blk<TJ>::b4 *Uv) {
+    using B4 = typename Blk<TJ>::b4;
+    using B2 = typename Blk<TJ>::b2;
+    bool sing = false;
+    {
+        const int gs = 1 << lgp, gl = t & (gs - 1), ng = NT >> lgp;
+        const int beg = G.flev_ptr[l], cnt = G.flev_ptr[l + 1] - beg;
+        for (int b0 = 0; b0 < cnt; b0 += ng) {
+            const int w = b0 + (t >> lgp);
+            const bool on = w < cnt;
+            const int j = on ? G.flev_steps[beg + w] : 0;
+            B4 D;
+            B2 yj;
+            D.x = D.y = D.z = D.w = (TJ)0;
+            yj.x = yj.y = (TJ)0;
+            if (on && gl == 0) {
+                D = fac[j];
+                yj = ys[j];
+            }
+            if (on)
+                for (int q = G.dg_ptr[j] + gl; q < G.dg_ptr[j + 1]; q += gs) {
+                    const int p = G.dg_pos[q], k = G.dg_k[q];
+                    const B4 lt = Lv[p];
+                    D = bsub(D, bm(lt, bm(dinv[k], Uv[p])));
+                    const B2 v = bmv(lt, zs[k]);
+                    yj.x -= v.x;
+                    yj.y -= v.y;
+                }
+            for (int o = gs >> 1; o > 0; o >>= 1) {
+                D = bsum_xor(D, o);
+                yj = b2sum_xor(yj, o);
+            }
+            if (on && gl == 0) {
+                const TJ det = D.x * D.w - D.y * D.z;
+                sing |= (det == (TJ)0 || !isfinite(det));
+                const TJ rd = (TJ)1 / det;
+                B4 inv;
+                inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
+                dinv[j] = inv;
+                ys[j] = yj;
+                zs[j] = bmv(inv, yj);
+            }
+        }
+    }
+    {
+        const int te = (t + rot) & (NT - 1);
+        const int gs = 1 << lge, gl = te & (gs - 1), ng = NT >> lge;
+        const int beg = G.fent_ptr[l], cnt = G.fent_ptr[l + 1] - beg;
+        for (int b0 = 0; b0 < cnt; b0 += ng) {
+            const int e = b0 + (te >> lge);
+            const bool on = e < cnt;
+            const int p = on ? G.fent_p[beg + e] : 0;
+            B4 aL, aU;
+            aL.x = aL.y = aL.z = aL.w = (TJ)0;
+            aU = aL;
+            if (on && gl == 0) { aL = Lv[p]; aU = Uv[p]; }
+            if (on)
+                for (int r = G.og_ptr[p] + gl; r < G.og_ptr[p + 1]; r += gs) {
+                    const int x = G.og_a[r], y = G.og_b[r];
+                    const B4 dk = dinv[G.og_k[r]];
+                    aL = bsub(aL, bm(Lv[y], bm(dk, Uv[x])));
+                    aU = bsub(aU, bm(Lv[x], bm(dk, Uv[y])));
+                }
+            for (int o = gs >> 1; o > 0; o >>= 1) {
+                aL = bsum_xor(aL, o);
+                aU = bsum_xor(aU, o);
+            }
+            if (on && gl == 0) {
+                Uv[p] = aU;
+                Lv[p] = aL;
+            }
+        }
+    }
+    return sing;
+}
+
 template <typename TJ>
 __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
     using B4 = typename Blk<TJ>::b4;
@@ -664,23 +766,40 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
             // syncs, lanes grouped by lvl_group_w, and the block meets at a
             // barrier only where a wide level follows; wide levels use the
             // whole block, lanes grouped by lvl_group.
+            // With lu1 each level is one pass (lu_level1: pivots and entries
+            // side by side, L unscaled) and needs one barrier instead of two.
+            B2 *zs = (B2 *)(ism + L.zs);
             for (int l = 0; l < T.nfl; l++) {
                 if (a.narrow && (G.lvl_narrow[l] & 1)) {
                     if (warp == 0) {
-                        const bool sing = lu_pivots<TJ, 32>(G, l, a.no_group ? 0 : G.lvl_group_w[3 * l], lane, fac,
-                                                             dinv, ys, Lv, Uv);
+                        const int gp = a.no_group ? 0 : G.lvl_group_w[3 * l];
+                        const int ge = a.no_group ? 0 : G.lvl_group_w[3 * l + 1];
+                        bool sing;
+                        if (a.lu1) {
+                            sing = lu_level1<TJ, 32>(G, l, gp, ge, a.no_group ? 0 : G.lvl_rot[l] >> 16, lane, fac,
+                                                     dinv, ys, zs, Lv, Uv);
+                        } else {
+                            sing = lu_pivots<TJ, 32>(G, l, gp, lane, fac, dinv, ys, Lv, Uv);
+                            __syncwarp();
+                            lu_entries<TJ, 32>(G, l, ge, lane, dinv, Lv, Uv);
+                        }
                         if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
-                        __syncwarp();
-                        lu_entries<TJ, 32>(G, l, a.no_group ? 0 : G.lvl_group_w[3 * l + 1], lane, dinv, Lv, Uv);
                         __syncwarp();
                     }
                     if (l + 1 == T.nfl || !(G.lvl_narrow[l + 1] & 1)) __syncthreads();
                 } else {
-                    const bool sing = lu_pivots<TJ, kThreads>(G, l, a.no_group ? 0 : G.lvl_group[3 * l], tid, fac,
-                                                              dinv, ys, Lv, Uv);
-                    if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
-                    __syncthreads();
-                    lu_entries<TJ, kThreads>(G, l, a.no_group ? 0 : G.lvl_group[3 * l + 1], tid, dinv, Lv, Uv);
+                    const int gp = a.no_group ? 0 : G.lvl_group[3 * l];
+                    const int ge = a.no_group ? 0 : G.lvl_group[3 * l + 1];
+                    if (a.lu1) {
+                        const bool sing = lu_level1<TJ, kThreads>(G, l, gp, ge, a.no_group ? 0 : G.lvl_rot[l] & 0xffff,
+                                                                  tid, fac, dinv, ys, zs, Lv, Uv);
+                        if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                    } else {
+                        const bool sing = lu_pivots<TJ, kThreads>(G, l, gp, tid, fac, dinv, ys, Lv, Uv);
+                        if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                        __syncthreads();
+                        lu_entries<TJ, kThreads>(G, l, ge, tid, dinv, Lv, Uv);
+                    }
                     __syncthreads();
                 }
             }
@@ -921,10 +1040,17 @@ __global__ void __launch_bounds__(256, 2) k_nr_warp(Args a) {
             // LU fused with forward substitution, level by level, and the
             // backward substitution, as in the block kernel with 32 lanes
             bool sing = false;
+            B2 *zs = (B2 *)(ism + L.zs);
             for (int l = 0; l < T.nfl; l++) {
-                sing |= lu_pivots<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l] : 0, lane, fac, dinv, ys, Lv, Uv);
-                __syncwarp();
-                lu_entries<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l + 1] : 0, lane, dinv, Lv, Uv);
+                const int gp = a.warp_group ? G.lvl_group_w[3 * l] : 0, ge = a.warp_group ? G.lvl_group_w[3 * l + 1] : 0;
+                if (a.lu1) {
+                    sing |= lu_level1<TJ, 32>(G, l, gp, ge, a.warp_group ? G.lvl_rot[l] >> 16 : 0, lane, fac, dinv, ys,
+                                              zs, Lv, Uv);
+                } else {
+                    sing |= lu_pivots<TJ, 32>(G, l, gp, lane, fac, dinv, ys, Lv, Uv);
+                    __syncwarp();
+                    lu_entries<TJ, 32>(G, l, ge, lane, dinv, Lv, Uv);
+                }
                 __syncwarp();
             }
             if (__any_sync(FULL, sing)) { status = GBPF_E_SINGULAR; break; }
@@ -1256,6 +1382,7 @@ struct gbpf_batch {
     cudaEvent_t kev[6] = {};
     DevBuf topo_na;          // topologies planned for gbpf_batch_solve_noalloc
     void *h_in = nullptr, *h_out = nullptr;  // pinned mirrors of the input and output regions
+    bool start_is_default = false;           // the device V0 / theta0 hold the grids' own start
     size_t out_bytes = 0;
     size_t na_smem = 0, na_stride = 0;
     cudaGraphExec_t exec = nullptr;
@@ -1282,9 +1409,12 @@ struct gbpf_batch {
     // every instance on k_nr_block; warp_warps 0 = as many warps per block as
     // fit; handoff_it 0 = no hand-off; resume_group / warp_group switch the
     // grouped lanes of deep levels in the hand-off blocks and in the warps;
-    // narrow = 1 runs the narrow levels of the block kernel on one warp.
+    // narrow = 1 runs the narrow levels of the block kernel on one warp; lu1 /
+    // warp_lu1 = 1 factor in one pass per elimination level in the block
+    // kernel (block mode and hand-off) / in the warp kernel.
     struct Plan {
-        int warp_mode = 1, warp_warps = 0, handoff_it = kHandoffIt, resume_group = 1, warp_group = 1, narrow = 1;
+        int warp_mode = 1, warp_warps = 0, handoff_it = kHandoffIt, resume_group = 1, warp_group = 1, narrow = 0,
+            lu1 = 1, warp_lu1 = 0;
     } plan;
     gbpf_status rebuild() {
         CK(cudaStreamSynchronize(stream));
@@ -1393,6 +1523,17 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
     for (int l = 0; l < nbl; l++)
         if (S.blev_ptr[l + 1] - S.blev_ptr[l] <= 32) narrow[l] |= 2;
     o.lvl_narrow = put(narrow.data(), narrow.size() * 4);
+    // one-pass levels: the entries start past the lanes the pivots occupy
+    std::vector<int> rot(std::max(nfl, 1), 0);
+    for (int l = 0; l < nfl; l++) {
+        const int np = S.flev_ptr[l + 1] - S.flev_ptr[l];
+        const long long pb = (long long)np << grp[3 * l], pw = (long long)np << grpw[3 * l];
+        const int rb = pb < kThreads ? (int)align_up((size_t)pb, 32) : 0;
+        const int rw = (pw <= 16 && grpw[3 * l + 1] <= 4) ? 16 : 0;
+        rot[l] = (rb % kThreads) | (rw << 16);
+    }
+    o.lvl_rot = put(rot.data(), rot.size() * 4);
+    o.og_k = put(S.og_k.data(), S.og_k.size() * 4);
     o.yval32 = put(nullptr, (size_t)y.nnz * 8);
     DevBuf mem, tmp;
     CK(cudaMalloc(&mem.p, blob.size()));
@@ -1493,6 +1634,9 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
     }
     double *hV = (double *)h_in, *hT = (double *)((char *)h_in + nba), *hP = (double *)((char *)h_in + 2 * nba),
            *hQ = (double *)((char *)h_in + 3 * nba), *hQl = (double *)((char *)h_in + 4 * nba);
+    // the grids' own starting state (no V0 / theta0 given) is copied once and
+    // stays on the device while the instance layout is unchanged
+    const bool dflt = !V0 && !th0, keep_start = same && dflt && start_is_default;
     host_parallel((size_t)n, 1024, [&](size_t i0, size_t i1) {
         for (size_t i = i0; i < i1; i++) {
             const Grid &g = grids[inst_topo[i]];
@@ -1500,16 +1644,23 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
             for (int k = 0; k < g.nB; k++) {
                 const double pl = Pload ? Pload[o + k] : g.Pload[k], ql = Qload ? Qload[o + k] : g.Qload[k];
                 const double pg = Pg ? Pg[o + k] : g.Pg[k], qg = Qg ? Qg[o + k] : g.Qg[k];
-                hV[o + k] = V0 ? V0[o + k] : g.V0[k];
-                hT[o + k] = th0 ? th0[o + k] : g.theta0[k];
+                if (!keep_start) {
+                    hV[o + k] = V0 ? V0[o + k] : g.V0[k];
+                    hT[o + k] = th0 ? th0[o + k] : g.theta0[k];
+                }
                 hP[o + k] = pg - pl;
                 hQ[o + k] = qg - ql;
                 hQl[o + k] = ql;
             }
         }
     });
-    // one host->device copy of the whole input region
-    CK(cudaMemcpyAsync((void *)args.V0, h_in, 5 * nba, cudaMemcpyHostToDevice, stream));
+    // one host->device copy of the input region (without the starting state
+    // when it is already there)
+    if (keep_start)
+        CK(cudaMemcpyAsync((void *)args.Pliq, hP, 3 * nba, cudaMemcpyHostToDevice, stream));
+    else
+        CK(cudaMemcpyAsync((void *)args.V0, h_in, 5 * nba, cudaMemcpyHostToDevice, stream));
+    start_is_default = dflt;
     if (same) return GBPF_OK;
     CK(cudaStreamSynchronize(stream));
     if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
@@ -1544,6 +1695,7 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
             ra.resume = 1;
             ra.no_group = plan.resume_group ? 0 : 1;
             ra.narrow = plan.narrow;
+            ra.lu1 = plan.lu1;
             ra.queue = wa.handoff_q;
             ra.counter = args.counter + 2;
             ra.topo = (const Topo *)topo_resume.p;
@@ -1697,6 +1849,8 @@ gbpf_status gbpf_batch::build_graph() {
     wargs.slice = (int)slice;
     wargs.warp_group = plan.warp_group;
     args.narrow = plan.narrow;
+    args.lu1 = plan.lu1;
+    wargs.lu1 = plan.warp_lu1;
     handoff.reset();
     topo_resume.reset();
     wargs.handoff_it = 0;
@@ -1828,7 +1982,9 @@ gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
         *ms = best;
         return GBPF_OK;
     };
-    Plan cur = plan;
+    // from the default plan (knobs interact: grouping and one-pass levels of
+    // the block kernel only matter with a hand-off), two sweeps at most
+    Plan cur{};
     float cur_ms = 0;
     gbpf_status st = timed(cur, &cur_ms);
     if (st != GBPF_OK) return st;
@@ -1843,21 +1999,27 @@ gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
         {&Plan::handoff_it, {kHandoffIt, 6, 8, 16, 24, 0}, true, false},
         {&Plan::resume_group, {1, 0}, true, true},
         {&Plan::narrow, {1, 0}, false, false},
+        {&Plan::lu1, {1, 0}, false, false},
+        {&Plan::warp_lu1, {0, 1}, true, false},
     };
-    for (const Knob &k : knobs) {
-        if (k.needs_warp && (!any_warp || !cur.warp_mode)) continue;
-        if (k.needs_handoff && cur.handoff_it == 0) continue;
-        if (k.field == &Plan::warp_mode && !any_warp) continue;
-        const int start = cur.*(k.field);
-        for (int v : k.values) {
-            if (v == start) continue;
-            Plan c = cur;
-            c.*(k.field) = v;
-            float ms = 0;
-            st = timed(c, &ms);
-            if (st != GBPF_OK) return st;
-            if (ms < 0.98f * cur_ms) { cur = c; cur_ms = ms; }
+    for (int sweep = 0; sweep < 2; sweep++) {
+        bool changed = false;
+        for (const Knob &k : knobs) {
+            if (k.needs_warp && (!any_warp || !cur.warp_mode)) continue;
+            if (k.needs_handoff && cur.handoff_it == 0) continue;
+            if (k.field == &Plan::warp_mode && !any_warp) continue;
+            const int start = cur.*(k.field);
+            for (int v : k.values) {
+                if (v == start) continue;
+                Plan c = cur;
+                c.*(k.field) = v;
+                float ms = 0;
+                st = timed(c, &ms);
+                if (st != GBPF_OK) return st;
+                if (ms < 0.98f * cur_ms) { cur = c; cur_ms = ms; changed = true; }
+            }
         }
+        if (!changed) break;
     }
     plan = cur;
     st = rebuild();
@@ -1865,28 +2027,31 @@ gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
     return st;
 }
 
-static void plan_out(const gbpf_batch *b, int plan[10]) {
+static void plan_out(const gbpf_batch *b, int plan[12]) {
     plan[0] = b->plan.warp_mode;
     plan[1] = b->plan.warp_warps;
     plan[2] = b->plan.handoff_it;
     plan[3] = b->plan.resume_group;
     plan[4] = b->plan.warp_group;
     plan[5] = b->plan.narrow;
-    plan[6] = b->warp_warps;  // warps per block in use
-    plan[7] = b->n_warp_q;
-    plan[8] = b->n_block_q;
-    plan[9] = 0;
+    plan[6] = b->plan.lu1;
+    plan[7] = b->plan.warp_lu1;
+    plan[8] = b->warp_warps;  // warps per block in use
+    plan[9] = b->n_warp_q;
+    plan[10] = b->n_block_q;
+    plan[11] = 0;
 }
 
-extern "C" gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[10]) {
+extern "C" gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[12]) {
     ARGCHECK(b && plan);
     plan_out(b, plan);
     return GBPF_OK;
 }
 
-extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[6]) {
+extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[8]) {
     ARGCHECK(b && plan && (plan[0] == 0 || plan[0] == 1) && plan[1] >= 0 && plan[1] <= 8 && plan[2] >= 0 &&
-             (plan[3] == 0 || plan[3] == 1) && (plan[4] == 0 || plan[4] == 1) && (plan[5] == 0 || plan[5] == 1));
+             (plan[3] == 0 || plan[3] == 1) && (plan[4] == 0 || plan[4] == 1) && (plan[5] == 0 || plan[5] == 1) &&
+             (plan[6] == 0 || plan[6] == 1) && (plan[7] == 0 || plan[7] == 1));
     CK(cudaSetDevice(b->device));
     b->plan.warp_mode = plan[0];
     b->plan.warp_warps = plan[1];
@@ -1894,11 +2059,13 @@ extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[6]) {
     b->plan.resume_group = plan[3];
     b->plan.warp_group = plan[4];
     b->plan.narrow = plan[5];
+    b->plan.lu1 = plan[6];
+    b->plan.warp_lu1 = plan[7];
     if (!b->n_inst) return GBPF_OK;
     return b->rebuild();
 }
 
-extern "C" gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[10], float ms[2]) {
+extern "C" gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[12], float ms[2]) {
     ARGCHECK(b && b->exec && repeats > 0);
     CK(cudaSetDevice(b->device));
     float best = 0, first = 0;

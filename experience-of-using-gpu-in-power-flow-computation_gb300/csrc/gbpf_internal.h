@@ -60,6 +60,7 @@ struct Symbolic {
     std::vector<int> dg_ptr, dg_pos, dg_k;
     std::vector<long long> og_ptr;
     std::vector<int> og_a, og_b;
+    std::vector<int> og_k;  // the step k of each pair (both positions lie in idx(k))
     // Level schedules: forward (factor + L solve) and backward (U solve).
     std::vector<int> flev_ptr, flev_steps, blev_ptr, blev_steps;
     // Off-diagonal entries of each forward level, flat: entries

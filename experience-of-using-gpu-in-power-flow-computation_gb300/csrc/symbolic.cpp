@@ -192,6 +192,7 @@ Symbolic analyse(const Grid &g, const YPattern &y, std::string *why) {
     const long long npairs = S.og_ptr[S.nup];
     S.og_a.resize(npairs);
     S.og_b.resize(npairs);
+    S.og_k.resize(npairs);
     {
         std::vector<long long> f(S.og_ptr.begin(), S.og_ptr.end() - 1);
         for (int k = 0; k < n; k++)
@@ -200,6 +201,7 @@ Symbolic analyse(const Grid &g, const YPattern &y, std::string *why) {
                     const int p = pos_in(S.up_col[a], S.up_col[b]);
                     S.og_a[f[p]] = a;
                     S.og_b[f[p]] = b;
+                    S.og_k[f[p]] = k;
                     f[p]++;
                 }
     }

@@ -336,20 +336,25 @@ gbpf_status gbpf_batch_kernel_times(gbpf_batch *b, int repeats, double ms[3]);
  * plan[3] / plan[4] grouped lanes on levels with few pivots in those blocks /
  * in the warps (1 = on); plan[5] 1 = the thread-block kernel runs elimination
  * levels of at most 32 pivots and entries on one warp, without block
- * barriers between them.  get_plan also returns plan[6] warps per block in
- * use, plan[7] instances on warps, plan[8] instances on blocks (plan[9] = 0).
- * Setting a plan rebuilds the batch graph. */
-gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[10]);
-gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[6]);
+ * barriers between them; plan[6] / plan[7] 1 = the LU of the thread-block
+ * kernel / of the warp kernel takes one pass per elimination level (L kept
+ * unscaled, pivots and entries of a level side by side), 0 = two passes
+ * (pivots, then entries scaled by the pivot inverse).  get_plan also returns
+ * plan[8] warps per block in use, plan[9] instances on warps, plan[10]
+ * instances on blocks (plan[11] = 0).  Setting a plan rebuilds the batch
+ * graph. */
+gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[12]);
+gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[8]);
 
-/* Autotuner: a coordinate search over plan[0..5] on the current instances.
- * Each knob takes each of its values in turn with the others fixed; a value
- * is kept when the whole batch solve (best of `repeats` timed graph launches
- * after one warm-up, CUDA events on the batch stream) is at least 2 % faster.
+/* Autotuner: a coordinate search over plan[0..7] on the current instances,
+ * from the default plan.  Each knob takes each of its values in turn with the
+ * others fixed; a value is kept when the whole batch solve (best of `repeats`
+ * timed graph launches after one warm-up, CUDA events on the batch stream) is
+ * at least 2 % faster; a second sweep runs when the first changed the plan.
  * The best plan stays set; plan receives it (as gbpf_batch_get_plan) and
- * ms[0] / ms[1] the batch time of the starting and of the chosen plan.  The
+ * ms[0] / ms[1] the batch time of the default and of the chosen plan.  The
  * trial solves overwrite the instances' results. */
-gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[10], float ms[2]);
+gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[12], float ms[2]);
 
 /* Per-instance results of the last batch solve (any pointer may be NULL);
  * V/theta/P/Q packed like the inputs. */

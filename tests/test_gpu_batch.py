@@ -186,7 +186,10 @@ PLANS = [
     dict(handoff_it=0),                                 # no hand-off: long instances stay on their warp
     dict(handoff_it=6, warps_per_block=2),
     dict(warp_mode=0),                                  # every instance on a thread block
-    dict(warp_mode=0, narrow=0),                        # ... every level on the whole block
+    dict(warp_mode=0, narrow=1),                        # ... narrow levels on one warp
+    dict(lu1=0, narrow=1),                              # two passes per level (pivots, then entries)
+    dict(warp_mode=0, lu1=0),
+    dict(warp_lu1=1, handoff_it=8),                     # one-pass levels in the warps too
 ]
 
 
@@ -205,7 +208,8 @@ def test_batch_plans_match_oracle(gb, oracle, plan):
     Pl, Ql, Pg = Pl[pick], Ql[pick], Pg[pick]
     n = len(pick)
     b = gb.Batch([gb.read_grid(path)], tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1)
-    full = dict(warp_mode=1, warps_per_block=0, handoff_it=12, resume_group=1, warp_group=1, narrow=1)
+    full = dict(warp_mode=1, warps_per_block=0, handoff_it=12, resume_group=1, warp_group=1, narrow=0, lu1=1,
+                warp_lu1=0)
     full.update(plan)
     b.set_plan(**full)
     b.set_instances(np.zeros(n, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
@@ -246,3 +250,30 @@ def test_batch_autotune(gb, oracle):
             assert r["final_mismatch"][i] <= 1e-8
             if [e[1:] for e in b.events(i)] == [e[1:] for e in ref["events"][:16]]:
                 assert np.max(np.abs(b.slice(r["V"], i) - ref["V"])) < 1e-6
+
+
+def test_batch_starting_state_kept_or_replaced(gb):
+    """The grids' own start stays on the device between calls with the same
+    instances and no V0 / theta0; a given start replaces it and the next call
+    without one restores it."""
+    path = os.path.join(GOLDEN, "c2_s3.cdf")
+    g = gb.read_grid(path)
+    n = 64
+    gi = np.zeros(n, np.int32)
+    b = gb.Batch([g], tolerancia=1e-8, no_max_iter=50, lim_inj_reat=1)
+    b.set_instances(gi)
+    b.solve()
+    ref = b.results()
+    base = g.buses()
+    V0 = np.tile(base["V0"], n) * 0.97
+    b.set_instances(gi, V0=V0)
+    b.solve()
+    other = b.results()
+    assert not np.array_equal(other["iterations"], ref["iterations"]) or \
+        not np.array_equal(other["V"], ref["V"])
+    for _ in range(2):
+        b.set_instances(gi)
+        b.solve()
+        r = b.results()
+        np.testing.assert_array_equal(r["iterations"], ref["iterations"])
+        np.testing.assert_array_equal(r["V"], ref["V"])
