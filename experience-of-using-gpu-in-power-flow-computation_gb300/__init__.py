@@ -537,7 +537,7 @@ class Batch:
         _check(lib().gbpf_batch_get_plan(self.h, _p(a)), "gbpf_batch_get_plan")
         return dict(zip(self.PLAN_KEYS, (int(x) for x in a)))
 
-    def set_plan(self, warp_mode=1, warps_per_block=0, handoff_it=12, resume_group=1, warp_group=1, narrow=0,
+    def set_plan(self, warp_mode=1, warps_per_block=8, handoff_it=12, resume_group=1, warp_group=1, narrow=0,
                  lu1=1, warp_lu1=0):
         a = np.array([warp_mode, warps_per_block, handoff_it, resume_group, warp_group, narrow, lu1, warp_lu1],
                      np.int32)

@@ -45,6 +45,8 @@ constexpr int kWarps = kThreads / 32;
 // instance does, and a warp runs one Newton iteration several times slower
 // than a block.
 constexpr int kHandoffIt = 12;
+// Warps (instances) per block of the warp-per-instance kernel, at most
+constexpr int kWarpsMax = 16;
 
 template <typename T> struct Blk;
 template <> struct Blk<double> { using b4 = double4_32a; using b2 = double2; };
@@ -195,10 +197,12 @@ __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a -
 
 // Shared-memory layout of one instance (state + optionally the factor).
 struct Layout {
-    size_t V, th, cs, sn, ef, f32, P, Q, QL, act, lim, ys, zs, fac, dinv, total;
+    size_t V, th, cs, sn, ef, f32, P, Q, QL, act, lim, ys, zs, fac, total;
 };
+// with_zs: room for z = D^-1 y of the one-pass levels (lu_level1).  The
+// inverse of diagonal block j overwrites fac[j] once the block is factored.
 template <typename TJ>
-__host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fac_smem) {
+__host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fac_smem, int with_zs) {
     using B4 = typename Blk<TJ>::b4;
     using B2 = typename Blk<TJ>::b2;
     Layout L;
@@ -213,22 +217,16 @@ __host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fa
     // ys: the mismatch, then (forward) the substituted right-hand side, then
     // (backward, in place) the Newton step
     L.ys = take(sizeof(B2) * n, 16);
-    // zs: D_j^-1 y_j of the forward substitution (one-pass levels)
-    L.zs = take(sizeof(B2) * n, 16);
+    L.zs = with_zs ? take(sizeof(B2) * n, 16) : 0;
     const size_t nq = (size_t)n + 2 * (size_t)nup;
-    if (fac_smem) {
-        L.fac = take(sizeof(B4) * nq, 32);
-        L.dinv = take(sizeof(B4) * n, 32);
-    } else {
-        L.fac = L.dinv = 0;
-    }
+    L.fac = fac_smem ? take(sizeof(B4) * nq, 32) : 0;
     L.total = align_up(o, 32);
     return L;
 }
 // Factor slice in global scratch (used when it does not fit in shared memory).
 template <typename TJ> __host__ __device__ inline size_t scratch_bytes(int n, int nup) {
     using B4 = typename Blk<TJ>::b4;
-    return align_up(sizeof(B4) * ((size_t)n + 2 * (size_t)nup), 32) + align_up(sizeof(B4) * n, 32);
+    return align_up(sizeof(B4) * ((size_t)n + 2 * (size_t)nup), 32);
 }
 
 // Maxima of |x| over FP64 values taken on their bit patterns: with the sign
@@ -401,8 +399,7 @@ __device__ __forceinline__ bool lu_pivots(const TopoView &G, int l, int lg, int 
             const TJ rd = (TJ)1 / det;
             B4 inv;
             inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
-            fac[j] = D;
-            dinv[j] = inv;
+            dinv[j] = inv;  // the slot of D_j when dinv aliases the factor's diagonal
             ys[j] = yj;
         }
     }
@@ -594,7 +591,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
         }
         const TopoView G = bind(T.o, blob);
         const long long off = a.inst_off[inst];
-        const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, T.fac_smem);
+        const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, T.fac_smem, a.lu1);
         double *V = (double *)(ism + L.V), *th = (double *)(ism + L.th);
         double *cs = (double *)(ism + L.cs), *sn = (double *)(ism + L.sn);
         double2 *ef = (double2 *)(ism + L.ef);
@@ -603,15 +600,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
         unsigned char *act = ism + L.act;
         int *limQ = (int *)(ism + L.lim);
         B2 *ys = (B2 *)(ism + L.ys);
-        B4 *fac, *dinv;
-        if (T.fac_smem) {
-            fac = (B4 *)(ism + L.fac);
-            dinv = (B4 *)(ism + L.dinv);
-        } else {
-            char *base = a.scratch + (long long)blockIdx.x * a.scratch_stride;
-            fac = (B4 *)base;
-            dinv = (B4 *)(base + align_up(sizeof(B4) * ((size_t)T.n + 2 * (size_t)T.nup), 32));
-        }
+        // the inverse of each diagonal block overwrites it (dinv = fac)
+        B4 *fac = T.fac_smem ? (B4 *)(ism + L.fac) : (B4 *)(a.scratch + (long long)blockIdx.x * a.scratch_stride);
+        B4 *dinv = fac;
         const int n = T.n, nB = T.nB, nq = T.n + 2 * T.nup;
         B4 *Lv = fac + n, *Uv = fac + n + T.nup;
         if (!a.resume) {
@@ -870,7 +861,7 @@ __device__ __forceinline__ double warp_max(double v) {
 // (state and factor); the topology's read-only blob is read from global
 // memory through the L1 cache.
 template <typename TJ>
-__global__ void __launch_bounds__(256, 2) k_nr_warp(Args a) {
+__global__ void __launch_bounds__(32 * kWarpsMax, 1) k_nr_warp(Args a) {
     using B4 = typename Blk<TJ>::b4;
     using B2 = typename Blk<TJ>::b2;
     constexpr unsigned FULL = 0xffffffffu;
@@ -889,7 +880,7 @@ __global__ void __launch_bounds__(256, 2) k_nr_warp(Args a) {
         const Topo T = a.topo[t_id];
         const TopoView G = bind(T.o, T.blob);
         const long long off = a.inst_off[inst];
-        const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, 1);
+        const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, 1, a.lu1);
         double *V = (double *)(ism + L.V), *th = (double *)(ism + L.th);
         double *cs = (double *)(ism + L.cs), *sn = (double *)(ism + L.sn);
         double2 *ef = (double2 *)(ism + L.ef);
@@ -898,7 +889,7 @@ __global__ void __launch_bounds__(256, 2) k_nr_warp(Args a) {
         unsigned char *act = ism + L.act;
         int *limQ = (int *)(ism + L.lim);
         B2 *ys = (B2 *)(ism + L.ys);
-        B4 *fac = (B4 *)(ism + L.fac), *dinv = (B4 *)(ism + L.dinv);
+        B4 *fac = (B4 *)(ism + L.fac), *dinv = fac;  // block inverses overwrite the diagonal
         const int n = T.n, nB = T.nB, nq = T.n + 2 * T.nup;
         B4 *Lv = fac + n, *Uv = fac + n + T.nup;
         for (int k = lane; k < nB; k += 32) {
@@ -1407,13 +1398,14 @@ struct gbpf_batch {
     std::vector<int> topo_warp;  // per topology: served by k_nr_warp (1) or k_nr_block (0)
     // Launch plan (gbpf_batch_set_plan, gbpf_batch_autotune): warp_mode 0 puts
     // every instance on k_nr_block; warp_warps 0 = as many warps per block as
-    // fit; handoff_it 0 = no hand-off; resume_group / warp_group switch the
+    // fit (8 by default: more warps per SM measured no faster on the 118-bus
+    // batch); handoff_it 0 = no hand-off; resume_group / warp_group switch the
     // grouped lanes of deep levels in the hand-off blocks and in the warps;
     // narrow = 1 runs the narrow levels of the block kernel on one warp; lu1 /
     // warp_lu1 = 1 factor in one pass per elimination level in the block
     // kernel (block mode and hand-off) / in the warp kernel.
     struct Plan {
-        int warp_mode = 1, warp_warps = 0, handoff_it = kHandoffIt, resume_group = 1, warp_group = 1, narrow = 0,
+        int warp_mode = 1, warp_warps = 8, handoff_it = kHandoffIt, resume_group = 1, warp_group = 1, narrow = 0,
             lu1 = 1, warp_lu1 = 0;
     } plan;
     gbpf_status rebuild() {
@@ -1426,7 +1418,8 @@ struct gbpf_batch {
     // state and factor of one instance fit a warp's slice of shared memory
     bool warp_fits(const Topo &T) const {
         const bool fp32 = precision == GBPF_PREC_FP32_IR;
-        const Layout w = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1) : layout<double>(T.nB, T.n, T.nup, T.nPV, 1);
+        const Layout w = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1, plan.warp_lu1)
+                              : layout<double>(T.nB, T.n, T.nup, T.nPV, 1, plan.warp_lu1);
         return w.total <= (fp32 ? 40u : 56u) * 1024;
     }
     // learned warm start (solve_warm): features, prediction, chosen start, fallback queue
@@ -1726,7 +1719,8 @@ gbpf_status gbpf_batch::build_graph() {
         const Topo &T = topo_h[t];
         if (plan.warp_mode && warp_fits(T)) {
             warp_ok[t] = 1;
-            const Layout w = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1) : layout<double>(T.nB, T.n, T.nup, T.nPV, 1);
+            const Layout w = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1, plan.warp_lu1)
+                                  : layout<double>(T.nB, T.n, T.nup, T.nPV, 1, plan.warp_lu1);
             slice = std::max(slice, align_up(w.total, 128));
         }
     }
@@ -1752,8 +1746,10 @@ gbpf_status gbpf_batch::build_graph() {
     for (size_t t = 0; t < topo_h.size(); t++) {
         Topo &T = topo_h[t];
         if (warp_ok[t]) { T.fac_smem = 1; continue; }
-        Layout with = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1) : layout<double>(T.nB, T.n, T.nup, T.nPV, 1);
-        Layout without = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 0) : layout<double>(T.nB, T.n, T.nup, T.nPV, 0);
+        const int z = plan.lu1;
+        Layout with = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1, z) : layout<double>(T.nB, T.n, T.nup, T.nPV, 1, z);
+        Layout without =
+            fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 0, z) : layout<double>(T.nB, T.n, T.nup, T.nPV, 0, z);
         if (region + with.total <= budget) { T.fac_smem = 1; need = std::max(need, with.total); }
         else {
             T.fac_smem = 0;
@@ -1775,8 +1771,8 @@ gbpf_status gbpf_batch::build_graph() {
         for (size_t t = 0; t < topo_h.size(); t++) {
             if (!warp_ok[t]) continue;
             const Topo &T = topo_h[t];
-            state = std::max(state, fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1).total
-                                         : layout<double>(T.nB, T.n, T.nup, T.nPV, 1).total);
+            state = std::max(state, fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1, plan.lu1).total
+                                         : layout<double>(T.nB, T.n, T.nup, T.nPV, 1, plan.lu1).total);
             region_r = std::max(region_r, align_up((size_t)T.blob_bytes, 32));
         }
         const bool stage = state + region_r <= (size_t)maxsm;
@@ -1809,10 +1805,11 @@ gbpf_status gbpf_batch::build_graph() {
         else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double>, kThreads, resume_smem));
         resume_grid = std::max(1, std::min(n_warp_q, dev_sm * std::max(occ, 1)));
     }
-    // warp-mode plan: as many warps per block as fit in 200 KB, at most 8
+    // warp-mode plan: as many warps per block as fit in the block's shared
+    // memory, at most 16 (one block per SM; 128 registers a thread)
     warp_grid = 0;
     if (n_warp_q) {
-        warp_warps = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024) / slice));
+        warp_warps = (int)std::max<size_t>(1, std::min<size_t>(kWarpsMax, (size_t)maxsm / slice));
         if (plan.warp_warps > 0) warp_warps = std::min(warp_warps, plan.warp_warps);
         warp_smem = (size_t)warp_warps * slice;
         int occ = 0;
@@ -1995,7 +1992,7 @@ gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
     const std::vector<Knob> knobs = {
         {&Plan::warp_mode, {1, 0}, false, false},
         {&Plan::warp_group, {1, 0}, true, false},
-        {&Plan::warp_warps, {0, 6, 4, 2}, true, false},
+        {&Plan::warp_warps, {8, 0, 6, 4}, true, false},
         {&Plan::handoff_it, {kHandoffIt, 6, 8, 16, 24, 0}, true, false},
         {&Plan::resume_group, {1, 0}, true, true},
         {&Plan::narrow, {1, 0}, false, false},
@@ -2049,7 +2046,7 @@ extern "C" gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[12]) {
 }
 
 extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[8]) {
-    ARGCHECK(b && plan && (plan[0] == 0 || plan[0] == 1) && plan[1] >= 0 && plan[1] <= 8 && plan[2] >= 0 &&
+    ARGCHECK(b && plan && (plan[0] == 0 || plan[0] == 1) && plan[1] >= 0 && plan[1] <= kWarpsMax && plan[2] >= 0 &&
              (plan[3] == 0 || plan[3] == 1) && (plan[4] == 0 || plan[4] == 1) && (plan[5] == 0 || plan[5] == 1) &&
              (plan[6] == 0 || plan[6] == 1) && (plan[7] == 0 || plan[7] == 1));
     CK(cudaSetDevice(b->device));
@@ -2126,7 +2123,7 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
         for (auto &t : na) {
             t.blob_smem = 0;
             t.fac_smem = 0;
-            const Layout l = fp32 ? layout<float>(t.nB, t.n, t.nup, t.nPV, 0) : layout<double>(t.nB, t.n, t.nup, t.nPV, 0);
+            const Layout l = fp32 ? layout<float>(t.nB, t.n, t.nup, t.nPV, 0, 0) : layout<double>(t.nB, t.n, t.nup, t.nPV, 0, 0);
             b->na_smem = std::max(b->na_smem, l.total);
             b->na_stride = std::max(b->na_stride, align_up(fp32 ? scratch_bytes<float>(t.n, t.nup)
                                                                 : scratch_bytes<double>(t.n, t.nup), 256));

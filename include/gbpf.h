@@ -331,7 +331,7 @@ gbpf_status gbpf_batch_kernel_times(gbpf_batch *b, int repeats, double ms[3]);
  * solves one grid per process).  plan[0] warp mode: 1 = instances whose state
  * and factor fit a warp's slice of shared memory run one per warp, 0 = every
  * instance on a thread block of its own; plan[1] warps per block of the warp
- * kernel, 0 = as many as fit (at most 8); plan[2] the iteration at which an
+ * kernel (default 8), 0 = as many as fit (at most 16); plan[2] the iteration at which an
  * instance still running leaves its warp for a thread block (0 = never);
  * plan[3] / plan[4] grouped lanes on levels with few pivots in those blocks /
  * in the warps (1 = on); plan[5] 1 = the thread-block kernel runs elimination

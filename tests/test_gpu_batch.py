@@ -208,7 +208,7 @@ def test_batch_plans_match_oracle(gb, oracle, plan):
     Pl, Ql, Pg = Pl[pick], Ql[pick], Pg[pick]
     n = len(pick)
     b = gb.Batch([gb.read_grid(path)], tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1)
-    full = dict(warp_mode=1, warps_per_block=0, handoff_it=12, resume_group=1, warp_group=1, narrow=0, lu1=1,
+    full = dict(warp_mode=1, warps_per_block=8, handoff_it=12, resume_group=1, warp_group=1, narrow=0, lu1=1,
                 warp_lu1=0)
     full.update(plan)
     b.set_plan(**full)
