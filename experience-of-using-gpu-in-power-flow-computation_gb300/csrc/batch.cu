@@ -52,10 +52,16 @@ template <typename T> struct Blk;
 template <> struct Blk<double> { using b4 = double4_32a; using b2 = double2; };
 template <> struct Blk<float> { using b4 = float4; using b2 = float2; };
 
+// Explicit fused multiply-adds, so that every use of the 2x2 block products
+// below rounds the same way whatever the surrounding code lets the compiler
+// contract.
+__device__ __forceinline__ float fmx(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmx(double a, double b, double c) { return __fma_rn(a, b, c); }
+
 template <typename B4> __device__ __forceinline__ B4 bm(B4 a, B4 b) {
     B4 r;
-    r.x = a.x * b.x + a.y * b.z; r.y = a.x * b.y + a.y * b.w;
-    r.z = a.z * b.x + a.w * b.z; r.w = a.z * b.y + a.w * b.w;
+    r.x = fmx(a.x, b.x, a.y * b.z); r.y = fmx(a.x, b.y, a.y * b.w);
+    r.z = fmx(a.z, b.x, a.w * b.z); r.w = fmx(a.z, b.y, a.w * b.w);
     return r;
 }
 template <typename B4> __device__ __forceinline__ B4 bsub(B4 a, B4 b) {
@@ -68,8 +74,8 @@ template <typename B4> __device__ __forceinline__ B4 badd(B4 a, B4 b) {
 }
 template <typename B4, typename B2> __device__ __forceinline__ B2 bmv(B4 a, B2 v) {
     B2 r;
-    r.x = a.x * v.x + a.y * v.y;
-    r.y = a.z * v.x + a.w * v.y;
+    r.x = fmx(a.x, v.x, a.y * v.y);
+    r.y = fmx(a.z, v.x, a.w * v.y);
     return r;
 }
 // v plus the v of lane (lane ^ o): one butterfly step of a sum over lanes
@@ -104,6 +110,7 @@ struct TopoOff {
 struct Topo {
     int nB, nL, n, nup, nnzY, nPV, nfl, nbl, fac_smem, blob_smem, blob_bytes;
     const char *blob;  // global copy
+    const char *flat;  // the shared flat-start iteration (k_flat_start), or null
     TopoOff o;
 };
 // Pointers of a topology's arrays, bound to the staged (shared) or global blob.
@@ -191,6 +198,9 @@ struct Args {
     int narrow;
     // both kernels: one pass per elimination level (lu_level1) instead of two
     int lu1;
+    // warp kernel: nonzero *flat_on = every instance starts from its grid's own
+    // starting state, so iteration 0 takes Topo::flat (null: never)
+    const int *flat_on;
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
@@ -227,6 +237,31 @@ __host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fa
 template <typename TJ> __host__ __device__ inline size_t scratch_bytes(int n, int nup) {
     using B4 = typename Blk<TJ>::b4;
     return align_up(sizeof(B4) * ((size_t)n + 2 * (size_t)nup), 32);
+}
+
+// Iteration 0 from the grid's own starting state is the same for every
+// instance of a topology: the phasors, the injections P, Q, the Jacobian and
+// its factor depend on the topology and the start only; the instances differ
+// in the right-hand side (their loads and generation).  k_flat_start computes
+// that iteration once per topology into this layout and the warp kernel's
+// instances start from it (the forward and backward substitutions with their
+// own mismatch remain).
+struct FlatLayout {
+    size_t V0, th0, cs, sn, ef, f32, P, Q, fac, sing, total;
+};
+template <typename TJ> __host__ __device__ inline FlatLayout flat_layout(int nB, int nq) {
+    using B4 = typename Blk<TJ>::b4;
+    FlatLayout F;
+    size_t o = 0;
+    auto take = [&](size_t bytes, size_t al) { o = align_up(o, al); size_t r = o; o += bytes; return r; };
+    F.V0 = take(8 * (size_t)nB, 16); F.th0 = take(8 * (size_t)nB, 16);
+    F.cs = take(8 * (size_t)nB, 16); F.sn = take(8 * (size_t)nB, 16);
+    F.ef = take(16 * (size_t)nB, 16); F.f32 = take(16 * (size_t)nB, 16);
+    F.P = take(8 * (size_t)nB, 16); F.Q = take(8 * (size_t)nB, 16);
+    F.fac = take(sizeof(B4) * (size_t)nq, 32);
+    F.sing = take(4, 16);
+    F.total = align_up(o, 256);
+    return F;
 }
 
 // Maxima of |x| over FP64 values taken on their bit patterns: with the sign
@@ -350,6 +385,69 @@ __device__ __forceinline__ B4 diag_block32(float Pk, float Qk, float vk, float2 
     return blk;
 }
 
+// Phasor of bus k from th[k], V[k]: cos, sin, e = V (cos, sin) and, for the
+// FP32-LU form, the FP32 copies (cos, sin, V) its Jacobian reads.
+template <typename TJ>
+__device__ __forceinline__ void phasor(int k, const double *th, const double *V, double *cs, double *sn, double2 *ef,
+                                       float4 *f32) {
+    double s, c;
+    sincos(th[k], &s, &c);
+    cs[k] = c;
+    sn[k] = s;
+    ef[k] = make_double2(V[k] * c, V[k] * s);
+    if (sizeof(TJ) == 4) f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
+}
+
+// Jacobian block at factor position q (GPU/Jacobiano.cuh:252-344 formulas):
+// diagonal blocks q < n, L / U positions after; zero at fill-in positions.
+template <typename TJ>
+__device__ __forceinline__ typename Blk<TJ>::b4 jac_block(const TopoView &G, int q, int n, const unsigned char *act,
+                                                          const double *P, const double *Q, const double *V,
+                                                          const double *cs, const double *sn, const float4 *f32) {
+    using B4 = typename Blk<TJ>::b4;
+    B4 blk;
+    blk.x = blk.y = blk.z = blk.w = 0;
+    const int sl = G.ysl[q];
+    if (sl < 0) return blk;
+    const int k = G.rbus[q], mb = G.cbus[q];
+    const int ak = act[k];
+    if constexpr (sizeof(TJ) == 4) {
+        // FP32-LU form: FP32 copies of the phasors, V and Ybus
+        const float4 fk = f32[k];
+        const float2 y = G.yval32[sl];
+        if (q < n) {
+            blk = diag_block32<B4>((float)P[k], (float)Q[k], fk.z, y, ak);
+        } else {
+            const int am = act[mb];
+            const float4 fm = f32[mb];
+            const float tr = y.x * fm.x - y.y * fm.y, ti = y.x * fm.y + y.y * fm.x;
+            const float wr = fk.x * tr + fk.y * ti, wi = fk.y * tr - fk.x * ti;
+            blk.x = fk.z * fm.z * wi;
+            if (am) blk.y = fk.z * wr;
+            if (ak) blk.z = -fk.z * fm.z * wr;
+            if (ak && am) blk.w = fk.z * wi;
+        }
+    } else {
+        const double2 y = G.yval[sl];
+        const double Vk = V[k];
+        if (q < n) {
+            blk = diag_block<TJ, B4>(P[k], Q[k], Vk, y, ak);
+        } else {
+            // off-diagonal entries in the precision of the factor
+            const int am = act[mb];
+            const TJ ck = (TJ)cs[k], sk = (TJ)sn[k], cm = (TJ)cs[mb], sm = (TJ)sn[mb];
+            const TJ yr = (TJ)y.x, yi = (TJ)y.y, vk = (TJ)Vk, vm = (TJ)V[mb];
+            const TJ tr = yr * cm - yi * sm, ti = yr * sm + yi * cm;
+            const TJ wr = ck * tr + sk * ti, wi = sk * tr - ck * ti;
+            blk.x = vk * vm * wi;
+            if (am) blk.y = vk * wr;
+            if (ak) blk.z = -vk * vm * wr;
+            if (ak && am) blk.w = vk * wi;
+        }
+    }
+    return blk;
+}
+
 // One elimination level, shared by both Newton kernels.  NT threads take
 // part (t = 0..NT-1); a group of 2^lg of them shares one pivot (entry, row),
 // strides over its gather list and sums the partial updates with shuffles
@@ -460,6 +558,34 @@ __device__ __forceinline__ void back_rows(const TopoView &G, int l, int lg, int 
             }
         for (int o = gs >> 1; o > 0; o >>= 1) acc = b2sum_xor(acc, o);
         if (on && gl == 0) ys[j] = bmv(dinv[j], acc);
+    }
+}
+
+// Forward substitution alone on forward level l with a factor made earlier
+// (two-pass form, L scaled): y_j -= sum_k L(j,k) y_k, summed exactly as the
+// y part of lu_pivots with the same lane groups, so the result is the one the
+// fused factor-and-substitute pass gives.
+template <typename TJ, int NT>
+__device__ __forceinline__ void fwd_rows(const TopoView &G, int l, int lg, int t, const typename Blk<TJ>::b4 *Lv,
+                                         typename Blk<TJ>::b2 *ys) {
+    using B2 = typename Blk<TJ>::b2;
+    const int gs = 1 << lg, gl = t & (gs - 1), ng = NT >> lg;
+    const int beg = G.flev_ptr[l], cnt = G.flev_ptr[l + 1] - beg;
+    for (int b0 = 0; b0 < cnt; b0 += ng) {
+        const int w = b0 + (t >> lg);
+        const bool on = w < cnt;
+        const int j = on ? G.flev_steps[beg + w] : 0;
+        B2 yj;
+        yj.x = yj.y = (TJ)0;
+        if (on && gl == 0) yj = ys[j];
+        if (on)
+            for (int q = G.dg_ptr[j] + gl; q < G.dg_ptr[j + 1]; q += gs) {
+                const B2 v = bmv(Lv[G.dg_pos[q]], ys[G.dg_k[q]]);
+                yj.x -= v.x;
+                yj.y -= v.y;
+            }
+        for (int o = gs >> 1; o > 0; o >>= 1) yj = b2sum_xor(yj, o);
+        if (on && gl == 0) ys[j] = yj;
     }
 }
 
@@ -860,6 +986,49 @@ __device__ __forceinline__ double warp_max(double v) {
 // __syncwarp.  Each warp owns a slice of the block's dynamic shared memory
 // (state and factor); the topology's read-only blob is read from global
 // memory through the L1 cache.
+// Iteration 0 of every instance of topology T that starts from the grid's
+// own state (FlatLayout): one warp, the warp kernel's own arithmetic (same
+// functions, lane groups and order), so an instance that takes it gets the
+// values it would have computed itself.  Shared memory: ys (zero right-hand
+// side; only the factor is kept) and the active-voltage flags.
+template <typename TJ>
+__global__ void __launch_bounds__(32) k_flat_start(const Topo T, char *out, int warp_group) {
+    using B4 = typename Blk<TJ>::b4;
+    using B2 = typename Blk<TJ>::b2;
+    extern __shared__ __align__(16) unsigned char fsm[];
+    const int lane = threadIdx.x;
+    const TopoView G = bind(T.o, T.blob);
+    const int n = T.n, nB = T.nB, nq = T.n + 2 * T.nup;
+    const FlatLayout F = flat_layout<TJ>(nB, nq);
+    const double *V = (const double *)(out + F.V0), *th = (const double *)(out + F.th0);
+    double *cs = (double *)(out + F.cs), *sn = (double *)(out + F.sn), *P = (double *)(out + F.P),
+           *Q = (double *)(out + F.Q);
+    double2 *ef = (double2 *)(out + F.ef);
+    float4 *f32 = (float4 *)(out + F.f32);
+    B4 *fac = (B4 *)(out + F.fac), *Lv = fac + n, *Uv = fac + n + T.nup;
+    B2 *ys = (B2 *)fsm;
+    unsigned char *act = fsm + align_up(sizeof(B2) * n, 16);
+    for (int k = lane; k < nB; k += 32) {
+        phasor<TJ>(k, th, V, cs, sn, ef, f32);
+        act[k] = (G.type[k] == 0 || G.type[k] == 1);
+    }
+    for (int j = lane; j < n; j += 32) ys[j].x = ys[j].y = (TJ)0;
+    __syncwarp();
+    for (int k = lane; k < nB; k += 32) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
+    __syncwarp();
+    for (int q = lane; q < nq; q += 32) fac[q] = jac_block<TJ>(G, q, n, act, P, Q, V, cs, sn, f32);
+    __syncwarp();
+    bool sing = false;
+    for (int l = 0; l < T.nfl; l++) {
+        sing |= lu_pivots<TJ, 32>(G, l, warp_group ? G.lvl_group_w[3 * l] : 0, lane, fac, fac, ys, Lv, Uv);
+        __syncwarp();
+        lu_entries<TJ, 32>(G, l, warp_group ? G.lvl_group_w[3 * l + 1] : 0, lane, fac, Lv, Uv);
+        __syncwarp();
+    }
+    sing = __any_sync(0xffffffffu, sing);
+    if (lane == 0) *(int *)(out + F.sing) = sing ? 1 : 0;
+}
+
 template <typename TJ>
 __global__ void __launch_bounds__(32 * kWarpsMax, 1) k_nr_warp(Args a) {
     using B4 = typename Blk<TJ>::b4;
@@ -892,6 +1061,8 @@ __global__ void __launch_bounds__(32 * kWarpsMax, 1) k_nr_warp(Args a) {
         B4 *fac = (B4 *)(ism + L.fac), *dinv = fac;  // block inverses overwrite the diagonal
         const int n = T.n, nB = T.nB, nq = T.n + 2 * T.nup;
         B4 *Lv = fac + n, *Uv = fac + n + T.nup;
+        const char *flat = (T.flat && a.flat_on && *a.flat_on) ? T.flat : nullptr;
+        const FlatLayout F = flat_layout<TJ>(nB, nq);
         for (int k = lane; k < nB; k += 32) {
             V[k] = a.V0[off + k];
             th[k] = a.th0[off + k];
@@ -921,17 +1092,23 @@ __global__ void __launch_bounds__(32 * kWarpsMax, 1) k_nr_warp(Args a) {
                 parked = true;
                 break;
             }
-            if (sizeof(TJ) == 8 || it == 0)
+            const bool f0 = it == 0 && flat;
+            if (f0) {
+                // the shared iteration 0 of this topology's start
                 for (int k = lane; k < nB; k += 32) {
-                    double s, c;
-                    sincos(th[k], &s, &c);
-                    cs[k] = c;
-                    sn[k] = s;
-                    ef[k] = make_double2(V[k] * c, V[k] * s);
-                    if (sizeof(TJ) == 4) f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
+                    cs[k] = ((const double *)(flat + F.cs))[k];
+                    sn[k] = ((const double *)(flat + F.sn))[k];
+                    ef[k] = ((const double2 *)(flat + F.ef))[k];
+                    if (sizeof(TJ) == 4) f32[k] = ((const float4 *)(flat + F.f32))[k];
+                    P[k] = ((const double *)(flat + F.P))[k];
+                    Q[k] = ((const double *)(flat + F.Q))[k];
                 }
-            __syncwarp();
-            for (int k = lane; k < nB; k += 32) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
+            } else {
+                if (sizeof(TJ) == 8 || it == 0)
+                    for (int k = lane; k < nB; k += 32) phasor<TJ>(k, th, V, cs, sn, ef, f32);
+                __syncwarp();
+                for (int k = lane; k < nB; k += 32) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
+            }
             __syncwarp();
             if (a.lim && it >= 1 && it < a.max_iter && abits(maxDx) < tol10_bits) {
                 for (int i0 = 0; i0 < T.nPV; i0 += 32) {
@@ -983,70 +1160,41 @@ __global__ void __launch_bounds__(32 * kWarpsMax, 1) k_nr_warp(Args a) {
             if (mloc > kInfBits) { status = GBPF_E_NOCONV; break; }
             if (mloc <= tol_bits) break;
             if (it >= a.max_iter) { status = GBPF_E_NOCONV; break; }
-            for (int qq = lane; qq < nq; qq += 32) {
-                const int sl = G.ysl[qq];
-                B4 blk;
-                blk.x = blk.y = blk.z = blk.w = 0;
-                if (sl >= 0) {
-                    const int k = G.rbus[qq], mb = G.cbus[qq];
-                    const int ak = act[k];
-                    if constexpr (sizeof(TJ) == 4) {
-                        // FP32-LU form: FP32 copies of the phasors, V and Ybus
-                        const float4 fk = f32[k];
-                        const float2 y = G.yval32[sl];
-                        if (qq < n) {
-                            blk = diag_block32<B4>((float)P[k], (float)Q[k], fk.z, y, ak);
-                        } else {
-                            const int am = act[mb];
-                            const float4 fm = f32[mb];
-                            const float tr = y.x * fm.x - y.y * fm.y, ti = y.x * fm.y + y.y * fm.x;
-                            const float wr = fk.x * tr + fk.y * ti, wi = fk.y * tr - fk.x * ti;
-                            blk.x = fk.z * fm.z * wi;
-                            if (am) blk.y = fk.z * wr;
-                            if (ak) blk.z = -fk.z * fm.z * wr;
-                            if (ak && am) blk.w = fk.z * wi;
-                        }
-                    } else {
-                        const double2 y = G.yval[sl];
-                        const double Vk = V[k];
-                        if (qq < n) {
-                            blk = diag_block<TJ, B4>(P[k], Q[k], Vk, y, ak);
-                        } else {
-                            // off-diagonal entries in the precision of the factor
-                            const int am = act[mb];
-                            const TJ ck = (TJ)cs[k], sk = (TJ)sn[k], cm = (TJ)cs[mb], sm = (TJ)sn[mb];
-                            const TJ yr = (TJ)y.x, yi = (TJ)y.y, vk = (TJ)Vk, vm = (TJ)V[mb];
-                            const TJ tr = yr * cm - yi * sm, ti = yr * sm + yi * cm;
-                            const TJ wr = ck * tr + sk * ti, wi = sk * tr - ck * ti;
-                            blk.x = vk * vm * wi;
-                            if (am) blk.y = vk * wr;
-                            if (ak) blk.z = -vk * vm * wr;
-                            if (ak && am) blk.w = vk * wi;
-                        }
-                    }
-                }
-                fac[qq] = blk;
-            }
-            __syncwarp();
-            // LU fused with forward substitution, level by level, and the
-            // backward substitution, as in the block kernel with 32 lanes
-            bool sing = false;
-            B2 *zs = (B2 *)(ism + L.zs);
-            for (int l = 0; l < T.nfl; l++) {
-                const int gp = a.warp_group ? G.lvl_group_w[3 * l] : 0, ge = a.warp_group ? G.lvl_group_w[3 * l + 1] : 0;
-                if (a.lu1) {
-                    sing |= lu_level1<TJ, 32>(G, l, gp, ge, a.warp_group ? G.lvl_rot[l] >> 16 : 0, lane, fac, dinv, ys,
-                                              zs, Lv, Uv);
-                } else {
-                    sing |= lu_pivots<TJ, 32>(G, l, gp, lane, fac, dinv, ys, Lv, Uv);
+            const B4 *Ub = Uv, *Db = dinv;
+            if (f0) {
+                // the shared factor: forward substitution alone
+                const B4 *facS = (const B4 *)(flat + F.fac);
+                if (*(const int *)(flat + F.sing)) { status = GBPF_E_SINGULAR; break; }
+                for (int l = 0; l < T.nfl; l++) {
+                    fwd_rows<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l] : 0, lane, facS + n, ys);
                     __syncwarp();
-                    lu_entries<TJ, 32>(G, l, ge, lane, dinv, Lv, Uv);
                 }
+                Ub = facS + n + T.nup;
+                Db = facS;
+            } else {
+                for (int qq = lane; qq < nq; qq += 32) fac[qq] = jac_block<TJ>(G, qq, n, act, P, Q, V, cs, sn, f32);
                 __syncwarp();
+                // LU fused with forward substitution, level by level, as in
+                // the block kernel with 32 lanes
+                bool sing = false;
+                B2 *zs = (B2 *)(ism + L.zs);
+                for (int l = 0; l < T.nfl; l++) {
+                    const int gp = a.warp_group ? G.lvl_group_w[3 * l] : 0,
+                              ge = a.warp_group ? G.lvl_group_w[3 * l + 1] : 0;
+                    if (a.lu1) {
+                        sing |= lu_level1<TJ, 32>(G, l, gp, ge, a.warp_group ? G.lvl_rot[l] >> 16 : 0, lane, fac, dinv,
+                                                  ys, zs, Lv, Uv);
+                    } else {
+                        sing |= lu_pivots<TJ, 32>(G, l, gp, lane, fac, dinv, ys, Lv, Uv);
+                        __syncwarp();
+                        lu_entries<TJ, 32>(G, l, ge, lane, dinv, Lv, Uv);
+                    }
+                    __syncwarp();
+                }
+                if (__any_sync(FULL, sing)) { status = GBPF_E_SINGULAR; break; }
             }
-            if (__any_sync(FULL, sing)) { status = GBPF_E_SINGULAR; break; }
             for (int l = 0; l < T.nbl; l++) {
-                back_rows<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l + 2] : 0, lane, dinv, Uv, ys);
+                back_rows<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l + 2] : 0, lane, Db, Ub, ys);
                 __syncwarp();
             }
             unsigned long long md = 0;
@@ -1374,6 +1522,8 @@ struct gbpf_batch {
     DevBuf topo_na;          // topologies planned for gbpf_batch_solve_noalloc
     void *h_in = nullptr, *h_out = nullptr;  // pinned mirrors of the input and output regions
     bool start_is_default = false;           // the device V0 / theta0 hold the grids' own start
+    int flat_flag = 0;                       // host copy of the device flag behind Args::flat_on
+    DevBuf flat_mem;                         // k_flat_start outputs, one FlatLayout per topology
     size_t out_bytes = 0;
     size_t na_smem = 0, na_stride = 0;
     cudaGraphExec_t exec = nullptr;
@@ -1403,10 +1553,12 @@ struct gbpf_batch {
     // grouped lanes of deep levels in the hand-off blocks and in the warps;
     // narrow = 1 runs the narrow levels of the block kernel on one warp; lu1 /
     // warp_lu1 = 1 factor in one pass per elimination level in the block
-    // kernel (block mode and hand-off) / in the warp kernel.
+    // kernel (block mode and hand-off) / in the warp kernel; flat_shared = 1
+    // lets the warp kernel's instances take the shared iteration 0 of their
+    // topology when they start from the grid's own state (k_flat_start).
     struct Plan {
         int warp_mode = 1, warp_warps = 8, handoff_it = kHandoffIt, resume_group = 1, warp_group = 1, narrow = 0,
-            lu1 = 1, warp_lu1 = 0;
+            lu1 = 1, warp_lu1 = 0, flat_shared = 1;
     } plan;
     gbpf_status rebuild() {
         CK(cudaStreamSynchronize(stream));
@@ -1654,11 +1806,17 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
     else
         CK(cudaMemcpyAsync((void *)args.V0, h_in, 5 * nba, cudaMemcpyHostToDevice, stream));
     start_is_default = dflt;
-    if (same) return GBPF_OK;
-    CK(cudaStreamSynchronize(stream));
-    if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
-    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
-    return build_graph();
+    if (!same) {
+        CK(cudaStreamSynchronize(stream));
+        if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+        if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+        const gbpf_status st = build_graph();
+        if (st != GBPF_OK) return st;
+    }
+    // instances from the grids' own start may take the shared iteration 0
+    flat_flag = dflt ? 1 : 0;
+    CK(cudaMemcpyAsync((int *)counter.p + 8, &flat_flag, sizeof(int), cudaMemcpyHostToDevice, stream));
+    return GBPF_OK;
 }
 
 gbpf_status gbpf_batch::launch(cudaStream_t st) { return launch_with(st, args, wargs, true); }
@@ -1822,6 +1980,36 @@ gbpf_status gbpf_batch::build_graph() {
         }
         warp_grid = std::max(1, std::min((n_warp_q + warp_warps - 1) / warp_warps, dev_sm * std::max(occ, 1)));
     }
+    // the shared flat-start iteration of every warp-served topology
+    flat_mem.reset();
+    for (auto &T : topo_h) T.flat = nullptr;
+    if (n_warp_q && plan.flat_shared) {
+        std::vector<size_t> at(topo_h.size(), 0);
+        size_t total = 0;
+        for (size_t t = 0; t < topo_h.size(); t++) {
+            if (!warp_ok[t]) continue;
+            const Topo &T = topo_h[t];
+            const int nq = T.n + 2 * T.nup;
+            at[t] = total;
+            total += fp32 ? flat_layout<float>(T.nB, nq).total : flat_layout<double>(T.nB, nq).total;
+        }
+        CK(cudaMalloc(&flat_mem.p, total));
+        for (size_t t = 0; t < topo_h.size(); t++) {
+            if (!warp_ok[t]) continue;
+            Topo &T = topo_h[t];
+            const int nq = T.n + 2 * T.nup;
+            const FlatLayout F = fp32 ? flat_layout<float>(T.nB, nq) : flat_layout<double>(T.nB, nq);
+            char *o = (char *)flat_mem.p + at[t];
+            CK(cudaMemcpyAsync(o + F.V0, grids[t].V0.data(), 8 * (size_t)T.nB, cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(o + F.th0, grids[t].theta0.data(), 8 * (size_t)T.nB, cudaMemcpyHostToDevice, stream));
+            const size_t fs = align_up((fp32 ? 8 : 16) * (size_t)T.n, 16) + (size_t)T.nB;
+            if (fp32) k_flat_start<float><<<1, 32, fs, stream>>>(T, o, plan.warp_group);
+            else k_flat_start<double><<<1, 32, fs, stream>>>(T, o, plan.warp_group);
+            CK(cudaGetLastError());
+            T.flat = o;
+        }
+        CK(cudaStreamSynchronize(stream));
+    }
     scratch.reset();
     args.scratch = nullptr;
     args.scratch_stride = (long long)align_up(scr, 256);
@@ -1841,6 +2029,8 @@ gbpf_status gbpf_batch::build_graph() {
     args.queue = (const int *)queues.p + n_warp_q;
     args.queue_len = n_block_q;
     wargs.counter = (int *)counter.p + 1;
+    wargs.flat_on = (const int *)counter.p + 8;
+    args.flat_on = nullptr;
     wargs.queue = (const int *)queues.p;
     wargs.queue_len = n_warp_q;
     wargs.slice = (int)slice;
@@ -1912,6 +2102,7 @@ gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, 
     Args ba = args, wa = wargs;
     ba.V0 = wa.V0 = wV;
     ba.th0 = wa.th0 = wTh;
+    wa.flat_on = nullptr;  // predicted starts: no shared iteration 0
     ba.max_iter = wa.max_iter = std::min(max_iter, kWarmMaxIter);
     if ((st = launch_with(stream, ba, wa)) != GBPF_OK) return st;
     k_ws_check<<<(n_inst * 32 + 255) / 256, 256, 0, stream>>>(args, wV, wKind);
@@ -1998,6 +2189,7 @@ gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
         {&Plan::narrow, {1, 0}, false, false},
         {&Plan::lu1, {1, 0}, false, false},
         {&Plan::warp_lu1, {0, 1}, true, false},
+        {&Plan::flat_shared, {1, 0}, true, false},
     };
     for (int sweep = 0; sweep < 2; sweep++) {
         bool changed = false;
@@ -2024,7 +2216,7 @@ gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
     return st;
 }
 
-static void plan_out(const gbpf_batch *b, int plan[12]) {
+static void plan_out(const gbpf_batch *b, int plan[16]) {
     plan[0] = b->plan.warp_mode;
     plan[1] = b->plan.warp_warps;
     plan[2] = b->plan.handoff_it;
@@ -2033,22 +2225,23 @@ static void plan_out(const gbpf_batch *b, int plan[12]) {
     plan[5] = b->plan.narrow;
     plan[6] = b->plan.lu1;
     plan[7] = b->plan.warp_lu1;
-    plan[8] = b->warp_warps;  // warps per block in use
-    plan[9] = b->n_warp_q;
-    plan[10] = b->n_block_q;
-    plan[11] = 0;
+    plan[8] = b->plan.flat_shared;
+    plan[9] = b->warp_warps;  // warps per block in use
+    plan[10] = b->n_warp_q;
+    plan[11] = b->n_block_q;
+    for (int i = 12; i < 16; i++) plan[i] = 0;
 }
 
-extern "C" gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[12]) {
+extern "C" gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[16]) {
     ARGCHECK(b && plan);
     plan_out(b, plan);
     return GBPF_OK;
 }
 
-extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[8]) {
+extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[9]) {
     ARGCHECK(b && plan && (plan[0] == 0 || plan[0] == 1) && plan[1] >= 0 && plan[1] <= kWarpsMax && plan[2] >= 0 &&
              (plan[3] == 0 || plan[3] == 1) && (plan[4] == 0 || plan[4] == 1) && (plan[5] == 0 || plan[5] == 1) &&
-             (plan[6] == 0 || plan[6] == 1) && (plan[7] == 0 || plan[7] == 1));
+             (plan[6] == 0 || plan[6] == 1) && (plan[7] == 0 || plan[7] == 1) && (plan[8] == 0 || plan[8] == 1));
     CK(cudaSetDevice(b->device));
     b->plan.warp_mode = plan[0];
     b->plan.warp_warps = plan[1];
@@ -2058,11 +2251,12 @@ extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[8]) {
     b->plan.narrow = plan[5];
     b->plan.lu1 = plan[6];
     b->plan.warp_lu1 = plan[7];
+    b->plan.flat_shared = plan[8];
     if (!b->n_inst) return GBPF_OK;
     return b->rebuild();
 }
 
-extern "C" gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[12], float ms[2]) {
+extern "C" gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[16], float ms[2]) {
     ARGCHECK(b && b->exec && repeats > 0);
     CK(cudaSetDevice(b->device));
     float best = 0, first = 0;

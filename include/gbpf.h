@@ -339,14 +339,18 @@ gbpf_status gbpf_batch_kernel_times(gbpf_batch *b, int repeats, double ms[3]);
  * barriers between them; plan[6] / plan[7] 1 = the LU of the thread-block
  * kernel / of the warp kernel takes one pass per elimination level (L kept
  * unscaled, pivots and entries of a level side by side), 0 = two passes
- * (pivots, then entries scaled by the pivot inverse).  get_plan also returns
- * plan[8] warps per block in use, plan[9] instances on warps, plan[10]
- * instances on blocks (plan[11] = 0).  Setting a plan rebuilds the batch
- * graph. */
-gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[12]);
-gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[8]);
+ * (pivots, then entries scaled by the pivot inverse); plan[8] 1 = instances
+ * on warps that start from their grid's own starting state (no V0 / theta0
+ * given) take iteration 0 -- phasors, injections and the factored Jacobian,
+ * which depend on the topology and the start only -- from one computation per
+ * topology, and do only their own substitutions in it.  get_plan also
+ * returns plan[9] warps per block in use, plan[10] instances on warps,
+ * plan[11] instances on blocks (plan[12..15] = 0).  Setting a plan rebuilds
+ * the batch graph. */
+gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[16]);
+gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[9]);
 
-/* Autotuner: a coordinate search over plan[0..7] on the current instances,
+/* Autotuner: a coordinate search over plan[0..8] on the current instances,
  * from the default plan.  Each knob takes each of its values in turn with the
  * others fixed; a value is kept when the whole batch solve (best of `repeats`
  * timed graph launches after one warm-up, CUDA events on the batch stream) is
@@ -354,7 +358,7 @@ gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[8]);
  * The best plan stays set; plan receives it (as gbpf_batch_get_plan) and
  * ms[0] / ms[1] the batch time of the default and of the chosen plan.  The
  * trial solves overwrite the instances' results. */
-gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[12], float ms[2]);
+gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[16], float ms[2]);
 
 /* Per-instance results of the last batch solve (any pointer may be NULL);
  * V/theta/P/Q packed like the inputs. */

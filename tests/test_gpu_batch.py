@@ -277,3 +277,33 @@ def test_batch_starting_state_kept_or_replaced(gb):
         r = b.results()
         np.testing.assert_array_equal(r["iterations"], ref["iterations"])
         np.testing.assert_array_equal(r["V"], ref["V"])
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_batch_shared_flat_start_is_exact(gb, precision):
+    """Iteration 0 from the grids' own start, computed once per topology and
+    shared (plan flat_shared), gives bit-identical results to every instance
+    computing it itself; a given start (V0) bypasses it."""
+    import bench
+
+    path = os.path.join(GOLDEN, "c2_base.cdf")
+    g = gb.read_grid(path)
+    base = g.buses()
+    Pl, Ql, Pg = bench.scenarios(np, base, 4096, bench.BASE_SEED + 7)
+    pick = list(range(40)) + [1943, 2749, 3628, 4084]
+    Pl, Ql, Pg = Pl[pick].ravel(), Ql[pick].ravel(), Pg[pick].ravel()
+    n = len(pick)
+    out = []
+    for flat in (1, 0):
+        b = gb.Batch([g], precision=precision, tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1)
+        b.set_plan(flat_shared=flat)
+        b.set_instances(np.zeros(n, np.int32), Pload=Pl, Qload=Ql, Pg=Pg)
+        b.solve()
+        r = b.results()
+        r["events"] = [b.events(i) for i in range(n)]
+        out.append(r)
+    for k in ("iterations", "status", "final_mismatch", "V", "theta", "Pcalc", "Qcalc", "events"):
+        if k == "events":
+            assert out[0][k] == out[1][k]
+        else:
+            np.testing.assert_array_equal(out[0][k], out[1][k], err_msg=k)
