@@ -405,8 +405,8 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     achieved = bytes_launch / t_launch / 1e9
     # DRAM traffic of one k_nr_warp<float> launch of the 32,768 c2 scenarios
     # (ncu dram__bytes_read.sum + dram__bytes_write.sum, one-pass capture of the
-    # full-size run, profiles/k_nr_warp_fp32_c2_32768.md), scaled by instances
-    traffic = 202.9e6 * N_SCEN / 32768 if a.workload == "c2" else None
+    # full-size run with the default plan), scaled by instances
+    traffic = 201.7e6 * N_SCEN / 32768 if a.workload == "c2" else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": max(3, a.warmup), "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True,
@@ -431,7 +431,7 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
                      "traffic": traffic / 1e9 if traffic else None, "traffic_unit": "GB per launch",
                      "algorithmic_bytes_per_launch": bytes_launch,
                      "kernel_ms_per_launch": kt,
-                     "note": "FP64-pipe and dependent-latency bound (ncu: FP64 pipe ~50 % of active cycles); state "
+                     "note": "dependent-latency bound (ncu: issue 20 % of active cycles, FP64 pipe 31 %); state "
                              "lives in shared memory, the step's remaining time is the hand-off launch of the few "
                              "instances that run all 100 iterations"},
         "clocks": clk.summary(),
