@@ -659,6 +659,23 @@ def bench_single(a, gb, np, rank, dev, world, dist):
         r = s.solve(full=False)
         s.state()
     t_e2e = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    # config 3 also runs the FP32-LU form of the same solver (FP32 factor and
+    # substitutions, FP64 fill, mismatch, test and update): solves/s and its
+    # |V|, theta error against the FP64 solution
+    fp32 = None
+    if a.workload == "c3":
+        s32 = gb.Solver(grid, device=dev, tolerancia=1e-8, no_max_iter=100, lim_inj_reat=lim, metodo=0,
+                        precision=gb.PREC_FP32_IR)
+        r32 = s32.solve()
+        r64 = s.solve()
+        s32.time(max(3, a.warmup))
+        ms32 = s32.time(a.steps)
+        fp32 = {"solves_per_s": a.steps / (ms32 / 1e3), "ms_per_solve": ms32 / a.steps,
+                "iterations": r32["iterations"], "final_mismatch": r32["final_mismatch"],
+                "max_abs_err_V": float(np.max(np.abs(r32["V"] - r64["V"]))),
+                "max_abs_err_theta": float(np.max(np.abs(r32["theta"] - r64["theta"]))),
+                "same_switch_events": [e[1:] for e in r32["events"]] == [e[1:] for e in r64["events"]],
+                "phases": s32.profile(5)}
     peak, src = peak_hbm()
     if dense:
         # metodo = denso: per Newton iteration the N x N FP64 matrix is written
@@ -682,7 +699,7 @@ def bench_single(a, gb, np, rank, dev, world, dist):
         "config": {"workload": a.workload, "grid": desc, "nB": grid.nB, "tolerance": 1e-8, "lim_inj_reat": lim,
                    "form": ("metodo = denso: dense FP64 Jacobian and LU with partial pivoting, one solve per step"
                             if dense else "plain FP64, one solve per step"), "iterations": first["iterations"],
-                   "solver": info, "parallelism": f"replicas x{world}",
+                   "solver": info, "parallelism": f"replicas x{world}", "fp32_lu": fp32,
                    "l2": "working set fits in L2; no flush"},
         "e2e": {"value": world * a.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * grid.nB * 8,
                 "d2h_bytes_per_step": 4 * grid.nB * 8 + 32},

@@ -82,6 +82,11 @@ struct Dev {
     const int *ysl, *rbus, *cbus;
     blk4 *fac, *dinv;
     double2 *rhs, *ys, *xs;
+    // FP32-LU form (precision = GBPF_PREC_FP32_IR): the factor and the
+    // substitutions in FP32; fill, mismatch and update stay FP64
+    float4 *fac32, *dinv32;
+    float2 *ys32, *xs32;
+    int fp32;
     Ctl *ctl;
     double *hist;
     int *trig;       // [hist_cap] 1 where the limit check ran (chkLimQ's "\n")
@@ -317,74 +322,233 @@ __global__ void k_jfill(Dev d, int guard) {
             blk = mk4(H, am ? N : 0.0, ak ? M : 0.0, (ak && am) ? L : 0.0);
         }
     }
-    d.fac[q] = blk;
+    if (d.fp32) d.fac32[q] = make_float4((float)blk.x, (float)blk.y, (float)blk.z, (float)blk.w);
+    else d.fac[q] = blk;
 }
 
-// One forward level: Crout step j per warp (diagonal block, its inverse, the
-// L column and U row of j) fused with the forward substitution y_j.
+// Factor blocks and substitution vectors in the precision of the LU.
+template <typename TJ> struct SB;
+template <> struct SB<double> { using b4 = blk4; using b2 = double2; };
+template <> struct SB<float> { using b4 = float4; using b2 = float2; };
+template <typename TJ> __device__ __forceinline__ typename SB<TJ>::b4 *fac_of(const Dev &d);
+template <> __device__ __forceinline__ blk4 *fac_of<double>(const Dev &d) { return d.fac; }
+template <> __device__ __forceinline__ float4 *fac_of<float>(const Dev &d) { return d.fac32; }
+template <typename TJ> __device__ __forceinline__ typename SB<TJ>::b4 *dinv_of(const Dev &d);
+template <> __device__ __forceinline__ blk4 *dinv_of<double>(const Dev &d) { return d.dinv; }
+template <> __device__ __forceinline__ float4 *dinv_of<float>(const Dev &d) { return d.dinv32; }
+template <typename TJ> __device__ __forceinline__ typename SB<TJ>::b2 *ys_of(const Dev &d);
+template <> __device__ __forceinline__ double2 *ys_of<double>(const Dev &d) { return d.ys; }
+template <> __device__ __forceinline__ float2 *ys_of<float>(const Dev &d) { return d.ys32; }
+template <typename TJ> __device__ __forceinline__ typename SB<TJ>::b2 *xs_of(const Dev &d);
+template <> __device__ __forceinline__ double2 *xs_of<double>(const Dev &d) { return d.xs; }
+template <> __device__ __forceinline__ float2 *xs_of<float>(const Dev &d) { return d.xs32; }
+
+template <typename B4> __device__ __forceinline__ B4 mmT(B4 a, B4 b) {
+    B4 r;
+    r.x = a.x * b.x + a.y * b.z; r.y = a.x * b.y + a.y * b.w;
+    r.z = a.z * b.x + a.w * b.z; r.w = a.z * b.y + a.w * b.w;
+    return r;
+}
+template <typename B4, typename B2> __device__ __forceinline__ B2 mvT(B4 a, B2 v) {
+    B2 r;
+    r.x = a.x * v.x + a.y * v.y;
+    r.y = a.z * v.x + a.w * v.y;
+    return r;
+}
+template <typename B4> __device__ __forceinline__ B4 sub4T(B4 a, B4 b) {
+    a.x -= b.x; a.y -= b.y; a.z -= b.z; a.w -= b.w;
+    return a;
+}
+template <typename B4> __device__ __forceinline__ B4 add4T(B4 a, B4 b) {
+    a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
+    return a;
+}
+template <typename B4> __device__ __forceinline__ B4 xsum4(B4 v, int w) {  // sum over aligned groups of w lanes
+    for (int o = w >> 1; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        v.z += __shfl_xor_sync(0xffffffffu, v.z, o);
+        v.w += __shfl_xor_sync(0xffffffffu, v.w, o);
+    }
+    return v;
+}
+template <typename B2> __device__ __forceinline__ B2 xsum2(B2 v, int w) {
+    for (int o = w >> 1; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+template <typename B4> __device__ __forceinline__ B4 bcast4(B4 v, int src) {
+    v.x = __shfl_sync(0xffffffffu, v.x, src);
+    v.y = __shfl_sync(0xffffffffu, v.y, src);
+    v.z = __shfl_sync(0xffffffffu, v.z, src);
+    v.w = __shfl_sync(0xffffffffu, v.w, src);
+    return v;
+}
+
+// The pivot of step j: D_j = A_jj - sum L(j,k) U(k,j) given the gathered sum,
+// its inverse and y_j = rhs_j - (gathered sum); flags a singular block.
+template <typename TJ>
+__device__ __forceinline__ typename SB<TJ>::b4 pivot_done(const Dev &d, int j, typename SB<TJ>::b4 acc,
+                                                          typename SB<TJ>::b2 accy) {
+    using B4 = typename SB<TJ>::b4;
+    using B2 = typename SB<TJ>::b2;
+    B4 *fac = fac_of<TJ>(d);
+    const B4 D = sub4T(fac[j], acc);
+    const TJ det = D.x * D.w - D.y * D.z;
+    if (det == (TJ)0 || !isfinite(det)) {
+        d.ctl->status = GBPF_E_SINGULAR;
+        d.ctl->done = 1;
+    }
+    B4 inv;
+    inv.x = D.w / det; inv.y = -D.y / det; inv.z = -D.z / det; inv.w = D.x / det;
+    fac[j] = D;
+    dinv_of<TJ>(d)[j] = inv;
+    const double2 r = d.rhs[j];
+    B2 y;
+    y.x = (TJ)r.x - accy.x;
+    y.y = (TJ)r.y - accy.y;
+    ys_of<TJ>(d)[j] = y;
+    return inv;
+}
+
+// One forward level, one warp per Crout step j (diagonal block, its inverse,
+// the L column and U row of j) fused with the forward substitution y_j.
+template <typename TJ>
 __global__ void k_factor(Dev d, int beg, int cnt, int guard) {
+    using B4 = typename SB<TJ>::b4;
+    using B2 = typename SB<TJ>::b2;
     if (stopped(d, guard)) return;
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= cnt) return;
     const int j = d.flev_steps[beg + w];
-    const blk4 *Lv = d.fac + d.n, *Uv = d.fac + d.n + d.nup;
-    blk4 acc = mk4(0, 0, 0, 0);
-    double2 accy = make_double2(0, 0);
+    B4 *fac = fac_of<TJ>(d);
+    B4 *Lv = fac + d.n, *Uv = fac + d.n + d.nup;
+    const B2 *ys = ys_of<TJ>(d);
+    B4 acc;
+    acc.x = acc.y = acc.z = acc.w = (TJ)0;
+    B2 accy;
+    accy.x = accy.y = (TJ)0;
     for (int t = d.dg_ptr[j] + lane; t < d.dg_ptr[j + 1]; t += 32) {
         const int a = d.dg_pos[t];
-        const blk4 l = Lv[a];
-        acc = add4(acc, mm(l, Uv[a]));
-        const double2 v = mv(l, d.ys[d.dg_k[t]]);
+        const B4 l = Lv[a];
+        acc = add4T(acc, mmT(l, Uv[a]));
+        const B2 v = mvT(l, ys[d.dg_k[t]]);
         accy.x += v.x;
         accy.y += v.y;
     }
-    acc = warp_sum4(acc);
-    accy = warp_sum2(accy);
-    blk4 inv = mk4(0, 0, 0, 0);
-    if (lane == 0) {
-        const blk4 D = sub4(d.fac[j], acc);
-        const double det = D.x * D.w - D.y * D.z;
-        if (det == 0.0 || !isfinite(det)) {
-            d.ctl->status = GBPF_E_SINGULAR;
-            d.ctl->done = 1;
-        }
-        inv = mk4(D.w / det, -D.y / det, -D.z / det, D.x / det);
-        d.fac[j] = D;
-        d.dinv[j] = inv;
-        const double2 r = d.rhs[j];
-        d.ys[j] = make_double2(r.x - accy.x, r.y - accy.y);
-    }
-    inv = shfl4(inv, 0);
-    blk4 *Lw = d.fac + d.n, *Uw = d.fac + d.n + d.nup;
+    acc = xsum4(acc, 32);
+    accy = xsum2(accy, 32);
+    B4 inv;
+    inv.x = inv.y = inv.z = inv.w = (TJ)0;
+    if (lane == 0) inv = pivot_done<TJ>(d, j, acc, accy);
+    inv = bcast4(inv, 0);
     for (int p = d.up_ptr[j] + lane; p < d.up_ptr[j + 1]; p += 32) {
-        blk4 aL = Lw[p], aU = Uw[p];
+        B4 aL = Lv[p], aU = Uv[p];
         for (long long r = d.og_ptr[p]; r < d.og_ptr[p + 1]; r++) {
             const int a = d.og_a[r], b = d.og_b[r];
-            aL = sub4(aL, mm(Lv[b], Uv[a]));
-            aU = sub4(aU, mm(Lv[a], Uv[b]));
+            aL = sub4T(aL, mmT(Lv[b], Uv[a]));
+            aU = sub4T(aU, mmT(Lv[a], Uv[b]));
         }
-        Uw[p] = aU;
-        Lw[p] = mm(aL, inv);
+        Uv[p] = aU;
+        Lv[p] = mmT(aL, inv);
     }
 }
 
-// One backward level: x_j = D_j^-1 (y_j - sum_i U(j,i) x_i).
+// The same step for levels whose pivots carry long gather lists (the top of
+// the elimination tree of large grids): one 256-thread block per step j.  The
+// diagonal gather is spread over the block; each warp then takes entries of
+// row j in turn and its lanes split the entry's pair list, summed with
+// shuffles.
+constexpr int kFacBlk = 256;
+template <typename TJ>
+__global__ void __launch_bounds__(kFacBlk) k_factor_blk(Dev d, int beg, int guard) {
+    using B4 = typename SB<TJ>::b4;
+    using B2 = typename SB<TJ>::b2;
+    __shared__ B4 s_acc[kFacBlk / 32];
+    __shared__ B2 s_accy[kFacBlk / 32];
+    __shared__ B4 s_inv;
+    __shared__ int s_stop;
+    // blocks of this launch may set the stop flag (a singular pivot): read it
+    // once per block so that the whole block returns or none of it does
+    if (threadIdx.x == 0) s_stop = stopped(d, guard);
+    __syncthreads();
+    if (s_stop) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int j = d.flev_steps[beg + blockIdx.x];
+    B4 *fac = fac_of<TJ>(d);
+    B4 *Lv = fac + d.n, *Uv = fac + d.n + d.nup;
+    const B2 *ys = ys_of<TJ>(d);
+    B4 acc;
+    acc.x = acc.y = acc.z = acc.w = (TJ)0;
+    B2 accy;
+    accy.x = accy.y = (TJ)0;
+    for (int t = d.dg_ptr[j] + tid; t < d.dg_ptr[j + 1]; t += kFacBlk) {
+        const int a = d.dg_pos[t];
+        const B4 l = Lv[a];
+        acc = add4T(acc, mmT(l, Uv[a]));
+        const B2 v = mvT(l, ys[d.dg_k[t]]);
+        accy.x += v.x;
+        accy.y += v.y;
+    }
+    acc = xsum4(acc, 32);
+    accy = xsum2(accy, 32);
+    if (lane == 0) { s_acc[warp] = acc; s_accy[warp] = accy; }
+    __syncthreads();
+    if (tid == 0) {
+        for (int w = 1; w < kFacBlk / 32; w++) {
+            acc = add4T(acc, s_acc[w]);
+            accy.x += s_accy[w].x;
+            accy.y += s_accy[w].y;
+        }
+        s_inv = pivot_done<TJ>(d, j, acc, accy);
+    }
+    __syncthreads();
+    const B4 inv = s_inv;
+    for (int p = d.up_ptr[j] + warp; p < d.up_ptr[j + 1]; p += kFacBlk / 32) {
+        B4 aL, aU;
+        aL.x = aL.y = aL.z = aL.w = (TJ)0;
+        aU = aL;
+        for (long long r = d.og_ptr[p] + lane; r < d.og_ptr[p + 1]; r += 32) {
+            const int a = d.og_a[r], b = d.og_b[r];
+            aL = add4T(aL, mmT(Lv[b], Uv[a]));
+            aU = add4T(aU, mmT(Lv[a], Uv[b]));
+        }
+        aL = xsum4(aL, 32);
+        aU = xsum4(aU, 32);
+        if (lane == 0) {
+            Uv[p] = sub4T(Uv[p], aU);
+            Lv[p] = mmT(sub4T(Lv[p], aL), inv);
+        }
+    }
+}
+
+// One backward level: x_j = D_j^-1 (y_j - sum_i U(j,i) x_i), one warp per row.
+template <typename TJ>
 __global__ void k_bsolve(Dev d, int beg, int cnt, int guard) {
+    using B4 = typename SB<TJ>::b4;
+    using B2 = typename SB<TJ>::b2;
     if (stopped(d, guard)) return;
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= cnt) return;
     const int j = d.blev_steps[beg + w];
-    const blk4 *Uv = d.fac + d.n + d.nup;
-    double2 acc = make_double2(0, 0);
+    const B4 *Uv = fac_of<TJ>(d) + d.n + d.nup;
+    B2 *xs = xs_of<TJ>(d);
+    B2 acc;
+    acc.x = acc.y = (TJ)0;
     for (int p = d.up_ptr[j] + lane; p < d.up_ptr[j + 1]; p += 32) {
-        const double2 v = mv(Uv[p], d.xs[d.up_col[p]]);
+        const B2 v = mvT(Uv[p], xs[d.up_col[p]]);
         acc.x += v.x;
         acc.y += v.y;
     }
-    acc = warp_sum2(acc);
+    acc = xsum2(acc, 32);
     if (lane == 0) {
-        const double2 y = d.ys[j];
-        d.xs[j] = mv(d.dinv[j], make_double2(y.x - acc.x, y.y - acc.y));
+        const B2 y = ys_of<TJ>(d)[j];
+        B2 t;
+        t.x = y.x - acc.x;
+        t.y = y.y - acc.y;
+        xs[j] = mvT(dinv_of<TJ>(d)[j], t);
     }
 }
 
@@ -395,7 +559,7 @@ __global__ void k_update(Dev d, int guard) {
     double m = 0;
     if (j < d.n) {
         const int k = d.bus_of_blk[j];
-        const double2 x = d.xs[j];
+        const double2 x = d.fp32 ? make_double2((double)d.xs32[j].x, (double)d.xs32[j].y) : d.xs[j];
         d.th[k] += x.x;
         if (d.act[k]) d.V[k] += x.y;
         m = fmax(fabs(x.x), fabs(x.y));
@@ -499,16 +663,35 @@ struct gbpf_solver {
         k_update<<<cdiv_int(S.n, T), T, 0, stream>>>(d, guard);
     }
     void launch_factor_solve(int guard) {
+        launch_forward(guard);
+        launch_backward(guard);
+    }
+    void launch_forward(int guard) {
+        if (d.fp32) launch_forward_t<float>(guard);
+        else launch_forward_t<double>(guard);
+    }
+    void launch_backward(int guard) {
+        if (d.fp32) launch_backward_t<float>(guard);
+        else launch_backward_t<double>(guard);
+    }
+    // Levels whose steps carry more gather work than a warp should take on
+    // alone (level_heavy) run one block per step.
+    template <typename TJ> void launch_forward_t(int guard) {
         const int T = 256, W = T / 32;
         for (int l = 0; l < nfl(); l++) {
             const int beg = S.flev_ptr[l], cnt = S.flev_ptr[l + 1] - beg;
-            k_factor<<<cdiv_int(cnt, W), T, 0, stream>>>(d, beg, cnt, guard);
-        }
-        for (int l = 0; l < nbl(); l++) {
-            const int beg = S.blev_ptr[l], cnt = S.blev_ptr[l + 1] - beg;
-            k_bsolve<<<cdiv_int(cnt, W), T, 0, stream>>>(d, beg, cnt, guard);
+            if (level_heavy[l]) k_factor_blk<TJ><<<cnt, kFacBlk, 0, stream>>>(d, beg, guard);
+            else k_factor<TJ><<<cdiv_int(cnt, W), T, 0, stream>>>(d, beg, cnt, guard);
         }
     }
+    template <typename TJ> void launch_backward_t(int guard) {
+        const int T = 256, W = T / 32;
+        for (int l = 0; l < nbl(); l++) {
+            const int beg = S.blev_ptr[l], cnt = S.blev_ptr[l + 1] - beg;
+            k_bsolve<TJ><<<cdiv_int(cnt, W), T, 0, stream>>>(d, beg, cnt, guard);
+        }
+    }
+    std::vector<char> level_heavy;
     // metodo = denso: dense Jacobian, blocked LU with partial pivoting, the
     // triangular solves, update
     void launch_step_dense(int guard) {
@@ -630,7 +813,13 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
         d.og_ptr = A.take<long long>(nup + 1); d.og_a = A.take<int>(npairs + 1); d.og_b = A.take<int>(npairs + 1);
         d.flev_steps = A.take<int>(n); d.blev_steps = A.take<int>(n);
         d.ysl = A.take<int>(nq); d.rbus = A.take<int>(nq); d.cbus = A.take<int>(nq);
-        d.fac = A.take<blk4>(nq); d.dinv = A.take<blk4>(n);
+        d.fp32 = o.precision == GBPF_PREC_FP32_IR && !d.dense_rule;
+        if (d.fp32) {
+            d.fac32 = A.take<float4>(nq); d.dinv32 = A.take<float4>(n);
+            d.ys32 = A.take<float2>(n); d.xs32 = A.take<float2>(n);
+        } else {
+            d.fac = A.take<blk4>(nq); d.dinv = A.take<blk4>(n);
+        }
         d.rhs = A.take<double2>(n); d.ys = A.take<double2>(n); d.xs = A.take<double2>(n);
         d.ctl = A.take<Ctl>(1); d.hist = A.take<double>(hist_cap); d.trig = A.take<int>(hist_cap);
         d.events = A.take<int>(4 * kEventCap);
@@ -703,6 +892,16 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
     CK(up(d.fl_bmk, fbmk.data(), nL * sizeof(double)));
     CK(cudaStreamSynchronize(stream));
     setup_ms[2] = ms_since(tp);
+    // forward levels whose heaviest step (diagonal gather plus the pair lists
+    // of its row) exceeds 128 updates run one block per step
+    level_heavy.assign(nfl(), 0);
+    for (int l = 0; l < nfl(); l++)
+        for (int w = S.flev_ptr[l]; w < S.flev_ptr[l + 1] && !level_heavy[l]; w++) {
+            const int j = S.flev_steps[w];
+            long long work = S.dg_ptr[j + 1] - S.dg_ptr[j];
+            for (int p = S.up_ptr[j]; p < S.up_ptr[j + 1]; p++) work += S.og_ptr[p + 1] - S.og_ptr[p];
+            if (work > 128) level_heavy[l] = 1;
+        }
     tp = clk::now();
     // Ybus on the device, once per topology
     const int T = 256;
@@ -935,21 +1134,12 @@ extern "C" gbpf_status gbpf_solver_profile(gbpf_solver *s, int repeats, double m
     ARGCHECK(s && ms && bytes && repeats > 0);
     CK(cudaSetDevice(s->device));
     const Symbolic &S = s->S;
-    const int T = 256, W = T / 32, nq = S.n + 2 * S.nup;
+    const int T = 256, nq = S.n + 2 * S.nup;
     auto phase = [&](int ph) {
         if (ph == 0) s->launch_eval(0);
         else if (ph == 1) k_jfill<<<cdiv_int(nq, T), T, 0, s->stream>>>(s->d, 0);
-        else if (ph == 2) {
-            for (int l = 0; l < s->nfl(); l++) {
-                const int beg = S.flev_ptr[l], cnt = S.flev_ptr[l + 1] - beg;
-                k_factor<<<cdiv_int(cnt, W), T, 0, s->stream>>>(s->d, beg, cnt, 0);
-            }
-        } else {
-            for (int l = 0; l < s->nbl(); l++) {
-                const int beg = S.blev_ptr[l], cnt = S.blev_ptr[l + 1] - beg;
-                k_bsolve<<<cdiv_int(cnt, W), T, 0, s->stream>>>(s->d, beg, cnt, 0);
-            }
-        }
+        else if (ph == 2) s->launch_forward(0);
+        else s->launch_backward(0);
     };
     CK(cudaMemsetAsync(&s->d.ctl->done, 0, sizeof(int), s->stream));
     for (int ph = 0; ph < 4; ph++) {
@@ -1051,8 +1241,15 @@ extern "C" gbpf_status gbpf_eval_jacobian(gbpf_solver *s, const double *V, const
     k_jfill<<<cdiv_int(nq, T), T, 0, s->stream>>>(s->d, 0);
     CK(cudaGetLastError());
     std::vector<blk4> f(nq);
-    CK(cudaMemcpyAsync(f.data(), s->d.fac, nq * sizeof(blk4), cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
+    if (s->d.fp32) {
+        std::vector<float4> f32(nq);
+        CK(cudaMemcpyAsync(f32.data(), s->d.fac32, nq * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (int q = 0; q < nq; q++) f[q] = mk4(f32[q].x, f32[q].y, f32[q].z, f32[q].w);
+    } else {
+        CK(cudaMemcpyAsync(f.data(), s->d.fac, nq * sizeof(blk4), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
     std::vector<int> pn, qn;
     ref_numbering(s, limQ, pn, qn);
     int m = 0;
@@ -1090,10 +1287,13 @@ extern "C" gbpf_status gbpf_newton_step(gbpf_solver *s, const double *V, const d
     s->launch_factor_solve(0);
     CK(cudaGetLastError());
     std::vector<double2> x(S.n);
+    std::vector<float2> x32(s->d.fp32 ? S.n : 0);
     Ctl c;
-    CK(cudaMemcpyAsync(x.data(), s->d.xs, S.n * sizeof(double2), cudaMemcpyDeviceToHost, s->stream));
+    if (s->d.fp32) CK(cudaMemcpyAsync(x32.data(), s->d.xs32, S.n * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
+    else CK(cudaMemcpyAsync(x.data(), s->d.xs, S.n * sizeof(double2), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(&c, s->d.ctl, sizeof c, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
+    for (size_t j = 0; j < x32.size(); j++) x[j] = make_double2(x32[j].x, x32[j].y);
     if (c.status == GBPF_E_SINGULAR) { set_error("singular Jacobian"); return GBPF_E_SINGULAR; }
     for (int j = 0; j < S.n; j++) {
         const int k = S.bus_of_blk[j];
