@@ -424,8 +424,9 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
                    "parallelism": f"scenarios sharded x{world}"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nb * 8 * 3,
                 "d2h_bytes_per_step": nb * 8 * 4 + N_SCEN * 20,
-                "note": "per step: Pliq, Qliq, Qload up (the grid's own starting state stays on the device while "
-                        "the instance layout is unchanged); V, theta, Pcalc, Qcalc and per-instance results down"},
+                "note": "per step: the caller's Pload, Qload, Pg arrays up as they are (packed into Pliq, Qliq, "
+                        "Qload on the device; the start is the grid's own, kept on the device), V, theta, Pcalc, "
+                        "Qcalc and the per-instance results down into the caller's arrays"},
         "roofline": {"bound": "hbm", "kernel": main_kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src_note(src),
                      "traffic": traffic / 1e9 if traffic else None, "traffic_unit": "GB per launch",

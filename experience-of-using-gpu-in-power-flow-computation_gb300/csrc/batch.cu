@@ -24,7 +24,6 @@
 #include <memory>
 #include <mutex>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include "blocks.cuh"
@@ -1464,28 +1463,37 @@ gbpf_status noalloc_setup(int device, void **out) {
 }
 }  // namespace
 
-// Runs f(begin, end) over [0, n) split across up to 16 host threads (the
-// calling thread takes the first range), each range at least `grain` long:
-// the packing of scenario inputs into the pinned staging buffer and the
-// copies of results out of it are memory-bound host loops over hundreds of MB.
-template <typename F> void host_parallel(size_t n, size_t grain, F f) {
-    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
-    const size_t t = std::min<size_t>(std::min<size_t>(hw, 16), std::max<size_t>(1, n / std::max<size_t>(grain, 1)));
-    if (t <= 1) { f((size_t)0, n); return; }
-    const size_t step = (n + t - 1) / t;
-    std::vector<std::thread> pool;
-    for (size_t i = 1; i < t; i++) {
-        const size_t b = i * step, e = std::min(n, b + step);
-        if (b < e) pool.emplace_back(f, b, e);
+// Inputs of every instance packed on the device: V0, theta0, Pliq = Pg - Pload,
+// Qliq = Qg - Qload and Qload, each bus from the caller's array when it was
+// given (raw[q], copied up as they are: Pload, Qload, Pg, Qg, V0, theta0) or
+// from its grid's own values (dflt, six arrays of nB per topology at
+// dflt_off[t]).  One warp per instance.
+struct PackArgs {
+    const double *raw[6];
+    const double *dflt;
+    const long long *dflt_off;
+    const Topo *topo;
+    const int *inst_topo;
+    const long long *inst_off;
+    int n_inst;
+    double *V0, *th0, *Pliq, *Qliq, *Qload;
+};
+__global__ void k_pack_inputs(PackArgs a) {
+    const int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (inst >= a.n_inst) return;
+    const int t = a.inst_topo[inst];
+    const int nB = a.topo[t].nB;
+    const long long o = a.inst_off[inst];
+    const double *d = a.dflt + a.dflt_off[t];
+    for (int k = lane; k < nB; k += 32) {
+        double v[6];
+        for (int q = 0; q < 6; q++) v[q] = a.raw[q] ? a.raw[q][o + k] : d[(size_t)q * nB + k];
+        a.Pliq[o + k] = v[2] - v[0];
+        a.Qliq[o + k] = v[3] - v[1];
+        a.Qload[o + k] = v[1];
+        a.V0[o + k] = v[4];
+        a.th0[o + k] = v[5];
     }
-    f((size_t)0, std::min(n, step));
-    for (auto &th : pool) th.join();
-}
-
-void par_memcpy(void *dst, const void *src, size_t bytes) {
-    host_parallel(bytes, (size_t)8 << 20, [&](size_t b, size_t e) {
-        std::memcpy((char *)dst + b, (const char *)src + b, e - b);
-    });
 }
 
 // ---------------------------------------------------------------------------
@@ -1520,8 +1528,10 @@ struct gbpf_batch {
     // events around each kernel of the captured graph (block, warp, hand-off)
     cudaEvent_t kev[6] = {};
     DevBuf topo_na;          // topologies planned for gbpf_batch_solve_noalloc
-    void *h_in = nullptr, *h_out = nullptr;  // pinned mirrors of the input and output regions
-    bool start_is_default = false;           // the device V0 / theta0 hold the grids' own start
+    DevBuf raw_mem;                          // the caller's input arrays as copied up (six of Σ nB)
+    DevBuf dflt_mem;                         // the grids' own bus values, six arrays of nB per topology
+    std::vector<long long> dflt_off;         // per topology, in doubles
+    DevBuf dflt_off_d;
     int flat_flag = 0;                       // host copy of the device flag behind Args::flat_on
     DevBuf flat_mem;                         // k_flat_start outputs, one FlatLayout per topology
     size_t out_bytes = 0;
@@ -1539,8 +1549,6 @@ struct gbpf_batch {
         for (auto &e : kev) if (e) cudaEventDestroy(e);
         if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
-        if (h_in) cudaFreeHost(h_in);
-        if (h_out) cudaFreeHost(h_out);
     }
     gbpf_status add_topology(const Grid &g);
     gbpf_status set_instances(int n, const int *topo_of_inst, const double *Pload, const double *Qload,
@@ -1731,10 +1739,9 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
                                       const double *Pg, const double *Qg, const double *V0, const double *th0) {
     for (int i = 0; i < n; i++)
         if (tofi[i] < 0 || tofi[i] >= (int)grids.size()) { set_error("instance names an unknown grid"); return GBPF_E_ARG; }
-    // the previous copies out of the pinned staging buffers must be complete
-    CK(cudaStreamSynchronize(stream));
     const bool same = exec && n == n_inst && std::equal(tofi, tofi + n, inst_topo.begin());
     if (!same) {
+        CK(cudaStreamSynchronize(stream));
         n_inst = n;
         inst_topo.assign(tofi, tofi + n);
         inst_off.resize(n);
@@ -1747,14 +1754,14 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
     }
     const size_t nb = (size_t)n_bus_total * 8, nba = align_up(nb, 256);
     if (!same) {
-        // inputs: V0, th0, Pliq, Qliq, Qload (packed, one region with a pinned
-        // mirror); outputs: V, th, P, Q + per-instance results (pinned mirror)
+        // inputs: V0, th0, Pliq, Qliq, Qload (packed, one device region) and
+        // the caller's raw arrays; outputs: V, th, P, Q + per-instance results
         inst_mem.reset();
         out_mem.reset();
-        if (h_in) { cudaFreeHost(h_in); h_in = nullptr; }
-        if (h_out) { cudaFreeHost(h_out); h_out = nullptr; }
+        raw_mem.reset();
         const size_t in_bytes = 5 * nba + align_up(4 * (size_t)n, 256) + align_up(8 * (size_t)n, 256);
         CK(cudaMalloc(&inst_mem.p, in_bytes));
+        CK(cudaMalloc(&raw_mem.p, 6 * nba));
         char *bb = (char *)inst_mem.p;
         size_t o = 0;
         auto take = [&](size_t bytes) { char *r = bb + o; o += align_up(bytes, 256); return r; };
@@ -1764,7 +1771,7 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
         args.inst_off = (long long *)take(8 * (size_t)n);
         CK(cudaMemcpyAsync((void *)args.inst_topo, inst_topo.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, stream));
         CK(cudaMemcpyAsync((void *)args.inst_off, inst_off.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, stream));
-        out_bytes = 4 * nba + 3 * align_up(4 * (size_t)n, 256) + align_up(8 * (size_t)n, 256);
+        const size_t out_bytes = 4 * nba + 3 * align_up(4 * (size_t)n, 256) + align_up(8 * (size_t)n, 256);
         const size_t ev_bytes = align_up(16 * (size_t)n * ev_cap, 256);
         CK(cudaMalloc(&out_mem.p, out_bytes + ev_bytes));
         bb = (char *)out_mem.p;
@@ -1774,48 +1781,38 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
         args.n_events = (int *)take(4 * (size_t)n); args.mism = (double *)take(8 * (size_t)n);
         args.events = (int *)take(16 * (size_t)n * ev_cap);
         args.n_inst = n;
-        CK(cudaMallocHost(&h_in, 5 * nba));
-        CK(cudaMallocHost(&h_out, out_bytes));
-    }
-    double *hV = (double *)h_in, *hT = (double *)((char *)h_in + nba), *hP = (double *)((char *)h_in + 2 * nba),
-           *hQ = (double *)((char *)h_in + 3 * nba), *hQl = (double *)((char *)h_in + 4 * nba);
-    // the grids' own starting state (no V0 / theta0 given) is copied once and
-    // stays on the device while the instance layout is unchanged
-    const bool dflt = !V0 && !th0, keep_start = same && dflt && start_is_default;
-    host_parallel((size_t)n, 1024, [&](size_t i0, size_t i1) {
-        for (size_t i = i0; i < i1; i++) {
-            const Grid &g = grids[inst_topo[i]];
-            const long long o = inst_off[i];
-            for (int k = 0; k < g.nB; k++) {
-                const double pl = Pload ? Pload[o + k] : g.Pload[k], ql = Qload ? Qload[o + k] : g.Qload[k];
-                const double pg = Pg ? Pg[o + k] : g.Pg[k], qg = Qg ? Qg[o + k] : g.Qg[k];
-                if (!keep_start) {
-                    hV[o + k] = V0 ? V0[o + k] : g.V0[k];
-                    hT[o + k] = th0 ? th0[o + k] : g.theta0[k];
-                }
-                hP[o + k] = pg - pl;
-                hQ[o + k] = qg - ql;
-                hQl[o + k] = ql;
-            }
-        }
-    });
-    // one host->device copy of the input region (without the starting state
-    // when it is already there)
-    if (keep_start)
-        CK(cudaMemcpyAsync((void *)args.Pliq, hP, 3 * nba, cudaMemcpyHostToDevice, stream));
-    else
-        CK(cudaMemcpyAsync((void *)args.V0, h_in, 5 * nba, cudaMemcpyHostToDevice, stream));
-    start_is_default = dflt;
-    if (!same) {
         CK(cudaStreamSynchronize(stream));
         if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
         if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
         const gbpf_status st = build_graph();
         if (st != GBPF_OK) return st;
     }
+    // the caller's arrays go up as they are (one copy each; on a GPU that
+    // reads pageable host memory through the host page tables, as GB300 does,
+    // at the rate of a pinned copy); the packing runs on the device
+    const double *user[6] = {Pload, Qload, Pg, Qg, V0, th0};
+    PackArgs pa{};
+    for (int q = 0; q < 6; q++) {
+        if (!user[q]) continue;
+        double *dst = (double *)((char *)raw_mem.p + q * nba);
+        CK(cudaMemcpyAsync(dst, user[q], nb, cudaMemcpyHostToDevice, stream));
+        pa.raw[q] = dst;
+    }
+    pa.dflt = (const double *)dflt_mem.p;
+    pa.dflt_off = (const long long *)dflt_off_d.p;
+    pa.topo = (const Topo *)topo_d.p;
+    pa.inst_topo = args.inst_topo;
+    pa.inst_off = args.inst_off;
+    pa.n_inst = n;
+    pa.V0 = (double *)args.V0; pa.th0 = (double *)args.th0; pa.Pliq = (double *)args.Pliq;
+    pa.Qliq = (double *)args.Qliq; pa.Qload = (double *)args.Qload;
+    k_pack_inputs<<<(unsigned)(((long long)n * 32 + 255) / 256), 256, 0, stream>>>(pa);
+    CK(cudaGetLastError());
     // instances from the grids' own start may take the shared iteration 0
-    flat_flag = dflt ? 1 : 0;
+    flat_flag = (!V0 && !th0) ? 1 : 0;
     CK(cudaMemcpyAsync((int *)counter.p + 8, &flat_flag, sizeof(int), cudaMemcpyHostToDevice, stream));
+    // the caller may reuse its arrays on return, pinned ones included
+    CK(cudaStreamSynchronize(stream));
     return GBPF_OK;
 }
 
@@ -2309,6 +2306,19 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
         gbpf_status st = b->add_topology(grids[i]->g);
         if (st != GBPF_OK) return st;
     }
+    {
+        // the grids' own bus values, for instances that do not give theirs
+        std::vector<double> dv;
+        for (const Grid &g : b->grids) {
+            b->dflt_off.push_back((long long)dv.size());
+            for (const std::vector<double> *v : {&g.Pload, &g.Qload, &g.Pg, &g.Qg, &g.V0, &g.theta0})
+                dv.insert(dv.end(), v->begin(), v->end());
+        }
+        CK(cudaMalloc(&b->dflt_mem.p, 8 * dv.size()));
+        CK(cudaMemcpy(b->dflt_mem.p, dv.data(), 8 * dv.size(), cudaMemcpyHostToDevice));
+        CK(cudaMalloc(&b->dflt_off_d.p, 8 * b->dflt_off.size()));
+        CK(cudaMemcpy(b->dflt_off_d.p, b->dflt_off.data(), 8 * b->dflt_off.size(), cudaMemcpyHostToDevice));
+    }
     // plan for the allocation-free entry point: blobs read from global memory,
     // factors in slices of the static scratch
     {
@@ -2451,26 +2461,24 @@ extern "C" gbpf_status gbpf_batch_time(gbpf_batch *b, int repeats, double *ms_to
 
 extern "C" gbpf_status gbpf_batch_results(gbpf_batch *b, int *iterations, int *status, double *final_mismatch,
                                           int *n_events, double *V, double *theta, double *Pcalc, double *Qcalc) {
-    ARGCHECK(b && b->n_inst > 0 && b->h_out);
+    ARGCHECK(b && b->n_inst > 0);
     CK(cudaSetDevice(b->device));
     const size_t n = b->n_inst, nb = (size_t)b->n_bus_total * 8;
-    const bool state = V || theta || Pcalc || Qcalc;
-    // one device->host copy into the pinned mirror: the whole output region,
-    // or only its per-instance tail when no state is wanted
-    const char *dev = (const char *)b->out_mem.p;
-    const size_t tail = (const char *)b->args.iters - dev;
-    if (state) CK(cudaMemcpyAsync(b->h_out, dev, b->out_bytes, cudaMemcpyDeviceToHost, b->stream));
-    else CK(cudaMemcpyAsync((char *)b->h_out + tail, dev + tail, b->out_bytes - tail, cudaMemcpyDeviceToHost, b->stream));
+    // straight into the caller's arrays, one copy each (no staging, no host copy)
+    auto down = [&](void *dst, const void *src, size_t bytes) -> gbpf_status {
+        if (dst) CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, b->stream));
+        return GBPF_OK;
+    };
+    gbpf_status st;
+    if ((st = down(iterations, b->args.iters, 4 * n)) != GBPF_OK) return st;
+    if ((st = down(status, b->args.status, 4 * n)) != GBPF_OK) return st;
+    if ((st = down(final_mismatch, b->args.mism, 8 * n)) != GBPF_OK) return st;
+    if ((st = down(n_events, b->args.n_events, 4 * n)) != GBPF_OK) return st;
+    if ((st = down(V, b->args.V, nb)) != GBPF_OK) return st;
+    if ((st = down(theta, b->args.th, nb)) != GBPF_OK) return st;
+    if ((st = down(Pcalc, b->args.P, nb)) != GBPF_OK) return st;
+    if ((st = down(Qcalc, b->args.Q, nb)) != GBPF_OK) return st;
     CK(cudaStreamSynchronize(b->stream));
-    auto host = [&](const void *d) { return (const char *)b->h_out + ((const char *)d - dev); };
-    if (iterations) std::memcpy(iterations, host(b->args.iters), 4 * n);
-    if (status) std::memcpy(status, host(b->args.status), 4 * n);
-    if (final_mismatch) std::memcpy(final_mismatch, host(b->args.mism), 8 * n);
-    if (n_events) std::memcpy(n_events, host(b->args.n_events), 4 * n);
-    if (V) par_memcpy(V, host(b->args.V), nb);
-    if (theta) par_memcpy(theta, host(b->args.th), nb);
-    if (Pcalc) par_memcpy(Pcalc, host(b->args.P), nb);
-    if (Qcalc) par_memcpy(Qcalc, host(b->args.Q), nb);
     return GBPF_OK;
 }
 

@@ -304,10 +304,11 @@ void gbpf_batch_free(gbpf_batch *b);
 
 /* Instances: grid_of_inst[i] picks the topology of instance i; the bus arrays
  * are packed in instance order (instance i occupies nB of its grid entries)
- * and may be NULL (= the grid's own values).  The arrays are packed into a
- * pinned staging buffer and copied to the device in one transfer (the caller
- * may reuse them on return).  Calling again with the same grid_of_inst only
- * replaces the inputs; a different list re-plans the launch. */
+ * and may be NULL (= the grid's own values).  Each given array is copied to
+ * the device as it is (one transfer) and the inputs are packed there; the
+ * caller may reuse the arrays on return.  Calling again with the same
+ * grid_of_inst only replaces the inputs; a different list re-plans the
+ * launch. */
 gbpf_status gbpf_batch_set_instances(gbpf_batch *b, int n_inst, const int *grid_of_inst,
                                      const double *Pload, const double *Qload, const double *Pg,
                                      const double *Qg, const double *V0, const double *theta0);
@@ -361,7 +362,8 @@ gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[9]);
 gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[16], float ms[2]);
 
 /* Per-instance results of the last batch solve (any pointer may be NULL);
- * V/theta/P/Q packed like the inputs. */
+ * V/theta/P/Q packed like the inputs.  Each array is copied from the device
+ * straight into the caller's memory (one transfer, no staging copy). */
 gbpf_status gbpf_batch_results(gbpf_batch *b, int *iterations, int *status, double *final_mismatch,
                                int *n_events, double *V, double *theta, double *Pcalc, double *Qcalc);
 
