@@ -688,7 +688,8 @@ def bench_single(a, gb, np, rank, dev, world, dist):
         achieved = 3 * N * N * 8 / t_it / 1e9
         top, prof = "dense fill + LU + solves", {"matrix_order": N, "iterations": first["iterations"],
                                                  "ms_per_iteration": 1e3 * t_it,
-                                                 "lu_fp64_gflops": (2 / 3 * N ** 3 + 2 * N * N) / t_it / 1e9}
+                                                 "lu_fp64_gflops": (2 / 3 * N ** 3 + 2 * N * N) / t_it / 1e9,
+                                                 "phases": s.profile(5)}
     else:
         prof = s.profile(10)
         top = max(prof, key=lambda k: prof[k]["ms"])

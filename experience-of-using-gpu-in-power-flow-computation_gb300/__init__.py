@@ -398,7 +398,10 @@ class Solver:
         ms = np.zeros(4)
         by = np.zeros(4, np.int64)
         _check(lib().gbpf_solver_profile(self.h, int(repeats), _p(ms), _p(by)), "gbpf_solver_profile")
-        names = ("injections_mismatch", "jacobian_fill", "factor_forward", "backward")
+        if int(self.options.metodo) == METODO["denso"]:
+            names = ("injections_mismatch", "dense_fill", "dense_lu", "dense_solve")
+        else:
+            names = ("injections_mismatch", "jacobian_fill", "factor_forward", "backward")
         return {k: dict(ms=float(m), bytes=int(b)) for k, m, b in zip(names, ms, by)}
 
     # kernel-level entry points

@@ -695,9 +695,19 @@ struct gbpf_solver {
     // metodo = denso: dense Jacobian, blocked LU with partial pivoting, the
     // triangular solves, update
     void launch_step_dense(int guard) {
+        const int T = 256;
+        launch_dense_fill(guard);
+        launch_dense_lu(guard);
+        launch_dense_solve(guard);
+        k_update<<<cdiv_int(S.n, T), T, 0, stream>>>(d, guard);
+    }
+    void launch_dense_fill(int guard) {
         const int T = 256, N = d.N;
         k_dzero<<<std::min(cdiv_int((long long)N * N / 2, T), 4096), T, 0, stream>>>(d, guard);
         k_dfill<<<cdiv_int(g.nB, T), T, 0, stream>>>(d, guard);
+    }
+    void launch_dense_lu(int guard) {
+        const int T = 256, N = d.N;
         for (int k0 = 0; k0 < N; k0 += kDPanel) {
             const int k1 = std::min(N, k0 + kDPanel);
             k_dpanel<<<1, kDPanelThreads, 0, stream>>>(d, k0, guard);
@@ -708,8 +718,9 @@ struct gbpf_solver {
                 k_dgemm<<<dim3(t, t), 256, 0, stream>>>(d, k0, guard);
             }
         }
-        k_dsolve<<<1, kDSolveThreads, (size_t)N * sizeof(double), stream>>>(d, guard);
-        k_update<<<cdiv_int(S.n, T), T, 0, stream>>>(d, guard);
+    }
+    void launch_dense_solve(int guard) {
+        k_dsolve<<<1, kDSolveThreads, (size_t)d.N * sizeof(double), stream>>>(d, guard);
     }
     void launch_eval(int guard) {  // injections, limits, mismatch
         const int T = 256;
@@ -1135,9 +1146,15 @@ extern "C" gbpf_status gbpf_solver_profile(gbpf_solver *s, int repeats, double m
     CK(cudaSetDevice(s->device));
     const Symbolic &S = s->S;
     const int T = 256, nq = S.n + 2 * S.nup;
+    const bool dense = s->d.dense_rule;
     auto phase = [&](int ph) {
         if (ph == 0) s->launch_eval(0);
-        else if (ph == 1) k_jfill<<<cdiv_int(nq, T), T, 0, s->stream>>>(s->d, 0);
+        else if (dense) {
+            // metodo = denso: dense fill, the blocked LU, the triangular solves
+            if (ph == 1) s->launch_dense_fill(0);
+            else if (ph == 2) s->launch_dense_lu(0);
+            else s->launch_dense_solve(0);
+        } else if (ph == 1) k_jfill<<<cdiv_int(nq, T), T, 0, s->stream>>>(s->d, 0);
         else if (ph == 2) s->launch_forward(0);
         else s->launch_backward(0);
     };
@@ -1154,15 +1171,28 @@ extern "C" gbpf_status gbpf_solver_profile(gbpf_solver *s, int repeats, double m
     }
     CK(cudaGetLastError());
     const long long nB = s->g.nB, nnzY = s->y.nnz, n = S.n, nup = S.nup, np = S.pairs();
+    // block and vector sizes of the factor's precision
+    const long long b4 = s->d.fp32 ? 16 : 32, b2 = s->d.fp32 ? 8 : 16;
     // injections: Y values + columns + row pointers, V/theta/phasors, P/Q out;
     // mismatch: Pliq/Qliq/act/QliqLim, rhs out
     bytes[0] = 16 * nnzY + 4 * nnzY + 4 * (nB + 1) + 8 * nB * 2 + 16 * nB + 16 * nB + 8 * nB * 4 + 4 * nB + 16 * n;
+    if (dense) {
+        const long long N = s->d.N;
+        // fill: the N x N matrix zeroed and written (Y values and bus state read)
+        bytes[1] = 8 * N * N + 16 * nnzY + 8 * nB * 5;
+        // blocked LU: each element read and written once by the panel sweep
+        // (lower bound), pivots
+        bytes[2] = 16 * N * N + 4 * N;
+        // triangular solves: the factor read once, rhs and x
+        bytes[3] = 8 * N * N + 8 * N * 2 + 4 * N;
+        return GBPF_OK;
+    }
     // fill: map (3 ints per block), Y values, bus state, blocks out
-    bytes[1] = 12LL * nq + 16 * nnzY + 8 * nB * 5 + 4 * nB + 32LL * nq;
+    bytes[1] = 12LL * nq + 16 * nnzY + 8 * nB * 5 + 4 * nB + b4 * nq;
     // factor + forward: blocks in/out, diagonal inverses, gather lists, rhs, y
-    bytes[2] = 64LL * nq + 32 * n + 4 * (n + 1) + 8 * nup + 4 * (nup + 1) + 8 * (nup + 1) + 8 * np + 16 * n * 2 + 4 * n;
+    bytes[2] = 2 * b4 * nq + b4 * n + 4 * (n + 1) + 8 * nup + 4 * (nup + 1) + 8 * (nup + 1) + 8 * np + (16 + b2) * n + 4 * n;
     // backward: U blocks, inverses, columns, y in, x out
-    bytes[3] = 32LL * nup + 32 * n + 4 * (n + 1) + 4 * nup + 16 * n * 2 + 4 * n;
+    bytes[3] = b4 * nup + b4 * n + 4 * (n + 1) + 4 * nup + 2 * b2 * n + 4 * n;
     return GBPF_OK;
 }
 

@@ -258,7 +258,9 @@ gbpf_status gbpf_solver_setup_times(const gbpf_solver *s, double ms[5]);
  * last solve's state left on the device, `repeats` passes after one warm-up):
  * [0] injections + limits + mismatch, [1] Jacobian fill, [2] LU
  * factorisation fused with forward substitution (all levels), [3] backward
- * substitution (all levels); bytes[] = algorithmic bytes of one pass. */
+ * substitution (all levels); with metodo = denso [1] the dense fill, [2] the
+ * blocked LU, [3] the triangular solves.  bytes[] = algorithmic bytes of one
+ * pass (in the factor's precision). */
 gbpf_status gbpf_solver_profile(gbpf_solver *s, int repeats, double ms[4], long long bytes[4]);
 
 /* ------------------------------------------------------------------------ */
