@@ -136,6 +136,89 @@ __global__ void __launch_bounds__(kDPanelThreads) k_dpanel(Dev d, int k0, int gu
     }
 }
 
+// The same panel factorisation with the panel (rows k0 .. N-1 of its nb
+// columns) in shared memory and one thread per panel row: the pivot search is
+// an argmax on the integer order of |a| (NaN counted as +inf, the first row of
+// the largest magnitude wins, as idamax), the interchange and the broadcast of
+// the pivot row go through one shared buffer, and each thread scales and
+// updates its own row with the pivot's reciprocal (as LAPACK's dgetf2 does for
+// pivots above the underflow threshold).  Two barriers per column instead of
+// four and no FP64 compares.  For panels of at most kDPanelSmemRows rows;
+// dynamic shared memory (rows + 1) x nb doubles.
+constexpr int kDPanelSmemRows = 832;
+__device__ __forceinline__ unsigned long long dabs_key(double v) {
+    unsigned long long k = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    return k > 0x7ff0000000000000ull ? 0x7ff0000000000000ull : k;  // NaN -> +inf
+}
+__global__ void __launch_bounds__(kDPanelThreads) k_dpanel_smem(Dev d, int k0, int guard) {
+    if (stopped(d, guard)) return;
+    extern __shared__ double P[];  // column-major, leading dimension R; then the pivot row (nb)
+    __shared__ unsigned long long skey[kDPanelThreads / 32];
+    __shared__ int sidx[kDPanelThreads / 32];
+    __shared__ int spiv;
+    const int N = d.N, R = N - k0, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nb = min(kDPanel, R);
+    double *A = d.A, *prow = P + (size_t)R * nb;
+    for (int i = tid; i < R * nb; i += kDPanelThreads) {
+        const int c = i / R, r = i - c * R;
+        P[i] = A[(size_t)(k0 + c) * N + k0 + r];
+    }
+    __syncthreads();
+    for (int jj = 0; jj < nb; jj++) {
+        // argmax over rows jj..R-1 of column jj
+        unsigned long long key = 0;
+        int bi = R;
+        for (int r = jj + tid; r < R; r += kDPanelThreads) {
+            const unsigned long long k = dabs_key(P[(size_t)jj * R + r]);
+            if (bi == R || k > key) { key = k; bi = r; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (oi < R && (bi == R || ok > key || (ok == key && oi < bi))) { key = ok; bi = oi; }
+        }
+        if (lane == 0) { skey[warp] = key; sidx[warp] = bi; }
+        __syncthreads();
+        if (warp == 0) {
+            key = lane < kDPanelThreads / 32 ? skey[lane] : 0;
+            bi = lane < kDPanelThreads / 32 ? sidx[lane] : R;
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (oi < R && (bi == R || ok > key || (ok == key && oi < bi))) { key = ok; bi = oi; }
+            }
+            if (lane == 0) {
+                int p = bi;
+                if (p >= R || key == 0 || key >= 0x7ff0000000000000ull) {
+                    d.ctl->status = GBPF_E_SINGULAR;
+                    d.ctl->done = 1;
+                    p = jj;
+                }
+                d.ipiv[k0 + jj] = k0 + p;
+                spiv = p;
+            }
+        }
+        // the pivot row into the shared buffer (row p: it becomes row jj)
+        __syncthreads();
+        const int p = spiv;
+        if (tid < nb) prow[tid] = P[(size_t)tid * R + p];
+        if (p != jj && tid < nb) P[(size_t)tid * R + p] = P[(size_t)tid * R + jj];
+        __syncthreads();
+        if (tid < nb) P[(size_t)tid * R + jj] = prow[tid];
+        const double inv = 1.0 / prow[jj];
+        for (int r = jj + 1 + tid; r < R; r += kDPanelThreads) {
+            const double l = P[(size_t)jj * R + r] * inv;
+            P[(size_t)jj * R + r] = l;
+            for (int c = jj + 1; c < nb; c++) P[(size_t)c * R + r] -= l * prow[c];
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < R * nb; i += kDPanelThreads) {
+        const int c = i / R, r = i - c * R;
+        A[(size_t)(k0 + c) * N + k0 + r] = P[i];
+    }
+}
+
 // The panel's interchanges (in order) on every column outside the panel.
 __global__ void k_dlaswp(Dev d, int k0, int guard) {
     if (stopped(d, guard)) return;

@@ -710,7 +710,12 @@ struct gbpf_solver {
         const int T = 256, N = d.N;
         for (int k0 = 0; k0 < N; k0 += kDPanel) {
             const int k1 = std::min(N, k0 + kDPanel);
-            k_dpanel<<<1, kDPanelThreads, 0, stream>>>(d, k0, guard);
+            if (N - k0 <= kDPanelSmemRows)
+                k_dpanel_smem<<<1, kDPanelThreads,
+                                (size_t)(N - k0 + 1) * std::min(kDPanel, N - k0) * sizeof(double), stream>>>(d, k0,
+                                                                                                           guard);
+            else
+                k_dpanel<<<1, kDPanelThreads, 0, stream>>>(d, k0, guard);
             k_dlaswp<<<cdiv_int(N, T), T, 0, stream>>>(d, k0, guard);
             if (k1 < N) {
                 k_dtrsm<<<cdiv_int(N - k1, 128), 128, 0, stream>>>(d, k0, guard);
@@ -928,8 +933,11 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
 }
 
 gbpf_status gbpf_solver::build_graph() {
-    if (d.dense_rule)
+    if (d.dense_rule) {
         CK(cudaFuncSetAttribute(k_dsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, d.N * (int)sizeof(double)));
+        CK(cudaFuncSetAttribute(k_dpanel_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (kDPanelSmemRows + 1) * kDPanel * (int)sizeof(double)));
+    }
     CK(cudaGraphCreate(&graph, 0));
     cudaGraphConditionalHandle h;
     CK(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault));
