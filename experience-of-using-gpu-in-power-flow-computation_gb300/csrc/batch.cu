@@ -1527,14 +1527,13 @@ struct gbpf_batch {
     cudaEvent_t fork = nullptr, join = nullptr;
     // events around each kernel of the captured graph (block, warp, hand-off)
     cudaEvent_t kev[6] = {};
-    DevBuf topo_na;          // topologies planned for gbpf_batch_solve_noalloc
-    DevBuf raw_mem;                          // the caller's input arrays as copied up (six of Σ nB)
-    DevBuf dflt_mem;                         // the grids' own bus values, six arrays of nB per topology
-    std::vector<long long> dflt_off;         // per topology, in doubles
+    DevBuf topo_na;                   // topologies planned for gbpf_batch_solve_noalloc
+    DevBuf raw_mem;                   // the caller's input arrays as copied up (six of Σ nB)
+    DevBuf dflt_mem;                  // the grids' own bus values, six arrays of nB per topology
+    std::vector<long long> dflt_off;  // per topology, in doubles
     DevBuf dflt_off_d;
-    int flat_flag = 0;                       // host copy of the device flag behind Args::flat_on
-    DevBuf flat_mem;                         // k_flat_start outputs, one FlatLayout per topology
-    size_t out_bytes = 0;
+    int flat_flag = 0;                // host copy of the device flag behind Args::flat_on
+    DevBuf flat_mem;                  // k_flat_start outputs, one FlatLayout per topology
     size_t na_smem = 0, na_stride = 0;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;

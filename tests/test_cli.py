@@ -96,3 +96,40 @@ def test_cli_benchmark_csv_and_report(gb, tmp_path):
         for x in f[2:3] + f[4:17]:
             assert "," in x and "." not in x
             assert float(x.replace(",", ".")) >= 0
+
+
+def test_cli_matpower_input(gb, tmp_path):
+    """arq_entrada naming a MATPOWER case: same lines and table as for the
+    golden solve of the reference's own reader (m_edge.m, limits on: five
+    switch events)."""
+    m = "m_edge.m"
+    gold = load_golden("m_edge_lim1.json")
+    shutil.copy(os.path.join(GOLDEN, m), tmp_path / m)
+    (tmp_path / "data.txt").write_text(DATA.format(metodo="esparso", cdf=m))
+    out = subprocess.run([gb.CLI_PATH], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.splitlines()
+    barra = [l for l in lines if l.startswith("Barra ")]
+    assert barra == [f"Barra {b} [{i}]: {EVENT_TEXT[c]}" for (_, b, i, c) in gold["events"]]
+    assert len([l for l in lines if l.startswith("max(g) = ")]) == gold["iterations"] + 1
+    start = lines.index("                                 FLUXOS DE POTENCIA")
+    rows = [l for l in lines[start + 2:] if len(l) > 80 and l[6:10].strip().isdigit()]
+    assert len(rows) == gold["nB"]
+    V = np.array([float(r[10:21]) for r in rows])
+    assert np.max(np.abs(V - np.array(gold["V"]))) <= 6e-6
+
+
+def test_cli_fp32_lu_key(gb, tmp_path):
+    """precisao = FP32 (the one added data.txt key) runs the single-grid
+    solver's FP32-LU form: converged, same table within the print precision."""
+    cdf = "c2_s3.cdf"
+    gold = load_golden("c2_s3_lim1.json")
+    shutil.copy(os.path.join(GOLDEN, cdf), tmp_path / cdf)
+    (tmp_path / "data.txt").write_text(DATA.format(metodo="esparso", cdf=cdf) + "precisao       = FP32;\n")
+    out = subprocess.run([gb.CLI_PATH], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.splitlines()
+    start = lines.index("                                 FLUXOS DE POTENCIA")
+    rows = [l for l in lines[start + 2:] if len(l) > 80 and l[6:10].strip().isdigit()]
+    V = np.array([float(r[10:21]) for r in rows])
+    assert np.max(np.abs(V - np.array(gold["V"]))) <= 6e-6
