@@ -344,33 +344,58 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     r = fast.results(state=False)
     conv = int((r["status"] == 0).sum())
     assert np.all(r["final_mismatch"][r["status"] == 0] <= 1e-8)
-    # device-resident: CUDA events on the batch stream
+    # a second batch of the same scenarios and plan: two batches in flight, so
+    # that one step's hand-off tail (the few scenarios that run all
+    # no_max_iter iterations on a few SMs) runs beside the next step's bulk
+    twin = gb.Batch(grids, device=dev, precision=gb.PREC_FP32_IR, **opts)
+    twin.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
+    pl = fast.plan()
+    twin.set_plan(**{k: pl[k] for k in ("warp_mode", "warps_per_block", "handoff_it", "resume_group",
+                                        "warp_group", "narrow", "lu1", "warp_lu1", "flat_shared")})
+    twin.solve()
+    assert np.array_equal(twin.results(state=False)["status"], r["status"])
+    pair = [fast, twin]
+    # device-resident: CUDA events on the batch streams; every step is a full
+    # solve of all scenarios, steps alternate between the two batches
+    gb.time_pipelined(pair, max(3, a.warmup))
     fast.time(max(3, a.warmup))
     if dist:
         dist.barrier()
     with Clocks(dev) as clk:
-        ms = fast.time(a.steps)
+        ms = gb.time_pipelined(pair, a.steps)
     if dist:
         dist.barrier()
+    ms_serial = fast.time(a.steps)
     t_dev = max_over_ranks(ms / 1e3, dist, dev)
     total_conv = sum_over_ranks(conv, dist, dev)
     value = total_conv * a.steps / t_dev
-    # end to end: host buffers through the API every step
+    serial = total_conv * a.steps / max_over_ranks(ms_serial / 1e3, dist, dev)
+    # end to end: host arrays through the API every step (inputs up, solve,
+    # results down into host arrays), double-buffered: step k's inputs go up
+    # and its solve is launched before step k-1's results are read back
     nb = len(Pl)
-    res = None
-    for _ in range(max(3, a.warmup)):
-        fast.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
-        fast.solve()
-        res = fast.results(state=True, out=res)
+    outs = [None, None]
+
+    def e2e_steps(k):
+        for i in range(k):
+            b = pair[i % 2]
+            b.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
+            b.launch()
+            if i >= 1:
+                j = (i - 1) % 2
+                outs[j] = pair[j].results(state=True, out=outs[j])
+        j = (k - 1) % 2
+        outs[j] = pair[j].results(state=True, out=outs[j])
+
+    e2e_steps(max(3, a.warmup))
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
-    for _ in range(a.steps):
-        fast.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
-        fast.solve()
-        res = fast.results(state=True, out=res)
+    e2e_steps(a.steps)
     t_e2e = max_over_ranks(time.perf_counter() - t0, dist, dev)
     e2e = total_conv * a.steps / t_e2e
+    res = outs[(a.steps - 1) % 2]
+    assert np.array_equal(res["iterations"], r["iterations"])
     # the plain FP64 form (one scenario per gbpf_solve) and batched FP64, same scenarios
     plain = None
     if cdf is not None:
@@ -418,6 +443,9 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
                    "max_iterations": int(np.max(r["iterations"])),
                    "plain_fp64_solves_per_s": plain, "batched_fp64_solves_per_s": batched64,
                    "speedup_vs_plain_fp64": (value / plain) if plain else None,
+                   "in_flight": "2 batches of the same scenarios on two streams, steps alternating; each step a full "
+                                "solve of every scenario",
+                   "serial_solves_per_s": serial,
                    "l2": (f"inputs+outputs {nb * 8 * 9 / 2**20:.0f} MiB > L2 (129 MB)" if nb * 72 > L2_BYTES else
                           f"inputs+outputs {nb * 8 * 9 / 2**20:.1f} MiB < L2; no flush"),
                    "batch": info, "plan": fast.plan(), "autotune": tune,
@@ -426,7 +454,8 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
                 "d2h_bytes_per_step": nb * 8 * 4 + N_SCEN * 20,
                 "note": "per step: the caller's Pload, Qload, Pg arrays up as they are (packed into Pliq, Qliq, "
                         "Qload on the device; the start is the grid's own, kept on the device), V, theta, Pcalc, "
-                        "Qcalc and the per-instance results down into the caller's arrays"},
+                        "Qcalc and the per-instance results down into the caller's arrays; double-buffered (step "
+                        "k is launched before step k-1's results are read)"},
         "roofline": {"bound": "hbm", "kernel": main_kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src_note(src),
                      "traffic": traffic / 1e9 if traffic else None, "traffic_unit": "GB per launch",

@@ -45,6 +45,7 @@ EXPORTS = [
     "gbpf_batch_solve_warm", "gbpf_mlp_set_loss_metric", "gbpf_solver_setup_times", "gbpf_batch_kernel_times",
     "gbpf_grid_write_m", "gbpf_grid_ybus_form", "gbpf_grid_set_ybus_form",
     "gbpf_batch_get_plan", "gbpf_batch_set_plan", "gbpf_batch_autotune",
+    "gbpf_batch_launch", "gbpf_batch_wait", "gbpf_batch_time_pipelined",
 ]
 
 
@@ -241,6 +242,16 @@ class Grid:
 
     def set_ybus_form(self, form):
         _check(lib().gbpf_grid_set_ybus_form(self.h, int(form)), "gbpf_grid_set_ybus_form")
+
+
+def time_pipelined(batches, steps):
+    """gbpf_batch_time_pipelined: device ms of `steps` solves spread
+    round-robin over the batches, each on its own stream."""
+    arr = (ctypes.c_void_p * len(batches))(*[b.h.value for b in batches])
+    ms = ctypes.c_double()
+    _check(lib().gbpf_batch_time_pipelined(arr, len(batches), int(steps), ctypes.byref(ms)),
+           "gbpf_batch_time_pipelined")
+    return ms.value
 
 
 def read_grid(path, v_inicial=1.0, theta_inicial=0.0):
@@ -488,6 +499,13 @@ class Batch:
 
     def solve(self):
         _check(lib().gbpf_batch_solve(self.h), "gbpf_batch_solve")
+
+    def launch(self):
+        """gbpf_batch_launch: the solve without waiting for it."""
+        _check(lib().gbpf_batch_launch(self.h), "gbpf_batch_launch")
+
+    def wait(self):
+        _check(lib().gbpf_batch_wait(self.h), "gbpf_batch_wait")
 
     def time(self, repeats):
         ms = ctypes.c_double()

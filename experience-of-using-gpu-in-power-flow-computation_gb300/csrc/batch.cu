@@ -2445,6 +2445,46 @@ extern "C" gbpf_status gbpf_batch_solve(gbpf_batch *b) {
     return GBPF_OK;
 }
 
+extern "C" gbpf_status gbpf_batch_launch(gbpf_batch *b) {
+    ARGCHECK(b && b->exec);
+    CK(cudaSetDevice(b->device));
+    CK(cudaGraphLaunch(b->exec, b->stream));
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_batch_wait(gbpf_batch *b) {
+    ARGCHECK(b);
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamSynchronize(b->stream));
+    return GBPF_OK;
+}
+
+// `steps` solves spread round-robin over the batches (each on its own
+// stream, so one batch's hand-off tail runs beside the next batch's bulk),
+// timed with CUDA events: a start event on the first batch's stream that
+// every other stream waits for, an end event on each stream, the longest
+// span.  All batches must live on one device.
+extern "C" gbpf_status gbpf_batch_time_pipelined(gbpf_batch *const *bs, int n, int steps, double *ms) {
+    ARGCHECK(bs && n > 0 && steps > 0 && ms);
+    for (int i = 0; i < n; i++) ARGCHECK(bs[i] && bs[i]->exec && bs[i]->device == bs[0]->device);
+    CK(cudaSetDevice(bs[0]->device));
+    for (int i = 0; i < n; i++) CK(cudaStreamSynchronize(bs[i]->stream));
+    cudaEvent_t start = bs[0]->ev0;
+    CK(cudaEventRecord(start, bs[0]->stream));
+    for (int i = 1; i < n; i++) CK(cudaStreamWaitEvent(bs[i]->stream, start, 0));
+    for (int k = 0; k < steps; k++) CK(cudaGraphLaunch(bs[k % n]->exec, bs[k % n]->stream));
+    float worst = 0;
+    for (int i = 0; i < n && i < steps; i++) {
+        CK(cudaEventRecord(bs[i]->ev1, bs[i]->stream));
+        CK(cudaEventSynchronize(bs[i]->ev1));
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, start, bs[i]->ev1));
+        worst = std::max(worst, t);
+    }
+    *ms = worst;
+    return GBPF_OK;
+}
+
 extern "C" gbpf_status gbpf_batch_time(gbpf_batch *b, int repeats, double *ms_total) {
     ARGCHECK(b && b->exec && repeats > 0 && ms_total);
     CK(cudaSetDevice(b->device));

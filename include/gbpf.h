@@ -319,6 +319,19 @@ gbpf_status gbpf_batch_set_instances(gbpf_batch *b, int n_inst, const int *grid_
  * persistent kernel, one thread block per instance at a time). */
 gbpf_status gbpf_batch_solve(gbpf_batch *b);
 
+/* The solve of gbpf_batch_solve without the wait: the graph is launched on
+ * the batch's stream and the call returns.  gbpf_batch_wait waits for it.
+ * Calls on one batch are ordered (set_instances and results wait for the
+ * batch's earlier work); two batches in flight on their own streams let one
+ * batch's bulk run beside the other's tail and its copies. */
+gbpf_status gbpf_batch_launch(gbpf_batch *b);
+gbpf_status gbpf_batch_wait(gbpf_batch *b);
+
+/* `steps` solves spread round-robin over n batches, each on its own stream;
+ * *ms = device ms from a common start event to the last batch's end (CUDA
+ * events).  All batches on one device. */
+gbpf_status gbpf_batch_time_pipelined(gbpf_batch *const *bs, int n, int steps, double *ms);
+
 /* `repeats` batch solves back to back on the batch stream; device ms. */
 gbpf_status gbpf_batch_time(gbpf_batch *b, int repeats, double *ms_total);
 

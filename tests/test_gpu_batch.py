@@ -307,3 +307,32 @@ def test_batch_shared_flat_start_is_exact(gb, precision):
             assert out[0][k] == out[1][k]
         else:
             np.testing.assert_array_equal(out[0][k], out[1][k], err_msg=k)
+
+
+def test_two_batches_in_flight(gb):
+    """gbpf_batch_launch on two batches (own streams, overlapping on the GPU)
+    gives each batch the results of a plain solve; time_pipelined runs."""
+    path = os.path.join(GOLDEN, "c2_s8.cdf")
+    g = gb.read_grid(path)
+    base = g.buses()
+    rng = np.random.default_rng(21)
+    n = 256
+    lf = np.exp(rng.normal(0, 0.1, (n, g.nB)))
+    Pl, Ql = (base["Pload"] * lf).ravel(), (base["Qload"] * lf).ravel()
+    gi = np.zeros(n, np.int32)
+    ref = gb.Batch([g], tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1)
+    ref.set_instances(gi, Pload=Pl, Qload=Ql)
+    ref.solve()
+    want = ref.results()
+    pair = [gb.Batch([g], tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1) for _ in range(2)]
+    for b in pair:
+        b.set_instances(gi, Pload=Pl, Qload=Ql)
+    for _ in range(3):
+        for b in pair:
+            b.launch()
+    for b in pair:
+        b.wait()
+        got = b.results()
+        for k in ("iterations", "status", "V", "theta"):
+            np.testing.assert_array_equal(got[k], want[k], err_msg=k)
+    assert gb.time_pipelined(pair, 4) > 0
