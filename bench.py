@@ -5,15 +5,19 @@ Workload c2 (default): the seeded synthetic 118-bus meshed grid (1 slack, 53 PV,
 64 PQ, 177 lines + 9 transformers), 32,768 load scenarios (per-bus load x
 lognormal(sigma 0.1), generator P x U(0.9, 1.1)), reactive limits on, flat start,
 tolerance 1e-8 p.u., no_max_iter 100.  A step solves all 32,768 scenarios.  About
-one scenario in 2,000 never converges (the PV/PQ switching cycles) and runs all
-100 iterations, which bounds the time of any batch from below; a larger batch
-amortises that tail.
+one scenario in 1,100 never converges (Newton oscillates or PV/PQ-cycles) and
+runs all 100 iterations on a few SMs at the end of the step; two batches of the
+same scenarios are kept in flight on two streams, steps alternating between
+them, so that one step's tail runs beside the next step's bulk.
   value    batched, FP32 LU + FP64 mismatch/test/update, inputs resident in
            device memory; one graph launch per step, CUDA events on the batch
-           stream; counts converged scenarios only
-  e2e      the same through the public API with host buffers: host->device copy
-           of every scenario's injections and start, the solve, device->host copy
-           of |V|, theta, iterations and status, every step
+           streams; counts converged scenarios only (config.serial_solves_per_s:
+           one batch, step after step)
+  e2e      the same through the public API with host arrays: host->device copy
+           of every scenario's loads and generation, the solve, device->host
+           copy of |V|, theta, P, Q, iterations and status, every step
+           (double-buffered: step k is launched before step k-1's results are
+           read back)
   config   also reports the plain FP64 form (one scenario per gbpf_solve, the
            oracle-matching path) and batched FP64 on the same scenarios
 Other workloads: c2-plain (one FP64 solve of the grid per step), c3 (the
@@ -27,7 +31,7 @@ fallback, over 8,192 held-out scenarios).
   python bench.py --impl reference     the CPU restatement of the reference
                                        path (oracle/) on every host core
 Multi-GPU (torch.distributed.run, one process per GPU): scenarios are sharded
-over ranks (weak scaling: every rank solves its own 4,096), no collective in
+over ranks (weak scaling: every rank solves its own 32,768), no collective in
 the data path; a single grid does not shard, so c2-plain/c3 run replicas.
 """
 import argparse
