@@ -200,6 +200,9 @@ struct Args {
     // warp kernel: nonzero *flat_on = every instance starts from its grid's own
     // starting state, so iteration 0 takes Topo::flat (null: never)
     const int *flat_on;
+    // FP32-LU form: 1 = phasors rotated by the Newton step in the update
+    // (rotate_phasor), 0 = a full sincos of the new angles each iteration
+    int rotate;
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
@@ -763,7 +766,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
         for (;;) {
             // phasors (the FP32-LU form rotates them in the update after the
             // first pass) and injections
-            if (sizeof(TJ) == 8 || fresh)
+            if (sizeof(TJ) == 8 || fresh || !a.rotate)
                 for (int k = tid; k < nB; k += kThreads) {
                     double s, c;
                     sincos(th[k], &s, &c);
@@ -940,7 +943,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
                 const double dt = (double)ys[j].x, dv = (double)ys[j].y;
                 th[k] += dt;
                 if (act[k]) V[k] += dv;
-                if (sizeof(TJ) == 4) {
+                if (sizeof(TJ) == 4 && a.rotate) {
                     double c = cs[k], s = sn[k];
                     rotate_phasor(th[k], dt, c, s);
                     cs[k] = c;
@@ -1103,7 +1106,7 @@ __global__ void __launch_bounds__(32 * kWarpsMax, 1) k_nr_warp(Args a) {
                     Q[k] = ((const double *)(flat + F.Q))[k];
                 }
             } else {
-                if (sizeof(TJ) == 8 || it == 0)
+                if (sizeof(TJ) == 8 || it == 0 || !a.rotate)
                     for (int k = lane; k < nB; k += 32) phasor<TJ>(k, th, V, cs, sn, ef, f32);
                 __syncwarp();
                 for (int k = lane; k < nB; k += 32) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
@@ -1202,7 +1205,7 @@ __global__ void __launch_bounds__(32 * kWarpsMax, 1) k_nr_warp(Args a) {
                 const double dt = (double)ys[j].x, dv = (double)ys[j].y;
                 th[k] += dt;
                 if (act[k]) V[k] += dv;
-                if (sizeof(TJ) == 4) {
+                if (sizeof(TJ) == 4 && a.rotate) {
                     double c = cs[k], s = sn[k];
                     rotate_phasor(th[k], dt, c, s);
                     cs[k] = c;
@@ -1562,10 +1565,12 @@ struct gbpf_batch {
     // warp_lu1 = 1 factor in one pass per elimination level in the block
     // kernel (block mode and hand-off) / in the warp kernel; flat_shared = 1
     // lets the warp kernel's instances take the shared iteration 0 of their
-    // topology when they start from the grid's own state (k_flat_start).
+    // topology when they start from the grid's own state (k_flat_start);
+    // rotate = 1 updates the FP32-LU form's phasors by rotation instead of a
+    // sincos per iteration (measured slower on GB300, kept as a knob).
     struct Plan {
         int warp_mode = 1, warp_warps = 8, handoff_it = kHandoffIt, resume_group = 1, warp_group = 1, narrow = 0,
-            lu1 = 1, warp_lu1 = 0, flat_shared = 1;
+            lu1 = 1, warp_lu1 = 0, flat_shared = 1, rotate = 0;
     } plan;
     gbpf_status rebuild() {
         CK(cudaStreamSynchronize(stream));
@@ -1843,6 +1848,7 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
             ra.no_group = plan.resume_group ? 0 : 1;
             ra.narrow = plan.narrow;
             ra.lu1 = plan.lu1;
+            ra.rotate = plan.rotate;
             ra.queue = wa.handoff_q;
             ra.counter = args.counter + 2;
             ra.topo = (const Topo *)topo_resume.p;
@@ -2034,6 +2040,7 @@ gbpf_status gbpf_batch::build_graph() {
     args.narrow = plan.narrow;
     args.lu1 = plan.lu1;
     wargs.lu1 = plan.warp_lu1;
+    args.rotate = wargs.rotate = plan.rotate;
     handoff.reset();
     topo_resume.reset();
     wargs.handoff_it = 0;
@@ -2186,6 +2193,7 @@ gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
         {&Plan::lu1, {1, 0}, false, false},
         {&Plan::warp_lu1, {0, 1}, true, false},
         {&Plan::flat_shared, {1, 0}, true, false},
+        {&Plan::rotate, {0, 1}, false, false},
     };
     for (int sweep = 0; sweep < 2; sweep++) {
         bool changed = false;
@@ -2222,10 +2230,11 @@ static void plan_out(const gbpf_batch *b, int plan[16]) {
     plan[6] = b->plan.lu1;
     plan[7] = b->plan.warp_lu1;
     plan[8] = b->plan.flat_shared;
-    plan[9] = b->warp_warps;  // warps per block in use
-    plan[10] = b->n_warp_q;
-    plan[11] = b->n_block_q;
-    for (int i = 12; i < 16; i++) plan[i] = 0;
+    plan[9] = b->plan.rotate;
+    plan[10] = b->warp_warps;  // warps per block in use
+    plan[11] = b->n_warp_q;
+    plan[12] = b->n_block_q;
+    for (int i = 13; i < 16; i++) plan[i] = 0;
 }
 
 extern "C" gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[16]) {
@@ -2234,10 +2243,11 @@ extern "C" gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[16]) {
     return GBPF_OK;
 }
 
-extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[9]) {
+extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[10]) {
     ARGCHECK(b && plan && (plan[0] == 0 || plan[0] == 1) && plan[1] >= 0 && plan[1] <= kWarpsMax && plan[2] >= 0 &&
              (plan[3] == 0 || plan[3] == 1) && (plan[4] == 0 || plan[4] == 1) && (plan[5] == 0 || plan[5] == 1) &&
-             (plan[6] == 0 || plan[6] == 1) && (plan[7] == 0 || plan[7] == 1) && (plan[8] == 0 || plan[8] == 1));
+             (plan[6] == 0 || plan[6] == 1) && (plan[7] == 0 || plan[7] == 1) && (plan[8] == 0 || plan[8] == 1) &&
+             (plan[9] == 0 || plan[9] == 1));
     CK(cudaSetDevice(b->device));
     b->plan.warp_mode = plan[0];
     b->plan.warp_warps = plan[1];
@@ -2248,6 +2258,7 @@ extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[9]) {
     b->plan.lu1 = plan[6];
     b->plan.warp_lu1 = plan[7];
     b->plan.flat_shared = plan[8];
+    b->plan.rotate = plan[9];
     if (!b->n_inst) return GBPF_OK;
     return b->rebuild();
 }

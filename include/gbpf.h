@@ -359,14 +359,16 @@ gbpf_status gbpf_batch_kernel_times(gbpf_batch *b, int repeats, double ms[3]);
  * on warps that start from their grid's own starting state (no V0 / theta0
  * given) take iteration 0 -- phasors, injections and the factored Jacobian,
  * which depend on the topology and the start only -- from one computation per
- * topology, and do only their own substitutions in it.  get_plan also
- * returns plan[9] warps per block in use, plan[10] instances on warps,
- * plan[11] instances on blocks (plan[12..15] = 0).  Setting a plan rebuilds
- * the batch graph. */
+ * topology, and do only their own substitutions in it; plan[9] 1 = the
+ * FP32-LU form updates its phasors by rotating them through the Newton step
+ * instead of a sincos of every angle each iteration (0, the default, measured
+ * faster on GB300).  get_plan also returns plan[10] warps per block in use,
+ * plan[11] instances on warps, plan[12] instances on blocks (plan[13..15] =
+ * 0).  Setting a plan rebuilds the batch graph. */
 gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[16]);
-gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[9]);
+gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[10]);
 
-/* Autotuner: a coordinate search over plan[0..8] on the current instances,
+/* Autotuner: a coordinate search over plan[0..9] on the current instances,
  * from the default plan.  Each knob takes each of its values in turn with the
  * others fixed; a value is kept when the whole batch solve (best of `repeats`
  * timed graph launches after one warm-up, CUDA events on the batch stream) is

@@ -85,13 +85,17 @@ def test_batch_mixed_topologies_fp64(gb, oracle, tmp_path):
         assert np.max(np.abs(b.slice(r["theta"], i) - ref["theta"])) < 1e-9
 
 
-def test_batch_fp32_lu_accuracy(gb, oracle):
+@pytest.mark.parametrize("rotate", [0, 1], ids=["sincos", "rotation"])
+def test_batch_fp32_lu_accuracy(gb, oracle, rotate):
     path = os.path.join(GOLDEN, "c2_base.cdf")
     og = oracle.Grid(path)
     n = 32
     Pl, Ql, Pg = scenarios(og, n, 11)
-    b, r = run_batch(gb, [gb.read_grid(path)], np.zeros(n, np.int32), Pl.ravel(), Ql.ravel(), Pg.ravel(),
-                     precision=gb.PREC_FP32_IR)
+    b = gb.Batch([gb.read_grid(path)], tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1, precision=gb.PREC_FP32_IR)
+    b.set_plan(rotate=rotate)
+    b.set_instances(np.zeros(n, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
+    b.solve()
+    r = b.results()
     for i in range(n):
         ref = oracle_solve(og, Pl[i], Ql[i], Pg[i], 1)
         assert r["status"][i] == 0 and r["final_mismatch"][i] <= 1e-8
@@ -190,6 +194,7 @@ PLANS = [
     dict(lu1=0, narrow=1),                              # two passes per level (pivots, then entries)
     dict(warp_mode=0, lu1=0),
     dict(warp_lu1=1, handoff_it=8),                     # one-pass levels in the warps too
+    dict(rotate=1),                                     # FP32 phasors by rotation (FP64 here: no effect)
 ]
 
 
