@@ -197,8 +197,8 @@ struct Args {
     int narrow;
     // both kernels: one pass per elimination level (lu_level1) instead of two
     int lu1;
-    // warp kernel: nonzero *flat_on = every instance starts from its grid's own
-    // starting state, so iteration 0 takes Topo::flat (null: never)
+    // nonzero *flat_on = every instance starts from its grid's own starting
+    // state, so iteration 0 takes Topo::flat (null: never)
     const int *flat_on;
     // FP32-LU form: 1 = phasors rotated by the Newton step in the update
     // (rotate_phasor), 0 = a full sincos of the new angles each iteration
@@ -763,21 +763,29 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
         }
         __syncthreads();
         bool fresh = true;
+        // iteration 0 from the grid's own start: the topology's shared copy
+        const char *flat = (!a.resume && T.flat && a.flat_on && *a.flat_on) ? T.flat : nullptr;
+        const FlatLayout F = flat_layout<TJ>(nB, nq);
         for (;;) {
-            // phasors (the FP32-LU form rotates them in the update after the
-            // first pass) and injections
-            if (sizeof(TJ) == 8 || fresh || !a.rotate)
+            const bool f0 = flat && s_it == 0;
+            if (f0) {
                 for (int k = tid; k < nB; k += kThreads) {
-                    double s, c;
-                    sincos(th[k], &s, &c);
-                    cs[k] = c;
-                    sn[k] = s;
-                    ef[k] = make_double2(V[k] * c, V[k] * s);
-                    if (sizeof(TJ) == 4) f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
+                    cs[k] = ((const double *)(flat + F.cs))[k];
+                    sn[k] = ((const double *)(flat + F.sn))[k];
+                    ef[k] = ((const double2 *)(flat + F.ef))[k];
+                    if (sizeof(TJ) == 4) f32[k] = ((const float4 *)(flat + F.f32))[k];
+                    P[k] = ((const double *)(flat + F.P))[k];
+                    Q[k] = ((const double *)(flat + F.Q))[k];
                 }
+            } else {
+                // phasors (the FP32-LU form may rotate them in the update
+                // instead) and injections
+                if (sizeof(TJ) == 8 || fresh || !a.rotate)
+                    for (int k = tid; k < nB; k += kThreads) phasor<TJ>(k, th, V, cs, sn, ef, f32);
+                __syncthreads();
+                for (int k = tid; k < nB; k += kThreads) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
+            }
             fresh = false;
-            __syncthreads();
-            for (int k = tid; k < nB; k += kThreads) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
             __syncthreads();
             const int it = s_it;
             // reactive limits (chkLimQ) when the previous step was small
@@ -832,94 +840,68 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
             }
             __syncthreads();
             if (s_done) break;
-            // Jacobian fill at every factor position (zeros at fill-in)
-            for (int q = tid; q < nq; q += kThreads) {
-                const int s = G.ysl[q];
-                B4 blk;
-                blk.x = blk.y = blk.z = blk.w = 0;
-                if (s >= 0) {
-                    const int k = G.rbus[q], mb = G.cbus[q];
-                    const int ak = act[k];
-                    if constexpr (sizeof(TJ) == 4) {
-                        // FP32-LU form: FP32 copies of the phasors, V and Ybus
-                        const float4 fk = f32[k];
-                        const float2 y = G.yval32[s];
-                        if (q < n) {
-                            blk = diag_block32<B4>((float)P[k], (float)Q[k], fk.z, y, ak);
-                        } else {
-                            const int am = act[mb];
-                            const float4 fm = f32[mb];
-                            const float tr = y.x * fm.x - y.y * fm.y, ti = y.x * fm.y + y.y * fm.x;
-                            const float wr = fk.x * tr + fk.y * ti, wi = fk.y * tr - fk.x * ti;
-                            blk.x = fk.z * fm.z * wi;
-                            if (am) blk.y = fk.z * wr;
-                            if (ak) blk.z = -fk.z * fm.z * wr;
-                            if (ak && am) blk.w = fk.z * wi;
-                        }
-                    } else {
-                        const double2 y = G.yval[s];
-                        const double Vk = V[k];
-                        if (q < n) {
-                            blk = diag_block<TJ, B4>(P[k], Q[k], Vk, y, ak);
-                        } else {
-                            // off-diagonal entries in the precision of the factor
-                            const int am = act[mb];
-                            const TJ ck = (TJ)cs[k], sk = (TJ)sn[k], cm = (TJ)cs[mb], sm = (TJ)sn[mb];
-                            const TJ yr = (TJ)y.x, yi = (TJ)y.y, vk = (TJ)Vk, vm = (TJ)V[mb];
-                            const TJ tr = yr * cm - yi * sm, ti = yr * sm + yi * cm;
-                            const TJ wr = ck * tr + sk * ti, wi = sk * tr - ck * ti;
-                            blk.x = vk * vm * wi;
-                            if (am) blk.y = vk * wr;
-                            if (ak) blk.z = -vk * vm * wr;
-                            if (ak && am) blk.w = vk * wi;
-                        }
-                    }
-                }
-                fac[q] = blk;
-            }
-            __syncthreads();
-            // LU factorisation fused with forward substitution, one level at a
-            // time, in two passes: pivots (diagonal block, its inverse, y_j),
-            // then the level's off-diagonal entries.  A level narrow enough
-            // for one warp (lvl_narrow) runs on warp 0 alone with warp
-            // syncs, lanes grouped by lvl_group_w, and the block meets at a
-            // barrier only where a wide level follows; wide levels use the
-            // whole block, lanes grouped by lvl_group.
-            // With lu1 each level is one pass (lu_level1: pivots and entries
-            // side by side, L unscaled) and needs one barrier instead of two.
-            B2 *zs = (B2 *)(ism + L.zs);
-            for (int l = 0; l < T.nfl; l++) {
-                if (a.narrow && (G.lvl_narrow[l] & 1)) {
-                    if (warp == 0) {
-                        const int gp = a.no_group ? 0 : G.lvl_group_w[3 * l];
-                        const int ge = a.no_group ? 0 : G.lvl_group_w[3 * l + 1];
-                        bool sing;
-                        if (a.lu1) {
-                            sing = lu_level1<TJ, 32>(G, l, gp, ge, a.no_group ? 0 : G.lvl_rot[l] >> 16, lane, fac,
-                                                     dinv, ys, zs, Lv, Uv);
-                        } else {
-                            sing = lu_pivots<TJ, 32>(G, l, gp, lane, fac, dinv, ys, Lv, Uv);
-                            __syncwarp();
-                            lu_entries<TJ, 32>(G, l, ge, lane, dinv, Lv, Uv);
-                        }
-                        if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
-                        __syncwarp();
-                    }
-                    if (l + 1 == T.nfl || !(G.lvl_narrow[l + 1] & 1)) __syncthreads();
-                } else {
-                    const int gp = a.no_group ? 0 : G.lvl_group[3 * l];
-                    const int ge = a.no_group ? 0 : G.lvl_group[3 * l + 1];
-                    if (a.lu1) {
-                        const bool sing = lu_level1<TJ, kThreads>(G, l, gp, ge, a.no_group ? 0 : G.lvl_rot[l] & 0xffff,
-                                                                  tid, fac, dinv, ys, zs, Lv, Uv);
-                        if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
-                    } else {
-                        const bool sing = lu_pivots<TJ, kThreads>(G, l, gp, tid, fac, dinv, ys, Lv, Uv);
-                        if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
-                        __syncthreads();
-                        lu_entries<TJ, kThreads>(G, l, ge, tid, dinv, Lv, Uv);
-                    }
+            const B4 *Ub = Uv, *Db = dinv;
+            if (f0) {
+                // the shared factor of iteration 0: forward substitution alone
+                const B4 *facS = (const B4 *)(flat + F.fac);
+                if (*(const int *)(flat + F.sing)) {
+                    if (tid == 0) { s_status = GBPF_E_SINGULAR; s_done = 1; }
                     __syncthreads();
+                    break;
+                }
+                for (int l = 0; l < T.nfl; l++) {
+                    fwd_rows<TJ, kThreads>(G, l, a.no_group ? 0 : G.lvl_group[3 * l], tid, facS + n, ys);
+                    __syncthreads();
+                }
+                Ub = facS + n + T.nup;
+                Db = facS;
+            } else {
+                // Jacobian fill at every factor position (zeros at fill-in)
+                for (int q = tid; q < nq; q += kThreads) fac[q] = jac_block<TJ>(G, q, n, act, P, Q, V, cs, sn, f32);
+                __syncthreads();
+                // LU factorisation fused with forward substitution, one level at a
+                // time, in two passes: pivots (diagonal block, its inverse, y_j),
+                // then the level's off-diagonal entries.  A level narrow enough
+                // for one warp (lvl_narrow) runs on warp 0 alone with warp
+                // syncs, lanes grouped by lvl_group_w, and the block meets at a
+                // barrier only where a wide level follows; wide levels use the
+                // whole block, lanes grouped by lvl_group.
+                // With lu1 each level is one pass (lu_level1: pivots and entries
+                // side by side, L unscaled) and needs one barrier instead of two.
+                B2 *zs = (B2 *)(ism + L.zs);
+                for (int l = 0; l < T.nfl; l++) {
+                    if (a.narrow && (G.lvl_narrow[l] & 1)) {
+                        if (warp == 0) {
+                            const int gp = a.no_group ? 0 : G.lvl_group_w[3 * l];
+                            const int ge = a.no_group ? 0 : G.lvl_group_w[3 * l + 1];
+                            bool sing;
+                            if (a.lu1) {
+                                sing = lu_level1<TJ, 32>(G, l, gp, ge, a.no_group ? 0 : G.lvl_rot[l] >> 16, lane, fac,
+                                                         dinv, ys, zs, Lv, Uv);
+                            } else {
+                                sing = lu_pivots<TJ, 32>(G, l, gp, lane, fac, dinv, ys, Lv, Uv);
+                                __syncwarp();
+                                lu_entries<TJ, 32>(G, l, ge, lane, dinv, Lv, Uv);
+                            }
+                            if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                            __syncwarp();
+                        }
+                        if (l + 1 == T.nfl || !(G.lvl_narrow[l + 1] & 1)) __syncthreads();
+                    } else {
+                        const int gp = a.no_group ? 0 : G.lvl_group[3 * l];
+                        const int ge = a.no_group ? 0 : G.lvl_group[3 * l + 1];
+                        if (a.lu1) {
+                            const bool sing = lu_level1<TJ, kThreads>(G, l, gp, ge, a.no_group ? 0 : G.lvl_rot[l] & 0xffff,
+                                                                      tid, fac, dinv, ys, zs, Lv, Uv);
+                            if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                        } else {
+                            const bool sing = lu_pivots<TJ, kThreads>(G, l, gp, tid, fac, dinv, ys, Lv, Uv);
+                            if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                            __syncthreads();
+                            lu_entries<TJ, kThreads>(G, l, ge, tid, dinv, Lv, Uv);
+                        }
+                        __syncthreads();
+                    }
                 }
             }
             if (s_done) break;
@@ -927,12 +909,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
             for (int l = 0; l < T.nbl; l++) {
                 if (a.narrow && (G.lvl_narrow[l] & 2)) {
                     if (warp == 0) {
-                        back_rows<TJ, 32>(G, l, a.no_group ? 0 : G.lvl_group_w[3 * l + 2], lane, dinv, Uv, ys);
+                        back_rows<TJ, 32>(G, l, a.no_group ? 0 : G.lvl_group_w[3 * l + 2], lane, Db, Ub, ys);
                         __syncwarp();
                     }
                     if (l + 1 == T.nbl || !(G.lvl_narrow[l + 1] & 2)) __syncthreads();
                 } else {
-                    back_rows<TJ, kThreads>(G, l, a.no_group ? 0 : G.lvl_group[3 * l + 2], tid, dinv, Uv, ys);
+                    back_rows<TJ, kThreads>(G, l, a.no_group ? 0 : G.lvl_group[3 * l + 2], tid, Db, Ub, ys);
                     __syncthreads();
                 }
             }
@@ -1329,7 +1311,7 @@ constexpr int kSelThreads = 256;
 __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *pred, int ldp, const float *omean,
                                                            const float *oscale, double *sV, double *sTh, double4_32a *ef,
                                                            int *kind) {
-    __shared__ double red[2][kSelThreads / 32];
+    __shared__ unsigned long long red[2][kSelThreads / 32];
     const int inst = blockIdx.x, tid = threadIdx.x;
     const Topo T = a.topo[a.inst_topo[inst]];
     const TopoView G = bind(T.o, T.blob);
@@ -1337,6 +1319,10 @@ __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *
     const int nB = T.nB;
     const float *pr = pred + (size_t)inst * ldp;
     double4_32a *e = ef + off;
+    // the own (flat) start's injections: the topology's shared iteration 0
+    // when the instances start from the grid's own state, else computed here
+    const char *flat = (T.flat && a.flat_on && *a.flat_on) ? T.flat : nullptr;
+    const FlatLayout F = flat_layout<float>(nB, T.n + 2 * T.nup);  // P, Q offsets do not depend on the precision
     for (int k = tid; k < nB; k += kSelThreads) {
         const int ty = G.type[k];
         const double v0 = a.V0[off + k], t0 = a.th0[off + k];
@@ -1344,13 +1330,13 @@ __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *
         const double t = ty == 3 ? t0 : (double)pr[nB + k] * oscale[nB + k] + omean[nB + k];
         sV[off + k] = v;
         sTh[off + k] = t;
-        double s, c, s0, c0;
+        double s, c, s0 = 0, c0 = 0;
         sincos(t, &s, &c);
-        sincos(t0, &s0, &c0);
+        if (!flat) sincos(t0, &s0, &c0);
         e[k] = double4_32a{v * c, v * s, v0 * c0, v0 * s0};
     }
     __syncthreads();
-    double mp = 0, mf = 0;
+    unsigned long long mp = 0, mf = 0;
     for (int k = tid; k < nB; k += kSelThreads) {
         const int ty = G.type[k];
         if (ty == 3) continue;
@@ -1358,31 +1344,38 @@ __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *
         for (int p = G.yptr[k]; p < G.yptr[k + 1]; p++) {
             const double2 y = G.yval[p];
             const double4_32a u = e[G.ycol[p]];
-            ir += y.x * u.x - y.y * u.y;
-            ii += y.x * u.y + y.y * u.x;
-            jr += y.x * u.z - y.y * u.w;
-            ji += y.x * u.w + y.y * u.z;
+            ir = fma(y.x, u.x, ir);
+            ir = fma(-y.y, u.y, ir);
+            ii = fma(y.x, u.y, ii);
+            ii = fma(y.y, u.x, ii);
+            if (!flat) {
+                jr = fma(y.x, u.z, jr);
+                jr = fma(-y.y, u.w, jr);
+                ji = fma(y.x, u.w, ji);
+                ji = fma(y.y, u.z, ji);
+            }
         }
         const double4_32a u = e[k];
         const double pl = a.Pliq[off + k];
-        double tp = fabs(pl - (u.x * ir + u.y * ii)), tf = fabs(pl - (u.z * jr + u.w * ji));
+        const double pf = flat ? ((const double *)(flat + F.P))[k] : fma(u.z, jr, u.w * ji);
+        unsigned long long tp = abits(pl - fma(u.x, ir, u.y * ii)), tf = abits(pl - pf);
         if (ty == 0 || ty == 1) {
             const double ql = a.Qliq[off + k];
-            tp = fmax(tp, fabs(ql - (u.y * ir - u.x * ii)));
-            tf = fmax(tf, fabs(ql - (u.w * jr - u.z * ji)));
+            const double qf = flat ? ((const double *)(flat + F.Q))[k] : fma(u.w, jr, -u.z * ji);
+            tp = umax64(tp, abits(ql - fma(u.y, ir, -u.x * ii)));
+            tf = umax64(tf, abits(ql - qf));
         }
-        if (tp != tp) tp = INFINITY;
-        if (tf != tf) tf = INFINITY;
-        mp = fmax(mp, tp);
-        mf = fmax(mf, tf);
+        mp = umax64(mp, tp);
+        mf = umax64(mf, tf);
     }
-    mp = warp_max(mp);
-    mf = warp_max(mf);
+    mp = warp_umax(mp);
+    mf = warp_umax(mf);
     if ((tid & 31) == 0) { red[0][tid >> 5] = mp; red[1][tid >> 5] = mf; }
     __syncthreads();
     mp = red[0][0];
     mf = red[1][0];
-    for (int w = 1; w < kSelThreads / 32; w++) { mp = fmax(mp, red[0][w]); mf = fmax(mf, red[1][w]); }
+    for (int w = 1; w < kSelThreads / 32; w++) { mp = umax64(mp, red[0][w]); mf = umax64(mf, red[1][w]); }
+    // NaN patterns order above every number: a NaN predicted mismatch loses
     const bool use = mp < mf;
     if (!use)
         for (int k = tid; k < nB; k += kSelThreads) {
@@ -1982,14 +1975,13 @@ gbpf_status gbpf_batch::build_graph() {
         }
         warp_grid = std::max(1, std::min((n_warp_q + warp_warps - 1) / warp_warps, dev_sm * std::max(occ, 1)));
     }
-    // the shared flat-start iteration of every warp-served topology
+    // the shared flat-start iteration of every topology
     flat_mem.reset();
     for (auto &T : topo_h) T.flat = nullptr;
-    if (n_warp_q && plan.flat_shared) {
+    if (plan.flat_shared) {
         std::vector<size_t> at(topo_h.size(), 0);
         size_t total = 0;
         for (size_t t = 0; t < topo_h.size(); t++) {
-            if (!warp_ok[t]) continue;
             const Topo &T = topo_h[t];
             const int nq = T.n + 2 * T.nup;
             at[t] = total;
@@ -1997,7 +1989,6 @@ gbpf_status gbpf_batch::build_graph() {
         }
         CK(cudaMalloc(&flat_mem.p, total));
         for (size_t t = 0; t < topo_h.size(); t++) {
-            if (!warp_ok[t]) continue;
             Topo &T = topo_h[t];
             const int nq = T.n + 2 * T.nup;
             const FlatLayout F = fp32 ? flat_layout<float>(T.nB, nq) : flat_layout<double>(T.nB, nq);
@@ -2031,8 +2022,7 @@ gbpf_status gbpf_batch::build_graph() {
     args.queue = (const int *)queues.p + n_warp_q;
     args.queue_len = n_block_q;
     wargs.counter = (int *)counter.p + 1;
-    wargs.flat_on = (const int *)counter.p + 8;
-    args.flat_on = nullptr;
+    wargs.flat_on = args.flat_on = (const int *)counter.p + 8;
     wargs.queue = (const int *)queues.p;
     wargs.queue_len = n_warp_q;
     wargs.slice = (int)slice;
@@ -2105,7 +2095,7 @@ gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, 
     Args ba = args, wa = wargs;
     ba.V0 = wa.V0 = wV;
     ba.th0 = wa.th0 = wTh;
-    wa.flat_on = nullptr;  // predicted starts: no shared iteration 0
+    ba.flat_on = wa.flat_on = nullptr;  // predicted starts: no shared iteration 0
     ba.max_iter = wa.max_iter = std::min(max_iter, kWarmMaxIter);
     if ((st = launch_with(stream, ba, wa)) != GBPF_OK) return st;
     k_ws_check<<<(n_inst * 32 + 255) / 256, 256, 0, stream>>>(args, wV, wKind);

@@ -341,3 +341,25 @@ def test_two_batches_in_flight(gb):
         for k in ("iterations", "status", "V", "theta"):
             np.testing.assert_array_equal(got[k], want[k], err_msg=k)
     assert gb.time_pipelined(pair, 4) > 0
+
+
+def test_block_mode_shared_flat_start(gb, oracle):
+    """Thread-block instances take the shared iteration 0 too (a two-pass
+    factor made once per topology, the blocks' own iterations after it):
+    the oracle's FP64 answers with and without it."""
+    path = os.path.join(GOLDEN, "c2_s3.cdf")
+    og = oracle.Grid(path)
+    n = 24
+    Pl, Ql, Pg = scenarios(og, n, 13)
+    for flat in (1, 0):
+        b = gb.Batch([gb.read_grid(path)], tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1)
+        b.set_plan(warp_mode=0, flat_shared=flat)
+        b.set_instances(np.zeros(n, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
+        b.solve()
+        r = b.results()
+        assert b.plan()["block_instances"] == n
+        for i in range(n):
+            ref = oracle_solve(og, Pl[i], Ql[i], Pg[i], 1)
+            assert r["iterations"][i] == ref["iterations"] and b.events(i) == ref["events"][:16], (flat, i)
+            if ref["converged"]:
+                assert np.max(np.abs(b.slice(r["V"], i) - ref["V"])) < 1e-9
