@@ -630,7 +630,8 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
                               "frac": train_tflops / tpeak,
                               "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained" if peaks else "fallback"},
         "clocks": clk.summary(),
-        "gpu_launches": a.steps * (1 + 4 + 1 + 1 + 1 + (1 if (kind == 2).any() else 0)),
+        # features, 4 network layers, start choice, queue order, Newton (restarts included)
+        "gpu_launches": a.steps * (1 + 4 + 1 + 1 + 1),
     }
     if rank == 0 and not a.no_cpu_baseline:
         cdf = write_grid(grid)

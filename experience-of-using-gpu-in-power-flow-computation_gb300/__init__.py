@@ -45,7 +45,7 @@ EXPORTS = [
     "gbpf_batch_solve_warm", "gbpf_mlp_set_loss_metric", "gbpf_solver_setup_times", "gbpf_batch_kernel_times",
     "gbpf_grid_write_m", "gbpf_grid_ybus_form", "gbpf_grid_set_ybus_form",
     "gbpf_batch_get_plan", "gbpf_batch_set_plan", "gbpf_batch_autotune",
-    "gbpf_batch_launch", "gbpf_batch_wait", "gbpf_batch_time_pipelined",
+    "gbpf_batch_launch", "gbpf_batch_wait", "gbpf_batch_time_pipelined", "gbpf_batch_warm_phases",
 ]
 
 
@@ -594,13 +594,17 @@ class Batch:
         """gbpf_batch_solve_warm: Newton from the network's predicted start
         (flat-start fallback).  Returns start_kind (0 own start, 1 predicted
         start converged, 2 predicted start failed and was replaced),
-        warm_iterations and the device time in ms."""
+        warm_iterations, the device time in ms and its phases
+        (gbpf_batch_warm_phases)."""
         kind = np.zeros(self.n_inst, np.int32)
         wit = np.zeros(self.n_inst, np.int32)
         ms = ctypes.c_double()
         _check(lib().gbpf_batch_solve_warm(self.h, mlp.h, _p(kind), _p(wit), ctypes.byref(ms)),
                "gbpf_batch_solve_warm")
-        return dict(start_kind=kind, warm_iterations=wit, ms=ms.value)
+        ph = np.zeros(3)
+        _check(lib().gbpf_batch_warm_phases(self.h, _p(ph)), "gbpf_batch_warm_phases")
+        return dict(start_kind=kind, warm_iterations=wit, ms=ms.value,
+                    phases_ms=dict(network=ph[0], start_choice=ph[1], newton=ph[2]))
 
     def slice(self, arr, inst):
         return arr[self.offsets[inst]:self.offsets[inst + 1]]

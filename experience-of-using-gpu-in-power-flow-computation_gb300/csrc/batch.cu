@@ -203,6 +203,17 @@ struct Args {
     // FP32-LU form: 1 = phasors rotated by the Newton step in the update
     // (rotate_phasor), 0 = a full sincos of the new angles each iteration
     int rotate;
+    // learned warm start (kind null: none).  kind[inst] = 1: the instance
+    // starts from Vp/thp (the prediction) with at most warm_max_iter
+    // iterations; when that run fails -- no convergence, or a PQ bus's |V|
+    // ending more than warm_max_dv from the prediction (another, low-voltage
+    // solution) -- it starts again from its own start in the same launch, and
+    // kind becomes 2.  witers[inst] = the predicted run's iterations.  kind 0:
+    // the own start (V0/th0, flat_on), max_iter iterations.
+    int *kind, *witers;
+    const double *Vp, *thp;
+    int warm_max_iter;
+    double warm_max_dv;
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
@@ -733,211 +744,235 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
         B4 *dinv = fac;
         const int n = T.n, nB = T.nB, nq = T.n + 2 * T.nup;
         B4 *Lv = fac + n, *Uv = fac + n + T.nup;
-        if (!a.resume) {
-            // initLim (GPU/limiteInjReat.cuh:188-224) and the starting state
-            for (int k = tid; k < nB; k += kThreads) {
-                V[k] = a.V0[off + k];
-                th[k] = a.th0[off + k];
-                QL[k] = a.Qliq[off + k];
-                act[k] = (G.type[k] == 0 || G.type[k] == 1);
-            }
-            for (int i = tid; i < T.nPV; i += kThreads) limQ[i] = 0;
-            if (tid == 0) { s_done = 0; s_status = 0; s_it = 0; s_nev = 0; s_maxDx = INFINITY; }
-        } else {
-            // the state a warp parked at the hand-off
-            for (int k = tid; k < nB; k += kThreads) {
-                V[k] = a.V[off + k];
-                th[k] = a.th[off + k];
-                QL[k] = a.Q[off + k];
-                act[k] = (G.type[k] == 0 || G.type[k] == 1);
-            }
-            __syncthreads();
-            for (int i = tid; i < T.nPV; i += kThreads) {
-                limQ[i] = (int)a.P[off + i];
-                act[G.pv_bus[i]] = limQ[i];
-            }
-            if (tid == 0) {
-                s_done = 0; s_status = 0;
-                s_it = a.iters[inst]; s_nev = a.n_events[inst]; s_maxDx = a.mism[inst];
-            }
-        }
-        __syncthreads();
-        bool fresh = true;
-        // iteration 0 from the grid's own start: the topology's shared copy
-        const char *flat = (!a.resume && T.flat && a.flat_on && *a.flat_on) ? T.flat : nullptr;
-        const FlatLayout F = flat_layout<TJ>(nB, nq);
+        int wk = a.kind ? a.kind[inst] : 0;
+        bool from_park = a.resume;
+        // a failed run from a predicted start runs again from the own start
         for (;;) {
-            const bool f0 = flat && s_it == 0;
-            if (f0) {
+            const bool pred = wk == 1;
+            const int mi = pred ? a.warm_max_iter : a.max_iter;
+            if (!from_park) {
+                // initLim (GPU/limiteInjReat.cuh:188-224) and the starting state
+                const double *v0 = pred ? a.Vp : a.V0, *t0 = pred ? a.thp : a.th0;
                 for (int k = tid; k < nB; k += kThreads) {
-                    cs[k] = ((const double *)(flat + F.cs))[k];
-                    sn[k] = ((const double *)(flat + F.sn))[k];
-                    ef[k] = ((const double2 *)(flat + F.ef))[k];
-                    if (sizeof(TJ) == 4) f32[k] = ((const float4 *)(flat + F.f32))[k];
-                    P[k] = ((const double *)(flat + F.P))[k];
-                    Q[k] = ((const double *)(flat + F.Q))[k];
+                    V[k] = v0[off + k];
+                    th[k] = t0[off + k];
+                    QL[k] = a.Qliq[off + k];
+                    act[k] = (G.type[k] == 0 || G.type[k] == 1);
                 }
+                for (int i = tid; i < T.nPV; i += kThreads) limQ[i] = 0;
+                if (tid == 0) { s_done = 0; s_status = 0; s_it = 0; s_nev = 0; s_maxDx = INFINITY; }
             } else {
-                // phasors (the FP32-LU form may rotate them in the update
-                // instead) and injections
-                if (sizeof(TJ) == 8 || fresh || !a.rotate)
-                    for (int k = tid; k < nB; k += kThreads) phasor<TJ>(k, th, V, cs, sn, ef, f32);
+                // the state a warp parked at the hand-off
+                for (int k = tid; k < nB; k += kThreads) {
+                    V[k] = a.V[off + k];
+                    th[k] = a.th[off + k];
+                    QL[k] = a.Q[off + k];
+                    act[k] = (G.type[k] == 0 || G.type[k] == 1);
+                }
                 __syncthreads();
-                for (int k = tid; k < nB; k += kThreads) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
-            }
-            fresh = false;
-            __syncthreads();
-            const int it = s_it;
-            // reactive limits (chkLimQ) when the previous step was small
-            if (a.lim && it >= 1 && it < a.max_iter && abits(s_maxDx) < tol10_bits) {
                 for (int i = tid; i < T.nPV; i += kThreads) {
-                    const int b = G.pv_bus[i];
-                    const double ql = a.Qload[off + b], qg = Q[b] + ql;
-                    int code = 0;
-                    if (qg < G.Qmin[i] - a.tol) {
-                        if (!limQ[i]) code = 1;
-                        else if (QL[b] != G.Qmin[i] - ql) code = 2;
-                        limQ[i] = 1;
-                        QL[b] = G.Qmin[i] - ql;
-                    } else if (qg > G.Qmax[i] + a.tol) {
-                        if (!limQ[i]) code = 3;
-                        else if (QL[b] != G.Qmax[i] - ql) code = 4;
-                        limQ[i] = 1;
-                        QL[b] = G.Qmax[i] - ql;
-                    } else {
-                        if (limQ[i]) code = 5;
-                        limQ[i] = 0;
+                    limQ[i] = (int)a.P[off + i];
+                    act[G.pv_bus[i]] = limQ[i];
+                }
+                if (tid == 0) {
+                    s_done = 0; s_status = 0;
+                    s_it = a.iters[inst]; s_nev = a.n_events[inst]; s_maxDx = a.mism[inst];
+                }
+            }
+            __syncthreads();
+            bool fresh = true;
+            // iteration 0 from the grid's own start: the topology's shared copy
+            const char *flat = (!from_park && !pred && T.flat && a.flat_on && *a.flat_on) ? T.flat : nullptr;
+            const FlatLayout F = flat_layout<TJ>(nB, nq);
+            for (;;) {
+                const bool f0 = flat && s_it == 0;
+                if (f0) {
+                    for (int k = tid; k < nB; k += kThreads) {
+                        cs[k] = ((const double *)(flat + F.cs))[k];
+                        sn[k] = ((const double *)(flat + F.sn))[k];
+                        ef[k] = ((const double2 *)(flat + F.ef))[k];
+                        if (sizeof(TJ) == 4) f32[k] = ((const float4 *)(flat + F.f32))[k];
+                        P[k] = ((const double *)(flat + F.P))[k];
+                        Q[k] = ((const double *)(flat + F.Q))[k];
                     }
-                    act[b] = limQ[i];
-                    if (code) {
-                        const int e = atomicAdd(&s_nev, 1);
-                        if (e < a.ev_cap) {
-                            int *ev = a.events + ((long long)inst * a.ev_cap + e) * 4;
-                            ev[0] = it; ev[1] = b + 1; ev[2] = i; ev[3] = code;
+                } else {
+                    // phasors (the FP32-LU form may rotate them in the update
+                    // instead) and injections
+                    if (sizeof(TJ) == 8 || fresh || !a.rotate)
+                        for (int k = tid; k < nB; k += kThreads) phasor<TJ>(k, th, V, cs, sn, ef, f32);
+                    __syncthreads();
+                    for (int k = tid; k < nB; k += kThreads) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
+                }
+                fresh = false;
+                __syncthreads();
+                const int it = s_it;
+                // reactive limits (chkLimQ) when the previous step was small
+                if (a.lim && it >= 1 && it < mi && abits(s_maxDx) < tol10_bits) {
+                    for (int i = tid; i < T.nPV; i += kThreads) {
+                        const int b = G.pv_bus[i];
+                        const double ql = a.Qload[off + b], qg = Q[b] + ql;
+                        int code = 0;
+                        if (qg < G.Qmin[i] - a.tol) {
+                            if (!limQ[i]) code = 1;
+                            else if (QL[b] != G.Qmin[i] - ql) code = 2;
+                            limQ[i] = 1;
+                            QL[b] = G.Qmin[i] - ql;
+                        } else if (qg > G.Qmax[i] + a.tol) {
+                            if (!limQ[i]) code = 3;
+                            else if (QL[b] != G.Qmax[i] - ql) code = 4;
+                            limQ[i] = 1;
+                            QL[b] = G.Qmax[i] - ql;
+                        } else {
+                            if (limQ[i]) code = 5;
+                            limQ[i] = 0;
+                        }
+                        act[b] = limQ[i];
+                        if (code) {
+                            const int e = atomicAdd(&s_nev, 1);
+                            if (e < a.ev_cap) {
+                                int *ev = a.events + ((long long)inst * a.ev_cap + e) * 4;
+                                ev[0] = it; ev[1] = b + 1; ev[2] = i; ev[3] = code;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+                // mismatch (FP64) and convergence test
+                unsigned long long m = 0;
+                for (int j = tid; j < n; j += kThreads) {
+                    const int k = G.bus_of_blk[j];
+                    const double gp = a.Pliq[off + k] - P[k];
+                    const double gq = act[k] ? QL[k] - Q[k] : 0.0;
+                    B2 r;
+                    r.x = (TJ)gp;
+                    r.y = (TJ)gq;
+                    ys[j] = r;
+                    m = umax64(m, umax64(abits(gp), abits(gq)));
+                }
+                m = block_umax(m, red);
+                if (tid == 0) {
+                    s_maxG = __longlong_as_double((long long)m);
+                    if (m > kInfBits) { s_status = GBPF_E_NOCONV; s_done = 1; }
+                    else if (m <= tol_bits) s_done = 1;
+                    else if (it >= mi) { s_status = GBPF_E_NOCONV; s_done = 1; }
+                }
+                __syncthreads();
+                if (s_done) break;
+                const B4 *Ub = Uv, *Db = dinv;
+                if (f0) {
+                    // the shared factor of iteration 0: forward substitution alone
+                    const B4 *facS = (const B4 *)(flat + F.fac);
+                    if (*(const int *)(flat + F.sing)) {
+                        if (tid == 0) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                        __syncthreads();
+                        break;
+                    }
+                    for (int l = 0; l < T.nfl; l++) {
+                        fwd_rows<TJ, kThreads>(G, l, a.no_group ? 0 : G.lvl_group[3 * l], tid, facS + n, ys);
+                        __syncthreads();
+                    }
+                    Ub = facS + n + T.nup;
+                    Db = facS;
+                } else {
+                    // Jacobian fill at every factor position (zeros at fill-in)
+                    for (int q = tid; q < nq; q += kThreads) fac[q] = jac_block<TJ>(G, q, n, act, P, Q, V, cs, sn, f32);
+                    __syncthreads();
+                    // LU factorisation fused with forward substitution, one level at a
+                    // time, in two passes: pivots (diagonal block, its inverse, y_j),
+                    // then the level's off-diagonal entries.  A level narrow enough
+                    // for one warp (lvl_narrow) runs on warp 0 alone with warp
+                    // syncs, lanes grouped by lvl_group_w, and the block meets at a
+                    // barrier only where a wide level follows; wide levels use the
+                    // whole block, lanes grouped by lvl_group.
+                    // With lu1 each level is one pass (lu_level1: pivots and entries
+                    // side by side, L unscaled) and needs one barrier instead of two.
+                    B2 *zs = (B2 *)(ism + L.zs);
+                    for (int l = 0; l < T.nfl; l++) {
+                        if (a.narrow && (G.lvl_narrow[l] & 1)) {
+                            if (warp == 0) {
+                                const int gp = a.no_group ? 0 : G.lvl_group_w[3 * l];
+                                const int ge = a.no_group ? 0 : G.lvl_group_w[3 * l + 1];
+                                bool sing;
+                                if (a.lu1) {
+                                    sing = lu_level1<TJ, 32>(G, l, gp, ge, a.no_group ? 0 : G.lvl_rot[l] >> 16, lane,
+                                                             fac, dinv, ys, zs, Lv, Uv);
+                                } else {
+                                    sing = lu_pivots<TJ, 32>(G, l, gp, lane, fac, dinv, ys, Lv, Uv);
+                                    __syncwarp();
+                                    lu_entries<TJ, 32>(G, l, ge, lane, dinv, Lv, Uv);
+                                }
+                                if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                                __syncwarp();
+                            }
+                            if (l + 1 == T.nfl || !(G.lvl_narrow[l + 1] & 1)) __syncthreads();
+                        } else {
+                            const int gp = a.no_group ? 0 : G.lvl_group[3 * l];
+                            const int ge = a.no_group ? 0 : G.lvl_group[3 * l + 1];
+                            if (a.lu1) {
+                                const int rot = a.no_group ? 0 : G.lvl_rot[l] & 0xffff;
+                                const bool sing = lu_level1<TJ, kThreads>(G, l, gp, ge, rot, tid, fac, dinv, ys, zs,
+                                                                          Lv, Uv);
+                                if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                            } else {
+                                const bool sing = lu_pivots<TJ, kThreads>(G, l, gp, tid, fac, dinv, ys, Lv, Uv);
+                                if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                                __syncthreads();
+                                lu_entries<TJ, kThreads>(G, l, ge, tid, dinv, Lv, Uv);
+                            }
+                            __syncthreads();
                         }
                     }
                 }
-                __syncthreads();
-            }
-            // mismatch (FP64) and convergence test
-            unsigned long long m = 0;
-            for (int j = tid; j < n; j += kThreads) {
-                const int k = G.bus_of_blk[j];
-                const double gp = a.Pliq[off + k] - P[k];
-                const double gq = act[k] ? QL[k] - Q[k] : 0.0;
-                B2 r;
-                r.x = (TJ)gp;
-                r.y = (TJ)gq;
-                ys[j] = r;
-                m = umax64(m, umax64(abits(gp), abits(gq)));
-            }
-            m = block_umax(m, red);
-            if (tid == 0) {
-                s_maxG = __longlong_as_double((long long)m);
-                if (m > kInfBits) { s_status = GBPF_E_NOCONV; s_done = 1; }
-                else if (m <= tol_bits) s_done = 1;
-                else if (it >= a.max_iter) { s_status = GBPF_E_NOCONV; s_done = 1; }
-            }
-            __syncthreads();
-            if (s_done) break;
-            const B4 *Ub = Uv, *Db = dinv;
-            if (f0) {
-                // the shared factor of iteration 0: forward substitution alone
-                const B4 *facS = (const B4 *)(flat + F.fac);
-                if (*(const int *)(flat + F.sing)) {
-                    if (tid == 0) { s_status = GBPF_E_SINGULAR; s_done = 1; }
-                    __syncthreads();
-                    break;
-                }
-                for (int l = 0; l < T.nfl; l++) {
-                    fwd_rows<TJ, kThreads>(G, l, a.no_group ? 0 : G.lvl_group[3 * l], tid, facS + n, ys);
-                    __syncthreads();
-                }
-                Ub = facS + n + T.nup;
-                Db = facS;
-            } else {
-                // Jacobian fill at every factor position (zeros at fill-in)
-                for (int q = tid; q < nq; q += kThreads) fac[q] = jac_block<TJ>(G, q, n, act, P, Q, V, cs, sn, f32);
-                __syncthreads();
-                // LU factorisation fused with forward substitution, one level at a
-                // time, in two passes: pivots (diagonal block, its inverse, y_j),
-                // then the level's off-diagonal entries.  A level narrow enough
-                // for one warp (lvl_narrow) runs on warp 0 alone with warp
-                // syncs, lanes grouped by lvl_group_w, and the block meets at a
-                // barrier only where a wide level follows; wide levels use the
-                // whole block, lanes grouped by lvl_group.
-                // With lu1 each level is one pass (lu_level1: pivots and entries
-                // side by side, L unscaled) and needs one barrier instead of two.
-                B2 *zs = (B2 *)(ism + L.zs);
-                for (int l = 0; l < T.nfl; l++) {
-                    if (a.narrow && (G.lvl_narrow[l] & 1)) {
+                if (s_done) break;
+                // backward substitution, level by level, narrow levels on warp 0
+                for (int l = 0; l < T.nbl; l++) {
+                    if (a.narrow && (G.lvl_narrow[l] & 2)) {
                         if (warp == 0) {
-                            const int gp = a.no_group ? 0 : G.lvl_group_w[3 * l];
-                            const int ge = a.no_group ? 0 : G.lvl_group_w[3 * l + 1];
-                            bool sing;
-                            if (a.lu1) {
-                                sing = lu_level1<TJ, 32>(G, l, gp, ge, a.no_group ? 0 : G.lvl_rot[l] >> 16, lane, fac,
-                                                         dinv, ys, zs, Lv, Uv);
-                            } else {
-                                sing = lu_pivots<TJ, 32>(G, l, gp, lane, fac, dinv, ys, Lv, Uv);
-                                __syncwarp();
-                                lu_entries<TJ, 32>(G, l, ge, lane, dinv, Lv, Uv);
-                            }
-                            if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
+                            back_rows<TJ, 32>(G, l, a.no_group ? 0 : G.lvl_group_w[3 * l + 2], lane, Db, Ub, ys);
                             __syncwarp();
                         }
-                        if (l + 1 == T.nfl || !(G.lvl_narrow[l + 1] & 1)) __syncthreads();
+                        if (l + 1 == T.nbl || !(G.lvl_narrow[l + 1] & 2)) __syncthreads();
                     } else {
-                        const int gp = a.no_group ? 0 : G.lvl_group[3 * l];
-                        const int ge = a.no_group ? 0 : G.lvl_group[3 * l + 1];
-                        if (a.lu1) {
-                            const bool sing = lu_level1<TJ, kThreads>(G, l, gp, ge, a.no_group ? 0 : G.lvl_rot[l] & 0xffff,
-                                                                      tid, fac, dinv, ys, zs, Lv, Uv);
-                            if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
-                        } else {
-                            const bool sing = lu_pivots<TJ, kThreads>(G, l, gp, tid, fac, dinv, ys, Lv, Uv);
-                            if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
-                            __syncthreads();
-                            lu_entries<TJ, kThreads>(G, l, ge, tid, dinv, Lv, Uv);
-                        }
+                        back_rows<TJ, kThreads>(G, l, a.no_group ? 0 : G.lvl_group[3 * l + 2], tid, Db, Ub, ys);
                         __syncthreads();
                     }
                 }
-            }
-            if (s_done) break;
-            // backward substitution, level by level, narrow levels on warp 0
-            for (int l = 0; l < T.nbl; l++) {
-                if (a.narrow && (G.lvl_narrow[l] & 2)) {
-                    if (warp == 0) {
-                        back_rows<TJ, 32>(G, l, a.no_group ? 0 : G.lvl_group_w[3 * l + 2], lane, Db, Ub, ys);
-                        __syncwarp();
+                // update (FP64 state) and max|dx|
+                unsigned long long md = 0;
+                for (int j = tid; j < n; j += kThreads) {
+                    const int k = G.bus_of_blk[j];
+                    const double dt = (double)ys[j].x, dv = (double)ys[j].y;
+                    th[k] += dt;
+                    if (act[k]) V[k] += dv;
+                    if (sizeof(TJ) == 4 && a.rotate) {
+                        double c = cs[k], s = sn[k];
+                        rotate_phasor(th[k], dt, c, s);
+                        cs[k] = c;
+                        sn[k] = s;
+                        ef[k] = make_double2(V[k] * c, V[k] * s);
+                        f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
                     }
-                    if (l + 1 == T.nbl || !(G.lvl_narrow[l + 1] & 2)) __syncthreads();
-                } else {
-                    back_rows<TJ, kThreads>(G, l, a.no_group ? 0 : G.lvl_group[3 * l + 2], tid, Db, Ub, ys);
-                    __syncthreads();
+                    md = umax64(md, umax64(abits(dt), abits(dv)));
                 }
+                md = block_umax(md, red);
+                if (tid == 0) { s_maxDx = __longlong_as_double((long long)md); s_it = it + 1; }
+                __syncthreads();
             }
-            // update (FP64 state) and max|dx|
-            unsigned long long md = 0;
-            for (int j = tid; j < n; j += kThreads) {
-                const int k = G.bus_of_blk[j];
-                const double dt = (double)ys[j].x, dv = (double)ys[j].y;
-                th[k] += dt;
-                if (act[k]) V[k] += dv;
-                if (sizeof(TJ) == 4 && a.rotate) {
-                    double c = cs[k], s = sn[k];
-                    rotate_phasor(th[k], dt, c, s);
-                    cs[k] = c;
-                    sn[k] = s;
-                    ef[k] = make_double2(V[k] * c, V[k] * s);
-                    f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
-                }
-                md = umax64(md, umax64(abits(dt), abits(dv)));
+            if (!pred) break;
+            // the predicted run: kept, or started again from the own start
+            unsigned long long dv = 0;
+            for (int k = tid; k < nB; k += kThreads)
+                if (G.type[k] == 0 || G.type[k] == 1) dv = umax64(dv, abits(V[k] - a.Vp[off + k]));
+            dv = block_umax(dv, red);
+            const bool fail = s_status != 0 || dv > abits(a.warm_max_dv);
+            if (tid == 0) {
+                a.witers[inst] = s_it;
+                if (fail) a.kind[inst] = 2;
             }
-            md = block_umax(md, red);
-            if (tid == 0) { s_maxDx = __longlong_as_double((long long)md); s_it = it + 1; }
             __syncthreads();
+            if (!fail) break;
+            wk = 2;
+            from_park = false;
         }
         // results
         for (int k = tid; k < nB; k += kThreads) {
@@ -956,14 +991,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
     }
 }
 
-
-__device__ __forceinline__ double warp_max(double v) {
-    for (int o = 16; o > 0; o >>= 1) {
-        const double t = __shfl_xor_sync(0xffffffffu, v, o);
-        v = (t > v || t != t) ? t : v;
-    }
-    return v;
-}
 
 // One instance per warp: the same Newton loop as k_nr_block with the 32 lanes
 // of a warp in place of the threads of a block, so the only barriers are
@@ -1045,163 +1072,186 @@ __global__ void __launch_bounds__(32 * kWarpsMax, 1) k_nr_warp(Args a) {
         B4 *fac = (B4 *)(ism + L.fac), *dinv = fac;  // block inverses overwrite the diagonal
         const int n = T.n, nB = T.nB, nq = T.n + 2 * T.nup;
         B4 *Lv = fac + n, *Uv = fac + n + T.nup;
-        const char *flat = (T.flat && a.flat_on && *a.flat_on) ? T.flat : nullptr;
         const FlatLayout F = flat_layout<TJ>(nB, nq);
-        for (int k = lane; k < nB; k += 32) {
-            V[k] = a.V0[off + k];
-            th[k] = a.th0[off + k];
-            QL[k] = a.Qliq[off + k];
-            act[k] = (G.type[k] == 0 || G.type[k] == 1);
-        }
-        for (int i = lane; i < T.nPV; i += 32) limQ[i] = 0;
-        int it = 0, status = 0, nev = 0;
-        double maxDx = INFINITY, maxG = 0;
-        bool parked = false;
-        __syncwarp();
+        int wk = a.kind ? a.kind[inst] : 0;
+        int it, status, nev;
+        double maxDx, maxG;
+        bool parked;
+        // a failed run from a predicted start runs again from the own start
         for (;;) {
-            if (a.handoff_it > 0 && it == a.handoff_it) {
-                // still iterating: park the state for the block-per-instance kernel
-                for (int k = lane; k < nB; k += 32) {
-                    a.V[off + k] = V[k];
-                    a.th[off + k] = th[k];
-                    a.Q[off + k] = QL[k];
-                }
-                for (int i = lane; i < T.nPV; i += 32) a.P[off + i] = (double)limQ[i];
-                if (lane == 0) {
-                    a.iters[inst] = it;
-                    a.n_events[inst] = nev;
-                    a.mism[inst] = maxDx;
-                    a.handoff_q[atomicAdd(a.handoff_n, 1)] = inst;
-                }
-                parked = true;
-                break;
+            const bool pred = wk == 1;
+            const int mi = pred ? a.warm_max_iter : a.max_iter;
+            const char *flat = (!pred && T.flat && a.flat_on && *a.flat_on) ? T.flat : nullptr;
+            const double *v0 = pred ? a.Vp : a.V0, *t0 = pred ? a.thp : a.th0;
+            for (int k = lane; k < nB; k += 32) {
+                V[k] = v0[off + k];
+                th[k] = t0[off + k];
+                QL[k] = a.Qliq[off + k];
+                act[k] = (G.type[k] == 0 || G.type[k] == 1);
             }
-            const bool f0 = it == 0 && flat;
-            if (f0) {
-                // the shared iteration 0 of this topology's start
-                for (int k = lane; k < nB; k += 32) {
-                    cs[k] = ((const double *)(flat + F.cs))[k];
-                    sn[k] = ((const double *)(flat + F.sn))[k];
-                    ef[k] = ((const double2 *)(flat + F.ef))[k];
-                    if (sizeof(TJ) == 4) f32[k] = ((const float4 *)(flat + F.f32))[k];
-                    P[k] = ((const double *)(flat + F.P))[k];
-                    Q[k] = ((const double *)(flat + F.Q))[k];
-                }
-            } else {
-                if (sizeof(TJ) == 8 || it == 0 || !a.rotate)
-                    for (int k = lane; k < nB; k += 32) phasor<TJ>(k, th, V, cs, sn, ef, f32);
-                __syncwarp();
-                for (int k = lane; k < nB; k += 32) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
-            }
+            for (int i = lane; i < T.nPV; i += 32) limQ[i] = 0;
+            it = 0, status = 0, nev = 0;
+            maxDx = INFINITY, maxG = 0;
+            parked = false;
             __syncwarp();
-            if (a.lim && it >= 1 && it < a.max_iter && abits(maxDx) < tol10_bits) {
-                for (int i0 = 0; i0 < T.nPV; i0 += 32) {
-                    const int i = i0 + lane;
-                    int code = 0, b = 0;
-                    if (i < T.nPV) {
-                        b = G.pv_bus[i];
-                        const double ql = a.Qload[off + b], qg = Q[b] + ql;
-                        if (qg < G.Qmin[i] - a.tol) {
-                            if (!limQ[i]) code = 1;
-                            else if (QL[b] != G.Qmin[i] - ql) code = 2;
-                            limQ[i] = 1;
-                            QL[b] = G.Qmin[i] - ql;
-                        } else if (qg > G.Qmax[i] + a.tol) {
-                            if (!limQ[i]) code = 3;
-                            else if (QL[b] != G.Qmax[i] - ql) code = 4;
-                            limQ[i] = 1;
-                            QL[b] = G.Qmax[i] - ql;
-                        } else {
-                            if (limQ[i]) code = 5;
-                            limQ[i] = 0;
+            for (;;) {
+                if (a.handoff_it > 0 && it == a.handoff_it) {
+                    // still iterating: park the state for the block-per-instance kernel
+                    for (int k = lane; k < nB; k += 32) {
+                        a.V[off + k] = V[k];
+                        a.th[off + k] = th[k];
+                        a.Q[off + k] = QL[k];
+                    }
+                    for (int i = lane; i < T.nPV; i += 32) a.P[off + i] = (double)limQ[i];
+                    if (lane == 0) {
+                        a.iters[inst] = it;
+                        a.n_events[inst] = nev;
+                        a.mism[inst] = maxDx;
+                        a.handoff_q[atomicAdd(a.handoff_n, 1)] = inst;
+                    }
+                    parked = true;
+                    break;
+                }
+                const bool f0 = it == 0 && flat;
+                if (f0) {
+                    // the shared iteration 0 of this topology's start
+                    for (int k = lane; k < nB; k += 32) {
+                        cs[k] = ((const double *)(flat + F.cs))[k];
+                        sn[k] = ((const double *)(flat + F.sn))[k];
+                        ef[k] = ((const double2 *)(flat + F.ef))[k];
+                        if (sizeof(TJ) == 4) f32[k] = ((const float4 *)(flat + F.f32))[k];
+                        P[k] = ((const double *)(flat + F.P))[k];
+                        Q[k] = ((const double *)(flat + F.Q))[k];
+                    }
+                } else {
+                    if (sizeof(TJ) == 8 || it == 0 || !a.rotate)
+                        for (int k = lane; k < nB; k += 32) phasor<TJ>(k, th, V, cs, sn, ef, f32);
+                    __syncwarp();
+                    for (int k = lane; k < nB; k += 32) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
+                }
+                __syncwarp();
+                if (a.lim && it >= 1 && it < mi && abits(maxDx) < tol10_bits) {
+                    for (int i0 = 0; i0 < T.nPV; i0 += 32) {
+                        const int i = i0 + lane;
+                        int code = 0, b = 0;
+                        if (i < T.nPV) {
+                            b = G.pv_bus[i];
+                            const double ql = a.Qload[off + b], qg = Q[b] + ql;
+                            if (qg < G.Qmin[i] - a.tol) {
+                                if (!limQ[i]) code = 1;
+                                else if (QL[b] != G.Qmin[i] - ql) code = 2;
+                                limQ[i] = 1;
+                                QL[b] = G.Qmin[i] - ql;
+                            } else if (qg > G.Qmax[i] + a.tol) {
+                                if (!limQ[i]) code = 3;
+                                else if (QL[b] != G.Qmax[i] - ql) code = 4;
+                                limQ[i] = 1;
+                                QL[b] = G.Qmax[i] - ql;
+                            } else {
+                                if (limQ[i]) code = 5;
+                                limQ[i] = 0;
+                            }
+                            act[b] = limQ[i];
                         }
-                        act[b] = limQ[i];
+                        // events in PV order, as chkLimQ prints them
+                        const unsigned m = __ballot_sync(FULL, code != 0);
+                        const int e = nev + __popc(m & lt_mask);
+                        if (code && e < a.ev_cap) {
+                            int *ev = a.events + ((long long)inst * a.ev_cap + e) * 4;
+                            ev[0] = it; ev[1] = b + 1; ev[2] = i; ev[3] = code;
+                        }
+                        nev += __popc(m);
                     }
-                    // events in PV order, as chkLimQ prints them
-                    const unsigned m = __ballot_sync(FULL, code != 0);
-                    const int e = nev + __popc(m & lt_mask);
-                    if (code && e < a.ev_cap) {
-                        int *ev = a.events + ((long long)inst * a.ev_cap + e) * 4;
-                        ev[0] = it; ev[1] = b + 1; ev[2] = i; ev[3] = code;
-                    }
-                    nev += __popc(m);
-                }
-                __syncwarp();
-            }
-            unsigned long long mloc = 0;
-            for (int j = lane; j < n; j += 32) {
-                const int k = G.bus_of_blk[j];
-                const double gp = a.Pliq[off + k] - P[k];
-                const double gq = act[k] ? QL[k] - Q[k] : 0.0;
-                B2 r;
-                r.x = (TJ)gp;
-                r.y = (TJ)gq;
-                ys[j] = r;
-                mloc = umax64(mloc, umax64(abits(gp), abits(gq)));
-            }
-            mloc = warp_umax(mloc);
-            maxG = __longlong_as_double((long long)mloc);
-            if (mloc > kInfBits) { status = GBPF_E_NOCONV; break; }
-            if (mloc <= tol_bits) break;
-            if (it >= a.max_iter) { status = GBPF_E_NOCONV; break; }
-            const B4 *Ub = Uv, *Db = dinv;
-            if (f0) {
-                // the shared factor: forward substitution alone
-                const B4 *facS = (const B4 *)(flat + F.fac);
-                if (*(const int *)(flat + F.sing)) { status = GBPF_E_SINGULAR; break; }
-                for (int l = 0; l < T.nfl; l++) {
-                    fwd_rows<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l] : 0, lane, facS + n, ys);
                     __syncwarp();
                 }
-                Ub = facS + n + T.nup;
-                Db = facS;
-            } else {
-                for (int qq = lane; qq < nq; qq += 32) fac[qq] = jac_block<TJ>(G, qq, n, act, P, Q, V, cs, sn, f32);
-                __syncwarp();
-                // LU fused with forward substitution, level by level, as in
-                // the block kernel with 32 lanes
-                bool sing = false;
-                B2 *zs = (B2 *)(ism + L.zs);
-                for (int l = 0; l < T.nfl; l++) {
-                    const int gp = a.warp_group ? G.lvl_group_w[3 * l] : 0,
-                              ge = a.warp_group ? G.lvl_group_w[3 * l + 1] : 0;
-                    if (a.lu1) {
-                        sing |= lu_level1<TJ, 32>(G, l, gp, ge, a.warp_group ? G.lvl_rot[l] >> 16 : 0, lane, fac, dinv,
-                                                  ys, zs, Lv, Uv);
-                    } else {
-                        sing |= lu_pivots<TJ, 32>(G, l, gp, lane, fac, dinv, ys, Lv, Uv);
+                unsigned long long mloc = 0;
+                for (int j = lane; j < n; j += 32) {
+                    const int k = G.bus_of_blk[j];
+                    const double gp = a.Pliq[off + k] - P[k];
+                    const double gq = act[k] ? QL[k] - Q[k] : 0.0;
+                    B2 r;
+                    r.x = (TJ)gp;
+                    r.y = (TJ)gq;
+                    ys[j] = r;
+                    mloc = umax64(mloc, umax64(abits(gp), abits(gq)));
+                }
+                mloc = warp_umax(mloc);
+                maxG = __longlong_as_double((long long)mloc);
+                if (mloc > kInfBits) { status = GBPF_E_NOCONV; break; }
+                if (mloc <= tol_bits) break;
+                if (it >= mi) { status = GBPF_E_NOCONV; break; }
+                const B4 *Ub = Uv, *Db = dinv;
+                if (f0) {
+                    // the shared factor: forward substitution alone
+                    const B4 *facS = (const B4 *)(flat + F.fac);
+                    if (*(const int *)(flat + F.sing)) { status = GBPF_E_SINGULAR; break; }
+                    for (int l = 0; l < T.nfl; l++) {
+                        fwd_rows<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l] : 0, lane, facS + n, ys);
                         __syncwarp();
-                        lu_entries<TJ, 32>(G, l, ge, lane, dinv, Lv, Uv);
                     }
+                    Ub = facS + n + T.nup;
+                    Db = facS;
+                } else {
+                    for (int qq = lane; qq < nq; qq += 32) fac[qq] = jac_block<TJ>(G, qq, n, act, P, Q, V, cs, sn, f32);
+                    __syncwarp();
+                    // LU fused with forward substitution, level by level, as in
+                    // the block kernel with 32 lanes
+                    bool sing = false;
+                    B2 *zs = (B2 *)(ism + L.zs);
+                    for (int l = 0; l < T.nfl; l++) {
+                        const int gp = a.warp_group ? G.lvl_group_w[3 * l] : 0,
+                                  ge = a.warp_group ? G.lvl_group_w[3 * l + 1] : 0;
+                        if (a.lu1) {
+                            sing |= lu_level1<TJ, 32>(G, l, gp, ge, a.warp_group ? G.lvl_rot[l] >> 16 : 0, lane, fac, dinv,
+                                                      ys, zs, Lv, Uv);
+                        } else {
+                            sing |= lu_pivots<TJ, 32>(G, l, gp, lane, fac, dinv, ys, Lv, Uv);
+                            __syncwarp();
+                            lu_entries<TJ, 32>(G, l, ge, lane, dinv, Lv, Uv);
+                        }
+                        __syncwarp();
+                    }
+                    if (__any_sync(FULL, sing)) { status = GBPF_E_SINGULAR; break; }
+                }
+                for (int l = 0; l < T.nbl; l++) {
+                    back_rows<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l + 2] : 0, lane, Db, Ub, ys);
                     __syncwarp();
                 }
-                if (__any_sync(FULL, sing)) { status = GBPF_E_SINGULAR; break; }
-            }
-            for (int l = 0; l < T.nbl; l++) {
-                back_rows<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l + 2] : 0, lane, Db, Ub, ys);
+                unsigned long long md = 0;
+                for (int j = lane; j < n; j += 32) {
+                    const int k = G.bus_of_blk[j];
+                    const double dt = (double)ys[j].x, dv = (double)ys[j].y;
+                    th[k] += dt;
+                    if (act[k]) V[k] += dv;
+                    if (sizeof(TJ) == 4 && a.rotate) {
+                        double c = cs[k], s = sn[k];
+                        rotate_phasor(th[k], dt, c, s);
+                        cs[k] = c;
+                        sn[k] = s;
+                        ef[k] = make_double2(V[k] * c, V[k] * s);
+                        f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
+                    }
+                    md = umax64(md, umax64(abits(dt), abits(dv)));
+                }
+                maxDx = __longlong_as_double((long long)warp_umax(md));
+                it++;
                 __syncwarp();
             }
-            unsigned long long md = 0;
-            for (int j = lane; j < n; j += 32) {
-                const int k = G.bus_of_blk[j];
-                const double dt = (double)ys[j].x, dv = (double)ys[j].y;
-                th[k] += dt;
-                if (act[k]) V[k] += dv;
-                if (sizeof(TJ) == 4 && a.rotate) {
-                    double c = cs[k], s = sn[k];
-                    rotate_phasor(th[k], dt, c, s);
-                    cs[k] = c;
-                    sn[k] = s;
-                    ef[k] = make_double2(V[k] * c, V[k] * s);
-                    f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
-                }
-                md = umax64(md, umax64(abits(dt), abits(dv)));
-            }
-            maxDx = __longlong_as_double((long long)warp_umax(md));
-            it++;
             __syncwarp();
+            if (parked || !pred) break;
+            // the predicted run: kept, or started again from the own start
+            unsigned long long dv = 0;
+            for (int k = lane; k < nB; k += 32)
+                if (G.type[k] == 0 || G.type[k] == 1) dv = umax64(dv, abits(V[k] - a.Vp[off + k]));
+            const bool fail = status != 0 || warp_umax(dv) > abits(a.warm_max_dv);
+            if (lane == 0) {
+                a.witers[inst] = it;
+                if (fail) a.kind[inst] = 2;
+            }
+            __syncwarp();
+            if (!fail) break;
+            wk = 2;
         }
-        __syncwarp();
         if (parked) continue;
         for (int k = lane; k < nB; k += 32) {
             a.V[off + k] = V[k];
@@ -1304,23 +1354,28 @@ __global__ void k_ws_features(const double *Pliq, const double *Qliq, const doub
 // max |g| of the first Newton iteration: P rows of the non-slack buses, Q rows
 // of the PQ buses, as in k_nr_block / k_nr_warp at iteration 0 -- is below
 // that of the instance's own (flat) start; otherwise the own start is used.
-// Both mismatches come out of one pass over the Ybus rows.  Writes the chosen
-// start to sV/sTh and kind[inst] = 1 (predicted) or 0.  ef holds the phasors
-// (V cos th, V sin th) of both starts, interleaved per bus.
+// The two mismatches only rank the starts, so they are computed in FP32
+// (phasors by sincosf, one pass over the Ybus rows for both starts); the
+// shared flat iteration's P, Q (FP64) stand in for the own start's
+// injections when the instances start from the grid's own state.  Writes
+// the predicted start (FP64) to sV/sTh, kind[inst] = 1 (predicted) or 0,
+// and the instance's queue class (k_ws_order) to cls_out, counted in hist.
+// ef holds the FP32 phasors (V cos th, V sin th) of both starts, per bus.
 constexpr int kSelThreads = 256;
+constexpr int kOrderClasses = 64;
+__device__ __forceinline__ unsigned fabits(float x) { return __float_as_uint(x) & 0x7fffffffu; }
+__device__ __forceinline__ unsigned warp_umax32(unsigned v) { return __reduce_max_sync(0xffffffffu, v); }
 __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *pred, int ldp, const float *omean,
-                                                           const float *oscale, double *sV, double *sTh, double4_32a *ef,
-                                                           int *kind) {
-    __shared__ unsigned long long red[2][kSelThreads / 32];
+                                                           const float *oscale, double *sV, double *sTh, float4 *ef,
+                                                           int *kind, int *cls_out, int *hist) {
+    __shared__ unsigned red[2][kSelThreads / 32];
     const int inst = blockIdx.x, tid = threadIdx.x;
     const Topo T = a.topo[a.inst_topo[inst]];
     const TopoView G = bind(T.o, T.blob);
     const long long off = a.inst_off[inst];
     const int nB = T.nB;
     const float *pr = pred + (size_t)inst * ldp;
-    double4_32a *e = ef + off;
-    // the own (flat) start's injections: the topology's shared iteration 0
-    // when the instances start from the grid's own state, else computed here
+    float4 *e = ef + off;
     const char *flat = (T.flat && a.flat_on && *a.flat_on) ? T.flat : nullptr;
     const FlatLayout F = flat_layout<float>(nB, T.n + 2 * T.nup);  // P, Q offsets do not depend on the precision
     for (int k = tid; k < nB; k += kSelThreads) {
@@ -1330,65 +1385,83 @@ __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *
         const double t = ty == 3 ? t0 : (double)pr[nB + k] * oscale[nB + k] + omean[nB + k];
         sV[off + k] = v;
         sTh[off + k] = t;
-        double s, c, s0 = 0, c0 = 0;
-        sincos(t, &s, &c);
-        if (!flat) sincos(t0, &s0, &c0);
-        e[k] = double4_32a{v * c, v * s, v0 * c0, v0 * s0};
+        float s, c, s0 = 0.f, c0 = 0.f;
+        sincosf((float)t, &s, &c);
+        if (!flat) sincosf((float)t0, &s0, &c0);
+        e[k] = make_float4((float)v * c, (float)v * s, (float)v0 * c0, (float)v0 * s0);
     }
     __syncthreads();
-    unsigned long long mp = 0, mf = 0;
+    unsigned mp = 0, mf = 0;
     for (int k = tid; k < nB; k += kSelThreads) {
         const int ty = G.type[k];
         if (ty == 3) continue;
-        double ir = 0, ii = 0, jr = 0, ji = 0;
+        float ir = 0.f, ii = 0.f, jr = 0.f, ji = 0.f;
         for (int p = G.yptr[k]; p < G.yptr[k + 1]; p++) {
-            const double2 y = G.yval[p];
-            const double4_32a u = e[G.ycol[p]];
-            ir = fma(y.x, u.x, ir);
-            ir = fma(-y.y, u.y, ir);
-            ii = fma(y.x, u.y, ii);
-            ii = fma(y.y, u.x, ii);
+            const double2 yd = G.yval[p];
+            const float yr = (float)yd.x, yi = (float)yd.y;
+            const float4 u = e[G.ycol[p]];
+            ir = fmaf(yr, u.x, fmaf(-yi, u.y, ir));
+            ii = fmaf(yr, u.y, fmaf(yi, u.x, ii));
             if (!flat) {
-                jr = fma(y.x, u.z, jr);
-                jr = fma(-y.y, u.w, jr);
-                ji = fma(y.x, u.w, ji);
-                ji = fma(y.y, u.z, ji);
+                jr = fmaf(yr, u.z, fmaf(-yi, u.w, jr));
+                ji = fmaf(yr, u.w, fmaf(yi, u.z, ji));
             }
         }
-        const double4_32a u = e[k];
+        const float4 u = e[k];
         const double pl = a.Pliq[off + k];
-        const double pf = flat ? ((const double *)(flat + F.P))[k] : fma(u.z, jr, u.w * ji);
-        unsigned long long tp = abits(pl - fma(u.x, ir, u.y * ii)), tf = abits(pl - pf);
+        const float pf = flat ? (float)(pl - ((const double *)(flat + F.P))[k]) : (float)pl - fmaf(u.z, jr, u.w * ji);
+        unsigned tp = fabits((float)pl - fmaf(u.x, ir, u.y * ii)), tf = fabits(pf);
         if (ty == 0 || ty == 1) {
             const double ql = a.Qliq[off + k];
-            const double qf = flat ? ((const double *)(flat + F.Q))[k] : fma(u.w, jr, -u.z * ji);
-            tp = umax64(tp, abits(ql - fma(u.y, ir, -u.x * ii)));
-            tf = umax64(tf, abits(ql - qf));
+            const float qf = flat ? (float)(ql - ((const double *)(flat + F.Q))[k]) : (float)ql - fmaf(u.w, jr, -u.z * ji);
+            tp = max(tp, fabits((float)ql - fmaf(u.y, ir, -u.x * ii)));
+            tf = max(tf, fabits(qf));
         }
-        mp = umax64(mp, tp);
-        mf = umax64(mf, tf);
+        mp = max(mp, tp);
+        mf = max(mf, tf);
     }
-    mp = warp_umax(mp);
-    mf = warp_umax(mf);
+    mp = warp_umax32(mp);
+    mf = warp_umax32(mf);
     if ((tid & 31) == 0) { red[0][tid >> 5] = mp; red[1][tid >> 5] = mf; }
     __syncthreads();
-    mp = red[0][0];
-    mf = red[1][0];
-    for (int w = 1; w < kSelThreads / 32; w++) { mp = umax64(mp, red[0][w]); mf = umax64(mf, red[1][w]); }
-    // NaN patterns order above every number: a NaN predicted mismatch loses
-    const bool use = mp < mf;
-    if (!use)
-        for (int k = tid; k < nB; k += kSelThreads) {
-            sV[off + k] = a.V0[off + k];
-            sTh[off + k] = a.th0[off + k];
-        }
-    if (tid == 0) kind[inst] = use ? 1 : 0;
+    if (tid == 0) {
+        for (int w = 1; w < kSelThreads / 32; w++) { mp = max(mp, red[0][w]); mf = max(mf, red[1][w]); }
+        // NaN patterns order above every number: a NaN predicted mismatch loses
+        const bool use = mp < mf;
+        kind[inst] = use ? 1 : 0;
+        // the queue position class: the chosen start's mismatch, two classes
+        // per binade from 2^-24 up (clamped to 0..kOrderClasses-1; inf and NaN
+        // in the top class)
+        const unsigned key = use ? mp : mf;
+        const int cls = max(0, min(kOrderClasses - 1, (int)(key >> 22) - 2 * (127 - 24)));
+        cls_out[inst] = cls;
+        atomicAdd(&hist[cls], 1);
+    }
 }
 
-// A converged instance that started from the prediction is rejected (kind 3,
-// solved again from its own start) when its |V| lies far from the predicted
-// start: Newton from a poor start can land on another solution of the
-// power-flow equations (a low-voltage one), which the flat start avoids.
+// The work queue of a warm-started launch, by falling start mismatch: the
+// instances expected to take longest (and those likely to fail from the
+// prediction and start again) are claimed first, so that they do not form
+// the launch's tail.  hist[c] counts class c; cursor[] starts zeroed.  The
+// order inside a class is whichever the atomics give: every instance's result
+// is independent of its queue position.
+__global__ void k_ws_order(const int *cls, const int *hist, int *cursor, int n_inst, int *queue) {
+    __shared__ int start[kOrderClasses];
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int c = kOrderClasses - 1; c >= 0; c--) { start[c] = s; s += hist[c]; }
+    }
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_inst; i += gridDim.x * blockDim.x) {
+        const int c = cls[i];
+        queue[start[c] + atomicAdd(&cursor[c], 1)] = i;
+    }
+}
+
+// A converged run from the prediction is rejected (and the instance solved
+// again from its own start) when a PQ bus's |V| lies more than this from the
+// predicted start: Newton from a poor start can land on another solution of
+// the power-flow equations (a low-voltage one), which the flat start avoids.
 // Angles are not compared: a smooth angle offset in the prediction is cheap
 // for Newton to remove and does not signal another solution.
 constexpr double kWarmMaxDV = 0.05;
@@ -1396,20 +1469,6 @@ constexpr double kWarmMaxDV = 0.05;
 // enough to be chosen converges in a handful, and a failing one would
 // otherwise hold its block for no_max_iter iterations before the fallback.
 constexpr int kWarmMaxIter = 10;
-__global__ void k_ws_check(Args a, const double *sV, int *kind) {
-    const int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (inst >= a.n_inst || kind[inst] != 1) return;
-    const Topo T = a.topo[a.inst_topo[inst]];
-    const TopoView G = bind(T.o, T.blob);
-    const long long off = a.inst_off[inst];
-    double dv = 0;
-    for (int k = lane; k < T.nB; k += 32) {
-        const int ty = G.type[k];
-        if (ty == 0 || ty == 1) dv = fmax(dv, fabs(a.V[off + k] - sV[off + k]));
-    }
-    dv = warp_max(dv);
-    if (lane == 0 && !(dv <= kWarmMaxDV)) kind[inst] = 3;
-}
 
 // Owning device allocation (movable, not copyable).
 struct DevBuf {
@@ -1502,6 +1561,10 @@ struct gbpf_batch {
     int max_iter = 100, lim = 0, ev_cap = 16;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // learned warm start: events after the network and after the start
+    // choice, and the last call's phase times (network, choice, Newton)
+    cudaEvent_t wev[2] = {nullptr, nullptr};
+    float warm_ms[3] = {0, 0, 0};
     std::vector<Grid> grids;
     std::vector<YPattern> ys;
     std::vector<Symbolic> syms;
@@ -1539,6 +1602,7 @@ struct gbpf_batch {
         if (graph) cudaGraphDestroy(graph);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        for (auto &e : wev) if (e) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
         if (join) cudaEventDestroy(join);
         for (auto &e : kev) if (e) cudaEventDestroy(e);
@@ -1579,14 +1643,14 @@ struct gbpf_batch {
                               : layout<double>(T.nB, T.n, T.nup, T.nPV, 1, plan.warp_lu1);
         return w.total <= (fp32 ? 40u : 56u) * 1024;
     }
-    // learned warm start (solve_warm): features, prediction, chosen start, fallback queue
+    // learned warm start (solve_warm): features, prediction, chosen start, queue order
     DevBuf warm_mem;
     int warm_n = 0;
     __nv_bfloat16 *wX = nullptr;
     float *wPred = nullptr;
     double *wV = nullptr, *wTh = nullptr;
-    double4_32a *wEF = nullptr;
-    int *wKind = nullptr, *wQueue = nullptr;
+    float4 *wEF = nullptr;
+    int *wKind = nullptr, *wQueue = nullptr, *wIters = nullptr, *wCls = nullptr, *wHist = nullptr;
     gbpf_status launch(cudaStream_t st);
     gbpf_status launch_with(cudaStream_t st, const Args &ba, const Args &wa, bool timed = false);
     gbpf_status build_graph();
@@ -2035,6 +2099,9 @@ gbpf_status gbpf_batch::build_graph() {
     topo_resume.reset();
     wargs.handoff_it = 0;
     if (use_handoff) {
+        // a resumed instance whose predicted start failed starts again from
+        // the shared iteration 0
+        for (size_t t = 0; t < rt.size(); t++) rt[t].flat = topo_h[t].flat;
         CK(cudaMalloc(&topo_resume.p, sizeof(Topo) * rt.size()));
         CK(cudaMemcpy(topo_resume.p, rt.data(), sizeof(Topo) * rt.size(), cudaMemcpyHostToDevice));
         CK(cudaMalloc(&handoff.p, 4 * (size_t)n_warp_q + 256));
@@ -2076,58 +2143,55 @@ gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, 
         warm_mem.reset();
         const size_t xb = align_up(2 * (size_t)n_inst * sh.kin, 256), pb = align_up(4 * (size_t)n_inst * sh.outp, 256),
                      vb = align_up(8 * (size_t)n_bus_total, 256), ib = align_up(4 * (size_t)n_inst, 256);
-        CK(cudaMalloc(&warm_mem.p, xb + pb + 6 * vb + 2 * ib));
+        CK(cudaMalloc(&warm_mem.p, xb + pb + 4 * vb + 4 * ib + 8 * kOrderClasses));
         char *p = (char *)warm_mem.p;
         wX = (__nv_bfloat16 *)p; wPred = (float *)(p + xb);
-        wV = (double *)(p + xb + pb); wTh = (double *)(p + xb + pb + vb); wEF = (double4_32a *)(p + xb + pb + 2 * vb);
-        wKind = (int *)(p + xb + pb + 6 * vb); wQueue = (int *)(p + xb + pb + 6 * vb + ib);
+        p += xb + pb;
+        wV = (double *)p; wTh = (double *)(p + vb); wEF = (float4 *)(p + 2 * vb);
+        p += 4 * vb;
+        wKind = (int *)p; wQueue = (int *)(p + ib); wIters = (int *)(p + 2 * ib); wCls = (int *)(p + 3 * ib);
+        wHist = (int *)(p + 4 * ib);  // class counts, then the order's cursors
         warm_n = n_inst;
     }
     CK(cudaEventRecord(ev0, stream));
+    CK(cudaMemsetAsync(wHist, 0, 8 * kOrderClasses, stream));
     k_ws_features<<<1024, 256, 0, stream>>>(args.Pliq, args.Qliq, args.V0, args.inst_off, n_inst, nB, sh.n_in, sh.kin,
                                             sh.in_mean, sh.in_iscale, wX);
     CK(cudaGetLastError());
     gbpf_status st = gbpf::mlp_infer(m, wX, n_inst, wPred, stream);
     if (st != GBPF_OK) return st;
+    CK(cudaEventRecord(wev[0], stream));
     k_ws_select<<<n_inst, kSelThreads, 0, stream>>>(args, wPred, sh.outp, sh.out_mean, sh.out_scale, wV, wTh, wEF,
-                                                     wKind);
+                                                     wKind, wCls, wHist);
     CK(cudaGetLastError());
+    const int order_blocks = std::min((n_inst + 255) / 256, 1024);
+    k_ws_order<<<order_blocks, 256, 0, stream>>>(wCls, wHist, wHist + kOrderClasses, n_inst, wQueue);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(wev[1], stream));
+    // one launch: predicted starts, own starts, and the restarts of failed
+    // predictions, in the order k_ws_order gave
     Args ba = args, wa = wargs;
-    ba.V0 = wa.V0 = wV;
-    ba.th0 = wa.th0 = wTh;
-    ba.flat_on = wa.flat_on = nullptr;  // predicted starts: no shared iteration 0
-    ba.max_iter = wa.max_iter = std::min(max_iter, kWarmMaxIter);
+    for (Args *x : {&ba, &wa}) {
+        x->kind = wKind;
+        x->witers = wIters;
+        x->Vp = wV;
+        x->thp = wTh;
+        x->warm_max_iter = std::min(max_iter, kWarmMaxIter);
+        x->warm_max_dv = kWarmMaxDV;
+    }
+    (wa.queue_len ? wa.queue : ba.queue) = wQueue;
     if ((st = launch_with(stream, ba, wa)) != GBPF_OK) return st;
-    k_ws_check<<<(n_inst * 32 + 255) / 256, 256, 0, stream>>>(args, wV, wKind);
-    CK(cudaGetLastError());
-    std::vector<int> kind(n_inst), status(n_inst), iters(n_inst);
+    std::vector<int> kind(n_inst), witers(n_inst);
     CK(cudaMemcpyAsync(kind.data(), wKind, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
-    CK(cudaMemcpyAsync(status.data(), args.status, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
-    CK(cudaMemcpyAsync(iters.data(), args.iters, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
-    std::vector<int> fw, fb;
-    for (int i = 0; i < n_inst; i++) {
-        if (witers_out) witers_out[i] = kind[i] ? iters[i] : 0;
-        if (kind[i] == 3 || (kind[i] == 1 && status[i] != GBPF_OK)) {
-            kind[i] = 2;
-            (topo_warp[inst_topo[i]] ? fw : fb).push_back(i);
-        }
-    }
-    if (!fw.empty() || !fb.empty()) {
-        // the fallback: the same launch from the instances' own starts
-        if (!fw.empty()) CK(cudaMemcpyAsync(wQueue, fw.data(), 4 * fw.size(), cudaMemcpyHostToDevice, stream));
-        if (!fb.empty())
-            CK(cudaMemcpyAsync(wQueue + fw.size(), fb.data(), 4 * fb.size(), cudaMemcpyHostToDevice, stream));
-        Args bf = args, wf = wargs;
-        wf.queue = wQueue;
-        wf.queue_len = (int)fw.size();
-        bf.queue = wQueue + fw.size();
-        bf.queue_len = (int)fb.size();
-        if ((st = launch_with(stream, bf, wf)) != GBPF_OK) return st;
-    }
+    if (witers_out) CK(cudaMemcpyAsync(witers.data(), wIters, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
     CK(cudaEventRecord(ev1, stream));
     CK(cudaEventSynchronize(ev1));
     if (ms) CK(cudaEventElapsedTime(ms, ev0, ev1));
+    CK(cudaEventElapsedTime(&warm_ms[0], ev0, wev[0]));
+    CK(cudaEventElapsedTime(&warm_ms[1], wev[0], wev[1]));
+    CK(cudaEventElapsedTime(&warm_ms[2], wev[1], ev1));
+    if (witers_out)
+        for (int i = 0; i < n_inst; i++) witers_out[i] = kind[i] ? witers[i] : 0;
     if (kind_out) std::copy(kind.begin(), kind.end(), kind_out);
     return GBPF_OK;
 }
@@ -2297,6 +2361,7 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
     CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&b->ev0));
     CK(cudaEventCreate(&b->ev1));
+    for (auto &e : b->wev) CK(cudaEventCreate(&e));
     CK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
@@ -2548,6 +2613,12 @@ extern "C" gbpf_status gbpf_batch_solve_warm(gbpf_batch *b, gbpf_mlp *m, int *st
     gbpf_status st = b->solve_warm(m, start_kind, warm_iterations, &t);
     if (ms) *ms = t;
     return st;
+}
+
+extern "C" gbpf_status gbpf_batch_warm_phases(const gbpf_batch *b, double ms[3]) {
+    ARGCHECK(b && ms);
+    for (int i = 0; i < 3; i++) ms[i] = b->warm_ms[i];
+    return GBPF_OK;
 }
 
 extern "C" gbpf_status gbpf_batch_info(const gbpf_batch *b, long long info[8]) {

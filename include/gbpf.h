@@ -480,16 +480,23 @@ gbpf_status gbpf_mlp_set_norm(gbpf_mlp *m, const float *in_mean, const float *in
  * initial mismatch is smaller than that of the instance's own start
  * (V0/theta0 of gbpf_batch_set_instances, by default the flat start), else
  * from its own start.  Instances whose predicted start does not converge are
- * solved again from their own start.  Results as for gbpf_batch_solve
- * (gbpf_batch_results).  start_kind[i] (may be NULL): 0 own start chosen up
+ * solved again from their own start, in the same launch.  Instances are
+ * served in order of falling start mismatch.  Results as for
+ * gbpf_batch_solve (gbpf_batch_results); an instance on its own start gets
+ * no_max_iter iterations.  start_kind[i] (may be NULL): 0 own start chosen up
  * front, 1 predicted start converged, 2 predicted start failed (no
  * convergence within min(no_max_iter, 10) iterations, or a solution whose
  * |V| lies more than 0.05 p.u. from the prediction) and was replaced;
  * warm_iterations[i] (may be NULL): iterations of the predicted-start
  * attempt (0 when not attempted); *ms (may be NULL): device time of the whole
- * sequence, the fallback decision included. */
+ * sequence, network inference included. */
 gbpf_status gbpf_batch_solve_warm(gbpf_batch *b, gbpf_mlp *m, int *start_kind, int *warm_iterations,
                                   double *ms);
+
+/* Device time of the last gbpf_batch_solve_warm by phase: ms[0] the network
+ * (features and inference), ms[1] the start choice and the queue order, ms[2]
+ * the Newton launch (restarts included).  Zeros before the first call. */
+gbpf_status gbpf_batch_warm_phases(const gbpf_batch *b, double ms[3]);
 
 /* info[0..7] = topologies, instances, packed buses, resident thread blocks,
  * dynamic shared memory per block of the block-per-instance kernel,

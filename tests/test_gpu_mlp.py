@@ -13,7 +13,10 @@
 * Training on the GPU reduces the loss.
 * What the trained network gains: batched Newton from the predicted start
   needs fewer iterations than from the flat start, on held-out scenarios,
-  and converges to the same solution (|V|, theta within 1e-6)."""
+  and converges to the same solution (|V|, theta within 1e-6).
+* Instances of a warm-started launch that run from their own start (chosen
+  up front, or after a failed predicted run, restarted in the same launch)
+  match the flat-start solve bit for bit, non-converging ones included."""
 import numpy as np
 import pytest
 
@@ -141,22 +144,21 @@ def _scenarios(base, n, rng):
     return base["Pload"] * lf, base["Qload"] * lf, base["Pg"] * gf
 
 
-def test_warm_start_saves_iterations(gb):
+@pytest.fixture(scope="module")
+def warm_net(gb):
+    """A 118-bus grid and a network trained on 4,096 of its solved load
+    scenarios (loss: the squared linearised mismatch of the predicted start
+    plus 1 % MSE)."""
     grid = gb.generate(2, 20261205)
     base = grid.buses()
     nB = grid.nB
     rng = np.random.default_rng(5)
-    opts = dict(tolerancia=1e-8, no_max_iter=30, lim_inj_reat=0)
-    solver = gb.Batch([grid], precision=gb.PREC_FP64, **opts)
-
-    def solve(Pl, Ql, Pg):
-        n = len(Pl)
-        solver.set_instances(np.zeros(n, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
-        solver.solve()
-        return solver.results()
-
+    solver = gb.Batch([grid], precision=gb.PREC_FP64, tolerancia=1e-8, no_max_iter=30, lim_inj_reat=0)
     Pl, Ql, Pg = _scenarios(base, 4096, rng)
-    r = solve(Pl, Ql, Pg)
+    solver.set_instances(np.zeros(len(Pl), np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
+    solver.solve()
+    r = solver.results()
+    solver.close()
     ok = r["status"] == 0
     assert ok.mean() > 0.95
     V, th = r["V"].reshape(-1, nB)[ok], r["theta"].reshape(-1, nB)[ok]
@@ -164,11 +166,26 @@ def test_warm_start_saves_iterations(gb):
     Y = np.concatenate([V, th], axis=1)
     m = gb.MLP(3 * nB, 2 * nB, width=256, n_layers=3, seed=5)
     m.set_data(X, Y)
-    # loss = squared linearised mismatch of the predicted start (+ 1 % MSE)
     plain = gb.Solver(grid, tolerancia=1e-8, no_max_iter=30, lim_inj_reat=0)
     M = gb.warm_loss_metric(plain, V.mean(0), th.mean(0), m.norm()["out_scale"])
     m.set_loss_metric(M, 0.01)
     loss, _ = m.train(40, batch=128, lr=1e-3, lr_final=1e-5, seed=5)
+    return grid, m, loss
+
+
+def test_warm_start_saves_iterations(gb, warm_net):
+    grid, m, loss = warm_net
+    base = grid.buses()
+    nB = grid.nB
+    rng = np.random.default_rng(55)
+    solver = gb.Batch([grid], precision=gb.PREC_FP64, tolerancia=1e-8, no_max_iter=30, lim_inj_reat=0)
+
+    def solve(Pl, Ql, Pg):
+        n = len(Pl)
+        solver.set_instances(np.zeros(n, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
+        solver.solve()
+        return solver.results()
+
     assert loss[-1] < 0.05 * loss[0]
     # held-out scenarios: flat start, then the learned start
     Pl, Ql, Pg = _scenarios(base, 512, rng)
@@ -188,3 +205,59 @@ def test_warm_start_saves_iterations(gb):
     it_flat = flat["iterations"][both].mean()
     it_warm = (warm["iterations"] + np.where(kind == 2, w["warm_iterations"], 0))[both].mean()
     assert it_warm < it_flat - 0.5, (it_warm, it_flat)
+
+
+@pytest.mark.parametrize("prec", ["PREC_FP64", "PREC_FP32_IR"])
+def test_warm_start_own_start_runs_match_flat_start(gb, warm_net, prec):
+    """Instances that run from their own start in a warm-started launch -- the
+    ones whose prediction was not chosen (start kind 0) and the ones whose
+    predicted run failed and started again in the same launch (kind 2) -- give
+    exactly what the flat-start solve gives: iterations (no_max_iter for the
+    non-converging), status, switch events, |V| and theta bit for bit.  The
+    network is the one of test_warm_start_saves_iterations; reactive limits
+    are on, and a fifth of the scenarios are loaded past the point where
+    Newton converges."""
+    grid, m, _ = warm_net
+    base = grid.buses()
+    nB = grid.nB
+    rng = np.random.default_rng(6)
+    opts = dict(tolerancia=1e-8, no_max_iter=30, lim_inj_reat=1)
+    solver = gb.Batch([grid], precision=getattr(gb, prec), **opts)
+    Pl, Ql, Pg = _scenarios(base, 256, rng)
+    heavy = rng.uniform(1.8, 2.6, (64, nB))
+    Pl = np.concatenate([Pl, base["Pload"] * heavy])
+    Ql = np.concatenate([Ql, base["Qload"] * heavy])
+    Pg = np.concatenate([Pg, np.tile(base["Pg"], (64, 1))])
+    order = rng.permutation(len(Pl))
+    Pl, Ql, Pg = Pl[order], Ql[order], Pg[order]
+    n = len(Pl)
+    solver.set_instances(np.zeros(n, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
+    solver.solve()
+    flat = solver.results()
+    ev_flat = [solver.events(i) for i in range(n)]
+    ok = flat["status"] == 0
+    assert 0 < (~ok).sum() < n // 2
+    w = solver.solve_warm(m)
+    warm = solver.results()
+    kind = w["start_kind"]
+    own = kind != 1
+    assert own.any() and (kind == 1).any()
+    # some non-converging scenario ran from its own start for all no_max_iter iterations
+    assert (own & ~ok).any()
+    sel = np.repeat(own, nB)
+    for k in ("iterations", "status", "n_events"):
+        np.testing.assert_array_equal(warm[k][own], flat[k][own], err_msg=k)
+    np.testing.assert_array_equal(warm["V"][sel], flat["V"][sel])
+    np.testing.assert_array_equal(warm["theta"][sel], flat["theta"][sel])
+    for i in np.flatnonzero(own):
+        np.testing.assert_array_equal(solver.events(i), ev_flat[i])
+    assert np.all(w["warm_iterations"][kind == 0] == 0)
+    assert np.all((w["warm_iterations"][kind == 2] >= 1) & (w["warm_iterations"][kind == 2] <= 10))
+    # the predicted runs that were kept converged; without limit switches on
+    # either path, to the flat start's solution
+    assert np.all(warm["status"][kind == 1] == 0)
+    kept = (kind == 1) & ok & (flat["n_events"] == 0) & (warm["n_events"] == 0)
+    assert kept.any()
+    s1 = np.repeat(kept, nB)
+    assert np.max(np.abs(warm["V"][s1] - flat["V"][s1])) <= 1e-6
+    assert np.max(np.abs(warm["theta"][s1] - flat["theta"][s1])) <= 1e-6
