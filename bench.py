@@ -355,7 +355,8 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     twin.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
     pl = fast.plan()
     twin.set_plan(**{k: pl[k] for k in ("warp_mode", "warps_per_block", "handoff_it", "resume_group",
-                                        "warp_group", "narrow", "lu1", "warp_lu1", "flat_shared", "rotate")})
+                                        "warp_group", "narrow", "lu1", "warp_lu1", "flat_shared", "rotate",
+                                        "gstate")})
     twin.solve()
     assert np.array_equal(twin.results(state=False)["status"], r["status"])
     pair = [fast, twin]

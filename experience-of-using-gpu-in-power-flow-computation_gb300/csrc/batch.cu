@@ -214,6 +214,10 @@ struct Args {
     const double *Vp, *thp;
     int warm_max_iter;
     double warm_max_dv;
+    // block kernel with its state in global memory (layout gs): the region of
+    // block b starts at gstate + b * gstate_stride
+    unsigned char *gstate;
+    long long gstate_stride;
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
@@ -221,21 +225,39 @@ __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a -
 // Shared-memory layout of one instance (state + optionally the factor).
 struct Layout {
     size_t V, th, cs, sn, ef, f32, P, Q, QL, act, lim, ys, zs, fac, total;
+    size_t gtotal;  // bytes of the global state region (gs)
 };
 // with_zs: room for z = D^-1 y of the one-pass levels (lu_level1).  The
 // inverse of diagonal block j overwrites fac[j] once the block is factored.
+// gs: the per-bus arrays that no thread reads for another bus's row -- theta,
+// P, Q, QL and, in the FP32-LU form (whose Jacobian reads the FP32 copies),
+// V, cos, sin -- live in a per-block region of global memory (offsets from
+// its start, gtotal bytes; L2-resident) instead of shared memory, which
+// halves the shared memory of an instance.
 template <typename TJ>
-__host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fac_smem, int with_zs) {
+__host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fac_smem, int with_zs, int gs = 0) {
     using B4 = typename Blk<TJ>::b4;
     using B2 = typename Blk<TJ>::b2;
+    constexpr bool f32_form = sizeof(TJ) == 4;
     Layout L;
-    size_t o = 0;
+    size_t o = 0, og = 0;
     auto take = [&](size_t bytes, size_t al) { o = align_up(o, al); size_t r = o; o += bytes; return r; };
-    L.V = take(8 * nB, 16); L.th = take(8 * nB, 16); L.cs = take(8 * nB, 16); L.sn = take(8 * nB, 16);
+    auto takeg = [&](size_t bytes, size_t al) {
+        if (!gs) return take(bytes, al);
+        og = align_up(og, al);
+        size_t r = og;
+        og += bytes;
+        return r;
+    };
+    L.V = f32_form ? takeg(8 * nB, 16) : take(8 * nB, 16);
+    L.th = takeg(8 * nB, 16);
+    L.cs = f32_form ? takeg(8 * nB, 16) : take(8 * nB, 16);
+    L.sn = f32_form ? takeg(8 * nB, 16) : take(8 * nB, 16);
     // e = V cos th, f = V sin th (FP64); cos, sin, V in FP32 for the FP32-LU form's Jacobian
     L.ef = take(16 * (size_t)nB, 16);
-    L.f32 = take(sizeof(TJ) == 4 ? 16 * (size_t)nB : 0, 16);
-    L.P = take(8 * nB, 16); L.Q = take(8 * nB, 16); L.QL = take(8 * nB, 16);
+    L.f32 = take(f32_form ? 16 * (size_t)nB : 0, 16);
+    L.P = takeg(8 * nB, 16); L.Q = takeg(8 * nB, 16); L.QL = takeg(8 * nB, 16);
+    L.gtotal = align_up(og, 256);
     L.act = take(nB, 16); L.lim = take(4 * (size_t)(nPV + 1), 16);
     // ys: the mismatch, then (forward) the substituted right-hand side, then
     // (backward, in place) the Newton step
@@ -693,13 +715,13 @@ __device__ __forceinline__ bool lu_level1(const TopoView &G, int l, int lgp, int
     return sing;
 }
 
-template <typename TJ>
+template <typename TJ, bool GS>
 __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
     using B4 = typename Blk<TJ>::b4;
     using B2 = typename Blk<TJ>::b2;
     extern __shared__ __align__(32) unsigned char smem[];
     __shared__ unsigned long long red[kWarps];
-    __shared__ int s_inst, s_done, s_status, s_it, s_nev, s_topo;
+    __shared__ int s_inst, s_done, s_status, s_it, s_nev, s_topo, s_wcnt[kWarps];
     __shared__ double s_maxG, s_maxDx;
     const unsigned long long tol_bits = abits(a.tol), tol10_bits = abits(a.tol * 10.);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -730,12 +752,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
         }
         const TopoView G = bind(T.o, blob);
         const long long off = a.inst_off[inst];
-        const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, T.fac_smem, a.lu1);
-        double *V = (double *)(ism + L.V), *th = (double *)(ism + L.th);
-        double *cs = (double *)(ism + L.cs), *sn = (double *)(ism + L.sn);
+        const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, T.fac_smem, a.lu1, GS);
+        // the state arrays layout() moves to global memory (GS)
+        unsigned char *gst = GS ? a.gstate + (long long)blockIdx.x * a.gstate_stride : ism;
+        unsigned char *vst = (GS && sizeof(TJ) == 4) ? gst : ism;
+        double *V = (double *)(vst + L.V), *th = (double *)(gst + L.th);
+        double *cs = (double *)(vst + L.cs), *sn = (double *)(vst + L.sn);
         double2 *ef = (double2 *)(ism + L.ef);
         float4 *f32 = (float4 *)(ism + L.f32);
-        double *P = (double *)(ism + L.P), *Q = (double *)(ism + L.Q), *QL = (double *)(ism + L.QL);
+        double *P = (double *)(gst + L.P), *Q = (double *)(gst + L.Q), *QL = (double *)(gst + L.QL);
         unsigned char *act = ism + L.act;
         int *limQ = (int *)(ism + L.lim);
         B2 *ys = (B2 *)(ism + L.ys);
@@ -808,32 +833,44 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
                 const int it = s_it;
                 // reactive limits (chkLimQ) when the previous step was small
                 if (a.lim && it >= 1 && it < mi && abits(s_maxDx) < tol10_bits) {
-                    for (int i = tid; i < T.nPV; i += kThreads) {
-                        const int b = G.pv_bus[i];
-                        const double ql = a.Qload[off + b], qg = Q[b] + ql;
-                        int code = 0;
-                        if (qg < G.Qmin[i] - a.tol) {
-                            if (!limQ[i]) code = 1;
-                            else if (QL[b] != G.Qmin[i] - ql) code = 2;
-                            limQ[i] = 1;
-                            QL[b] = G.Qmin[i] - ql;
-                        } else if (qg > G.Qmax[i] + a.tol) {
-                            if (!limQ[i]) code = 3;
-                            else if (QL[b] != G.Qmax[i] - ql) code = 4;
-                            limQ[i] = 1;
-                            QL[b] = G.Qmax[i] - ql;
-                        } else {
-                            if (limQ[i]) code = 5;
-                            limQ[i] = 0;
-                        }
-                        act[b] = limQ[i];
-                        if (code) {
-                            const int e = atomicAdd(&s_nev, 1);
-                            if (e < a.ev_cap) {
-                                int *ev = a.events + ((long long)inst * a.ev_cap + e) * 4;
-                                ev[0] = it; ev[1] = b + 1; ev[2] = i; ev[3] = code;
+                    for (int i0 = 0; i0 < T.nPV; i0 += kThreads) {
+                        const int i = i0 + tid;
+                        int code = 0, b = 0;
+                        if (i < T.nPV) {
+                            b = G.pv_bus[i];
+                            const double ql = a.Qload[off + b], qg = Q[b] + ql;
+                            if (qg < G.Qmin[i] - a.tol) {
+                                if (!limQ[i]) code = 1;
+                                else if (QL[b] != G.Qmin[i] - ql) code = 2;
+                                limQ[i] = 1;
+                                QL[b] = G.Qmin[i] - ql;
+                            } else if (qg > G.Qmax[i] + a.tol) {
+                                if (!limQ[i]) code = 3;
+                                else if (QL[b] != G.Qmax[i] - ql) code = 4;
+                                limQ[i] = 1;
+                                QL[b] = G.Qmax[i] - ql;
+                            } else {
+                                if (limQ[i]) code = 5;
+                                limQ[i] = 0;
                             }
+                            act[b] = limQ[i];
                         }
+                        // events in PV order, as chkLimQ prints them: a
+                        // block-wide exclusive count of the events before i
+                        const unsigned m = __ballot_sync(0xffffffffu, code != 0);
+                        if (lane == 0) s_wcnt[warp] = __popc(m);
+                        __syncthreads();
+                        int e = s_nev + __popc(m & ((1u << lane) - 1u)), tot = 0;
+                        for (int w = 0; w < kWarps; w++) {
+                            if (w < warp) e += s_wcnt[w];
+                            tot += s_wcnt[w];
+                        }
+                        if (code && e < a.ev_cap) {
+                            int *ev = a.events + ((long long)inst * a.ev_cap + e) * 4;
+                            ev[0] = it; ev[1] = b + 1; ev[2] = i; ev[3] = code;
+                        }
+                        __syncthreads();
+                        if (tid == 0) s_nev += tot;
                     }
                     __syncthreads();
                 }
@@ -1624,11 +1661,16 @@ struct gbpf_batch {
     // lets the warp kernel's instances take the shared iteration 0 of their
     // topology when they start from the grid's own state (k_flat_start);
     // rotate = 1 updates the FP32-LU form's phasors by rotation instead of a
-    // sincos per iteration (measured slower on GB300, kept as a knob).
+    // sincos per iteration (measured slower on GB300, kept as a knob);
+    // gstate = 1 lets the block kernel keep part of its state in global
+    // memory (layout gs) where that fits more instances per SM or moves
+    // factors into shared memory, 2 wherever it fits, 0 never.
     struct Plan {
         int warp_mode = 1, warp_warps = 8, handoff_it = kHandoffIt, resume_group = 1, warp_group = 1, narrow = 0,
-            lu1 = 1, warp_lu1 = 0, flat_shared = 1, rotate = 0;
+            lu1 = 1, warp_lu1 = 0, flat_shared = 1, rotate = 0, gstate = 1;
     } plan;
+    bool block_gs = false;  // the block-mode launch keeps its state in global memory
+    DevBuf gstate_mem;
     gbpf_status rebuild() {
         CK(cudaStreamSynchronize(stream));
         if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
@@ -1887,8 +1929,13 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
         CK(cudaEventRecord(fork, st));
         CK(cudaStreamWaitEvent(side, fork, 0));
         if (timed) CK(cudaEventRecordWithFlags(kev[0], side, cudaEventRecordExternal));
-        if (fp32) k_nr_block<float><<<grid_blocks, kThreads, smem, side>>>(ba);
-        else k_nr_block<double><<<grid_blocks, kThreads, smem, side>>>(ba);
+        if (fp32) {
+            if (block_gs) k_nr_block<float, true><<<grid_blocks, kThreads, smem, side>>>(ba);
+            else k_nr_block<float, false><<<grid_blocks, kThreads, smem, side>>>(ba);
+        } else {
+            if (block_gs) k_nr_block<double, true><<<grid_blocks, kThreads, smem, side>>>(ba);
+            else k_nr_block<double, false><<<grid_blocks, kThreads, smem, side>>>(ba);
+        }
         CK(cudaGetLastError());
         if (timed) CK(cudaEventRecordWithFlags(kev[1], side, cudaEventRecordExternal));
     }
@@ -1910,8 +1957,8 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
             ra.counter = args.counter + 2;
             ra.topo = (const Topo *)topo_resume.p;
             ra.blob_region = resume_region;
-            if (fp32) k_nr_block<float><<<resume_grid, kThreads, resume_smem, st>>>(ra);
-            else k_nr_block<double><<<resume_grid, kThreads, resume_smem, st>>>(ra);
+            if (fp32) k_nr_block<float, false><<<resume_grid, kThreads, resume_smem, st>>>(ra);
+            else k_nr_block<double, false><<<resume_grid, kThreads, resume_smem, st>>>(ra);
             CK(cudaGetLastError());
             if (timed) CK(cudaEventRecordWithFlags(kev[4], st, cudaEventRecordExternal));
         }
@@ -1953,27 +2000,65 @@ gbpf_status gbpf_batch::build_graph() {
     // Block-mode shared-memory plan: the blob is staged in shared memory when
     // at most 48 KB; the factor stays in shared memory when blob region +
     // state + factor fit in 110 KB, otherwise it lives in global scratch.
+    // With plan.gstate the plan is also made with part of the state in global
+    // memory (layout gs), and that one is taken when it fits more blocks per
+    // SM, or as many with more factors in shared memory.
     const size_t budget = 110 * 1024, blob_cap = 48 * 1024;
-    size_t region = 0, need = 0, scr = 0;
+    size_t region = 0;
     for (size_t t = 0; t < topo_h.size(); t++) {
         Topo &T = topo_h[t];
         T.blob_smem = !warp_ok[t] && (size_t)T.blob_bytes <= blob_cap;
         if (T.blob_smem) region = std::max(region, align_up((size_t)T.blob_bytes, 32));
     }
-    for (size_t t = 0; t < topo_h.size(); t++) {
-        Topo &T = topo_h[t];
-        if (warp_ok[t]) { T.fac_smem = 1; continue; }
-        const int z = plan.lu1;
-        Layout with = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1, z) : layout<double>(T.nB, T.n, T.nup, T.nPV, 1, z);
-        Layout without =
-            fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 0, z) : layout<double>(T.nB, T.n, T.nup, T.nPV, 0, z);
-        if (region + with.total <= budget) { T.fac_smem = 1; need = std::max(need, with.total); }
-        else {
-            T.fac_smem = 0;
-            need = std::max(need, without.total);
-            scr = std::max(scr, fp32 ? scratch_bytes<float>(T.n, T.nup) : scratch_bytes<double>(T.n, T.nup));
+    auto blk_fn = [&](bool gs) -> const void * {
+        if (fp32) return gs ? (const void *)k_nr_block<float, true> : (const void *)k_nr_block<float, false>;
+        return gs ? (const void *)k_nr_block<double, true> : (const void *)k_nr_block<double, false>;
+    };
+    struct BlockPlan {
+        size_t need = 0, scr = 0, gst = 0;
+        std::vector<int> fac;
+        int nfac = 0, occ = 0;
+    };
+    auto plan_blocks = [&](int gs, BlockPlan &bp) -> gbpf_status {
+        bp.fac.assign(topo_h.size(), 1);
+        for (size_t t = 0; t < topo_h.size(); t++) {
+            if (warp_ok[t]) continue;
+            const Topo &T = topo_h[t];
+            const int z = plan.lu1;
+            const Layout with = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1, z, gs)
+                                     : layout<double>(T.nB, T.n, T.nup, T.nPV, 1, z, gs);
+            const Layout without = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 0, z, gs)
+                                        : layout<double>(T.nB, T.n, T.nup, T.nPV, 0, z, gs);
+            bp.gst = std::max(bp.gst, with.gtotal);
+            if (region + with.total <= budget) {
+                bp.nfac++;
+                bp.need = std::max(bp.need, with.total);
+            } else {
+                bp.fac[t] = 0;
+                bp.need = std::max(bp.need, without.total);
+                bp.scr = std::max(bp.scr, fp32 ? scratch_bytes<float>(T.n, T.nup) : scratch_bytes<double>(T.n, T.nup));
+            }
+        }
+        const size_t sm = bp.need + region;
+        if (!n_block_q || sm > (size_t)maxsm) return GBPF_OK;
+        CK(cudaFuncSetAttribute(blk_fn(gs), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bp.occ, blk_fn(gs), kThreads, sm));
+        return GBPF_OK;
+    };
+    BlockPlan bp, bg;
+    gbpf_status pst = plan_blocks(0, bp);
+    if (pst != GBPF_OK) return pst;
+    block_gs = false;
+    if (plan.gstate && n_block_q) {
+        if ((pst = plan_blocks(1, bg)) != GBPF_OK) return pst;
+        if ((plan.gstate == 2 && bg.occ > 0) || bg.occ > bp.occ ||
+            (bg.occ == bp.occ && bg.occ > 0 && bg.nfac > bp.nfac)) {
+            bp = bg;
+            block_gs = true;
         }
     }
+    for (size_t t = 0; t < topo_h.size(); t++) topo_h[t].fac_smem = bp.fac[t];
+    const size_t need = bp.need, scr = bp.scr;
     args.blob_region = (int)region;
     smem = n_block_q ? need + region : 0;
     if (smem > (size_t)maxsm) { set_error("instance state does not fit in shared memory"); return GBPF_E_UNSUPPORTED; }
@@ -2004,23 +2089,28 @@ gbpf_status gbpf_batch::build_graph() {
     grid_blocks = 0;
     resume_grid = 0;
     {
-        const size_t attr = std::max(smem, use_handoff ? resume_smem : 0);
-        if (attr) {
-            if (fp32) CK(cudaFuncSetAttribute(k_nr_block<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)attr));
-            else CK(cudaFuncSetAttribute(k_nr_block<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)attr));
-        }
+        // the resume launch always keeps its state in shared memory
+        size_t attr_sm = use_handoff ? resume_smem : 0;
+        if (!block_gs) attr_sm = std::max(attr_sm, smem);
+        if (attr_sm) CK(cudaFuncSetAttribute(blk_fn(false), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)attr_sm));
+        if (block_gs) CK(cudaFuncSetAttribute(blk_fn(true), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
     if (n_block_q) {
         int occ = 0;
-        if (fp32) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float>, kThreads, smem));
-        else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double>, kThreads, smem));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, blk_fn(block_gs), kThreads, smem));
         grid_blocks = std::max(1, std::min(n_block_q, dev_sm * std::max(occ, 1)));
     }
     if (use_handoff) {
         int occ = 0;
-        if (fp32) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float>, kThreads, resume_smem));
-        else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double>, kThreads, resume_smem));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, blk_fn(false), kThreads, resume_smem));
         resume_grid = std::max(1, std::min(n_warp_q, dev_sm * std::max(occ, 1)));
+    }
+    gstate_mem.reset();
+    args.gstate = nullptr;
+    args.gstate_stride = block_gs ? (long long)align_up(bp.gst, 256) : 0;
+    if (block_gs) {
+        CK(cudaMalloc(&gstate_mem.p, (size_t)args.gstate_stride * grid_blocks));
+        args.gstate = (unsigned char *)gstate_mem.p;
     }
     // warp-mode plan: as many warps per block as fit in the block's shared
     // memory, at most 16 (one block per SM; 128 registers a thread)
@@ -2236,24 +2326,28 @@ gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
     if (first_ms) *first_ms = cur_ms;
     bool any_warp = false;
     for (const Topo &T : topo_h) any_warp |= warp_fits(T);
-    struct Knob { int Plan::*field; std::vector<int> values; bool needs_warp, needs_handoff; };
+    bool any_block = false;  // some topology runs on k_nr_block in warp mode too
+    for (const Topo &T : topo_h) any_block |= !warp_fits(T);
+    struct Knob { int Plan::*field; std::vector<int> values; bool needs_warp, needs_handoff, needs_block; };
     const std::vector<Knob> knobs = {
-        {&Plan::warp_mode, {1, 0}, false, false},
-        {&Plan::warp_group, {1, 0}, true, false},
-        {&Plan::warp_warps, {8, 0, 6, 4}, true, false},
-        {&Plan::handoff_it, {kHandoffIt, 6, 8, 16, 24, 0}, true, false},
-        {&Plan::resume_group, {1, 0}, true, true},
-        {&Plan::narrow, {1, 0}, false, false},
-        {&Plan::lu1, {1, 0}, false, false},
-        {&Plan::warp_lu1, {0, 1}, true, false},
-        {&Plan::flat_shared, {1, 0}, true, false},
-        {&Plan::rotate, {0, 1}, false, false},
+        {&Plan::warp_mode, {1, 0}, false, false, false},
+        {&Plan::warp_group, {1, 0}, true, false, false},
+        {&Plan::warp_warps, {8, 0, 6, 4}, true, false, false},
+        {&Plan::handoff_it, {kHandoffIt, 6, 8, 16, 24, 0}, true, false, false},
+        {&Plan::resume_group, {1, 0}, true, true, false},
+        {&Plan::narrow, {1, 0}, false, false, false},
+        {&Plan::lu1, {1, 0}, false, false, false},
+        {&Plan::warp_lu1, {0, 1}, true, false, false},
+        {&Plan::flat_shared, {1, 0}, false, false, false},
+        {&Plan::rotate, {0, 1}, false, false, false},
+        {&Plan::gstate, {1, 0}, false, false, true},
     };
     for (int sweep = 0; sweep < 2; sweep++) {
         bool changed = false;
         for (const Knob &k : knobs) {
             if (k.needs_warp && (!any_warp || !cur.warp_mode)) continue;
             if (k.needs_handoff && cur.handoff_it == 0) continue;
+            if (k.needs_block && !any_block && cur.warp_mode) continue;
             if (k.field == &Plan::warp_mode && !any_warp) continue;
             const int start = cur.*(k.field);
             for (int v : k.values) {
@@ -2285,10 +2379,12 @@ static void plan_out(const gbpf_batch *b, int plan[16]) {
     plan[7] = b->plan.warp_lu1;
     plan[8] = b->plan.flat_shared;
     plan[9] = b->plan.rotate;
-    plan[10] = b->warp_warps;  // warps per block in use
-    plan[11] = b->n_warp_q;
-    plan[12] = b->n_block_q;
-    for (int i = 13; i < 16; i++) plan[i] = 0;
+    plan[10] = b->plan.gstate;
+    plan[11] = b->warp_warps;  // warps per block in use
+    plan[12] = b->n_warp_q;
+    plan[13] = b->n_block_q;
+    plan[14] = b->block_gs;
+    plan[15] = 0;
 }
 
 extern "C" gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[16]) {
@@ -2297,11 +2393,11 @@ extern "C" gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[16]) {
     return GBPF_OK;
 }
 
-extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[10]) {
+extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[11]) {
     ARGCHECK(b && plan && (plan[0] == 0 || plan[0] == 1) && plan[1] >= 0 && plan[1] <= kWarpsMax && plan[2] >= 0 &&
              (plan[3] == 0 || plan[3] == 1) && (plan[4] == 0 || plan[4] == 1) && (plan[5] == 0 || plan[5] == 1) &&
              (plan[6] == 0 || plan[6] == 1) && (plan[7] == 0 || plan[7] == 1) && (plan[8] == 0 || plan[8] == 1) &&
-             (plan[9] == 0 || plan[9] == 1));
+             (plan[9] == 0 || plan[9] == 1) && plan[10] >= 0 && plan[10] <= 2);
     CK(cudaSetDevice(b->device));
     b->plan.warp_mode = plan[0];
     b->plan.warp_warps = plan[1];
@@ -2313,6 +2409,7 @@ extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[10]) {
     b->plan.warp_lu1 = plan[7];
     b->plan.flat_shared = plan[8];
     b->plan.rotate = plan[9];
+    b->plan.gstate = plan[10];
     if (!b->n_inst) return GBPF_OK;
     return b->rebuild();
 }
@@ -2477,18 +2574,18 @@ extern "C" gbpf_status gbpf_batch_solve_noalloc(gbpf_batch *b, int n_inst, const
     int dev_sm = 0, occ = 0;
     CK(cudaDeviceGetAttribute(&dev_sm, cudaDevAttrMultiProcessorCount, b->device));
     cudaFuncAttributes fa{};
-    if (fp32) CK(cudaFuncGetAttributes(&fa, k_nr_block<float>));
-    else CK(cudaFuncGetAttributes(&fa, k_nr_block<double>));
+    if (fp32) CK(cudaFuncGetAttributes(&fa, k_nr_block<float, false>));
+    else CK(cudaFuncGetAttributes(&fa, k_nr_block<double, false>));
     if ((size_t)fa.maxDynamicSharedSizeBytes < b->na_smem) {
-        if (fp32) CK(cudaFuncSetAttribute(k_nr_block<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->na_smem));
-        else CK(cudaFuncSetAttribute(k_nr_block<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->na_smem));
+        const void *fn = fp32 ? (const void *)k_nr_block<float, false> : (const void *)k_nr_block<double, false>;
+        CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->na_smem));
     }
-    if (fp32) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float>, kThreads, b->na_smem));
-    else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double>, kThreads, b->na_smem));
+    if (fp32) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float, false>, kThreads, b->na_smem));
+    else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double, false>, kThreads, b->na_smem));
     const long long slices = (long long)((kNoAllocBytes - o_slices) / b->na_stride);
     const int grid = (int)std::max(1LL, std::min<long long>({(long long)n_inst, (long long)dev_sm * std::max(occ, 1), slices}));
-    if (fp32) k_nr_block<float><<<grid, kThreads, b->na_smem, s>>>(a);
-    else k_nr_block<double><<<grid, kThreads, b->na_smem, s>>>(a);
+    if (fp32) k_nr_block<float, false><<<grid, kThreads, b->na_smem, s>>>(a);
+    else k_nr_block<double, false><<<grid, kThreads, b->na_smem, s>>>(a);
     CK(cudaGetLastError());
     return GBPF_OK;
 }
