@@ -23,7 +23,7 @@ them, so that one step's tail runs beside the next step's bulk.
 Other workloads: c2-plain (one FP64 solve of the grid per step), c3 (the
 15,104-bus grid, one FP64 solve per step), c4 (4,096 instances of 14..472-bus
 grids, batched FP32), c5 (the learned warm start on the 1,888-bus grid: 50,000
-training solves, the 5664 -> 3 x 512 -> 3776 network trained for 20 epochs on
+training solves, the 5664 -> 3 x 512 -> 3776 network trained for 60 epochs on
 the GPU, then a step = batched FP32 Newton from the predicted start, flat-start
 fallback, over 8,192 held-out scenarios).
 
@@ -519,7 +519,7 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
     Y = gb.warm_targets(V, th)
     gen.close()
     del r, Pl, Ql, Pg
-    width, batch, epochs, lam = 512, 256, 20, 1.0
+    width, batch, epochs, lam = 512, 256, 60, 1.0
     m = gb.MLP(3 * nB, 2 * nB, width=width, n_layers=3, skip=True, seed=BASE_SEED + 5, device=dev)
     m.set_data(X, Y)
     plain = gb.Solver(grid, device=dev, metodo=0, **opts)

@@ -1406,6 +1406,7 @@ __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *
                                                            const float *oscale, double *sV, double *sTh, float4 *ef,
                                                            int *kind, int *cls_out, int *hist) {
     __shared__ unsigned red[2][kSelThreads / 32];
+    __shared__ float tred[2][kSelThreads / 32];
     const int inst = blockIdx.x, tid = threadIdx.x;
     const Topo T = a.topo[a.inst_topo[inst]];
     const TopoView G = bind(T.o, T.blob);
@@ -1415,6 +1416,7 @@ __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *
     float4 *e = ef + off;
     const char *flat = (T.flat && a.flat_on && *a.flat_on) ? T.flat : nullptr;
     const FlatLayout F = flat_layout<float>(nB, T.n + 2 * T.nup);  // P, Q offsets do not depend on the precision
+    float tlo = INFINITY, thi = -INFINITY;  // spread of the predicted angles
     for (int k = tid; k < nB; k += kSelThreads) {
         const int ty = G.type[k];
         const double v0 = a.V0[off + k], t0 = a.th0[off + k];
@@ -1422,6 +1424,9 @@ __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *
         const double t = ty == 3 ? t0 : (double)pr[nB + k] * oscale[nB + k] + omean[nB + k];
         sV[off + k] = v;
         sTh[off + k] = t;
+        // NaN stays NaN through the spread and lands in the top class
+        tlo = (float)t < tlo || t != t ? (float)t : tlo;
+        thi = (float)t > thi || t != t ? (float)t : thi;
         float s, c, s0 = 0.f, c0 = 0.f;
         sincosf((float)t, &s, &c);
         if (!flat) sincosf((float)t0, &s0, &c0);
@@ -1459,27 +1464,48 @@ __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *
     }
     mp = warp_umax32(mp);
     mf = warp_umax32(mf);
-    if ((tid & 31) == 0) { red[0][tid >> 5] = mp; red[1][tid >> 5] = mf; }
+    for (int o = 16; o > 0; o >>= 1) {
+        const float l = __shfl_xor_sync(0xffffffffu, tlo, o), h = __shfl_xor_sync(0xffffffffu, thi, o);
+        tlo = l < tlo || l != l ? l : tlo;
+        thi = h > thi || h != h ? h : thi;
+    }
+    if ((tid & 31) == 0) {
+        red[0][tid >> 5] = mp;
+        red[1][tid >> 5] = mf;
+        tred[0][tid >> 5] = tlo;
+        tred[1][tid >> 5] = thi;
+    }
     __syncthreads();
     if (tid == 0) {
-        for (int w = 1; w < kSelThreads / 32; w++) { mp = max(mp, red[0][w]); mf = max(mf, red[1][w]); }
+        for (int w = 1; w < kSelThreads / 32; w++) {
+            mp = max(mp, red[0][w]);
+            mf = max(mf, red[1][w]);
+            tlo = tred[0][w] < tlo || tred[0][w] != tred[0][w] ? tred[0][w] : tlo;
+            thi = tred[1][w] > thi || tred[1][w] != tred[1][w] ? tred[1][w] : thi;
+        }
         // NaN patterns order above every number: a NaN predicted mismatch loses
         const bool use = mp < mf;
         kind[inst] = use ? 1 : 0;
-        // the queue position class: the chosen start's mismatch, two classes
-        // per binade from 2^-24 up (clamped to 0..kOrderClasses-1; inf and NaN
-        // in the top class)
-        const unsigned key = use ? mp : mf;
-        const int cls = max(0, min(kOrderClasses - 1, (int)(key >> 22) - 2 * (127 - 24)));
+        // The queue position class: the spread of the predicted angles, the
+        // network's estimate of how stressed the scenario is.  Scenarios
+        // beyond the point where Newton converges have the largest spreads
+        // (measured on the 1,888-bus c5 scenarios: every non-converging one
+        // ranked in the top 4 %, where ranking by load or by start mismatch
+        // placed them at random), and they take the longest -- a failed
+        // predicted run and then no_max_iter iterations -- so they go first.
+        // Eight classes per binade over [2^-6, 4) rad (clamped; NaN on top).
+        const float spread = thi - tlo;
+        const unsigned key = spread != spread ? 0x7fc00000u : fabits(spread);
+        const int cls = max(0, min(kOrderClasses - 1, (int)(key >> 20) - (121 << 3)));
         cls_out[inst] = cls;
         atomicAdd(&hist[cls], 1);
     }
 }
 
-// The work queue of a warm-started launch, by falling start mismatch: the
-// instances expected to take longest (and those likely to fail from the
-// prediction and start again) are claimed first, so that they do not form
-// the launch's tail.  hist[c] counts class c; cursor[] starts zeroed.  The
+// The work queue of a warm-started launch, by falling class (k_ws_select:
+// the predicted angle spread): the instances expected to take longest -- a
+// failed predicted run, then the full run from their own start -- are
+// claimed first, so that they do not form the launch's tail.  hist[c] counts class c; cursor[] starts zeroed.  The
 // order inside a class is whichever the atomics give: every instance's result
 // is independent of its queue position.
 __global__ void k_ws_order(const int *cls, const int *hist, int *cursor, int n_inst, int *queue) {

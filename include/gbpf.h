@@ -486,7 +486,8 @@ gbpf_status gbpf_mlp_set_norm(gbpf_mlp *m, const float *in_mean, const float *in
  * (V0/theta0 of gbpf_batch_set_instances, by default the flat start), else
  * from its own start.  Instances whose predicted start does not converge are
  * solved again from their own start, in the same launch.  Instances are
- * served in order of falling start mismatch.  Results as for
+ * served in order of falling predicted angle spread (max - min theta of the
+ * prediction), the most stressed scenarios first.  Results as for
  * gbpf_batch_solve (gbpf_batch_results); an instance on its own start gets
  * no_max_iter iterations.  start_kind[i] (may be NULL): 0 own start chosen up
  * front, 1 predicted start converged, 2 predicted start failed (no
