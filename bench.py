@@ -552,9 +552,12 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
         dist.barrier()
     with Clocks(dev) as clk:
         t_steps = 0.0
+        phases = dict(network=0.0, start_choice=0.0, newton=0.0)
         for _ in range(a.steps):
             w = fast.solve_warm(m)
             t_steps += w["ms"]
+            for k in phases:
+                phases[k] += w["phases_ms"][k] / a.steps
     if dist:
         dist.barrier()
     rw = fast.results()
@@ -587,7 +590,7 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
     peak, src = peak_hbm()
     nb_tot = C5_TEST * nB
     bytes_launch = nb_tot * 8 * 5 + nb_tot * 8 * 4 + C5_TEST * 20
-    achieved = bytes_launch / (t_steps / a.steps / 1e3) / 1e9
+    achieved = bytes_launch / (phases["newton"] / 1e3) / 1e9
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if src == "measured" else {}
     tpeak = peaks.get("bf16_tflops_sustained", 1700.0)
     line = {
@@ -605,6 +608,8 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
                    "train_generation_s": t_gen, "train_s": train_ms / 1e3,
                    "train_loss_first_last": [float(loss[0]), float(loss[-1])],
                    "converged_per_step": conv,
+                   "phases_ms": {k: round(v, 4) for k, v in phases.items()},
+                   "plan": fast.plan(),
                    "mean_iterations_flat_fp32": float(r32["iterations"].mean()),
                    "mean_iterations_warm_fp32": float(it_w.mean()),
                    "mean_iterations_flat_fp64": float(r64["iterations"].mean()),
@@ -622,7 +627,8 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
                    "parallelism": f"scenarios sharded x{world}"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nb_tot * 8 * 3,
                 "d2h_bytes_per_step": nb_tot * 8 * 4 + C5_TEST * 20},
-        "roofline": {"bound": "hbm", "kernel": "k_nr_block<float> (one persistent launch per step)",
+        "roofline": {"bound": "hbm", "kernel": "k_nr_block<float, GS> (one persistent launch per step; "
+                                               "achieved over its phase of the step)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src_note(src), "traffic": None,
                      "note": "dependent-load latency bound (factor in L2-resident scratch)"},

@@ -229,16 +229,20 @@ struct Layout {
 };
 // with_zs: room for z = D^-1 y of the one-pass levels (lu_level1).  The
 // inverse of diagonal block j overwrites fac[j] once the block is factored.
-// gs: the per-bus arrays that no thread reads for another bus's row -- theta,
-// P, Q, QL and, in the FP32-LU form (whose Jacobian reads the FP32 copies),
-// V, cos, sin -- live in a per-block region of global memory (offsets from
-// its start, gtotal bytes; L2-resident) instead of shared memory, which
-// halves the shared memory of an instance.
+// gs = 1: the per-bus arrays that no thread reads for another bus's row --
+// theta, P, Q, QL and, in the FP32-LU form (whose Jacobian reads the FP32
+// copies), V, cos, sin -- live in a per-block region of global memory
+// (offsets from its start, gtotal bytes; L2-resident) instead of shared
+// memory, which halves the shared memory of an instance.  gs = 2: every
+// per-bus array but the flags and y, z goes there (the phasors too, read for
+// the neighbours in the injections and the Jacobian fill), leaving shared
+// memory to the factor and the substitutions, the latency-critical part.
 template <typename TJ>
 __host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fac_smem, int with_zs, int gs = 0) {
     using B4 = typename Blk<TJ>::b4;
     using B2 = typename Blk<TJ>::b2;
     constexpr bool f32_form = sizeof(TJ) == 4;
+    const bool vg = gs >= 2 || f32_form;  // V, cos, sin with gs
     Layout L;
     size_t o = 0, og = 0;
     auto take = [&](size_t bytes, size_t al) { o = align_up(o, al); size_t r = o; o += bytes; return r; };
@@ -249,13 +253,13 @@ __host__ __device__ inline Layout layout(int nB, int n, int nup, int nPV, int fa
         og += bytes;
         return r;
     };
-    L.V = f32_form ? takeg(8 * nB, 16) : take(8 * nB, 16);
+    L.V = vg ? takeg(8 * nB, 16) : take(8 * nB, 16);
     L.th = takeg(8 * nB, 16);
-    L.cs = f32_form ? takeg(8 * nB, 16) : take(8 * nB, 16);
-    L.sn = f32_form ? takeg(8 * nB, 16) : take(8 * nB, 16);
+    L.cs = vg ? takeg(8 * nB, 16) : take(8 * nB, 16);
+    L.sn = vg ? takeg(8 * nB, 16) : take(8 * nB, 16);
     // e = V cos th, f = V sin th (FP64); cos, sin, V in FP32 for the FP32-LU form's Jacobian
-    L.ef = take(16 * (size_t)nB, 16);
-    L.f32 = take(f32_form ? 16 * (size_t)nB : 0, 16);
+    L.ef = gs >= 2 ? takeg(16 * (size_t)nB, 16) : take(16 * (size_t)nB, 16);
+    L.f32 = gs >= 2 ? takeg(f32_form ? 16 * (size_t)nB : 0, 16) : take(f32_form ? 16 * (size_t)nB : 0, 16);
     L.P = takeg(8 * nB, 16); L.Q = takeg(8 * nB, 16); L.QL = takeg(8 * nB, 16);
     L.gtotal = align_up(og, 256);
     L.act = take(nB, 16); L.lim = take(4 * (size_t)(nPV + 1), 16);
@@ -715,7 +719,7 @@ __device__ __forceinline__ bool lu_level1(const TopoView &G, int l, int lgp, int
     return sing;
 }
 
-template <typename TJ, bool GS>
+template <typename TJ, int GS>
 __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
     using B4 = typename Blk<TJ>::b4;
     using B2 = typename Blk<TJ>::b2;
@@ -755,11 +759,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
         const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, T.fac_smem, a.lu1, GS);
         // the state arrays layout() moves to global memory (GS)
         unsigned char *gst = GS ? a.gstate + (long long)blockIdx.x * a.gstate_stride : ism;
-        unsigned char *vst = (GS && sizeof(TJ) == 4) ? gst : ism;
+        unsigned char *vst = (GS >= 2 || (GS && sizeof(TJ) == 4)) ? gst : ism;
+        unsigned char *pst = GS >= 2 ? gst : ism;  // phasors
         double *V = (double *)(vst + L.V), *th = (double *)(gst + L.th);
         double *cs = (double *)(vst + L.cs), *sn = (double *)(vst + L.sn);
-        double2 *ef = (double2 *)(ism + L.ef);
-        float4 *f32 = (float4 *)(ism + L.f32);
+        double2 *ef = (double2 *)(pst + L.ef);
+        float4 *f32 = (float4 *)(pst + L.f32);
         double *P = (double *)(gst + L.P), *Q = (double *)(gst + L.Q), *QL = (double *)(gst + L.QL);
         unsigned char *act = ism + L.act;
         int *limQ = (int *)(ism + L.lim);
@@ -1362,6 +1367,16 @@ __global__ void k_batch_stamps(const double *r, const double *x, const double *b
             return GBPF_E_CUDA;                                                      \
         }                                                                            \
     } while (0)
+// a kernel launch's configuration error, reported with the source line
+#define CK_LAUNCH()                                                                  \
+    do {                                                                             \
+        cudaError_t e_ = cudaGetLastError();                                         \
+        if (e_ != cudaSuccess) {                                                     \
+            set_error(std::string("kernel launch at batch.cu:") + std::to_string(__LINE__) + ": " + \
+                      cudaGetErrorString(e_));                                       \
+            return GBPF_E_CUDA;                                                      \
+        }                                                                            \
+    } while (0)
 
 // ---------------------------------------------------------------------------
 // learned warm start
@@ -1617,6 +1632,14 @@ __global__ void k_pack_inputs(PackArgs a) {
 // ---------------------------------------------------------------------------
 // host object
 // ---------------------------------------------------------------------------
+// The block kernel of a state placement level (layout gs), as a function
+// handle for attributes and occupancy queries.
+template <typename TJ> const void *blk_kernel(int gs) {
+    if (gs == 2) return (const void *)k_nr_block<TJ, 2>;
+    if (gs == 1) return (const void *)k_nr_block<TJ, 1>;
+    return (const void *)k_nr_block<TJ, 0>;
+}
+
 struct gbpf_batch {
     int device = 0;
     int precision = 0;
@@ -1689,13 +1712,14 @@ struct gbpf_batch {
     // rotate = 1 updates the FP32-LU form's phasors by rotation instead of a
     // sincos per iteration (measured slower on GB300, kept as a knob);
     // gstate = 1 lets the block kernel keep part of its state in global
-    // memory (layout gs) where that fits more instances per SM or moves
-    // factors into shared memory, 2 wherever it fits, 0 never.
+    // memory (layout gs = 1 or 2) where that fits more instances per SM or
+    // moves factors into shared memory; 2 takes gs = 1 and 3 gs = 2 wherever
+    // they fit; 0 never.
     struct Plan {
         int warp_mode = 1, warp_warps = 8, handoff_it = kHandoffIt, resume_group = 1, warp_group = 1, narrow = 0,
             lu1 = 1, warp_lu1 = 0, flat_shared = 1, rotate = 0, gstate = 1;
     } plan;
-    bool block_gs = false;  // the block-mode launch keeps its state in global memory
+    int block_gs = 0;  // placement level of the block-mode launch's state (layout gs)
     DevBuf gstate_mem;
     gbpf_status rebuild() {
         CK(cudaStreamSynchronize(stream));
@@ -1849,7 +1873,7 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
                                                           (const double *)(tb + t_bsh),
                                                           (double2 *)((char *)mem.p + o.yval),
                                                           (float2 *)((char *)mem.p + o.yval32), y.nnz);
-    CK(cudaGetLastError());
+    CK_LAUNCH();
     CK(cudaStreamSynchronize(stream));
     Topo t{};
     t.nB = nB; t.nL = nL; t.n = n; t.nup = nup; t.nnzY = y.nnz; t.nPV = g.nPV; t.nfl = nfl; t.nbl = nbl;
@@ -1936,7 +1960,7 @@ gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Ploa
     pa.V0 = (double *)args.V0; pa.th0 = (double *)args.th0; pa.Pliq = (double *)args.Pliq;
     pa.Qliq = (double *)args.Qliq; pa.Qload = (double *)args.Qload;
     k_pack_inputs<<<(unsigned)(((long long)n * 32 + 255) / 256), 256, 0, stream>>>(pa);
-    CK(cudaGetLastError());
+    CK_LAUNCH();
     // instances from the grids' own start may take the shared iteration 0
     flat_flag = (!V0 && !th0) ? 1 : 0;
     CK(cudaMemcpyAsync((int *)counter.p + 8, &flat_flag, sizeof(int), cudaMemcpyHostToDevice, stream));
@@ -1956,20 +1980,34 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
         CK(cudaStreamWaitEvent(side, fork, 0));
         if (timed) CK(cudaEventRecordWithFlags(kev[0], side, cudaEventRecordExternal));
         if (fp32) {
-            if (block_gs) k_nr_block<float, true><<<grid_blocks, kThreads, smem, side>>>(ba);
-            else k_nr_block<float, false><<<grid_blocks, kThreads, smem, side>>>(ba);
+            if (block_gs == 2) k_nr_block<float, 2><<<grid_blocks, kThreads, smem, side>>>(ba);
+            else if (block_gs == 1) k_nr_block<float, 1><<<grid_blocks, kThreads, smem, side>>>(ba);
+            else k_nr_block<float, 0><<<grid_blocks, kThreads, smem, side>>>(ba);
         } else {
-            if (block_gs) k_nr_block<double, true><<<grid_blocks, kThreads, smem, side>>>(ba);
-            else k_nr_block<double, false><<<grid_blocks, kThreads, smem, side>>>(ba);
+            if (block_gs == 2) k_nr_block<double, 2><<<grid_blocks, kThreads, smem, side>>>(ba);
+            else if (block_gs == 1) k_nr_block<double, 1><<<grid_blocks, kThreads, smem, side>>>(ba);
+            else k_nr_block<double, 0><<<grid_blocks, kThreads, smem, side>>>(ba);
         }
-        CK(cudaGetLastError());
+        {
+            const cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) {
+                cudaFuncAttributes fa{};
+                cudaFuncGetAttributes(&fa, fp32 ? blk_kernel<float>(block_gs) : blk_kernel<double>(block_gs));
+                set_error(std::string("k_nr_block launch (") + std::to_string(grid_blocks) + " blocks, " +
+                          std::to_string(smem) + " B dynamic shared memory; the kernel allows " +
+                          std::to_string(fa.maxDynamicSharedSizeBytes) + " B dynamic, " +
+                          std::to_string(fa.sharedSizeBytes) + " B static, " + std::to_string(fa.numRegs) +
+                          " registers, " + std::to_string(fa.localSizeBytes) + " B local): " + cudaGetErrorString(e));
+                return GBPF_E_CUDA;
+            }
+        }
         if (timed) CK(cudaEventRecordWithFlags(kev[1], side, cudaEventRecordExternal));
     }
     if (wa.queue_len) {
         if (timed) CK(cudaEventRecordWithFlags(kev[2], st, cudaEventRecordExternal));
         if (fp32) k_nr_warp<float><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wa);
         else k_nr_warp<double><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wa);
-        CK(cudaGetLastError());
+        CK_LAUNCH();
         if (timed) CK(cudaEventRecordWithFlags(kev[3], st, cudaEventRecordExternal));
         if (wa.handoff_it > 0) {
             // the instances the warps parked, one block each, same arithmetic
@@ -1983,9 +2021,9 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
             ra.counter = args.counter + 2;
             ra.topo = (const Topo *)topo_resume.p;
             ra.blob_region = resume_region;
-            if (fp32) k_nr_block<float, false><<<resume_grid, kThreads, resume_smem, st>>>(ra);
-            else k_nr_block<double, false><<<resume_grid, kThreads, resume_smem, st>>>(ra);
-            CK(cudaGetLastError());
+            if (fp32) k_nr_block<float, 0><<<resume_grid, kThreads, resume_smem, st>>>(ra);
+            else k_nr_block<double, 0><<<resume_grid, kThreads, resume_smem, st>>>(ra);
+            CK_LAUNCH();
             if (timed) CK(cudaEventRecordWithFlags(kev[4], st, cudaEventRecordExternal));
         }
     }
@@ -2036,16 +2074,16 @@ gbpf_status gbpf_batch::build_graph() {
         T.blob_smem = !warp_ok[t] && (size_t)T.blob_bytes <= blob_cap;
         if (T.blob_smem) region = std::max(region, align_up((size_t)T.blob_bytes, 32));
     }
-    auto blk_fn = [&](bool gs) -> const void * {
-        if (fp32) return gs ? (const void *)k_nr_block<float, true> : (const void *)k_nr_block<float, false>;
-        return gs ? (const void *)k_nr_block<double, true> : (const void *)k_nr_block<double, false>;
+    auto blk_fn = [&](int gs) -> const void * {
+        if (fp32) return blk_kernel<float>(gs);
+        return blk_kernel<double>(gs);
     };
     struct BlockPlan {
         size_t need = 0, scr = 0, gst = 0;
         std::vector<int> fac;
         int nfac = 0, occ = 0;
     };
-    auto plan_blocks = [&](int gs, BlockPlan &bp) -> gbpf_status {
+    auto plan_blocks = [&](int gs, size_t budget, BlockPlan &bp) -> gbpf_status {
         bp.fac.assign(topo_h.size(), 1);
         for (size_t t = 0; t < topo_h.size(); t++) {
             if (warp_ok[t]) continue;
@@ -2071,16 +2109,26 @@ gbpf_status gbpf_batch::build_graph() {
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bp.occ, blk_fn(gs), kThreads, sm));
         return GBPF_OK;
     };
-    BlockPlan bp, bg;
-    gbpf_status pst = plan_blocks(0, bp);
+    // Placement level: gstate 2 / 3 take level 1 / 2 where it fits; gstate 1
+    // the level with the most blocks per SM, then the most factors in shared
+    // memory, then the least state in global memory (measured on 1,888-bus
+    // instances: FP32 level 1, 2 blocks per SM, 1.56x level 0, and 1.45x level
+    // 2 with the factor given the whole of shared memory at 1 block per SM;
+    // FP64 level 2, 2 blocks per SM, 1.26x).
+    BlockPlan bp;
+    gbpf_status pst = plan_blocks(0, budget, bp);
     if (pst != GBPF_OK) return pst;
-    block_gs = false;
+    block_gs = 0;
     if (plan.gstate && n_block_q) {
-        if ((pst = plan_blocks(1, bg)) != GBPF_OK) return pst;
-        if ((plan.gstate == 2 && bg.occ > 0) || bg.occ > bp.occ ||
-            (bg.occ == bp.occ && bg.occ > 0 && bg.nfac > bp.nfac)) {
-            bp = bg;
-            block_gs = true;
+        for (int gs = 1; gs <= 2; gs++) {
+            BlockPlan c;
+            if ((pst = plan_blocks(gs, budget, c)) != GBPF_OK) return pst;
+            const bool take = plan.gstate >= 2 ? (gs == plan.gstate - 1 && c.occ > 0)
+                                               : (c.occ > bp.occ || (c.occ == bp.occ && c.occ > 0 && c.nfac > bp.nfac));
+            if (take) {
+                bp = c;
+                block_gs = gs;
+            }
         }
     }
     for (size_t t = 0; t < topo_h.size(); t++) topo_h[t].fac_smem = bp.fac[t];
@@ -2118,8 +2166,8 @@ gbpf_status gbpf_batch::build_graph() {
         // the resume launch always keeps its state in shared memory
         size_t attr_sm = use_handoff ? resume_smem : 0;
         if (!block_gs) attr_sm = std::max(attr_sm, smem);
-        if (attr_sm) CK(cudaFuncSetAttribute(blk_fn(false), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)attr_sm));
-        if (block_gs) CK(cudaFuncSetAttribute(blk_fn(true), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (attr_sm) CK(cudaFuncSetAttribute(blk_fn(0), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)attr_sm));
+        if (block_gs) CK(cudaFuncSetAttribute(blk_fn(block_gs), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
     if (n_block_q) {
         int occ = 0;
@@ -2128,7 +2176,7 @@ gbpf_status gbpf_batch::build_graph() {
     }
     if (use_handoff) {
         int occ = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, blk_fn(false), kThreads, resume_smem));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, blk_fn(0), kThreads, resume_smem));
         resume_grid = std::max(1, std::min(n_warp_q, dev_sm * std::max(occ, 1)));
     }
     gstate_mem.reset();
@@ -2178,7 +2226,7 @@ gbpf_status gbpf_batch::build_graph() {
             const size_t fs = align_up((fp32 ? 8 : 16) * (size_t)T.n, 16) + (size_t)T.nB;
             if (fp32) k_flat_start<float><<<1, 32, fs, stream>>>(T, o, plan.warp_group);
             else k_flat_start<double><<<1, 32, fs, stream>>>(T, o, plan.warp_group);
-            CK(cudaGetLastError());
+            CK_LAUNCH();
             T.flat = o;
         }
         CK(cudaStreamSynchronize(stream));
@@ -2273,16 +2321,16 @@ gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, 
     CK(cudaMemsetAsync(wHist, 0, 8 * kOrderClasses, stream));
     k_ws_features<<<1024, 256, 0, stream>>>(args.Pliq, args.Qliq, args.V0, args.inst_off, n_inst, nB, sh.n_in, sh.kin,
                                             sh.in_mean, sh.in_iscale, wX);
-    CK(cudaGetLastError());
+    CK_LAUNCH();
     gbpf_status st = gbpf::mlp_infer(m, wX, n_inst, wPred, stream);
     if (st != GBPF_OK) return st;
     CK(cudaEventRecord(wev[0], stream));
     k_ws_select<<<n_inst, kSelThreads, 0, stream>>>(args, wPred, sh.outp, sh.out_mean, sh.out_scale, wV, wTh, wEF,
                                                      wKind, wCls, wHist);
-    CK(cudaGetLastError());
+    CK_LAUNCH();
     const int order_blocks = std::min((n_inst + 255) / 256, 1024);
     k_ws_order<<<order_blocks, 256, 0, stream>>>(wCls, wHist, wHist + kOrderClasses, n_inst, wQueue);
-    CK(cudaGetLastError());
+    CK_LAUNCH();
     CK(cudaEventRecord(wev[1], stream));
     // one launch: predicted starts, own starts, and the restarts of failed
     // predictions, in the order k_ws_order gave
@@ -2423,7 +2471,7 @@ extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[11]) {
     ARGCHECK(b && plan && (plan[0] == 0 || plan[0] == 1) && plan[1] >= 0 && plan[1] <= kWarpsMax && plan[2] >= 0 &&
              (plan[3] == 0 || plan[3] == 1) && (plan[4] == 0 || plan[4] == 1) && (plan[5] == 0 || plan[5] == 1) &&
              (plan[6] == 0 || plan[6] == 1) && (plan[7] == 0 || plan[7] == 1) && (plan[8] == 0 || plan[8] == 1) &&
-             (plan[9] == 0 || plan[9] == 1) && plan[10] >= 0 && plan[10] <= 2);
+             (plan[9] == 0 || plan[9] == 1) && plan[10] >= 0 && plan[10] <= 3);
     CK(cudaSetDevice(b->device));
     b->plan.warp_mode = plan[0];
     b->plan.warp_warps = plan[1];
@@ -2600,19 +2648,19 @@ extern "C" gbpf_status gbpf_batch_solve_noalloc(gbpf_batch *b, int n_inst, const
     int dev_sm = 0, occ = 0;
     CK(cudaDeviceGetAttribute(&dev_sm, cudaDevAttrMultiProcessorCount, b->device));
     cudaFuncAttributes fa{};
-    if (fp32) CK(cudaFuncGetAttributes(&fa, k_nr_block<float, false>));
-    else CK(cudaFuncGetAttributes(&fa, k_nr_block<double, false>));
+    if (fp32) CK(cudaFuncGetAttributes(&fa, k_nr_block<float, 0>));
+    else CK(cudaFuncGetAttributes(&fa, k_nr_block<double, 0>));
     if ((size_t)fa.maxDynamicSharedSizeBytes < b->na_smem) {
-        const void *fn = fp32 ? (const void *)k_nr_block<float, false> : (const void *)k_nr_block<double, false>;
+        const void *fn = fp32 ? (const void *)k_nr_block<float, 0> : (const void *)k_nr_block<double, 0>;
         CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->na_smem));
     }
-    if (fp32) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float, false>, kThreads, b->na_smem));
-    else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double, false>, kThreads, b->na_smem));
+    if (fp32) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float, 0>, kThreads, b->na_smem));
+    else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double, 0>, kThreads, b->na_smem));
     const long long slices = (long long)((kNoAllocBytes - o_slices) / b->na_stride);
     const int grid = (int)std::max(1LL, std::min<long long>({(long long)n_inst, (long long)dev_sm * std::max(occ, 1), slices}));
-    if (fp32) k_nr_block<float, false><<<grid, kThreads, b->na_smem, s>>>(a);
-    else k_nr_block<double, false><<<grid, kThreads, b->na_smem, s>>>(a);
-    CK(cudaGetLastError());
+    if (fp32) k_nr_block<float, 0><<<grid, kThreads, b->na_smem, s>>>(a);
+    else k_nr_block<double, 0><<<grid, kThreads, b->na_smem, s>>>(a);
+    CK_LAUNCH();
     return GBPF_OK;
 }
 

@@ -362,13 +362,16 @@ gbpf_status gbpf_batch_kernel_times(gbpf_batch *b, int repeats, double ms[3]);
  * topology, and do only their own substitutions in it; plan[9] 1 = the
  * FP32-LU form updates its phasors by rotating them through the Newton step
  * instead of a sincos of every angle each iteration (0, the default, measured
- * faster on GB300); plan[10] 1 = thread-block instances may keep the per-bus
- * arrays that no other bus's row reads (theta, P, Q and, in the FP32-LU form,
- * |V| and the FP64 phasor) in an L2-resident global region instead of shared
- * memory, taken when that fits more instances per SM or more factors in
- * shared memory; 2 = always, 0 = never.  get_plan also returns plan[11] warps per block in use,
- * plan[12] instances on warps, plan[13] instances on blocks, plan[14] 1 when
- * the block launch keeps that state in global memory (plan[15] = 0).
+ * faster on GB300); plan[10] the placement of thread-block instances'
+ * state: level 1 keeps the per-bus arrays that no other bus's row reads
+ * (theta, P, Q and, in the FP32-LU form, |V| and the FP64 phasor) in an
+ * L2-resident global region instead of shared memory, level 2 every per-bus
+ * array but the flags and the substitution vectors; plan[10] = 1 takes the
+ * level with the most instances per SM, then the most factors in shared
+ * memory, then the lower level; 2 = level 1, 3 = level 2 wherever they fit;
+ * 0 = level 0 (all in shared memory).  get_plan also returns plan[11] warps
+ * per block in use, plan[12] instances on warps, plan[13] instances on
+ * blocks, plan[14] the placement level in use (plan[15] = 0).
  * Setting a plan rebuilds the batch graph. */
 gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[16]);
 gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[11]);

@@ -368,11 +368,13 @@ def test_block_mode_shared_flat_start(gb, oracle):
 @pytest.mark.parametrize("prec", ["PREC_FP64", "PREC_FP32_IR"])
 def test_block_state_in_global_memory_is_exact(gb, prec):
     """Thread-block instances with part of their state in global memory (plan
-    gstate 2; the default picks it where it fits more instances per SM, e.g.
-    the FP32-LU form of a 1,888-bus grid) do the same arithmetic as with all
-    of it in shared memory: iterations, statuses, switch events, |V| and
-    theta bit for bit, for a grid whose factor is in shared memory and one
-    whose factor is in global scratch."""
+    gstate 2: the own-bus arrays; gstate 3: every per-bus array but the flags
+    and y, z; the default picks the level with the most instances per SM, e.g.
+    level 1 for the FP32-LU form of a 1,888-bus grid, level 2 for its FP64
+    form) do the same arithmetic as with all of it in shared memory:
+    iterations, statuses, switch events, |V| and theta bit for bit, for a grid
+    whose factor is in shared memory and one whose factor is in global
+    scratch."""
     import bench
 
     for grid in (gb.read_grid(os.path.join(GOLDEN, "c2_s3.cdf")), gb.generate(3, bench.BASE_SEED + 5, tiles=16)):
@@ -383,16 +385,18 @@ def test_block_state_in_global_memory_is_exact(gb, prec):
         Pl, Ql = base["Pload"] * lf, base["Qload"] * lf
         Pg = base["Pg"] * rng.uniform(0.85, 1.15, (n, grid.nB))
         out = []
-        for gstate in (0, 2):
+        for gstate, level in ((0, 0), (2, 1), (3, 2)):
             b = gb.Batch([grid], precision=getattr(gb, prec), tolerancia=1e-8, no_max_iter=30, lim_inj_reat=1)
             b.set_plan(warp_mode=0, gstate=gstate)
             b.set_instances(np.zeros(n, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
             b.solve()
-            assert b.plan()["block_state_global"] == (gstate == 2)
+            assert b.plan()["block_state_global"] == level
             out.append((b.results(), [b.events(i) for i in range(n)], b.info()))
-        (r0, e0, i0), (r1, e1, i1) = out
+        r0, e0, i0 = out[0]
         assert (r0["status"] == 0).mean() > 0.9
-        for k in ("iterations", "status", "n_events", "V", "theta", "Pcalc", "Qcalc", "final_mismatch"):
-            np.testing.assert_array_equal(r1[k], r0[k], err_msg=k)
-        assert e1 == e0
-        assert i1["smem_bytes"] < i0["smem_bytes"]
+        for r1, e1, i1 in out[1:]:
+            for k in ("iterations", "status", "n_events", "V", "theta", "Pcalc", "Qcalc", "final_mismatch"):
+                np.testing.assert_array_equal(r1[k], r0[k], err_msg=k)
+            assert e1 == e0
+        assert out[2][2]["smem_bytes"] < out[1][2]["smem_bytes"] < i0["smem_bytes"]
+        assert out[2][2]["factors_in_smem"] >= i0["factors_in_smem"]
