@@ -719,8 +719,11 @@ __device__ __forceinline__ bool lu_level1(const TopoView &G, int l, int lgp, int
     return sing;
 }
 
+// GS: the state placement level of layout(); 3 = level 2 compiled for four
+// blocks per SM (64 registers a thread) instead of two.
 template <typename TJ, int GS>
-__global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
+__global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) {
+    constexpr int LV = GS > 2 ? 2 : GS;
     using B4 = typename Blk<TJ>::b4;
     using B2 = typename Blk<TJ>::b2;
     extern __shared__ __align__(32) unsigned char smem[];
@@ -756,11 +759,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_nr_block(Args a) {
         }
         const TopoView G = bind(T.o, blob);
         const long long off = a.inst_off[inst];
-        const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, T.fac_smem, a.lu1, GS);
-        // the state arrays layout() moves to global memory (GS)
-        unsigned char *gst = GS ? a.gstate + (long long)blockIdx.x * a.gstate_stride : ism;
-        unsigned char *vst = (GS >= 2 || (GS && sizeof(TJ) == 4)) ? gst : ism;
-        unsigned char *pst = GS >= 2 ? gst : ism;  // phasors
+        const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, T.fac_smem, a.lu1, LV);
+        // the state arrays layout() moves to global memory (LV)
+        unsigned char *gst = LV ? a.gstate + (long long)blockIdx.x * a.gstate_stride : ism;
+        unsigned char *vst = (LV >= 2 || (LV && sizeof(TJ) == 4)) ? gst : ism;
+        unsigned char *pst = LV >= 2 ? gst : ism;  // phasors
         double *V = (double *)(vst + L.V), *th = (double *)(gst + L.th);
         double *cs = (double *)(vst + L.cs), *sn = (double *)(vst + L.sn);
         double2 *ef = (double2 *)(pst + L.ef);
@@ -1635,6 +1638,7 @@ __global__ void k_pack_inputs(PackArgs a) {
 // The block kernel of a state placement level (layout gs), as a function
 // handle for attributes and occupancy queries.
 template <typename TJ> const void *blk_kernel(int gs) {
+    if (gs == 3) return (const void *)k_nr_block<TJ, 3>;
     if (gs == 2) return (const void *)k_nr_block<TJ, 2>;
     if (gs == 1) return (const void *)k_nr_block<TJ, 1>;
     return (const void *)k_nr_block<TJ, 0>;
@@ -1712,9 +1716,10 @@ struct gbpf_batch {
     // rotate = 1 updates the FP32-LU form's phasors by rotation instead of a
     // sincos per iteration (measured slower on GB300, kept as a knob);
     // gstate = 1 lets the block kernel keep part of its state in global
-    // memory (layout gs = 1 or 2) where that fits more instances per SM or
-    // moves factors into shared memory; 2 takes gs = 1 and 3 gs = 2 wherever
-    // they fit; 0 never.
+    // memory (layout gs = 1 or 2, the latter also compiled for four blocks
+    // per SM: level 3) where that fits more instances per SM or moves factors
+    // into shared memory; 2, 3, 4 take level 1, 2, 3 wherever it fits; 0
+    // never.
     struct Plan {
         int warp_mode = 1, warp_warps = 8, handoff_it = kHandoffIt, resume_group = 1, warp_group = 1, narrow = 0,
             lu1 = 1, warp_lu1 = 0, flat_shared = 1, rotate = 0, gstate = 1;
@@ -1980,11 +1985,13 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
         CK(cudaStreamWaitEvent(side, fork, 0));
         if (timed) CK(cudaEventRecordWithFlags(kev[0], side, cudaEventRecordExternal));
         if (fp32) {
-            if (block_gs == 2) k_nr_block<float, 2><<<grid_blocks, kThreads, smem, side>>>(ba);
+            if (block_gs == 3) k_nr_block<float, 3><<<grid_blocks, kThreads, smem, side>>>(ba);
+            else if (block_gs == 2) k_nr_block<float, 2><<<grid_blocks, kThreads, smem, side>>>(ba);
             else if (block_gs == 1) k_nr_block<float, 1><<<grid_blocks, kThreads, smem, side>>>(ba);
             else k_nr_block<float, 0><<<grid_blocks, kThreads, smem, side>>>(ba);
         } else {
-            if (block_gs == 2) k_nr_block<double, 2><<<grid_blocks, kThreads, smem, side>>>(ba);
+            if (block_gs == 3) k_nr_block<double, 3><<<grid_blocks, kThreads, smem, side>>>(ba);
+            else if (block_gs == 2) k_nr_block<double, 2><<<grid_blocks, kThreads, smem, side>>>(ba);
             else if (block_gs == 1) k_nr_block<double, 1><<<grid_blocks, kThreads, smem, side>>>(ba);
             else k_nr_block<double, 0><<<grid_blocks, kThreads, smem, side>>>(ba);
         }
@@ -2089,10 +2096,11 @@ gbpf_status gbpf_batch::build_graph() {
             if (warp_ok[t]) continue;
             const Topo &T = topo_h[t];
             const int z = plan.lu1;
-            const Layout with = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1, z, gs)
-                                     : layout<double>(T.nB, T.n, T.nup, T.nPV, 1, z, gs);
-            const Layout without = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 0, z, gs)
-                                        : layout<double>(T.nB, T.n, T.nup, T.nPV, 0, z, gs);
+            const int lv = std::min(gs, 2);
+            const Layout with = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1, z, lv)
+                                     : layout<double>(T.nB, T.n, T.nup, T.nPV, 1, z, lv);
+            const Layout without = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 0, z, lv)
+                                        : layout<double>(T.nB, T.n, T.nup, T.nPV, 0, z, lv);
             bp.gst = std::max(bp.gst, with.gtotal);
             if (region + with.total <= budget) {
                 bp.nfac++;
@@ -2109,18 +2117,20 @@ gbpf_status gbpf_batch::build_graph() {
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bp.occ, blk_fn(gs), kThreads, sm));
         return GBPF_OK;
     };
-    // Placement level: gstate 2 / 3 take level 1 / 2 where it fits; gstate 1
-    // the level with the most blocks per SM, then the most factors in shared
-    // memory, then the least state in global memory (measured on 1,888-bus
-    // instances: FP32 level 1, 2 blocks per SM, 1.56x level 0, and 1.45x level
-    // 2 with the factor given the whole of shared memory at 1 block per SM;
-    // FP64 level 2, 2 blocks per SM, 1.26x).
+    // Placement level: gstate 2 / 3 / 4 take level 1 / 2 / 3 where it fits;
+    // gstate 1 the level with the most blocks per SM, then the most factors in
+    // shared memory, then the least state in global memory.  Measured on
+    // 8,192 instances of a 1,888-bus grid (solves/s): FP32 level 0 124 k
+    // (1 block per SM), 1 194 k (2), 2 199 k (2), 3 290 k (4; 279 k at 5 and
+    // 217 k at 6 blocks per SM, where spills grow), and 133 k with the factor
+    // given the whole of shared memory at 1 block per SM; FP64 57 k, 58 k,
+    // 71 k, 71 k (3 blocks per SM).
     BlockPlan bp;
     gbpf_status pst = plan_blocks(0, budget, bp);
     if (pst != GBPF_OK) return pst;
     block_gs = 0;
     if (plan.gstate && n_block_q) {
-        for (int gs = 1; gs <= 2; gs++) {
+        for (int gs = 1; gs <= 3; gs++) {
             BlockPlan c;
             if ((pst = plan_blocks(gs, budget, c)) != GBPF_OK) return pst;
             const bool take = plan.gstate >= 2 ? (gs == plan.gstate - 1 && c.occ > 0)
@@ -2414,7 +2424,7 @@ gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
         {&Plan::warp_lu1, {0, 1}, true, false, false},
         {&Plan::flat_shared, {1, 0}, false, false, false},
         {&Plan::rotate, {0, 1}, false, false, false},
-        {&Plan::gstate, {1, 0}, false, false, true},
+        {&Plan::gstate, {1, 0, 2, 3, 4}, false, false, true},
     };
     for (int sweep = 0; sweep < 2; sweep++) {
         bool changed = false;
@@ -2471,7 +2481,7 @@ extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[11]) {
     ARGCHECK(b && plan && (plan[0] == 0 || plan[0] == 1) && plan[1] >= 0 && plan[1] <= kWarpsMax && plan[2] >= 0 &&
              (plan[3] == 0 || plan[3] == 1) && (plan[4] == 0 || plan[4] == 1) && (plan[5] == 0 || plan[5] == 1) &&
              (plan[6] == 0 || plan[6] == 1) && (plan[7] == 0 || plan[7] == 1) && (plan[8] == 0 || plan[8] == 1) &&
-             (plan[9] == 0 || plan[9] == 1) && plan[10] >= 0 && plan[10] <= 3);
+             (plan[9] == 0 || plan[9] == 1) && plan[10] >= 0 && plan[10] <= 4);
     CK(cudaSetDevice(b->device));
     b->plan.warp_mode = plan[0];
     b->plan.warp_warps = plan[1];

@@ -366,9 +366,10 @@ gbpf_status gbpf_batch_kernel_times(gbpf_batch *b, int repeats, double ms[3]);
  * state: level 1 keeps the per-bus arrays that no other bus's row reads
  * (theta, P, Q and, in the FP32-LU form, |V| and the FP64 phasor) in an
  * L2-resident global region instead of shared memory, level 2 every per-bus
- * array but the flags and the substitution vectors; plan[10] = 1 takes the
- * level with the most instances per SM, then the most factors in shared
- * memory, then the lower level; 2 = level 1, 3 = level 2 wherever they fit;
+ * array but the flags and the substitution vectors, level 3 is level 2
+ * compiled for four blocks per SM (64 registers a thread); plan[10] = 1 takes
+ * the level with the most instances per SM, then the most factors in shared
+ * memory, then the lower level; 2, 3, 4 = level 1, 2, 3 wherever it fits;
  * 0 = level 0 (all in shared memory).  get_plan also returns plan[11] warps
  * per block in use, plan[12] instances on warps, plan[13] instances on
  * blocks, plan[14] the placement level in use (plan[15] = 0).

@@ -369,9 +369,9 @@ def test_block_mode_shared_flat_start(gb, oracle):
 def test_block_state_in_global_memory_is_exact(gb, prec):
     """Thread-block instances with part of their state in global memory (plan
     gstate 2: the own-bus arrays; gstate 3: every per-bus array but the flags
-    and y, z; the default picks the level with the most instances per SM, e.g.
-    level 1 for the FP32-LU form of a 1,888-bus grid, level 2 for its FP64
-    form) do the same arithmetic as with all of it in shared memory:
+    and y, z; gstate 4: that, compiled for four blocks per SM; the default
+    picks the level with the most instances per SM, e.g. level 3 for a 1,888-bus
+    grid) do the same arithmetic as with all of it in shared memory:
     iterations, statuses, switch events, |V| and theta bit for bit, for a grid
     whose factor is in shared memory and one whose factor is in global
     scratch."""
@@ -385,7 +385,7 @@ def test_block_state_in_global_memory_is_exact(gb, prec):
         Pl, Ql = base["Pload"] * lf, base["Qload"] * lf
         Pg = base["Pg"] * rng.uniform(0.85, 1.15, (n, grid.nB))
         out = []
-        for gstate, level in ((0, 0), (2, 1), (3, 2)):
+        for gstate, level in ((0, 0), (2, 1), (3, 2), (4, 3)):
             b = gb.Batch([grid], precision=getattr(gb, prec), tolerancia=1e-8, no_max_iter=30, lim_inj_reat=1)
             b.set_plan(warp_mode=0, gstate=gstate)
             b.set_instances(np.zeros(n, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
@@ -400,3 +400,4 @@ def test_block_state_in_global_memory_is_exact(gb, prec):
             assert e1 == e0
         assert out[2][2]["smem_bytes"] < out[1][2]["smem_bytes"] < i0["smem_bytes"]
         assert out[2][2]["factors_in_smem"] >= i0["factors_in_smem"]
+        assert out[3][2]["blocks"] >= out[2][2]["blocks"]
