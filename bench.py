@@ -356,7 +356,7 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     pl = fast.plan()
     twin.set_plan(**{k: pl[k] for k in ("warp_mode", "warps_per_block", "handoff_it", "resume_group",
                                         "warp_group", "narrow", "lu1", "warp_lu1", "flat_shared", "rotate",
-                                        "gstate")})
+                                        "gstate", "warp_gstate")})
     twin.solve()
     assert np.array_equal(twin.results(state=False)["status"], r["status"])
     pair = [fast, twin]

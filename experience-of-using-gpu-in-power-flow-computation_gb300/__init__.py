@@ -550,25 +550,25 @@ class Batch:
         return [tuple(int(x) for x in ev[4 * i:4 * i + 4]) for i in range(n.value)]
 
     PLAN_KEYS = ("warp_mode", "warps_per_block", "handoff_it", "resume_group", "warp_group", "narrow", "lu1",
-                 "warp_lu1", "flat_shared", "rotate", "gstate", "warps_per_block_used", "warp_instances",
-                 "block_instances", "block_state_global")
+                 "warp_lu1", "flat_shared", "rotate", "gstate", "warp_gstate", "warps_per_block_used",
+                 "warp_instances", "block_instances", "block_state_global", "warp_state_global")
 
     def plan(self):
         """The launch plan (gbpf_batch_get_plan)."""
-        a = np.zeros(16, np.int32)
+        a = np.zeros(20, np.int32)
         _check(lib().gbpf_batch_get_plan(self.h, _p(a)), "gbpf_batch_get_plan")
         return dict(zip(self.PLAN_KEYS, (int(x) for x in a)))
 
     def set_plan(self, warp_mode=1, warps_per_block=8, handoff_it=12, resume_group=1, warp_group=1, narrow=0,
-                 lu1=1, warp_lu1=0, flat_shared=1, rotate=0, gstate=1):
+                 lu1=1, warp_lu1=0, flat_shared=1, rotate=0, gstate=1, warp_gstate=1):
         a = np.array([warp_mode, warps_per_block, handoff_it, resume_group, warp_group, narrow, lu1, warp_lu1,
-                      flat_shared, rotate, gstate], np.int32)
+                      flat_shared, rotate, gstate, warp_gstate], np.int32)
         _check(lib().gbpf_batch_set_plan(self.h, _p(a)), "gbpf_batch_set_plan")
 
     def autotune(self, repeats=3):
         """Coordinate search over the launch plan on the current instances;
         returns (plan, ms of the starting plan, ms of the chosen plan)."""
-        a = np.zeros(16, np.int32)
+        a = np.zeros(20, np.int32)
         ms = np.zeros(2, np.float32)
         _check(lib().gbpf_batch_autotune(self.h, int(repeats), _p(a), _p(ms)), "gbpf_batch_autotune")
         return dict(zip(self.PLAN_KEYS, (int(x) for x in a))), float(ms[0]), float(ms[1])

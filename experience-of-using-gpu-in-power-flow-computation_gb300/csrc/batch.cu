@@ -1085,8 +1085,12 @@ __global__ void __launch_bounds__(32) k_flat_start(const Topo T, char *out, int 
     if (lane == 0) *(int *)(out + F.sing) = sing ? 1 : 0;
 }
 
-template <typename TJ>
-__global__ void __launch_bounds__(32 * kWarpsMax, 1) k_nr_warp(Args a) {
+// GS: the state placement level of layout() (the region of warp w of block b
+// starts at gstate + (b * warps per block + w) * gstate_stride); 3 = level 2
+// compiled for two blocks of 16 warps per SM (64 registers a thread).
+template <typename TJ, int GS>
+__global__ void __launch_bounds__(32 * kWarpsMax, GS == 3 ? 2 : 1) k_nr_warp(Args a) {
+    constexpr int LV = GS > 2 ? 2 : GS;
     using B4 = typename Blk<TJ>::b4;
     using B2 = typename Blk<TJ>::b2;
     constexpr unsigned FULL = 0xffffffffu;
@@ -1105,12 +1109,16 @@ __global__ void __launch_bounds__(32 * kWarpsMax, 1) k_nr_warp(Args a) {
         const Topo T = a.topo[t_id];
         const TopoView G = bind(T.o, T.blob);
         const long long off = a.inst_off[inst];
-        const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, 1, a.lu1);
-        double *V = (double *)(ism + L.V), *th = (double *)(ism + L.th);
-        double *cs = (double *)(ism + L.cs), *sn = (double *)(ism + L.sn);
-        double2 *ef = (double2 *)(ism + L.ef);
-        float4 *f32 = (float4 *)(ism + L.f32);
-        double *P = (double *)(ism + L.P), *Q = (double *)(ism + L.Q), *QL = (double *)(ism + L.QL);
+        const Layout L = layout<TJ>(T.nB, T.n, T.nup, T.nPV, 1, a.lu1, LV);
+        unsigned char *gst =
+            LV ? a.gstate + ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * a.gstate_stride : ism;
+        unsigned char *vst = (LV >= 2 || (LV && sizeof(TJ) == 4)) ? gst : ism;
+        unsigned char *pst = LV >= 2 ? gst : ism;  // phasors
+        double *V = (double *)(vst + L.V), *th = (double *)(gst + L.th);
+        double *cs = (double *)(vst + L.cs), *sn = (double *)(vst + L.sn);
+        double2 *ef = (double2 *)(pst + L.ef);
+        float4 *f32 = (float4 *)(pst + L.f32);
+        double *P = (double *)(gst + L.P), *Q = (double *)(gst + L.Q), *QL = (double *)(gst + L.QL);
         unsigned char *act = ism + L.act;
         int *limQ = (int *)(ism + L.lim);
         B2 *ys = (B2 *)(ism + L.ys);
@@ -1637,6 +1645,12 @@ __global__ void k_pack_inputs(PackArgs a) {
 // ---------------------------------------------------------------------------
 // The block kernel of a state placement level (layout gs), as a function
 // handle for attributes and occupancy queries.
+template <typename TJ> const void *warp_kernel(int gs) {
+    if (gs == 3) return (const void *)k_nr_warp<TJ, 3>;
+    if (gs == 2) return (const void *)k_nr_warp<TJ, 2>;
+    if (gs == 1) return (const void *)k_nr_warp<TJ, 1>;
+    return (const void *)k_nr_warp<TJ, 0>;
+}
 template <typename TJ> const void *blk_kernel(int gs) {
     if (gs == 3) return (const void *)k_nr_block<TJ, 3>;
     if (gs == 2) return (const void *)k_nr_block<TJ, 2>;
@@ -1722,10 +1736,11 @@ struct gbpf_batch {
     // never.
     struct Plan {
         int warp_mode = 1, warp_warps = 8, handoff_it = kHandoffIt, resume_group = 1, warp_group = 1, narrow = 0,
-            lu1 = 1, warp_lu1 = 0, flat_shared = 1, rotate = 0, gstate = 1;
+            lu1 = 1, warp_lu1 = 0, flat_shared = 1, rotate = 0, gstate = 1, warp_gstate = 1;
     } plan;
     int block_gs = 0;  // placement level of the block-mode launch's state (layout gs)
-    DevBuf gstate_mem;
+    int warp_gs = 0;   // ... and of the warp launch's
+    DevBuf gstate_mem, warp_gstate_mem;
     gbpf_status rebuild() {
         CK(cudaStreamSynchronize(stream));
         if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
@@ -2012,8 +2027,18 @@ gbpf_status gbpf_batch::launch_with(cudaStream_t st, const Args &ba, const Args 
     }
     if (wa.queue_len) {
         if (timed) CK(cudaEventRecordWithFlags(kev[2], st, cudaEventRecordExternal));
-        if (fp32) k_nr_warp<float><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wa);
-        else k_nr_warp<double><<<warp_grid, 32 * warp_warps, warp_smem, st>>>(wa);
+        const dim3 wg(warp_grid), wb(32 * warp_warps);
+        if (fp32) {
+            if (warp_gs == 3) k_nr_warp<float, 3><<<wg, wb, warp_smem, st>>>(wa);
+            else if (warp_gs == 2) k_nr_warp<float, 2><<<wg, wb, warp_smem, st>>>(wa);
+            else if (warp_gs == 1) k_nr_warp<float, 1><<<wg, wb, warp_smem, st>>>(wa);
+            else k_nr_warp<float, 0><<<wg, wb, warp_smem, st>>>(wa);
+        } else {
+            if (warp_gs == 3) k_nr_warp<double, 3><<<wg, wb, warp_smem, st>>>(wa);
+            else if (warp_gs == 2) k_nr_warp<double, 2><<<wg, wb, warp_smem, st>>>(wa);
+            else if (warp_gs == 1) k_nr_warp<double, 1><<<wg, wb, warp_smem, st>>>(wa);
+            else k_nr_warp<double, 0><<<wg, wb, warp_smem, st>>>(wa);
+        }
         CK_LAUNCH();
         if (timed) CK(cudaEventRecordWithFlags(kev[3], st, cudaEventRecordExternal));
         if (wa.handoff_it > 0) {
@@ -2118,8 +2143,9 @@ gbpf_status gbpf_batch::build_graph() {
         return GBPF_OK;
     };
     // Placement level: gstate 2 / 3 / 4 take level 1 / 2 / 3 where it fits;
-    // gstate 1 the level with the most blocks per SM, then the most factors in
-    // shared memory, then the least state in global memory.  Measured on
+    // gstate 1 a level with at least 1.5x the blocks per SM (global state
+    // costs latency, which only more blocks per SM win back), else one with
+    // as many and more factors in shared memory, else the lower.  Measured on
     // 8,192 instances of a 1,888-bus grid (solves/s): FP32 level 0 124 k
     // (1 block per SM), 1 194 k (2), 2 199 k (2), 3 290 k (4; 279 k at 5 and
     // 217 k at 6 blocks per SM, where spills grow), and 133 k with the factor
@@ -2134,7 +2160,8 @@ gbpf_status gbpf_batch::build_graph() {
             BlockPlan c;
             if ((pst = plan_blocks(gs, budget, c)) != GBPF_OK) return pst;
             const bool take = plan.gstate >= 2 ? (gs == plan.gstate - 1 && c.occ > 0)
-                                               : (c.occ > bp.occ || (c.occ == bp.occ && c.occ > 0 && c.nfac > bp.nfac));
+                                               : (2 * c.occ >= 3 * bp.occ && c.occ > 0) ||
+                                                     (c.occ == bp.occ && c.occ > 0 && c.nfac > bp.nfac);
             if (take) {
                 bp = c;
                 block_gs = gs;
@@ -2197,22 +2224,58 @@ gbpf_status gbpf_batch::build_graph() {
         args.gstate = (unsigned char *)gstate_mem.p;
     }
     // warp-mode plan: as many warps per block as fit in the block's shared
-    // memory, at most 16 (one block per SM; 128 registers a thread)
+    // memory, at most 16 (128 registers a thread; 64 at level 3), capped by
+    // plan.warp_warps.  Placement level as for the blocks (plan.warp_gstate):
+    // 1 = a level with at least 1.5x the warps per SM.  Measured on 32,768
+    // instances of a 118-bus grid: FP32 level 0 8 warps per SM, warp kernel
+    // 8.14 ms; level 2 16 warps per SM, 6.65 ms; FP64 level 0 7 warps per SM
+    // 25.3 ms, level 2 8 warps per SM 25.8 ms.
     warp_grid = 0;
+    warp_gs = 0;
+    size_t warp_gstride = 0;
     if (n_warp_q) {
-        warp_warps = (int)std::max<size_t>(1, std::min<size_t>(kWarpsMax, (size_t)maxsm / slice));
-        if (plan.warp_warps > 0) warp_warps = std::min(warp_warps, plan.warp_warps);
-        warp_smem = (size_t)warp_warps * slice;
-        int occ = 0;
-        if (fp32) {
-            CK(cudaFuncSetAttribute(k_nr_warp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warp_smem));
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_warp<float>, 32 * warp_warps, warp_smem));
-        } else {
-            CK(cudaFuncSetAttribute(k_nr_warp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warp_smem));
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_warp<double>, 32 * warp_warps, warp_smem));
+        struct WarpPlan { int warps = 0, occ = 0; size_t slice = 0, gst = 0; };
+        auto plan_warps = [&](int gs, WarpPlan &wp) -> gbpf_status {
+            const int lv = std::min(gs, 2);
+            for (size_t t = 0; t < topo_h.size(); t++) {
+                if (!warp_ok[t]) continue;
+                const Topo &T = topo_h[t];
+                const Layout w = fp32 ? layout<float>(T.nB, T.n, T.nup, T.nPV, 1, plan.warp_lu1, lv)
+                                      : layout<double>(T.nB, T.n, T.nup, T.nPV, 1, plan.warp_lu1, lv);
+                wp.slice = std::max(wp.slice, align_up(w.total, 128));
+                wp.gst = std::max(wp.gst, w.gtotal);
+            }
+            wp.warps = (int)std::max<size_t>(1, std::min<size_t>(kWarpsMax, (size_t)maxsm / wp.slice));
+            if (plan.warp_warps > 0) wp.warps = std::min(wp.warps, plan.warp_warps);
+            const size_t sm = (size_t)wp.warps * wp.slice;
+            const void *fn = fp32 ? warp_kernel<float>(gs) : warp_kernel<double>(gs);
+            CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&wp.occ, fn, 32 * wp.warps, sm));
+            return GBPF_OK;
+        };
+        WarpPlan wp;
+        gbpf_status wst = plan_warps(0, wp);
+        if (wst != GBPF_OK) return wst;
+        if (plan.warp_gstate) {
+            for (int gs = 1; gs <= 3; gs++) {
+                WarpPlan c;
+                if ((wst = plan_warps(gs, c)) != GBPF_OK) return wst;
+                const bool take = plan.warp_gstate >= 2 ? (gs == plan.warp_gstate - 1 && c.occ > 0)
+                                                        : 2 * c.occ * c.warps >= 3 * wp.occ * wp.warps;
+                if (take) {
+                    wp = c;
+                    warp_gs = gs;
+                }
+            }
         }
-        warp_grid = std::max(1, std::min((n_warp_q + warp_warps - 1) / warp_warps, dev_sm * std::max(occ, 1)));
+        slice = wp.slice;
+        warp_warps = wp.warps;
+        warp_smem = (size_t)warp_warps * slice;
+        warp_grid = std::max(1, std::min((n_warp_q + warp_warps - 1) / warp_warps, dev_sm * std::max(wp.occ, 1)));
+        warp_gstride = warp_gs ? align_up(wp.gst, 256) : 0;
     }
+    warp_gstate_mem.reset();
+    if (warp_gs) CK(cudaMalloc(&warp_gstate_mem.p, warp_gstride * (size_t)warp_grid * warp_warps));
     // the shared flat-start iteration of every topology
     flat_mem.reset();
     for (auto &T : topo_h) T.flat = nullptr;
@@ -2264,6 +2327,8 @@ gbpf_status gbpf_batch::build_graph() {
     wargs.queue = (const int *)queues.p;
     wargs.queue_len = n_warp_q;
     wargs.slice = (int)slice;
+    wargs.gstate = (unsigned char *)warp_gstate_mem.p;
+    wargs.gstate_stride = (long long)warp_gstride;
     wargs.warp_group = plan.warp_group;
     args.narrow = plan.narrow;
     args.lu1 = plan.lu1;
@@ -2425,6 +2490,7 @@ gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
         {&Plan::flat_shared, {1, 0}, false, false, false},
         {&Plan::rotate, {0, 1}, false, false, false},
         {&Plan::gstate, {1, 0, 2, 3, 4}, false, false, true},
+        {&Plan::warp_gstate, {1, 0, 2, 3, 4}, true, false, false},
     };
     for (int sweep = 0; sweep < 2; sweep++) {
         bool changed = false;
@@ -2452,7 +2518,7 @@ gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
     return st;
 }
 
-static void plan_out(const gbpf_batch *b, int plan[16]) {
+static void plan_out(const gbpf_batch *b, int plan[20]) {
     plan[0] = b->plan.warp_mode;
     plan[1] = b->plan.warp_warps;
     plan[2] = b->plan.handoff_it;
@@ -2464,24 +2530,26 @@ static void plan_out(const gbpf_batch *b, int plan[16]) {
     plan[8] = b->plan.flat_shared;
     plan[9] = b->plan.rotate;
     plan[10] = b->plan.gstate;
-    plan[11] = b->warp_warps;  // warps per block in use
-    plan[12] = b->n_warp_q;
-    plan[13] = b->n_block_q;
-    plan[14] = b->block_gs;
-    plan[15] = 0;
+    plan[11] = b->plan.warp_gstate;
+    plan[12] = b->warp_warps;  // warps per block in use
+    plan[13] = b->n_warp_q;
+    plan[14] = b->n_block_q;
+    plan[15] = b->block_gs;
+    plan[16] = b->warp_gs;
+    for (int i = 17; i < 20; i++) plan[i] = 0;
 }
 
-extern "C" gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[16]) {
+extern "C" gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[20]) {
     ARGCHECK(b && plan);
     plan_out(b, plan);
     return GBPF_OK;
 }
 
-extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[11]) {
+extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[12]) {
     ARGCHECK(b && plan && (plan[0] == 0 || plan[0] == 1) && plan[1] >= 0 && plan[1] <= kWarpsMax && plan[2] >= 0 &&
              (plan[3] == 0 || plan[3] == 1) && (plan[4] == 0 || plan[4] == 1) && (plan[5] == 0 || plan[5] == 1) &&
              (plan[6] == 0 || plan[6] == 1) && (plan[7] == 0 || plan[7] == 1) && (plan[8] == 0 || plan[8] == 1) &&
-             (plan[9] == 0 || plan[9] == 1) && plan[10] >= 0 && plan[10] <= 4);
+             (plan[9] == 0 || plan[9] == 1) && plan[10] >= 0 && plan[10] <= 4 && plan[11] >= 0 && plan[11] <= 4);
     CK(cudaSetDevice(b->device));
     b->plan.warp_mode = plan[0];
     b->plan.warp_warps = plan[1];
@@ -2494,11 +2562,12 @@ extern "C" gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[11]) {
     b->plan.flat_shared = plan[8];
     b->plan.rotate = plan[9];
     b->plan.gstate = plan[10];
+    b->plan.warp_gstate = plan[11];
     if (!b->n_inst) return GBPF_OK;
     return b->rebuild();
 }
 
-extern "C" gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[16], float ms[2]) {
+extern "C" gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[20], float ms[2]) {
     ARGCHECK(b && b->exec && repeats > 0);
     CK(cudaSetDevice(b->device));
     float best = 0, first = 0;

@@ -368,16 +368,18 @@ gbpf_status gbpf_batch_kernel_times(gbpf_batch *b, int repeats, double ms[3]);
  * L2-resident global region instead of shared memory, level 2 every per-bus
  * array but the flags and the substitution vectors, level 3 is level 2
  * compiled for four blocks per SM (64 registers a thread); plan[10] = 1 takes
- * the level with the most instances per SM, then the most factors in shared
- * memory, then the lower level; 2, 3, 4 = level 1, 2, 3 wherever it fits;
- * 0 = level 0 (all in shared memory).  get_plan also returns plan[11] warps
- * per block in use, plan[12] instances on warps, plan[13] instances on
- * blocks, plan[14] the placement level in use (plan[15] = 0).
- * Setting a plan rebuilds the batch graph. */
-gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[16]);
-gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[11]);
+ * a level with at least 1.5x the instances per SM, else one with as many and
+ * more factors in shared memory, else the lower level; 2, 3, 4 = level 1, 2,
+ * 3 wherever it fits; 0 = level 0 (all in shared memory); plan[11] the same
+ * for the warp kernel's instances (level 3 there: two blocks of 16 warps per
+ * SM).  get_plan also returns plan[12]
+ * warps per block in use, plan[13] instances on warps, plan[14] instances on
+ * blocks, plan[15] / plan[16] the placement level in use for blocks / warps
+ * (plan[17..19] = 0).  Setting a plan rebuilds the batch graph. */
+gbpf_status gbpf_batch_get_plan(const gbpf_batch *b, int plan[20]);
+gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[12]);
 
-/* Autotuner: a coordinate search over plan[0..10] on the current instances,
+/* Autotuner: a coordinate search over plan[0..11] on the current instances,
  * from the default plan.  Each knob takes each of its values in turn with the
  * others fixed; a value is kept when the whole batch solve (best of `repeats`
  * timed graph launches after one warm-up, CUDA events on the batch stream) is
@@ -385,7 +387,7 @@ gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[11]);
  * The best plan stays set; plan receives it (as gbpf_batch_get_plan) and
  * ms[0] / ms[1] the batch time of the default and of the chosen plan.  The
  * trial solves overwrite the instances' results. */
-gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[16], float ms[2]);
+gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[20], float ms[2]);
 
 /* Per-instance results of the last batch solve (any pointer may be NULL);
  * V/theta/P/Q packed like the inputs.  Each array is copied from the device

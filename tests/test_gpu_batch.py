@@ -195,6 +195,8 @@ PLANS = [
     dict(warp_mode=0, lu1=0),
     dict(warp_lu1=1, handoff_it=8),                     # one-pass levels in the warps too
     dict(rotate=1),                                     # FP32 phasors by rotation (FP64 here: no effect)
+    dict(warp_gstate=3, warps_per_block=0),             # warp state in global memory, 16 warps per block
+    dict(warp_mode=0, gstate=4),                        # block state in global memory, 4 blocks per SM
 ]
 
 
@@ -401,3 +403,34 @@ def test_block_state_in_global_memory_is_exact(gb, prec):
         assert out[2][2]["smem_bytes"] < out[1][2]["smem_bytes"] < i0["smem_bytes"]
         assert out[2][2]["factors_in_smem"] >= i0["factors_in_smem"]
         assert out[3][2]["blocks"] >= out[2][2]["blocks"]
+
+
+@pytest.mark.parametrize("prec", ["PREC_FP64", "PREC_FP32_IR"])
+def test_warp_state_in_global_memory_is_exact(gb, prec):
+    """The warp kernel with its state placed in global memory (plan
+    warp_gstate 2, 3, 4: levels 1, 2 and 3, the last at 64 registers a
+    thread) gives what it gives with all of it in shared memory, bit for bit,
+    stragglers handed to blocks included."""
+    path = os.path.join(GOLDEN, "c2_s3.cdf")
+    grid = gb.read_grid(path)
+    base = grid.buses()
+    rng = np.random.default_rng(9)
+    n = 96
+    lf = rng.uniform(0.8, 1.2, (n, grid.nB))
+    Pl, Ql = base["Pload"] * lf, base["Qload"] * lf
+    Pg = base["Pg"] * rng.uniform(0.9, 1.1, (n, grid.nB))
+    out = []
+    for wg, level in ((0, 0), (2, 1), (3, 2), (4, 3)):
+        b = gb.Batch([grid], precision=getattr(gb, prec), tolerancia=1e-8, no_max_iter=30, lim_inj_reat=1)
+        b.set_plan(warp_gstate=wg, handoff_it=6)
+        b.set_instances(np.zeros(n, np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
+        b.solve()
+        pl = b.plan()
+        assert pl["warp_state_global"] == level and pl["warp_instances"] == n
+        out.append((b.results(), [b.events(i) for i in range(n)]))
+    r0, e0 = out[0]
+    assert (r0["status"] == 0).mean() > 0.8 and (r0["iterations"] > 6).any()
+    for r1, e1 in out[1:]:
+        for k in ("iterations", "status", "n_events", "V", "theta", "Pcalc", "Qcalc", "final_mismatch"):
+            np.testing.assert_array_equal(r1[k], r0[k], err_msg=k)
+        assert e1 == e0
