@@ -2512,6 +2512,21 @@ gbpf_status gbpf_batch::autotune(int repeats, float *best_ms, float *first_ms) {
         }
         if (!changed) break;
     }
+    // joint trials the one-knob search cannot reach: the 64-register warp
+    // kernel (level 3) pays off only with more warps per block than the
+    // default, each change alone is slower (118-bus FP32: level 3 with 9
+    // warps per block, 18 per SM, 5 % faster than level 2 with 8)
+    if (any_warp && cur.warp_mode) {
+        for (int w : {9, 10, 12}) {
+            Plan c = cur;
+            c.warp_gstate = 4;
+            c.warp_warps = w;
+            float ms = 0;
+            st = timed(c, &ms);
+            if (st != GBPF_OK) return st;
+            if (ms < 0.98f * cur_ms) { cur = c; cur_ms = ms; }
+        }
+    }
     plan = cur;
     st = rebuild();
     if (best_ms) *best_ms = cur_ms;

@@ -383,8 +383,9 @@ gbpf_status gbpf_batch_set_plan(gbpf_batch *b, const int plan[12]);
  * from the default plan.  Each knob takes each of its values in turn with the
  * others fixed; a value is kept when the whole batch solve (best of `repeats`
  * timed graph launches after one warm-up, CUDA events on the batch stream) is
- * at least 2 % faster; a second sweep runs when the first changed the plan.
- * The best plan stays set; plan receives it (as gbpf_batch_get_plan) and
+ * at least 2 % faster; a second sweep runs when the first changed the plan,
+ * then joint trials of the warp kernel's placement level 3 with 9, 10 and 12
+ * warps per block (each change alone is slower).  The best plan stays set; plan receives it (as gbpf_batch_get_plan) and
  * ms[0] / ms[1] the batch time of the default and of the chosen plan.  The
  * trial solves overwrite the instances' results. */
 gbpf_status gbpf_batch_autotune(gbpf_batch *b, int repeats, int plan[20], float ms[2]);
