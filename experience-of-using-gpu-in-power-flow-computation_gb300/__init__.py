@@ -46,6 +46,7 @@ EXPORTS = [
     "gbpf_grid_write_m", "gbpf_grid_ybus_form", "gbpf_grid_set_ybus_form",
     "gbpf_batch_get_plan", "gbpf_batch_set_plan", "gbpf_batch_autotune",
     "gbpf_batch_launch", "gbpf_batch_wait", "gbpf_batch_time_pipelined", "gbpf_batch_warm_phases",
+    "gbpf_batch_solve_warm_launch", "gbpf_batch_solve_warm_wait",
 ]
 
 
@@ -590,6 +591,22 @@ class Batch:
             self.h, len(gi), _p(gi), vp(V0), vp(theta0), vp(Pliq), vp(Qliq), vp(Qload), vp(V), vp(theta),
             vp(Pcalc), vp(Qcalc), vp(iterations), vp(status), vp(final_mismatch), vp(stream)),
             "gbpf_batch_solve_noalloc")
+
+    def solve_warm_launch(self, mlp):
+        """gbpf_batch_solve_warm_launch: the warm-started solve without
+        waiting for it; solve_warm_wait() returns what solve_warm returns."""
+        _check(lib().gbpf_batch_solve_warm_launch(self.h, mlp.h), "gbpf_batch_solve_warm_launch")
+
+    def solve_warm_wait(self):
+        kind = np.zeros(self.n_inst, np.int32)
+        wit = np.zeros(self.n_inst, np.int32)
+        ms = ctypes.c_double()
+        _check(lib().gbpf_batch_solve_warm_wait(self.h, _p(kind), _p(wit), ctypes.byref(ms)),
+               "gbpf_batch_solve_warm_wait")
+        ph = np.zeros(3)
+        _check(lib().gbpf_batch_warm_phases(self.h, _p(ph)), "gbpf_batch_warm_phases")
+        return dict(start_kind=kind, warm_iterations=wit, ms=ms.value,
+                    phases_ms=dict(network=ph[0], start_choice=ph[1], newton=ph[2]))
 
     def solve_warm(self, mlp):
         """gbpf_batch_solve_warm: Newton from the network's predicted start

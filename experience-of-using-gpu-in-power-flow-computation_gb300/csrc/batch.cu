@@ -425,14 +425,18 @@ __device__ __forceinline__ B4 diag_block32(float Pk, float Qk, float vk, float2 
 }
 
 // Phasor of bus k from th[k], V[k]: cos, sin, e = V (cos, sin) and, for the
-// FP32-LU form, the FP32 copies (cos, sin, V) its Jacobian reads.
+// FP32-LU form, the FP32 copies (cos, sin, V) its Jacobian reads.  The FP64
+// cos, sin are stored only where something reads them (keep_cs: the FP64
+// Jacobian, the phasor rotation).
 template <typename TJ>
 __device__ __forceinline__ void phasor(int k, const double *th, const double *V, double *cs, double *sn, double2 *ef,
-                                       float4 *f32) {
+                                       float4 *f32, bool keep_cs = true) {
     double s, c;
     sincos(th[k], &s, &c);
-    cs[k] = c;
-    sn[k] = s;
+    if (keep_cs) {
+        cs[k] = c;
+        sn[k] = s;
+    }
     ef[k] = make_double2(V[k] * c, V[k] * s);
     if (sizeof(TJ) == 4) f32[k] = make_float4((float)c, (float)s, (float)V[k], 0.f);
 }
@@ -731,6 +735,7 @@ __global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) 
     __shared__ int s_inst, s_done, s_status, s_it, s_nev, s_topo, s_wcnt[kWarps];
     __shared__ double s_maxG, s_maxDx;
     const unsigned long long tol_bits = abits(a.tol), tol10_bits = abits(a.tol * 10.);
+    const bool keep_cs = sizeof(TJ) == 8 || a.rotate;  // who reads the FP64 cos, sin
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     unsigned char *ism = smem + a.blob_region;  // per-instance region
     if (tid == 0) s_topo = -1;
@@ -821,8 +826,10 @@ __global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) 
                 const bool f0 = flat && s_it == 0;
                 if (f0) {
                     for (int k = tid; k < nB; k += kThreads) {
-                        cs[k] = ((const double *)(flat + F.cs))[k];
-                        sn[k] = ((const double *)(flat + F.sn))[k];
+                        if (keep_cs) {
+                            cs[k] = ((const double *)(flat + F.cs))[k];
+                            sn[k] = ((const double *)(flat + F.sn))[k];
+                        }
                         ef[k] = ((const double2 *)(flat + F.ef))[k];
                         if (sizeof(TJ) == 4) f32[k] = ((const float4 *)(flat + F.f32))[k];
                         P[k] = ((const double *)(flat + F.P))[k];
@@ -832,7 +839,7 @@ __global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) 
                     // phasors (the FP32-LU form may rotate them in the update
                     // instead) and injections
                     if (sizeof(TJ) == 8 || fresh || !a.rotate)
-                        for (int k = tid; k < nB; k += kThreads) phasor<TJ>(k, th, V, cs, sn, ef, f32);
+                        for (int k = tid; k < nB; k += kThreads) phasor<TJ>(k, th, V, cs, sn, ef, f32, keep_cs);
                     __syncthreads();
                     for (int k = tid; k < nB; k += kThreads) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
                 }
@@ -1099,6 +1106,7 @@ __global__ void __launch_bounds__(32 * kWarpsMax, GS == 3 ? 2 : 1) k_nr_warp(Arg
     unsigned char *ism = smem + (size_t)(threadIdx.x >> 5) * a.slice;
     const unsigned lt_mask = (1u << lane) - 1u;
     const unsigned long long tol_bits = abits(a.tol), tol10_bits = abits(a.tol * 10.);
+    const bool keep_cs = sizeof(TJ) == 8 || a.rotate;  // who reads the FP64 cos, sin
     for (;;) {
         int q = 0;
         if (lane == 0) q = atomicAdd(a.counter, 1);
@@ -1169,8 +1177,10 @@ __global__ void __launch_bounds__(32 * kWarpsMax, GS == 3 ? 2 : 1) k_nr_warp(Arg
                 if (f0) {
                     // the shared iteration 0 of this topology's start
                     for (int k = lane; k < nB; k += 32) {
-                        cs[k] = ((const double *)(flat + F.cs))[k];
-                        sn[k] = ((const double *)(flat + F.sn))[k];
+                        if (keep_cs) {
+                            cs[k] = ((const double *)(flat + F.cs))[k];
+                            sn[k] = ((const double *)(flat + F.sn))[k];
+                        }
                         ef[k] = ((const double2 *)(flat + F.ef))[k];
                         if (sizeof(TJ) == 4) f32[k] = ((const float4 *)(flat + F.f32))[k];
                         P[k] = ((const double *)(flat + F.P))[k];
@@ -1178,7 +1188,7 @@ __global__ void __launch_bounds__(32 * kWarpsMax, GS == 3 ? 2 : 1) k_nr_warp(Arg
                     }
                 } else {
                     if (sizeof(TJ) == 8 || it == 0 || !a.rotate)
-                        for (int k = lane; k < nB; k += 32) phasor<TJ>(k, th, V, cs, sn, ef, f32);
+                        for (int k = lane; k < nB; k += 32) phasor<TJ>(k, th, V, cs, sn, ef, f32, keep_cs);
                     __syncwarp();
                     for (int k = lane; k < nB; k += 32) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
                 }
@@ -1707,6 +1717,9 @@ struct gbpf_batch {
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         for (auto &e : wev) if (e) cudaEventDestroy(e);
+        if (mwork) gbpf::mlp_work_free(mwork);
+        if (h_kind) cudaFreeHost(h_kind);
+        if (h_witers) cudaFreeHost(h_witers);
         if (fork) cudaEventDestroy(fork);
         if (join) cudaEventDestroy(join);
         for (auto &e : kev) if (e) cudaEventDestroy(e);
@@ -1767,6 +1780,13 @@ struct gbpf_batch {
     gbpf_status launch_with(cudaStream_t st, const Args &ba, const Args &wa, bool timed = false);
     gbpf_status build_graph();
     gbpf_status solve_warm(gbpf_mlp *m, int *kind, int *warm_iters, float *ms);
+    // the same in two halves: everything enqueued on the batch stream, then
+    // the wait and the per-instance start kinds
+    gbpf_status warm_launch(gbpf_mlp *m);
+    gbpf_status warm_wait(int *kind, int *warm_iters, float *ms);
+    gbpf::MlpWork *mwork = nullptr;      // the network's activations for this batch
+    int *h_kind = nullptr, *h_witers = nullptr;  // pinned copies of wKind, wIters
+    bool warm_pending = false;
 };
 
 gbpf_status gbpf_batch::add_topology(const Grid &g) {
@@ -1910,6 +1930,7 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
 
 gbpf_status gbpf_batch::set_instances(int n, const int *tofi, const double *Pload, const double *Qload,
                                       const double *Pg, const double *Qg, const double *V0, const double *th0) {
+    if (warm_pending) { set_error("a warm-started solve is in flight: wait for it first"); return GBPF_E_ARG; }
     for (int i = 0; i < n; i++)
         if (tofi[i] < 0 || tofi[i] >= (int)grids.size()) { set_error("instance names an unknown grid"); return GBPF_E_ARG; }
     const bool same = exec && n == n_inst && std::equal(tofi, tofi + n, inst_topo.begin());
@@ -2367,7 +2388,14 @@ gbpf_status gbpf_batch::build_graph() {
 // from the prediction, are solved again from their own start.  kind[i]: 0 own start chosen up front, 1 predicted
 // start converged, 2 predicted start failed and the own start was used.
 gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, float *ms) {
+    gbpf_status st = warm_launch(m);
+    if (st != GBPF_OK) return st;
+    return warm_wait(kind_out, witers_out, ms);
+}
+
+gbpf_status gbpf_batch::warm_launch(gbpf_mlp *m) {
     if (!exec || n_inst < 1) { set_error("no instances: call gbpf_batch_set_instances first"); return GBPF_E_ARG; }
+    if (warm_pending) { set_error("a warm-started solve is in flight: wait for it first"); return GBPF_E_ARG; }
     const gbpf::MlpShape sh = gbpf::mlp_shape(m);
     const int t0 = inst_topo[0];
     const int nB = grids[t0].nB;
@@ -2380,9 +2408,13 @@ gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, 
     if (sh.device != device) { set_error("network and batch live on different devices"); return GBPF_E_ARG; }
     if (warm_n != n_inst) {
         warm_mem.reset();
+        if (h_kind) { cudaFreeHost(h_kind); h_kind = nullptr; }
+        if (h_witers) { cudaFreeHost(h_witers); h_witers = nullptr; }
         const size_t xb = align_up(2 * (size_t)n_inst * sh.kin, 256), pb = align_up(4 * (size_t)n_inst * sh.outp, 256),
                      vb = align_up(8 * (size_t)n_bus_total, 256), ib = align_up(4 * (size_t)n_inst, 256);
         CK(cudaMalloc(&warm_mem.p, xb + pb + 4 * vb + 4 * ib + 8 * kOrderClasses));
+        CK(cudaMallocHost(&h_kind, 4 * (size_t)n_inst));
+        CK(cudaMallocHost(&h_witers, 4 * (size_t)n_inst));
         char *p = (char *)warm_mem.p;
         wX = (__nv_bfloat16 *)p; wPred = (float *)(p + xb);
         p += xb + pb;
@@ -2392,12 +2424,13 @@ gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, 
         wHist = (int *)(p + 4 * ib);  // class counts, then the order's cursors
         warm_n = n_inst;
     }
+    if (!mwork) mwork = gbpf::mlp_work_create();
     CK(cudaEventRecord(ev0, stream));
     CK(cudaMemsetAsync(wHist, 0, 8 * kOrderClasses, stream));
     k_ws_features<<<1024, 256, 0, stream>>>(args.Pliq, args.Qliq, args.V0, args.inst_off, n_inst, nB, sh.n_in, sh.kin,
                                             sh.in_mean, sh.in_iscale, wX);
     CK_LAUNCH();
-    gbpf_status st = gbpf::mlp_infer(m, wX, n_inst, wPred, stream);
+    gbpf_status st = gbpf::mlp_infer(m, wX, n_inst, wPred, stream, mwork);
     if (st != GBPF_OK) return st;
     CK(cudaEventRecord(wev[0], stream));
     k_ws_select<<<n_inst, kSelThreads, 0, stream>>>(args, wPred, sh.outp, sh.out_mean, sh.out_scale, wV, wTh, wEF,
@@ -2420,18 +2453,24 @@ gbpf_status gbpf_batch::solve_warm(gbpf_mlp *m, int *kind_out, int *witers_out, 
     }
     (wa.queue_len ? wa.queue : ba.queue) = wQueue;
     if ((st = launch_with(stream, ba, wa)) != GBPF_OK) return st;
-    std::vector<int> kind(n_inst), witers(n_inst);
-    CK(cudaMemcpyAsync(kind.data(), wKind, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
-    if (witers_out) CK(cudaMemcpyAsync(witers.data(), wIters, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h_kind, wKind, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h_witers, wIters, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
     CK(cudaEventRecord(ev1, stream));
+    warm_pending = true;
+    return GBPF_OK;
+}
+
+gbpf_status gbpf_batch::warm_wait(int *kind_out, int *witers_out, float *ms) {
+    if (!warm_pending) { set_error("no warm-started solve in flight"); return GBPF_E_ARG; }
+    warm_pending = false;
     CK(cudaEventSynchronize(ev1));
     if (ms) CK(cudaEventElapsedTime(ms, ev0, ev1));
     CK(cudaEventElapsedTime(&warm_ms[0], ev0, wev[0]));
     CK(cudaEventElapsedTime(&warm_ms[1], wev[0], wev[1]));
     CK(cudaEventElapsedTime(&warm_ms[2], wev[1], ev1));
     if (witers_out)
-        for (int i = 0; i < n_inst; i++) witers_out[i] = kind[i] ? witers[i] : 0;
-    if (kind_out) std::copy(kind.begin(), kind.end(), kind_out);
+        for (int i = 0; i < n_inst; i++) witers_out[i] = h_kind[i] ? h_witers[i] : 0;
+    if (kind_out) std::copy(h_kind, h_kind + n_inst, kind_out);
     return GBPF_OK;
 }
 
@@ -2876,6 +2915,21 @@ extern "C" gbpf_status gbpf_batch_solve_warm(gbpf_batch *b, gbpf_mlp *m, int *st
     CK(cudaSetDevice(b->device));
     float t = 0;
     gbpf_status st = b->solve_warm(m, start_kind, warm_iterations, &t);
+    if (ms) *ms = t;
+    return st;
+}
+
+extern "C" gbpf_status gbpf_batch_solve_warm_launch(gbpf_batch *b, gbpf_mlp *m) {
+    ARGCHECK(b && m);
+    CK(cudaSetDevice(b->device));
+    return b->warm_launch(m);
+}
+
+extern "C" gbpf_status gbpf_batch_solve_warm_wait(gbpf_batch *b, int *start_kind, int *warm_iterations, double *ms) {
+    ARGCHECK(b);
+    CK(cudaSetDevice(b->device));
+    float t = 0;
+    gbpf_status st = b->warm_wait(start_kind, warm_iterations, &t);
     if (ms) *ms = t;
     return st;
 }

@@ -989,19 +989,36 @@ MlpShape mlp_shape(const gbpf_mlp *m) {
     return s;
 }
 
-gbpf_status mlp_infer(gbpf_mlp *m, const bf16 *X, int n, float *out, cudaStream_t st) {
+struct MlpWork {
+    Work w;
+    int cap = 0;
+    const gbpf_mlp *net = nullptr;
+    int hidden = 0, n_hidden = 0;
+};
+MlpWork *mlp_work_create() { return new MlpWork(); }
+void mlp_work_free(MlpWork *w) { delete w; }
+
+gbpf_status mlp_infer(gbpf_mlp *m, const bf16 *X, int n, float *out, cudaStream_t st, MlpWork *mw) {
     if (n < 1) return GBPF_OK;
-    if (n > m->iw_cap) {
-        gbpf_status s = m->make_work(m->iw, n, false);
+    Work &w = mw ? mw->w : m->iw;
+    int &cap = mw ? mw->cap : m->iw_cap;
+    if (mw && (mw->net != m || mw->hidden != m->hidden || mw->n_hidden != m->n_hidden)) {
+        cap = 0;
+        mw->net = m;
+        mw->hidden = m->hidden;
+        mw->n_hidden = m->n_hidden;
+    }
+    if (n > cap) {
+        gbpf_status s = m->make_work(w, n, false);
         if (s != GBPF_OK) return s;
-        m->iw_cap = n;
+        cap = n;
     }
     CUtensorMap mX;
     gbpf_status s = make_map(&mX, X, m->kin, n, m->kin);
     if (s != GBPF_OK) return s;
-    // the hidden-layer maps were made for iw_cap rows: rows n.. are never
+    // the hidden-layer maps were made for cap rows: rows n.. are never
     // written in this call and only feed masked output rows
-    return m->forward(st, m->iw, mX, 0, n, nullptr, 0, out, false);
+    return m->forward(st, w, mX, 0, n, nullptr, 0, out, false);
 }
 }  // namespace gbpf
 

@@ -18,9 +18,18 @@ struct MlpShape {
 };
 MlpShape mlp_shape(const gbpf_mlp *m);
 
+// Inference workspace owned by a caller, so that callers that share a
+// network (two batches in flight) can run its forward pass at the same time
+// on their own streams.  Grows to the largest n seen; remade for another
+// network.
+struct MlpWork;
+MlpWork *mlp_work_create();
+void mlp_work_free(MlpWork *w);
+
 // Forward pass of normalised bf16 features X [n, kin] (device) into normalised
-// outputs out [n, outp] (device, fp32), on stream st.  Workspace is owned by
-// the network and grows to the largest n seen.
-gbpf_status mlp_infer(gbpf_mlp *m, const __nv_bfloat16 *X, int n, float *out, cudaStream_t st);
+// outputs out [n, outp] (device, fp32), on stream st, in workspace w (null:
+// the network's own).
+gbpf_status mlp_infer(gbpf_mlp *m, const __nv_bfloat16 *X, int n, float *out, cudaStream_t st,
+                      MlpWork *w = nullptr);
 
 }  // namespace gbpf

@@ -506,6 +506,16 @@ gbpf_status gbpf_mlp_set_norm(gbpf_mlp *m, const float *in_mean, const float *in
 gbpf_status gbpf_batch_solve_warm(gbpf_batch *b, gbpf_mlp *m, int *start_kind, int *warm_iterations,
                                   double *ms);
 
+/* gbpf_batch_solve_warm in two halves: _launch enqueues every step on the
+ * batch's stream and returns; _wait waits for it and fills start_kind,
+ * warm_iterations and *ms as gbpf_batch_solve_warm does.  Between the two the
+ * caller may work with other batches (each batch has its own stream and its
+ * own workspace for the network, so batches that share a network can have
+ * warm-started solves in flight at once); gbpf_batch_set_instances on this
+ * batch is refused until the wait. */
+gbpf_status gbpf_batch_solve_warm_launch(gbpf_batch *b, gbpf_mlp *m);
+gbpf_status gbpf_batch_solve_warm_wait(gbpf_batch *b, int *start_kind, int *warm_iterations, double *ms);
+
 /* Device time of the last gbpf_batch_solve_warm by phase: ms[0] the network
  * (features and inference), ms[1] the start choice and the queue order, ms[2]
  * the Newton launch (restarts included).  Zeros before the first call. */

@@ -261,3 +261,38 @@ def test_warm_start_own_start_runs_match_flat_start(gb, warm_net, prec):
     s1 = np.repeat(kept, nB)
     assert np.max(np.abs(warm["V"][s1] - flat["V"][s1])) <= 1e-6
     assert np.max(np.abs(warm["theta"][s1] - flat["theta"][s1])) <= 1e-6
+
+
+def test_warm_start_in_flight_on_two_batches(gb, warm_net):
+    """Two batches sharing one network, both warm-started solves launched
+    before either is waited for (each batch has its own stream and network
+    workspace): each gives what its synchronous solve_warm gives."""
+    grid, m, _ = warm_net
+    base = grid.buses()
+    opts = dict(tolerancia=1e-8, no_max_iter=30, lim_inj_reat=0)
+    rng = np.random.default_rng(77)
+    sets = [_scenarios(base, n, rng) for n in (300, 517)]
+    ref = []
+    for Pl, Ql, Pg in sets:
+        b = gb.Batch([grid], precision=gb.PREC_FP32_IR, **opts)
+        b.set_instances(np.zeros(len(Pl), np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
+        w = b.solve_warm(m)
+        ref.append((w, b.results()))
+        b.close()
+    bs = []
+    for Pl, Ql, Pg in sets:
+        b = gb.Batch([grid], precision=gb.PREC_FP32_IR, **opts)
+        b.set_instances(np.zeros(len(Pl), np.int32), Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
+        b.solve_warm_launch(m)
+        bs.append(b)
+    with pytest.raises(gb.GbpfError):
+        bs[0].set_instances(np.zeros(len(sets[0][0]), np.int32))  # refused while in flight
+    for b, (w0, r0) in zip(bs, ref):
+        w = b.solve_warm_wait()
+        r = b.results()
+        np.testing.assert_array_equal(w["start_kind"], w0["start_kind"])
+        np.testing.assert_array_equal(w["warm_iterations"], w0["warm_iterations"])
+        for k in ("iterations", "status", "V", "theta"):
+            np.testing.assert_array_equal(r[k], r0[k], err_msg=k)
+        with pytest.raises(gb.GbpfError):
+            b.solve_warm_wait()  # nothing in flight
