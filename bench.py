@@ -430,13 +430,20 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     # the dominant kernel's own time per launch: CUDA events recorded inside
     # the graph around each kernel, on the stream it runs on
     kt = fast.kernel_times(max(3, a.steps // 4))
-    main_kernel = "k_nr_warp<float>" if info["warp_instances"] else "k_nr_block<float>"
+    pl_k = fast.plan()
+    main_kernel = (f"k_nr_warp<float, {pl_k['warp_state_global']}>" if info["warp_instances"] else
+                   f"k_nr_block<float, {pl_k['block_state_global']}>")
     t_launch = (kt["warp"] if info["warp_instances"] else kt["block"]) / 1e3
     achieved = bytes_launch / t_launch / 1e9
-    # DRAM traffic of one k_nr_warp<float> launch of the 32,768 c2 scenarios
-    # (ncu dram__bytes_read.sum + dram__bytes_write.sum, one-pass capture of the
-    # full-size run with the default plan), scaled by instances
-    traffic = 201.7e6 * N_SCEN / 32768 if a.workload == "c2" else None
+    # DRAM traffic of one k_nr_warp<float, level> launch of the 32,768 c2
+    # scenarios (ncu dram__bytes_read.sum + dram__bytes_write.sum, one-pass
+    # captures of full-size runs), by state placement level and warps per
+    # block, scaled by instances; null for a plan shape not captured
+    measured = {(0, 8): 201.7e6, (3, 4): 264.4e6, (3, 6): 243.6e6, (3, 8): 233.2e6, (3, 9): 243.8e6,
+                (3, 10): 264.3e6, (3, 12): 218.5e6}
+    pl_now = fast.plan()
+    key = (pl_now["warp_state_global"], pl_now["warps_per_block_used"])
+    traffic = measured[key] * N_SCEN / 32768 if a.workload == "c2" and key in measured else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": max(3, a.warmup), "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True,
@@ -466,9 +473,10 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
                      "traffic": traffic / 1e9 if traffic else None, "traffic_unit": "GB per launch",
                      "algorithmic_bytes_per_launch": bytes_launch,
                      "kernel_ms_per_launch": kt,
-                     "note": "dependent-latency bound (ncu: issue 20 % of active cycles, FP64 pipe 31 %); state "
-                             "lives in shared memory, the step's remaining time is the hand-off launch of the few "
-                             "instances that run all 100 iterations"},
+                     "note": "dependent-latency bound (ncu: issue ~25 % of active cycles, FP64 pipe ~33 %, stalls "
+                             "on L2 loads of the placed state and on shared memory); the working set stays in L2 "
+                             "and DRAM traffic is the inputs and outputs once; the step's remaining time is the "
+                             "hand-off launch of the few instances that run all 100 iterations"},
         "clocks": clk.summary(),
         "gpu_launches": a.steps * launches_per_solve(fast.plan()),
     }
