@@ -46,7 +46,7 @@ EXPORTS = [
     "gbpf_grid_write_m", "gbpf_grid_ybus_form", "gbpf_grid_set_ybus_form",
     "gbpf_batch_get_plan", "gbpf_batch_set_plan", "gbpf_batch_autotune",
     "gbpf_batch_launch", "gbpf_batch_wait", "gbpf_batch_time_pipelined", "gbpf_batch_warm_phases",
-    "gbpf_batch_solve_warm_launch", "gbpf_batch_solve_warm_wait",
+    "gbpf_batch_solve_warm_launch", "gbpf_batch_solve_warm_wait", "gbpf_solver_set_lu_launch",
 ]
 
 
@@ -393,6 +393,11 @@ class Solver:
         n = ctypes.c_int()
         _check(lib().gbpf_solver_triggers(self.h, _p(t), cap, ctypes.byref(n)), "gbpf_solver_triggers")
         return t[:n.value].copy()
+
+    def set_lu_launch(self, mode):
+        """gbpf_solver_set_lu_launch: 0 auto, 1 one kernel per level, 2 all
+        levels in one single-block kernel."""
+        _check(lib().gbpf_solver_set_lu_launch(self.h, int(mode)), "gbpf_solver_set_lu_launch")
 
     def info(self):
         a = np.zeros(8, np.int64)

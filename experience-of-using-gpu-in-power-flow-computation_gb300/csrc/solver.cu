@@ -79,6 +79,8 @@ struct Dev {
     const long long *og_ptr;
     const int *og_a, *og_b;
     const int *flev_steps, *blev_steps;
+    const int *flev_ptr, *blev_ptr;  // level boundaries (k_lu_fused)
+    int nfl, nbl;
     const int *ysl, *rbus, *cbus;
     blk4 *fac, *dinv;
     double2 *rhs, *ys, *xs;
@@ -413,16 +415,12 @@ __device__ __forceinline__ typename SB<TJ>::b4 pivot_done(const Dev &d, int j, t
     return inv;
 }
 
-// One forward level, one warp per Crout step j (diagonal block, its inverse,
-// the L column and U row of j) fused with the forward substitution y_j.
+// Crout step j on one warp (diagonal block, its inverse, the L column and U
+// row of j) fused with the forward substitution y_j.
 template <typename TJ>
-__global__ void k_factor(Dev d, int beg, int cnt, int guard) {
+__device__ __forceinline__ void factor_step(const Dev &d, int j, int lane) {
     using B4 = typename SB<TJ>::b4;
     using B2 = typename SB<TJ>::b2;
-    if (stopped(d, guard)) return;
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= cnt) return;
-    const int j = d.flev_steps[beg + w];
     B4 *fac = fac_of<TJ>(d);
     B4 *Lv = fac + d.n, *Uv = fac + d.n + d.nup;
     const B2 *ys = ys_of<TJ>(d);
@@ -454,6 +452,15 @@ __global__ void k_factor(Dev d, int beg, int cnt, int guard) {
         Uv[p] = aU;
         Lv[p] = mmT(aL, inv);
     }
+}
+
+// One forward level, one warp per step.
+template <typename TJ>
+__global__ void k_factor(Dev d, int beg, int cnt, int guard) {
+    if (stopped(d, guard)) return;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= cnt) return;
+    factor_step<TJ>(d, d.flev_steps[beg + w], lane);
 }
 
 // The same step for levels whose pivots carry long gather lists (the top of
@@ -524,15 +531,11 @@ __global__ void __launch_bounds__(kFacBlk) k_factor_blk(Dev d, int beg, int guar
     }
 }
 
-// One backward level: x_j = D_j^-1 (y_j - sum_i U(j,i) x_i), one warp per row.
+// Backward row j on one warp: x_j = D_j^-1 (y_j - sum_i U(j,i) x_i).
 template <typename TJ>
-__global__ void k_bsolve(Dev d, int beg, int cnt, int guard) {
+__device__ __forceinline__ void bsolve_step(const Dev &d, int j, int lane) {
     using B4 = typename SB<TJ>::b4;
     using B2 = typename SB<TJ>::b2;
-    if (stopped(d, guard)) return;
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= cnt) return;
-    const int j = d.blev_steps[beg + w];
     const B4 *Uv = fac_of<TJ>(d) + d.n + d.nup;
     B2 *xs = xs_of<TJ>(d);
     B2 acc;
@@ -549,6 +552,48 @@ __global__ void k_bsolve(Dev d, int beg, int cnt, int guard) {
         t.x = y.x - acc.x;
         t.y = y.y - acc.y;
         xs[j] = mvT(dinv_of<TJ>(d)[j], t);
+    }
+}
+
+// One backward level, one warp per row.
+template <typename TJ>
+__global__ void k_bsolve(Dev d, int beg, int cnt, int guard) {
+    if (stopped(d, guard)) return;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= cnt) return;
+    bsolve_step<TJ>(d, d.blev_steps[beg + w], lane);
+}
+
+// Every forward level and then every backward level in one block of
+// kFusedThreads, a barrier between levels, one warp per step as in
+// k_factor / k_bsolve: for grids whose levels are so small that their own
+// launches would cost more than their work.  A singular pivot stops it at the
+// next level boundary, as the per-level launches stop (guard).
+constexpr int kFusedThreads = 512;
+// Largest Jacobian block order that takes k_lu_fused by default.  Measured on
+// single solves (ms per solve, per-level launches -> k_lu_fused): FP32 57
+// buses 0.99 -> 0.57, 118 0.79 -> 0.46, 236 5.7 -> 3.5, 472 18.5 -> 13.3, 944
+// 19.8 -> 23.3, 1,888 1.35 -> 1.73; FP64 57 1.99 -> 1.76, 118 1.53 -> 1.40,
+// 236 16.9 -> 19.6 (one SM's FP64 pipe is too small for more).
+constexpr int kFusedMaxN32 = 600, kFusedMaxN64 = 150;
+template <typename TJ>
+__global__ void __launch_bounds__(kFusedThreads, 1) k_lu_fused(Dev d, int guard) {
+    __shared__ int s_stop;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int W = kFusedThreads / 32;
+    for (int l = 0; l < d.nfl + d.nbl; l++) {
+        if (threadIdx.x == 0) s_stop = stopped(d, guard);
+        __syncthreads();
+        if (s_stop) return;
+        if (l < d.nfl) {
+            const int beg = d.flev_ptr[l], cnt = d.flev_ptr[l + 1] - beg;
+            for (int w = warp; w < cnt; w += W) factor_step<TJ>(d, d.flev_steps[beg + w], lane);
+        } else {
+            const int lb = l - d.nfl;
+            const int beg = d.blev_ptr[lb], cnt = d.blev_ptr[lb + 1] - beg;
+            for (int w = warp; w < cnt; w += W) bsolve_step<TJ>(d, d.blev_steps[beg + w], lane);
+        }
+        __syncthreads();
     }
 }
 
@@ -676,8 +721,15 @@ struct gbpf_solver {
     }
     // Levels whose steps carry more gather work than a warp should take on
     // alone (level_heavy) run one block per step.
+    // lu_fused: every level in one k_lu_fused launch (made by launch_forward;
+    // launch_backward then launches nothing)
+    int lu_fused = 0;
     template <typename TJ> void launch_forward_t(int guard) {
         const int T = 256, W = T / 32;
+        if (lu_fused) {
+            k_lu_fused<TJ><<<1, kFusedThreads, 0, stream>>>(d, guard);
+            return;
+        }
         for (int l = 0; l < nfl(); l++) {
             const int beg = S.flev_ptr[l], cnt = S.flev_ptr[l + 1] - beg;
             if (level_heavy[l]) k_factor_blk<TJ><<<cnt, kFacBlk, 0, stream>>>(d, beg, guard);
@@ -686,6 +738,7 @@ struct gbpf_solver {
     }
     template <typename TJ> void launch_backward_t(int guard) {
         const int T = 256, W = T / 32;
+        if (lu_fused) return;
         for (int l = 0; l < nbl(); l++) {
             const int beg = S.blev_ptr[l], cnt = S.blev_ptr[l + 1] - beg;
             k_bsolve<TJ><<<cdiv_int(cnt, W), T, 0, stream>>>(d, beg, cnt, guard);
@@ -828,6 +881,7 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
         d.dg_ptr = A.take<int>(n + 1); d.dg_pos = A.take<int>(nup + 1); d.dg_k = A.take<int>(nup + 1);
         d.og_ptr = A.take<long long>(nup + 1); d.og_a = A.take<int>(npairs + 1); d.og_b = A.take<int>(npairs + 1);
         d.flev_steps = A.take<int>(n); d.blev_steps = A.take<int>(n);
+        d.flev_ptr = A.take<int>(S.flev_ptr.size()); d.blev_ptr = A.take<int>(S.blev_ptr.size());
         d.ysl = A.take<int>(nq); d.rbus = A.take<int>(nq); d.cbus = A.take<int>(nq);
         d.fp32 = o.precision == GBPF_PREC_FP32_IR && !d.dense_rule;
         if (d.fp32) {
@@ -898,6 +952,10 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
     CK(up(d.og_b, S.og_b.data(), npairs * sizeof(int)));
     CK(up(d.flev_steps, S.flev_steps.data(), n * sizeof(int)));
     CK(up(d.blev_steps, S.blev_steps.data(), n * sizeof(int)));
+    CK(up(d.flev_ptr, S.flev_ptr.data(), S.flev_ptr.size() * sizeof(int)));
+    CK(up(d.blev_ptr, S.blev_ptr.data(), S.blev_ptr.size() * sizeof(int)));
+    d.nfl = nfl();
+    d.nbl = nbl();
     CK(up(d.ysl, S.ysl.data(), nq * sizeof(int)));
     CK(up(d.rbus, S.rbus.data(), nq * sizeof(int)));
     CK(up(d.cbus, S.cbus.data(), nq * sizeof(int)));
@@ -909,14 +967,16 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
     CK(cudaStreamSynchronize(stream));
     setup_ms[2] = ms_since(tp);
     // forward levels whose heaviest step (diagonal gather plus the pair lists
-    // of its row) exceeds 128 updates run one block per step
+    // of its row) exceeds heavy_work updates run one block per step (measured
+    // on 236- to 15,104-bus grids: thresholds from 0 to 128 within 2 %)
+    const long long heavy_work = 128;
     level_heavy.assign(nfl(), 0);
     for (int l = 0; l < nfl(); l++)
         for (int w = S.flev_ptr[l]; w < S.flev_ptr[l + 1] && !level_heavy[l]; w++) {
             const int j = S.flev_steps[w];
             long long work = S.dg_ptr[j + 1] - S.dg_ptr[j];
             for (int p = S.up_ptr[j]; p < S.up_ptr[j + 1]; p++) work += S.og_ptr[p + 1] - S.og_ptr[p];
-            if (work > 128) level_heavy[l] = 1;
+            if (work > heavy_work) level_heavy[l] = 1;
         }
     tp = clk::now();
     // Ybus on the device, once per topology
@@ -927,6 +987,7 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
     CK(cudaStreamSynchronize(stream));
     setup_ms[0] += ms_since(tp);
     tp = clk::now();
+    lu_fused = !d.dense_rule && n <= (d.fp32 ? kFusedMaxN32 : kFusedMaxN64);
     const gbpf_status st = build_graph();
     setup_ms[4] = ms_since(tp);
     return st;
@@ -977,7 +1038,7 @@ gbpf_status gbpf_solver::build_graph() {
     size_t nn = 0;
     CK(cudaGraphGetNodes(graph, nullptr, &nn));
     graph_nodes = (int)nn;
-    kernels_per_iter = nfl() + nbl() + 3 + 3 + (opt.lim_inj_reat && g.nPV ? 1 : 0) + 1;
+    kernels_per_iter = (lu_fused ? 1 : nfl() + nbl()) + 3 + 3 + (opt.lim_inj_reat && g.nPV ? 1 : 0) + 1;
     if (d.dense_rule) {
         const int panels = (d.N + kDPanel - 1) / kDPanel;
         kernels_per_iter = 2 + 4 * panels - 2 + 2 + 3 + (opt.lim_inj_reat && g.nPV ? 1 : 0) + 1;
@@ -1109,6 +1170,19 @@ extern "C" gbpf_status gbpf_solver_flows(gbpf_solver *s, double *Pdp, double *Pp
     if (Qdp) CK(cudaMemcpy(Qdp, s->d.Qdp, b, cudaMemcpyDeviceToHost));
     if (Qpd) CK(cudaMemcpy(Qpd, s->d.Qpd, b, cudaMemcpyDeviceToHost));
     return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_solver_set_lu_launch(gbpf_solver *s, int mode) {
+    ARGCHECK(s && mode >= 0 && mode <= 2);
+    if (s->d.dense_rule) { set_error("metodo = denso has no level-scheduled LU"); return GBPF_E_ARG; }
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    const int fused = mode == 2 || (mode == 0 && s->S.n <= (s->d.fp32 ? kFusedMaxN32 : kFusedMaxN64));
+    if (fused == s->lu_fused) return GBPF_OK;
+    s->lu_fused = fused;
+    if (s->exec) { cudaGraphExecDestroy(s->exec); s->exec = nullptr; }
+    if (s->graph) { cudaGraphDestroy(s->graph); s->graph = nullptr; }
+    return s->build_graph();
 }
 
 extern "C" gbpf_status gbpf_solver_info(const gbpf_solver *s, long long info[8]) {

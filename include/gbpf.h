@@ -236,6 +236,15 @@ gbpf_status gbpf_solver_triggers(gbpf_solver *s, int *trig, int cap, int *n);
  * GPU/PQcalc.cuh:523-557, computed on the device). */
 gbpf_status gbpf_solver_flows(gbpf_solver *s, double *Pdp, double *Ppd, double *Qdp, double *Qpd);
 
+/* How the LU and triangular solves are launched inside the solve graph:
+ * 1 = one kernel per elimination level (forward, with the LU step, then
+ * backward); 2 = every level in one single-block kernel with a barrier
+ * between levels (k_lu_fused: same per-step arithmetic, no per-level launch);
+ * 0 = 2 up to 600 block rows (buses - 1) in the FP32-LU form and 150 in FP64,
+ * else 1 (the default).  Rebuilds
+ * the graph.  Not for metodo = denso. */
+gbpf_status gbpf_solver_set_lu_launch(gbpf_solver *s, int mode);
+
 /* Solver facts: info[0..7] = nB, n blocks (nB-1), factor blocks (off-diagonal
  * per triangle), update pairs, forward levels, backward levels, graph nodes,
  * kernels launched per Newton iteration. */
