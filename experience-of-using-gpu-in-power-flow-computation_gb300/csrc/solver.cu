@@ -403,8 +403,17 @@ __device__ __forceinline__ typename SB<TJ>::b4 pivot_done(const Dev &d, int j, t
         d.ctl->status = GBPF_E_SINGULAR;
         d.ctl->done = 1;
     }
+    // FP64: one reciprocal, since a division is a chain of dependent FP64
+    // operations, the slowest thing on a small grid's critical path.  FP32
+    // keeps four divisions (cheap there; the FP32-LU form's rounding decides
+    // borderline limit switches, and the golden cases were checked with it).
     B4 inv;
-    inv.x = D.w / det; inv.y = -D.y / det; inv.z = -D.z / det; inv.w = D.x / det;
+    if constexpr (sizeof(TJ) == 8) {
+        const TJ rd = (TJ)1 / det;
+        inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
+    } else {
+        inv.x = D.w / det; inv.y = -D.y / det; inv.z = -D.z / det; inv.w = D.x / det;
+    }
     fac[j] = D;
     dinv_of<TJ>(d)[j] = inv;
     const double2 r = d.rhs[j];
