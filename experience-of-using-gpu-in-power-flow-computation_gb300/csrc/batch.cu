@@ -9,9 +9,13 @@
 // Jacobian fill (GPU/Jacobiano.cuh:252-344), a static-pivot block LU with
 // forward/backward substitution in place of cusolverSpDcsrlsvqr
 // (GPU/newtonRaphson.cuh:455-478), and the update (GPU/newtonRaphson.cuh:76-119).
-// The state lives in shared memory; the LU factor too when it fits, else in a
-// per-block slice of a global scratch buffer.  All synchronisation is
-// __syncthreads between phases and LU levels: no kernel launches inside a solve.
+// Small topologies run one instance per warp (k_nr_warp), larger ones one per
+// block (k_nr_block); the state lives in shared memory, or partly in an
+// L2-resident per-block (per-warp) region where that fits more instances per
+// SM (layout(), placement levels 0-3); the LU factor in shared memory when it
+// fits, else in a per-block slice of a global scratch buffer.  All
+// synchronisation is __syncthreads / __syncwarp between phases and LU levels:
+// no kernel launches inside a solve.
 //
 // TJ = precision of the Jacobian, the factor and the substitutions (double:
 // the oracle-matching form; float: FP32 LU with FP64 mismatch, test and update).

@@ -12,7 +12,9 @@
 // The whole loop is one CUDA graph: a prologue (reset, injections, limits,
 // mismatch, test) followed by a conditional WHILE node whose body is one Newton
 // iteration; the test kernel sets the loop condition on the device, so a solve
-// is one graph launch and one host synchronisation.
+// is one graph launch and one host synchronisation.  The LU and substitutions
+// run one kernel per elimination level, or for small grids every level in one
+// single-block kernel (k_lu_fused).
 //
 // Jacobian layout: 2x2 blocks per non-slack bus ([dP/dth dP/dV; dQ/dth dQ/dV]),
 // with a Q row and V column for every non-slack bus.  Buses that are PV (not at
