@@ -6,9 +6,9 @@ Workload c2 (default): the seeded synthetic 118-bus meshed grid (1 slack, 53 PV,
 lognormal(sigma 0.1), generator P x U(0.9, 1.1)), reactive limits on, flat start,
 tolerance 1e-8 p.u., no_max_iter 100.  A step solves all 32,768 scenarios.  About
 one scenario in 1,100 never converges (Newton oscillates or PV/PQ-cycles) and
-runs all 100 iterations on a few SMs at the end of the step; two batches of the
-same scenarios are kept in flight on two streams, steps alternating between
-them, so that one step's tail runs beside the next step's bulk.
+runs all 100 iterations on a few SMs at the end of the step; four batches of
+the same scenarios are kept in flight, one stream each, steps going round them,
+so that one step's tail runs beside the next steps' bulk.
   value    batched, FP32 LU + FP64 mismatch/test/update, inputs resident in
            device memory; one graph launch per step, CUDA events on the batch
            streams; counts converged scenarios only (config.serial_solves_per_s:
@@ -16,8 +16,8 @@ them, so that one step's tail runs beside the next step's bulk.
   e2e      the same through the public API with host arrays: host->device copy
            of every scenario's loads and generation, the solve, device->host
            copy of |V|, theta, P, Q, iterations and status, every step
-           (double-buffered: step k is launched before step k-1's results are
-           read back)
+           (four in flight: step k is launched before step k-3's results are
+           read back; c5: two)
   config   also reports the plain FP64 form (one scenario per gbpf_solve, the
            oracle-matching path) and batched FP64 on the same scenarios
 Other workloads: c2-plain (one FP64 solve of the grid per step), c3 (the
@@ -52,6 +52,7 @@ METRIC = "converged PF solves/s on 1 GB300 @ mismatch<=1e-8 pu"
 UNIT = "solves/s"
 N_SCEN = 4096           # c4 instances (and the default c2 CPU sample size)
 N_SCEN_C2 = 32768       # c2 scenarios per step
+IN_FLIGHT = 4           # c2/c4: batches of the same scenarios in flight, one stream each
 L2_BYTES = 129 * 1024 * 1024
 
 
@@ -348,20 +349,23 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     r = fast.results(state=False)
     conv = int((r["status"] == 0).sum())
     assert np.all(r["final_mismatch"][r["status"] == 0] <= 1e-8)
-    # a second batch of the same scenarios and plan: two batches in flight, so
-    # that one step's hand-off tail (the few scenarios that run all
-    # no_max_iter iterations on a few SMs) runs beside the next step's bulk
-    twin = gb.Batch(grids, device=dev, precision=gb.PREC_FP32_IR, **opts)
-    twin.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
+    # more batches of the same scenarios and plan, IN_FLIGHT in all, each on
+    # its own stream: one step's hand-off tail (the few scenarios that run all
+    # no_max_iter iterations on a few SMs) runs beside the next steps' bulk
     pl = fast.plan()
-    twin.set_plan(**{k: pl[k] for k in ("warp_mode", "warps_per_block", "handoff_it", "resume_group",
-                                        "warp_group", "narrow", "lu1", "warp_lu1", "flat_shared", "rotate",
-                                        "gstate", "warp_gstate")})
-    twin.solve()
-    assert np.array_equal(twin.results(state=False)["status"], r["status"])
-    pair = [fast, twin]
+    ring = [fast]
+    for _ in range(IN_FLIGHT - 1):
+        twin = gb.Batch(grids, device=dev, precision=gb.PREC_FP32_IR, **opts)
+        twin.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
+        twin.set_plan(**{k: pl[k] for k in ("warp_mode", "warps_per_block", "handoff_it", "resume_group",
+                                            "warp_group", "narrow", "lu1", "warp_lu1", "flat_shared", "rotate",
+                                            "gstate", "warp_gstate")})
+        twin.solve()
+        assert np.array_equal(twin.results(state=False)["status"], r["status"])
+        ring.append(twin)
+    pair = ring
     # device-resident: CUDA events on the batch streams; every step is a full
-    # solve of all scenarios, steps alternate between the two batches
+    # solve of all scenarios, steps go round the batches
     gb.time_pipelined(pair, max(3, a.warmup))
     fast.time(max(3, a.warmup))
     if dist:
@@ -376,21 +380,24 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     value = total_conv * a.steps / t_dev
     serial = total_conv * a.steps / max_over_ranks(ms_serial / 1e3, dist, dev)
     # end to end: host arrays through the API every step (inputs up, solve,
-    # results down into host arrays), double-buffered: step k's inputs go up
-    # and its solve is launched before step k-1's results are read back
+    # results down into host arrays), round the same batches: step i's inputs
+    # go up and its solve is launched before step i-(IN_FLIGHT-1)'s results are
+    # read back
     nb = len(Pl)
-    outs = [None, None]
+    kf = len(pair)
+    outs = [None] * kf
 
     def e2e_steps(k):
         for i in range(k):
-            b = pair[i % 2]
+            b = pair[i % kf]
             b.set_instances(gi, Pload=Pl, Qload=Ql, Pg=Pg)
             b.launch()
-            if i >= 1:
-                j = (i - 1) % 2
+            if i >= kf - 1:
+                j = (i - kf + 1) % kf
                 outs[j] = pair[j].results(state=True, out=outs[j])
-        j = (k - 1) % 2
-        outs[j] = pair[j].results(state=True, out=outs[j])
+        for i in range(max(0, k - kf + 1), k):
+            j = i % kf
+            outs[j] = pair[j].results(state=True, out=outs[j])
 
     e2e_steps(max(3, a.warmup))
     if dist:
@@ -399,7 +406,7 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     e2e_steps(a.steps)
     t_e2e = max_over_ranks(time.perf_counter() - t0, dist, dev)
     e2e = total_conv * a.steps / t_e2e
-    res = outs[(a.steps - 1) % 2]
+    res = outs[(a.steps - 1) % kf]
     assert np.array_equal(res["iterations"], r["iterations"])
     # the plain FP64 form (one scenario per gbpf_solve) and batched FP64, same scenarios
     plain = None
@@ -455,8 +462,8 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
                    "max_iterations": int(np.max(r["iterations"])),
                    "plain_fp64_solves_per_s": plain, "batched_fp64_solves_per_s": batched64,
                    "speedup_vs_plain_fp64": (value / plain) if plain else None,
-                   "in_flight": "2 batches of the same scenarios on two streams, steps alternating; each step a full "
-                                "solve of every scenario",
+                   "in_flight": f"{IN_FLIGHT} batches of the same scenarios, one stream each, steps going round "
+                                "them; each step a full solve of every scenario",
                    "serial_solves_per_s": serial,
                    "l2": (f"inputs+outputs {nb * 8 * 9 / 2**20:.0f} MiB > L2 (129 MB)" if nb * 72 > L2_BYTES else
                           f"inputs+outputs {nb * 8 * 9 / 2**20:.1f} MiB < L2; no flush"),
@@ -466,8 +473,8 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
                 "d2h_bytes_per_step": nb * 8 * 4 + N_SCEN * 20,
                 "note": "per step: the caller's Pload, Qload, Pg arrays up as they are (packed into Pliq, Qliq, "
                         "Qload on the device; the start is the grid's own, kept on the device), V, theta, Pcalc, "
-                        "Qcalc and the per-instance results down into the caller's arrays; double-buffered (step "
-                        "k is launched before step k-1's results are read)"},
+                        f"Qcalc and the per-instance results down into the caller's arrays; {IN_FLIGHT} batches in "
+                        f"flight (step k is launched before step k-{IN_FLIGHT - 1}'s results are read)"},
         "roofline": {"bound": "hbm", "kernel": main_kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src_note(src),
                      "traffic": traffic / 1e9 if traffic else None, "traffic_unit": "GB per launch",
