@@ -662,11 +662,18 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
                    "parallelism": f"scenarios sharded x{world}"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nb_tot * 8 * 3,
                 "d2h_bytes_per_step": nb_tot * 8 * 4 + C5_TEST * 20},
-        "roofline": {"bound": "hbm", "kernel": "k_nr_block<float, GS> (one persistent launch per step; "
-                                               "achieved over its phase of the step)",
+        "roofline": {"bound": "hbm", "kernel": f"k_nr_block<float, {fast.plan()['block_state_global']}> (one "
+                                               "persistent launch per step; achieved over its phase of the step)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src_note(src), "traffic": None,
-                     "note": "dependent-load latency bound (factor in L2-resident scratch)"},
+                     "peak_source": peak_src_note(src),
+                     # ncu dram__bytes_read.sum + dram__bytes_write.sum of the
+                     # level-3 launch on 2,048 flat-start scenarios (4.89 GB),
+                     # scaled by scenarios and by iterations a scenario
+                     "traffic": 4.889e9 * C5_TEST / 2048 * float(it_w.mean()) / 4.86 / 1e9,
+                     "traffic_unit": "GB per launch (scaled from a 2,048-scenario capture)",
+                     "note": "dependent-load latency bound: ~200 MB of per-block factors and state exceed the L2, "
+                             "so lines go to DRAM and back at ~5 % of its bandwidth; the misses' latency is the "
+                             "main stall"},
         "roofline_training": {"bound": "tensor", "kernel": "k_gemm (tcgen05 bf16, all training GEMMs)",
                               "achieved": train_tflops, "peak": tpeak, "unit": "TFLOP/s",
                               "frac": train_tflops / tpeak,
