@@ -503,7 +503,8 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
                    "parallelism": f"scenarios sharded x{world}"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nb * 8 * 3,
                 "d2h_bytes_per_step": nb * 8 * 4 + N_SCEN * 20,
-                "note": "per step: the caller's Pload, Qload, Pg arrays up as they are (packed into Pliq, Qliq, "
+                "note": "per step: the caller's Pload, Qload, Pg arrays (pinned host memory) up as they are "
+                        "(packed into Pliq, Qliq, "
                         "Qload on the device; the start is the grid's own, kept on the device), V, theta, Pcalc, "
                         f"Qcalc and the per-instance results down into the caller's arrays; {IN_FLIGHT} batches in "
                         f"flight (step k is launched before step k-{IN_FLIGHT - 1}'s results are read)"},
