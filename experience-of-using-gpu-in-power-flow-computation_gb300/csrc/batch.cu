@@ -2172,8 +2172,8 @@ gbpf_status gbpf_batch::build_graph() {
     // costs latency, which only more blocks per SM win back), else one with
     // as many and more factors in shared memory, else the lower.  Measured on
     // 8,192 instances of a 1,888-bus grid (solves/s): FP32 level 0 124 k
-    // (1 block per SM), 1 194 k (2), 2 199 k (2), 3 290 k (4; 279 k at 5 and
-    // 217 k at 6 blocks per SM, where spills grow), and 133 k with the factor
+    // (1 block per SM), 1 194 k (2), 2 199 k (2), 3 290 k (4; 259 k at 3,
+    // 279 k at 5 and 217 k at 6 blocks per SM, where spills grow), and 133 k with the factor
     // given the whole of shared memory at 1 block per SM; FP64 57 k, 58 k,
     // 71 k, 71 k (3 blocks per SM).
     BlockPlan bp;
