@@ -47,6 +47,7 @@ EXPORTS = [
     "gbpf_batch_get_plan", "gbpf_batch_set_plan", "gbpf_batch_autotune",
     "gbpf_batch_launch", "gbpf_batch_wait", "gbpf_batch_time_pipelined", "gbpf_batch_warm_phases",
     "gbpf_batch_solve_warm_launch", "gbpf_batch_solve_warm_wait", "gbpf_solver_set_lu_launch",
+    "gbpf_batch_time_warm_pipelined",
 ]
 
 
@@ -252,6 +253,16 @@ def time_pipelined(batches, steps):
     ms = ctypes.c_double()
     _check(lib().gbpf_batch_time_pipelined(arr, len(batches), int(steps), ctypes.byref(ms)),
            "gbpf_batch_time_pipelined")
+    return ms.value
+
+
+def time_warm_pipelined(batches, mlp, steps):
+    """gbpf_batch_time_warm_pipelined: device ms of `steps` warm-started
+    solves spread round-robin over the batches, each on its own stream."""
+    arr = (ctypes.c_void_p * len(batches))(*[b.h.value for b in batches])
+    ms = ctypes.c_double()
+    _check(lib().gbpf_batch_time_warm_pipelined(arr, len(batches), mlp.h, int(steps), ctypes.byref(ms)),
+           "gbpf_batch_time_warm_pipelined")
     return ms.value
 
 

@@ -1682,6 +1682,7 @@ struct gbpf_batch {
     // learned warm start: events after the network and after the start
     // choice, and the last call's phase times (network, choice, Newton)
     cudaEvent_t wev[2] = {nullptr, nullptr};
+    cudaEvent_t pev[2] = {nullptr, nullptr};  // gbpf_batch_time_warm_pipelined: start, end
     float warm_ms[3] = {0, 0, 0};
     std::vector<Grid> grids;
     std::vector<YPattern> ys;
@@ -1721,6 +1722,7 @@ struct gbpf_batch {
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         for (auto &e : wev) if (e) cudaEventDestroy(e);
+        for (auto &e : pev) if (e) cudaEventDestroy(e);
         if (mwork) gbpf::mlp_work_free(mwork);
         if (h_kind) cudaFreeHost(h_kind);
         if (h_witers) cudaFreeHost(h_witers);
@@ -2670,6 +2672,7 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
     CK(cudaEventCreate(&b->ev0));
     CK(cudaEventCreate(&b->ev1));
     for (auto &e : b->wev) CK(cudaEventCreate(&e));
+    for (auto &e : b->pev) CK(cudaEventCreate(&e));
     CK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
@@ -2920,6 +2923,44 @@ extern "C" gbpf_status gbpf_batch_solve_warm(gbpf_batch *b, gbpf_mlp *m, int *st
     float t = 0;
     gbpf_status st = b->solve_warm(m, start_kind, warm_iterations, &t);
     if (ms) *ms = t;
+    return st;
+}
+
+// `steps` warm-started solves spread round-robin over the batches, each on
+// its own stream: a batch whose previous solve is still in flight is waited
+// for (on the host) before it is launched again, while the others run.
+// Device time from a start event every stream waits for to the last stream's
+// end event.
+extern "C" gbpf_status gbpf_batch_time_warm_pipelined(gbpf_batch *const *bs, int n, gbpf_mlp *m, int steps,
+                                                      double *ms) {
+    ARGCHECK(bs && n > 0 && steps > 0 && ms && m);
+    for (int i = 0; i < n; i++)
+        ARGCHECK(bs[i] && bs[i]->exec && bs[i]->device == bs[0]->device && !bs[i]->warm_pending);
+    CK(cudaSetDevice(bs[0]->device));
+    for (int i = 0; i < n; i++) CK(cudaStreamSynchronize(bs[i]->stream));
+    cudaEvent_t start = bs[0]->pev[0];
+    CK(cudaEventRecord(start, bs[0]->stream));
+    for (int i = 1; i < n; i++) CK(cudaStreamWaitEvent(bs[i]->stream, start, 0));
+    gbpf_status st = GBPF_OK;
+    for (int k = 0; k < steps && st == GBPF_OK; k++) {
+        gbpf_batch *b = bs[k % n];
+        if (b->warm_pending) st = b->warm_wait(nullptr, nullptr, nullptr);
+        if (st == GBPF_OK) st = b->warm_launch(m);
+    }
+    float worst = 0;
+    for (int i = 0; i < n; i++) {
+        if (bs[i]->warm_pending) {
+            const gbpf_status w = bs[i]->warm_wait(nullptr, nullptr, nullptr);
+            if (st == GBPF_OK) st = w;
+        }
+        if (i >= steps) continue;
+        CK(cudaEventRecord(bs[i]->pev[1], bs[i]->stream));
+        CK(cudaEventSynchronize(bs[i]->pev[1]));
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, start, bs[i]->pev[1]));
+        worst = std::max(worst, t);
+    }
+    *ms = worst;
     return st;
 }
 

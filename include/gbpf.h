@@ -525,6 +525,12 @@ gbpf_status gbpf_batch_solve_warm(gbpf_batch *b, gbpf_mlp *m, int *start_kind, i
 gbpf_status gbpf_batch_solve_warm_launch(gbpf_batch *b, gbpf_mlp *m);
 gbpf_status gbpf_batch_solve_warm_wait(gbpf_batch *b, int *start_kind, int *warm_iterations, double *ms);
 
+/* Device ms of `steps` warm-started solves spread round-robin over n batches
+ * (all on one device, none with a warm-started solve in flight), each on its
+ * own stream; a batch is waited for before it is launched again.  From a
+ * start event every stream waits for to the latest stream's end. */
+gbpf_status gbpf_batch_time_warm_pipelined(gbpf_batch *const *bs, int n, gbpf_mlp *m, int steps, double *ms);
+
 /* Device time of the last gbpf_batch_solve_warm by phase: ms[0] the network
  * (features and inference), ms[1] the start choice and the queue order, ms[2]
  * the Newton launch (restarts included).  Zeros before the first call. */

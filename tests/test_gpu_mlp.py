@@ -266,7 +266,8 @@ def test_warm_start_own_start_runs_match_flat_start(gb, warm_net, prec):
 def test_warm_start_in_flight_on_two_batches(gb, warm_net):
     """Two batches sharing one network, both warm-started solves launched
     before either is waited for (each batch has its own stream and network
-    workspace): each gives what its synchronous solve_warm gives."""
+    workspace): each gives what its synchronous solve_warm gives, also after
+    the timed round-robin of gbpf_batch_time_warm_pipelined."""
     grid, m, _ = warm_net
     base = grid.buses()
     opts = dict(tolerancia=1e-8, no_max_iter=30, lim_inj_reat=0)
@@ -296,3 +297,8 @@ def test_warm_start_in_flight_on_two_batches(gb, warm_net):
             np.testing.assert_array_equal(r[k], r0[k], err_msg=k)
         with pytest.raises(gb.GbpfError):
             b.solve_warm_wait()  # nothing in flight
+    # timed round-robin over both batches: every step a full warm-started
+    # solve, the results of each batch's last step those of its own solve
+    assert gb.time_warm_pipelined(bs, m, 5) > 0
+    for b, (w0, r0) in zip(bs, ref):
+        np.testing.assert_array_equal(b.results()["V"], r0["V"])
