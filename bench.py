@@ -497,8 +497,9 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     achieved = bytes_launch / t_launch / 1e9
     # DRAM traffic of one k_nr_warp<float, level> launch of the 32,768 c2
     # scenarios (ncu dram__bytes_read.sum + dram__bytes_write.sum, one-pass
-    # captures of full-size runs), by state placement level and warps per
-    # block, scaled by instances; null for a plan shape not captured
+    # captures of full-size runs with the hand-off at iteration 12), by state
+    # placement level and warps per block, scaled by instances; null for a
+    # plan shape not captured
     measured = {(0, 8): 201.7e6, (3, 4): 264.4e6, (3, 6): 243.6e6, (3, 8): 233.2e6, (3, 9): 243.8e6,
                 (3, 10): 264.3e6, (3, 12): 218.5e6}
     pl_now = fast.plan()
