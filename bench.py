@@ -176,11 +176,19 @@ def _oracle_shard(task):
 
 
 def cpu_baseline_scenarios(cdf, lim, seed, total, target_s=12.0):
-    """The oracle on one host core over a bounded sample of the scenarios."""
+    """The oracle on one host core over a bounded sample of the scenarios
+    (about target_s seconds: the per-scenario time comes from runs of 64 and
+    256 scenarios, so that a call's fixed cost -- loading the grid -- does not
+    count as solving)."""
+    _oracle_shard((cdf, 0, 8, seed, lim, 1, total))
     t0 = time.perf_counter()
     _oracle_shard((cdf, 0, 64, seed, lim, 1, total))
-    dt = time.perf_counter() - t0
-    n = max(64, min(total, int(64 * target_s / max(dt, 1e-6))))
+    t64 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    _oracle_shard((cdf, 0, 256, seed, lim, 1, total))
+    t256 = time.perf_counter() - t0
+    per = max((t256 - t64) / 192, t256 / 256 / 4, 1e-7)
+    n = max(64, min(total, int(target_s / per)))
     t0 = time.perf_counter()
     conv = _oracle_shard((cdf, 0, n, seed, lim, 1, total))
     dt = time.perf_counter() - t0
