@@ -20,6 +20,7 @@ CLI_PATH = os.path.join(HERE, "lib", "gbpf")
 OK, E_INPUT, E_SINGULAR, E_NOCONV, E_CUDA, E_TIMEOUT, E_OOM, E_ARG, E_UNSUPPORTED = range(9)
 METODO = {"esparso": 0, "denso": 1, "hibridoA": 2, "hibridoB": 3, "hibridoC": 4, "nda": 5}
 PREC_FP64, PREC_FP32_IR = 0, 1
+FORM_GRAPH, FORM_PERSISTENT = 1, 2
 YBUS_CDF, YBUS_MATPOWER = 0, 1
 EVENT_TEXT = {
     1: "PV -> PQ (limite superior)",
@@ -47,7 +48,8 @@ EXPORTS = [
     "gbpf_batch_get_plan", "gbpf_batch_set_plan", "gbpf_batch_autotune",
     "gbpf_batch_launch", "gbpf_batch_wait", "gbpf_batch_time_pipelined", "gbpf_batch_warm_phases",
     "gbpf_batch_solve_warm_launch", "gbpf_batch_solve_warm_wait", "gbpf_solver_set_lu_launch",
-    "gbpf_batch_time_warm_pipelined",
+    "gbpf_batch_time_warm_pipelined", "gbpf_batch_events_all", "gbpf_mlp_set_wait_limit",
+    "gbpf_solver_set_form", "gbpf_solver_get_form",
 ]
 
 
@@ -410,6 +412,18 @@ class Solver:
         levels in one single-block kernel."""
         _check(lib().gbpf_solver_set_lu_launch(self.h, int(mode)), "gbpf_solver_set_lu_launch")
 
+    def set_form(self, form):
+        """gbpf_solver_set_form: FORM_GRAPH (per-phase kernels in a CUDA graph)
+        or FORM_PERSISTENT (the whole Newton loop in one block-kernel launch)."""
+        _check(lib().gbpf_solver_set_form(self.h, int(form)), "gbpf_solver_set_form")
+
+    def form(self):
+        """gbpf_solver_get_form: the form gbpf_solve runs and its kernel
+        launches per solve (plus, for the graph form, per iteration)."""
+        a = np.zeros(3, np.int32)
+        _check(lib().gbpf_solver_get_form(self.h, _p(a)), "gbpf_solver_get_form")
+        return dict(form=int(a[0]), launches=int(a[1]), launches_per_iteration=int(a[2]))
+
     def info(self):
         a = np.zeros(8, np.int64)
         _check(lib().gbpf_solver_info(self.h, _p(a)), "gbpf_solver_info")
@@ -565,6 +579,15 @@ class Batch:
         if st not in (OK, E_ARG):
             raise GbpfError(st, "gbpf_batch_events")
         return [tuple(int(x) for x in ev[4 * i:4 * i + 4]) for i in range(n.value)]
+
+    def events_all(self, cap=16):
+        """Switch events of every instance (gbpf_batch_events_all): an array
+        [n_inst, cap, 4] (iteration, bus, PV position, code; zero-padded) and
+        the per-instance event counts."""
+        ev = np.zeros(self.n_inst * cap * 4, np.int32)
+        n = np.zeros(self.n_inst, np.int32)
+        _check(lib().gbpf_batch_events_all(self.h, _p(ev), int(cap), _p(n)), "gbpf_batch_events_all")
+        return ev.reshape(self.n_inst, cap, 4), n
 
     PLAN_KEYS = ("warp_mode", "warps_per_block", "handoff_it", "resume_group", "warp_group", "narrow", "lu1",
                  "warp_lu1", "flat_shared", "rotate", "gstate", "warp_gstate", "warps_per_block_used",
@@ -729,6 +752,11 @@ class MLP:
         k = 0 if A is None else Ac.shape[1]
         _check(lib().gbpf_mlp_set_loss_metric(self.h, _p(Ac), int(k), ctypes.c_float(lam)),
                "gbpf_mlp_set_loss_metric")
+
+    def set_wait_limit(self, cycles=0):
+        """gbpf_mlp_set_wait_limit: the GEMMs' operand-ring wait limit in SM
+        clock cycles (0: the default, about 2 s)."""
+        _check(lib().gbpf_mlp_set_wait_limit(self.h, ctypes.c_longlong(int(cycles))), "gbpf_mlp_set_wait_limit")
 
     def predict(self, X):
         X = np.ascontiguousarray(np.atleast_2d(X), np.float32)

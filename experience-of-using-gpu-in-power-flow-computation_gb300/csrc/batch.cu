@@ -222,6 +222,15 @@ struct Args {
     // block b starts at gstate + b * gstate_stride
     unsigned char *gstate;
     long long gstate_stride;
+    // one-instance launches for the single-grid solver (gbpf::one_record;
+    // null in batch launches): max|g| of every iteration and 1 where the
+    // reactive-limit check ran (hist_cap entries), the final PV limit flags,
+    // and the solve's control record
+    double *hist;
+    int *trig;
+    int hist_cap;
+    int *limq_out;
+    gbpf::SolveCtl *ctl_out;
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
@@ -802,6 +811,8 @@ __global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) 
                     act[k] = (G.type[k] == 0 || G.type[k] == 1);
                 }
                 for (int i = tid; i < T.nPV; i += kThreads) limQ[i] = 0;
+                if (a.trig)
+                    for (int k = tid; k < a.hist_cap; k += kThreads) a.trig[k] = 0;
                 if (tid == 0) { s_done = 0; s_status = 0; s_it = 0; s_nev = 0; s_maxDx = INFINITY; }
             } else {
                 // the state a warp parked at the hand-off
@@ -852,6 +863,7 @@ __global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) 
                 const int it = s_it;
                 // reactive limits (chkLimQ) when the previous step was small
                 if (a.lim && it >= 1 && it < mi && abits(s_maxDx) < tol10_bits) {
+                    if (a.trig && tid == 0 && it < a.hist_cap) a.trig[it] = 1;
                     for (int i0 = 0; i0 < T.nPV; i0 += kThreads) {
                         const int i = i0 + tid;
                         int code = 0, b = 0;
@@ -908,6 +920,7 @@ __global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) 
                 m = block_umax(m, red);
                 if (tid == 0) {
                     s_maxG = __longlong_as_double((long long)m);
+                    if (a.hist && it < a.hist_cap) a.hist[it] = s_maxG;
                     if (m > kInfBits) { s_status = GBPF_E_NOCONV; s_done = 1; }
                     else if (m <= tol_bits) s_done = 1;
                     else if (it >= mi) { s_status = GBPF_E_NOCONV; s_done = 1; }
@@ -1042,6 +1055,19 @@ __global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) 
             a.status[inst] = s_status;
             a.mism[inst] = s_maxG;
             a.n_events[inst] = s_nev;
+        }
+        if (a.limq_out)
+            for (int i = tid; i < T.nPV; i += kThreads) a.limq_out[i] = limQ[i];
+        if (a.ctl_out && tid == 0) {
+            gbpf::SolveCtl c{};
+            c.it = s_it;
+            c.done = 1;
+            c.status = s_status;
+            c.n_events = s_nev;
+            c.maxG = (unsigned long long)__double_as_longlong(s_maxG);
+            c.maxDx = (unsigned long long)__double_as_longlong(s_maxDx);
+            c.converged = s_status == 0;
+            *a.ctl_out = c;
         }
         __syncthreads();
     }
@@ -1712,7 +1738,9 @@ struct gbpf_batch {
     DevBuf dflt_off_d;
     int flat_flag = 0;                // host copy of the device flag behind Args::flat_on
     DevBuf flat_mem;                  // k_flat_start outputs, one FlatLayout per topology
-    size_t na_smem = 0, na_stride = 0;
+    // gbpf_batch_solve_noalloc, per topology: shared memory of one instance
+    // (whole state in shared memory) and the bytes of its factor slice
+    std::vector<size_t> na_smem, na_stride;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
 
@@ -2324,6 +2352,14 @@ gbpf_status gbpf_batch::build_graph() {
             CK(cudaMemcpyAsync(o + F.V0, grids[t].V0.data(), 8 * (size_t)T.nB, cudaMemcpyHostToDevice, stream));
             CK(cudaMemcpyAsync(o + F.th0, grids[t].theta0.data(), 8 * (size_t)T.nB, cudaMemcpyHostToDevice, stream));
             const size_t fs = align_up((fp32 ? 8 : 16) * (size_t)T.n, 16) + (size_t)T.nB;
+            // the warp keeps y and the bus flags in shared memory: beyond the
+            // opt-in limit (FP64 past ~13,900 buses) the topology has no shared
+            // iteration 0 and its instances compute their own
+            if (fs > (size_t)maxsm) continue;
+            if (fs > 48 * 1024) {
+                if (fp32) CK(cudaFuncSetAttribute(k_flat_start<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs));
+                else CK(cudaFuncSetAttribute(k_flat_start<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs));
+            }
             if (fp32) k_flat_start<float><<<1, 32, fs, stream>>>(T, o, plan.warp_group);
             else k_flat_start<double><<<1, 32, fs, stream>>>(T, o, plan.warp_group);
             CK_LAUNCH();
@@ -2704,9 +2740,9 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
             t.blob_smem = 0;
             t.fac_smem = 0;
             const Layout l = fp32 ? layout<float>(t.nB, t.n, t.nup, t.nPV, 0, 0) : layout<double>(t.nB, t.n, t.nup, t.nPV, 0, 0);
-            b->na_smem = std::max(b->na_smem, l.total);
-            b->na_stride = std::max(b->na_stride, align_up(fp32 ? scratch_bytes<float>(t.n, t.nup)
-                                                                : scratch_bytes<double>(t.n, t.nup), 256));
+            b->na_smem.push_back(l.total);
+            b->na_stride.push_back(align_up(fp32 ? scratch_bytes<float>(t.n, t.nup) : scratch_bytes<double>(t.n, t.nup),
+                                            256));
         }
         CK(cudaMalloc(&b->topo_na.p, sizeof(Topo) * na.size()));
         CK(cudaMemcpy(b->topo_na.p, na.data(), sizeof(Topo) * na.size(), cudaMemcpyHostToDevice));
@@ -2718,15 +2754,15 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
     return GBPF_OK;
 }
 
-// For callers that cannot allocate device memory at solve time (allocation is
-// forbidden in their stream-capture region, or their memory is owned by
-// another allocator): the batch Newton solve on caller-owned device buffers,
-// with every scratch byte in g_noalloc_scratch.  The batch handle is made
-// beforehand with gbpf_batch_create (which does allocate, once).  Calls share
-// the scratch, so calls that overlap on the GPU race; the work counter is
-// cleared at the start of each call, everything else is fully rewritten.
-// Switch events are not recorded.  Asynchronous on `stream` (NULL = the
-// batch's own stream).
+// For callers that cannot allocate device memory while they solve (see
+// gbpf.h): the batch Newton solve on caller-owned device buffers, with every
+// scratch byte in g_noalloc_scratch.  The batch handle is made beforehand with
+// gbpf_batch_create (which does allocate, once).  Calls share the scratch, so
+// calls that overlap on the GPU race; the work counter is cleared at the start
+// of each call and everything else is fully rewritten.  Switch events are not
+// recorded.  grid_of_inst is read before the call returns (the per-call
+// metadata is staged from it by one copy); the solve itself is asynchronous
+// on `stream` (NULL = the batch's own stream).
 extern "C" gbpf_status gbpf_batch_solve_noalloc(gbpf_batch *b, int n_inst, const int *grid_of_inst,
                                                 const double *V0, const double *theta0, const double *Pliq,
                                                 const double *Qliq, const double *Qload, double *V,
@@ -2744,17 +2780,35 @@ extern "C" gbpf_status gbpf_batch_solve_noalloc(gbpf_batch *b, int n_inst, const
                  o_off = o_topo + align_up(4 * (size_t)n_inst, 256),
                  o_nev = o_off + align_up(8 * (size_t)n_inst, 256),
                  o_slices = o_nev + align_up(4 * (size_t)n_inst, 256);
-    if (o_slices + b->na_stride > kNoAllocBytes) {
+    // shared memory and factor slice sized by the grids this call names
+    size_t smem = 0, stride = 0;
+    for (int i = 0; i < n_inst; i++) {
+        const int t = grid_of_inst[i];
+        if (t < 0 || t >= nt) { set_error("instance names an unknown grid"); return GBPF_E_ARG; }
+        smem = std::max(smem, b->na_smem[t]);
+        stride = std::max(stride, b->na_stride[t]);
+    }
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device));
+    if (smem > (size_t)optin) {
+        set_error("gbpf_batch_solve_noalloc: an instance's state needs " + std::to_string(smem >> 10) +
+                  " KiB of shared memory; a block holds at most " + std::to_string(optin >> 10) +
+                  " KiB (use gbpf_batch_solve for this grid)");
+        return GBPF_E_ARG;
+    }
+    if (o_slices + stride > kNoAllocBytes) {
         set_error("gbpf_batch_solve_noalloc: " + std::to_string(n_inst) + " instances need " +
-                  std::to_string((o_slices + b->na_stride) >> 10) + " KiB of scratch; the static scratch holds " +
+                  std::to_string((o_slices + stride) >> 10) + " KiB of scratch; the static scratch holds " +
                   std::to_string(kNoAllocBytes >> 10) + " KiB");
         return GBPF_E_ARG;
     }
-    std::vector<int> queue(n_inst), topo(n_inst);
-    std::vector<long long> off(n_inst);
+    // queue | topology ids | bus offsets, laid out as in the scratch, in one
+    // host buffer and one copy (a pageable copy: staged before it returns)
+    std::vector<unsigned char> meta(o_nev - o_queue);
+    int *queue = (int *)meta.data(), *topo = (int *)(meta.data() + (o_topo - o_queue));
+    long long *off = (long long *)(meta.data() + (o_off - o_queue));
     long long o = 0;
     for (int i = 0; i < n_inst; i++) {
-        if (grid_of_inst[i] < 0 || grid_of_inst[i] >= nt) { set_error("instance names an unknown grid"); return GBPF_E_ARG; }
         queue[i] = i;
         topo[i] = grid_of_inst[i];
         off[i] = o;
@@ -2763,9 +2817,7 @@ extern "C" gbpf_status gbpf_batch_solve_noalloc(gbpf_batch *b, int n_inst, const
     cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
     char *sc = (char *)base;
     CK(cudaMemsetAsync(sc, 0, sizeof(int), s));
-    CK(cudaMemcpyAsync(sc + o_queue, queue.data(), 4 * (size_t)n_inst, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(sc + o_topo, topo.data(), 4 * (size_t)n_inst, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(sc + o_off, off.data(), 8 * (size_t)n_inst, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sc + o_queue, meta.data(), meta.size(), cudaMemcpyHostToDevice, s));
     Args a{};
     a.topo = (const Topo *)b->topo_na.p;
     a.n_inst = n_inst;
@@ -2782,7 +2834,7 @@ extern "C" gbpf_status gbpf_batch_solve_noalloc(gbpf_batch *b, int n_inst, const
     a.queue = (const int *)(sc + o_queue);
     a.queue_len = n_inst;
     a.scratch = sc + o_slices;
-    a.scratch_stride = (long long)b->na_stride;
+    a.scratch_stride = (long long)stride;
     a.blob_region = 0;
     const bool fp32 = b->precision == GBPF_PREC_FP32_IR;
     int dev_sm = 0, occ = 0;
@@ -2790,16 +2842,16 @@ extern "C" gbpf_status gbpf_batch_solve_noalloc(gbpf_batch *b, int n_inst, const
     cudaFuncAttributes fa{};
     if (fp32) CK(cudaFuncGetAttributes(&fa, k_nr_block<float, 0>));
     else CK(cudaFuncGetAttributes(&fa, k_nr_block<double, 0>));
-    if ((size_t)fa.maxDynamicSharedSizeBytes < b->na_smem) {
+    if ((size_t)fa.maxDynamicSharedSizeBytes < smem) {
         const void *fn = fp32 ? (const void *)k_nr_block<float, 0> : (const void *)k_nr_block<double, 0>;
-        CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->na_smem));
+        CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
-    if (fp32) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float, 0>, kThreads, b->na_smem));
-    else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double, 0>, kThreads, b->na_smem));
-    const long long slices = (long long)((kNoAllocBytes - o_slices) / b->na_stride);
+    if (fp32) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<float, 0>, kThreads, smem));
+    else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nr_block<double, 0>, kThreads, smem));
+    const long long slices = (long long)((kNoAllocBytes - o_slices) / stride);
     const int grid = (int)std::max(1LL, std::min<long long>({(long long)n_inst, (long long)dev_sm * std::max(occ, 1), slices}));
-    if (fp32) k_nr_block<float, 0><<<grid, kThreads, b->na_smem, s>>>(a);
-    else k_nr_block<double, 0><<<grid, kThreads, b->na_smem, s>>>(a);
+    if (fp32) k_nr_block<float, 0><<<grid, kThreads, smem, s>>>(a);
+    else k_nr_block<double, 0><<<grid, kThreads, smem, s>>>(a);
     CK_LAUNCH();
     return GBPF_OK;
 }
@@ -2916,6 +2968,28 @@ extern "C" gbpf_status gbpf_batch_events(gbpf_batch *b, int inst, int *ev, int c
     return have > b->ev_cap ? GBPF_E_ARG : GBPF_OK;
 }
 
+extern "C" gbpf_status gbpf_batch_events_all(gbpf_batch *b, int *ev, int cap, int *n) {
+    ARGCHECK(b && b->n_inst > 0 && ev && n && cap > 0 && cap <= 16);
+    CK(cudaSetDevice(b->device));
+    const size_t ni = (size_t)b->n_inst, ec = (size_t)b->ev_cap;
+    std::vector<int> e(ni * ec * 4);
+    CK(cudaMemcpyAsync(n, b->args.n_events, 4 * ni, cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaMemcpyAsync(e.data(), b->args.events, e.size() * 4, cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    std::fill(ev, ev + ni * (size_t)cap * 4, 0);
+    int idx[16];
+    for (size_t i = 0; i < ni; i++) {
+        const int *src = e.data() + i * ec * 4;
+        const int m = std::min(std::min(n[i], (int)ec), cap);
+        for (int k = 0; k < m; k++) idx[k] = k;
+        std::sort(idx, idx + m, [&](int x, int y) {
+            return src[4 * x] != src[4 * y] ? src[4 * x] < src[4 * y] : src[4 * x + 2] < src[4 * y + 2];
+        });
+        for (int k = 0; k < m; k++) std::copy(src + 4 * idx[k], src + 4 * idx[k] + 4, ev + (i * cap + k) * 4);
+    }
+    return GBPF_OK;
+}
+
 extern "C" gbpf_status gbpf_batch_solve_warm(gbpf_batch *b, gbpf_mlp *m, int *start_kind, int *warm_iterations,
                                              double *ms) {
     ARGCHECK(b && m);
@@ -3000,3 +3074,66 @@ extern "C" gbpf_status gbpf_batch_info(const gbpf_batch *b, long long info[8]) {
     (void)bs;
     return GBPF_OK;
 }
+
+// ------------------------------------------------- one-instance solve (solver)
+// The single-grid solver's persistent form: a batch of one topology and one
+// instance whose block-mode launch reads the solver's start and injections and
+// writes the solver's state, events, history and control record in place, so
+// that a whole Newton solve is one kernel launch.
+struct gbpf::OneSolve {
+    gbpf_batch *b = nullptr;
+    ~OneSolve() {
+        if (b) gbpf_batch_free(b);
+    }
+};
+
+gbpf_status gbpf::one_create(const Grid &g, const gbpf_options &o, int device, OneSolve **out) {
+    *out = nullptr;
+    auto s = std::make_unique<OneSolve>();
+    gbpf_grid gg{g};
+    const gbpf_grid *gp = &gg;
+    gbpf_status st = gbpf_batch_create(&gp, 1, &o, device, &s->b);
+    if (st != GBPF_OK) return st;
+    gbpf_batch *b = s->b;
+    // one block, every per-bus array in shared memory, one-pass levels, no
+    // hand-off, iteration 0 from the shared copy when the start is the grid's
+    b->plan.warp_mode = 0;
+    b->plan.handoff_it = 0;
+    b->plan.gstate = 0;
+    b->plan.lu1 = 1;
+    b->plan.narrow = 0;
+    b->plan.flat_shared = 1;
+    const int gi = 0;
+    st = b->set_instances(1, &gi, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    if (st != GBPF_OK) return st;
+    if (b->n_block_q != 1 || b->n_warp_q != 0 || b->block_gs != 0 || b->grid_blocks != 1) {
+        set_error("one-instance solve: the grid's state does not fit one block's shared memory");
+        return GBPF_E_UNSUPPORTED;
+    }
+    *out = s.release();
+    return GBPF_OK;
+}
+
+gbpf_status gbpf::one_record(OneSolve *s, void *stream, const OneIO &io) {
+    gbpf_batch *b = s->b;
+    cudaStream_t st = (cudaStream_t)stream;
+    Args a = b->args;
+    a.V0 = io.V0; a.th0 = io.th0; a.Pliq = io.Pliq; a.Qliq = io.Qliq; a.Qload = io.Qload;
+    a.V = io.V; a.th = io.th; a.P = io.P; a.Q = io.Q;
+    a.events = io.events;
+    a.ev_cap = io.ev_cap;
+    a.hist = io.hist;
+    a.trig = io.trig;
+    a.hist_cap = io.hist_cap;
+    a.limq_out = io.limQ;
+    a.ctl_out = io.ctl;
+    a.flat_on = io.flat_on;
+    a.kind = nullptr;
+    CK(cudaMemsetAsync(a.counter, 0, 4 * sizeof(int), st));
+    if (b->precision == GBPF_PREC_FP32_IR) k_nr_block<float, 0><<<1, kThreads, b->smem, st>>>(a);
+    else k_nr_block<double, 0><<<1, kThreads, b->smem, st>>>(a);
+    CK_LAUNCH();
+    return GBPF_OK;
+}
+
+void gbpf::one_free(OneSolve *s) { delete s; }

@@ -78,6 +78,45 @@ Symbolic analyse(const Grid &g, const YPattern &y, std::string *why);
 // Ordering used by analyse(): minimum degree on the bus graph.
 std::vector<int> min_degree_order(int n, const std::vector<std::vector<int>> &adj);
 
+// Control record of one single-grid solve in device memory, written by the
+// solver's graph kernels or by the one-instance batch launch below.
+struct SolveCtl {
+    int it;                    // Newton updates done
+    int done;                  // loop finished (converged, iteration cap, failure)
+    int status;                // gbpf_status
+    int n_events;              // switch events recorded (may exceed the log capacity)
+    unsigned long long maxG;   // bits of max|g| (non-negative doubles order as integers)
+    unsigned long long maxDx;  // bits of max|dx| of the last step
+    int converged;
+    int pad;
+};
+
+// The single-grid solver's device arrays that a one-instance launch of the
+// batch's block kernel reads (start, injections, loads) and writes (state,
+// switch events, max|g| per iteration, limit-check flags, final PV limit
+// flags, control record).  flat_on: device flag, nonzero when V0/th0 are the
+// grid's own start (iteration 0 then comes from the topology's shared copy).
+struct OneIO {
+    const double *V0, *th0, *Pliq, *Qliq, *Qload;
+    double *V, *th, *P, *Q;
+    int *events;
+    int ev_cap;
+    double *hist;
+    int *trig;
+    int hist_cap;
+    int *limQ;
+    SolveCtl *ctl;
+    const int *flat_on;
+};
+// The whole Newton solve of one grid as one persistent launch of the batch's
+// block kernel (one instance, state in shared memory).  one_create fails with
+// GBPF_E_UNSUPPORTED when the grid's state does not fit one block's shared
+// memory; one_record enqueues the launch on `stream` (a cudaStream_t).
+struct OneSolve;
+gbpf_status one_create(const Grid &g, const gbpf_options &o, int device, OneSolve **out);
+gbpf_status one_record(OneSolve *s, void *stream, const OneIO &io);
+void one_free(OneSolve *s);
+
 }  // namespace gbpf
 
 struct gbpf_grid {

@@ -21,9 +21,12 @@
 // the Adam epilogue refreshes both the bf16 weights and their transpose, so
 // no transpose kernel runs inside a step.
 //
-// Every wait on an mbarrier is bounded (kWaitCycles); a wait that runs out
-// sets the network's error word, the CTA stops issuing work, waits (bounded)
-// for its copies in flight, frees its tensor memory and returns.
+// Every wait on an mbarrier is bounded.  The operand ring's waits take the
+// launch's limit (EpiArgs::wait, set per network by gbpf_mlp_set_wait_limit;
+// 0 = kWaitCycles); a wait that runs out sets the network's error word, the
+// CTA stops issuing work, waits for its tensor-core operations (the
+// accumulator barrier) and its copies in flight with the fixed kWaitCycles
+// bound, frees its tensor memory and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -99,6 +102,7 @@ struct EpiArgs {
     const float *sched;   // learning-rate schedule {first step, steps, final lr}
     float lr, b1, b2, eps;
     int *err;
+    long long wait;       // limit of the operand-ring waits in clock cycles (0: kWaitCycles)
 };
 
 // Learning rate of Adam step t (1-based): cosine decay from lr to sched[2]
@@ -131,12 +135,31 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *b, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait for the phase with the given parity to complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity) {
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for the phase with the given parity to complete, at most
+// `limit` clock cycles.  Limits below kPollBelow poll with the non-blocking
+// test_wait, so that a short limit runs out when it says (try_wait may
+// suspend the thread for a while before it reports an incomplete phase).
+constexpr long long kPollBelow = 100000;
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, long long limit = kWaitCycles) {
+    if (limit < kPollBelow) {
+        const long long t0 = clock64();
+        while (!mbar_test_wait(b, parity))
+            if (clock64() - t0 > limit) return false;
+        return true;
+    }
     if (mbar_try_wait(b, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(b, parity))
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > limit) return false;
     return true;
 }
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
@@ -309,6 +332,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     // k-tiles 0..nk1-1 from (ta, tb), then nk2 from (ta2, tb2) into the same
     // accumulator: C = A B^T + A2 B2^T (K2 = 0: one pair)
     const int nk1 = (K + BK - 1) / BK, nk = nk1 + (K2 + BK - 1) / BK;
+    const long long wl = e.wait > 0 ? e.wait : kWaitCycles;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
@@ -333,7 +357,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         int kt = 0;
         for (; kt < nk; kt++) {
             const int s = kt % STAGES;
-            if (kt >= STAGES && !mbar_wait(&empty[s], ((kt / STAGES) - 1) & 1)) { *fail = 1; break; }
+            if (kt >= STAGES && !mbar_wait(&empty[s], ((kt / STAGES) - 1) & 1, wl)) { *fail = 1; break; }
             if (*fail) break;
             unsigned char *sa = smem + s * kStageBytes, *sb = sa + kTileBytes;
             mbar_expect_tx(&full[s], kStageBytes);
@@ -351,7 +375,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         int kt = 0;
         for (; kt < nk; kt++) {
             const int s = kt % STAGES;
-            if (!mbar_wait(&full[s], (kt / STAGES) & 1)) { *fail = 1; break; }
+            if (!mbar_wait(&full[s], (kt / STAGES) & 1, wl)) { *fail = 1; break; }
             tc_fence_after();
             const uint32_t sa = smem_u32(smem + s * kStageBytes), sb = sa + kTileBytes;
             const uint64_t da = sw128_desc(sa), db = sw128_desc(sb);
@@ -668,6 +692,7 @@ struct gbpf_mlp {
     std::vector<float> in_mean, in_iscale, out_mean, out_scale;  // host copies
     float *d_in_mean = nullptr, *d_in_iscale = nullptr, *d_out_mean = nullptr, *d_out_scale = nullptr;
     int *d_t = nullptr, *d_err = nullptr;
+    long long wait_cycles = 0;  // operand-ring wait limit of every GEMM (0: kWaitCycles)
     float *d_loss = nullptr, *d_sched = nullptr;
     long long steps_done = 0;  // Adam steps taken (host copy of *d_t)
     // data set
@@ -847,6 +872,7 @@ gbpf_status gbpf_mlp::forward(cudaStream_t st, Work &w, const CUtensorMap &mX, i
     for (int l = 0; l < nl; l++) {
         EpiArgs e{};
         e.err = d_err;
+        e.wait = wait_cycles;
         e.bias = L[l].b;
         e.a_row0 = l == 0 ? x_row0 : 0;
         const CUtensorMap &ta = l == 0 ? mX : w.mH[l - 1];
@@ -886,6 +912,7 @@ gbpf_status gbpf_mlp::forward(cudaStream_t st, Work &w, const CUtensorMap &mX, i
         // r = e A (loss |r|^2), then dLoss/dy = 2 (r A^T + lam e) / (rows * n_out)
         EpiArgs e{};
         e.err = d_err;
+        e.wait = wait_cycles;
         e.mode = EPI_PROJ;
         e.loss = d_loss;
         e.H = w.Rb; e.ldh = w.kp;
@@ -893,6 +920,7 @@ gbpf_status gbpf_mlp::forward(cudaStream_t st, Work &w, const CUtensorMap &mX, i
         if (s != GBPF_OK) return s;
         EpiArgs g{};
         g.err = d_err;
+        g.wait = wait_cycles;
         g.mode = EPI_LOSS_GRAD;
         g.lam = lam;
         g.gscale = 2.f / ((float)M * (float)n_out);
@@ -917,6 +945,7 @@ gbpf_status gbpf_mlp::backward(cudaStream_t st, Work &w, const CUtensorMap &mXT,
         if (l > 0) {
             EpiArgs e{};
             e.err = d_err;
+            e.wait = wait_cycles;
             e.mode = EPI_BWD_HIDDEN;
             e.Z = w.Z[l - 1]; e.ldz = hidden;
             e.H = w.dZ[l - 1]; e.ldh = hidden;
@@ -925,6 +954,7 @@ gbpf_status gbpf_mlp::backward(cudaStream_t st, Work &w, const CUtensorMap &mXT,
         }
         EpiArgs e{};
         e.err = d_err;
+        e.wait = wait_cycles;
         e.b_row0 = l == 0 ? xt_row0 : 0;
         if (adam) {
             e.mode = EPI_WGRAD_ADAM;
@@ -948,6 +978,7 @@ gbpf_status gbpf_mlp::backward(cudaStream_t st, Work &w, const CUtensorMap &mXT,
         Layer &k = L[nl];
         EpiArgs e{};
         e.err = d_err;
+        e.wait = wait_cycles;
         e.b_row0 = xt_row0;
         if (adam) {
             e.mode = EPI_WGRAD_ADAM;
@@ -1026,6 +1057,25 @@ gbpf_status mlp_infer(gbpf_mlp *m, const bf16 *X, int n, float *out, cudaStream_
 // C ABI
 // ---------------------------------------------------------------------------
 #define ARG(c) do { if (!(c)) { set_error("invalid argument: " #c); return GBPF_E_ARG; } } while (0)
+
+namespace {
+// The network's error word (set by a GEMM whose wait ran out): read after a
+// call's GEMMs and cleared, so that the next call starts clean.
+gbpf_status take_err(gbpf_mlp *m) {
+    int err = 0;
+    CK(cudaMemcpy(&err, m->d_err, 4, cudaMemcpyDeviceToHost));
+    if (!err) return GBPF_OK;
+    CK(cudaMemset(m->d_err, 0, 4));
+    set_error("a tensor-core GEMM wait ran out");
+    return GBPF_E_TIMEOUT;
+}
+}  // namespace
+
+extern "C" gbpf_status gbpf_mlp_set_wait_limit(gbpf_mlp *m, long long cycles) {
+    ARG(m && cycles >= 0);
+    m->wait_cycles = cycles;
+    return GBPF_OK;
+}
 
 extern "C" gbpf_status gbpf_mlp_create(int n_in, int n_hidden_width, int n_hidden_layers, int n_out,
                                        int linear_skip, unsigned long long seed, int device, gbpf_mlp **out) {
@@ -1131,6 +1181,7 @@ extern "C" gbpf_status gbpf_mlp_train(gbpf_mlp *m, int epochs, int batch, float 
     // (lr_final == lr: constant), read by the Adam kernels from the device
     const float sched[3] = {(float)m->steps_done, lr_final == lr ? 0.f : (float)epochs * m->graph_steps, lr_final};
     CK(cudaMemcpyAsync(m->d_sched, sched, sizeof(sched), cudaMemcpyHostToDevice, m->stream));
+    CK(cudaMemsetAsync(m->d_err, 0, 4, m->stream));
     uint64_t rs = seed ^ 0xa5a5a5a5ull;
     std::vector<int> perm(n);
     double total = 0;
@@ -1148,9 +1199,7 @@ extern "C" gbpf_status gbpf_mlp_train(gbpf_mlp *m, int epochs, int batch, float 
         CK(cudaEventElapsedTime(&ms, m->e0, m->e1));
         total += ms;
         m->steps_done += m->graph_steps;
-        int err = 0;
-        CK(cudaMemcpy(&err, m->d_err, 4, cudaMemcpyDeviceToHost));
-        if (err) { set_error("a tensor-core GEMM wait ran out"); return GBPF_E_TIMEOUT; }
+        { const gbpf_status te = take_err(m); if (te != GBPF_OK) return te; }
         if (epoch_loss) epoch_loss[ep] = loss / ((float)steps * batch * m->n_out);
     }
     if (ms_total) *ms_total = total;
@@ -1169,14 +1218,13 @@ extern "C" gbpf_status gbpf_mlp_predict(gbpf_mlp *m, const float *X, int n, floa
     CK(cudaMalloc(&buf.p, xb + 4 * (size_t)n * m->outp));
     CK(cudaMemcpyAsync(buf.p, hx.data(), 2 * (size_t)n * m->kin, cudaMemcpyHostToDevice, m->stream));
     float *out = (float *)((char *)buf.p + xb);
+    CK(cudaMemsetAsync(m->d_err, 0, 4, m->stream));
     gbpf_status s = gbpf::mlp_infer(m, (const bf16 *)buf.p, n, out, m->stream);
     if (s != GBPF_OK) return s;
     std::vector<float> hy((size_t)n * m->outp);
     CK(cudaMemcpyAsync(hy.data(), out, 4 * hy.size(), cudaMemcpyDeviceToHost, m->stream));
     CK(cudaStreamSynchronize(m->stream));
-    int err = 0;
-    CK(cudaMemcpy(&err, m->d_err, 4, cudaMemcpyDeviceToHost));
-    if (err) { set_error("a tensor-core GEMM wait ran out"); return GBPF_E_TIMEOUT; }
+    { const gbpf_status te = take_err(m); if (te != GBPF_OK) return te; }
     for (int i = 0; i < n; i++)
         for (int k = 0; k < m->n_out; k++)
             Y[(size_t)i * m->n_out + k] = hy[(size_t)i * m->outp + k] * m->out_scale[k] + m->out_mean[k];
@@ -1212,14 +1260,13 @@ extern "C" gbpf_status gbpf_mlp_gradients(gbpf_mlp *m, const float *Xn, const fl
     if ((s = make_map(&mX, dx, m->kin, n, m->kin)) != GBPF_OK) return s;
     if ((s = make_map(&mXT, dxt, n, m->kin, n)) != GBPF_OK) return s;
     CK(cudaMemsetAsync(m->d_loss, 0, 4, m->stream));
+    CK(cudaMemsetAsync(m->d_err, 0, 4, m->stream));
     if ((s = m->forward(m->stream, w, mX, 0, n, dy, 0, nullptr, true)) != GBPF_OK) return s;
     if ((s = m->backward(m->stream, w, mXT, 0, n, false)) != GBPF_OK) return s;
     float l = 0;
     CK(cudaMemcpyAsync(&l, m->d_loss, 4, cudaMemcpyDeviceToHost, m->stream));
     CK(cudaStreamSynchronize(m->stream));
-    int err = 0;
-    CK(cudaMemcpy(&err, m->d_err, 4, cudaMemcpyDeviceToHost));
-    if (err) { set_error("a tensor-core GEMM wait ran out"); return GBPF_E_TIMEOUT; }
+    { const gbpf_status te = take_err(m); if (te != GBPF_OK) return te; }
     if (loss) *loss = l / ((float)n * m->n_out);
     // gradients of the real (unpadded) parameters, layer after layer
     size_t ow = 0, ob = 0;

@@ -45,16 +45,7 @@ namespace {
 
 constexpr int kEventCap = 4096;
 
-struct Ctl {
-    int it;          // Newton updates done
-    int done;        // loop finished (converged, iteration cap, failure)
-    int status;      // gbpf_status
-    int n_events;    // switch events recorded (may exceed the log capacity)
-    unsigned long long maxG;   // bits of max|g| (non-negative doubles order as integers)
-    unsigned long long maxDx;  // bits of max|dx| of the last step
-    int converged;
-    int pad;
-};
+using Ctl = gbpf::SolveCtl;
 
 // Every device pointer and size a kernel needs, passed by value.
 struct Dev {
@@ -696,8 +687,22 @@ struct gbpf_solver {
     // wall ms of the set-up phases: Ybus, device allocation, uploads, symbolic
     // analysis (ordering + factor structure), graph construction
     double setup_ms[5] = {0, 0, 0, 0, 0};
+    // Persistent form: the whole Newton loop as one launch of the batch's
+    // block kernel on this solver's arrays (gbpf::one_record), then the branch
+    // flows, in a graph of its own (pexec).  form: GBPF_FORM_GRAPH or
+    // GBPF_FORM_PERSISTENT, the one gbpf_solve runs.
+    gbpf::OneSolve *one = nullptr;
+    cudaGraph_t pgraph = nullptr;
+    cudaGraphExec_t pexec = nullptr;
+    int form = GBPF_FORM_GRAPH;
+    int *flat_on = nullptr;   // device flag: the start is the grid's own
+    int flat_on_h = 1;
 
     ~gbpf_solver() {
+        if (pexec) cudaGraphExecDestroy(pexec);
+        if (pgraph) cudaGraphDestroy(pgraph);
+        if (one) gbpf::one_free(one);
+        if (flat_on) cudaFree(flat_on);
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         if (dmem) cudaFree(dmem);
@@ -801,7 +806,9 @@ struct gbpf_solver {
 
     gbpf_status build(const Grid &grid, const gbpf_options &o, int dev);
     gbpf_status build_graph();
+    gbpf_status build_persistent();
     gbpf_status run(gbpf_result *r);
+    cudaGraphExec_t active() const { return form == GBPF_FORM_PERSISTENT ? pexec : exec; }
 };
 
 gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev) {
@@ -999,9 +1006,51 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
     setup_ms[0] += ms_since(tp);
     tp = clk::now();
     lu_fused = !d.dense_rule && n <= (d.fp32 ? kFusedMaxN32 : kFusedMaxN64);
-    const gbpf_status st = build_graph();
+    gbpf_status st = build_graph();
+    // the persistent form where the grid's state fits one block's shared
+    // memory (metodo = esparso); it is the default in FP64.  The FP32-LU form
+    // keeps the graph by default: its block kernel's one-pass FP32 levels
+    // round the Newton step differently, and on a 118-bus grid with reactive
+    // limits that kept every step above the limit trigger's 10 tol until
+    // convergence, so no PV bus switched (the graph form's FP32 steps follow
+    // the FP64 switch path there).
+    if (st == GBPF_OK && !d.dense_rule) {
+        const std::string keep = gbpf::last_error();
+        if (build_persistent() == GBPF_OK) form = d.fp32 ? GBPF_FORM_GRAPH : GBPF_FORM_PERSISTENT;
+        else set_error(keep);
+    }
     setup_ms[4] = ms_since(tp);
     return st;
+}
+
+// The persistent form's graph: one launch of the batch's block kernel that
+// runs the whole Newton loop on this solver's arrays, then the branch flows.
+gbpf_status gbpf_solver::build_persistent() {
+    gbpf_status st = gbpf::one_create(g, opt, device, &one);
+    if (st != GBPF_OK) return st;
+    CK(cudaMalloc(&flat_on, sizeof(int)));
+    CK(cudaMemcpy(flat_on, &flat_on_h, sizeof(int), cudaMemcpyHostToDevice));
+    gbpf::OneIO io{};
+    io.V0 = d.V0; io.th0 = d.th0; io.Pliq = d.Pliq; io.Qliq = d.Qliq; io.Qload = d.Qload;
+    io.V = d.V; io.th = d.th; io.P = d.P; io.Q = d.Q;
+    io.events = d.events;
+    io.ev_cap = kEventCap;
+    io.hist = d.hist;
+    io.trig = d.trig;
+    io.hist_cap = d.hist_cap;
+    io.limQ = d.limQ;
+    io.ctl = d.ctl;
+    io.flat_on = flat_on;
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    st = gbpf::one_record(one, stream, io);
+    if (g.nL) k_flows<<<cdiv_int(g.nL, 256), 256, 0, stream>>>(d);
+    cudaGraph_t gr = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(stream, &gr);
+    if (st != GBPF_OK) { if (gr) cudaGraphDestroy(gr); return st; }
+    CK(e);
+    pgraph = gr;
+    CK(cudaGraphInstantiate(&pexec, pgraph, 0));
+    return GBPF_OK;
 }
 
 gbpf_status gbpf_solver::build_graph() {
@@ -1059,7 +1108,7 @@ gbpf_status gbpf_solver::build_graph() {
 
 gbpf_status gbpf_solver::run(gbpf_result *r) {
     CK(cudaSetDevice(device));
-    CK(cudaGraphLaunch(exec, stream));
+    CK(cudaGraphLaunch(active(), stream));
     CK(cudaMemcpyAsync(&last, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     if (r) {
@@ -1107,6 +1156,16 @@ extern "C" gbpf_status gbpf_solver_set_start(gbpf_solver *s, const double *V0, c
     CK(cudaSetDevice(s->device));
     if (V0) CK(cudaMemcpyAsync(s->d.V0, V0, b, cudaMemcpyHostToDevice, s->stream));
     if (theta0) CK(cudaMemcpyAsync(s->d.th0, theta0, b, cudaMemcpyHostToDevice, s->stream));
+    if ((V0 || theta0) && s->flat_on) {
+        // the persistent form takes iteration 0 from the topology's shared copy
+        // only while the start is the grid's own
+        const bool own = (!V0 || std::equal(V0, V0 + s->g.nB, s->g.V0.begin())) &&
+                         (!theta0 || std::equal(theta0, theta0 + s->g.nB, s->g.theta0.begin()));
+        if ((int)own != s->flat_on_h) {
+            s->flat_on_h = own;
+            CK(cudaMemcpyAsync(s->flat_on, &s->flat_on_h, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+        }
+    }
     if (Pliq) CK(cudaMemcpyAsync(s->d.Pliq, Pliq, b, cudaMemcpyHostToDevice, s->stream));
     if (Qliq) CK(cudaMemcpyAsync(s->d.Qliq, Qliq, b, cudaMemcpyHostToDevice, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -1196,6 +1255,31 @@ extern "C" gbpf_status gbpf_solver_set_lu_launch(gbpf_solver *s, int mode) {
     return s->build_graph();
 }
 
+extern "C" gbpf_status gbpf_solver_set_form(gbpf_solver *s, int form) {
+    ARGCHECK(s && (form == GBPF_FORM_GRAPH || form == GBPF_FORM_PERSISTENT));
+    if (form == GBPF_FORM_PERSISTENT && !s->pexec) {
+        set_error("this grid has no persistent form (metodo = denso, or its state does not fit one block's shared "
+                  "memory)");
+        return GBPF_E_UNSUPPORTED;
+    }
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    s->form = form;
+    return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_solver_get_form(const gbpf_solver *s, int out[3]) {
+    ARGCHECK(s && out);
+    out[0] = s->form;
+    // persistent: the Newton kernel and the flows; graph: reset, injections
+    // (+ limits), mismatch and control before the loop, flows after
+    const int flows = s->g.nL ? 1 : 0;
+    const int eval = 4 + (s->opt.lim_inj_reat && s->g.nPV ? 1 : 0);
+    out[1] = s->form == GBPF_FORM_PERSISTENT ? 1 + flows : 1 + eval + flows;
+    out[2] = s->form == GBPF_FORM_PERSISTENT ? 0 : s->kernels_per_iter;
+    return GBPF_OK;
+}
+
 extern "C" gbpf_status gbpf_solver_info(const gbpf_solver *s, long long info[8]) {
     ARGCHECK(s && info);
     info[0] = s->g.nB;
@@ -1213,7 +1297,7 @@ extern "C" gbpf_status gbpf_solver_time(gbpf_solver *s, int repeats, double *ms_
     ARGCHECK(s && ms_total && repeats > 0);
     CK(cudaSetDevice(s->device));
     CK(cudaEventRecord(s->ev0, s->stream));
-    for (int i = 0; i < repeats; i++) CK(cudaGraphLaunch(s->exec, s->stream));
+    for (int i = 0; i < repeats; i++) CK(cudaGraphLaunch(s->active(), s->stream));
     CK(cudaEventRecord(s->ev1, s->stream));
     CK(cudaEventSynchronize(s->ev1));
     float ms = 0;

@@ -70,6 +70,17 @@ typedef enum {
     GBPF_PREC_FP32_IR = 1     /* FP32 LU and triangular solves + FP64 refinement  */
 } gbpf_precision;
 
+/* How gbpf_solve runs the Newton loop (not a data.txt key of the reference;
+ * both replace the host loop of mNR, GPU/newtonRaphson.cuh:283-565).
+ * GRAPH: one CUDA graph whose device-side WHILE node repeats the iteration's
+ * kernels (injections, limits, mismatch, fill, factor, substitutions,
+ * update), each phase spread over the whole GPU.  PERSISTENT: the whole loop
+ * as one launch of one thread block (the batch's block-per-instance kernel on
+ * the solver's own arrays), for grids whose state fits a block's shared
+ * memory: no per-phase launches, so a small grid's solve is bound by its own
+ * dependent latency only. */
+typedef enum { GBPF_FORM_GRAPH = 1, GBPF_FORM_PERSISTENT = 2 } gbpf_form;
+
 /* The data.txt options, namespace global of GPU/sistInfo.h:37-60, with the
  * same defaults. */
 typedef struct {
@@ -245,6 +256,18 @@ gbpf_status gbpf_solver_flows(gbpf_solver *s, double *Pdp, double *Ppd, double *
  * the graph.  Not for metodo = denso. */
 gbpf_status gbpf_solver_set_lu_launch(gbpf_solver *s, int mode);
 
+/* The form gbpf_solve runs (gbpf_form).  gbpf_solver_create picks
+ * GBPF_FORM_PERSISTENT for metodo = esparso in FP64 wherever the grid's state
+ * fits one block's shared memory (up to ~1,900 buses) and GBPF_FORM_GRAPH
+ * otherwise (the FP32-LU form may still be set to PERSISTENT); in FP64 the
+ * same iterations, switch events, |V|, theta, history and flows come out of
+ * both.  set: GBPF_E_UNSUPPORTED when the grid cannot run
+ * PERSISTENT.  get: out[0] = the form, out[1] = kernel launches per solve of
+ * it (for GRAPH: before the loop, per iteration and after; out[2] = per
+ * iteration). */
+gbpf_status gbpf_solver_set_form(gbpf_solver *s, int form);
+gbpf_status gbpf_solver_get_form(const gbpf_solver *s, int out[3]);
+
 /* Solver facts: info[0..7] = nB, n blocks (nB-1), factor blocks (off-diagonal
  * per triangle), update pairs, forward levels, backward levels, graph nodes,
  * kernels launched per Newton iteration. */
@@ -409,19 +432,31 @@ gbpf_status gbpf_batch_results(gbpf_batch *b, int *iterations, int *status, doub
  * gbpf_solver_events. */
 gbpf_status gbpf_batch_events(gbpf_batch *b, int inst, int *ev, int cap, int *n);
 
-/* For callers that cannot allocate device memory when they solve: their
- * solves run inside a stream-capture region where allocation is not allowed,
- * or their device memory belongs to another allocator.  No counterpart in the
- * reference.  Solves n_inst instances like gbpf_batch_set_instances +
- * gbpf_batch_solve, on caller-owned DEVICE buffers packed in instance order
- * (V0, theta0, Pliq, Qliq, Qload in; V, theta, Pcalc, Qcalc, iterations,
- * status, final_mismatch out); grid_of_inst is a HOST array.  Allocates
- * nothing: all scratch lives in one static 8 MiB device array, each GPU that
- * loads the library holds it until exit, and every call shares it, so calls
- * that overlap on the GPU race.  gbpf_batch_create does the one-time set-up
- * for its device.  Rejects with GBPF_E_ARG an instance count or a factor that
- * does not fit the scratch.  Does not record switch events.  Asynchronous on
- * `stream` (a cudaStream_t; NULL = the batch's stream). */
+/* Switch events of every instance in one call: ev[(i * cap + k) * 4 ..] holds
+ * event k of instance i (cap <= 16, sorted as gbpf_batch_events sorts them,
+ * unused slots zero) and n[i] the events instance i recorded (it may exceed
+ * cap, which then keeps the first cap).  The bulk form of gbpf_batch_events,
+ * for comparing the switch paths of two precisions scenario by scenario
+ * (the reference prints them per solve, GPU/limiteInjReat.cuh:12-34). */
+gbpf_status gbpf_batch_events_all(gbpf_batch *b, int *ev, int cap, int *n);
+
+/* For callers that cannot allocate device memory when they solve.  No
+ * counterpart in the reference.  cudaMalloc can synchronise the device and
+ * takes an unbounded time, so a caller with a fixed cycle time (a real-time
+ * contingency loop, a control-room state estimator) forbids it after
+ * start-up; other callers run inside a host framework whose device memory
+ * belongs to its own allocator.  Solves n_inst instances like
+ * gbpf_batch_set_instances + gbpf_batch_solve, on caller-owned DEVICE buffers
+ * packed in instance order (V0, theta0, Pliq, Qliq, Qload in; V, theta, Pcalc,
+ * Qcalc, iterations, status, final_mismatch out); grid_of_inst is a HOST
+ * array, read before the call returns.  Allocates nothing: all scratch lives
+ * in one static 8 MiB device array, each GPU that loads the library holds it
+ * until exit, and every call shares it, so calls that overlap on the GPU race.
+ * gbpf_batch_create does the one-time set-up for its device (the array's
+ * device address).  Rejects with GBPF_E_ARG an instance count or a factor that
+ * does not fit the scratch, and a grid whose state does not fit one block's
+ * shared memory.  Does not record switch events.  The solve is asynchronous
+ * on `stream` (a cudaStream_t; NULL = the batch's stream). */
 gbpf_status gbpf_batch_solve_noalloc(gbpf_batch *b, int n_inst, const int *grid_of_inst,
                                      const double *V0, const double *theta0, const double *Pliq,
                                      const double *Qliq, const double *Qload, double *V,
@@ -473,6 +508,17 @@ gbpf_status gbpf_mlp_train(gbpf_mlp *m, int epochs, int batch, float lr, float l
  * makes |e A| the linearised mismatch of the predicted start, which is what
  * decides how many Newton iterations the start saves. */
 gbpf_status gbpf_mlp_set_loss_metric(gbpf_mlp *m, const float *A, int k, float lam);
+
+/* Limit of the operand-ring mbarrier waits of the network's tensor-core GEMMs,
+ * in SM clock cycles (0 = the default, about 2 s at 2 GHz; no counterpart in
+ * the reference, which has no network).  A wait that runs out makes the GEMM
+ * stop issuing work, wait for its tensor-core operations and copies already in
+ * flight (fixed ~2 s bound), free its tensor memory and return; the call then
+ * returns GBPF_E_TIMEOUT and the handle stays usable.  Applies to GEMMs
+ * launched afterwards by gbpf_mlp_predict, gbpf_mlp_gradients and the
+ * warm-started solves; the training graph keeps the limit in force when
+ * gbpf_mlp_train first builds it. */
+gbpf_status gbpf_mlp_set_wait_limit(gbpf_mlp *m, long long cycles);
 
 /* Y [n, n_out] = network(X [n, n_in]), raw units in and out. */
 gbpf_status gbpf_mlp_predict(gbpf_mlp *m, const float *X, int n, float *Y);

@@ -8,13 +8,17 @@ that replays the reference GPU Newton loop and its limit rules.  Inputs are
 * the synthetic grids written here (c1.cdf: 14-bus, c2_*.cdf: 118-bus, and the
   MATPOWER cases m_edge.m and c2_tx.m), which are committed so that the GPU
   box, which has no reference checkout, reads the very same bytes, and
-* the reference's IEEE cases, read in place from the reference checkout (only
-  their solutions are stored, as ieee_*.json).
+* the reference's IEEE cases (GPU/ieee14.cdf ... GPU/ieee118x64.cdf), copied
+  byte for byte from the reference checkout into ieee/*.cdf.gz (gzip, no name
+  or time stamp, so a rerun writes the same bytes), so that the GPU tests read
+  the reference's own inputs; their solutions are ieee_*.json (.json.gz above
+  1,000 buses).
 
 Run from the repository root after building the library and the harness:
     python -c "import __graft_entry__ as g; g.build()"
     python tests/golden/make_golden.py [/path/to/reference]
 """
+import gzip
 import importlib
 import json
 import os
@@ -30,7 +34,9 @@ gb = importlib.import_module("experience-of-using-gpu-in-power-flow-computation_
 
 REF_NR = os.path.join(ROOT, "oracle", "_ref", "ref_nr")
 BASE_SEED = 20261203
-IEEE = ["ieee14", "ieee30", "ieee57", "ieee118", "ieee118x2", "ieee118x4", "ieee118x8"]
+IEEE = ["ieee14", "ieee30", "ieee57", "ieee118", "ieee118x2", "ieee118x4", "ieee118x8", "ieee118x16", "ieee118x32",
+        "ieee118x64"]
+IEEE_DIR = os.path.join(HERE, "ieee")
 STATE_KEYS = ("V", "theta", "Pcalc", "Qcalc", "Pdp", "Ppd", "Qdp", "Qpd")
 
 
@@ -114,9 +120,23 @@ def with_transformer_charging(grid):
 
 
 def write(name, rec):
-    with open(os.path.join(HERE, name), "w") as f:
-        json.dump(rec, f, indent=0, separators=(",", ":"))
-        f.write("\n")
+    text = json.dumps(rec, indent=0, separators=(",", ":")) + "\n"
+    if name.endswith(".gz"):
+        with open(os.path.join(HERE, name), "wb") as f:
+            f.write(gzip.compress(text.encode(), compresslevel=9, mtime=0))
+    else:
+        with open(os.path.join(HERE, name), "w") as f:
+            f.write(text)
+
+
+def copy_fixture(src, case):
+    """The reference's input file as a gzip fixture (deterministic bytes)."""
+    os.makedirs(IEEE_DIR, exist_ok=True)
+    with open(src, "rb") as f:
+        data = f.read()
+    with open(os.path.join(IEEE_DIR, case + ".cdf.gz"), "wb") as f:
+        f.write(gzip.compress(data, compresslevel=9, mtime=0))
+    return "ieee/" + case + ".cdf.gz"
 
 
 def main():
@@ -159,20 +179,21 @@ def main():
         write(out, r)
         index.append(dict(cdf=name, golden=out, tol=tol, max_iter=maxit, lim=lim, iterations=r["iterations"],
                           events=len(r["events"])))
-    # IEEE cases of the reference, solutions only
+    # IEEE cases of the reference: the input as a fixture, and its solutions
     for case in IEEE:
         path = os.path.join(ref_root, "GPU", case + ".cdf")
         if not os.path.exists(path):
             continue
+        fixture = copy_fixture(path, case)
         for lim in (0, 1):
             r = run_ref(path, 1e-8, 100, lim)
             if not r["converged"]:  # diverging switch cycles: keep the history, not the state
                 for k in STATE_KEYS:
                     r.pop(k, None)
                 r["events"] = r["events"][:40]
-            out = f"ieee_{case}_lim{lim}.json"
+            out = f"ieee_{case}_lim{lim}.json" + (".gz" if r.get("nB", 0) > 1000 else "")
             write(out, r)
-            index.append(dict(cdf=case + ".cdf", golden=out, tol=1e-8, max_iter=100, lim=lim,
+            index.append(dict(cdf=case + ".cdf", fixture=fixture, golden=out, tol=1e-8, max_iter=100, lim=lim,
                               iterations=r["iterations"], events=len(r["events"])))
     with open(os.path.join(HERE, "index.json"), "w") as f:
         json.dump(index, f, indent=1)

@@ -9,7 +9,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, ieee_cases, ieee_path, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -55,6 +55,55 @@ def test_batch_fp64_matches_oracle(gb, oracle, cdf):
         assert np.max(np.abs(b.slice(r["V"], i) - ref["V"])) < 1e-9
         assert np.max(np.abs(b.slice(r["theta"], i) - ref["theta"])) < 1e-9
     assert b.info()["factors_in_smem"] == 1
+
+
+@pytest.mark.parametrize("case", ieee_cases(max_buses=3776), ids=lambda c: c["golden"])
+def test_batch_fp64_matches_reference_golden_on_ieee(gb, case):
+    """The reference's own IEEE inputs as batch instances (three copies of the
+    case's own loads): identical iterations and switch events, |V|, theta
+    within 1e-9 of the reference-built golden, in every copy."""
+    g = gb.read_grid(ieee_path(case))
+    gold = load_golden(case["golden"])
+    n = 3
+    b, r = run_batch(gb, [g], np.zeros(n, np.int32), None, None, None, no_max_iter=case["max_iter"],
+                     lim_inj_reat=case["lim"])
+    for i in range(n):
+        assert r["iterations"][i] == gold["iterations"], i
+        assert (r["status"][i] == 0) == bool(gold["converged"]), i
+        ev = [list(e) for e in b.events(i)]
+        assert ev == gold["events"][:len(ev)] and len(ev) == min(16, len(gold["events"]))
+        if gold["converged"]:
+            assert r["final_mismatch"][i] <= gold["tol"]
+            assert np.max(np.abs(b.slice(r["V"], i) - np.array(gold["V"]))) < 1e-9
+            assert np.max(np.abs(b.slice(r["theta"], i) - np.array(gold["theta"]))) < 1e-9
+
+
+def test_batch_rejects_grids_beyond_shared_memory(gb):
+    """A block keeps each instance's substitution vectors and bus flags in
+    shared memory; the 7,552-bus ieee118x64 needs more than a block has, which
+    the batch reports (GBPF_E_UNSUPPORTED) instead of launching.  The
+    single-grid solver takes that grid (test_gpu_parity)."""
+    case = next(c for c in ieee_cases() if c["cdf"] == "ieee118x64.cdf")
+    b = gb.Batch([gb.read_grid(ieee_path(case))], tolerancia=1e-8, no_max_iter=100)
+    with pytest.raises(gb.GbpfError) as e:
+        b.set_instances(np.zeros(2, np.int32))
+    assert e.value.status == gb.E_UNSUPPORTED
+    assert "shared memory" in str(e.value)
+
+
+def test_batch_mixed_ieee_topologies_fp64(gb):
+    """Every IEEE case up to 944 buses in one launch, instances interleaved."""
+    cases = [c for c in ieee_cases(max_buses=944) if c["lim"] == 1]
+    grids = [gb.read_grid(ieee_path(c)) for c in cases]
+    golds = [load_golden(c["golden"]) for c in cases]
+    inst = np.tile(np.arange(len(cases), dtype=np.int32), 4)
+    b, r = run_batch(gb, grids, inst, None, None, None)
+    for i, t in enumerate(inst):
+        gold = golds[t]
+        assert r["iterations"][i] == gold["iterations"], (i, cases[t]["cdf"])
+        if gold["converged"]:
+            assert np.max(np.abs(b.slice(r["V"], i) - np.array(gold["V"]))) < 1e-9
+            assert np.max(np.abs(b.slice(r["theta"], i) - np.array(gold["theta"]))) < 1e-9
 
 
 def test_batch_mixed_topologies_fp64(gb, oracle, tmp_path):

@@ -12,7 +12,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, committed_cases, load_golden
+from conftest import GOLDEN, committed_cases, ieee_cases, ieee_path, load_golden
 from test_gpu_parity import STATE_TOL, check_solution, solver
 
 pytestmark = pytest.mark.gpu
@@ -27,6 +27,15 @@ DENSO = 1
 def test_dense_solve_matches_reference_golden(gb, case):
     grid, s = solver(gb, os.path.join(GOLDEN, case["cdf"]), tolerancia=case["tol"],
                      no_max_iter=case["max_iter"], lim_inj_reat=case["lim"], metodo=DENSO)
+    check_solution(s.solve(), load_golden(case["golden"]))
+
+
+# The reference's IEEE inputs up to 1,888 buses (N = 3,774); their parallel
+# branches all run in one direction, so calcYbus and calcYbusSp agree there.
+@pytest.mark.parametrize("case", ieee_cases(max_buses=1888), ids=lambda c: c["golden"])
+def test_dense_solve_matches_reference_golden_on_ieee(gb, case):
+    grid, s = solver(gb, ieee_path(case), tolerancia=case["tol"], no_max_iter=case["max_iter"],
+                     lim_inj_reat=case["lim"], metodo=DENSO)
     check_solution(s.solve(), load_golden(case["golden"]))
 
 

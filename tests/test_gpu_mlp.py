@@ -302,3 +302,21 @@ def test_warm_start_in_flight_on_two_batches(gb, warm_net):
     assert gb.time_warm_pipelined(bs, m, 5) > 0
     for b, (w0, r0) in zip(bs, ref):
         np.testing.assert_array_equal(b.results()["V"], r0["V"])
+
+
+def test_gemm_wait_limit_runs_out_and_the_handle_recovers(gb):
+    """A GEMM whose operand-ring waits may last 1 clock cycle cannot wait for
+    its first TMA tile (hundreds of cycles away): every such wait runs out, the
+    CTA drains its copies and tensor-core work, frees its tensor memory and
+    returns, and the call reports GBPF_E_TIMEOUT.  With the default limit the
+    same handle predicts again, bit for bit what it predicted before."""
+    m = gb.MLP(1024, 256, width=256, n_layers=2, skip=True, seed=21)
+    X = np.random.default_rng(21).normal(size=(512, 1024)).astype(np.float32)
+    before = m.predict(X)
+    m.set_wait_limit(1)
+    with pytest.raises(gb.GbpfError) as e:
+        m.predict(X)
+    assert e.value.status == gb.E_TIMEOUT
+    assert "wait ran out" in str(e.value)
+    m.set_wait_limit(0)
+    np.testing.assert_array_equal(m.predict(X), before)

@@ -12,7 +12,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, committed_cases, load_golden
+from conftest import GOLDEN, case_path, committed_cases, ieee_cases, ieee_path, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -124,11 +124,46 @@ def check_solution(res, gold):
             assert np.max(np.abs(res[k] - np.array(gold[k]))) < 1e-7, k
 
 
-@pytest.mark.parametrize("case", committed_cases(), ids=lambda c: c["golden"])
-def test_solve_matches_reference_golden(gb, case):
-    grid, s = solver(gb, os.path.join(GOLDEN, case["cdf"]), tolerancia=case["tol"],
+@pytest.mark.parametrize("form", ["graph", "persistent"])
+@pytest.mark.parametrize("case", committed_cases() + ieee_cases(), ids=lambda c: c["golden"])
+def test_solve_matches_reference_golden(gb, case, form):
+    """Synthetic grids and the reference's own IEEE inputs (ieee14 ... the
+    7,552-bus ieee118x64, with and without reactive limits, including the
+    100-iteration PV/PQ cycle of ieee118x4 with limits), in both forms of
+    gbpf_solve: the graph of per-phase kernels and the one persistent launch
+    (grids whose state fits a block's shared memory)."""
+    grid, s = solver(gb, case_path(case), tolerancia=case["tol"],
                      no_max_iter=case["max_iter"], lim_inj_reat=case["lim"])
-    check_solution(s.solve(), load_golden(case["golden"]))
+    if form == "graph":
+        s.set_form(gb.FORM_GRAPH)
+    elif s.form()["form"] != gb.FORM_PERSISTENT:
+        pytest.skip("the grid's state does not fit one block's shared memory")
+    gold = load_golden(case["golden"])
+    res = s.solve()
+    check_solution(res, gold)
+    # max|g| per iteration; a non-converging PV/PQ cycle amplifies rounding
+    # differences over its 100 iterations, so there only the first ten count
+    h = np.array(gold["hist"])[:-1] if gold["converged"] else np.array(gold["hist"])[:10]
+    np.testing.assert_allclose(res["hist"][:len(h)], h, rtol=1e-6, atol=1e-12)
+
+
+@pytest.mark.parametrize("case", [c for c in committed_cases() + ieee_cases() if c["lim"] == 1],
+                         ids=lambda c: c["golden"])
+def test_fp32_lu_solve_against_reference_golden(gb, case):
+    """The FP32-LU form (FP32 factor and substitutions, FP64 mismatch, test
+    and update) on the same inputs: max|g| <= tol in FP64 and |V|, theta
+    within 1e-6 of the reference's FP64 solution where it takes the FP64
+    switch path; the switch path itself is reported, not required."""
+    grid, s = solver(gb, case_path(case), tolerancia=case["tol"], no_max_iter=case["max_iter"],
+                     lim_inj_reat=case["lim"], precision=gb.PREC_FP32_IR)
+    gold = load_golden(case["golden"])
+    res = s.solve()
+    if not gold["converged"]:
+        return
+    assert res["converged"] and res["final_mismatch"] <= gold["tol"]
+    if [list(e[1:]) for e in res["events"]] == [e[1:] for e in gold["events"]]:
+        assert np.max(np.abs(res["V"] - np.array(gold["V"]))) < 1e-6
+        assert np.max(np.abs(res["theta"] - np.array(gold["theta"]))) < 1e-6
 
 
 def compare_with_oracle(gb, oracle, grid, path, lim, tol=1e-8, max_iter=60):
@@ -246,3 +281,60 @@ def test_lu_launch_forms_agree(gb, prec):
         assert a["iterations"] == b["iterations"] and a["events"] == b["events"]
         for k in ("V", "theta", "Pcalc", "Qcalc"):
             np.testing.assert_allclose(a[k], b[k], rtol=0, atol=1e-12, err_msg=k)
+
+
+@pytest.mark.parametrize("precision,lim", [("PREC_FP64", 1), ("PREC_FP32_IR", 0)])
+def test_persistent_form_equals_graph_form(gb, precision, lim):
+    """The default FP64 form of a small grid is the persistent launch; on a
+    grid that switches PV buses it gives what the graph form gives:
+    iterations, events, max|g| per iteration, the limit-check iterations,
+    state and flows (to rounding: the two sum the LU updates in different
+    orders), also after set_start moves the start away from the grid's own
+    and back.  The FP32-LU form (graph by default; persistent on request)
+    without reactive limits: both within 1e-6 of each other."""
+    path = os.path.join(GOLDEN, "c2_s8.cdf")
+    grid = gb.read_grid(path)
+    opts = dict(tolerancia=1e-8, no_max_iter=100, lim_inj_reat=lim, metodo=0, precision=getattr(gb, precision))
+    p, g = gb.Solver(grid, **opts), gb.Solver(grid, **opts)
+    if precision == "PREC_FP64":
+        assert p.form()["form"] == gb.FORM_PERSISTENT and p.form()["launches"] == 2
+    else:
+        assert p.form()["form"] == gb.FORM_GRAPH
+        p.set_form(gb.FORM_PERSISTENT)
+    g.set_form(gb.FORM_GRAPH)
+    b = grid.buses()
+    rng = np.random.default_rng(4)
+    starts = [None, (b["V0"] * (1 + 0.01 * rng.standard_normal(grid.nB)), b["theta0"] + 0.05 * rng.standard_normal(grid.nB)),
+              (b["V0"], b["theta0"])]
+    tol = 1e-12 if precision == "PREC_FP64" else 1e-6
+    for st in starts:
+        if st is not None:
+            for x in (p, g):
+                x.set_start(V0=st[0], theta0=st[1])
+        rp, rg = p.solve(), g.solve()
+        assert rp["converged"] and rg["converged"]
+        assert [e[1:] for e in rp["events"]] == [e[1:] for e in rg["events"]]
+        assert rp["nPQlim"] == rg["nPQlim"]
+        if st is None and lim:
+            assert len(rp["events"]) > 0
+        if precision == "PREC_FP64":
+            assert rp["iterations"] == rg["iterations"] and rp["events"] == rg["events"]
+            np.testing.assert_array_equal(p.triggers(), g.triggers())
+            np.testing.assert_allclose(rp["hist"], rg["hist"], rtol=1e-6, atol=1e-12)
+        for k in ("V", "theta"):
+            assert np.max(np.abs(rp[k] - rg[k])) < tol, k
+        for k in ("Pcalc", "Qcalc", "Pdp", "Ppd", "Qdp", "Qpd"):
+            assert np.max(np.abs(rp[k] - rg[k])) < 1e3 * tol, k
+
+
+def test_form_selection(gb):
+    """The persistent form is offered where the grid's state fits one block's
+    shared memory: not for the 7,552-bus ieee118x64, never for metodo = denso."""
+    case = next(c for c in ieee_cases() if c["cdf"] == "ieee118x64.cdf")
+    big = gb.Solver(gb.read_grid(ieee_path(case)), tolerancia=1e-8, no_max_iter=100, metodo=0)
+    assert big.form()["form"] == gb.FORM_GRAPH
+    with pytest.raises(gb.GbpfError) as e:
+        big.set_form(gb.FORM_PERSISTENT)
+    assert e.value.status == gb.E_UNSUPPORTED
+    dense = gb.Solver(gb.read_grid(os.path.join(GOLDEN, "c1.cdf")), tolerancia=1e-8, no_max_iter=100, metodo=1)
+    assert dense.form()["form"] == gb.FORM_GRAPH

@@ -7,7 +7,7 @@ import re
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, REFERENCE_GPU, ROOT
+from conftest import GOLDEN, ROOT, ieee_cases, ieee_path
 
 DATA_TXT = """metodo         = esparso;        // esparso, denso or hibridoC
 openmp         = OFF;
@@ -89,15 +89,15 @@ def test_options_load_missing_file(gb, tmp_path):
 
 def _cases():
     out = [os.path.join(GOLDEN, f) for f in sorted(os.listdir(GOLDEN)) if f.endswith(".cdf")]
-    for c in ("ieee14", "ieee57", "ieee118", "ieee118x2"):
-        p = os.path.join(REFERENCE_GPU, c + ".cdf")
-        if os.path.exists(p):
-            out.append(p)
+    # the reference's own IEEE inputs (committed fixtures)
+    out += [c for c in ieee_cases() if c["lim"] == 0]
     return out
 
 
-@pytest.mark.parametrize("path", _cases(), ids=os.path.basename)
+@pytest.mark.parametrize("path", _cases(), ids=lambda p: p["cdf"] if isinstance(p, dict) else os.path.basename(p))
 def test_reader_matches_oracle_reader(gb, oracle, path):
+    if isinstance(path, dict):
+        path = ieee_path(path)
     g = gb.read_grid(path)
     o = oracle.Grid(path)
     assert (g.nB, g.nL, g.nPV, g.nPQ, g.slack) == (o.nB, o.nL, o.nPV, o.nPQ, o.slack)
@@ -117,9 +117,7 @@ def test_reader_matches_oracle_reader(gb, oracle, path):
 
 
 def test_parallel_branch_merge_notices(gb):
-    p = os.path.join(REFERENCE_GPU, "ieee118.cdf")
-    if not os.path.exists(p):
-        pytest.skip("reference checkout not present")
+    p = ieee_path(next(c for c in ieee_cases() if c["cdf"] == "ieee118.cdf"))
     g = gb.read_grid(p)
     assert g.nL == 179  # 186 branch lines, 7 parallel pairs merged
     assert sum(n.startswith("Ramo ") for n in g.notices) == 7

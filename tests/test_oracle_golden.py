@@ -5,7 +5,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, REFERENCE_GPU, committed_cases, ieee_cases, load_golden
+from conftest import GOLDEN, REFERENCE_GPU, committed_cases, ieee_cases, ieee_path, load_golden
 
 STATE_TOL = 1e-9  # |V| and theta, from the parity target
 
@@ -33,11 +33,18 @@ def test_oracle_matches_reference_on_synthetic(oracle, case):
 
 @pytest.mark.parametrize("case", ieee_cases(), ids=lambda c: c["golden"])
 def test_oracle_matches_reference_on_ieee(oracle, case):
-    path = os.path.join(REFERENCE_GPU, case["cdf"])
-    if not os.path.exists(path):
-        pytest.skip("reference checkout not present")
-    g = oracle.Grid(path)
+    g = oracle.Grid(ieee_path(case))
     check(g.solve(case["tol"], case["max_iter"], case["lim"]), load_golden(case["golden"]))
+
+
+@pytest.mark.parametrize("case", [c for c in ieee_cases() if c["lim"] == 0], ids=lambda c: c["cdf"])
+def test_ieee_fixture_is_the_reference_file(case):
+    """The committed fixture holds the reference's input byte for byte."""
+    src = os.path.join(REFERENCE_GPU, case["cdf"])
+    if not os.path.exists(src):
+        pytest.skip("reference checkout not present")
+    with open(src, "rb") as f, open(ieee_path(case), "rb") as g:
+        assert f.read() == g.read()
 
 
 def test_switch_cases_are_covered():
