@@ -103,6 +103,12 @@ struct EpiArgs {
     float lr, b1, b2, eps;
     int *err;
     long long wait;       // limit of the operand-ring waits in clock cycles (0: kWaitCycles)
+    // split-K (training GEMMs with few output tiles): gridDim.z CTAs share an
+    // output tile, each over its range of k-tiles; partial tiles go to ws
+    // (column-major 128 x 128 fp32 per split) and the last CTA of the tile to
+    // arrive (ws_cnt) sums them in split order and runs the epilogue
+    float *ws;
+    int *ws_cnt;
 };
 
 // Learning rate of Adam step t (1-based): cosine decay from lr to sched[2]
@@ -333,6 +339,9 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     // accumulator: C = A B^T + A2 B2^T (K2 = 0: one pair)
     const int nk1 = (K + BK - 1) / BK, nk = nk1 + (K2 + BK - 1) / BK;
     const long long wl = e.wait > 0 ? e.wait : kWaitCycles;
+    // this CTA's k-tiles [kb, ke) (the whole range unless split)
+    const int S = gridDim.z, z = blockIdx.z;
+    const int kb = (int)((long long)nk * z / S), ke = (int)((long long)nk * (z + 1) / S);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
@@ -353,11 +362,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     const uint32_t tmem = *tmem_slot;
 
     if (warp == 0 && lane == 0) {
-        // TMA producer
-        int kt = 0;
-        for (; kt < nk; kt++) {
-            const int s = kt % STAGES;
-            if (kt >= STAGES && !mbar_wait(&empty[s], ((kt / STAGES) - 1) & 1, wl)) { *fail = 1; break; }
+        // TMA producer (j counts this CTA's k-tiles: ring slot and phase)
+        int j = 0;
+        for (; j < ke - kb; j++) {
+            const int kt = kb + j, s = j % STAGES;
+            if (j >= STAGES && !mbar_wait(&empty[s], ((j / STAGES) - 1) & 1, wl)) { *fail = 1; break; }
             if (*fail) break;
             unsigned char *sa = smem + s * kStageBytes, *sb = sa + kTileBytes;
             mbar_expect_tx(&full[s], kStageBytes);
@@ -369,22 +378,22 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                 tma_load_2d(sb, &tb2, (kt - nk1) * BK, n0, &full[s]);
             }
         }
-        *issued = kt;
+        *issued = j;
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
-        int kt = 0;
-        for (; kt < nk; kt++) {
-            const int s = kt % STAGES;
-            if (!mbar_wait(&full[s], (kt / STAGES) & 1, wl)) { *fail = 1; break; }
+        int j = 0;
+        for (; j < ke - kb; j++) {
+            const int s = j % STAGES;
+            if (!mbar_wait(&full[s], (j / STAGES) & 1, wl)) { *fail = 1; break; }
             tc_fence_after();
             const uint32_t sa = smem_u32(smem + s * kStageBytes), sb = sa + kTileBytes;
             const uint64_t da = sw128_desc(sa), db = sw128_desc(sb);
 #pragma unroll
             for (int kk = 0; kk < BK / 16; kk++)  // K = 16 per instruction: +32 B along the swizzled row
-                mma_bf16(tmem, da + (uint64_t)(2 * kk), db + (uint64_t)(2 * kk), (kt | kk) != 0);
+                mma_bf16(tmem, da + (uint64_t)(2 * kk), db + (uint64_t)(2 * kk), (j | kk) != 0);
             mma_commit(&empty[s]);
         }
-        *consumed = kt;
+        *consumed = j;
         mma_commit(accf);
     }
     __syncwarp();
@@ -398,8 +407,48 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         if (threadIdx.x == 0) {
             if (e.err) atomicExch(e.err, 1);
             // copies issued but never consumed are still in flight: wait for them
-            for (int kt = *consumed; kt < *issued; kt++) (void)mbar_wait(&full[kt % STAGES], (kt / STAGES) & 1);
+            for (int j = *consumed; j < *issued; j++) (void)mbar_wait(&full[j % STAGES], (j / STAGES) & 1);
         }
+    }
+    // split-K: every split stores its partial tile; the last to arrive goes on
+    // with the epilogue, the others are done
+    __shared__ int s_last;
+    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+    const int arow = warp * 32 + lane;  // accumulator row (TMEM lane) of this thread
+    if (S > 1 && !*fail) {
+        float *part = e.ws + ((size_t)tile * S + z) * BM * BN;
+        for (int c = 0; c < BN / 16; c++) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v);
+#pragma unroll
+            for (int q = 0; q < 16; q++) part[(size_t)(c * 16 + q) * BM + arow] = v[q];
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s_last = atomicAdd(e.ws_cnt + tile, 1) == S - 1;
+            if (s_last) e.ws_cnt[tile] = 0;  // ready for the next GEMM that splits this tile
+        }
+        __syncthreads();
+        __threadfence();
+    }
+    // the accumulator's 16 columns c*16.. of this thread's row: from tensor
+    // memory, or the sum of the splits' partial tiles in split order
+    auto acc16 = [&](int c, float (&v)[16]) {
+        if (S == 1) {
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v);
+            return;
+        }
+        const float *base = e.ws + (size_t)tile * S * BM * BN + (size_t)(c * 16) * BM + arow;
+#pragma unroll
+        for (int q = 0; q < 16; q++) v[q] = 0.f;
+        for (int zz = 0; zz < S; zz++) {
+#pragma unroll
+            for (int q = 0; q < 16; q++) v[q] += __ldcg(base + (size_t)zz * BM * BN + (size_t)q * BM);
+        }
+    };
+    if (*fail || (S > 1 && !s_last)) {
+        // nothing more to do for this CTA
     } else if (e.mode == EPI_WGRAD_ADAM) {
         // Adam over the gradient tile, staged through shared memory (the
         // operand ring is idle once the accumulator is complete) so that each
@@ -407,11 +456,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         // weights and moments, 4 bf16 weights per lane.  Row stride 132 floats
         // keeps the float4 stores of 8 consecutive rows on distinct banks.
         constexpr int kLd = BN + 4;
-        float *tile = (float *)smem;
+        float *stile = (float *)smem;
         for (int c = 0; c < BN / 16; c++) {
             float v[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v);
-            float4 *d = (float4 *)(tile + (warp * 32 + lane) * kLd + c * 16);
+            acc16(c, v);
+            float4 *d = (float4 *)(stile + (warp * 32 + lane) * kLd + c * 16);
 #pragma unroll
             for (int k = 0; k < 4; k++) d[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
         }
@@ -419,27 +468,49 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         const int ti = *e.adam_t + 1;
         const float t = (float)ti, lr = sched_lr(e.lr, e.sched, ti);
         const float c1 = 1.f / (1.f - powf(e.b1, t)), c2 = 1.f / (1.f - powf(e.b2, t));
+        // Each warp takes kAdamRows rows at a time and issues all their master
+        // and moment loads before it computes, so that 3 kAdamRows float4
+        // loads per lane are in flight (one row at a time left the epilogue
+        // waiting on memory latency: 4 warps per SM cannot cover it).  The
+        // fp32 state is streamed (evict-first): for the skip it is 257 MB,
+        // more than the L2, and would push the operands out.
+        constexpr int kWarpsG = kGemmThreads / 32, kAdamRows = 8;
         const int col = lane * 4, n = n0 + col;
-        for (int r = warp; r < BM; r += kGemmThreads / 32) {
-            const int m = m0 + r;
-            if (m >= e.M || n >= e.N) continue;
-            const float4 g = *(const float4 *)(tile + r * kLd + col);
-            const size_t i = (size_t)m * e.ldw + n;
-            float4 w = *(const float4 *)(e.Wm + i), am = *(const float4 *)(e.Am + i), av = *(const float4 *)(e.Av + i);
-            float *wp = &w.x, *mp = &am.x, *vp = &av.x;
-            const float *gp = &g.x;
-            __align__(8) bf16 wb[4];
+        for (int r0 = warp; r0 < BM; r0 += kAdamRows * kWarpsG) {
+            float4 g[kAdamRows], w[kAdamRows], am[kAdamRows], av[kAdamRows];
+            size_t idx[kAdamRows];
+            bool ok[kAdamRows];
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                mp[k] = e.b1 * mp[k] + (1.f - e.b1) * gp[k];
-                vp[k] = e.b2 * vp[k] + (1.f - e.b2) * gp[k] * gp[k];
-                wp[k] -= lr * (mp[k] * c1) / (sqrtf(vp[k] * c2) + e.eps);
-                wb[k] = __float2bfloat16_rn(wp[k]);
+            for (int u = 0; u < kAdamRows; u++) {
+                const int r = r0 + u * kWarpsG, m = m0 + r;
+                ok[u] = r < BM && m < e.M && n < e.N;
+                idx[u] = (size_t)m * e.ldw + n;
+                if (ok[u]) {
+                    g[u] = *(const float4 *)(stile + r * kLd + col);
+                    w[u] = __ldcs((const float4 *)(e.Wm + idx[u]));
+                    am[u] = __ldcs((const float4 *)(e.Am + idx[u]));
+                    av[u] = __ldcs((const float4 *)(e.Av + idx[u]));
+                }
             }
-            *(float4 *)(e.Wm + i) = w;
-            *(float4 *)(e.Am + i) = am;
-            *(float4 *)(e.Av + i) = av;
-            *(uint2 *)(e.Wb + (size_t)m * e.ldwb + n) = *(const uint2 *)wb;
+#pragma unroll
+            for (int u = 0; u < kAdamRows; u++) {
+                if (!ok[u]) continue;
+                const int m = m0 + r0 + u * kWarpsG;
+                float *wp = &w[u].x, *mp = &am[u].x, *vp = &av[u].x;
+                const float *gp = &g[u].x;
+                __align__(8) bf16 wb[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    mp[k] = e.b1 * mp[k] + (1.f - e.b1) * gp[k];
+                    vp[k] = e.b2 * vp[k] + (1.f - e.b2) * gp[k] * gp[k];
+                    wp[k] -= lr * (mp[k] * c1) / (sqrtf(vp[k] * c2) + e.eps);
+                    wb[k] = __float2bfloat16_rn(wp[k]);
+                }
+                __stcs((float4 *)(e.Wm + idx[u]), w[u]);
+                __stcs((float4 *)(e.Am + idx[u]), am[u]);
+                __stcs((float4 *)(e.Av + idx[u]), av[u]);
+                *(uint2 *)(e.Wb + (size_t)m * e.ldwb + n) = *(const uint2 *)wb;
+            }
         }
     } else {
         const int row = m0 + warp * 32 + lane;
@@ -449,7 +520,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             const int nb = n0 + c * 16;
             if (nb >= e.N) break;  // uniform across the CTA
             float v[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v);
+            acc16(c, v);
             if (!rv) continue;
             // N is a multiple of 8: two groups of 8 columns, vector accesses
 #pragma unroll
@@ -615,12 +686,26 @@ gbpf_status make_map(CUtensorMap *m, const void *base, int inner, long long rows
     return GBPF_OK;
 }
 
+// Split-K for GEMMs with fewer output tiles than SMs (the mini-batch GEMMs
+// of training, M = batch): S splits per tile with S x tiles <= SMs and at
+// least kSplitMinTiles k-tiles per split; only where the caller passes the
+// workspace (e.ws, e.ws_cnt: training, one stream).
+constexpr int kSplitMax = 8, kSplitMinTiles = 8;
 gbpf_status gemm2(cudaStream_t st, const CUtensorMap &ta, const CUtensorMap &tb, const CUtensorMap &ta2,
                   const CUtensorMap &tb2, int M, int N, int K, int K2, const EpiArgs &e) {
     EpiArgs x = e;
     x.M = M;
     x.N = N;
-    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
+    const int gx = (N + BN - 1) / BN, gy = (M + BM - 1) / BM, tiles = gx * gy;
+    const int nk = (K + BK - 1) / BK + (K2 + BK - 1) / BK;
+    int S = 1;
+    if (x.ws && x.ws_cnt) {
+        int dev = 0, sms = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        S = std::max(1, std::min({kSplitMax, sms / tiles, nk / kSplitMinTiles}));
+    }
+    dim3 grid(gx, gy, S);
     k_gemm<<<grid, kGemmThreads, kGemmSmem, st>>>(ta, tb, ta2, tb2, K, K2, x);
     CK(cudaGetLastError());
     return GBPF_OK;
@@ -689,6 +774,11 @@ struct gbpf_mlp {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     std::vector<Layer> L;
     Dev params, norm, misc;
+    // split-K workspace of the training GEMMs: one 128 x 128 fp32 partial per
+    // CTA (at most one CTA per SM splits) and one arrival counter per tile
+    Dev splitk;
+    float *ws = nullptr;
+    int *ws_cnt = nullptr;
     std::vector<float> in_mean, in_iscale, out_mean, out_scale;  // host copies
     float *d_in_mean = nullptr, *d_in_iscale = nullptr, *d_out_mean = nullptr, *d_out_scale = nullptr;
     int *d_t = nullptr, *d_err = nullptr;
@@ -802,6 +892,15 @@ gbpf_status gbpf_mlp::init(int n_in_, int hidden_, int n_hidden_, int n_out_, in
     if (st != GBPF_OK) return st;
     CK(cudaMalloc(&misc.p, 256));
     CK(cudaMemset(misc.p, 0, 256));
+    {
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        const size_t part = (size_t)BM * BN * sizeof(float);
+        CK(cudaMalloc(&splitk.p, (size_t)sms * part + 4 * (size_t)sms));
+        ws = (float *)splitk.p;
+        ws_cnt = (int *)((char *)splitk.p + (size_t)sms * part);
+        CK(cudaMemset(ws_cnt, 0, 4 * (size_t)sms));
+    }
     d_t = (int *)misc.p;
     d_err = d_t + 1;
     d_loss = (float *)(d_t + 2);
@@ -873,6 +972,7 @@ gbpf_status gbpf_mlp::forward(cudaStream_t st, Work &w, const CUtensorMap &mX, i
         EpiArgs e{};
         e.err = d_err;
         e.wait = wait_cycles;
+        if (train) { e.ws = ws; e.ws_cnt = ws_cnt; }
         e.bias = L[l].b;
         e.a_row0 = l == 0 ? x_row0 : 0;
         const CUtensorMap &ta = l == 0 ? mX : w.mH[l - 1];
@@ -913,6 +1013,8 @@ gbpf_status gbpf_mlp::forward(cudaStream_t st, Work &w, const CUtensorMap &mX, i
         EpiArgs e{};
         e.err = d_err;
         e.wait = wait_cycles;
+        e.ws = ws;
+        e.ws_cnt = ws_cnt;
         e.mode = EPI_PROJ;
         e.loss = d_loss;
         e.H = w.Rb; e.ldh = w.kp;
@@ -921,6 +1023,8 @@ gbpf_status gbpf_mlp::forward(cudaStream_t st, Work &w, const CUtensorMap &mX, i
         EpiArgs g{};
         g.err = d_err;
         g.wait = wait_cycles;
+        g.ws = ws;
+        g.ws_cnt = ws_cnt;
         g.mode = EPI_LOSS_GRAD;
         g.lam = lam;
         g.gscale = 2.f / ((float)M * (float)n_out);
@@ -946,6 +1050,8 @@ gbpf_status gbpf_mlp::backward(cudaStream_t st, Work &w, const CUtensorMap &mXT,
             EpiArgs e{};
             e.err = d_err;
             e.wait = wait_cycles;
+            e.ws = ws;
+            e.ws_cnt = ws_cnt;
             e.mode = EPI_BWD_HIDDEN;
             e.Z = w.Z[l - 1]; e.ldz = hidden;
             e.H = w.dZ[l - 1]; e.ldh = hidden;
@@ -955,6 +1061,8 @@ gbpf_status gbpf_mlp::backward(cudaStream_t st, Work &w, const CUtensorMap &mXT,
         EpiArgs e{};
         e.err = d_err;
         e.wait = wait_cycles;
+        e.ws = ws;
+        e.ws_cnt = ws_cnt;
         e.b_row0 = l == 0 ? xt_row0 : 0;
         if (adam) {
             e.mode = EPI_WGRAD_ADAM;
@@ -979,6 +1087,8 @@ gbpf_status gbpf_mlp::backward(cudaStream_t st, Work &w, const CUtensorMap &mXT,
         EpiArgs e{};
         e.err = d_err;
         e.wait = wait_cycles;
+        e.ws = ws;
+        e.ws_cnt = ws_cnt;
         e.b_row0 = xt_row0;
         if (adam) {
             e.mode = EPI_WGRAD_ADAM;
