@@ -75,8 +75,11 @@ struct Symbolic {
 };
 Symbolic analyse(const Grid &g, const YPattern &y, std::string *why);
 
-// Ordering used by analyse(): minimum degree on the bus graph.
+// Ordering used by analyse(): minimum degree on the bus graph, then the
+// perfect elimination order of its filled graph with the shortest elimination
+// tree (reduce_height: same fill, fewer levels).
 std::vector<int> min_degree_order(int n, const std::vector<std::vector<int>> &adj);
+std::vector<int> reduce_height(int n, const std::vector<std::vector<int>> &adj, const std::vector<int> &ord);
 
 // Control record of one single-grid solve in device memory, written by the
 // solver's graph kernels or by the one-instance batch launch below.

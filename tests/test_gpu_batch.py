@@ -483,3 +483,31 @@ def test_warp_state_in_global_memory_is_exact(gb, prec):
         for k in ("iterations", "status", "n_events", "V", "theta", "Pcalc", "Qcalc", "final_mismatch"):
             np.testing.assert_array_equal(r1[k], r0[k], err_msg=k)
         assert e1 == e0
+
+
+@pytest.mark.parametrize("workload,n", [("c2", 4096), ("c5", 1024)])
+def test_fp32_bench_scenarios_against_fp64(gb, workload, n):
+    """The bench's FP32-LU answers against batched FP64, scenario by scenario
+    (bench.fp64_check: both converge, same switch path -- bus, PV position and
+    code of every PV<->PQ switch -- and |V|, theta within 1e-6).  c2 (the
+    118-bus grid with reactive limits): at most 0.2 % of the FP64-converged
+    scenarios left out; c5 (1,888 buses, limits off): none.  The counted ones
+    are within 1e-7."""
+    import bench  # the repository root is on sys.path (conftest)
+    grid = gb.read_grid(bench.grid_file(bench.workload_files(workload)[0]))
+    draw = bench.scenarios if workload == "c2" else bench.c5_scenarios
+    Pl, Ql, Pg = (x.ravel() for x in draw(np, grid.buses(), n, bench.draw_seed(workload, 0)))
+    lim, maxit = (1, 100) if workload == "c2" else (0, 30)
+    res = {}
+    for prec in ("PREC_FP32_IR", "PREC_FP64"):
+        b = gb.Batch([grid], tolerancia=1e-8, no_max_iter=maxit, lim_inj_reat=lim, precision=getattr(gb, prec))
+        b.set_instances(np.zeros(n, np.int32), Pload=Pl, Qload=Ql, Pg=Pg)
+        b.solve()
+        res[prec] = (b, b.results(state=True))
+    (b32, r32), (b64, r64) = res["PREC_FP32_IR"], res["PREC_FP64"]
+    ok, rec = bench.fp64_check(np, b32, r32, b64, r64, b32.offsets)
+    assert rec["compared"] == n
+    left_out = rec["fp64_converged"] - rec["counted"]
+    assert left_out <= (0.002 * n if workload == "c2" else 0), rec
+    assert rec["max_abs_err_vs_fp64"]["V"] < 1e-7 and rec["max_abs_err_vs_fp64"]["theta"] < 1e-7, rec
+    assert np.all(r32["final_mismatch"][ok] <= 1e-8)
