@@ -74,11 +74,12 @@ WORKLOADS = ["c5", "c2", "c2-plain", "c2-dense", "c3", "c4", "c5-dense"]
 # command and the raw figures are in the named profiles/ summary).  A bench
 # line scales them by the instance-iterations of its own launch.
 TRAFFIC = {
-    # kernel family: (dram bytes, lts bytes, per instance-iteration; summary)
-    "k_nr_block<float": (1.950397e9 / 4207, 13.357179e9 / 4207,
-                         "profiles/k_nr_block_fp32_level3_c5_1024_bytes.md (level 3, 1,024 scenarios, flat start)"),
-    "k_nr_warp<float": (93.784e6 / 65671, 2.964886e9 / 65671,
-                        "profiles/k_nr_warp_fp32_level2_c2_16384_bytes.md (level 2, 16,384 scenarios)"),
+    # (workload, kernel family): (dram bytes, lts bytes, per instance-iteration; summary)
+    ("c5", "k_nr_block<float"): (1.950397e9 / 4207, 13.357179e9 / 4207,
+                                 "profiles/k_nr_block_fp32_level3_c5_1024_bytes.md (level 3, 1,024 scenarios, "
+                                 "flat start)"),
+    ("c2", "k_nr_warp<float"): (93.784e6 / 65671, 2.964886e9 / 65671,
+                                "profiles/k_nr_warp_fp32_level2_c2_16384_bytes.md (level 2, 16,384 scenarios)"),
 }
 
 
@@ -297,13 +298,13 @@ def bytes_per_iteration(sz, lu_value_bytes):
             + 32 * sz["dimJ"] + 4)
 
 
-def roofline(kernel, alg_bytes, kernel_s, inst_iters, pk, l2_gbs, note):
+def roofline(kernel, alg_bytes, kernel_s, inst_iters, pk, l2_gbs, note, workload=None):
     """The roofline object of a bench line: algorithmic bytes of one launch of
     the dominant kernel over its CUDA-event time, against the measured HBM
     peak and the L2 copy bandwidth measured in this run; DRAM and L2 traffic
     scaled from the kernel's small-case ncu capture where one exists."""
     achieved = alg_bytes / kernel_s / 1e9
-    tr = next((v for k, v in TRAFFIC.items() if kernel.startswith(k)), None)
+    tr = next((v for (w, k), v in TRAFFIC.items() if w == workload and kernel.startswith(k)), None)
     out = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": pk["hbm"], "unit": "GB/s",
            "frac": achieved / pk["hbm"], "peak_source": peak_src_note(pk["src"]),
            "traffic": tr[0] * inst_iters / 1e9 if tr else None, "traffic_unit": "GB per launch",
@@ -820,7 +821,7 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
         "roofline": roofline(kernel, alg, t_launch, int(kernel_its.sum()), pk, l2,
                              "dependent-latency bound: the per-instance state, factor and topology stay in shared "
                              "memory and L2, so the algorithmic bytes come from on-chip memory; DRAM carries the "
-                             "inputs and outputs"),
+                             "inputs and outputs", workload=a.workload),
         "clocks": clk.summary(),
         "gpu_launches": a.steps * launches_per_solve(pl_k),
     }
@@ -1017,7 +1018,7 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
                 "d2h_bytes_per_step": n_test * nB * 8 * 4 + n_test * 20},
         "roofline": roofline(kernel, alg, phases["newton"] / 1e3, inst_iters, pk, l2,
                              "one persistent Newton launch per step (restarts included), timed over its phase of "
-                             "the step; dependent-load latency bound"),
+                             "the step; dependent-load latency bound", workload="c5"),
         "roofline_training": {"bound": "tensor", "kernel": "k_gemm (tcgen05 bf16, all training GEMMs)",
                               "achieved": train_tflops, "peak": pk["bf16"], "unit": "TFLOP/s",
                               "frac": train_tflops / pk["bf16"],

@@ -550,7 +550,7 @@ __device__ __forceinline__ bool lu_pivots(const TopoView &G, int l, int lg, int 
         if (on && gl == 0) {
             const TJ det = D.x * D.w - D.y * D.z;
             sing |= (det == (TJ)0 || !isfinite(det));
-            const TJ rd = (TJ)1 / det;
+            const TJ rd = rcp_rn(det);
             B4 inv;
             inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
             dinv[j] = inv;  // the slot of D_j when dinv aliases the factor's diagonal
@@ -695,7 +695,7 @@ __device__ __forceinline__ bool lu_level1(const TopoView &G, int l, int lgp, int
             if (on && gl == 0) {
                 const TJ det = D.x * D.w - D.y * D.z;
                 sing |= (det == (TJ)0 || !isfinite(det));
-                const TJ rd = (TJ)1 / det;
+                const TJ rd = rcp_rn(det);
                 B4 inv;
                 inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
                 dinv[j] = inv;
@@ -3095,12 +3095,14 @@ gbpf_status gbpf::one_create(const Grid &g, const gbpf_options &o, int device, O
     gbpf_status st = gbpf_batch_create(&gp, 1, &o, device, &s->b);
     if (st != GBPF_OK) return st;
     gbpf_batch *b = s->b;
-    // one block, every per-bus array in shared memory, one-pass levels, no
-    // hand-off, iteration 0 from the shared copy when the start is the grid's
+    // one block, every per-bus array in shared memory, no hand-off, iteration
+    // 0 from the shared copy when the start is the grid's.  One-pass levels
+    // below 1,000 blocks, two-pass above (measured FP64: 118 buses 0.34 vs
+    // 0.38 ms one- vs two-pass; 1,888 buses 1.77 vs 1.61 ms)
     b->plan.warp_mode = 0;
     b->plan.handoff_it = 0;
     b->plan.gstate = 0;
-    b->plan.lu1 = 1;
+    b->plan.lu1 = g.nB - 1 < 1000 ? 1 : 0;
     b->plan.narrow = 0;
     b->plan.flat_shared = 1;
     const int gi = 0;

@@ -10,6 +10,12 @@ __host__ __device__ __forceinline__ blk4 mk4(double a, double b, double c, doubl
     return r;
 }
 
+// Correctly rounded reciprocal of a pivot block's determinant: the same value
+// as 1 / det (one real number, one rounding), by the reciprocal intrinsic
+// rather than a general division.
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
+
 // ------------------------------------------------------------------ helpers
 __device__ __forceinline__ blk4 mm(blk4 a, blk4 b) {  // 2x2 row-major product
     return mk4(a.x * b.x + a.y * b.z, a.x * b.y + a.y * b.w,

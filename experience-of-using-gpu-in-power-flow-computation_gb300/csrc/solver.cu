@@ -402,7 +402,7 @@ __device__ __forceinline__ typename SB<TJ>::b4 pivot_done(const Dev &d, int j, t
     // borderline limit switches, and the golden cases were checked with it).
     B4 inv;
     if constexpr (sizeof(TJ) == 8) {
-        const TJ rd = (TJ)1 / det;
+        const TJ rd = rcp_rn(det);
         inv.x = D.w * rd; inv.y = -D.y * rd; inv.z = -D.z * rd; inv.w = D.x * rd;
     } else {
         inv.x = D.w / det; inv.y = -D.y / det; inv.z = -D.z / det; inv.w = D.x / det;
