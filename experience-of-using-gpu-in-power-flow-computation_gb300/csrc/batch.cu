@@ -1468,9 +1468,13 @@ constexpr int kSelThreads = 256;
 constexpr int kOrderClasses = 64;
 __device__ __forceinline__ unsigned fabits(float x) { return __float_as_uint(x) & 0x7fffffffu; }
 __device__ __forceinline__ unsigned warp_umax32(unsigned v) { return __reduce_max_sync(0xffffffffu, v); }
+// SH: the phasors of the instance's two starts live in dynamic shared memory
+// (16 B per bus) for the row gathers; otherwise in ef (global).
+template <bool SH>
 __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *pred, int ldp, const float *omean,
                                                            const float *oscale, double *sV, double *sTh, float4 *ef,
                                                            int *kind, int *cls_out, int *hist) {
+    extern __shared__ float4 sel_ef[];
     __shared__ unsigned red[2][kSelThreads / 32];
     __shared__ float tred[2][kSelThreads / 32];
     const int inst = blockIdx.x, tid = threadIdx.x;
@@ -1479,7 +1483,7 @@ __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *
     const long long off = a.inst_off[inst];
     const int nB = T.nB;
     const float *pr = pred + (size_t)inst * ldp;
-    float4 *e = ef + off;
+    float4 *e = SH ? sel_ef : ef + off;
     const char *flat = (T.flat && a.flat_on && *a.flat_on) ? T.flat : nullptr;
     const FlatLayout F = flat_layout<float>(nB, T.n + 2 * T.nup);  // P, Q offsets do not depend on the precision
     float tlo = INFINITY, thi = -INFINITY;  // spread of the predicted angles
@@ -1505,8 +1509,8 @@ __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *
         if (ty == 3) continue;
         float ir = 0.f, ii = 0.f, jr = 0.f, ji = 0.f;
         for (int p = G.yptr[k]; p < G.yptr[k + 1]; p++) {
-            const double2 yd = G.yval[p];
-            const float yr = (float)yd.x, yi = (float)yd.y;
+            const float2 yf = G.yval32[p];  // the FP64 values rounded to FP32
+            const float yr = yf.x, yi = yf.y;
             const float4 u = e[G.ycol[p]];
             ir = fmaf(yr, u.x, fmaf(-yi, u.y, ir));
             ii = fmaf(yr, u.y, fmaf(yi, u.x, ii));
@@ -2475,8 +2479,22 @@ gbpf_status gbpf_batch::warm_launch(gbpf_mlp *m) {
     gbpf_status st = gbpf::mlp_infer(m, wX, n_inst, wPred, stream, mwork);
     if (st != GBPF_OK) return st;
     CK(cudaEventRecord(wev[0], stream));
-    k_ws_select<<<n_inst, kSelThreads, 0, stream>>>(args, wPred, sh.outp, sh.out_mean, sh.out_scale, wV, wTh, wEF,
-                                                     wKind, wCls, wHist);
+    {
+        // the two starts' phasors in shared memory when the largest grid's fit
+        size_t sel = 0;
+        for (const Topo &T : topo_h) sel = std::max(sel, 16 * (size_t)T.nB);
+        int optin = 0;
+        CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+        if (sel <= (size_t)optin) {
+            if (sel > 48 * 1024)
+                CK(cudaFuncSetAttribute(k_ws_select<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sel));
+            k_ws_select<true><<<n_inst, kSelThreads, sel, stream>>>(args, wPred, sh.outp, sh.out_mean, sh.out_scale,
+                                                                    wV, wTh, wEF, wKind, wCls, wHist);
+        } else {
+            k_ws_select<false><<<n_inst, kSelThreads, 0, stream>>>(args, wPred, sh.outp, sh.out_mean, sh.out_scale,
+                                                                   wV, wTh, wEF, wKind, wCls, wHist);
+        }
+    }
     CK_LAUNCH();
     const int order_blocks = std::min((n_inst + 255) / 256, 1024);
     k_ws_order<<<order_blocks, 256, 0, stream>>>(wCls, wHist, wHist + kOrderClasses, n_inst, wQueue);

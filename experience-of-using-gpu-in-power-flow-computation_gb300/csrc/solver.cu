@@ -1118,10 +1118,13 @@ gbpf_status gbpf_solver::run(gbpf_result *r) {
         r->n_events = last.n_events;
         std::memcpy(&r->final_mismatch, &last.maxG, sizeof(double));
         int npq = 0;
-        // nPQlim = original PQ buses + PV buses at a limit (read back with the events)
-        std::vector<int> lq(g.nPV);
-        if (g.nPV) CK(cudaMemcpy(lq.data(), d.limQ, g.nPV * sizeof(int), cudaMemcpyDeviceToHost));
-        for (int v : lq) npq += v;
+        // nPQlim = original PQ buses + PV buses at a limit (read back only when a
+        // PV bus switched: every flag starts at 0)
+        if (g.nPV && last.n_events > 0) {
+            std::vector<int> lq(g.nPV);
+            CK(cudaMemcpy(lq.data(), d.limQ, g.nPV * sizeof(int), cudaMemcpyDeviceToHost));
+            for (int v : lq) npq += v;
+        }
         r->nPQlim = g.nPQ + npq;
     }
     return last.status == GBPF_OK ? GBPF_OK : (gbpf_status)last.status;
