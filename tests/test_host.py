@@ -209,3 +209,25 @@ def test_symbolic_analysis(gb, kind, kw):
     assert a["closed"] == 1
     assert a["forward_levels"] >= 1 and a["backward_levels"] >= 1
     assert a["factor_blocks"] >= (a["jacobian_blocks"] - a["blocks"]) // 2
+
+
+@pytest.mark.parametrize("name,blocks,levels", [("c2_base.cdf", 237, 21)])
+def test_height_reduced_ordering(gb, name, blocks, levels):
+    """The factor's ordering: minimum degree, then a perfect elimination order
+    of its filled graph with the shortest elimination tree.  On the 118-bus
+    grid: the minimum-degree fill (237 off-diagonal blocks, 145 update pairs)
+    in 21 levels instead of 30; the pattern stays closed under fill."""
+    a = gb.read_grid(os.path.join(GOLDEN, name)).analyse()
+    assert a["closed"] == 1
+    assert a["factor_blocks"] == blocks and a["update_pairs"] == 145
+    assert a["forward_levels"] == a["backward_levels"] == levels
+
+
+def test_height_reduction_on_the_tiled_grids(gb):
+    """1,888 and 15,104 buses: fewer levels than minimum degree alone (35 and
+    109) with no more factor blocks (4,253 and 36,872)."""
+    import bench
+    for f, lv, fb in (("c5_base.cdf.gz", 35, 4253), ("c3_base.cdfx.gz", 109, 36872)):
+        a = gb.read_grid(bench.grid_file(f)).analyse()
+        assert a["closed"] == 1
+        assert a["forward_levels"] < lv and a["factor_blocks"] <= fb, (f, a)
