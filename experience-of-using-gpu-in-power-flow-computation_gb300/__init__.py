@@ -408,8 +408,9 @@ class Solver:
         return t[:n.value].copy()
 
     def set_lu_launch(self, mode):
-        """gbpf_solver_set_lu_launch: 0 auto, 1 one kernel per level, 2 all
-        levels in one single-block kernel."""
+        """gbpf_solver_set_lu_launch: 0 auto, 1 one kernel per level (heavy
+        levels as pivots + entries), 2 all levels in one single-block kernel,
+        3 as 1 with heavy levels one block per step."""
         _check(lib().gbpf_solver_set_lu_launch(self.h, int(mode)), "gbpf_solver_set_lu_launch")
 
     def set_form(self, form):

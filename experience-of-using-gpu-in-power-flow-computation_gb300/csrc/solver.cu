@@ -72,6 +72,7 @@ struct Dev {
     const long long *og_ptr;
     const int *og_a, *og_b;
     const int *flev_steps, *blev_steps;
+    const int *fent_p, *fent_j;      // off-diagonal entries of each forward level, flat (k_factor_ent)
     const int *flev_ptr, *blev_ptr;  // level boundaries (k_lu_fused)
     int nfl, nbl;
     const int *ysl, *rbus, *cbus;
@@ -533,6 +534,79 @@ __global__ void __launch_bounds__(kFacBlk) k_factor_blk(Dev d, int beg, int guar
     }
 }
 
+// Levels with many entries per step (the top of the elimination tree of large
+// grids) in two launches instead of k_factor_blk's one: k_factor_piv computes
+// every pivot of the level (diagonal gather over a block, inverse, forward
+// value), then k_factor_ent takes every off-diagonal entry of the level -- U(j,i)
+// and the scaled L(i,j) of all its steps, flat -- one warp each across the
+// whole GPU, where k_factor_blk's block walked its step's entries eight at a
+// time.  Per entry the same lanes, pair order and reduction as k_factor_blk,
+// so the factor is the same.
+template <typename TJ>
+__global__ void __launch_bounds__(kFacBlk) k_factor_piv(Dev d, int beg, int guard) {
+    using B4 = typename SB<TJ>::b4;
+    using B2 = typename SB<TJ>::b2;
+    __shared__ B4 s_acc[kFacBlk / 32];
+    __shared__ B2 s_accy[kFacBlk / 32];
+    __shared__ int s_stop;
+    if (threadIdx.x == 0) s_stop = stopped(d, guard);
+    __syncthreads();
+    if (s_stop) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int j = d.flev_steps[beg + blockIdx.x];
+    B4 *fac = fac_of<TJ>(d);
+    const B4 *Lv = fac + d.n, *Uv = fac + d.n + d.nup;
+    const B2 *ys = ys_of<TJ>(d);
+    B4 acc;
+    acc.x = acc.y = acc.z = acc.w = (TJ)0;
+    B2 accy;
+    accy.x = accy.y = (TJ)0;
+    for (int t = d.dg_ptr[j] + tid; t < d.dg_ptr[j + 1]; t += kFacBlk) {
+        const int a = d.dg_pos[t];
+        const B4 l = Lv[a];
+        acc = add4T(acc, mmT(l, Uv[a]));
+        const B2 v = mvT(l, ys[d.dg_k[t]]);
+        accy.x += v.x;
+        accy.y += v.y;
+    }
+    acc = xsum4(acc, 32);
+    accy = xsum2(accy, 32);
+    if (lane == 0) { s_acc[warp] = acc; s_accy[warp] = accy; }
+    __syncthreads();
+    if (tid == 0) {
+        for (int w = 1; w < kFacBlk / 32; w++) {
+            acc = add4T(acc, s_acc[w]);
+            accy.x += s_accy[w].x;
+            accy.y += s_accy[w].y;
+        }
+        (void)pivot_done<TJ>(d, j, acc, accy);
+    }
+}
+template <typename TJ>
+__global__ void k_factor_ent(Dev d, int ebeg, int ecnt, int guard) {
+    using B4 = typename SB<TJ>::b4;
+    if (stopped(d, guard)) return;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= ecnt) return;
+    const int p = d.fent_p[ebeg + w], j = d.fent_j[ebeg + w];
+    B4 *fac = fac_of<TJ>(d);
+    B4 *Lv = fac + d.n, *Uv = fac + d.n + d.nup;
+    B4 aL, aU;
+    aL.x = aL.y = aL.z = aL.w = (TJ)0;
+    aU = aL;
+    for (long long r = d.og_ptr[p] + lane; r < d.og_ptr[p + 1]; r += 32) {
+        const int a = d.og_a[r], b = d.og_b[r];
+        aL = add4T(aL, mmT(Lv[b], Uv[a]));
+        aU = add4T(aU, mmT(Lv[a], Uv[b]));
+    }
+    aL = xsum4(aL, 32);
+    aU = xsum4(aU, 32);
+    if (lane == 0) {
+        Uv[p] = sub4T(Uv[p], aU);
+        Lv[p] = mmT(sub4T(Lv[p], aL), dinv_of<TJ>(d)[j]);
+    }
+}
+
 // Backward row j on one warp: x_j = D_j^-1 (y_j - sum_i U(j,i) x_i).
 template <typename TJ>
 __device__ __forceinline__ void bsolve_step(const Dev &d, int j, int lane) {
@@ -748,8 +822,15 @@ struct gbpf_solver {
         }
         for (int l = 0; l < nfl(); l++) {
             const int beg = S.flev_ptr[l], cnt = S.flev_ptr[l + 1] - beg;
-            if (level_heavy[l]) k_factor_blk<TJ><<<cnt, kFacBlk, 0, stream>>>(d, beg, guard);
-            else k_factor<TJ><<<cdiv_int(cnt, W), T, 0, stream>>>(d, beg, cnt, guard);
+            const int ebeg = S.fent_ptr[l], ecnt = S.fent_ptr[l + 1] - ebeg;
+            if (level_heavy[l] && split_heavy) {
+                k_factor_piv<TJ><<<cnt, kFacBlk, 0, stream>>>(d, beg, guard);
+                if (ecnt) k_factor_ent<TJ><<<cdiv_int(ecnt, W), T, 0, stream>>>(d, ebeg, ecnt, guard);
+            } else if (level_heavy[l]) {
+                k_factor_blk<TJ><<<cnt, kFacBlk, 0, stream>>>(d, beg, guard);
+            } else {
+                k_factor<TJ><<<cdiv_int(cnt, W), T, 0, stream>>>(d, beg, cnt, guard);
+            }
         }
     }
     template <typename TJ> void launch_backward_t(int guard) {
@@ -761,6 +842,9 @@ struct gbpf_solver {
         }
     }
     std::vector<char> level_heavy;
+    // heavy levels as two launches (k_factor_piv + k_factor_ent) rather than
+    // k_factor_blk (gbpf_solver_set_lu_launch mode 3 / 1)
+    int split_heavy = 1;
     // metodo = denso: dense Jacobian, blocked LU with partial pivoting, the
     // triangular solves, update
     void launch_step_dense(int guard) {
@@ -899,6 +983,7 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
         d.dg_ptr = A.take<int>(n + 1); d.dg_pos = A.take<int>(nup + 1); d.dg_k = A.take<int>(nup + 1);
         d.og_ptr = A.take<long long>(nup + 1); d.og_a = A.take<int>(npairs + 1); d.og_b = A.take<int>(npairs + 1);
         d.flev_steps = A.take<int>(n); d.blev_steps = A.take<int>(n);
+        d.fent_p = A.take<int>(nup + 1); d.fent_j = A.take<int>(nup + 1);
         d.flev_ptr = A.take<int>(S.flev_ptr.size()); d.blev_ptr = A.take<int>(S.blev_ptr.size());
         d.ysl = A.take<int>(nq); d.rbus = A.take<int>(nq); d.cbus = A.take<int>(nq);
         d.fp32 = o.precision == GBPF_PREC_FP32_IR && !d.dense_rule;
@@ -969,6 +1054,10 @@ gbpf_status gbpf_solver::build(const Grid &grid, const gbpf_options &o, int dev)
     CK(up(d.og_a, S.og_a.data(), npairs * sizeof(int)));
     CK(up(d.og_b, S.og_b.data(), npairs * sizeof(int)));
     CK(up(d.flev_steps, S.flev_steps.data(), n * sizeof(int)));
+    if (nup) {
+        CK(up(d.fent_p, S.fent_p.data(), nup * sizeof(int)));
+        CK(up(d.fent_j, S.fent_j.data(), nup * sizeof(int)));
+    }
     CK(up(d.blev_steps, S.blev_steps.data(), n * sizeof(int)));
     CK(up(d.flev_ptr, S.flev_ptr.data(), S.flev_ptr.size() * sizeof(int)));
     CK(up(d.blev_ptr, S.blev_ptr.data(), S.blev_ptr.size() * sizeof(int)));
@@ -1098,7 +1187,10 @@ gbpf_status gbpf_solver::build_graph() {
     size_t nn = 0;
     CK(cudaGraphGetNodes(graph, nullptr, &nn));
     graph_nodes = (int)nn;
-    kernels_per_iter = (lu_fused ? 1 : nfl() + nbl()) + 3 + 3 + (opt.lim_inj_reat && g.nPV ? 1 : 0) + 1;
+    int split_levels = 0;
+    if (!lu_fused && split_heavy)
+        for (int l = 0; l < nfl(); l++) split_levels += level_heavy[l] && S.fent_ptr[l + 1] > S.fent_ptr[l];
+    kernels_per_iter = (lu_fused ? 1 : nfl() + nbl() + split_levels) + 3 + 3 + (opt.lim_inj_reat && g.nPV ? 1 : 0) + 1;
     if (d.dense_rule) {
         const int panels = (d.N + kDPanel - 1) / kDPanel;
         kernels_per_iter = 2 + 4 * panels - 2 + 2 + 3 + (opt.lim_inj_reat && g.nPV ? 1 : 0) + 1;
@@ -1246,13 +1338,15 @@ extern "C" gbpf_status gbpf_solver_flows(gbpf_solver *s, double *Pdp, double *Pp
 }
 
 extern "C" gbpf_status gbpf_solver_set_lu_launch(gbpf_solver *s, int mode) {
-    ARGCHECK(s && mode >= 0 && mode <= 2);
+    ARGCHECK(s && mode >= 0 && mode <= 3);
     if (s->d.dense_rule) { set_error("metodo = denso has no level-scheduled LU"); return GBPF_E_ARG; }
     CK(cudaSetDevice(s->device));
     CK(cudaStreamSynchronize(s->stream));
     const int fused = mode == 2 || (mode == 0 && s->S.n <= (s->d.fp32 ? kFusedMaxN32 : kFusedMaxN64));
-    if (fused == s->lu_fused) return GBPF_OK;
+    const int split = mode == 3 ? 0 : 1;
+    if (fused == s->lu_fused && split == s->split_heavy) return GBPF_OK;
     s->lu_fused = fused;
+    s->split_heavy = split;
     if (s->exec) { cudaGraphExecDestroy(s->exec); s->exec = nullptr; }
     if (s->graph) { cudaGraphDestroy(s->graph); s->graph = nullptr; }
     return s->build_graph();

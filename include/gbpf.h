@@ -249,11 +249,14 @@ gbpf_status gbpf_solver_flows(gbpf_solver *s, double *Pdp, double *Ppd, double *
 
 /* How the LU and triangular solves are launched inside the solve graph:
  * 1 = one kernel per elimination level (forward, with the LU step, then
- * backward); 2 = every level in one single-block kernel with a barrier
- * between levels (k_lu_fused: same per-step arithmetic, no per-level launch);
- * 0 = 2 up to 600 block rows (buses - 1) in the FP32-LU form and 150 in FP64,
- * else 1 (the default).  Rebuilds
- * the graph.  Not for metodo = denso. */
+ * backward), levels whose steps carry long gather lists as two kernels (the
+ * level's pivots, one block each, then all its off-diagonal entries, one warp
+ * each); 3 = as 1 but those levels as one kernel of one block per step (its
+ * entries walked by that block); 2 = every level in one single-block kernel
+ * with a barrier between levels (k_lu_fused: same per-step arithmetic, no
+ * per-level launch); 0 = 2 up to 600 block rows (buses - 1) in the FP32-LU
+ * form and 150 in FP64, else 1 (the default).  1 and 3 give the same factor.
+ * Rebuilds the graph.  Not for metodo = denso. */
 gbpf_status gbpf_solver_set_lu_launch(gbpf_solver *s, int mode);
 
 /* The form gbpf_solve runs (gbpf_form).  gbpf_solver_create picks

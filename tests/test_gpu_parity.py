@@ -338,3 +338,25 @@ def test_form_selection(gb):
     assert e.value.status == gb.E_UNSUPPORTED
     dense = gb.Solver(gb.read_grid(os.path.join(GOLDEN, "c1.cdf")), tolerancia=1e-8, no_max_iter=100, metodo=1)
     assert dense.form()["form"] == gb.FORM_GRAPH
+
+
+@pytest.mark.parametrize("precision", ["PREC_FP64", "PREC_FP32_IR"])
+@pytest.mark.parametrize("name,lim", [("c4_472.cdf.gz", 1), ("c3_base.cdfx.gz", 1)])
+def test_split_heavy_levels_equal_block_per_step(gb, precision, name, lim):
+    """The graph form's heavy elimination levels as two launches (pivots, then
+    every off-diagonal entry on its own warp) give the same factor as one
+    block per step walking its entries: bit-identical solves."""
+    import bench
+    grid = gb.read_grid(bench.grid_file(name))
+    out = []
+    for mode in (1, 3):
+        s = gb.Solver(grid, tolerancia=1e-8, no_max_iter=100, lim_inj_reat=lim, metodo=0,
+                      precision=getattr(gb, precision))
+        s.set_form(gb.FORM_GRAPH)
+        s.set_lu_launch(mode)
+        out.append(s.solve())
+        s.close()
+    a, b = out
+    assert a["converged"] and a["iterations"] == b["iterations"] and a["events"] == b["events"]
+    np.testing.assert_array_equal(a["V"], b["V"])
+    np.testing.assert_array_equal(a["theta"], b["theta"])
