@@ -49,7 +49,7 @@ EXPORTS = [
     "gbpf_batch_launch", "gbpf_batch_wait", "gbpf_batch_time_pipelined", "gbpf_batch_warm_phases",
     "gbpf_batch_solve_warm_launch", "gbpf_batch_solve_warm_wait", "gbpf_solver_set_lu_launch",
     "gbpf_batch_time_warm_pipelined", "gbpf_batch_events_all", "gbpf_mlp_set_wait_limit",
-    "gbpf_solver_set_form", "gbpf_solver_get_form",
+    "gbpf_solver_set_form", "gbpf_solver_get_form", "gbpf_batch_follow",
 ]
 
 
@@ -631,6 +631,11 @@ class Batch:
             self.h, len(gi), _p(gi), vp(V0), vp(theta0), vp(Pliq), vp(Qliq), vp(Qload), vp(V), vp(theta),
             vp(Pcalc), vp(Qcalc), vp(iterations), vp(status), vp(final_mismatch), vp(stream)),
             "gbpf_batch_solve_noalloc")
+
+    def follow(self, prev):
+        """gbpf_batch_follow: this batch's next warm-started solve starts on the
+        device after prev's last one has ended."""
+        _check(lib().gbpf_batch_follow(self.h, prev.h), "gbpf_batch_follow")
 
     def solve_warm_launch(self, mlp):
         """gbpf_batch_solve_warm_launch: the warm-started solve without
