@@ -302,6 +302,15 @@ def test_warm_start_in_flight_on_two_batches(gb, warm_net):
     assert gb.time_warm_pipelined(bs, m, 5) > 0
     for b, (w0, r0) in zip(bs, ref):
         np.testing.assert_array_equal(b.results()["V"], r0["V"])
+    # chained on the device (gbpf_batch_follow): the second starts when the
+    # first has ended, the host enqueues both before waiting; same answers
+    bs[0].solve_warm_launch(m)
+    bs[1].follow(bs[0])
+    bs[1].solve_warm_launch(m)
+    for b, (w0, r0) in zip(bs, ref):
+        w = b.solve_warm_wait()
+        np.testing.assert_array_equal(w["start_kind"], w0["start_kind"])
+        np.testing.assert_array_equal(b.results()["theta"], r0["theta"])
 
 
 def test_gemm_wait_limit_runs_out_and_the_handle_recovers(gb):
