@@ -841,6 +841,25 @@ def train_flops_per_step(nb, width, B, k_metric):
     return 2.0 * B * (fwd + metric + dh + dw)
 
 
+def fp64_check_c2(gb, np, dev, rank, n=N_SCEN_C2):
+    """The FP32-LU form against FP64 on the c2 draw (118-bus grid, reactive
+    limits on, n scenarios, default launch plans): fp64_check's record, with
+    the grid and count named."""
+    grid = gb.read_grid(grid_file("c2_base.cdf"))
+    Pl, Ql, Pg = (x.ravel() for x in scenarios(np, grid.buses(), n, draw_seed("c2", rank)))
+    res = []
+    for prec in (gb.PREC_FP32_IR, gb.PREC_FP64):
+        b = gb.Batch([grid], device=dev, precision=prec, tolerancia=1e-8, no_max_iter=100, lim_inj_reat=1)
+        b.set_instances(np.zeros(n, np.int32), Pload=Pl, Qload=Ql, Pg=Pg)
+        b.solve()
+        res.append((b, b.results(state=True)))
+    (b32, r32), (b64, r64) = res
+    _, rec = fp64_check(np, b32, r32, b64, r64, b32.offsets)
+    for b, _ in res:
+        b.close()
+    return {"grid": "c2_base.cdf (118 buses, reactive limits on)", **rec}
+
+
 def bench_c5(a, gb, np, rank, dev, world, dist):
     n_train = a.train or C5_TRAIN
     n_test = a.scenarios or C5_TEST
@@ -970,6 +989,10 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
     twin.close()
     # the plain FP64 form: one held-out scenario per gbpf_solve
     plain_rate, plain_info = plain_fp64_rate(gb, grid, dev, Pt, Qt, Gt, min(n_test, 128), 0, 30)
+    # the same FP32-LU form where PV buses switch (c5 has no reactive limits):
+    # the c2 draw (118-bus grid, limits on), FP32 against FP64 scenario by
+    # scenario, outside the timed region
+    check_lim = fp64_check_c2(gb, np, dev, rank)
     pk = peaks()
     l2 = l2_copy_gbs(dev)
     sz = path_sizes(grid)
@@ -993,7 +1016,7 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
                    "train_solves": n_train, "train_converged": int(ok.sum()),
                    "train_generation_s": t_gen, "train_s": train_ms / 1e3,
                    "train_loss_first_last": [float(loss[0]), float(loss[-1])],
-                   "converged_per_step": conv, "fp64_check": check,
+                   "converged_per_step": conv, "fp64_check": check, "fp64_check_with_reactive_limits": check_lim,
                    "in_flight": "2 batches of the same scenarios, one stream each, steps alternating, each step "
                                 "started on the device when the previous one ends (the host enqueues ahead); each "
                                 "step a full warm-started solve of every scenario",
