@@ -1709,6 +1709,13 @@ struct gbpf_batch {
     int max_iter = 100, lim = 0, ev_cap = 16;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // warm-started solves in flight on several batches: newton_done marks the
+    // end of this batch's last Newton launch; follow_ev (another batch's
+    // newton_done, set by gbpf_batch_follow) is waited for on the device just
+    // before this batch's next Newton launch, so that the features, network
+    // and start choice run beside the other batch's Newton tail but the two
+    // Newton launches never share the L2
+    cudaEvent_t newton_done = nullptr, follow_ev = nullptr;
     // learned warm start: events after the network and after the start
     // choice, and the last call's phase times (network, choice, Newton)
     cudaEvent_t wev[2] = {nullptr, nullptr};
@@ -1753,6 +1760,7 @@ struct gbpf_batch {
         if (graph) cudaGraphDestroy(graph);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (newton_done) cudaEventDestroy(newton_done);
         for (auto &e : wev) if (e) cudaEventDestroy(e);
         for (auto &e : pev) if (e) cudaEventDestroy(e);
         if (mwork) gbpf::mlp_work_free(mwork);
@@ -2512,7 +2520,12 @@ gbpf_status gbpf_batch::warm_launch(gbpf_mlp *m) {
         x->warm_max_dv = kWarmMaxDV;
     }
     (wa.queue_len ? wa.queue : ba.queue) = wQueue;
+    if (follow_ev) {
+        CK(cudaStreamWaitEvent(stream, follow_ev, 0));
+        follow_ev = nullptr;
+    }
     if ((st = launch_with(stream, ba, wa)) != GBPF_OK) return st;
+    CK(cudaEventRecord(newton_done, stream));
     CK(cudaMemcpyAsync(h_kind, wKind, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(h_witers, wIters, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
     CK(cudaEventRecord(ev1, stream));
@@ -2725,6 +2738,7 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
     CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&b->ev0));
     CK(cudaEventCreate(&b->ev1));
+    CK(cudaEventCreateWithFlags(&b->newton_done, cudaEventDisableTiming));
     for (auto &e : b->wev) CK(cudaEventCreate(&e));
     for (auto &e : b->pev) CK(cudaEventCreate(&e));
     CK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
@@ -3037,12 +3051,13 @@ extern "C" gbpf_status gbpf_batch_time_warm_pipelined(gbpf_batch *const *bs, int
     for (int k = 0; k < steps && st == GBPF_OK; k++) {
         gbpf_batch *b = bs[k % n];
         if (b->warm_pending) st = b->warm_wait(nullptr, nullptr, nullptr);
-        // each step starts on the device when the previous one has ended: two
-        // Newton launches side by side would share the L2 that each one's
-        // per-block slices nearly fill (measured: 472-477 k solves/s side by
-        // side against 485 k one after the other on the 1,888-bus scenarios),
-        // while the host still enqueues ahead
-        if (st == GBPF_OK && k > 0 && n > 1) CK(cudaStreamWaitEvent(b->stream, bs[(k - 1) % n]->ev1, 0));
+        // each step's Newton launch starts on the device when the previous
+        // step's has ended: two Newton launches side by side would share the
+        // L2 that each one's per-block slices nearly fill (measured: 472-477 k
+        // solves/s side by side against 485 k one after the other on the
+        // 1,888-bus scenarios); its features, network and start choice still
+        // run beside the previous Newton launch's tail
+        if (st == GBPF_OK && k > 0 && n > 1) b->follow_ev = bs[(k - 1) % n]->newton_done;
         if (st == GBPF_OK) st = b->warm_launch(m);
     }
     float worst = 0;
@@ -3063,9 +3078,8 @@ extern "C" gbpf_status gbpf_batch_time_warm_pipelined(gbpf_batch *const *bs, int
 }
 
 extern "C" gbpf_status gbpf_batch_follow(gbpf_batch *b, const gbpf_batch *prev) {
-    ARGCHECK(b && prev && b->device == prev->device);
-    CK(cudaSetDevice(b->device));
-    CK(cudaStreamWaitEvent(b->stream, prev->ev1, 0));
+    ARGCHECK(b && prev && b != prev && b->device == prev->device);
+    b->follow_ev = prev->newton_done;
     return GBPF_OK;
 }
 
