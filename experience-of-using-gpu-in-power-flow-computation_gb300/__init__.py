@@ -633,9 +633,8 @@ class Batch:
             "gbpf_batch_solve_noalloc")
 
     def follow(self, prev):
-        """gbpf_batch_follow: the Newton launch of this batch's next
-        warm-started solve starts on the device after prev's last one has
-        ended (the network and start choice before it may overlap)."""
+        """gbpf_batch_follow: this batch's next warm-started solve starts on
+        the device after prev's last one has ended."""
         _check(lib().gbpf_batch_follow(self.h, prev.h), "gbpf_batch_follow")
 
     def solve_warm_launch(self, mlp):

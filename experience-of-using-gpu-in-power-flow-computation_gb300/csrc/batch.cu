@@ -1709,13 +1709,16 @@ struct gbpf_batch {
     int max_iter = 100, lim = 0, ev_cap = 16;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    // warm-started solves in flight on several batches: newton_done marks the
-    // end of this batch's last Newton launch; follow_ev (another batch's
-    // newton_done, set by gbpf_batch_follow) is waited for on the device just
-    // before this batch's next Newton launch, so that the features, network
-    // and start choice run beside the other batch's Newton tail but the two
-    // Newton launches never share the L2
-    cudaEvent_t newton_done = nullptr, follow_ev = nullptr;
+    // warm-started solves in flight on several batches: step_done marks the
+    // end of this batch's last warm-started solve (its result copies
+    // included); follow_ev (another batch's step_done, set by
+    // gbpf_batch_follow) is waited for on the device before this batch's next
+    // warm-started solve starts.  Chaining whole solves keeps two Newton
+    // launches from sharing the L2; letting the next solve's network and
+    // start choice run beside the previous Newton launch's tail was measured
+    // slower (466-467 k against 478 k solves/s one after the other on the
+    // 1,888-bus scenarios: they share the same L2)
+    cudaEvent_t step_done = nullptr, follow_ev = nullptr;
     // learned warm start: events after the network and after the start
     // choice, and the last call's phase times (network, choice, Newton)
     cudaEvent_t wev[2] = {nullptr, nullptr};
@@ -1760,7 +1763,7 @@ struct gbpf_batch {
         if (graph) cudaGraphDestroy(graph);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
-        if (newton_done) cudaEventDestroy(newton_done);
+        if (step_done) cudaEventDestroy(step_done);
         for (auto &e : wev) if (e) cudaEventDestroy(e);
         for (auto &e : pev) if (e) cudaEventDestroy(e);
         if (mwork) gbpf::mlp_work_free(mwork);
@@ -2479,6 +2482,10 @@ gbpf_status gbpf_batch::warm_launch(gbpf_mlp *m) {
         warm_n = n_inst;
     }
     if (!mwork) mwork = gbpf::mlp_work_create();
+    if (follow_ev) {
+        CK(cudaStreamWaitEvent(stream, follow_ev, 0));
+        follow_ev = nullptr;
+    }
     CK(cudaEventRecord(ev0, stream));
     CK(cudaMemsetAsync(wHist, 0, 8 * kOrderClasses, stream));
     k_ws_features<<<1024, 256, 0, stream>>>(args.Pliq, args.Qliq, args.V0, args.inst_off, n_inst, nB, sh.n_in, sh.kin,
@@ -2520,15 +2527,11 @@ gbpf_status gbpf_batch::warm_launch(gbpf_mlp *m) {
         x->warm_max_dv = kWarmMaxDV;
     }
     (wa.queue_len ? wa.queue : ba.queue) = wQueue;
-    if (follow_ev) {
-        CK(cudaStreamWaitEvent(stream, follow_ev, 0));
-        follow_ev = nullptr;
-    }
     if ((st = launch_with(stream, ba, wa)) != GBPF_OK) return st;
-    CK(cudaEventRecord(newton_done, stream));
     CK(cudaMemcpyAsync(h_kind, wKind, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(h_witers, wIters, 4 * (size_t)n_inst, cudaMemcpyDeviceToHost, stream));
     CK(cudaEventRecord(ev1, stream));
+    CK(cudaEventRecord(step_done, stream));
     warm_pending = true;
     return GBPF_OK;
 }
@@ -2738,7 +2741,7 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
     CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&b->ev0));
     CK(cudaEventCreate(&b->ev1));
-    CK(cudaEventCreateWithFlags(&b->newton_done, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&b->step_done, cudaEventDisableTiming));
     for (auto &e : b->wev) CK(cudaEventCreate(&e));
     for (auto &e : b->pev) CK(cudaEventCreate(&e));
     CK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
@@ -3051,13 +3054,12 @@ extern "C" gbpf_status gbpf_batch_time_warm_pipelined(gbpf_batch *const *bs, int
     for (int k = 0; k < steps && st == GBPF_OK; k++) {
         gbpf_batch *b = bs[k % n];
         if (b->warm_pending) st = b->warm_wait(nullptr, nullptr, nullptr);
-        // each step's Newton launch starts on the device when the previous
-        // step's has ended: two Newton launches side by side would share the
-        // L2 that each one's per-block slices nearly fill (measured: 472-477 k
-        // solves/s side by side against 485 k one after the other on the
-        // 1,888-bus scenarios); its features, network and start choice still
-        // run beside the previous Newton launch's tail
-        if (st == GBPF_OK && k > 0 && n > 1) b->follow_ev = bs[(k - 1) % n]->newton_done;
+        // each step starts on the device when the previous one has ended: two
+        // Newton launches side by side would share the L2 that each one's
+        // per-block slices nearly fill (measured: 472-477 k solves/s side by
+        // side against 485 k one after the other on the 1,888-bus
+        // scenarios); the host still enqueues ahead
+        if (st == GBPF_OK && k > 0 && n > 1) b->follow_ev = bs[(k - 1) % n]->step_done;
         if (st == GBPF_OK) st = b->warm_launch(m);
     }
     float worst = 0;
@@ -3079,7 +3081,7 @@ extern "C" gbpf_status gbpf_batch_time_warm_pipelined(gbpf_batch *const *bs, int
 
 extern "C" gbpf_status gbpf_batch_follow(gbpf_batch *b, const gbpf_batch *prev) {
     ARGCHECK(b && prev && b != prev && b->device == prev->device);
-    b->follow_ev = prev->newton_done;
+    b->follow_ev = prev->step_done;
     return GBPF_OK;
 }
 

@@ -564,12 +564,11 @@ gbpf_status gbpf_mlp_set_norm(gbpf_mlp *m, const float *in_mean, const float *in
 gbpf_status gbpf_batch_solve_warm(gbpf_batch *b, gbpf_mlp *m, int *start_kind, int *warm_iterations,
                                   double *ms);
 
-/* Order two batches' warm-started solves on the device: the Newton launch of
- * the next solve enqueued with gbpf_batch_solve_warm_launch on b starts when
- * prev's last warm-started Newton launch has ended (b's features, network
- * and start choice may run beside it), while the host goes on enqueueing.
- * For keeping two batches in flight without their Newton launches sharing the
- * GPU's L2 (no counterpart in the reference). */
+/* Order two batches' warm-started solves on the device: the next solve
+ * enqueued with gbpf_batch_solve_warm_launch on b starts when prev's last
+ * warm-started solve (its result copies included) has ended, while the host
+ * goes on enqueueing.  For keeping two batches in flight without their Newton
+ * launches sharing the GPU's L2 (no counterpart in the reference). */
 gbpf_status gbpf_batch_follow(gbpf_batch *b, const gbpf_batch *prev);
 
 /* gbpf_batch_solve_warm in two halves: _launch enqueues every step on the
@@ -585,7 +584,7 @@ gbpf_status gbpf_batch_solve_warm_wait(gbpf_batch *b, int *start_kind, int *warm
 /* Device ms of `steps` warm-started solves spread round-robin over n batches
  * (all on one device, none with a warm-started solve in flight), each on its
  * own stream; a batch is waited for before it is launched again, and each
- * solve's Newton launch starts after the previous one's (as
+ * solve starts on the device after the previous one has ended (as
  * gbpf_batch_follow), so the host enqueues ahead without two Newton launches
  * sharing the L2.  From a start event every stream waits for to the latest
  * stream's end. */
