@@ -298,6 +298,13 @@ def bytes_per_iteration(sz, lu_value_bytes):
             + 32 * sz["dimJ"] + 4)
 
 
+def chord_bytes_saved(sz, lu_value_bytes):
+    """Algorithmic bytes one chord iteration (iteration 0 of a predicted run:
+    the shared factor of the Jacobian at the network's mean output) does not
+    move: the Jacobian fill and the numeric LU of bytes_per_iteration."""
+    return 12 * sz["nnzJ"] + 16 * sz["nnzY"] + 32 * sz["nB"] + 2 * (lu_value_bytes + 4) * sz["nnzLU"]
+
+
 def roofline(kernel, alg_bytes, kernel_s, inst_iters, pk, l2_gbs, note, workload=None):
     """The roofline object of a bench line: algorithmic bytes of one launch of
     the dominant kernel over its CUDA-event time, against the measured HBM
@@ -999,7 +1006,10 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
     # the Newton launch processes every iteration of every instance, the
     # failed predicted runs included
     inst_iters = int(it_w.sum())
-    alg = float(bytes_per_iteration(sz, 4) * inst_iters)
+    # iteration 0 of each predicted run is a chord step on the shared factor
+    pred_it = np.where(kind == 1, rw["iterations"], np.where(kind == 2, w["warm_iterations"], 0))
+    chords = int((pred_it >= 1).sum())
+    alg = float(bytes_per_iteration(sz, 4) * inst_iters - chord_bytes_saved(sz, 4) * chords)
     kernel = f"k_nr_block<float, {fast.plan()['block_state_global']}>"
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -1009,7 +1019,9 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
                    "grids": workload_files("c5"),
                    "instances_per_gpu": n_test, "tolerance": 1e-8, "no_max_iter": 30,
                    "form": "batched, FP32 LU + FP64 mismatch/test/update, learned warm start with flat-start "
-                           "fallback (network inference, start choice and Newton inside the timed region)",
+                           "fallback; iteration 0 of a predicted run a chord step on the factor of the Jacobian "
+                           "at the network's mean output (network inference, start choice and Newton inside the "
+                           "timed region)",
                    "network": f"{3 * nB} -> 3 x {width} GELU -> {2 * nB} + linear skip, bf16 weights, fp32 "
                               f"accumulation; loss |e A|^2 + {lam} |e|^2 (A = S J0^T); Adam lr {lr0:g} cosine to "
                               f"1e-5, {epochs} epochs, batch {batch}",
@@ -1024,6 +1036,7 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
                                           / max_over_ranks(t_serial / 1e3, dist, dev),
                    "phases_ms": {k: round(v, 4) for k, v in phases.items()},
                    "ns_per_instance_iteration": phases["newton"] * 1e6 / inst_iters,
+                   "chord_iterations_per_step": chords,
                    "path_sizes": sz,
                    "plan": fast.plan(), "autotune": tune,
                    "mean_iterations_flat_fp32": float(r32["iterations"].mean()),

@@ -218,6 +218,11 @@ struct Args {
     const double *Vp, *thp;
     int warm_max_iter;
     double warm_max_dv;
+    // the warm start's reference iteration (FlatLayout, k_flat_start at the
+    // network's mean output; null: none): iteration 0 of a predicted run
+    // takes its factor -- a chord step with the Jacobian of the mean solution
+    // -- in place of the instance's own Jacobian and factorisation
+    const char *wref;
     // block kernel with its state in global memory (layout gs): the region of
     // block b starts at gstate + b * gstate_stride
     unsigned char *gstate;
@@ -837,8 +842,11 @@ __global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) 
             // iteration 0 from the grid's own start: the topology's shared copy
             const char *flat = (!from_park && !pred && T.flat && a.flat_on && *a.flat_on) ? T.flat : nullptr;
             const FlatLayout F = flat_layout<TJ>(nB, nq);
+            // iteration 0 from a predicted start: the reference factor, unless singular
+            const char *wref = (!from_park && pred && a.wref && !*(const int *)(a.wref + F.sing)) ? a.wref : nullptr;
             for (;;) {
                 const bool f0 = flat && s_it == 0;
+                const bool c0 = wref && s_it == 0;
                 if (f0) {
                     for (int k = tid; k < nB; k += kThreads) {
                         if (keep_cs) {
@@ -928,10 +936,12 @@ __global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) 
                 __syncthreads();
                 if (s_done) break;
                 const B4 *Ub = Uv, *Db = dinv;
-                if (f0) {
-                    // the shared factor of iteration 0: forward substitution alone
-                    const B4 *facS = (const B4 *)(flat + F.fac);
-                    if (*(const int *)(flat + F.sing)) {
+                if (f0 || c0) {
+                    // a shared factor (the grid's start, or the warm start's
+                    // reference): forward substitution alone
+                    const char *sb = f0 ? flat : wref;
+                    const B4 *facS = (const B4 *)(sb + F.fac);
+                    if (*(const int *)(sb + F.sing)) {
                         if (tid == 0) { s_status = GBPF_E_SINGULAR; s_done = 1; }
                         __syncthreads();
                         break;
@@ -1173,6 +1183,8 @@ __global__ void __launch_bounds__(32 * kWarpsMax, GS == 3 ? 2 : 1) k_nr_warp(Arg
             const bool pred = wk == 1;
             const int mi = pred ? a.warm_max_iter : a.max_iter;
             const char *flat = (!pred && T.flat && a.flat_on && *a.flat_on) ? T.flat : nullptr;
+            // iteration 0 from a predicted start: the reference factor, unless singular
+            const char *wref = (pred && a.wref && !*(const int *)(a.wref + F.sing)) ? a.wref : nullptr;
             const double *v0 = pred ? a.Vp : a.V0, *t0 = pred ? a.thp : a.th0;
             for (int k = lane; k < nB; k += 32) {
                 V[k] = v0[off + k];
@@ -1274,10 +1286,12 @@ __global__ void __launch_bounds__(32 * kWarpsMax, GS == 3 ? 2 : 1) k_nr_warp(Arg
                 if (mloc <= tol_bits) break;
                 if (it >= mi) { status = GBPF_E_NOCONV; break; }
                 const B4 *Ub = Uv, *Db = dinv;
-                if (f0) {
-                    // the shared factor: forward substitution alone
-                    const B4 *facS = (const B4 *)(flat + F.fac);
-                    if (*(const int *)(flat + F.sing)) { status = GBPF_E_SINGULAR; break; }
+                if (f0 || (wref && it == 0)) {
+                    // a shared factor (the grid's start, or the warm start's
+                    // reference): forward substitution alone
+                    const char *sb = f0 ? flat : wref;
+                    const B4 *facS = (const B4 *)(sb + F.fac);
+                    if (*(const int *)(sb + F.sing)) { status = GBPF_E_SINGULAR; break; }
                     for (int l = 0; l < T.nfl; l++) {
                         fwd_rows<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l] : 0, lane, facS + n, ys);
                         __syncwarp();
@@ -1752,6 +1766,14 @@ struct gbpf_batch {
     DevBuf dflt_off_d;
     int flat_flag = 0;                // host copy of the device flag behind Args::flat_on
     DevBuf flat_mem;                  // k_flat_start outputs, one FlatLayout per topology
+    // the warm start's reference iteration (Args::wref): k_flat_start at the
+    // network's mean output, with the PV set points and the slack angle of the
+    // grid; made again when the mean, the grid or the lane grouping changes
+    DevBuf wref_mem;
+    const char *wref = nullptr;
+    std::vector<float> wref_key;
+    std::vector<double> wref_h;  // the reference state uploaded: |V|, then theta
+    gbpf_status make_wref(const gbpf::MlpShape &sh, int t0);
     // gbpf_batch_solve_noalloc, per topology: shared memory of one instance
     // (whole state in shared memory) and the bytes of its factor slice
     std::vector<size_t> na_smem, na_stride;
@@ -2482,10 +2504,12 @@ gbpf_status gbpf_batch::warm_launch(gbpf_mlp *m) {
         warm_n = n_inst;
     }
     if (!mwork) mwork = gbpf::mlp_work_create();
+    gbpf_status st0;
     if (follow_ev) {
         CK(cudaStreamWaitEvent(stream, follow_ev, 0));
         follow_ev = nullptr;
     }
+    if ((st0 = make_wref(sh, t0)) != GBPF_OK) return st0;
     CK(cudaEventRecord(ev0, stream));
     CK(cudaMemsetAsync(wHist, 0, 8 * kOrderClasses, stream));
     k_ws_features<<<1024, 256, 0, stream>>>(args.Pliq, args.Qliq, args.V0, args.inst_off, n_inst, nB, sh.n_in, sh.kin,
@@ -2525,6 +2549,7 @@ gbpf_status gbpf_batch::warm_launch(gbpf_mlp *m) {
         x->thp = wTh;
         x->warm_max_iter = std::min(max_iter, kWarmMaxIter);
         x->warm_max_dv = kWarmMaxDV;
+        x->wref = wref;
     }
     (wa.queue_len ? wa.queue : ba.queue) = wQueue;
     if ((st = launch_with(stream, ba, wa)) != GBPF_OK) return st;
@@ -2533,6 +2558,48 @@ gbpf_status gbpf_batch::warm_launch(gbpf_mlp *m) {
     CK(cudaEventRecord(ev1, stream));
     CK(cudaEventRecord(step_done, stream));
     warm_pending = true;
+    return GBPF_OK;
+}
+
+gbpf_status gbpf_batch::make_wref(const gbpf::MlpShape &sh, int t0) {
+    std::vector<float> key(sh.h_out_mean, sh.h_out_mean + sh.n_out);
+    key.push_back((float)t0);
+    key.push_back((float)plan.warp_group);
+    if (key == wref_key) return GBPF_OK;
+    wref = nullptr;
+    wref_key.clear();
+    const Topo &T = topo_h[t0];
+    const Grid &g = grids[t0];
+    const bool fp32 = precision == GBPF_PREC_FP32_IR;
+    const int nq = T.n + 2 * T.nup;
+    const FlatLayout F = fp32 ? flat_layout<float>(T.nB, nq) : flat_layout<double>(T.nB, nq);
+    // k_flat_start's shared memory (y and the bus flags); past the opt-in
+    // limit the predicted runs factor their own iteration 0
+    const size_t fs = align_up((fp32 ? 8 : 16) * (size_t)T.n, 16) + (size_t)T.nB;
+    int maxsm = 0;
+    CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    if (fs <= (size_t)maxsm) {
+        wref_mem.reset();
+        CK(cudaMalloc(&wref_mem.p, F.total));
+        wref_h.assign(2 * (size_t)T.nB, 0.0);
+        for (int k = 0; k < T.nB; k++) {
+            const int ty = g.type[k];
+            wref_h[k] = (ty == 0 || ty == 1) ? (double)sh.h_out_mean[k] : g.V0[k];
+            wref_h[T.nB + k] = ty == 3 ? g.theta0[k] : (double)sh.h_out_mean[T.nB + k];
+        }
+        char *o = (char *)wref_mem.p;
+        CK(cudaMemcpyAsync(o + F.V0, wref_h.data(), 8 * (size_t)T.nB, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(o + F.th0, wref_h.data() + T.nB, 8 * (size_t)T.nB, cudaMemcpyHostToDevice, stream));
+        if (fs > 48 * 1024) {
+            if (fp32) CK(cudaFuncSetAttribute(k_flat_start<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs));
+            else CK(cudaFuncSetAttribute(k_flat_start<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs));
+        }
+        if (fp32) k_flat_start<float><<<1, 32, fs, stream>>>(T, o, plan.warp_group);
+        else k_flat_start<double><<<1, 32, fs, stream>>>(T, o, plan.warp_group);
+        CK_LAUNCH();
+        wref = o;
+    }
+    wref_key = key;
     return GBPF_OK;
 }
 

@@ -1134,6 +1134,7 @@ MlpShape mlp_shape(const gbpf_mlp *m) {
     MlpShape s;
     s.n_in = m->n_in; s.kin = m->kin; s.n_out = m->n_out; s.outp = m->outp; s.device = m->device;
     s.in_mean = m->d_in_mean; s.in_iscale = m->d_in_iscale; s.out_mean = m->d_out_mean; s.out_scale = m->d_out_scale;
+    s.h_out_mean = m->out_mean.data();
     return s;
 }
 

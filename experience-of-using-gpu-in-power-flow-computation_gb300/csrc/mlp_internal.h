@@ -15,6 +15,7 @@ struct MlpShape {
     int n_in, kin, n_out, outp, device;  // outp: n_out rounded up to a multiple of 8 (row length of out)
     const float *in_mean, *in_iscale;    // device [n_in]: x_norm = (x - mean) * iscale
     const float *out_mean, *out_scale;   // device [n_out]: y = y_norm * scale + mean
+    const float *h_out_mean;             // host copy of out_mean
 };
 MlpShape mlp_shape(const gbpf_mlp *m);
 

@@ -550,9 +550,13 @@ gbpf_status gbpf_mlp_set_norm(gbpf_mlp *m, const float *in_mean, const float *in
  * initial mismatch is smaller than that of the instance's own start
  * (V0/theta0 of gbpf_batch_set_instances, by default the flat start), else
  * from its own start.  Instances whose predicted start does not converge are
- * solved again from their own start, in the same launch.  Instances are
- * served in order of falling predicted angle spread (max - min theta of the
- * prediction), the most stressed scenarios first.  Results as for
+ * solved again from their own start, in the same launch.  Iteration 0 of a
+ * predicted run is a chord step: its Newton system is solved with the factor
+ * of the Jacobian at the network's mean output (out_mean, with the grid's PV
+ * set points and slack angle), factored once per network and grid, instead
+ * of the instance's own Jacobian; later iterations are full Newton steps.
+ * Instances are served in order of falling predicted angle spread (max - min
+ * theta of the prediction), the most stressed scenarios first.  Results as for
  * gbpf_batch_solve (gbpf_batch_results); an instance on its own start gets
  * no_max_iter iterations.  start_kind[i] (may be NULL): 0 own start chosen up
  * front, 1 predicted start converged, 2 predicted start failed (no

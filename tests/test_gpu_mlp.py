@@ -207,6 +207,50 @@ def test_warm_start_saves_iterations(gb, warm_net):
     assert it_warm < it_flat - 0.5, (it_warm, it_flat)
 
 
+def test_warm_start_iteration0_is_a_chord_step_at_the_mean_output(gb):
+    """Iteration 0 of a predicted run factors no Jacobian of its own: it solves
+    with the shared factor of the Jacobian at the network's mean output.  With
+    every weight zero the network predicts that mean for every scenario, so
+    the chord step is the Newton step from the predicted start: iterations,
+    status, |V| and theta equal those of a plain solve started from the same
+    state (the two factors differ in rounding only)."""
+    grid = gb.generate(2, 20261205)
+    base = grid.buses()
+    nB, n = grid.nB, 256
+    rng = np.random.default_rng(11)
+    b = gb.Batch([grid], precision=gb.PREC_FP64, tolerancia=1e-8, no_max_iter=30, lim_inj_reat=0)
+    Pl, Ql, Pg = _scenarios(base, n, rng)
+    gi = np.zeros(n, np.int32)
+    b.set_instances(gi, Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel())
+    b.solve()
+    r = b.results()
+    ok = r["status"] == 0
+    assert ok.mean() > 0.95
+    mV = r["V"].reshape(-1, nB)[ok].mean(0).astype(np.float32)
+    mt = r["theta"].reshape(-1, nB)[ok].mean(0).astype(np.float32)
+    m = gb.MLP(3 * nB, 2 * nB, width=64, n_layers=2, seed=1)
+    m.set_norm(np.zeros(3 * nB, np.float32), np.ones(3 * nB, np.float32), np.concatenate([mV, mt]),
+               np.ones(2 * nB, np.float32))
+    m.set_params([(np.zeros_like(W), None if c is None else np.zeros_like(c)) for W, c in m.params()])
+    w = b.solve_warm(m)
+    warm = b.results()
+    kind = w["start_kind"]
+    t = base["type"]
+    V0 = np.where(t >= 2, base["V0"], mV.astype(np.float64))
+    th0 = np.where(t == 3, base["theta0"], mt.astype(np.float64))
+    b.set_instances(gi, Pload=Pl.ravel(), Qload=Ql.ravel(), Pg=Pg.ravel(), V0=np.tile(V0, n), theta0=np.tile(th0, n))
+    b.solve()
+    plain = b.results()
+    b.close()
+    sel = kind == 1
+    assert sel.mean() > 0.9
+    assert np.array_equal(warm["iterations"][sel], plain["iterations"][sel])
+    assert np.array_equal(warm["status"][sel], plain["status"][sel])
+    rows = np.repeat(sel, nB)
+    assert np.max(np.abs(warm["V"][rows] - plain["V"][rows])) <= 1e-10
+    assert np.max(np.abs(warm["theta"][rows] - plain["theta"][rows])) <= 1e-10
+
+
 @pytest.mark.parametrize("prec", ["PREC_FP64", "PREC_FP32_IR"])
 def test_warm_start_own_start_runs_match_flat_start(gb, warm_net, prec):
     """Instances that run from their own start in a warm-started launch -- the
