@@ -30,7 +30,9 @@ Other workloads: c2 (the 118-bus config-2 grid, limits on, 32,768 load
 scenarios per step, batched FP32 LU from the flat start, four batches in
 flight), c2-plain (one FP64 solve of the 118-bus grid per step), c2-dense
 (metodo = denso), c3 (the 15,104-bus grid, one FP64 solve per step, and its
-FP32-LU form), c4 (4,096 instances of 14..472-bus grids), c5-dense.
+FP32-LU form), c4 (4,096 instances of 14..472-bus grids), c5-dense.  A
+default (c5) run on one GPU also benches c2, c4 and c3 after the headline and
+reports them under "secondary_workloads" (--no-secondary skips them).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c5]
   python bench.py --impl reference     the reference path restated in C
@@ -95,6 +97,8 @@ def args():
                    help="scenarios per step (c2: default 32768, c4: 4096; c5: held-out, default 8192); smaller cases "
                         "for profiler captures")
     p.add_argument("--train", type=int, default=0, help="c5 training solves (default 50000)")
+    p.add_argument("--no-secondary", action="store_true",
+                   help="workload c5: skip the c2, c4 and c3 summaries that follow the headline")
     p.add_argument("--no-autotune", action="store_true",
                    help="batched workloads: keep the default launch plan instead of the autotuner's")
     return p.parse_args()
@@ -1172,6 +1176,54 @@ def bench_single(a, gb, np, rank, dev, world, dist):
     return line
 
 
+SECONDARY = ("c2", "c4", "c3")
+
+
+def secondary_summaries(a, gb, np, rank, dev, world, dist):
+    """The other configurations, run after the headline in the same process
+    (N = 1 only) and reported inside its line: c2 (32,768 load scenarios of
+    the 118-bus grid with reactive limits, FP32 LU checked against FP64, its
+    plain FP64 form and the one-core oracle beside it), c4 (4,096 instances of
+    14..472-bus grids) and c3 (one 15,104-bus solve, FP64 and FP32 LU).  Each
+    is a full bench of its own (same timing rules and steps, at most 50);
+    one that fails is reported with its error instead of ending the run."""
+    import copy
+
+    out = {}
+    for wl in SECONDARY:
+        b = copy.copy(a)
+        b.workload = wl
+        b.steps = min(a.steps, 50)
+        b.warmup = max(3, min(a.warmup, 5))
+        b.scenarios = 0
+        b.no_cpu_baseline = wl != "c2"
+        try:
+            if wl in ("c2", "c4"):
+                ln = bench_batch(b, gb, np, rank, dev, world, dist)
+            else:
+                ln = bench_single(b, gb, np, rank, dev, world, dist)
+        except Exception as ex:  # reported, so that the headline line still prints
+            out[wl] = {"error": f"{type(ex).__name__}: {ex}"[:400]}
+            continue
+        cfg = ln["config"]
+        keep = ("form", "grid", "instances_per_gpu", "nB", "iterations", "mean_iterations", "max_iterations",
+                "converged_per_step", "plain_fp64_solves_per_s", "batched_fp64_solves_per_s",
+                "speedup_vs_plain_fp64", "ns_per_instance_iteration", "ms_per_iteration", "fp32_lu", "l2")
+        summ = {"value": ln["value"], "unit": ln["unit"], "ms_per_step": ln["ms_per_step"], "steps": ln["steps"],
+                "warmup": ln["warmup"], "dtype": ln["dtype"], "e2e": ln.get("e2e"), "clocks": ln.get("clocks"),
+                "gpu_launches": ln.get("gpu_launches"),
+                "config": {k: cfg[k] for k in keep if k in cfg}}
+        if "fp64_check" in cfg:
+            summ["config"]["fp64_check"] = cfg["fp64_check"]
+        rl = ln.get("roofline") or {}
+        summ["roofline"] = {k: rl.get(k) for k in ("bound", "kernel", "kernel_phase", "achieved", "peak", "unit",
+                                                   "frac") if k in rl}
+        if "cpu_baseline" in ln:
+            summ["cpu_baseline"] = ln["cpu_baseline"]
+        out[wl] = summ
+    return out
+
+
 def main():
     a = args()
     if a.impl == "reference":
@@ -1191,6 +1243,8 @@ def main():
         line = bench_batch(a, gb, np, rank, local_rank, world, dist)
     elif a.workload == "c5":
         line = bench_c5(a, gb, np, rank, local_rank, world, dist)
+        if world == 1 and not a.no_secondary and not a.scenarios and not a.train:
+            line["secondary_workloads"] = secondary_summaries(a, gb, np, rank, local_rank, world, dist)
     else:
         line = bench_single(a, gb, np, rank, local_rank, world, dist)
     if rank == 0:

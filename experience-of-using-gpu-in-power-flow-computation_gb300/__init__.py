@@ -49,7 +49,7 @@ EXPORTS = [
     "gbpf_batch_launch", "gbpf_batch_wait", "gbpf_batch_time_pipelined", "gbpf_batch_warm_phases",
     "gbpf_batch_solve_warm_launch", "gbpf_batch_solve_warm_wait", "gbpf_solver_set_lu_launch",
     "gbpf_batch_time_warm_pipelined", "gbpf_batch_events_all", "gbpf_mlp_set_wait_limit",
-    "gbpf_solver_set_form", "gbpf_solver_get_form", "gbpf_batch_follow",
+    "gbpf_solver_set_form", "gbpf_solver_get_form", "gbpf_batch_follow", "gbpf_solve_traced",
 ]
 
 
@@ -326,6 +326,23 @@ def device_info(device=0):
 
 
 # ---------------------------------------------------------------------- solver
+_PI, _PD = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+
+
+class _Trace(ctypes.Structure):
+    """gbpf_trace (include/gbpf.h): one stage record of gbpf_solve_traced."""
+    _fields_ = [("stage", ctypes.c_int), ("iteration", ctypes.c_int), ("nB", ctypes.c_int), ("nPV", ctypes.c_int),
+                ("nPQlim", ctypes.c_int), ("nPVlim", ctypes.c_int), ("done", ctypes.c_int),
+                ("converged", ctypes.c_int), ("max_g", ctypes.c_double), ("limit_check", ctypes.c_int),
+                ("n_events", ctypes.c_int), ("events", _PI), ("P", _PD), ("Q", _PD), ("V", _PD), ("theta", _PD),
+                ("QliqLim", _PD), ("limQ", _PI), ("pv_lim", _PI), ("pq_lim", _PI), ("n_g", ctypes.c_int),
+                ("g", _PD), ("nnzJ", ctypes.c_int), ("jrow", _PI), ("jcol", _PI), ("jval", _PD)]
+
+
+_TRACE_FN = ctypes.CFUNCTYPE(None, ctypes.POINTER(_Trace), ctypes.c_void_p)
+TRACE_EVAL, TRACE_JACOBIAN, TRACE_STEP, TRACE_UPDATE = 0, 1, 2, 3
+
+
 class Solver:
     """mNR on one GPU: device-resident Newton loop captured in a CUDA graph."""
 
@@ -367,6 +384,47 @@ class Solver:
             out["events"] = self.events()
             out["hist"] = self.history()
             out.update(self.flows())
+        return out
+
+    def solve_traced(self, fn=None):
+        """gbpf_solve_traced: the solve stage by stage (the graph form's kernels,
+        one host sync per stage).  Returns the result dict of solve() plus
+        "trace", one dict per stage record (gbpf_trace: stage, iteration,
+        P, Q, V, theta, QliqLim, limQ, pv_lim, pq_lim, g, J rows/cols/values,
+        events, ...); fn(record) is also called with each record when given."""
+        recs = []
+
+        def cb(tp, _user):
+            t = tp.contents
+            nB, nPV = t.nB, t.nPV
+            arr = lambda ptr, n, dt: np.ctypeslib.as_array(ptr, shape=(n,)).astype(dt) if n > 0 and ptr else \
+                np.zeros(0, dt)
+            rec = dict(stage=t.stage, iteration=t.iteration, nPQlim=t.nPQlim, nPVlim=t.nPVlim, done=t.done,
+                       converged=t.converged, max_g=t.max_g, limit_check=t.limit_check,
+                       events=[tuple(int(x) for x in arr(t.events, 4 * t.n_events, np.int32)[4 * i:4 * i + 4])
+                               for i in range(t.n_events)],
+                       P=arr(t.P, nB, np.float64), Q=arr(t.Q, nB, np.float64), V=arr(t.V, nB, np.float64),
+                       theta=arr(t.theta, nB, np.float64), QliqLim=arr(t.QliqLim, nB, np.float64),
+                       limQ=arr(t.limQ, nPV, np.int32), pv_lim=arr(t.pv_lim, t.nPVlim, np.int32),
+                       pq_lim=arr(t.pq_lim, t.nPQlim, np.int32), g=arr(t.g, t.n_g, np.float64),
+                       jrow=arr(t.jrow, t.nnzJ, np.int32), jcol=arr(t.jcol, t.nnzJ, np.int32),
+                       jval=arr(t.jval, t.nnzJ, np.float64))
+            recs.append(rec)
+            if fn is not None:
+                fn(rec)
+
+        c_cb = _TRACE_FN(cb)
+        r = _Result()
+        st = lib().gbpf_solve_traced(self.h, ctypes.byref(r), c_cb, None)
+        if st not in (OK, E_NOCONV, E_SINGULAR):
+            raise GbpfError(st, "gbpf_solve_traced")
+        out = dict(status=r.status, converged=bool(r.converged), iterations=r.iterations,
+                   n_events=r.n_events, nPQlim=r.nPQlim, final_mismatch=r.final_mismatch)
+        out.update(self.state())
+        out["events"] = self.events()
+        out["hist"] = self.history()
+        out.update(self.flows())
+        out["trace"] = recs
         return out
 
     def set_start(self, V0=None, theta0=None, Pliq=None, Qliq=None):

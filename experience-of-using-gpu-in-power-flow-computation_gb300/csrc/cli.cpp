@@ -143,6 +143,152 @@ static void print_report(const gbpf_options &o, const RunTimes &t) {
     std::printf("*****************************************\n");
 }
 
+// showVec (GPU/dim.h:11-37): '[' before the first value, one value a line, a
+// space before the others and ']' after the last, fixed with prec decimals.
+// An empty vector prints "[]" (the reference reads outside the array there).
+static void show_vec(const double *v, int n, int prec) {
+    if (n <= 0) { std::printf("[]\n"); return; }
+    std::printf("[%.*f\n", prec, v[0]);
+    for (int i = 1; i < n - 1; i++) std::printf(" %.*f\n", prec, v[i]);
+    std::printf(" %.*f]\n", prec, v[n - 1]);
+}
+static void show_vec(const int *v, int n) {
+    if (n <= 0) { std::printf("[]\n"); return; }
+    std::printf("[%d\n", v[0]);
+    for (int i = 1; i < n - 1; i++) std::printf(" %d\n", v[i]);
+    std::printf(" %d]\n", v[n - 1]);
+}
+
+static void print_events(const int *ev, int n) {  // chkLimQ, GPU/limiteInjReat.cuh:6-34
+    std::printf("\n");
+    for (int e = 0; e < n; e++)
+        std::printf("Barra %d [%d]: %s\n", ev[4 * e + 1], ev[4 * e + 2], EVENT_TEXT[ev[4 * e + 3]]);
+}
+
+// verbose_mode = ON: the dumps of mNR printed from gbpf_solve_traced's records,
+// in the reference's order (GPU/newtonRaphson.cuh:270-563, GPU/Jacobiano.cuh:
+// 216-220 and 382-410, GPU/PQcalc.cuh:304-320 and 417-432 for denso).
+struct Verbose {
+    const gbpf_options *o = nullptr;
+    std::vector<double> Qmin, Qmax;
+    std::vector<double> prevJ;  // the Jacobian value array as the last fill left it
+    bool started = false;
+};
+
+static void verbose_trace(const gbpf_trace *t, void *user) {
+    Verbose &vb = *(Verbose *)user;
+    const gbpf_options &o = *vb.o;
+    const int it = t->iteration, nB = t->nB;
+    const bool dense = o.metodo == GBPF_METODO_DENSO;
+    switch (t->stage) {
+    case GBPF_TRACE_EVAL: {
+        if (it >= o.no_max_iter) return;  // the loop has ended before this evaluation
+        if (!vb.started) {
+            vb.started = true;
+            if (o.lim_inj_reat) {  // printAlLim after initLim, GPU/limiteInjReat.cuh:226-242
+                std::printf("nPQlim = %d\nnPVlim = %d\n", t->nPQlim, t->nPVlim);
+                std::printf("limQ:\n");
+                show_vec(t->limQ, t->nPV);
+                std::printf("barrasPVlim:\n");
+                show_vec(t->pv_lim, t->nPVlim);
+                std::printf("barrasPQlim:\n");
+                show_vec(t->pq_lim, t->nPQlim);
+                std::printf("limQinf:\n");
+                show_vec(vb.Qmin.data(), t->nPV, 4);
+                std::printf("limQsup:\n");
+                show_vec(vb.Qmax.data(), t->nPV, 4);
+                std::printf("QliqLim:\n");
+                show_vec(t->QliqLim, nB, 4);
+            }
+        }
+        std::printf("\n****************************************************************** ITERACAO %d "
+                    "******************************************************************\n", it);
+        if (dense) {  // d_dnCalcPf_sha / d_dnCalcQf_sha print every bus
+            for (int k = 1; k <= nB; k++) std::printf("P_%d\t= %f\n", k, t->P[k - 1]);
+            for (int k = 1; k <= nB; k++) std::printf("Q_%d\t= %f\n", k, t->Q[k - 1]);
+        }
+        if (t->limit_check) {
+            print_events(t->events, t->n_events);
+            vb.prevJ.clear();  // a new stencil, its values zeroed (GPU/limiteInjReat.cuh:149-150)
+        }
+        std::printf("Pcalc^(%d) =\n", it);
+        show_vec(t->P, nB, 4);
+        std::printf("\nQcalc^(%d) =\n", it);
+        show_vec(t->Q, nB, 4);
+        std::printf("\ndeltaP^(%d) =\n", it);
+        show_vec(t->g, nB - 1, 4);
+        std::printf("\ndeltaQ^(%d) =\n", it);
+        show_vec(t->g + nB - 1, t->nPQlim, 4);
+        std::printf("\nlimQ:\n");
+        show_vec(t->limQ, t->nPV);
+        std::printf("\nbarrasPVlim:\n");
+        show_vec(t->pv_lim, t->nPVlim);
+        std::printf("\nbarrasPQlim:\n");
+        show_vec(t->pq_lim, t->nPQlim);
+        std::printf("\nlimQinf:\n");
+        show_vec(vb.Qmin.data(), t->nPV, 4);
+        std::printf("\nlimQsup:\n");
+        show_vec(vb.Qmax.data(), t->nPV, 4);
+        std::printf("\nQliqLim:\n");
+        show_vec(t->QliqLim, nB, 4);
+        std::printf("\nmax(g) = %e", t->max_g);
+        if (t->converged) std::printf("\n\nbreak!\nmax(g) = %e\n\n", t->max_g);
+        else if (!t->done) std::printf("     ...     continua:\n\n");
+        break;
+    }
+    case GBPF_TRACE_JACOBIAN: {
+        const int nnz = t->nnzJ, dim = t->n_g;
+        if (dense) {  // calcJacLim's JacobianoN, showMat (GPU/dim.h:157-167)
+            std::vector<double> A((size_t)dim * dim, 0.0);
+            for (int e = 0; e < nnz; e++) A[(size_t)t->jrow[e] * dim + t->jcol[e]] = t->jval[e];
+            std::printf("JacobianoN =\n\n[");
+            for (int r = 0; r < dim; r++) {
+                for (int c = 0; c < dim; c++) std::printf("%5.1f ", A[(size_t)r * dim + c]);
+                std::printf("\n ");
+            }
+            std::printf("]\n\n");
+        } else {
+            // SpCalcJac fills H, L, M, N in turn and prints the value array
+            // after the first three; entries not yet filled hold the last fill's
+            // values, or zero on a new stencil (GPU/limiteInjReat.cuh:86-87)
+            std::vector<double> cur(vb.prevJ.size() == (size_t)nnz ? vb.prevJ : std::vector<double>(nnz, 0.0));
+            const int np = nB - 1;
+            const char *name[3] = {"H", "L", "M"};
+            for (int part = 0; part < 3; part++) {
+                for (int e = 0; e < nnz; e++) {
+                    const bool prow = t->jrow[e] < np, pcol = t->jcol[e] < np;
+                    const bool in = part == 0 ? (prow && pcol) : part == 1 ? (!prow && !pcol) : (!prow && pcol);
+                    if (in) cur[e] = t->jval[e];
+                }
+                std::printf("%s^(%d) =\n", name[part], it);
+                show_vec(cur.data(), nnz, 5);
+            }
+            std::printf("J^(%d) =\n", it);
+            show_vec(t->jval, nnz, 5);
+            vb.prevJ.assign(t->jval, t->jval + nnz);
+        }
+        std::printf("V^(%d) = \n", it);
+        show_vec(t->V, nB, 5);
+        std::printf("theta^(%d) = \n", it);
+        show_vec(t->theta, nB, 5);
+        std::printf("deltaPQ = \n");
+        show_vec(t->g, t->n_g, 5);
+        break;
+    }
+    case GBPF_TRACE_STEP:
+        std::printf("\n (deltaX)g^(%d) = \n", it);
+        show_vec(t->g, t->n_g, 5);
+        break;
+    case GBPF_TRACE_UPDATE:
+        std::printf("V^(%d) = \n", it);
+        show_vec(t->V, nB, 6);
+        std::printf("theta^(%d) = \n", it);
+        show_vec(t->theta, nB, 6);
+        break;
+    default: break;
+    }
+}
+
 static int fail(const char *what, gbpf_status st) {
     std::fprintf(stderr, "gbpf: %s: %s (%s)\n", what, gbpf_status_str(st), gbpf_last_error());
     return 1;
@@ -218,8 +364,19 @@ int main(int argc, char **argv) {
     st = gbpf_solver_create(g, &o, 0, &s);
     if (st != GBPF_OK) return fail("solver setup", st);
     gbpf_result r{};
+    Verbose vb;
     auto t0 = clk::now();
-    st = gbpf_solve(s, &r);
+    if (o.verbose_mode) {
+        int dims[8];
+        gbpf_grid_dims(g, dims);
+        vb.o = &o;
+        vb.Qmin.resize(dims[2] + 1);
+        vb.Qmax.resize(dims[2] + 1);
+        gbpf_grid_pvpq(g, nullptr, vb.Qmin.data(), vb.Qmax.data(), nullptr, nullptr);
+        st = gbpf_solve_traced(s, &r, verbose_trace, &vb);
+    } else {
+        st = gbpf_solve(s, &r);
+    }
     tm.processo = ms_since(t0);
     if (st != GBPF_OK && st != GBPF_E_NOCONV) return fail("solve", st);
     {
@@ -246,13 +403,14 @@ int main(int argc, char **argv) {
     gbpf_solver_events(s, ev.data(), 4096, &ne);
     const int last = r.converged ? r.iterations : std::min(r.iterations, o.no_max_iter) - 1;
     int e = 0;
-    for (int it = 0; it <= last && it < nh; it++) {
+    for (int it = 0; it <= last && it < nh && !o.verbose_mode; it++) {  // verbose: printed as it ran
         if (it < nt && trig[it]) {
-            std::printf("\n");
-            for (; e < ne && ev[4 * e] == it; e++)
-                std::printf("Barra %d [%d]: %s\n", ev[4 * e + 1], ev[4 * e + 2], EVENT_TEXT[ev[4 * e + 3]]);
+            int e1 = e;
+            while (e1 < ne && ev[4 * e1] == it) e1++;
+            print_events(ev.data() + 4 * e, e1 - e);
+            e = e1;
         }
-        if (o.verbose_mode || (o.output_iter && !o.laconic_mode)) std::printf("\nmax(g) = %e", hist[it]);
+        if (o.output_iter && !o.laconic_mode) std::printf("\nmax(g) = %e", hist[it]);
     }
 
     if (!o.laconic_mode && o.output_ans) {  // impressao2, GPU/impressao.h:47-80

@@ -892,6 +892,7 @@ struct gbpf_solver {
     gbpf_status build_graph();
     gbpf_status build_persistent();
     gbpf_status run(gbpf_result *r);
+    gbpf_status finish(gbpf_result *r);
     cudaGraphExec_t active() const { return form == GBPF_FORM_PERSISTENT ? pexec : exec; }
 };
 
@@ -1201,6 +1202,12 @@ gbpf_status gbpf_solver::build_graph() {
 gbpf_status gbpf_solver::run(gbpf_result *r) {
     CK(cudaSetDevice(device));
     CK(cudaGraphLaunch(active(), stream));
+    return finish(r);
+}
+
+// Reads the control record of the solve just enqueued on the stream into
+// `last` and the caller's result.
+gbpf_status gbpf_solver::finish(gbpf_result *r) {
     CK(cudaMemcpyAsync(&last, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     if (r) {
@@ -1605,6 +1612,169 @@ extern "C" gbpf_status gbpf_newton_step(gbpf_solver *s, const double *V, const d
         if (qn[k] >= 0) dx[qn[k]] = x[j].y;
     }
     return GBPF_OK;
+}
+
+// The graph form's Newton loop driven from the host one stage at a time: the
+// same kernels (unguarded: the host decides when to stop, on the control
+// record k_control writes), the device state copied back after each stage
+// and handed to fn in the reference's numbering.  For verbose_mode dumps
+// (GPU/newtonRaphson.cuh:284-563), so the copies and syncs do not matter.
+extern "C" gbpf_status gbpf_solve_traced(gbpf_solver *s, gbpf_result *r, gbpf_trace_fn fn, void *user) {
+    ARGCHECK(s && fn);
+    CK(cudaSetDevice(s->device));
+    const Grid &g = s->g;
+    const Symbolic &S = s->S;
+    const Dev &d = s->d;
+    cudaStream_t st = s->stream;
+    const int T = 256, nB = g.nB, nPV = g.nPV, n = S.n, nq = n + 2 * S.nup;
+    const auto D2H = cudaMemcpyDeviceToHost;
+    std::vector<double> P(nB), Q(nB), V(nB), th(nB), QL(nB), gv(2 * (size_t)nB), jv;
+    std::vector<int> limQ(nPV + 1), pvl, pql, ev, jr, jc, pn, qn;
+    std::vector<double2> x(n);
+    std::vector<float2> x32(n);
+    std::vector<blk4> f(nq);
+    std::vector<float4> f32(nq);
+    Ctl c{};
+    int seen = 0, trig = 0;
+    gbpf_trace t{};
+    t.nB = nB;
+    t.nPV = nPV;
+    // state, limit flags and control record; the lists and numbering they imply
+    auto read_state = [&]() -> gbpf_status {
+        const size_t b = nB * sizeof(double);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(P.data(), d.P, b, D2H, st));
+        CK(cudaMemcpyAsync(Q.data(), d.Q, b, D2H, st));
+        CK(cudaMemcpyAsync(V.data(), d.V, b, D2H, st));
+        CK(cudaMemcpyAsync(th.data(), d.th, b, D2H, st));
+        CK(cudaMemcpyAsync(QL.data(), d.QliqLim, b, D2H, st));
+        if (nPV) CK(cudaMemcpyAsync(limQ.data(), d.limQ, nPV * sizeof(int), D2H, st));
+        CK(cudaMemcpyAsync(&c, d.ctl, sizeof(Ctl), D2H, st));
+        CK(cudaStreamSynchronize(st));
+        ref_numbering(s, limQ.data(), pn, qn);
+        pvl.clear();
+        pql.clear();
+        for (int i = 0; i < nPV; i++) if (!limQ[i]) pvl.push_back(g.pv[i]);
+        for (int k = 0; k < nB; k++) if (qn[k] >= 0) pql.push_back(k + 1);
+        t.iteration = c.it;
+        t.nPQlim = (int)pql.size();
+        t.nPVlim = (int)pvl.size();
+        t.n_g = nB - 1 + t.nPQlim;
+        t.P = P.data(); t.Q = Q.data(); t.V = V.data(); t.theta = th.data(); t.QliqLim = QL.data();
+        t.limQ = limQ.data(); t.pv_lim = pvl.data(); t.pq_lim = pql.data();
+        t.g = gv.data();
+        t.n_events = 0; t.events = nullptr; t.limit_check = 0;
+        t.nnzJ = 0; t.jrow = t.jcol = nullptr; t.jval = nullptr;
+        return GBPF_OK;
+    };
+    // a per-block pair vector (rhs, or the step) in the reference's numbering
+    auto to_ref = [&](const double2 *v) {
+        for (int j = 0; j < n; j++) {
+            const int k = S.bus_of_blk[j];
+            gv[pn[k]] = v[j].x;
+            if (qn[k] >= 0) gv[qn[k]] = v[j].y;
+        }
+    };
+    gbpf_status ret = GBPF_OK;
+    k_reset<<<cdiv_int(std::max(nB, d.hist_cap), T), T, 0, st>>>(d);
+    for (;;) {
+        // injections, limit check, mismatch, convergence test
+        s->launch_eval(0);
+        k_control<<<1, 1, 0, st>>>(d, cudaGraphConditionalHandle{}, 0);
+        if ((ret = read_state()) != GBPF_OK) return ret;
+        CK(cudaMemcpy(&trig, d.trig + std::min(c.it, d.hist_cap - 1), sizeof(int), D2H));
+        const int have = std::min(c.n_events, kEventCap);
+        ev.assign(4 * (size_t)std::max(have - seen, 0), 0);
+        if (have > seen) {
+            CK(cudaMemcpy(ev.data(), d.events + 4 * (size_t)seen, ev.size() * sizeof(int), D2H));
+            // appended in arbitrary order; chkLimQ prints them by PV position
+            std::vector<int> idx(have - seen), e2(ev.size());
+            for (size_t i = 0; i < idx.size(); i++) idx[i] = (int)i;
+            std::sort(idx.begin(), idx.end(), [&](int a, int b) { return ev[4 * a + 2] < ev[4 * b + 2]; });
+            for (size_t i = 0; i < idx.size(); i++) std::copy_n(&ev[4 * idx[i]], 4, &e2[4 * i]);
+            ev.swap(e2);
+        }
+        std::vector<double2> rhs(n);
+        CK(cudaMemcpy(rhs.data(), d.rhs, n * sizeof(double2), D2H));
+        to_ref(rhs.data());
+        t.stage = GBPF_TRACE_EVAL;
+        t.done = c.done;
+        t.converged = c.converged;
+        std::memcpy(&t.max_g, &c.maxG, sizeof(double));
+        t.limit_check = trig;
+        t.n_events = (int)(ev.size() / 4);
+        t.events = ev.data();
+        seen = std::max(seen, have);
+        fn(&t, user);
+        if (c.done) break;
+        // Jacobian (also in metodo = denso, whose dump is the same entries)
+        k_jfill<<<cdiv_int(nq, T), T, 0, st>>>(d, 0);
+        CK(cudaGetLastError());
+        if (d.fp32) {
+            CK(cudaMemcpyAsync(f32.data(), d.fac32, nq * sizeof(float4), D2H, st));
+            CK(cudaStreamSynchronize(st));
+            for (int q = 0; q < nq; q++) f[q] = mk4(f32[q].x, f32[q].y, f32[q].z, f32[q].w);
+        } else {
+            CK(cudaMemcpyAsync(f.data(), d.fac, nq * sizeof(blk4), D2H, st));
+            CK(cudaStreamSynchronize(st));
+        }
+        std::vector<std::pair<long long, double>> ent;
+        for (int q = 0; q < nq; q++) {
+            if (S.ysl[q] < 0) continue;
+            const int k = S.rbus[q], cb = S.cbus[q];
+            const double e[4] = {f[q].x, f[q].y, f[q].z, f[q].w};
+            const int rr[4] = {pn[k], pn[k], qn[k], qn[k]}, cc[4] = {pn[cb], qn[cb], pn[cb], qn[cb]};
+            for (int u = 0; u < 4; u++)
+                if (rr[u] >= 0 && cc[u] >= 0) ent.push_back({(long long)rr[u] * (nB + nB) + cc[u], e[u]});
+        }
+        std::sort(ent.begin(), ent.end(),
+                  [](const std::pair<long long, double> &a, const std::pair<long long, double> &b) {
+                      return a.first < b.first;
+                  });
+        jr.resize(ent.size());
+        jc.resize(ent.size());
+        jv.resize(ent.size());
+        for (size_t i = 0; i < ent.size(); i++) {
+            jr[i] = (int)(ent[i].first / (nB + nB));
+            jc[i] = (int)(ent[i].first % (nB + nB));
+            jv[i] = ent[i].second;
+        }
+        t.stage = GBPF_TRACE_JACOBIAN;
+        t.nnzJ = (int)ent.size();
+        t.jrow = jr.data(); t.jcol = jc.data(); t.jval = jv.data();
+        t.n_events = 0; t.events = nullptr;
+        fn(&t, user);
+        t.nnzJ = 0; t.jrow = t.jcol = nullptr; t.jval = nullptr;
+        // linear solve
+        if (d.dense_rule) {
+            s->launch_dense_fill(0);
+            s->launch_dense_lu(0);
+            s->launch_dense_solve(0);
+        } else {
+            s->launch_factor_solve(0);
+        }
+        CK(cudaGetLastError());
+        if (d.fp32) {
+            CK(cudaMemcpyAsync(x32.data(), d.xs32, n * sizeof(float2), D2H, st));
+        } else {
+            CK(cudaMemcpyAsync(x.data(), d.xs, n * sizeof(double2), D2H, st));
+        }
+        CK(cudaMemcpyAsync(&c, d.ctl, sizeof(Ctl), D2H, st));
+        CK(cudaStreamSynchronize(st));
+        if (c.done) break;  // a singular pivot ends the solve before the update, as in the graph
+        if (d.fp32) for (int j = 0; j < n; j++) x[j] = make_double2(x32[j].x, x32[j].y);
+        to_ref(x.data());
+        t.stage = GBPF_TRACE_STEP;
+        fn(&t, user);
+        // update
+        k_update<<<cdiv_int(n, T), T, 0, st>>>(d, 0);
+        if ((ret = read_state()) != GBPF_OK) return ret;
+        t.stage = GBPF_TRACE_UPDATE;
+        fn(&t, user);
+    }
+    if (g.nL) k_flows<<<cdiv_int(g.nL, T), T, 0, st>>>(d);
+    CK(cudaGetLastError());
+    return s->finish(r);
 }
 
 extern "C" const char *gbpf_last_error(void) { return gbpf::last_error().c_str(); }

@@ -247,6 +247,56 @@ gbpf_status gbpf_solver_triggers(gbpf_solver *s, int *trig, int cap, int *n);
  * GPU/PQcalc.cuh:523-557, computed on the device). */
 gbpf_status gbpf_solver_flows(gbpf_solver *s, double *Pdp, double *Ppd, double *Qdp, double *Qpd);
 
+/* Iteration trace: the intermediate values the reference prints when
+ * verbose_mode = ON (GPU/newtonRaphson.cuh:150-156,270-272,284-286,392-427,
+ * 433-450,539-563; GPU/Jacobiano.cuh:216-220,382-410).  One record per stage
+ * of each Newton iteration, in the order the reference's loop reaches them. */
+typedef enum {
+    GBPF_TRACE_EVAL = 0,     /* injections, the reactive-limit check (when its
+                              * trigger fired) and the mismatch, with the
+                              * convergence test's outcome */
+    GBPF_TRACE_JACOBIAN = 1, /* the Jacobian at the current state; g is still
+                              * the mismatch */
+    GBPF_TRACE_STEP = 2,     /* the Newton step: g holds dx */
+    GBPF_TRACE_UPDATE = 3    /* the state after the update */
+} gbpf_trace_stage;
+
+typedef struct {
+    int stage;                 /* gbpf_trace_stage */
+    int iteration;             /* iterPon.iteracao */
+    int nB, nPV, nPQlim, nPVlim;
+    int done, converged;       /* EVAL: the loop ends here / converged */
+    double max_g;              /* EVAL: max|g| */
+    int limit_check;           /* EVAL: 1 when chkLimQ ran in this iteration */
+    int n_events;              /* EVAL: switches of this iteration's check, */
+    const int *events;         /* 4 ints each as gbpf_solver_events */
+    const double *P, *Q;       /* [nB] injections at the current state */
+    const double *V, *theta;   /* [nB] the current state */
+    const double *QliqLim;     /* [nB] */
+    const int *limQ;           /* [nPV] 1 = PV bus held at a Q limit */
+    const int *pv_lim;         /* barrasPVlim [nPVlim], 1-based buses */
+    const int *pq_lim;         /* barrasPQlim [nPQlim], 1-based, ascending */
+    int n_g;                   /* nB - 1 + nPQlim */
+    const double *g;           /* EVAL, JACOBIAN: mismatch gLim; STEP: dx;
+                                * in the reference's numbering (P rows of the
+                                * non-slack buses in bus order, then Q rows in
+                                * barrasPQlim order) */
+    int nnzJ;                  /* JACOBIAN: entries, in the reference's CSR */
+    const int *jrow, *jcol;    /* order (rows, then columns, ascending; */
+    const double *jval;        /* 0-based, same numbering as g) */
+} gbpf_trace;
+
+typedef void (*gbpf_trace_fn)(const gbpf_trace *t, void *user);
+
+/* A solve that stops after every stage of every iteration, copies the
+ * device state to host buffers and calls fn(record, user); the arrays are
+ * valid during the call only.  Runs the graph form's kernels one stage at a
+ * time (one host synchronisation per stage, for inspection, not speed), so
+ * iterations, switch events, state and flows are those of the graph form;
+ * gbpf_solver_state / _events / _history / _flows read its results
+ * afterwards.  Used by the gbpf driver for verbose_mode = ON. */
+gbpf_status gbpf_solve_traced(gbpf_solver *s, gbpf_result *r, gbpf_trace_fn fn, void *user);
+
 /* How the LU and triangular solves are launched inside the solve graph:
  * 1 = one kernel per elimination level (forward, with the LU step, then
  * backward), levels whose steps carry long gather lists as two kernels (the

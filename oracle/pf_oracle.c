@@ -907,7 +907,56 @@ static void push_event(orc_result *r, int it, int bus, int pvpos, int code) {
     r->n_events++;
 }
 
-int orc_solve(const orc_grid *g, const orc_opts *o, orc_result *r) {
+/* ------------------------------------------------------------------------- */
+/* verbose_mode dumps of mNR (GPU/newtonRaphson.cuh:150-156,270-272,284-286,   */
+/* 392-427,433-450,539-563; GPU/Jacobiano.cuh:216-220,382-410;                 */
+/* GPU/PQcalc.cuh:304-320,417-432) written to vf when it is not NULL.          */
+/* ------------------------------------------------------------------------- */
+static const char *EV_TEXT[6] = {"", "PV -> PQ (limite superior)", "PQ (limite inferior) -> PQ (limite superior)",
+                                 "PV -> PQ (limite inferior)", "PQ (limite superior) -> PQ (limite inferior)",
+                                 "PQ -> PV"};
+
+/* showVec, GPU/dim.h:11-37 (fixed, prec decimals); "[]" for an empty vector */
+static void vshow(FILE *f, const double *v, int n, int prec) {
+    if (n <= 0) { fputs("[]\n", f); return; }
+    fprintf(f, "[%.*f\n", prec, v[0]);
+    for (int i = 1; i < n - 1; i++) fprintf(f, " %.*f\n", prec, v[i]);
+    fprintf(f, " %.*f]\n", prec, v[n - 1]);
+}
+static void vshowi(FILE *f, const int *v, int n) {
+    if (n <= 0) { fputs("[]\n", f); return; }
+    fprintf(f, "[%d\n", v[0]);
+    for (int i = 1; i < n - 1; i++) fprintf(f, " %d\n", v[i]);
+    fprintf(f, " %d]\n", v[n - 1]);
+}
+
+/* the lists and limits block printed by printAlLim (GPU/limiteInjReat.cuh:226-242)
+ * and, with a leading blank line each, by mNR after the mismatch (:399-414) */
+static void vlists(FILE *f, const orc_grid *g, const int *limQ, const int *pvlim, int nPVlim, const int *pqlim,
+                   int nPQlim, const double *QliqLim, const char *sep) {
+    fprintf(f, "%slimQ:\n", sep);
+    vshowi(f, limQ, g->nPV);
+    fprintf(f, "%sbarrasPVlim:\n", sep);
+    vshowi(f, pvlim, nPVlim);
+    fprintf(f, "%sbarrasPQlim:\n", sep);
+    vshowi(f, pqlim, nPQlim);
+    fprintf(f, "%slimQinf:\n", sep);
+    vshow(f, g->Qmin, g->nPV, 4);
+    fprintf(f, "%slimQsup:\n", sep);
+    vshow(f, g->Qmax, g->nPV, 4);
+    fprintf(f, "%sQliqLim:\n", sep);
+    vshow(f, QliqLim, g->nB, 4);
+}
+
+static int solve_impl(const orc_grid *g, const orc_opts *o, orc_result *r, FILE *vf);
+
+int orc_solve(const orc_grid *g, const orc_opts *o, orc_result *r) { return solve_impl(g, o, r, NULL); }
+
+int orc_solve_verbose(const orc_grid *g, const orc_opts *o, orc_result *r, void *out) {
+    return solve_impl(g, o, r, (FILE *)out);
+}
+
+static int solve_impl(const orc_grid *g, const orc_opts *o, orc_result *r, FILE *vf) {
     memset(r, 0, sizeof(*r));
     int n = g->nB, nPV = g->nPV, nPQ = g->nPQ, s = g->slack - 1;
     orc_ybus y;
@@ -929,11 +978,27 @@ int orc_solve(const orc_grid *g, const orc_opts *o, orc_result *r) {
     r->hist = (double *)xcalloc(o->no_max_iter + 1, sizeof(double));
     int it, converged = 0, status = 0;
     double maxG = 0;
+    int *pvlim = (int *)xcalloc(nPV + 1, sizeof(int));
+    double *prevJ = NULL; /* the Jacobian value array as the last fill left it (NULL: a new, zeroed stencil) */
+    int prevN = 0;
+    memcpy(pvlim, g->barrasPV, nPV * sizeof(int));
+    if (vf && o->lim_inj_reat) {
+        fprintf(vf, "nPQlim = %d\nnPVlim = %d\n", nPQlim, nPVlim);
+        vlists(vf, g, limQ, pvlim, nPVlim, pqlim, nPQlim, QliqLim, "");
+    }
     for (it = 0; it < o->no_max_iter; it++) {
+        if (vf)
+            fprintf(vf, "\n****************************************************************** ITERACAO %d "
+                        "******************************************************************\n", it);
         orc_pq(&y, V, th, P, Q);
+        if (vf && g->dense_ybus) {
+            for (int k = 0; k < n; k++) fprintf(vf, "P_%d\t= %f\n", k + 1, P[k]);
+            for (int k = 0; k < n; k++) fprintf(vf, "Q_%d\t= %f\n", k + 1, Q[k]);
+        }
         /* limit trigger on the previous step, GPU/newtonRaphson.cuh:309-384 */
         if (it >= 1 && o->lim_inj_reat && maxi(dx, ngLim) < o->tol * 10.) {
             /* chkLimQ, GPU/limiteInjReat.cuh:5-40 */
+            int ev0 = r->n_events;
             for (int i = 0; i < nPV; i++) {
                 int b = g->barrasPV[i] - 1;
                 double qg = Q[b] + g->Qload[b];
@@ -964,6 +1029,15 @@ int orc_solve(const orc_grid *g, const orc_opts *o, orc_result *r) {
             while (a < nPQ) pqlim[c++] = g->barrasPQ[a++];
             nPQlim = c;
             ngLim = nPQlim + nPQlim + nPVlim;
+            c = 0;
+            for (int i = 0; i < nPV; i++) if (!limQ[i]) pvlim[c++] = g->barrasPV[i];
+            if (vf) {
+                fputs("\n", vf);
+                for (int e = ev0; e < r->n_events; e++)
+                    fprintf(vf, "Barra %d [%d]: %s\n", r->ev_bus[e], r->ev_pvpos[e], EV_TEXT[r->ev_code[e]]);
+            }
+            free(prevJ); /* Jstencil0based + d_attSparse: new stencil, values zeroed */
+            prevJ = NULL;
         }
         /* calcResPLim / calcResQLim, GPU/newtonRaphson.cuh:35-58 */
         int m = 0;
@@ -971,18 +1045,88 @@ int orc_solve(const orc_grid *g, const orc_opts *o, orc_result *r) {
         for (int i = 0; i < nPQlim; i++) { int b = pqlim[i] - 1; gl[m++] = QliqLim[b] - Q[b]; }
         maxG = maxi(gl, ngLim);
         r->hist[r->n_hist++] = maxG;
-        if (maxG <= o->tol) { converged = 1; break; } /* :421-426 */
+        if (vf) {
+            fprintf(vf, "Pcalc^(%d) =\n", it);
+            vshow(vf, P, n, 4);
+            fprintf(vf, "\nQcalc^(%d) =\n", it);
+            vshow(vf, Q, n, 4);
+            fprintf(vf, "\ndeltaP^(%d) =\n", it);
+            vshow(vf, gl, n - 1, 4);
+            fprintf(vf, "\ndeltaQ^(%d) =\n", it);
+            vshow(vf, gl + n - 1, nPQlim, 4);
+            vlists(vf, g, limQ, pvlim, nPVlim, pqlim, nPQlim, QliqLim, "\n");
+            fprintf(vf, "\nmax(g) = %e", maxG);
+        }
+        if (maxG <= o->tol) { /* :421-426 */
+            if (vf) fprintf(vf, "\n\nbreak!\nmax(g) = %e\n\n", maxG);
+            converged = 1;
+            break;
+        }
+        if (vf) fputs("     ...     continua:\n\n", vf);
         int dim, nnz, *rp, *cl;
         double *vl;
         orc_jacobian(g, &y, V, th, P, Q, pqlim, nPQlim, &dim, &nnz, &rp, &cl, &vl);
+        if (vf && g->dense_ybus) { /* calcJacLim's JacobianoN, showMat GPU/dim.h:157-167 */
+            fputs("JacobianoN =\n\n[", vf);
+            for (int i = 0; i < dim; i++) {
+                int p = rp[i];
+                for (int j = 0; j < dim; j++) {
+                    double a = 0;
+                    if (p < rp[i + 1] && cl[p] == j) a = vl[p++];
+                    fprintf(vf, "%5.1f ", a);
+                }
+                fputs("\n ", vf);
+            }
+            fputs("]\n\n", vf);
+        } else if (vf) { /* SpCalcJac: H, L, M filled in turn, the array printed after each */
+            double *cur = (double *)xcalloc(nnz + 1, sizeof(double));
+            if (prevJ && prevN == nnz) memcpy(cur, prevJ, nnz * sizeof(double));
+            const char *name[3] = {"H", "L", "M"};
+            for (int part = 0; part < 3; part++) {
+                for (int i = 0; i < dim; i++)
+                    for (int p = rp[i]; p < rp[i + 1]; p++) {
+                        int prow = i < n - 1, pcol = cl[p] < n - 1;
+                        if (part == 0 ? (prow && pcol) : part == 1 ? (!prow && !pcol) : (!prow && pcol)) cur[p] = vl[p];
+                    }
+                fprintf(vf, "%s^(%d) =\n", name[part], it);
+                vshow(vf, cur, nnz, 5);
+            }
+            free(cur);
+            fprintf(vf, "J^(%d) =\n", it);
+            vshow(vf, vl, nnz, 5);
+            free(prevJ);
+            prevJ = (double *)xcalloc(nnz + 1, sizeof(double));
+            memcpy(prevJ, vl, nnz * sizeof(double));
+            prevN = nnz;
+        }
+        if (vf) {
+            fprintf(vf, "V^(%d) = \n", it);
+            vshow(vf, V, n, 5);
+            fprintf(vf, "theta^(%d) = \n", it);
+            vshow(vf, th, n, 5);
+            fputs("deltaPQ = \n", vf);
+            vshow(vf, gl, ngLim, 5);
+        }
         status = orc_sparse_solve(dim, rp, cl, vl, gl, dx);
         free(rp); free(cl); free(vl);
         if (status) break;
+        if (vf) {
+            fprintf(vf, "\n (deltaX)g^(%d) = \n", it);
+            vshow(vf, dx, ngLim, 5);
+        }
         /* attOlim / attVlim, GPU/newtonRaphson.cuh:76-100 */
         m = 0;
         for (int k = 0; k < n; k++) if (k != s) th[k] += dx[m++];
         for (int i = 0; i < nPQlim; i++) V[pqlim[i] - 1] += dx[n - 1 + i];
+        if (vf) {
+            fprintf(vf, "V^(%d) = \n", it + 1);
+            vshow(vf, V, n, 6);
+            fprintf(vf, "theta^(%d) = \n", it + 1);
+            vshow(vf, th, n, 6);
+        }
     }
+    free(prevJ);
+    free(pvlim);
     if (!converged && !status) it = o->no_max_iter;
     r->status = status;
     r->converged = converged;

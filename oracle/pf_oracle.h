@@ -106,6 +106,12 @@ int orc_sparse_solve(int n, const int *rowptr, const int *col, const double *val
 /* Full NR solve with the reference GPU driver's control flow
  * (GPU/newtonRaphson.cuh:171-565). */
 int orc_solve(const orc_grid *g, const orc_opts *o, orc_result *r);
+/* The same solve, writing the reference's verbose_mode dumps to out (FILE *):
+ * printAlLim, the per-iteration banner, injections, mismatch, limit lists,
+ * max(g), the H/L/M/J value arrays (or the dense JacobianoN when
+ * g->dense_ybus), the state, the step and the updated state, in the order and
+ * format of GPU/newtonRaphson.cuh:270-563. */
+int orc_solve_verbose(const orc_grid *g, const orc_opts *o, orc_result *r, void *out);
 void orc_result_free(orc_result *r);
 
 /* Branch flows P/Q from->to and to->from (GPU/PQcalc.cuh:523-557). */

@@ -130,3 +130,40 @@ def test_reference_arm_runs_without_the_library(tmp_path):
     assert line["impl"] == "reference" and line["steps"] == 2 and line["warmup"] == 1
     assert line["cpu_baseline"]["kind"] == "port" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_secondary_summaries_report_each_workload_and_survive_a_failure(monkeypatch):
+    """The c5 line's secondary workloads: each benched with a copy of the
+    arguments (the same timed steps, at most 50; the one-core oracle only beside c2), a
+    summary of its line kept, and a failing one reported by its error while
+    the others still run."""
+    import argparse
+
+    import numpy as np
+
+    calls = []
+
+    def fake_line(b, *rest):
+        calls.append((b.workload, b.steps, b.no_cpu_baseline))
+        if b.workload == "c4":
+            raise RuntimeError("no device")
+        line = {"value": 2.0, "unit": "solves/s", "ms_per_step": 1.5, "steps": b.steps, "warmup": b.warmup,
+                "dtype": "f64", "e2e": {"value": 1.0}, "clocks": {}, "gpu_launches": 3,
+                "config": {"form": "batched", "fp64_check": {"counted": 7}, "unrelated": 1},
+                "roofline": {"bound": "hbm", "frac": 0.25, "traffic": 1}}
+        if not b.no_cpu_baseline:
+            line["cpu_baseline"] = {"value": 5.0}
+        return line
+
+    monkeypatch.setattr(bench, "bench_batch", fake_line)
+    monkeypatch.setattr(bench, "bench_single", fake_line)
+    a = argparse.Namespace(workload="c5", steps=20, warmup=3, scenarios=0, train=0, no_cpu_baseline=False,
+                           no_autotune=False, no_secondary=False, gpus=1, impl="gbpf")
+    out = bench.secondary_summaries(a, None, np, 0, 0, 1, None)
+    assert calls == [("c2", 20, False), ("c4", 20, True), ("c3", 20, True)]
+    assert a.workload == "c5" and a.steps == 20
+    assert out["c4"] == {"error": "RuntimeError: no device"}
+    assert out["c2"]["value"] == 2.0 and out["c2"]["cpu_baseline"] == {"value": 5.0}
+    assert out["c2"]["config"] == {"form": "batched", "fp64_check": {"counted": 7}}
+    assert out["c2"]["roofline"] == {"bound": "hbm", "frac": 0.25}
+    assert "cpu_baseline" not in out["c3"]
