@@ -17,9 +17,10 @@
 //   * all four warps read the accumulator back with tcgen05.ld (warp w owns
 //     TMEM lanes 32w..32w+31 = output rows) and run a fused epilogue.
 // Backward products need A^T or B^T; the epilogues that produce an operand
-// also write its transpose (coalesced: 32 lanes = 32 consecutive rows), and
-// the Adam epilogue refreshes both the bf16 weights and their transpose, so
-// no transpose kernel runs inside a step.
+// also write its transpose (coalesced: 32 lanes = 32 consecutive rows).  The
+// weight-gradient GEMMs store fp32 gradients; one streaming kernel (k_adam)
+// then updates every weight, and k_transpose_bf16 refreshes the transposed
+// bf16 copies of the hidden layers' weights.
 //
 // Every wait on an mbarrier is bounded.  The operand ring's waits take the
 // launch's limit (EpiArgs::wait, set per network by gbpf_mlp_set_wait_limit;
@@ -48,10 +49,9 @@ typedef __nv_bfloat16 bf16;
 namespace {
 
 // Three ring stages (96 KB + barriers) so that two CTAs share an SM: one
-// CTA's epilogue (the Adam read-modify-write of fp32 masters and moments,
-// memory-bound) overlaps the other's main loop, and a 240-tile GEMM runs in
-// one wave on 152 SMs (measured with four stages and one CTA per SM: the dS +
-// Adam GEMM at 17 % of HBM with the tensor pipe 5 % busy, waiting)
+// CTA's epilogue overlaps the other's main loop, and a 240-tile GEMM runs in
+// one wave on 152 SMs (measured with four stages and one CTA per SM: a GEMM
+// with a memory-bound epilogue at 17 % of HBM with the tensor pipe 5 % busy)
 constexpr int BM = 128, BN = 128, BK = 64, STAGES = 3, kGemmThreads = 128, kGemmCtasPerSm = 2;
 constexpr uint32_t kTileBytes = BM * BK * 2;          // 16 KB per operand tile
 constexpr uint32_t kStageBytes = 2 * kTileBytes;      // A + B
@@ -68,7 +68,6 @@ enum Epi : int {
     EPI_OUT_TRAIN = 1,   // y = acc + b; d = y - target; loss += d^2; H = d * gscale; HT = H^T
     EPI_OUT_INFER = 2,   // out = acc + b
     EPI_BWD_HIDDEN = 3,  // dz = acc * gelu'(Z); H = dz; HT = dz^T
-    EPI_WGRAD_ADAM = 4,  // Adam on (Wm, Am, Av) with g = acc; Wb = bf16(W) (Wt by k_transpose_bf16)
     EPI_WGRAD_STORE = 5, // out = acc (gradient, fp32)
     EPI_OUT_RESID = 6,   // e = acc + b - target; E32 = e; H = bf16(e); loss += lam e^2
     EPI_PROJ = 7,        // r = acc (= (e A)[m, n]); loss += r^2; H = bf16(r)
@@ -97,15 +96,6 @@ struct EpiArgs {
     int lde;
     float *out;
     int ldo;
-    float *Wm, *Am, *Av;
-    int ldw;
-    bf16 *Wb;
-    int ldwb;
-    bf16 *Wt;
-    int ldwt;
-    const int *adam_t;
-    const float *sched;   // learning-rate schedule {first step, steps, final lr}
-    float lr, b1, b2, eps;
     int *err;
     long long wait;       // limit of the operand-ring waits in clock cycles (0: kWaitCycles)
     // split-K (training GEMMs with few output tiles): gridDim.z CTAs share an
@@ -454,71 +444,6 @@ __global__ void __launch_bounds__(kGemmThreads, kGemmCtasPerSm)
     };
     if (*fail || (S > 1 && !s_last)) {
         // nothing more to do for this CTA
-    } else if (e.mode == EPI_WGRAD_ADAM) {
-        // Adam over the gradient tile, staged through shared memory (the
-        // operand ring is idle once the accumulator is complete) so that each
-        // warp then walks whole rows: float4 accesses to the fp32 master
-        // weights and moments, 4 bf16 weights per lane.  Row stride 132 floats
-        // keeps the float4 stores of 8 consecutive rows on distinct banks.
-        constexpr int kLd = BN + 4;
-        static_assert((size_t)BM * kLd * sizeof(float) <= (size_t)STAGES * kStageBytes,
-                      "the Adam staging tile must fit in the operand ring");
-        float *stile = (float *)smem;
-        for (int c = 0; c < BN / 16; c++) {
-            float v[16];
-            acc16(c, v);
-            float4 *d = (float4 *)(stile + (warp * 32 + lane) * kLd + c * 16);
-#pragma unroll
-            for (int k = 0; k < 4; k++) d[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
-        }
-        __syncthreads();
-        const int ti = *e.adam_t + 1;
-        const float t = (float)ti, lr = sched_lr(e.lr, e.sched, ti);
-        const float c1 = 1.f / (1.f - powf(e.b1, t)), c2 = 1.f / (1.f - powf(e.b2, t));
-        // Each warp takes kAdamRows rows at a time and issues all their master
-        // and moment loads before it computes, so that 3 kAdamRows float4
-        // loads per lane are in flight (one row at a time left the epilogue
-        // waiting on memory latency: 4 warps per SM cannot cover it).  The
-        // fp32 state is streamed (evict-first): for the skip it is 257 MB,
-        // more than the L2, and would push the operands out.
-        constexpr int kWarpsG = kGemmThreads / 32, kAdamRows = 8;
-        const int col = lane * 4, n = n0 + col;
-        for (int r0 = warp; r0 < BM; r0 += kAdamRows * kWarpsG) {
-            float4 g[kAdamRows], w[kAdamRows], am[kAdamRows], av[kAdamRows];
-            size_t idx[kAdamRows];
-            bool ok[kAdamRows];
-#pragma unroll
-            for (int u = 0; u < kAdamRows; u++) {
-                const int r = r0 + u * kWarpsG, m = m0 + r;
-                ok[u] = r < BM && m < e.M && n < e.N;
-                idx[u] = (size_t)m * e.ldw + n;
-                if (ok[u]) {
-                    g[u] = *(const float4 *)(stile + r * kLd + col);
-                    w[u] = __ldcs((const float4 *)(e.Wm + idx[u]));
-                    am[u] = __ldcs((const float4 *)(e.Am + idx[u]));
-                    av[u] = __ldcs((const float4 *)(e.Av + idx[u]));
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < kAdamRows; u++) {
-                if (!ok[u]) continue;
-                const int m = m0 + r0 + u * kWarpsG;
-                float *wp = &w[u].x, *mp = &am[u].x, *vp = &av[u].x;
-                const float *gp = &g[u].x;
-                __align__(8) bf16 wb[4];
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    mp[k] = e.b1 * mp[k] + (1.f - e.b1) * gp[k];
-                    vp[k] = e.b2 * vp[k] + (1.f - e.b2) * gp[k] * gp[k];
-                    wp[k] -= lr * (mp[k] * c1) / (sqrtf(vp[k] * c2) + e.eps);
-                    wb[k] = __float2bfloat16_rn(wp[k]);
-                }
-                __stcs((float4 *)(e.Wm + idx[u]), w[u]);
-                __stcs((float4 *)(e.Am + idx[u]), am[u]);
-                __stcs((float4 *)(e.Av + idx[u]), av[u]);
-                *(uint2 *)(e.Wb + (size_t)m * e.ldwb + n) = *(const uint2 *)wb;
-            }
-        }
     } else {
         const int row = m0 + warp * 32 + lane;
         const bool rv = row < e.M;
@@ -581,6 +506,68 @@ __global__ void k_bias(BiasJobs J, const int *adam_t, const float *sched, float 
     J.bm[j][r] = m;
     J.bv[j][r] = v;
     J.b[j][r] -= sched_lr(lr, sched, ti) * (m / (1.f - powf(b1, t))) / (sqrtf(v / (1.f - powf(b2, t))) + eps);
+}
+
+// Adam on every layer's weights in one streaming pass, after the
+// weight-gradient GEMMs stored their fp32 gradients: each weight's gradient,
+// master copy and two moments are read once and the master, moments and bf16
+// copy written once, four weights a thread and kAdamU groups of them in
+// flight (evict-first: 0.8 GB a step for the 1,888-bus network, more than the
+// L2).  In the GEMM's epilogue the same update ran tile by tile between main
+// loops and reached a third of the HBM bandwidth.
+struct AdamJobs {
+    const float *g[8];
+    float *W[8], *m[8], *v[8];
+    bf16 *Wb[8];
+    long long start[9];  // prefix over the jobs, in groups of four weights
+    int njobs;
+};
+constexpr int kAdamU = 4;
+
+__global__ void __launch_bounds__(256) k_adam(AdamJobs J, const int *adam_t, const float *sched, float lr, float b1,
+                                              float b2, float eps) {
+    const int ti = *adam_t + 1;
+    const float t = (float)ti, lrt = sched_lr(lr, sched, ti);
+    const float c1 = 1.f / (1.f - powf(b1, t)), c2 = 1.f / (1.f - powf(b2, t));
+    const long long total = J.start[J.njobs], stride = (long long)gridDim.x * blockDim.x;
+    for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < total; i0 += stride * kAdamU) {
+        float4 g[kAdamU], w[kAdamU], am[kAdamU], av[kAdamU];
+        int jb[kAdamU];
+        long long o[kAdamU];
+#pragma unroll
+        for (int u = 0; u < kAdamU; u++) {
+            const long long i = i0 + u * stride;
+            jb[u] = -1;
+            if (i >= total) continue;
+            int j = 0;
+            while (i >= J.start[j + 1]) j++;
+            jb[u] = j;
+            o[u] = 4 * (i - J.start[j]);
+            g[u] = __ldcs((const float4 *)(J.g[j] + o[u]));
+            w[u] = __ldcs((const float4 *)(J.W[j] + o[u]));
+            am[u] = __ldcs((const float4 *)(J.m[j] + o[u]));
+            av[u] = __ldcs((const float4 *)(J.v[j] + o[u]));
+        }
+#pragma unroll
+        for (int u = 0; u < kAdamU; u++) {
+            const int j = jb[u];
+            if (j < 0) continue;
+            float *wp = &w[u].x, *mp = &am[u].x, *vp = &av[u].x;
+            const float *gp = &g[u].x;
+            __align__(8) bf16 wb[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                mp[k] = b1 * mp[k] + (1.f - b1) * gp[k];
+                vp[k] = b2 * vp[k] + (1.f - b2) * gp[k] * gp[k];
+                wp[k] -= lrt * (mp[k] * c1) / (sqrtf(vp[k] * c2) + eps);
+                wb[k] = __float2bfloat16_rn(wp[k]);
+            }
+            __stcs((float4 *)(J.W[j] + o[u]), w[u]);
+            __stcs((float4 *)(J.m[j] + o[u]), am[u]);
+            __stcs((float4 *)(J.v[j] + o[u]), av[u]);
+            __stcs((uint2 *)(J.Wb[j] + o[u]), *(const uint2 *)wb);
+        }
+    }
 }
 
 __global__ void k_step(int *t) { *t += 1; }
@@ -1071,22 +1058,10 @@ gbpf_status gbpf_mlp::backward(cudaStream_t st, Work &w, const CUtensorMap &mXT,
         e.ws = ws;
         e.ws_cnt = ws_cnt;
         e.b_row0 = l == 0 ? xt_row0 : 0;
-        if (adam) {
-            e.mode = EPI_WGRAD_ADAM;
-            e.Wm = L[l].Wm; e.Am = L[l].Am; e.Av = L[l].Av; e.ldw = L[l].in;
-            e.Wb = L[l].Wb; e.ldwb = L[l].in; e.Wt = L[l].Wt; e.ldwt = L[l].out;
-            e.adam_t = d_t; e.sched = d_sched; e.lr = lr; e.b1 = b1; e.b2 = b2; e.eps = eps;
-        } else {
-            e.mode = EPI_WGRAD_STORE;
-            e.out = L[l].gW; e.ldo = L[l].in;
-        }
+        e.mode = EPI_WGRAD_STORE;
+        e.out = L[l].gW; e.ldo = L[l].in;
         const CUtensorMap &mIn = l == 0 ? mXT : w.mHT[l - 1];
         if ((s = gemm(st, mGT, mIn, L[l].out, L[l].in, M, e)) != GBPF_OK) return s;
-        if (adam) {
-            k_transpose_bf16<<<dim3((L[l].in + 31) / 32, (L[l].out + 31) / 32), dim3(32, 8), 0, st>>>(
-                L[l].Wb, L[l].out, L[l].in, L[l].Wt);
-            CK(cudaGetLastError());
-        }
     }
     if (has_skip) {
         // the skip's gradient dY^T X; its transpose is never needed
@@ -1097,16 +1072,33 @@ gbpf_status gbpf_mlp::backward(cudaStream_t st, Work &w, const CUtensorMap &mXT,
         e.ws = ws;
         e.ws_cnt = ws_cnt;
         e.b_row0 = xt_row0;
-        if (adam) {
-            e.mode = EPI_WGRAD_ADAM;
-            e.Wm = k.Wm; e.Am = k.Am; e.Av = k.Av; e.ldw = k.in;
-            e.Wb = k.Wb; e.ldwb = k.in; e.Wt = nullptr;
-            e.adam_t = d_t; e.sched = d_sched; e.lr = lr; e.b1 = b1; e.b2 = b2; e.eps = eps;
-        } else {
-            e.mode = EPI_WGRAD_STORE;
-            e.out = k.gW; e.ldo = k.in;
-        }
+        e.mode = EPI_WGRAD_STORE;
+        e.out = k.gW; e.ldo = k.in;
         if ((s = gemm(st, w.mdYT, mXT, k.out, k.in, M, e)) != GBPF_OK) return s;
+    }
+    if (adam) {
+        // every weight gradient is stored (and every input gradient that read
+        // the old transposed weights is done): Adam over all weights, then the
+        // transposed bf16 copies of the hidden layers' weights
+        AdamJobs A{};
+        A.njobs = nl + (has_skip ? 1 : 0);
+        A.start[0] = 0;
+        for (int j = 0; j < A.njobs; j++) {
+            Layer &y = L[j];
+            A.g[j] = y.gW; A.W[j] = y.Wm; A.m[j] = y.Am; A.v[j] = y.Av; A.Wb[j] = y.Wb;
+            A.start[j + 1] = A.start[j] + (long long)y.out * y.in / 4;
+        }
+        int dev_sm = 0;
+        CK(cudaDeviceGetAttribute(&dev_sm, cudaDevAttrMultiProcessorCount, device));
+        const long long groups = A.start[A.njobs];
+        const int blocks = (int)std::max(1LL, std::min<long long>(8LL * dev_sm, (groups + 255) / 256));
+        k_adam<<<blocks, 256, 0, st>>>(A, d_t, d_sched, lr, b1, b2, eps);
+        CK(cudaGetLastError());
+        for (int l = 0; l < nl; l++) {
+            k_transpose_bf16<<<dim3((L[l].in + 31) / 32, (L[l].out + 31) / 32), dim3(32, 8), 0, st>>>(
+                L[l].Wb, L[l].out, L[l].in, L[l].Wt);
+            CK(cudaGetLastError());
+        }
     }
     BiasJobs J{};
     J.njobs = nl;
