@@ -50,6 +50,7 @@ EXPORTS = [
     "gbpf_batch_solve_warm_launch", "gbpf_batch_solve_warm_wait", "gbpf_solver_set_lu_launch",
     "gbpf_batch_time_warm_pipelined", "gbpf_batch_events_all", "gbpf_mlp_set_wait_limit",
     "gbpf_solver_set_form", "gbpf_solver_get_form", "gbpf_batch_follow", "gbpf_solve_traced",
+    "gbpf_solver_set_plan",
 ]
 
 
@@ -470,6 +471,14 @@ class Solver:
         levels as pivots + entries), 2 all levels in one single-block kernel,
         3 as 1 with heavy levels one block per step."""
         _check(lib().gbpf_solver_set_lu_launch(self.h, int(mode)), "gbpf_solver_set_lu_launch")
+
+    def set_plan(self, lu1=-1, narrow=-1):
+        """gbpf_solver_set_plan: the persistent form's LU plan (lu1 one-pass
+        levels, narrow one-warp levels on warp 0); -1 keeps a knob.  Returns
+        the plan in force as a dict."""
+        out = np.zeros(2, np.int32)
+        _check(lib().gbpf_solver_set_plan(self.h, int(lu1), int(narrow), _p(out)), "gbpf_solver_set_plan")
+        return dict(lu1=int(out[0]), narrow=int(out[1]))
 
     def set_form(self, form):
         """gbpf_solver_set_form: FORM_GRAPH (per-phase kernels in a CUDA graph)

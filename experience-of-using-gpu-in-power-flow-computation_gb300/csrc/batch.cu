@@ -3252,4 +3252,22 @@ gbpf_status gbpf::one_record(OneSolve *s, void *stream, const OneIO &io) {
     return GBPF_OK;
 }
 
+gbpf_status gbpf::one_set_plan(OneSolve *s, int lu1, int narrow, int out[2]) {
+    gbpf_batch *b = s->b;
+    if (lu1 >= 0) b->plan.lu1 = lu1 ? 1 : 0;
+    if (narrow >= 0) b->plan.narrow = narrow ? 1 : 0;
+    if (lu1 >= 0 || narrow >= 0) {
+        // the launch arguments and the state layout follow the plan
+        CK(cudaSetDevice(b->device));
+        gbpf_status st = b->rebuild();
+        if (st != GBPF_OK) return st;
+        if (b->n_block_q != 1 || b->block_gs != 0 || b->grid_blocks != 1) {
+            set_error("one-instance solve: the plan's state does not fit one block's shared memory");
+            return GBPF_E_UNSUPPORTED;
+        }
+    }
+    if (out) { out[0] = b->plan.lu1; out[1] = b->plan.narrow; }
+    return GBPF_OK;
+}
+
 void gbpf::one_free(OneSolve *s) { delete s; }

@@ -118,6 +118,10 @@ struct OneIO {
 struct OneSolve;
 gbpf_status one_create(const Grid &g, const gbpf_options &o, int device, OneSolve **out);
 gbpf_status one_record(OneSolve *s, void *stream, const OneIO &io);
+// The launch's LU plan (lu1: one-pass levels; narrow: one-warp levels on warp
+// 0 alone); -1 keeps a knob.  out[0..1] = the plan in force.  Record again
+// afterwards.
+gbpf_status one_set_plan(OneSolve *s, int lu1, int narrow, int out[2]);
 void one_free(OneSolve *s);
 
 }  // namespace gbpf

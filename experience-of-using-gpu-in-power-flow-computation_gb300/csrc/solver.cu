@@ -891,6 +891,7 @@ struct gbpf_solver {
     gbpf_status build(const Grid &grid, const gbpf_options &o, int dev);
     gbpf_status build_graph();
     gbpf_status build_persistent();
+    gbpf_status record_persistent();
     gbpf_status run(gbpf_result *r);
     gbpf_status finish(gbpf_result *r);
     cudaGraphExec_t active() const { return form == GBPF_FORM_PERSISTENT ? pexec : exec; }
@@ -1120,6 +1121,15 @@ gbpf_status gbpf_solver::build_persistent() {
     if (st != GBPF_OK) return st;
     CK(cudaMalloc(&flat_on, sizeof(int)));
     CK(cudaMemcpy(flat_on, &flat_on_h, sizeof(int), cudaMemcpyHostToDevice));
+    return record_persistent();
+}
+
+// (Re)captures the persistent form's graph: the one-instance Newton launch on
+// this solver's arrays, then the branch flows.
+gbpf_status gbpf_solver::record_persistent() {
+    if (pexec) { cudaGraphExecDestroy(pexec); pexec = nullptr; }
+    if (pgraph) { cudaGraphDestroy(pgraph); pgraph = nullptr; }
+    gbpf_status st = GBPF_OK;
     gbpf::OneIO io{};
     io.V0 = d.V0; io.th0 = d.th0; io.Pliq = d.Pliq; io.Qliq = d.Qliq; io.Qload = d.Qload;
     io.V = d.V; io.th = d.th; io.P = d.P; io.Q = d.Q;
@@ -1370,6 +1380,20 @@ extern "C" gbpf_status gbpf_solver_set_form(gbpf_solver *s, int form) {
     CK(cudaStreamSynchronize(s->stream));
     s->form = form;
     return GBPF_OK;
+}
+
+extern "C" gbpf_status gbpf_solver_set_plan(gbpf_solver *s, int lu1, int narrow, int out[2]) {
+    ARGCHECK(s);
+    if (!s->one) {
+        set_error("this grid has no persistent form (metodo = denso, or its state does not fit one block's shared "
+                  "memory)");
+        return GBPF_E_UNSUPPORTED;
+    }
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    gbpf_status st = gbpf::one_set_plan(s->one, lu1, narrow, out);
+    if (st != GBPF_OK) return st;
+    return (lu1 >= 0 || narrow >= 0) ? s->record_persistent() : GBPF_OK;
 }
 
 extern "C" gbpf_status gbpf_solver_get_form(const gbpf_solver *s, int out[3]) {
