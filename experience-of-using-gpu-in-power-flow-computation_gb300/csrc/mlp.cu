@@ -515,11 +515,12 @@ __global__ void k_bias(BiasJobs J, const int *adam_t, const float *sched, float 
 // flight (evict-first: 0.8 GB a step for the 1,888-bus network, more than the
 // L2).  In the GEMM's epilogue the same update ran tile by tile between main
 // loops and reached a third of the HBM bandwidth.
+constexpr int kMaxAdamJobs = 9;  // up to 7 hidden layers + the output layer + the skip
 struct AdamJobs {
-    const float *g[8];
-    float *W[8], *m[8], *v[8];
-    bf16 *Wb[8];
-    long long start[9];  // prefix over the jobs, in groups of four weights
+    const float *g[kMaxAdamJobs];
+    float *W[kMaxAdamJobs], *m[kMaxAdamJobs], *v[kMaxAdamJobs];
+    bf16 *Wb[kMaxAdamJobs];
+    long long start[kMaxAdamJobs + 1];  // prefix over the jobs, in groups of four weights
     int njobs;
 };
 constexpr int kAdamU = 4;
@@ -1082,6 +1083,7 @@ gbpf_status gbpf_mlp::backward(cudaStream_t st, Work &w, const CUtensorMap &mXT,
         // transposed bf16 copies of the hidden layers' weights
         AdamJobs A{};
         A.njobs = nl + (has_skip ? 1 : 0);
+        if (A.njobs > kMaxAdamJobs) { set_error("too many layers for the Adam pass"); return GBPF_E_ARG; }
         A.start[0] = 0;
         for (int j = 0; j < A.njobs; j++) {
             Layer &y = L[j];
