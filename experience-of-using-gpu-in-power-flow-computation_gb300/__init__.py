@@ -472,13 +472,14 @@ class Solver:
         3 as 1 with heavy levels one block per step."""
         _check(lib().gbpf_solver_set_lu_launch(self.h, int(mode)), "gbpf_solver_set_lu_launch")
 
-    def set_plan(self, lu1=-1, narrow=-1):
+    def set_plan(self, lu1=-1, narrow=-1, quad=-1):
         """gbpf_solver_set_plan: the persistent form's LU plan (lu1 one-pass
-        levels, narrow one-warp levels on warp 0); -1 keeps a knob.  Returns
-        the plan in force as a dict."""
-        out = np.zeros(2, np.int32)
-        _check(lib().gbpf_solver_set_plan(self.h, int(lu1), int(narrow), _p(out)), "gbpf_solver_set_plan")
-        return dict(lu1=int(out[0]), narrow=int(out[1]))
+        levels, narrow one-warp levels on warp 0, quad FP64 blocks on four
+        lanes); -1 keeps a knob.  Returns the plan in force as a dict."""
+        out = np.zeros(3, np.int32)
+        _check(lib().gbpf_solver_set_plan(self.h, int(lu1), int(narrow), int(quad), _p(out)),
+               "gbpf_solver_set_plan")
+        return dict(lu1=int(out[0]), narrow=int(out[1]), quad=int(out[2]))
 
     def set_form(self, form):
         """gbpf_solver_set_form: FORM_GRAPH (per-phase kernels in a CUDA graph)

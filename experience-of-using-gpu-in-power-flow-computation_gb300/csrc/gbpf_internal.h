@@ -119,9 +119,10 @@ struct OneSolve;
 gbpf_status one_create(const Grid &g, const gbpf_options &o, int device, OneSolve **out);
 gbpf_status one_record(OneSolve *s, void *stream, const OneIO &io);
 // The launch's LU plan (lu1: one-pass levels; narrow: one-warp levels on warp
-// 0 alone); -1 keeps a knob.  out[0..1] = the plan in force.  Record again
+// 0 alone; quad: FP64 one-pass levels with a block's components on four
+// lanes); -1 keeps a knob.  out[0..2] = the plan in force.  Record again
 // afterwards.
-gbpf_status one_set_plan(OneSolve *s, int lu1, int narrow, int out[2]);
+gbpf_status one_set_plan(OneSolve *s, int lu1, int narrow, int quad, int out[3]);
 void one_free(OneSolve *s);
 
 }  // namespace gbpf

@@ -1382,7 +1382,7 @@ extern "C" gbpf_status gbpf_solver_set_form(gbpf_solver *s, int form) {
     return GBPF_OK;
 }
 
-extern "C" gbpf_status gbpf_solver_set_plan(gbpf_solver *s, int lu1, int narrow, int out[2]) {
+extern "C" gbpf_status gbpf_solver_set_plan(gbpf_solver *s, int lu1, int narrow, int quad, int out[3]) {
     ARGCHECK(s);
     if (!s->one) {
         set_error("this grid has no persistent form (metodo = denso, or its state does not fit one block's shared "
@@ -1391,9 +1391,9 @@ extern "C" gbpf_status gbpf_solver_set_plan(gbpf_solver *s, int lu1, int narrow,
     }
     CK(cudaSetDevice(s->device));
     CK(cudaStreamSynchronize(s->stream));
-    gbpf_status st = gbpf::one_set_plan(s->one, lu1, narrow, out);
+    gbpf_status st = gbpf::one_set_plan(s->one, lu1, narrow, quad, out);
     if (st != GBPF_OK) return st;
-    return (lu1 >= 0 || narrow >= 0) ? s->record_persistent() : GBPF_OK;
+    return (lu1 >= 0 || narrow >= 0 || quad >= 0) ? s->record_persistent() : GBPF_OK;
 }
 
 extern "C" gbpf_status gbpf_solver_get_form(const gbpf_solver *s, int out[3]) {

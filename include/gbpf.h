@@ -324,11 +324,13 @@ gbpf_status gbpf_solver_get_form(const gbpf_solver *s, int out[3]);
 /* The persistent form's LU plan: lu1 = 1 one-pass elimination levels (L kept
  * unscaled, so a level's entries need not wait for its pivots: one barrier a
  * level), 0 two-pass (pivots, then entries); narrow = 1 runs the levels
- * narrow enough for one warp on warp 0 alone with warp-level syncs.  -1 keeps
- * a knob (both -1: only reports).  out[0..1] (may be NULL) = the plan in
- * force.  Plans differ only in the order the LU sums its updates.  Rebuilds
- * the persistent graph; GBPF_E_UNSUPPORTED for a grid without that form. */
-gbpf_status gbpf_solver_set_plan(gbpf_solver *s, int lu1, int narrow, int out[2]);
+ * narrow enough for one warp on warp 0 alone with warp-level syncs; quad = 1
+ * (FP64, one-pass levels) spreads each 2x2 block's four components over four
+ * lanes, 0 keeps a block on one lane.  -1 keeps a knob (all -1: only
+ * reports).  out[0..2] (may be NULL) = lu1, narrow, quad in force.  Plans
+ * differ only in the order the LU sums its updates.  Rebuilds the persistent
+ * graph; GBPF_E_UNSUPPORTED for a grid without that form. */
+gbpf_status gbpf_solver_set_plan(gbpf_solver *s, int lu1, int narrow, int quad, int out[3]);
 
 /* Solver facts: info[0..7] = nB, n blocks (nB-1), factor blocks (off-diagonal
  * per triangle), update pairs, forward levels, backward levels, graph nodes,

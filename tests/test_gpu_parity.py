@@ -362,20 +362,22 @@ def test_split_heavy_levels_equal_block_per_step(gb, precision, name, lim):
     np.testing.assert_array_equal(a["theta"], b["theta"])
 
 
-@pytest.mark.parametrize("plan", [(1, 0), (1, 1), (0, 0), (0, 1)], ids=lambda p: f"lu1={p[0]},narrow={p[1]}")
+@pytest.mark.parametrize("plan", [(1, 0, 1), (1, 0, 0), (1, 1, 1), (0, 0, 1), (0, 1, 0)],
+                         ids=lambda p: f"lu1={p[0]},narrow={p[1]},quad={p[2]}")
 @pytest.mark.parametrize("case", [c for c in committed_cases() + ieee_cases(max_buses=1888)
                                   if c["golden"] in ("c2_s3_lim1.json", "c1_lim1.json", "ieee_ieee118_lim1.json",
                                                      "ieee_ieee118x4_lim0.json", "ieee_ieee118x16_lim0.json.gz")],
                          ids=lambda c: c["golden"])
 def test_persistent_plans_match_reference_golden(gb, case, plan):
     """gbpf_solver_set_plan: every LU plan of the persistent form (one- or
-    two-pass levels, one-warp narrow levels or not) holds the reference-built
-    golden -- identical iterations and switch events, |V| and theta within
-    1e-9 -- and reports the plan it set."""
+    two-pass levels, one-warp narrow levels or not, FP64 blocks on four lanes
+    or one) holds the reference-built golden -- identical iterations and
+    switch events, |V| and theta within 1e-9 -- and reports the plan it set."""
     grid, s = solver(gb, case_path(case), tolerancia=case["tol"], no_max_iter=case["max_iter"],
                      lim_inj_reat=case["lim"])
     if s.form()["form"] != gb.FORM_PERSISTENT:
         pytest.skip("the grid's state does not fit one block's shared memory")
-    assert s.set_plan(*plan) == dict(lu1=plan[0], narrow=plan[1])
-    assert s.set_plan() == dict(lu1=plan[0], narrow=plan[1])
+    want = dict(lu1=plan[0], narrow=plan[1], quad=plan[2])
+    assert s.set_plan(*plan) == want
+    assert s.set_plan() == want
     check_solution(s.solve(), load_golden(case["golden"]))
