@@ -458,11 +458,37 @@ __device__ __forceinline__ B4 diag_block32(float Pk, float Qk, float vk, float2 
 // FP32-LU form, the FP32 copies (cos, sin, V) its Jacobian reads.  The FP64
 // cos, sin are stored only where something reads them (keep_cs: the FP64
 // Jacobian, the phasor rotation).
+// Sine and cosine of a bus angle by the table method (P. T. P. Tang,
+// "Table-lookup algorithms for elementary functions and their error
+// analysis", 1991): theta = k h + d with h = 2 pi / 256 and |d| <= h / 2 (d
+// from two fused multiply-adds with 2 pi split in two parts), (cos, sin)(k h)
+// from a table made once per device (trig_table_setup), (cos, sin)(d) from
+// the Taylor polynomials to degree 6 and 7 (the first omitted terms are below
+// 2e-20 at |d| = pi / 256), combined by the angle-sum formulas: 16 FP64
+// instructions and one 16-byte load, about half of what a general sincos
+// spends on its range reduction, and within a few ulps of it (GB300 runs FP64
+// at 1/64 of FP32, and the phasors are the largest FP64 item of an iteration).
+constexpr int kTrigTab = 256;
+static __device__ double2 g_trig_tab[kTrigTab];  // (cos, sin)(2 pi i / 256)
+__device__ __forceinline__ void sincos_tab(double th, double *s, double *c) {
+    constexpr double kInvH = 40.74366543152520595683424342336;          // 256 / (2 pi)
+    constexpr double kHhi = 6.28318530717958623199592693708837 / 256.0;  // 2 pi rounded, / 256
+    constexpr double kHlo = 2.44929359829470635445e-16 / 256.0;          // 2 pi - its rounding, / 256
+    const double k = rint(th * kInvH);
+    const double d = fma(-k, kHlo, fma(-k, kHhi, th));
+    const double2 t = g_trig_tab[(int)(long long)k & (kTrigTab - 1)];
+    const double d2 = d * d;
+    const double cd = fma(d2, fma(d2, fma(d2, -1.0 / 720.0, 1.0 / 24.0), -0.5), 1.0);
+    const double sd = fma(d * d2, fma(d2, fma(d2, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0), d);
+    *c = fma(t.x, cd, -(t.y * sd));
+    *s = fma(t.y, cd, t.x * sd);
+}
+
 template <typename TJ>
 __device__ __forceinline__ void phasor(int k, const double *th, const double *V, double *cs, double *sn, double2 *ef,
                                        float4 *f32, bool keep_cs = true) {
     double s, c;
-    sincos(th[k], &s, &c);
+    sincos_tab(th[k], &s, &c);
     if (keep_cs) {
         cs[k] = c;
         sn[k] = s;
@@ -1870,6 +1896,25 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 namespace {
 constexpr int kMaxDevices = 64;
+std::mutex g_trig_mu;
+bool g_trig_done[kMaxDevices] = {};
+
+// The table of sincos_tab on `device` (current), once per device: cos and sin
+// of 2 pi i / 256 in long double, rounded to double.
+gbpf_status trig_table_setup(int device) {
+    if (device < 0 || device >= kMaxDevices) { set_error("device ordinal out of range"); return GBPF_E_ARG; }
+    std::lock_guard<std::mutex> lock(g_trig_mu);
+    if (g_trig_done[device]) return GBPF_OK;
+    double2 t[kTrigTab];
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    for (int i = 0; i < kTrigTab; i++) {
+        const long double a = two_pi * i / kTrigTab;
+        t[i] = make_double2((double)cosl(a), (double)sinl(a));
+    }
+    CK(cudaMemcpyToSymbol(g_trig_tab, t, sizeof t));
+    g_trig_done[device] = true;
+    return GBPF_OK;
+}
 std::mutex g_noalloc_mu;
 void *g_noalloc_ptr[kMaxDevices] = {};
 
@@ -3073,6 +3118,10 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
     b->max_iter = o->no_max_iter;
     b->lim = o->lim_inj_reat;
     CK(cudaSetDevice(device));
+    {
+        const gbpf_status st = trig_table_setup(device);
+        if (st != GBPF_OK) return st;
+    }
     CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&b->ev0));
     CK(cudaEventCreate(&b->ev1));
