@@ -77,7 +77,7 @@ WORKLOADS = ["c5", "c2", "c2-plain", "c2-dense", "c3", "c4", "c5-dense"]
 # line scales them by the instance-iterations of its own launch.
 TRAFFIC = {
     # (workload, kernel family): (dram bytes, lts bytes, per instance-iteration; summary)
-    ("c5", "k_nr_block<float"): (1.944947e9 / 4207, 11.880440e9 / 4207,
+    ("c5", "k_nr_block<float"): (1.976263e9 / 4207, 11.962471e9 / 4207,
                                  "profiles/k_nr_block_fp32_level3_c5_1024_bytes.md (level 3, 1,024 scenarios, "
                                  "flat start)"),
     ("c2", "k_nr_warp<float"): (93.784e6 / 65671, 2.964886e9 / 65671,
