@@ -108,7 +108,7 @@ template <typename B4> __device__ __forceinline__ B4 bcast(B4 v, int src) {
 struct TopoOff {
     int yptr, ycol, yval, type, pv_bus, Qmin, Qmax, bus_of_blk, up_ptr, up_col, dg_ptr, dg_pos, dg_k,
         og_ptr, og_a, og_b, flev_ptr, flev_steps, blev_ptr, blev_steps, ysl, rbus, cbus, fent_ptr, fent_p,
-        fent_j, lvl_group, lvl_group_w, lvl_narrow, lvl_rot, og_k, yval32, lvl_group4, lvl_rot4;
+        fent_j, lvl_group, lvl_group_w, lvl_narrow, lvl_rot, og_k, yval32, lvl_group4, lvl_rot4, inj_order;
 };
 struct Topo {
     int nB, nL, n, nup, nnzY, nPV, nfl, nbl, fac_smem, blob_smem, blob_bytes;
@@ -144,6 +144,10 @@ struct TopoView {
     // entries are rotated away from the pivots (-1: a level too wide for one
     // pass of quads, which keeps one lane a block)
     const int *lvl_group4, *lvl_rot4;
+    // the buses in falling order of their Ybus row's length (ties by index):
+    // the order the injections take the rows in, so that the 32 rows a warp
+    // walks together are about as long as each other
+    const int *inj_order;
 };
 __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     TopoView v;
@@ -166,6 +170,7 @@ __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     v.og_k = (const int *)(b + o.og_k);
     v.lvl_group4 = (const int *)(b + o.lvl_group4);
     v.lvl_rot4 = (const int *)(b + o.lvl_rot4);
+    v.inj_order = (const int *)(b + o.inj_order);
     v.yval32 = (const float2 *)(b + o.yval32);
     return v;
 }
@@ -1092,7 +1097,10 @@ __global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) 
                     if (sizeof(TJ) == 8 || fresh || !a.rotate)
                         for (int k = tid; k < nB; k += kThreads) phasor<TJ>(k, th, V, cs, sn, ef, f32, keep_cs);
                     __syncthreads();
-                    for (int k = tid; k < nB; k += kThreads) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
+                    for (int i = tid; i < nB; i += kThreads) {
+                        const int k = G.inj_order[i];
+                        injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
+                    }
                 }
                 fresh = false;
                 __syncthreads();
@@ -1371,7 +1379,10 @@ __global__ void __launch_bounds__(32) k_flat_start(const Topo T, char *out, int 
     }
     for (int j = lane; j < n; j += 32) ys[j].x = ys[j].y = (TJ)0;
     __syncwarp();
-    for (int k = lane; k < nB; k += 32) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
+    for (int i = lane; i < nB; i += 32) {
+        const int k = G.inj_order[i];
+        injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
+    }
     __syncwarp();
     for (int q = lane; q < nq; q += 32) fac[q] = jac_block<TJ>(G, q, n, act, P, Q, V, cs, sn, f32);
     __syncwarp();
@@ -1486,7 +1497,10 @@ __global__ void __launch_bounds__(32 * kWarpsMax, GS == 3 ? 2 : 1) k_nr_warp(Arg
                     if (sizeof(TJ) == 8 || it == 0 || !a.rotate)
                         for (int k = lane; k < nB; k += 32) phasor<TJ>(k, th, V, cs, sn, ef, f32, keep_cs);
                     __syncwarp();
-                    for (int k = lane; k < nB; k += 32) injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
+                    for (int i = lane; i < nB; i += 32) {
+        const int k = G.inj_order[i];
+        injection(G.yptr, G.ycol, G.yval, ef, k, P[k], Q[k]);
+    }
                 }
                 __syncwarp();
                 if (a.lim && it >= 1 && it < mi && abits(maxDx) < tol10_bits) {
@@ -2262,6 +2276,15 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
             rot4[l] = -1;
     }
     o.lvl_group4 = put(grp4.data(), grp4.size() * 4);
+    // injection row order: a warp's loop runs to its longest row, so rows of
+    // the same length go together (measured on the 1,888-bus grid: 1.84x the
+    // needed row steps in bus order)
+    std::vector<int> order(nB);
+    for (int k = 0; k < nB; k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+        return y.rowptr[a + 1] - y.rowptr[a] > y.rowptr[c + 1] - y.rowptr[c];
+    });
+    o.inj_order = put(order.data(), nB * 4);
     o.lvl_rot4 = put(rot4.data(), rot4.size() * 4);
     DevBuf mem, tmp;
     CK(cudaMalloc(&mem.p, blob.size()));
