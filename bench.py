@@ -6,7 +6,7 @@ seeded 1,888-bus grid (16 tied copies of the 118-bus config-2 generator,
 tests/golden/c5_base.cdf.gz), reactive limits off, flat start, tolerance 1e-8
 p.u.  Set-up, outside the timed region: 50,000 training scenarios (per-bus load
 x U(0.7, 1.3), generator P x U(0.85, 1.15)) solved by the batched FP64 Newton
-method, and the 5664 -> 3 x 512 -> 3776 network trained on them on the GPU
+method, and the 3776 -> 3 x 512 -> 3776 network trained on them on the GPU
 (tcgen05 GEMMs, 120 epochs).  A step is one warm-started solve of the 8,192
 held-out scenarios: network inference, start choice, batched Newton with the
 LU in FP32 and mismatch/test/update in FP64, flat-start fallback; two steps in
@@ -842,9 +842,9 @@ def bench_batch(a, gb, np, rank, dev, world, dist):
     return line
 
 
-def train_flops_per_step(nb, width, B, k_metric):
+def train_flops_per_step(nb, width, B, k_metric, n_in=None):
     """Multiply-add FLOPs of the tensor-core GEMMs of one training step."""
-    kin, out = 3 * nb, 2 * nb
+    kin, out = (n_in or 3 * nb), 2 * nb
     fwd = kin * width + 2 * width * width + width * out + kin * out
     metric = 2 * out * k_metric
     dh = out * width + 2 * width * width
@@ -888,15 +888,18 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
     t_gen = time.perf_counter() - t0
     ok = r["status"] == 0
     V, th = r["V"].reshape(-1, nB)[ok], r["theta"].reshape(-1, nB)[ok]
-    X = gb.warm_features(Pg[ok] - Pl[ok], base["Qg"] - Ql[ok], np.tile(base["V0"], (int(ok.sum()), 1)))
+    # features [Pliq | Qliq]: every scenario starts from the grid's own
+    # voltages, so V0 features would be constant (zeros once normalised)
+    X = gb.warm_features(Pg[ok] - Pl[ok], base["Qg"] - Ql[ok])
     Y = gb.warm_targets(V, th)
+    n_in = X.shape[1]
     gen.close()
     del r, Pl, Ql, Pg
     # batch 1024 at lr 2e-3, 120 epochs: against batch 256 at 1e-3 for 60
     # epochs, 3.5x the tensor-core rate (146 vs 42 TFLOP/s), 6.1 vs 10.8 s,
     # lower loss and fewer iterations from the predicted start (3.13 vs 3.27)
     width, batch, epochs, lam, lr0 = 512, 1024, 120, 1.0, 2e-3
-    m = gb.MLP(3 * nB, 2 * nB, width=width, n_layers=3, skip=True, seed=BASE_SEED + 5, device=dev)
+    m = gb.MLP(n_in, 2 * nB, width=width, n_layers=3, skip=True, seed=BASE_SEED + 5, device=dev)
     m.set_data(X, Y)
     plain = gb.Solver(grid, device=dev, metodo=0, **opts)
     A = gb.warm_loss_metric(plain, V.mean(0), th.mean(0), m.norm()["out_scale"])
@@ -904,7 +907,7 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
     m.set_loss_metric(A, lam)
     loss, train_ms = m.train(epochs, batch=batch, lr=lr0, lr_final=1e-5, seed=BASE_SEED + 5)
     steps_per_epoch = len(X) // batch
-    train_tflops = train_flops_per_step(nB, width, batch, (A.shape[1] + 7) // 8 * 8) * steps_per_epoch * epochs / (
+    train_tflops = train_flops_per_step(nB, width, batch, (A.shape[1] + 7) // 8 * 8, n_in) * steps_per_epoch * epochs / (
         train_ms / 1e3) / 1e12
     del X, Y, V, th
     # held-out scenarios
@@ -1026,7 +1029,7 @@ def bench_c5(a, gb, np, rank, dev, world, dist):
                            "fallback; iteration 0 of a predicted run a chord step on the factor of the Jacobian "
                            "at the network's mean output (network inference, start choice and Newton inside the "
                            "timed region)",
-                   "network": f"{3 * nB} -> 3 x {width} GELU -> {2 * nB} + linear skip, bf16 weights, fp32 "
+                   "network": f"{n_in} ([Pliq | Qliq]) -> 3 x {width} GELU -> {2 * nB} + linear skip, bf16 weights, fp32 "
                               f"accumulation; loss |e A|^2 + {lam} |e|^2 (A = S J0^T); Adam lr {lr0:g} cosine to "
                               f"1e-5, {epochs} epochs, batch {batch}",
                    "train_solves": n_train, "train_converged": int(ok.sum()),

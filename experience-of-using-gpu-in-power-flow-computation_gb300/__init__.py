@@ -742,10 +742,12 @@ class Batch:
 
 
 # ---------------------------------------------------------------- warm start
-def warm_features(Pliq, Qliq, V0):
+def warm_features(Pliq, Qliq, V0=None):
     """Network features of scenarios of one grid: rows [Pliq | Qliq | V0]
-    (arrays [n, nB] or [nB])."""
-    return np.concatenate([np.atleast_2d(Pliq), np.atleast_2d(Qliq), np.atleast_2d(V0)], axis=1).astype(np.float32)
+    (arrays [n, nB] or [nB]), or [Pliq | Qliq] without V0 (a network of
+    2 nB inputs, for scenarios whose starting voltages do not vary)."""
+    cols = [np.atleast_2d(Pliq), np.atleast_2d(Qliq)] + ([] if V0 is None else [np.atleast_2d(V0)])
+    return np.concatenate(cols, axis=1).astype(np.float32)
 
 
 def warm_targets(V, theta):

@@ -1716,6 +1716,8 @@ __global__ void k_batch_stamps(const double *r, const double *x, const double *b
 // ---------------------------------------------------------------------------
 // Network features of every instance, normalised, bf16: [Pliq | Qliq | V0]
 // over the instance's buses, zero padding up to kin.
+// Features [Pliq | Qliq | V0] of every instance (n_in = 3 nB), or [Pliq |
+// Qliq] (n_in = 2 nB), normalised, in bf16 rows of kin (zero padded).
 __global__ void k_ws_features(const double *Pliq, const double *Qliq, const double *V0, const long long *inst_off,
                               int n_inst, int nB, int n_in, int kin, const float *mean, const float *iscale,
                               __nv_bfloat16 *X) {
@@ -2816,8 +2818,8 @@ gbpf_status gbpf_batch::warm_launch(gbpf_mlp *m) {
     const int nB = grids[t0].nB;
     for (int i = 0; i < n_inst; i++)
         if (inst_topo[i] != t0) { set_error("warm start needs every instance on one grid"); return GBPF_E_ARG; }
-    if (sh.n_in != 3 * nB || sh.n_out != 2 * nB) {
-        set_error("network shape does not match the grid: inputs must be 3*nB and outputs 2*nB");
+    if ((sh.n_in != 3 * nB && sh.n_in != 2 * nB) || sh.n_out != 2 * nB) {
+        set_error("network shape does not match the grid: inputs must be 3*nB (or 2*nB) and outputs 2*nB");
         return GBPF_E_ARG;
     }
     if (sh.device != device) { set_error("network and batch live on different devices"); return GBPF_E_ARG; }

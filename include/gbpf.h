@@ -541,7 +541,10 @@ gbpf_status gbpf_batch_solve_noalloc(gbpf_batch *b, int n_inst, const int *grid_
  * a hidden width below the bus count cannot.  Layer index n_hidden_layers + 1
  * of gbpf_mlp_params is S (no bias).  For a warm start of a grid with nB
  * buses: n_in = 3*nB with features [Pliq | Qliq | V0] of every bus (p.u.,
- * file bus order) and n_out = 2*nB with outputs [|V| | theta]. */
+ * file bus order), or n_in = 2*nB with [Pliq | Qliq] where the scenarios'
+ * starting voltages do not vary (constant features normalise to zeros, which
+ * the network would multiply for nothing), and n_out = 2*nB with outputs
+ * [|V| | theta]. */
 typedef struct gbpf_mlp gbpf_mlp;
 gbpf_status gbpf_mlp_create(int n_in, int n_hidden_width, int n_hidden_layers, int n_out, int linear_skip,
                             unsigned long long seed, int device, gbpf_mlp **out);
@@ -605,7 +608,7 @@ gbpf_status gbpf_mlp_set_norm(gbpf_mlp *m, const float *in_mean, const float *in
                               const float *out_mean, const float *out_scale);
 
 /* Batched Newton from the network's start: the current instances (all on one
- * grid of nB buses; network n_in = 3*nB, n_out = 2*nB) are turned into
+ * grid of nB buses; network n_in = 3*nB or 2*nB, n_out = 2*nB) are turned into
  * features on the device, the network predicts |V| (PQ buses) and theta
  * (non-slack buses), and each instance starts from the prediction when its
  * initial mismatch is smaller than that of the instance's own start
