@@ -1718,20 +1718,22 @@ __global__ void k_batch_stamps(const double *r, const double *x, const double *b
 // over the instance's buses, zero padding up to kin.
 // Features [Pliq | Qliq | V0] of every instance (n_in = 3 nB), or [Pliq |
 // Qliq] (n_in = 2 nB), normalised, in bf16 rows of kin (zero padded).
+// One block row of instances (blockIdx.y) and columns across the threads of
+// blockIdx.x, so no thread divides a flat index by the row length.
 __global__ void k_ws_features(const double *Pliq, const double *Qliq, const double *V0, const long long *inst_off,
                               int n_inst, int nB, int n_in, int kin, const float *mean, const float *iscale,
                               __nv_bfloat16 *X) {
-    const long long total = (long long)n_inst * kin;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int inst = (int)(i / kin), c = (int)(i % kin);
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= kin) return;
+    const float mc = c < n_in ? mean[c] : 0.f, sc = c < n_in ? iscale[c] : 0.f;
+    for (int inst = blockIdx.y; inst < n_inst; inst += gridDim.y) {
         const long long off = inst_off[inst];
         float v = 0.f;
         if (c < n_in) {
             const double x = c < nB ? Pliq[off + c] : c < 2 * nB ? Qliq[off + c - nB] : V0[off + c - 2 * nB];
-            v = (float)((x - (double)mean[c]) * (double)iscale[c]);
+            v = (float)((x - (double)mc) * (double)sc);
         }
-        X[i] = __float2bfloat16_rn(v);
+        X[(long long)inst * kin + c] = __float2bfloat16_rn(v);
     }
 }
 
@@ -1773,7 +1775,10 @@ __global__ void __launch_bounds__(kSelThreads) k_ws_select(Args a, const float *
     float tlo = INFINITY, thi = -INFINITY;  // spread of the predicted angles
     for (int k = tid; k < nB; k += kSelThreads) {
         const int ty = G.type[k];
-        const double v0 = a.V0[off + k], t0 = a.th0[off + k];
+        // the own start: the grid's (the shared flat copy, read by every
+        // instance from L2) when the instances start from it
+        const double v0 = flat ? ((const double *)(flat + F.V0))[k] : a.V0[off + k];
+        const double t0 = flat ? ((const double *)(flat + F.th0))[k] : a.th0[off + k];
         const double v = (ty == 0 || ty == 1) ? (double)pr[k] * oscale[k] + omean[k] : v0;
         const double t = ty == 3 ? t0 : (double)pr[nB + k] * oscale[nB + k] + omean[nB + k];
         sV[off + k] = v;
@@ -2850,8 +2855,8 @@ gbpf_status gbpf_batch::warm_launch(gbpf_mlp *m) {
     if ((st0 = make_wref(sh, t0)) != GBPF_OK) return st0;
     CK(cudaEventRecord(ev0, stream));
     CK(cudaMemsetAsync(wHist, 0, 8 * kOrderClasses, stream));
-    k_ws_features<<<1024, 256, 0, stream>>>(args.Pliq, args.Qliq, args.V0, args.inst_off, n_inst, nB, sh.n_in, sh.kin,
-                                            sh.in_mean, sh.in_iscale, wX);
+    k_ws_features<<<dim3((sh.kin + 255) / 256, (unsigned)std::min(n_inst, 4096)), 256, 0, stream>>>(
+        args.Pliq, args.Qliq, args.V0, args.inst_off, n_inst, nB, sh.n_in, sh.kin, sh.in_mean, sh.in_iscale, wX);
     CK_LAUNCH();
     gbpf_status st = gbpf::mlp_infer(m, wX, n_inst, wPred, stream, mwork);
     if (st != GBPF_OK) return st;
