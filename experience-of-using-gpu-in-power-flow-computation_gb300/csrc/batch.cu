@@ -467,9 +467,10 @@ __device__ __forceinline__ B4 diag_block32(float Pk, float Qk, float vk, float2 
 // "Table-lookup algorithms for elementary functions and their error
 // analysis", 1991): theta = k h + d with h = 2 pi / 256 and |d| <= h / 2 (d
 // from two fused multiply-adds with 2 pi split in two parts), (cos, sin)(k h)
-// from a table made once per device (trig_table_setup), (cos, sin)(d) from
-// the Taylor polynomials to degree 6 and 7 (the first omitted terms are below
-// 2e-20 at |d| = pi / 256), combined by the angle-sum formulas: 16 FP64
+// from a table that each batch creation copies to the device
+// (trig_table_setup), (cos, sin)(d) from the Taylor polynomials to degree 6
+// and 7 (the first omitted terms are below 2e-20 at |d| = pi / 256),
+// combined by the angle-sum formulas: 16 FP64
 // instructions and one 16-byte load, about half of what a general sincos
 // spends on its range reduction, and within a few ulps of it (GB300 runs FP64
 // at 1/64 of FP32, and the phasors are the largest FP64 item of an iteration).
@@ -1917,23 +1918,21 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 namespace {
 constexpr int kMaxDevices = 64;
-std::mutex g_trig_mu;
-bool g_trig_done[kMaxDevices] = {};
-
-// The table of sincos_tab on `device` (current), once per device: cos and sin
-// of 2 pi i / 256 in long double, rounded to double.
-gbpf_status trig_table_setup(int device) {
-    if (device < 0 || device >= kMaxDevices) { set_error("device ordinal out of range"); return GBPF_E_ARG; }
-    std::lock_guard<std::mutex> lock(g_trig_mu);
-    if (g_trig_done[device]) return GBPF_OK;
-    double2 t[kTrigTab];
-    const long double two_pi = 6.283185307179586476925286766559005768L;
-    for (int i = 0; i < kTrigTab; i++) {
-        const long double a = two_pi * i / kTrigTab;
-        t[i] = make_double2((double)cosl(a), (double)sinl(a));
-    }
-    CK(cudaMemcpyToSymbol(g_trig_tab, t, sizeof t));
-    g_trig_done[device] = true;
+// The table of sincos_tab -- cos and sin of 2 pi i / 256 in long double,
+// rounded to double -- copied to the current device's symbol.  Every batch
+// creation copies it (4 KB, identical bytes each time), so a device whose
+// context was reset gets it again.
+gbpf_status trig_table_setup() {
+    static const std::vector<double2> table = [] {
+        std::vector<double2> t(kTrigTab);
+        const long double two_pi = 6.283185307179586476925286766559005768L;
+        for (int i = 0; i < kTrigTab; i++) {
+            const long double a = two_pi * i / kTrigTab;
+            t[i] = make_double2((double)cosl(a), (double)sinl(a));
+        }
+        return t;
+    }();
+    CK(cudaMemcpyToSymbol(g_trig_tab, table.data(), sizeof(double2) * kTrigTab));
     return GBPF_OK;
 }
 std::mutex g_noalloc_mu;
@@ -3149,7 +3148,7 @@ extern "C" gbpf_status gbpf_batch_create(const gbpf_grid *const *grids, int n_gr
     b->lim = o->lim_inj_reat;
     CK(cudaSetDevice(device));
     {
-        const gbpf_status st = trig_table_setup(device);
+        const gbpf_status st = trig_table_setup();
         if (st != GBPF_OK) return st;
     }
     CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
