@@ -108,7 +108,8 @@ template <typename B4> __device__ __forceinline__ B4 bcast(B4 v, int src) {
 struct TopoOff {
     int yptr, ycol, yval, type, pv_bus, Qmin, Qmax, bus_of_blk, up_ptr, up_col, dg_ptr, dg_pos, dg_k,
         og_ptr, og_a, og_b, flev_ptr, flev_steps, blev_ptr, blev_steps, ysl, rbus, cbus, fent_ptr, fent_p,
-        fent_j, lvl_group, lvl_group_w, lvl_narrow, lvl_rot, og_k, yval32, lvl_group4, lvl_rot4, inj_order;
+        fent_j, lvl_group, lvl_group_w, lvl_narrow, lvl_rot, og_k, yval32, lvl_group4, lvl_rot4, inj_order,
+        lvl_group4w, lvl_q4w;
 };
 struct Topo {
     int nB, nL, n, nup, nnzY, nPV, nfl, nbl, fac_smem, blob_smem, blob_bytes;
@@ -148,6 +149,10 @@ struct TopoView {
     // the order the injections take the rows in, so that the 32 rows a warp
     // walks together are about as long as each other
     const int *inj_order;
+    // the same quads on 32 lanes (lu_pivots_q / lu_entries_q <32>: eight
+    // quads): log2 of the quads per pivot [2 * l] and entry [2 * l + 1], and
+    // 1 where forward level l fits one pass of them (else one lane a block)
+    const int *lvl_group4w, *lvl_q4w;
 };
 __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     TopoView v;
@@ -171,6 +176,8 @@ __device__ __forceinline__ TopoView bind(const TopoOff &o, const char *b) {
     v.lvl_group4 = (const int *)(b + o.lvl_group4);
     v.lvl_rot4 = (const int *)(b + o.lvl_rot4);
     v.inj_order = (const int *)(b + o.inj_order);
+    v.lvl_group4w = (const int *)(b + o.lvl_group4w);
+    v.lvl_q4w = (const int *)(b + o.lvl_q4w);
     v.yval32 = (const float2 *)(b + o.yval32);
     return v;
 }
@@ -975,6 +982,73 @@ __device__ __forceinline__ void lu_entries_q(const TopoView &G, int l, int lg, i
     }
 }
 
+// Forward substitution alone on FP64 level l with the quads of lu_pivots_q:
+// y_j -= sum_k L(j,k) y_k summed exactly as lu_pivots_q's y part (same
+// quads, groups and order), so an instance on a factor made by the quad
+// pivots gets the y the fused pass would have given.
+template <int NT>
+__device__ __forceinline__ void fwd_rows_q(const TopoView &G, int l, int lg, int t, const double4_32a *Lv,
+                                           double2 *ys) {
+    const int c = t & 3, r = c >> 1, s = c & 1, qb = (t & 31) & ~3;
+    const unsigned qm = 0xfu << qb;
+    const int sA0 = qb + 2 * r, sA1 = sA0 + 1;
+    const int tl = t >> 2, gs = 1 << lg, gl = tl & (gs - 1), ng = (NT >> 2) >> lg;
+    const int beg = G.flev_ptr[l], cnt = G.flev_ptr[l + 1] - beg;
+    for (int b0 = 0; b0 < cnt; b0 += ng) {
+        const int w = b0 + (tl >> lg);
+        const bool on = w < cnt;
+        const int j = on ? G.flev_steps[beg + w] : 0;
+        double yr = 0.0;
+        if (on && gl == 0) yr = r ? ys[j].y : ys[j].x;
+        if (on)
+            for (int q = G.dg_ptr[j] + gl; q < G.dg_ptr[j + 1]; q += gs) {
+                const double lj = ((const double *)&Lv[G.dg_pos[q]])[c];
+                const double l0 = __shfl_sync(qm, lj, sA0), l1 = __shfl_sync(qm, lj, sA1);
+                const double2 yk = ys[G.dg_k[q]];
+                yr -= __fma_rn(l0, yk.x, l1 * yk.y);
+            }
+        for (int o = gs >> 1; o > 0; o >>= 1) yr += __shfl_xor_sync(0xffffffffu, yr, 4 * o);
+        if (on && gl == 0 && s == 0) ((double *)&ys[j])[r] = yr;
+    }
+}
+
+// fwd_rows on 32 lanes for a factor made by lu_two_pass_warp: the quads'
+// order on the levels that took them, else one lane a row.
+template <typename TJ>
+__device__ __forceinline__ void fwd_rows_warp(const TopoView &G, int l, bool grouped, bool quad, int lane,
+                                              const typename Blk<TJ>::b4 *Lv, typename Blk<TJ>::b2 *ys) {
+    if constexpr (sizeof(TJ) == 8) {
+        if (quad && G.lvl_q4w[l]) {
+            fwd_rows_q<32>(G, l, grouped ? G.lvl_group4w[2 * l] : 0, lane, Lv, ys);
+            return;
+        }
+    }
+    fwd_rows<TJ, 32>(G, l, grouped ? G.lvl_group_w[3 * l] : 0, lane, Lv, ys);
+}
+
+// Two-pass forward level l on 32 lanes (the warp kernel, the shared flat
+// start, a block's narrow levels): FP64 levels that fit the warp's eight
+// quads (lvl_q4w) take lu_pivots_q / lu_entries_q, the rest one lane a block.
+// grouped = 0 gives every pivot and entry one lane (quad) of its own.
+template <typename TJ>
+__device__ __forceinline__ bool lu_two_pass_warp(const TopoView &G, int l, bool grouped, bool quad, int lane,
+                                                 typename Blk<TJ>::b4 *fac, typename Blk<TJ>::b4 *dinv,
+                                                 typename Blk<TJ>::b2 *ys, typename Blk<TJ>::b4 *Lv,
+                                                 typename Blk<TJ>::b4 *Uv) {
+    if constexpr (sizeof(TJ) == 8) {
+        if (quad && G.lvl_q4w[l]) {
+            const bool sing = lu_pivots_q<32>(G, l, grouped ? G.lvl_group4w[2 * l] : 0, lane, fac, dinv, ys, Lv, Uv);
+            __syncwarp();
+            lu_entries_q<32>(G, l, grouped ? G.lvl_group4w[2 * l + 1] : 0, lane, dinv, Lv, Uv);
+            return sing;
+        }
+    }
+    const bool sing = lu_pivots<TJ, 32>(G, l, grouped ? G.lvl_group_w[3 * l] : 0, lane, fac, dinv, ys, Lv, Uv);
+    __syncwarp();
+    lu_entries<TJ, 32>(G, l, grouped ? G.lvl_group_w[3 * l + 1] : 0, lane, dinv, Lv, Uv);
+    return sing;
+}
+
 // GS: the state placement level of layout(); 3 = level 2 compiled for four
 // blocks per SM (64 registers a thread) instead of two.
 template <typename TJ, int GS>
@@ -1213,9 +1287,7 @@ __global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) 
                                     sing = lu_level1<TJ, 32>(G, l, gp, ge, a.no_group ? 0 : G.lvl_rot[l] >> 16, lane,
                                                              fac, dinv, ys, zs, Lv, Uv);
                                 } else {
-                                    sing = lu_pivots<TJ, 32>(G, l, gp, lane, fac, dinv, ys, Lv, Uv);
-                                    __syncwarp();
-                                    lu_entries<TJ, 32>(G, l, ge, lane, dinv, Lv, Uv);
+                                    sing = lu_two_pass_warp<TJ>(G, l, !a.no_group, a.quad, lane, fac, dinv, ys, Lv, Uv);
                                 }
                                 if (sing) { s_status = GBPF_E_SINGULAR; s_done = 1; }
                                 __syncwarp();
@@ -1358,7 +1430,7 @@ __global__ void __launch_bounds__(kThreads, GS == 3 ? 4 : 2) k_nr_block(Args a) 
 // values it would have computed itself.  Shared memory: ys (zero right-hand
 // side; only the factor is kept) and the active-voltage flags.
 template <typename TJ>
-__global__ void __launch_bounds__(32) k_flat_start(const Topo T, char *out, int warp_group) {
+__global__ void __launch_bounds__(32) k_flat_start(const Topo T, char *out, int warp_group, int quad) {
     using B4 = typename Blk<TJ>::b4;
     using B2 = typename Blk<TJ>::b2;
     extern __shared__ __align__(16) unsigned char fsm[];
@@ -1389,9 +1461,7 @@ __global__ void __launch_bounds__(32) k_flat_start(const Topo T, char *out, int 
     __syncwarp();
     bool sing = false;
     for (int l = 0; l < T.nfl; l++) {
-        sing |= lu_pivots<TJ, 32>(G, l, warp_group ? G.lvl_group_w[3 * l] : 0, lane, fac, fac, ys, Lv, Uv);
-        __syncwarp();
-        lu_entries<TJ, 32>(G, l, warp_group ? G.lvl_group_w[3 * l + 1] : 0, lane, fac, Lv, Uv);
+        sing |= lu_two_pass_warp<TJ>(G, l, warp_group != 0, quad != 0, lane, fac, fac, ys, Lv, Uv);
         __syncwarp();
     }
     sing = __any_sync(0xffffffffu, sing);
@@ -1562,7 +1632,7 @@ __global__ void __launch_bounds__(32 * kWarpsMax, GS == 3 ? 2 : 1) k_nr_warp(Arg
                     const B4 *facS = (const B4 *)(sb + F.fac);
                     if (*(const int *)(sb + F.sing)) { status = GBPF_E_SINGULAR; break; }
                     for (int l = 0; l < T.nfl; l++) {
-                        fwd_rows<TJ, 32>(G, l, a.warp_group ? G.lvl_group_w[3 * l] : 0, lane, facS + n, ys);
+                        fwd_rows_warp<TJ>(G, l, a.warp_group != 0, a.quad != 0, lane, facS + n, ys);
                         __syncwarp();
                     }
                     Ub = facS + n + T.nup;
@@ -1581,9 +1651,8 @@ __global__ void __launch_bounds__(32 * kWarpsMax, GS == 3 ? 2 : 1) k_nr_warp(Arg
                             sing |= lu_level1<TJ, 32>(G, l, gp, ge, a.warp_group ? G.lvl_rot[l] >> 16 : 0, lane, fac, dinv,
                                                       ys, zs, Lv, Uv);
                         } else {
-                            sing |= lu_pivots<TJ, 32>(G, l, gp, lane, fac, dinv, ys, Lv, Uv);
-                            __syncwarp();
-                            lu_entries<TJ, 32>(G, l, ge, lane, dinv, Lv, Uv);
+                            sing |= lu_two_pass_warp<TJ>(G, l, a.warp_group != 0, a.quad != 0, lane, fac, dinv, ys, Lv,
+                                                         Uv);
                         }
                         __syncwarp();
                     }
@@ -2249,6 +2318,7 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
     // block kernel's kThreads / 4 quads, and the entries' rotation past the
     // pivots' threads
     std::vector<int> grp4(2 * (size_t)std::max(nfl, 1), 0), rot4(std::max(nfl, 1), 0);
+    std::vector<int> grp4w(grp4.size(), 0), q4w(rot4.size(), 0);
     for (int l = 0; l < nfl; l++) {
         int md = 0, mo = 0;
         for (int w = S.flev_ptr[l]; w < S.flev_ptr[l + 1]; w++) {
@@ -2259,9 +2329,9 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
             const int pp = S.fent_p[e];
             mo = std::max(mo, (int)(S.og_ptr[pp + 1] - S.og_ptr[pp]));
         }
-        auto g4 = [](int count, int longest) {
+        auto g4 = [](int count, int longest, int quads = kThreads / 4) {
             int g = 0;
-            while (g < 3 && ((long long)count << (g + 1)) <= kThreads / 4 && (1 << g) < longest) g++;
+            while (g < 3 && ((long long)count << (g + 1)) <= quads && (1 << g) < longest) g++;
             return g;
         };
         const int np = S.flev_ptr[l + 1] - S.flev_ptr[l], ne = S.fent_ptr[l + 1] - S.fent_ptr[l];
@@ -2280,6 +2350,11 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
         if (((long long)np << grp4[2 * l]) > kThreads / 4 || ((long long)ne << grp4[2 * l + 1]) > kThreads / 4 ||
             walk(md, grp4[2 * l]) > 16 || walk(mo, grp4[2 * l + 1]) > 16)
             rot4[l] = -1;
+        // the warp's eight quads, by the same rule
+        grp4w[2 * l] = g4(np, md, 8);
+        grp4w[2 * l + 1] = g4(ne, mo, 8);
+        q4w[l] = ((long long)np << grp4w[2 * l]) <= 8 && ((long long)ne << grp4w[2 * l + 1]) <= 8 &&
+                 walk(md, grp4w[2 * l]) <= 16 && walk(mo, grp4w[2 * l + 1]) <= 16;
     }
     o.lvl_group4 = put(grp4.data(), grp4.size() * 4);
     // injection row order: a warp's loop runs to its longest row, so rows of
@@ -2292,6 +2367,8 @@ gbpf_status gbpf_batch::add_topology(const Grid &g) {
     });
     o.inj_order = put(order.data(), nB * 4);
     o.lvl_rot4 = put(rot4.data(), rot4.size() * 4);
+    o.lvl_group4w = put(grp4w.data(), grp4w.size() * 4);
+    o.lvl_q4w = put(q4w.data(), q4w.size() * 4);
     DevBuf mem, tmp;
     CK(cudaMalloc(&mem.p, blob.size()));
     CK(cudaMemcpyAsync(mem.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, stream));
@@ -2738,8 +2815,8 @@ gbpf_status gbpf_batch::build_graph() {
                 if (fp32) CK(cudaFuncSetAttribute(k_flat_start<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs));
                 else CK(cudaFuncSetAttribute(k_flat_start<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs));
             }
-            if (fp32) k_flat_start<float><<<1, 32, fs, stream>>>(T, o, plan.warp_group);
-            else k_flat_start<double><<<1, 32, fs, stream>>>(T, o, plan.warp_group);
+            if (fp32) k_flat_start<float><<<1, 32, fs, stream>>>(T, o, plan.warp_group, plan.quad);
+            else k_flat_start<double><<<1, 32, fs, stream>>>(T, o, plan.warp_group, plan.quad);
             CK_LAUNCH();
             T.flat = o;
         }
@@ -2773,7 +2850,7 @@ gbpf_status gbpf_batch::build_graph() {
     wargs.warp_group = plan.warp_group;
     args.narrow = plan.narrow;
     args.lu1 = plan.lu1;
-    args.quad = plan.quad;
+    args.quad = wargs.quad = plan.quad;
     wargs.lu1 = plan.warp_lu1;
     args.rotate = wargs.rotate = plan.rotate;
     handoff.reset();
@@ -2936,8 +3013,8 @@ gbpf_status gbpf_batch::make_wref(const gbpf::MlpShape &sh, int t0) {
             if (fp32) CK(cudaFuncSetAttribute(k_flat_start<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs));
             else CK(cudaFuncSetAttribute(k_flat_start<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs));
         }
-        if (fp32) k_flat_start<float><<<1, 32, fs, stream>>>(T, o, plan.warp_group);
-        else k_flat_start<double><<<1, 32, fs, stream>>>(T, o, plan.warp_group);
+        if (fp32) k_flat_start<float><<<1, 32, fs, stream>>>(T, o, plan.warp_group, plan.quad);
+        else k_flat_start<double><<<1, 32, fs, stream>>>(T, o, plan.warp_group, plan.quad);
         CK_LAUNCH();
         wref = o;
     }
